@@ -1,0 +1,203 @@
+/*
+ * vulkanpbrt_gb300.h -- C ABI of the GB300-native per-frame path of
+ * VulkanPBRT: path tracer (PBRTPipeline), temporal accumulator and the BMFR /
+ * BFR regression denoisers.
+ *
+ * Every entry point replaces a method of the reference's render-module C++
+ * classes; the comment above each names the reference interface (file:line,
+ * relative to the VulkanPBRT source tree). Conventions:
+ *   - every call returns int status: PBRT_OK (0) or a negative PbrtStatus;
+ *     pbrt_last_error() gives the calling thread's last message;
+ *   - handles are opaque and reference counted (pbrt_retain/pbrt_release);
+ *     an object retains the objects it was created from;
+ *   - images are device buffers the library owns, exposed through PbrtImage
+ *     views (the reference's public DescriptorImage attributes), rows packed,
+ *     layers consecutive;
+ *   - work is stream ordered on the cudaStream_t passed in (NULL = legacy
+ *     default stream). Calls on one handle are not reentrant: use one handle
+ *     per host thread or synchronise externally (the reference records and
+ *     submits from a single thread).
+ */
+#ifndef VULKANPBRT_GB300_H
+#define VULKANPBRT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define PBRT_API __attribute__((visibility("default")))
+#else
+#define PBRT_API
+#endif
+
+struct CUstream_st;
+typedef struct CUstream_st* pbrt_stream_t; /* == cudaStream_t */
+
+typedef enum PbrtStatus {
+  PBRT_OK = 0,
+  PBRT_ERROR_INVALID_ARGUMENT = -1,
+  PBRT_ERROR_CUDA = -2,
+  PBRT_ERROR_OUT_OF_MEMORY = -3,
+  PBRT_ERROR_UNSUPPORTED = -4,
+  PBRT_ERROR_ABORTED = -5,
+  PBRT_ERROR_TIMEOUT = -6
+} PbrtStatus;
+
+/* Texel formats of the reference's images (Vulkan VK_FORMAT_* names). */
+typedef enum PbrtFormat {
+  PBRT_FORMAT_R32_SFLOAT = 1,
+  PBRT_FORMAT_R32G32_SFLOAT = 2,
+  PBRT_FORMAT_R32G32B32A32_SFLOAT = 3,
+  PBRT_FORMAT_R16_SFLOAT = 4,
+  PBRT_FORMAT_R16G16_SFLOAT = 5,
+  PBRT_FORMAT_R16G16B16A16_SFLOAT = 6,
+  PBRT_FORMAT_R8_UNORM = 7,
+  PBRT_FORMAT_R8G8B8A8_UNORM = 8,
+  PBRT_FORMAT_B8G8R8A8_UNORM = 9
+} PbrtFormat;
+
+/* A device image: texel (x, y) of layer l is at
+ * data + l * layer_bytes + y * row_bytes + x * texel_bytes. */
+typedef struct PbrtImage {
+  void* data;
+  uint32_t width, height, layers;
+  int32_t format; /* PbrtFormat */
+  uint32_t texel_bytes;
+  size_t row_bytes, layer_bytes;
+} PbrtImage;
+
+/* RayTracingPushConstants (source/renderModules/PipelineStructs.hpp:6-13);
+ * matrices column-major as vsg::mat4 / GLSL mat4. */
+typedef struct PbrtPushConstants {
+  float view_inverse[16];
+  float proj_inverse[16];
+  float prev_view[16];
+  uint32_t frame_number;
+  uint32_t sample_number;
+} PbrtPushConstants;
+
+/* CameraMatrices (source/io/RenderIO.hpp) as Accumulator::set_camera_matrices
+ * reads it; has_proj says whether proj / inv_proj are set. */
+typedef struct PbrtCameraMatrices {
+  float view[16];
+  float inv_view[16];
+  float proj[16];
+  float inv_proj[16];
+  int32_t has_proj;
+} PbrtCameraMatrices;
+
+typedef struct PbrtGBuffer PbrtGBuffer;
+typedef struct PbrtIlluminationBuffer PbrtIlluminationBuffer;
+typedef struct PbrtAccumulationBuffer PbrtAccumulationBuffer;
+typedef struct PbrtAccumulator PbrtAccumulator;
+typedef struct PbrtBMFR PbrtBMFR;
+typedef struct PbrtBFR PbrtBFR;
+typedef struct PbrtScene PbrtScene;
+typedef struct PbrtPipeline PbrtPipeline;
+
+/* ---- library ---------------------------------------------------------- */
+PBRT_API const char* pbrt_version(void);
+/* Copies the calling thread's last error message (NUL terminated). */
+PBRT_API int pbrt_last_error(char* buffer, size_t size);
+/* Reference counting for every handle type above. */
+PBRT_API int pbrt_retain(void* handle);
+PBRT_API int pbrt_release(void* handle);
+
+/* ---- GBuffer (source/buffers/GBuffer.hpp:9-26) -------------------------
+ * Public images depth R32F, normal RG32F (theta, phi), material RGBA8,
+ * albedo RGBA8 (GBuffer.cpp:53-125). */
+PBRT_API int pbrt_gbuffer_create(uint32_t width, uint32_t height, PbrtGBuffer** out);
+PBRT_API int pbrt_gbuffer_images(const PbrtGBuffer* g, PbrtImage* depth, PbrtImage* normal, PbrtImage* material,
+                                 PbrtImage* albedo);
+
+/* ---- IlluminationBuffer family (source/buffers/IlluminationBuffer.hpp) --
+ * type: the subclass name's suffix. Image lists follow
+ * IlluminationBuffer.cpp:73-310: Final {BGRA8}, FinalDemodulated {BGRA8,
+ * RGBA16F illumination, RGBA16F illuminationSquared}, Demodulated {RGBA16F
+ * illumination, RGBA16F illuminationSquared}, DemodulatedFloat {RGBA32F},
+ * FinalFloat {RGBA32F}. */
+typedef enum PbrtIlluminationType {
+  PBRT_ILLUMINATION_FINAL = 0,
+  PBRT_ILLUMINATION_FINAL_DEMODULATED = 1,
+  PBRT_ILLUMINATION_DEMODULATED = 2,
+  PBRT_ILLUMINATION_DEMODULATED_FLOAT = 3,
+  PBRT_ILLUMINATION_FINAL_FLOAT = 4
+} PbrtIlluminationType;
+PBRT_API int pbrt_illumination_buffer_create(int32_t type, uint32_t width, uint32_t height,
+                                             PbrtIlluminationBuffer** out);
+PBRT_API int pbrt_illumination_buffer_images(const PbrtIlluminationBuffer* b, PbrtImage* images, uint32_t capacity,
+                                             uint32_t* count);
+
+/* ---- AccumulationBuffer (source/buffers/AccumulationBuffer.hpp:10-30) ---
+ * prev_illu, prev_illu_squared RGBA16F; prev_depth R32F; prev_normal RG32F;
+ * spp, prev_spp R8_UNORM; motion RG16F (AccumulationBuffer.cpp:245-339). */
+PBRT_API int pbrt_accumulation_buffer_create(uint32_t width, uint32_t height, PbrtAccumulationBuffer** out);
+typedef struct PbrtAccumulationImages {
+  PbrtImage prev_illu, prev_illu_squared, prev_depth, prev_normal, spp, prev_spp, motion;
+} PbrtAccumulationImages;
+PBRT_API int pbrt_accumulation_buffer_images(const PbrtAccumulationBuffer* a, PbrtAccumulationImages* out);
+/* AccumulationBuffer::copy_to_back_images (AccumulationBuffer.cpp:72-244):
+ * depth->prev_depth, normal->prev_normal, spp->prev_spp and the
+ * demodulated illumination (image 0, or image 1 of FinalDemodulated) ->
+ * prev_illu. */
+PBRT_API int pbrt_accumulation_buffer_copy_to_back_images(PbrtAccumulationBuffer* a, const PbrtGBuffer* g,
+                                                          const PbrtIlluminationBuffer* illumination,
+                                                          pbrt_stream_t stream);
+
+/* ---- Accumulator (source/renderModules/Accumulator.hpp:8-49) ----------- */
+PBRT_API int pbrt_accumulator_create(PbrtGBuffer* g, PbrtIlluminationBuffer* illumination, int32_t separate_matrices,
+                                     int32_t work_width, int32_t work_height, PbrtAccumulator** out);
+/* Accumulator::set_camera_matrices (Accumulator.cpp:85-117). */
+PBRT_API int pbrt_accumulator_set_camera_matrices(PbrtAccumulator* acc, int32_t frame_index,
+                                                  const PbrtCameraMatrices* cur, const PbrtCameraMatrices* prev);
+/* Accumulator::add_dispatch_to_command_graph (Accumulator.cpp:72-83). */
+PBRT_API int pbrt_accumulator_dispatch(PbrtAccumulator* acc, pbrt_stream_t stream);
+/* Public attributes accumulated_illumination (IlluminationBufferDemodulated)
+ * and accumulation_buffer (Accumulator.hpp:24-25); borrowed references. */
+PBRT_API int pbrt_accumulator_get_accumulated_illumination(PbrtAccumulator* acc, PbrtIlluminationBuffer** out);
+PBRT_API int pbrt_accumulator_get_accumulation_buffer(PbrtAccumulator* acc, PbrtAccumulationBuffer** out);
+
+/* ---- BMFR (source/renderModules/denoisers/BMFR.hpp:14-41) --------------
+ * BMFR(width, height, work_width, work_height, g_buffer, illu_buffer,
+ * acc_buffer, fitting_kernel = 256). illumination must be Demodulated or
+ * DemodulatedFloat (BMFR.cpp:58-63; here: an error instead of a silent
+ * half-built object). work sizes 8, 16 or 32 (square). */
+PBRT_API int pbrt_bmfr_create(uint32_t width, uint32_t height, uint32_t work_width, uint32_t work_height,
+                              PbrtGBuffer* g, PbrtIlluminationBuffer* illumination, PbrtAccumulationBuffer* acc,
+                              uint32_t fitting_kernel, PbrtBMFR** out);
+/* POSITION_TYPE specialisation constant (shaders/bmfrGeneral.comp:30-31;
+ * BMFR.cpp never sets it, so the reference runs 0 = screen xy + block-
+ * normalised depth). fp64_resolve = 1 re-solves, in FP64, every block whose
+ * R-factor diagonal ratio exceeds 1e6 (no reference counterpart; 0 keeps
+ * the reference's FP32 result). */
+PBRT_API int pbrt_bmfr_set_options(PbrtBMFR* b, int32_t position_type, int32_t fp64_resolve);
+/* BMFR::add_dispatch_to_command_graph (BMFR.cpp:203-230): the three
+ * dispatches bmfrPre -> bmfrFit -> bmfrPost, fused here into one kernel per
+ * 32x32 (or 16x16, 8x8) block. */
+PBRT_API int pbrt_bmfr_dispatch(PbrtBMFR* b, const PbrtPushConstants* pc, pbrt_stream_t stream);
+/* BMFR::get_final_descriptor_image (BMFR.cpp:231-234): B8G8R8A8_UNORM. */
+PBRT_API int pbrt_bmfr_final_image(const PbrtBMFR* b, PbrtImage* out);
+/* Private images exposed for inspection: denoised RGBA16F x 2 layers and
+ * weights R32F x 30 layers at block-grid size (BMFR.cpp:97-133). */
+PBRT_API int pbrt_bmfr_images(const PbrtBMFR* b, PbrtImage* denoised, PbrtImage* weights);
+/* Number of blocks re-solved in FP64 by the last dispatch (stream-ordered
+ * read; synchronises the stream). */
+PBRT_API int pbrt_bmfr_fp64_block_count(PbrtBMFR* b, pbrt_stream_t stream, uint32_t* count);
+
+/* ---- BFR (source/renderModules/denoisers/BFR.hpp:8-45) ----------------- */
+PBRT_API int pbrt_bfr_create(uint32_t width, uint32_t height, uint32_t work_width, uint32_t work_height,
+                             PbrtGBuffer* g, PbrtIlluminationBuffer* illumination, PbrtAccumulationBuffer* acc,
+                             PbrtBFR** out);
+/* BFR::add_dispatch_to_command_graph (BFR.cpp:128-138). */
+PBRT_API int pbrt_bfr_dispatch(PbrtBFR* b, const PbrtPushConstants* pc, pbrt_stream_t stream);
+PBRT_API int pbrt_bfr_final_image(const PbrtBFR* b, PbrtImage* out);
+PBRT_API int pbrt_bfr_images(const PbrtBFR* b, PbrtImage* denoised);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VULKANPBRT_GB300_H */

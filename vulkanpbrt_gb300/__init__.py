@@ -1,0 +1,26 @@
+"""vulkanpbrt_gb300: GB300-native (sm_103a) per-frame path of VulkanPBRT.
+
+The native library (csrc/, C ABI in include/vulkanpbrt_gb300.h) holds the
+path tracer, accumulator and BMFR/BFR denoisers; this package mirrors the
+reference's render-module classes over that ABI.
+"""
+from ._abi import PbrtError, declared_symbols, lib  # noqa: F401
+from .render_modules import (  # noqa: F401
+    BFR,
+    BMFR,
+    AccumulationBuffer,
+    Accumulator,
+    CameraMatrices,
+    Commands,
+    GBuffer,
+    IlluminationBuffer,
+    IlluminationBufferDemodulated,
+    IlluminationBufferDemodulatedFloat,
+    IlluminationBufferFinal,
+    IlluminationBufferFinalDemodulated,
+    IlluminationBufferFinalFloat,
+    Image,
+    PushConstants,
+)
+
+__version__ = "0.1.0"
