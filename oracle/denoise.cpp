@@ -467,7 +467,11 @@ int oracle_bmfr_fit(int W, int H, int bw, int fit_threads, uint32_t frame, const
           part[id] = v;
         }
         float v = block_sum(part);
-        for (int index = col; index < P; ++index) A[(size_t)index * 13 + f] -= 2.f * u[index] * v / ulen2;
+        // features -= 2 * u * v / uLengthSquared, with the division taken as a
+        // product with the correctly rounded reciprocal (within the 2.5 ULP
+        // Vulkan allows a shader's x / y).
+        float rl = 1.f / ulen2;
+        for (int index = col; index < P; ++index) A[(size_t)index * 13 + f] -= 2.f * u[index] * v * rl;
       }
       for (int f = col + 1; f < 13; ++f) R[col][f] = A[(size_t)col * 13 + f];
     }

@@ -36,6 +36,13 @@ def _pc(vp, cam, frame):
     return vp.PushConstants(view_inverse=cam.inv_view, proj_inverse=cam.inv_proj, prev_view=cam.view, frame_number=frame)
 
 
+# 8x8 and 16x16 blocks fit 10 features to 64 / 256 rows; some blocks are ill
+# conditioned enough that a 1-ulp sinf/cosf difference in the normal decode,
+# flipping one R16F-quantised feature, moves the output by a few percent.
+# 32x32 blocks (the reference's default) meet the bar on every pixel.
+MIN_FRACTION = {32: 0.999, 16: 0.998, 8: 0.998}
+
+
 @pytest.mark.parametrize("bw,fk,position_type", [(32, 256, 0), (16, 256, 0), (8, 64, 0), (32, 256, 2), (32, 256, 1)])
 def test_bmfr_matches_oracle(cuda, oracle, bw, fk, position_type):
     import vulkanpbrt_gb300 as vp
@@ -60,12 +67,45 @@ def test_bmfr_matches_oracle(cuda, oracle, bw, fk, position_type):
         fin = get(bm.get_final_descriptor_image())
         layer = (frame & 1) ^ 1
         frac = stats(f"bmfr bw={bw} pt={position_type} frame={frame} denoised", den[layer], den_ref[layer])
-        assert frac >= 0.999
+        assert frac >= MIN_FRACTION[bw]
         lsb = np.abs(fin.astype(int) - fin_ref.astype(int))
         print(f"  final: max |diff| {lsb.max()} LSB, >1 LSB on {(lsb > 1).mean() * 100:.4f}%")
         assert (lsb <= 1).mean() >= 0.999
         w = get(bm.weights)[..., 0]
         assert np.isfinite(w).mean() > 0.99
+
+
+@pytest.mark.parametrize("bw,fk", [(32, 256), (16, 256), (8, 64)])
+def test_bmfr_fit_is_bit_exact_when_inputs_agree(cuda, oracle, bw, fk):
+    """With normals whose decode is exact on both sides (theta = phi = 0) the
+    fit sees bit-identical features: weights and denoised output must then be
+    bit-identical to the oracle (same summation order, same rounding)."""
+    import vulkanpbrt_gb300 as vp
+    from vulkanpbrt_gb300.camera import col_major
+
+    W, H = 256, 160
+    den_ref = np.zeros((2, H, W, 4), np.float16)
+    for frame in (0, 1):
+        s = inputs(W, H, seed=7, frame=frame)
+        s["normal"] = np.zeros_like(s["normal"])
+        if frame == 0:
+            g, illu, acc, bm = _setup(vp, s, W, H, bw, "bmfr", fk)
+        else:
+            put(acc.motion, s["motion"])
+            put(acc.spp, s["spp"])
+            put(illu.illumination_images[0], s["noisy16"])
+            put(g.normal, s["normal"])
+        cam = s["camera"]
+        bm.dispatch(_pc(vp, cam, frame))
+        _, w_ref, fin_ref = oracle.bmfr(bw, fk, frame, 0, col_major(cam.inv_view), col_major(cam.inv_proj),
+                                        s["depth"], s["normal"], s["albedo"], s["noisy16"], s["motion"], s["spp"],
+                                        den_ref)
+        w = get(bm.weights)[..., 0]
+        assert np.array_equal(w, w_ref, equal_nan=True), f"weights differ in {(w != w_ref).sum()} entries"
+        den = get(bm.denoised)
+        assert np.array_equal(den.view(np.uint16), den_ref.view(np.uint16))
+        fin = get(bm.get_final_descriptor_image())
+        assert np.abs(fin.astype(int) - fin_ref.astype(int)).max() <= 1
 
 
 @pytest.mark.parametrize("bw", [16, 8, 32])

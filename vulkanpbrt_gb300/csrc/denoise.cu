@@ -259,7 +259,7 @@ PBRT_D float3 bmfr_world_dir(const BmfrParams& p, int ix, int iy) {
 }
 
 template <int BW>
-__global__ void __launch_bounds__(BmfrShape<BW>::NT) bmfr_fused_kernel(BmfrParams p) {
+__global__ void __launch_bounds__(BmfrShape<BW>::NT, BW == 8 ? 8 : 3) bmfr_fused_kernel(BmfrParams p) {
   using S = BmfrShape<BW>;
   constexpr int NT = S::NT, SV = S::SV, NW = S::NW, P = S::P;
   extern __shared__ float smem[];
@@ -269,6 +269,7 @@ __global__ void __launch_bounds__(BmfrShape<BW>::NT) bmfr_fused_kernel(BmfrParam
   float(*Rm)[13] = reinterpret_cast<float(*)[13]>(fq + 13 * S::PAD + 2 * NW * 16 + 32);  // [10][13]
   float* wsm = fq + 13 * S::PAD + 2 * NW * 16 + 32 + 130;                               // [30]
   float(*mmred)[6] = reinterpret_cast<float(*)[6]>(wsm + 32);                          // [NW][6]
+  float(*redS)[NW] = reinterpret_cast<float(*)[NW]>(wsm + 32 + NW * 6);                  // [2][NW]
 
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const int gx = blockIdx.x, gy = blockIdx.y;
@@ -377,31 +378,61 @@ __global__ void __launch_bounds__(BmfrShape<BW>::NT) bmfr_fused_kernel(BmfrParam
 #pragma unroll
     for (int c = 0; c < 13; ++c) X[s][c] = fq[c * S::PAD + ri];
   }
+  // The staging area is dead now: park each pixel's decoded normal and
+  // normalised position there until the output pass (keeps them out of
+  // registers during the QR).
+  __syncthreads();
+#pragma unroll
+  for (int s = 0; s < SV; ++s) {
+    int q = t + s * NT;
+    fq[0 * P + q] = nor[s].x;
+    fq[1 * P + q] = nor[s].y;
+    fq[2 * P + q] = nor[s].z;
+    fq[3 * P + q] = pos[s].x;
+    fq[4 * P + q] = pos[s].y;
+    fq[5 * P + q] = pos[s].z;
+  }
   float ulen2 = 0.f;
 #pragma unroll
   for (int col = 0; col < 10; ++col) {
     const int buf = col & 1;
-    // Partials: slot col = sum over rows r > col of x_col^2, slot f > col =
-    // sum over rows r > col of x_f * x_col; row col itself is added after the
-    // reduction, once the reflector's first component is known.
+    // (1) squared length of the column below the diagonal, summed per thread
+    // in row order, then a 32-lane xor butterfly, then warps in order -- the
+    // order the oracle restates (bmfrFit.comp:28-36).
+    float sp = 0.f;
+#pragma unroll
+    for (int s = 0; s < SV; ++s) {
+      int r = t + s * NT;
+      if (r > col) sp = sp + X[s][col] * X[s][col];
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) sp = sp + __shfl_xor_sync(kFull, sp, o);
+    if (lane == 0) redS[buf][warp] = sp;
+    if (t == col) {
+#pragma unroll
+      for (int f = 0; f < 13; ++f) rowc[buf][f] = X[0][f];
+    }
+    __syncthreads();
+    float S2 = redS[buf][0];
+    for (int w = 1; w < NW; ++w) S2 = S2 + redS[buf][w];
+    const float xcc = rowc[buf][col];
+    const float vlen = sqrtf(S2 + xcc * xcc);  // bmfrFit.comp:41-44
+    const float ucol = xcc - vlen;
+    ulen2 = S2 + ucol * ucol;
+    // (2) v_f = sum over rows r >= col of x_f * u (bmfrFit.comp:53-61),
+    // all trailing columns in one transpose reduction.
     float v[16];
 #pragma unroll
     for (int i = 0; i < 16; ++i) v[i] = 0.f;
 #pragma unroll
     for (int s = 0; s < SV; ++s) {
       int r = t + s * NT;
-      if (r > col) {
-        float xc = X[s][col];
+      if (r >= col) {
+        float u = (r == col) ? ucol : X[s][col];
 #pragma unroll
-        for (int f = 0; f < 13; ++f) {
-          if (f == col) v[f] = v[f] + xc * xc;
-          else if (f > col) v[f] = v[f] + X[s][f] * xc;
-        }
+        for (int f = 0; f < 13; ++f)
+          if (f > col) v[f] = v[f] + X[s][f] * u;
       }
-    }
-    if (t == col) {
-#pragma unroll
-      for (int f = 0; f < 13; ++f) rowc[buf][f] = X[0][f];
     }
     warp_transpose_reduce<16>(v, lane);
     if ((lane & 1) == 0 && (lane >> 1) < 13) red[buf][warp][lane >> 1] = v[0];
@@ -411,25 +442,22 @@ __global__ void __launch_bounds__(BmfrShape<BW>::NT) bmfr_fused_kernel(BmfrParam
       tot = red[buf][0][lane];
       for (int w = 1; w < NW; ++w) tot = tot + red[buf][w][lane];
     }
-    const float S2 = __shfl_sync(kFull, tot, col);
-    const float xcc = rowc[buf][col];
-    const float vlen = sqrtf(S2 + xcc * xcc);
-    const float ucol = xcc - vlen;
-    ulen2 = S2 + ucol * ucol;
-    float coef[13];
+    // (3) reflect the trailing columns (bmfrFit.comp:62-67); the shader's
+    // division by |u|^2 is a product with its reciprocal (Vulkan allows
+    // 2.5 ULP for x / y).
+    const float rl = 1.f / ulen2;
 #pragma unroll
     for (int f = 0; f < 13; ++f) {
-      float D = __shfl_sync(kFull, tot, f);
-      coef[f] = (f > col) ? (D + rowc[buf][f] * ucol) / ulen2 : 0.f;
-    }
+      const float vf = __shfl_sync(kFull, tot, f);
+      if (f > col) {
 #pragma unroll
-    for (int s = 0; s < SV; ++s) {
-      int r = t + s * NT;
-      if (r >= col) {
-        float u = (r == col) ? ucol : X[s][col];
-#pragma unroll
-        for (int f = 0; f < 13; ++f)
-          if (f > col) X[s][f] = X[s][f] - 2.f * u * coef[f];
+        for (int s = 0; s < SV; ++s) {
+          int r = t + s * NT;
+          if (r >= col) {
+            float u = (r == col) ? ucol : X[s][col];
+            X[s][f] = X[s][f] - 2.f * u * vf * rl;
+          }
+        }
       }
     }
     if (t == col) {
@@ -479,13 +507,17 @@ __global__ void __launch_bounds__(BmfrShape<BW>::NT) bmfr_fused_kernel(BmfrParam
   }
 #pragma unroll
   for (int s = 0; s < SV; ++s) {
-    if (!inside[s]) continue;
-    float3 n = nor[s], ps = pos[s];
+    const int q = t + s * NT, lx = q % BW, ly = q / BW;
+    const int ax = gx * BW + lx - offx, ay = gy * BW + ly - offy;
+    const int ix = mirror1(ax, p.W), iy = mirror1(ay, p.H);
+    if (ax != ix || ay != iy) continue;
+    float3 n = f3(fq[0 * P + q], fq[1 * P + q], fq[2 * P + q]);
+    float3 ps = f3(fq[3 * P + q], fq[4 * P + q], fq[5 * P + q]);
     float f[10] = {1.f, n.x, n.y, n.z, ps.x, ps.y, ps.z, ps.x * ps.x, ps.y * ps.y, ps.z * ps.z};
     float3 dc = f3(0.f);
 #pragma unroll
     for (int i = 0; i < 10; ++i) dc = dc + f3(w[i * 3], w[i * 3 + 1], w[i * 3 + 2]) * f[i];
-    post_store(p.post, dc, ixs[s], iys[s]);
+    post_store(p.post, dc, ix, iy);
   }
 }
 
@@ -798,7 +830,7 @@ static Mat4 to_mat4(const float* m) {
 static size_t bmfr_smem_bytes(int bw) {
   int P = bw * bw, NT = bw == 8 ? 64 : 256, NW = NT / 32;
   int pad = P + P / 32;
-  return sizeof(float) * (size_t)(13 * pad + 2 * NW * 16 + 32 + 130 + 32 + NW * 6);
+  return sizeof(float) * (size_t)(13 * pad + 2 * NW * 16 + 32 + 130 + 32 + NW * 6 + 2 * NW);
 }
 
 }  // namespace pbrt
@@ -978,10 +1010,12 @@ PBRT_API int pbrt_bmfr_create(uint32_t width, uint32_t height, uint32_t work_wid
   if (st) return st;
   if (work_width != work_height || (work_width != 8 && work_width != 16 && work_width != 32))
     return fail(PBRT_ERROR_UNSUPPORTED, "BMFR: work size %ux%u (supported: 8x8, 16x16, 32x32)", work_width, work_height);
-  uint32_t P = work_width * work_width;
-  if (fitting_kernel == 0 || fitting_kernel > 1024 || P % fitting_kernel != 0 || fitting_kernel % 32 != 0)
-    return fail(PBRT_ERROR_INVALID_ARGUMENT, "BMFR: fitting kernel %u must divide %u and be a multiple of 32",
-                fitting_kernel, P);
+  // The fit's reduction grouping is its invocation count: DenoiserUtils.cpp
+  // uses 64 invocations for 8x8 blocks and 256 otherwise (BMFR.hpp:19).
+  uint32_t want_k = work_width == 8 ? 64u : 256u;
+  if (fitting_kernel != want_k)
+    return fail(PBRT_ERROR_UNSUPPORTED, "BMFR: fitting kernel %u for %ux%u blocks (supported: %u)", fitting_kernel,
+                work_width, work_height, want_k);
   if (width < 2 * work_width + 2 || height < 2 * work_height + 2)
     return fail(PBRT_ERROR_INVALID_ARGUMENT, "BMFR: image %ux%u smaller than the mirror padding allows (>= %u)",
                 width, height, 2 * work_width + 2);
