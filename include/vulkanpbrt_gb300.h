@@ -57,7 +57,8 @@ typedef enum PbrtFormat {
   PBRT_FORMAT_R16G16B16A16_SFLOAT = 6,
   PBRT_FORMAT_R8_UNORM = 7,
   PBRT_FORMAT_R8G8B8A8_UNORM = 8,
-  PBRT_FORMAT_B8G8R8A8_UNORM = 9
+  PBRT_FORMAT_B8G8R8A8_UNORM = 9,
+  PBRT_FORMAT_R32_UINT = 10
 } PbrtFormat;
 
 /* A device image: texel (x, y) of layer l is at
@@ -196,6 +197,124 @@ PBRT_API int pbrt_bfr_create(uint32_t width, uint32_t height, uint32_t work_widt
 PBRT_API int pbrt_bfr_dispatch(PbrtBFR* b, const PbrtPushConstants* pc, pbrt_stream_t stream);
 PBRT_API int pbrt_bfr_final_image(const PbrtBFR* b, PbrtImage* out);
 PBRT_API int pbrt_bfr_images(const PbrtBFR* b, PbrtImage* denoised);
+
+/* ---- Scene (RayTracingSceneDescriptorCreationVisitor output) -----------
+ * The shader-side data model of source/scene/RayTracingVisitor.{hpp,cpp}:
+ * non-interleaved per-mesh positions / normals / uvs and u16 or u32 indices
+ * (RayTracingVisitor.cpp:29-168), ObjectInstance (ptStructures.glsl:10-15,
+ * RayTracingVisitor.hpp:37-43), WaveFrontMaterialPacked per mesh
+ * (RayTracingVisitor.hpp:44-53), vsg::Light::PackedLight
+ * (external/vsg/include/vsg/nodes/Light.h:23-37), five texture slots per
+ * mesh (diffuse, mr, normal, emissive, specular; RGBA8, bilinear, REPEAT,
+ * level 0) and the per-instance opacity flags PBRTPipeline::set_tlas reads
+ * (PBRTPipeline.cpp:38-56). pbrt_scene_create replaces the visitor's
+ * descriptor upload plus BuildAccelerationStructureTraversal: it flattens the
+ * instances to world-space triangles and builds the 8-wide BVH. */
+typedef struct PbrtMeshDesc {
+  const float* positions; /* 3 per vertex */
+  const float* normals;   /* 3 per vertex */
+  const float* uvs;       /* 2 per vertex */
+  uint32_t vertex_count;
+  const void* indices; /* uint16 (index_stride 2) or uint32 (4) */
+  uint32_t index_count;
+  uint32_t index_stride;
+} PbrtMeshDesc;
+typedef struct PbrtObjectInstance {
+  float object_mat[16]; /* column major */
+  int32_t mesh_id;
+  uint32_t index_stride;
+  int32_t pad[2];
+} PbrtObjectInstance;
+typedef struct PbrtMaterialPacked {
+  float ambient_roughness[4];
+  float diffuse_ior[4];
+  float specular_dissolve[4];
+  float transmittance_illum[4];
+  float emission_texture_id[4];
+  uint32_t category_id;
+  float pad[3];
+} PbrtMaterialPacked;
+typedef struct PbrtPackedLight {
+  float v0[3];
+  float type; /* 1 directional, 2 point, 5 area triangle */
+  float v1[3];
+  float radius;
+  float v2[3];
+  float angle;
+  float dir[3];
+  float angle2;
+  float color_ambient[4];
+  float color_diffuse[4];
+  float color_specular[4];
+  float strengths[3]; /* attenuation 1 / (x + y d + z d^2) */
+  float inclusive_strength;
+} PbrtPackedLight;
+typedef struct PbrtTextureDesc {
+  const uint8_t* rgba8;
+  uint32_t width, height;
+} PbrtTextureDesc;
+typedef struct PbrtSceneDesc {
+  uint32_t mesh_count;
+  const PbrtMeshDesc* meshes;
+  uint32_t instance_count;
+  const PbrtObjectInstance* instances;
+  const uint8_t* instance_opaque; /* NULL = all opaque */
+  const PbrtMaterialPacked* materials; /* mesh_count entries, indexed by mesh id */
+  uint32_t light_count;
+  const PbrtPackedLight* lights;
+  uint32_t texture_count; /* entry 0 should be the 1x1 white default */
+  const PbrtTextureDesc* textures;
+  const int32_t* mesh_textures; /* mesh_count x 5 texture indices */
+} PbrtSceneDesc;
+typedef struct PbrtSceneInfo {
+  uint32_t triangle_count, instance_count, bvh_nodes, bvh_depth, light_count;
+  uint64_t bvh_bytes, triangle_bytes;
+  double build_ms;
+} PbrtSceneInfo;
+PBRT_API int pbrt_scene_create(const PbrtSceneDesc* desc, PbrtScene** out);
+PBRT_API int pbrt_scene_info(const PbrtScene* scene, PbrtSceneInfo* info);
+/* Ray queries against the scene (no reference counterpart; the path tracer's
+ * traversal exposed for tests and throughput measurement). Device arrays of n
+ * float4 (origin, tmin) and (direction, tmax); hits_out float4 per ray
+ * (t, u, v, triangle key bits -- the instance-major flat triangle index, or
+ * 0xffffffff on a miss). scratch_u32x2: 8 bytes of device memory. */
+PBRT_API int pbrt_scene_trace_rays(PbrtScene* scene, const void* origins_tmin, const void* directions_tmax, uint32_t n,
+                                   int32_t any_hit, void* hits_out, void* scratch_u32x2, pbrt_stream_t stream);
+
+/* ---- PBRTPipeline (source/renderModules/PBRTPipeline.hpp:19-60) ---------
+ * PBRTPipeline(scene, g_buffer, illumination_buffer, write_g_buffer, ...):
+ * illumination DemodulatedFloat selects DEMOD_ILLUMINATION_FLOAT, FinalFloat
+ * selects FINAL_IMAGE (PBRTPipeline.cpp:171-229). Defaults follow the
+ * reference: max recursion depth 2, min 0, surface-strength light sampling
+ * (uniform above 800 lights, PBRTPipeline.cpp:92-96). */
+PBRT_API int pbrt_pipeline_create(PbrtScene* scene, PbrtGBuffer* g, PbrtIlluminationBuffer* illumination,
+                                  int32_t write_g_buffer, PbrtPipeline** out);
+/* light_sampling: 0 SAMPLE_SURFACE_STRENGTH, 1 SAMPLE_LIGHT_STRENGTH,
+ * 2 SAMPLE_UNIFORM (PBRTPipeline.hpp:32-37); the Infos UBO's
+ * minRecursionDepth / maxRecursionDepth (layoutPTUniform.glsl:4-9). */
+PBRT_API int pbrt_pipeline_set_config(PbrtPipeline* p, int32_t light_sampling, int32_t min_recursion_depth,
+                                      int32_t max_recursion_depth);
+/* PBRTPipeline::add_trace_rays_to_command_graph (PBRTPipeline.cpp:65-80):
+ * one sample per pixel into the illumination (and G-) buffer. The frame's
+ * launches are captured into a CUDA graph on first use. */
+PBRT_API int pbrt_pipeline_trace(PbrtPipeline* p, const PbrtPushConstants* pc, pbrt_stream_t stream);
+typedef struct PbrtTraceStats {
+  uint64_t frames, primary_rays, extension_rays, shadow_rays;
+  uint32_t error_flags; /* bit 0: a traversal ran out of stack */
+} PbrtTraceStats;
+/* BVH queries issued since creation / the last reset (stream-synchronising). */
+PBRT_API int pbrt_pipeline_stats(PbrtPipeline* p, pbrt_stream_t stream, PbrtTraceStats* out);
+PBRT_API int pbrt_pipeline_reset_stats(PbrtPipeline* p, pbrt_stream_t stream);
+/* R32_UINT per pixel: key of the primary ray's closest triangle (see
+ * pbrt_scene_trace_rays), 0xffffffff on a miss. */
+PBRT_API int pbrt_pipeline_debug_images(const PbrtPipeline* p, PbrtImage* primary_hit_key);
+
+/* ---- synthetic workloads (no reference counterpart) -------------------- */
+/* Procedural tileable value-noise RGBA8 texture: kind 0 albedo (sRGB-encoded
+ * colour, optional alpha holes), 1 specular (colour + roughness in alpha),
+ * 2 tangent-space normal map. out_rgba: size * size * 4 bytes of host memory. */
+PBRT_API int pbrt_synth_texture(uint64_t seed, uint32_t size, int32_t kind, const float* color, int32_t alpha_mask,
+                                float rough_lo, float rough_hi, uint8_t* out_rgba);
 
 #ifdef __cplusplus
 }

@@ -127,3 +127,108 @@ def bfr(bw, bh, frame, depth, normal, albedo, motion_f16, spp, noisy_f16, denois
                           threads_default() if threads is None else threads)
     assert rc == 0
     return final
+
+
+# ---------------------------------------------------------------------------
+# Path tracer
+
+
+class OrcScene(C.Structure):
+    _fields_ = [("mesh_count", C.c_uint32), ("mesh_vbase", C.c_void_p), ("mesh_ibase", C.c_void_p),
+                ("mesh_tex", C.c_void_p), ("pos", C.c_void_p), ("nor", C.c_void_p), ("uv", C.c_void_p),
+                ("idx", C.c_void_p), ("instance_count", C.c_uint32), ("inst_mat", C.c_void_p),
+                ("inst_mesh", C.c_void_p), ("inst_stride", C.c_void_p), ("inst_opaque", C.c_void_p),
+                ("inst_tri_count", C.c_void_p), ("materials", C.c_void_p), ("light_count", C.c_uint32),
+                ("lights", C.c_void_p), ("texture_count", C.c_uint32), ("tex_offset", C.c_void_p),
+                ("tex_w", C.c_void_p), ("tex_h", C.c_void_p), ("texels", C.c_void_p)]
+
+
+class OracleScene:
+    """A vulkanpbrt_gb300.scene.Scene packed into the oracle's plain arrays."""
+
+    def __init__(self, scene):
+        vb, ib, pos, nor, uv, idx = [], [], [], [], [], []
+        nv = 0
+        nw = 0
+        for m in scene.meshes:
+            vb.append(nv)
+            ib.append(nw)
+            pos.append(m.positions.reshape(-1))
+            nor.append(m.normals.reshape(-1))
+            uv.append(m.uvs.reshape(-1))
+            if m.index_stride == 4:
+                words = m.indices.astype(np.uint32)
+            else:
+                i16 = m.indices.astype(np.uint32)
+                if len(i16) % 2:
+                    i16 = np.append(i16, 0)
+                words = (i16[0::2] | (i16[1::2] << 16)).astype(np.uint32)
+                words = np.append(words, np.uint32(0))
+            idx.append(words)
+            nv += len(m.positions)
+            nw += len(words)
+        self.a = dict(
+            mesh_vbase=np.array(vb, np.uint32), mesh_ibase=np.array(ib, np.uint32),
+            mesh_tex=np.array(scene.mesh_textures, np.int32).reshape(-1),
+            pos=np.concatenate(pos).astype(np.float32), nor=np.concatenate(nor).astype(np.float32),
+            uv=np.concatenate(uv).astype(np.float32), idx=np.concatenate(idx).astype(np.uint32),
+            inst_mat=np.concatenate([np.asarray(m, np.float32).T.reshape(16) for m in scene.instance_mats]),
+            inst_mesh=np.array(scene.instance_mesh, np.int32),
+            inst_stride=np.array([scene.meshes[m].index_stride for m in scene.instance_mesh], np.uint32),
+            inst_opaque=scene.instance_opaque().astype(np.uint8),
+            inst_tri_count=np.array([scene.meshes[m].tri_count for m in scene.instance_mesh], np.uint32),
+            materials=np.stack(scene.materials).astype(np.float32).reshape(-1),
+            lights=(np.stack(scene.lights) if scene.lights else np.zeros((1, 32), np.float32)).astype(np.float32).reshape(-1),
+            tex_w=np.array([t.shape[1] for t in scene.textures], np.uint32),
+            tex_h=np.array([t.shape[0] for t in scene.textures], np.uint32),
+        )
+        offs, acc = [], 0
+        for t in scene.textures:
+            offs.append(acc)
+            acc += t.shape[0] * t.shape[1]
+        self.a["tex_offset"] = np.array(offs, np.uint64)
+        self.a["texels"] = np.concatenate([np.ascontiguousarray(t, np.uint8).reshape(-1) for t in scene.textures])
+        for k, v in self.a.items():
+            self.a[k] = np.ascontiguousarray(v)
+        s = OrcScene()
+        s.mesh_count = len(scene.meshes)
+        s.instance_count = len(scene.instance_mesh)
+        s.light_count = len(scene.lights)
+        s.texture_count = len(scene.textures)
+        for k, v in self.a.items():
+            setattr(s, k, v.ctypes.data)
+        self.c = s
+
+
+def render(oscene: OracleScene, W, H, inv_view, inv_proj, frame=0, sample=0, min_depth=0, max_depth=2, light_mode=0,
+           final_image=False, precision=32, frames=1, threads=None):
+    """Returns dict(illum [H,W,4] f32, depth, normal [H,W,2], material, albedo [H,W,4] u8, hit_key [H,W] u32, rays)."""
+    out = dict(illum=np.zeros((H, W, 4), np.float32), depth=np.zeros((H, W), np.float32),
+               normal=np.zeros((H, W, 2), np.float32), material=np.zeros((H, W, 4), np.uint8),
+               albedo=np.zeros((H, W, 4), np.uint8), hit_key=np.zeros((H, W), np.uint32))
+    rays = np.zeros(3, np.uint64)
+    rc = lib().oracle_render(C.byref(oscene.c), W, H, _p(_f32(inv_view)), _p(_f32(inv_proj)), C.c_uint32(frame),
+                             C.c_uint32(sample), min_depth, max_depth, light_mode, int(final_image), precision, frames,
+                             _p(out["illum"]), _p(out["depth"]), _p(out["normal"]), _p(out["material"]),
+                             _p(out["albedo"]), _p(out["hit_key"]), _p(rays),
+                             threads_default() if threads is None else threads)
+    assert rc == 0
+    out["rays"] = rays
+    return out
+
+
+def trace_rays(oscene: OracleScene, org_tmin: np.ndarray, dir_tmax: np.ndarray, any_hit=False, precision=64,
+               threads=None) -> np.ndarray:
+    n = len(org_tmin)
+    hits = np.zeros((n, 4), np.float32)
+    rc = lib().oracle_trace_rays(C.byref(oscene.c), _p(np.ascontiguousarray(org_tmin, np.float32)),
+                                 _p(np.ascontiguousarray(dir_tmax, np.float32)), C.c_uint32(n), int(any_hit),
+                                 _p(hits), precision, threads_default() if threads is None else threads)
+    assert rc == 0
+    return hits
+
+
+def rng_stream(x, y, frame, n) -> np.ndarray:
+    out = np.zeros(n, np.float32)
+    lib().oracle_rng_stream(C.c_uint32(x), C.c_uint32(y), C.c_uint32(frame), n, _p(out))
+    return out

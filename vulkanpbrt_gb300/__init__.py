@@ -23,4 +23,7 @@ from .render_modules import (  # noqa: F401
     PushConstants,
 )
 
+from .pipeline import PBRTPipeline, SceneHandle  # noqa: F401,E402
+from . import texsynth  # noqa: F401,E402  (registers pbrt_synth_texture)
+
 __version__ = "0.1.0"

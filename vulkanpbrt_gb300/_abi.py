@@ -33,6 +33,7 @@ FORMATS = {
     7: ("|u1", 1),  # R8_UNORM
     8: ("|u1", 4),  # R8G8B8A8_UNORM
     9: ("|u1", 4),  # B8G8R8A8_UNORM
+    10: ("<u4", 1),  # R32_UINT
 }
 
 

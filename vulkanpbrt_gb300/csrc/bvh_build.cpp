@@ -1,0 +1,298 @@
+// Host BVH build: binned SAH binary tree, then collapse to Node8 (see bvh.hpp).
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <future>
+#include <limits>
+#include <thread>
+
+#include "bvh.hpp"
+
+namespace pbrt {
+namespace {
+
+constexpr int kBins = 32;
+constexpr int kMaxLeaf = 3;
+constexpr uint32_t kParallelCutoff = 1u << 15;
+
+struct Box {
+  float lo[3] = {std::numeric_limits<float>::infinity(), std::numeric_limits<float>::infinity(),
+                 std::numeric_limits<float>::infinity()};
+  float hi[3] = {-std::numeric_limits<float>::infinity(), -std::numeric_limits<float>::infinity(),
+                 -std::numeric_limits<float>::infinity()};
+  void grow(const Box& b) {
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = std::min(lo[a], b.lo[a]);
+      hi[a] = std::max(hi[a], b.hi[a]);
+    }
+  }
+  void grow(const float* p) {
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = std::min(lo[a], p[a]);
+      hi[a] = std::max(hi[a], p[a]);
+    }
+  }
+  double area() const {
+    double d[3];
+    for (int a = 0; a < 3; ++a) d[a] = std::max(0.0, (double)hi[a] - (double)lo[a]);
+    return 2.0 * (d[0] * d[1] + d[1] * d[2] + d[2] * d[0]);
+  }
+  bool empty() const { return !(lo[0] <= hi[0]); }
+};
+
+struct BNode {
+  Box box;
+  int32_t left = -1, right = -1;  // children (internal) or -1 (leaf)
+  uint32_t begin = 0, count = 0;  // leaf range in the index array
+};
+
+struct Builder {
+  std::vector<Box> pbox;
+  std::vector<float> cent;  // 3 per prim
+  std::vector<uint32_t> idx;
+  std::vector<BNode> nodes;
+  std::atomic<uint32_t> next{0};
+
+  uint32_t alloc() { return next.fetch_add(1); }
+
+  void build(uint32_t ni, uint32_t begin, uint32_t count) {
+    BNode& nd = nodes[ni];
+    Box box, cb;
+    for (uint32_t i = begin; i < begin + count; ++i) {
+      box.grow(pbox[idx[i]]);
+      cb.grow(&cent[3 * idx[i]]);
+    }
+    nd.box = box;
+    nd.begin = begin;
+    nd.count = count;
+    if (count <= (uint32_t)kMaxLeaf) return;  // leaves hold up to 3 triangles
+    // Binned SAH over all three axes.
+    double best_cost = std::numeric_limits<double>::infinity();
+    int best_axis = -1, best_split = -1;
+    for (int a = 0; a < 3; ++a) {
+      float ext = cb.hi[a] - cb.lo[a];
+      if (!(ext > 0.f)) continue;
+      Box bb[kBins];
+      uint32_t bc[kBins] = {0};
+      float k = (float)kBins / ext;
+      for (uint32_t i = begin; i < begin + count; ++i) {
+        uint32_t p = idx[i];
+        int b = std::min(kBins - 1, (int)((cent[3 * p + a] - cb.lo[a]) * k));
+        bb[b].grow(pbox[p]);
+        bc[b]++;
+      }
+      double ra[kBins];
+      uint32_t rc[kBins];
+      Box acc;
+      uint32_t n = 0;
+      for (int b = kBins - 1; b > 0; --b) {
+        acc.grow(bb[b]);
+        n += bc[b];
+        ra[b] = acc.empty() ? 0.0 : acc.area();
+        rc[b] = n;
+      }
+      Box lacc;
+      uint32_t ln = 0;
+      for (int b = 0; b < kBins - 1; ++b) {
+        lacc.grow(bb[b]);
+        ln += bc[b];
+        if (ln == 0 || rc[b + 1] == 0) continue;
+        double c = (lacc.empty() ? 0.0 : lacc.area()) * ln + ra[b + 1] * rc[b + 1];
+        if (c < best_cost) {
+          best_cost = c;
+          best_axis = a;
+          best_split = b;
+        }
+      }
+    }
+    uint32_t mid;
+    if (best_axis < 0) {
+      mid = begin + count / 2;  // identical centroids: split by index
+    } else {
+      float k = (float)kBins / (cb.hi[best_axis] - cb.lo[best_axis]);
+      auto it = std::partition(idx.begin() + begin, idx.begin() + begin + count, [&](uint32_t p) {
+        int b = std::min(kBins - 1, (int)((cent[3 * p + best_axis] - cb.lo[best_axis]) * k));
+        return b <= best_split;
+      });
+      mid = (uint32_t)(it - idx.begin());
+      if (mid == begin || mid == begin + count) mid = begin + count / 2;
+    }
+    uint32_t l = alloc(), r = alloc();
+    nd.left = (int32_t)l;
+    nd.right = (int32_t)r;
+    uint32_t lc = mid - begin, rc = begin + count - mid;
+    if (count > kParallelCutoff) {
+      auto f = std::async(std::launch::async, [=]() { build(l, begin, lc); });
+      build(r, mid, rc);
+      f.get();
+    } else {
+      build(l, begin, lc);
+      build(r, mid, rc);
+    }
+  }
+};
+
+struct Collapser {
+  const Builder& b;
+  std::vector<Node8>& out;
+  std::vector<uint32_t>& tri_order;
+  Bvh8Stats st;
+
+  static uint8_t exponent_for(double extent) {
+    // smallest power of two s with extent / s <= 255 (extent taken in double)
+    if (!(extent > 0.0)) return 1;  // 2^-126
+    int e;
+    std::frexp(extent / 255.0, &e);  // extent/255 = m * 2^e with m in [0.5, 1), so 2^e > extent/255
+    return (uint8_t)std::min(254, std::max(1, e + 127));
+  }
+
+  void encode(uint32_t out_index, uint32_t bnode, int depth) {
+    st.depth = std::max(st.depth, depth);
+    // Open the largest child until 8 children (or only leaves remain).
+    std::vector<uint32_t> ch;
+    const BNode& root = b.nodes[bnode];
+    if (root.left < 0) {
+      ch.push_back(bnode);  // single leaf under this node
+    } else {
+      ch.push_back((uint32_t)root.left);
+      ch.push_back((uint32_t)root.right);
+      while (ch.size() < 8) {
+        int best = -1;
+        double best_area = -1.0;
+        for (size_t i = 0; i < ch.size(); ++i) {
+          const BNode& c = b.nodes[ch[i]];
+          if (c.left < 0) continue;
+          double a = c.box.area();
+          if (a > best_area) {
+            best_area = a;
+            best = (int)i;
+          }
+        }
+        if (best < 0) break;
+        uint32_t open = ch[best];
+        ch[best] = (uint32_t)b.nodes[open].left;
+        ch.push_back((uint32_t)b.nodes[open].right);
+      }
+    }
+    // Leaves with more than 3 triangles (identical centroids beyond the leaf
+    // size) cannot happen: build() splits them by index.
+    const Box& nb = root.box;
+    // Octant slot assignment around the node's centre.
+    float pc[3];
+    for (int a = 0; a < 3; ++a) pc[a] = 0.5f * (nb.lo[a] + nb.hi[a]);
+    int slot_of[8];
+    bool used[8] = {false};
+    std::vector<bool> placed(ch.size(), false);
+    for (size_t round = 0; round < ch.size(); ++round) {
+      double best = -std::numeric_limits<double>::infinity();
+      int bc = -1, bs = -1;
+      for (size_t i = 0; i < ch.size(); ++i) {
+        if (placed[i]) continue;
+        const Box& cbx = b.nodes[ch[i]].box;
+        double d[3];
+        for (int a = 0; a < 3; ++a) d[a] = 0.5 * ((double)cbx.lo[a] + cbx.hi[a]) - pc[a];
+        for (int s = 0; s < 8; ++s) {
+          if (used[s]) continue;
+          double score = (s & 1 ? d[0] : -d[0]) + (s & 2 ? d[1] : -d[1]) + (s & 4 ? d[2] : -d[2]);
+          if (score > best) {
+            best = score;
+            bc = (int)i;
+            bs = s;
+          }
+        }
+      }
+      placed[bc] = true;
+      used[bs] = true;
+      slot_of[bc] = bs;
+    }
+    uint32_t slot_child[8];
+    bool slot_used[8] = {false};
+    for (size_t i = 0; i < ch.size(); ++i) {
+      slot_child[slot_of[i]] = ch[i];
+      slot_used[slot_of[i]] = true;
+    }
+    Node8 n;
+    std::memset(&n, 0, sizeof(n));
+    n.px = nb.lo[0];
+    n.py = nb.lo[1];
+    n.pz = nb.lo[2];
+    uint8_t ex[3];
+    float scale[3];
+    for (int a = 0; a < 3; ++a) {
+      ex[a] = exponent_for((double)nb.hi[a] - (double)nb.lo[a]);
+      scale[a] = std::ldexp(1.0f, (int)ex[a] - 127);
+    }
+    n.ex = ex[0];
+    n.ey = ex[1];
+    n.ez = ex[2];
+    const float p[3] = {n.px, n.py, n.pz};
+    // internal children first (to allocate them consecutively), in slot order
+    std::vector<std::pair<uint32_t, uint32_t>> inner;  // (slot, bnode)
+    uint32_t tri_off = 0;
+    n.tri_base = (uint32_t)tri_order.size();
+    for (int s = 0; s < 8; ++s) {
+      if (!slot_used[s]) continue;
+      const BNode& c = b.nodes[slot_child[s]];
+      for (int a = 0; a < 3; ++a) {
+        double lo = std::floor(((double)c.box.lo[a] - p[a]) / scale[a]);
+        double hi = std::ceil(((double)c.box.hi[a] - p[a]) / scale[a]);
+        n.qlo[a][s] = (uint8_t)std::min(255.0, std::max(0.0, lo));
+        n.qhi[a][s] = (uint8_t)std::min(255.0, std::max(0.0, hi));
+      }
+      if (c.left >= 0) {
+        n.imask |= (uint8_t)(1u << s);
+        n.meta[s] = 0x80;
+        inner.push_back({(uint32_t)s, slot_child[s]});
+      } else {
+        n.meta[s] = (uint8_t)((c.count << 5) | tri_off);
+        for (uint32_t k = 0; k < c.count; ++k) tri_order.push_back(b.idx[c.begin + k]);
+        tri_off += c.count;
+        st.leaves++;
+      }
+    }
+    n.child_base = (uint32_t)out.size();
+    out.resize(out.size() + inner.size());
+    out[out_index] = n;
+    uint32_t base = n.child_base;
+    for (size_t i = 0; i < inner.size(); ++i) encode(base + (uint32_t)i, inner[i].second, depth + 1);
+  }
+};
+
+}  // namespace
+
+void build_bvh8(const float* v, size_t n, std::vector<Node8>& nodes, std::vector<uint32_t>& tri_order,
+                Bvh8Stats* stats) {
+  auto t0 = std::chrono::steady_clock::now();
+  Builder b;
+  b.pbox.resize(n);
+  b.cent.resize(3 * n);
+  b.idx.resize(n);
+  for (size_t i = 0; i < n; ++i) {
+    Box bx;
+    bx.grow(v + 9 * i);
+    bx.grow(v + 9 * i + 3);
+    bx.grow(v + 9 * i + 6);
+    b.pbox[i] = bx;
+    for (int a = 0; a < 3; ++a) b.cent[3 * i + a] = 0.5f * (bx.lo[a] + bx.hi[a]);
+    b.idx[i] = (uint32_t)i;
+  }
+  b.nodes.resize(std::max<size_t>(1, 2 * n));
+  uint32_t root = b.alloc();
+  b.build(root, 0, (uint32_t)n);
+  nodes.clear();
+  tri_order.clear();
+  tri_order.reserve(n);
+  nodes.resize(1);
+  Collapser c{b, nodes, tri_order, {}};
+  c.encode(0, root, 0);
+  if (stats) {
+    *stats = c.st;
+    stats->nodes = nodes.size();
+    stats->tris = tri_order.size();
+    stats->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
+}
+
+}  // namespace pbrt

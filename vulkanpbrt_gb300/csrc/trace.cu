@@ -1,0 +1,1234 @@
+// Wavefront path tracer on sm_103a: the per-frame path of ptRaygen.rgen with
+// ptClosesthit / ptAlphaHit / ptMiss / shadow.rmiss, NEE with multiple-
+// importance light sampling (lighting.glsl) and BRDF importance sampling
+// (sampling.glsl, brdf.glsl).
+//
+// One frame = raygen, then per bounce: closest-hit traversal of the ray
+// queue (persistent warps), shading (surface, next-event light choice, BRDF
+// sample, Russian roulette) that compacts surviving paths into the next ray
+// queue and shadow rays into the shadow queue with warp-aggregated atomics,
+// any-hit traversal of the shadow queue which resolves the pending NEE term,
+// and a final pass that clamps and demodulates. The launch sequence of a
+// frame is captured once in a CUDA graph and replayed.
+//
+// Path semantics follow the shaders, with one definition the shaders leave
+// open: when indirectLighting() returns early (zero BRDF, pdf < 1e-6 or a
+// Russian-roulette kill) the reference keeps iterating with a zero-length
+// view vector (NaN) whose outcome depends on the driver's min/max/clamp NaN
+// rules; here the path ends, which is what those early returns mean. A path
+// that misses also ends (later iterations add nothing and draw no numbers).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "internal.hpp"
+#include "shading.cuh"
+
+namespace pbrt {
+
+constexpr unsigned kFullMask = 0xffffffffu;
+
+// ---------------------------------------------------------------------------
+// Watertight ray/triangle test (Woop, Benthin & Wald, JCGT 2013), every
+// operation rounded explicitly (no contraction) so that the CPU oracle's FP32
+// test takes identical decisions.
+struct RayPre {
+  float3 o, d, inv;
+  int kx, ky, kz, oct;
+  float Sx, Sy, Sz;
+};
+
+PBRT_D float comp(float3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+
+PBRT_D RayPre ray_pre(float3 o, float3 d) {
+  RayPre r;
+  r.o = o;
+  r.d = d;
+  float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+  r.kz = (ax > ay && ax > az) ? 0 : (ay > az ? 1 : 2);
+  r.kx = (r.kz + 1) % 3;
+  r.ky = (r.kx + 1) % 3;
+  float dz = comp(d, r.kz);
+  if (dz < 0.f) {
+    int t = r.kx;
+    r.kx = r.ky;
+    r.ky = t;
+  }
+  r.Sx = __fdiv_rn(comp(d, r.kx), dz);
+  r.Sy = __fdiv_rn(comp(d, r.ky), dz);
+  r.Sz = __fdiv_rn(1.0f, dz);
+  // slab test reciprocals (tiny components clamped away from zero)
+  auto safe = [](float x) { return fabsf(x) < 1e-20f ? copysignf(1e-20f, x) : x; };
+  r.inv = f3(1.f / safe(d.x), 1.f / safe(d.y), 1.f / safe(d.z));
+  r.oct = (d.x < 0.f ? 1 : 0) | (d.y < 0.f ? 2 : 0) | (d.z < 0.f ? 4 : 0);
+  return r;
+}
+
+PBRT_D bool tri_intersect(const RayPre& r, float4 a, float4 b, float4 c, float tmin, float& t, float& u, float& v) {
+  float3 A = f3(__fsub_rn(a.x, r.o.x), __fsub_rn(a.y, r.o.y), __fsub_rn(a.z, r.o.z));
+  float3 B = f3(__fsub_rn(b.x, r.o.x), __fsub_rn(b.y, r.o.y), __fsub_rn(b.z, r.o.z));
+  float3 C = f3(__fsub_rn(c.x, r.o.x), __fsub_rn(c.y, r.o.y), __fsub_rn(c.z, r.o.z));
+  float Akz = comp(A, r.kz), Bkz = comp(B, r.kz), Ckz = comp(C, r.kz);
+  float Ax = __fsub_rn(comp(A, r.kx), __fmul_rn(r.Sx, Akz)), Ay = __fsub_rn(comp(A, r.ky), __fmul_rn(r.Sy, Akz));
+  float Bx = __fsub_rn(comp(B, r.kx), __fmul_rn(r.Sx, Bkz)), By = __fsub_rn(comp(B, r.ky), __fmul_rn(r.Sy, Bkz));
+  float Cx = __fsub_rn(comp(C, r.kx), __fmul_rn(r.Sx, Ckz)), Cy = __fsub_rn(comp(C, r.ky), __fmul_rn(r.Sy, Ckz));
+  float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+  float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+  float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+  if (U == 0.f || V == 0.f || W == 0.f) {  // edge cases re-evaluated exactly enough in FP64
+    U = (float)__dsub_rn(__dmul_rn((double)Cx, (double)By), __dmul_rn((double)Cy, (double)Bx));
+    V = (float)__dsub_rn(__dmul_rn((double)Ax, (double)Cy), __dmul_rn((double)Ay, (double)Cx));
+    W = (float)__dsub_rn(__dmul_rn((double)Bx, (double)Ay), __dmul_rn((double)By, (double)Ax));
+  }
+  if ((U < 0.f || V < 0.f || W < 0.f) && (U > 0.f || V > 0.f || W > 0.f)) return false;
+  float det = __fadd_rn(__fadd_rn(U, V), W);
+  if (det == 0.f) return false;
+  float Az = __fmul_rn(r.Sz, Akz), Bz = __fmul_rn(r.Sz, Bkz), Cz = __fmul_rn(r.Sz, Ckz);
+  float T = __fadd_rn(__fadd_rn(__fmul_rn(U, Az), __fmul_rn(V, Bz)), __fmul_rn(W, Cz));
+  float rcp = __fdiv_rn(1.0f, det);
+  t = __fmul_rn(T, rcp);
+  if (!(t > tmin)) return false;
+  u = __fmul_rn(V, rcp);
+  v = __fmul_rn(W, rcp);
+  return true;
+}
+
+// Result of a traversal: BVH-order triangle slot (-1 = miss) and attributes.
+struct Hit {
+  int tri;
+  float t, u, v;
+};
+
+template <bool ANY_HIT>
+PBRT_D Hit traverse(const SceneView& sc, const RayPre& r, float tmin, float tmax, int* err) {
+  Hit best;
+  best.tri = -1;
+  best.t = tmax;
+  best.u = best.v = 0.f;
+  uint32_t best_key = 0xffffffffu;
+  uint2 stack[kStackSize];
+  int sp = 0;
+  uint32_t node = 0;
+  const float4* nodes4 = reinterpret_cast<const float4*>(sc.nodes);
+  while (true) {
+    const float4 n0 = __ldg(nodes4 + 5 * node + 0);
+    const float4 n1 = __ldg(nodes4 + 5 * node + 1);
+    const float4 n2 = __ldg(nodes4 + 5 * node + 2);
+    const float4 n3 = __ldg(nodes4 + 5 * node + 3);
+    const float4 n4 = __ldg(nodes4 + 5 * node + 4);
+    const uint32_t emi = __float_as_uint(n0.w);
+    const float sx = __uint_as_float(((emi >> 0) & 0xffu) << 23);
+    const float sy = __uint_as_float(((emi >> 8) & 0xffu) << 23);
+    const float sz = __uint_as_float(((emi >> 16) & 0xffu) << 23);
+    const uint32_t imask = emi >> 24;
+    const uint32_t child_base = __float_as_uint(n1.x), tri_base = __float_as_uint(n1.y);
+    const uint32_t meta_lo = __float_as_uint(n1.z), meta_hi = __float_as_uint(n1.w);
+    // t = (p + scale * q - o) * inv = q * (scale * inv) + (p - o) * inv
+    const float adx = (n0.x - r.o.x) * r.inv.x, ady = (n0.y - r.o.y) * r.inv.y, adz = (n0.z - r.o.z) * r.inv.z;
+    const float scx = sx * r.inv.x, scy = sy * r.inv.y, scz = sz * r.inv.z;
+    const uint2 qlx = make_uint2(__float_as_uint(n2.x), __float_as_uint(n2.y));
+    const uint2 qly = make_uint2(__float_as_uint(n2.z), __float_as_uint(n2.w));
+    const uint2 qlz = make_uint2(__float_as_uint(n3.x), __float_as_uint(n3.y));
+    const uint2 qhx = make_uint2(__float_as_uint(n3.z), __float_as_uint(n3.w));
+    const uint2 qhy = make_uint2(__float_as_uint(n4.x), __float_as_uint(n4.y));
+    const uint2 qhz = make_uint2(__float_as_uint(n4.z), __float_as_uint(n4.w));
+    uint32_t inner = 0;
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+      const uint32_t meta = ((s < 4 ? meta_lo : meta_hi) >> (8 * (s & 3))) & 0xffu;
+      if (meta == 0) continue;
+      const int sh = 8 * (s & 3);
+      float lx = (float)(((s < 4 ? qlx.x : qlx.y) >> sh) & 0xffu), hx = (float)(((s < 4 ? qhx.x : qhx.y) >> sh) & 0xffu);
+      float ly = (float)(((s < 4 ? qly.x : qly.y) >> sh) & 0xffu), hy = (float)(((s < 4 ? qhy.x : qhy.y) >> sh) & 0xffu);
+      float lz = (float)(((s < 4 ? qlz.x : qlz.y) >> sh) & 0xffu), hz = (float)(((s < 4 ? qhz.x : qhz.y) >> sh) & 0xffu);
+      float tx0 = fmaf(lx, scx, adx), tx1 = fmaf(hx, scx, adx);
+      float ty0 = fmaf(ly, scy, ady), ty1 = fmaf(hy, scy, ady);
+      float tz0 = fmaf(lz, scz, adz), tz1 = fmaf(hz, scz, adz);
+      float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
+      float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), best.t));
+      // widened by a few ulp: the quantised boxes are conservative, the
+      // slab arithmetic must not undo that
+      tn = tn - fabsf(tn) * 4e-7f;
+      tf = tf + fabsf(tf) * 4e-7f;
+      if (!(tn <= tf)) continue;
+      if (meta & 0x80u) {
+        inner |= 1u << (s ^ r.oct);
+      } else {
+        const uint32_t cnt = meta >> 5, off = meta & 31u;
+        for (uint32_t k = 0; k < cnt; ++k) {
+          const uint32_t ti = tri_base + off + k;
+          const float4 a = __ldg(sc.tris + 3 * ti), b = __ldg(sc.tris + 3 * ti + 1), c = __ldg(sc.tris + 3 * ti + 2);
+          float t, u, v;
+          if (!tri_intersect(r, a, b, c, tmin, t, u, v)) continue;
+          const uint32_t key = __float_as_uint(a.w);
+          if (!(t < best.t || (t == best.t && key < best_key))) continue;
+          if (sc.any_alpha && !alpha_accept(sc, __float_as_uint(b.w), __float_as_uint(c.w), u, v)) continue;
+          best.tri = (int)ti;
+          best.t = t;
+          best.u = u;
+          best.v = v;
+          best_key = key;
+          if (ANY_HIT) return best;
+        }
+      }
+    }
+    if (inner) {
+      const int k = __ffs(inner) - 1;
+      inner &= inner - 1;
+      const int s = k ^ r.oct;
+      if (inner) {
+        if (sp == kStackSize) {
+          *err = 1;
+          return best;
+        }
+        stack[sp++] = make_uint2(child_base, (imask << 8) | inner);
+      }
+      node = child_base + __popc(imask & ((1u << s) - 1u));
+      continue;
+    }
+    if (sp == 0) break;
+    uint2 g = stack[--sp];
+    uint32_t m = g.y & 0xffu;
+    const uint32_t im = g.y >> 8;
+    const int k = __ffs(m) - 1;
+    m &= m - 1;
+    const int s = k ^ r.oct;
+    if (m) stack[sp++] = make_uint2(g.x, (im << 8) | m);
+    node = g.x + __popc(im & ((1u << s) - 1u));
+  }
+  return best;
+}
+
+// ---------------------------------------------------------------------------
+// Per-frame parameters and queues.
+struct FrameParams {
+  Mat4 inv_view, inv_proj;
+  uint32_t frame, sample;
+  int W, H;
+  int min_depth, max_depth;  // Infos.minRecursionDepth / maxRecursionDepth
+  int light_mode;            // 0 surface strength, 1 light strength, 2 uniform
+  int final_image;           // FINAL_IMAGE (progressive sRGB) instead of DEMOD_ILLUMINATION_FLOAT
+  int write_gbuffer;
+};
+
+struct Counters {
+  uint32_t ray[2];       // ray queue sizes (ping-pong)
+  uint32_t shadow;       // shadow queue size
+  uint32_t work_trace;   // persistent-warp work index, closest hit
+  uint32_t work_shadow;  // persistent-warp work index, any hit
+  uint32_t error;        // traversal stack overflow
+  uint32_t pad[2];
+  unsigned long long rays_primary, rays_extension, rays_shadow, frames;
+};
+
+struct Queues {
+  // ray queues (2, ping-pong): path index, origin|tmin, direction|tmax
+  uint32_t* pix[2];
+  float4* org[2];
+  float4* dir[2];
+  float4* hit;  // t, u, v, triangle slot (bits; -1 miss)
+  // shadow queue: path index, origin|tmin, direction|tmax, pending NEE, add term
+  uint32_t* spix;
+  float4* sorg;
+  float4* sdir;
+  float4* snee;  // unshadowed NEE contribution xyz, w = 0 primary / 1 indirect
+  float4* sadd;  // emission term added with it
+  // path state
+  uint4* rng;
+  float4* thr;   // throughput
+  float4* rad;   // accumulated radiance (finalColor)
+  float4* prev;  // previous vertex (worldSpacePos) xyz, w = loop index i (as int bits)
+  float4* alb;   // primary albedo xyz (float, for demodulation), w = transDepth (int bits)
+  uint32_t* prim_key;  // primary hit key per pixel (0xffffffff = miss), for parity tests
+};
+
+struct GBufferOut {
+  float* depth;
+  float2* normal;
+  uchar4* material;
+  uchar4* albedo;
+};
+
+// Warp-aggregated queue slot: one atomic per warp.
+PBRT_D int warp_alloc(uint32_t* counter, bool want) {
+  const unsigned active = __activemask();
+  const unsigned m = __ballot_sync(active, want);
+  if (m == 0) return -1;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(m) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
+  base = __shfl_sync(active, base, leader);
+  if (!want) return -1;
+  return (int)(base + __popc(m & ((1u << lane) - 1u)));
+}
+
+// ---------------------------------------------------------------------------
+__global__ void k_frame_begin(Counters* c, const FrameParams* fp) {
+  c->ray[0] = (uint32_t)(fp->W * fp->H);
+  c->ray[1] = 0;
+  c->shadow = 0;
+  c->work_trace = 0;
+  c->work_shadow = 0;
+  c->rays_primary += (unsigned long long)(fp->W * fp->H);
+  c->frames += 1;
+}
+
+__global__ void k_bounce_begin(Counters* c, int k) {
+  // queue k&1 was filled by the previous shade (or raygen)
+  if (k > 0) c->rays_extension += c->ray[k & 1];
+  c->ray[(k + 1) & 1] = 0;
+  c->shadow = 0;
+  c->work_trace = 0;
+  c->work_shadow = 0;
+}
+
+__global__ void k_bounce_end(Counters* c) { c->rays_shadow += c->shadow; }
+
+// createRay (camera.glsl:6-16) and the RNG seeding of ptRaygen.rgen:28-40.
+__global__ void k_raygen(const FrameParams* __restrict__ fpp, Queues q) {
+  const FrameParams& fp = *fpp;
+  const int N = fp.W * fp.H;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) {
+    const int x = p % fp.W, y = p / fp.W;
+    Rng re = rng_init((uint32_t)x, (uint32_t)y, fp.frame);
+    float pcx = (float)x + .5f, pcy = (float)y + .5f;
+    if (fp.final_image && fp.sample > 0) {  // antiAlias: only FINAL_IMAGE after the first sample
+      float jx = rng_next(re), jy = rng_next(re);
+      pcx += jx - .5f;
+      pcy += jy - .5f;
+    }
+    const float cx = pcx / (float)fp.W * 2.0f - 1.0f, cy = pcy / (float)fp.H * 2.0f - 1.0f;
+    const float4 org = fp.inv_view.c[3];
+    float4 d = mul(fp.inv_proj, make_float4(cx, cy, 1.f, 1.f));
+    float3 nd = normalize(f3(d.x, d.y, d.z));
+    d = mul(fp.inv_view, make_float4(nd.x, nd.y, nd.z, 0.f));
+    q.pix[0][p] = (uint32_t)p;
+    q.org[0][p] = make_float4(org.x, org.y, org.z, 0.001f);
+    q.dir[0][p] = make_float4(d.x, d.y, d.z, 10000.0f);
+    q.rng[p] = make_uint4(re.x, re.y, re.z, re.w);
+    q.thr[p] = make_float4(1.f, 1.f, 1.f, 0.f);
+    q.rad[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+    q.prev[p] = make_float4(org.x, org.y, org.z, __int_as_float(0));
+    q.alb[p] = make_float4(0.f, 0.f, 0.f, __int_as_float(0));
+  }
+}
+
+// Closest-hit traversal of the ray queue by persistent warps.
+__global__ void __launch_bounds__(128) k_trace_closest(SceneView sc, Queues q, Counters* c, int k) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t count = *((volatile uint32_t*)&c->ray[k & 1]);
+  const uint32_t* pix = q.pix[k & 1];
+  (void)pix;
+  const float4* org = q.org[k & 1];
+  const float4* dir = q.dir[k & 1];
+  int err = 0;
+  while (true) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(&c->work_trace, 32u);
+    base = __shfl_sync(kFullMask, base, 0);
+    if (base >= count) break;
+    const uint32_t i = base + lane;
+    if (i < count) {
+      const float4 o = org[i], d = dir[i];
+      RayPre r = ray_pre(f3(o.x, o.y, o.z), f3(d.x, d.y, d.z));
+      Hit h = traverse<false>(sc, r, o.w, d.w, &err);
+      q.hit[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
+    }
+  }
+  if (err) atomicOr(&c->error, 1u);
+}
+
+// Any-hit traversal of the shadow queue, then the NEE term is resolved into
+// the path's radiance (lighting.glsl:252-260, 286; ptRaygen.rgen:43-44).
+__global__ void __launch_bounds__(128) k_trace_shadow(SceneView sc, Queues q, Counters* c) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t count = *((volatile uint32_t*)&c->shadow);
+  int err = 0;
+  while (true) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(&c->work_shadow, 32u);
+    base = __shfl_sync(kFullMask, base, 0);
+    if (base >= count) break;
+    const uint32_t i = base + lane;
+    if (i < count) {
+      const float4 o = q.sorg[i], d = q.sdir[i];
+      RayPre r = ray_pre(f3(o.x, o.y, o.z), f3(d.x, d.y, d.z));
+      Hit h = traverse<true>(sc, r, o.w, d.w, &err);
+      const uint32_t p = q.spix[i];
+      const float4 nee4 = q.snee[i], add4 = q.sadd[i];
+      const float3 nee = h.tri >= 0 ? f3(0.f) : f3(nee4.x, nee4.y, nee4.z);
+      const float3 add = f3(add4.x, add4.y, add4.z);
+      float4 rd = q.rad[p];
+      float3 rad = f3(rd.x, rd.y, rd.z);
+      if (nee4.w == 0.f) {
+        rad = (f3(0.f) + nee) + add;  // finalColor = 0; += NEE; += emissive
+      } else {
+        rad = rad + (nee + add);  // finalColor += NEE + emissive * throughput
+      }
+      q.rad[p] = make_float4(rad.x, rad.y, rad.z, rd.w);
+    }
+  }
+  if (err) atomicOr(&c->error, 1u);
+}
+
+// sampleLight (lighting.glsl:19-227): returns the picked light's strength
+// (lightStrength), fills the direction, the pick pdf and the shadow ray's
+// tmax; traced = false when no shadow ray is cast.
+PBRT_D float3 sample_light(const SceneView& sc, int mode, float3 pos, float3 n, Rng& re, float3& l, float& pdf,
+                           float& shadow_tmax, bool& traced) {
+  const float tmin = 0.001f;
+  traced = false;
+  pdf = 0.f;
+  l = f3(0.f);
+  if (mode == 0) {
+    float strength_sum = 0.f, picked_strength = 0.f;
+    float3 picked_ls = f3(0.f);
+    float tmax = 1000.0f;
+    for (uint32_t i = 0; i < sc.light_count; ++i) {
+      const DevLight L = sc.lights[i];
+      const float3 ca = f3(L.col_ambient.x, L.col_ambient.y, L.col_ambient.z);
+      const float3 cd = f3(L.col_diffuse.x, L.col_diffuse.y, L.col_diffuse.z);
+      const float3 cs = f3(L.col_specular.x, L.col_specular.y, L.col_specular.z);
+      const float3 csum = ca + cd + cs;
+      const float csw = L.col_ambient.w + L.col_diffuse.w + L.col_specular.w;
+      const float power = ((csum.x + csum.y) + csum.z) + csw;  // dot(colA + colD + colS, vec4(1))
+      float strength = 0.f;
+      float3 ls = csum;
+      float cur_tmax = 1000.0f;
+      float3 cur_l = f3(0.f);
+      const int type = (int)L.v0_type.w;
+      const float3 v0 = f3(L.v0_type.x, L.v0_type.y, L.v0_type.z);
+      if (type == 1) {  // directional
+        float d = length(pos - v0);
+        float att = 1.0f / (L.strengths.x + L.strengths.y * d + L.strengths.z * d * d);
+        float3 ndir = -f3(L.dir_angle2.x, L.dir_angle2.y, L.dir_angle2.z);
+        strength = fmaxf(dot(n, ndir), 0.f) * power * att;
+        ls = ls * (dot(n, ndir) * att);
+        cur_l = normalize(ndir);
+      } else if (type == 2) {  // point
+        float d = length(pos - v0);
+        float att = 1.0f / (L.strengths.x + L.strengths.y * d + L.strengths.z * d * d);
+        float3 to = normalize(v0 - pos);
+        strength = fmaxf(dot(n, to), 0.f) * power * att;
+        ls = ls * (dot(n, to) * att);
+        cur_l = to;
+      } else if (type == 5) {  // area triangle
+        float ux = rng_next(re), uy = rng_next(re);
+        float sq = sqrtf(ux);
+        float bx = 1.0f - sq, by = uy * sq;  // sampleTriangle
+        const float3 p2 = f3(L.v1_strength.x, L.v1_strength.y, L.v1_strength.z);
+        const float3 p3 = f3(L.v2_angle.x, L.v2_angle.y, L.v2_angle.z);
+        float3 lp = v0 * (1.0f - bx - by) + p2 * bx + p3 * by;  // blerp
+        float3 ldir = lp - pos;
+        float3 ln = normalize(cross(p2 - v0, p3 - v0));
+        float d = length(ldir);
+        ldir = ldir / d;
+        float att = 1.0f / (L.strengths.x + L.strengths.y * d + L.strengths.z * d * d);
+        strength = fmaxf(dot(n, ldir), 0.f) * fmaxf(dot(-ldir, ln), 0.f) * power * att;
+        ls = ls * (fmaxf(dot(n, ldir), 0.f) * fmaxf(dot(-ldir, ln), 0.f) * att);
+        cur_l = ldir;
+        cur_tmax = d - tmin;
+      }
+      strength_sum += strength;
+      if (rng_next(re) < strength / strength_sum) {
+        picked_strength = strength;
+        picked_ls = ls;
+        tmax = cur_tmax;
+        l = cur_l;
+      }
+    }
+    if (strength_sum < 1e-6f || picked_strength < 1e-6f) {
+      pdf = 0.f;
+      l = f3(0.f);
+      return f3(0.f);
+    }
+    pdf = picked_strength / strength_sum;
+    shadow_tmax = tmax;
+    traced = true;
+    return picked_ls;
+  }
+  // LIGHT_STRENGTH (binary search over inclusive strengths) or UNIFORM
+  float rnd = rng_next(re);
+  int i;
+  float l_strength = 1.f;
+  if (mode == 1) {
+    float picked = rnd * sc.light_strength_sum;
+    int begin = 0, end = (int)sc.light_count, mid = (begin + end) / 2, cnt = 0;
+    while (end - begin > 1 && ++cnt < 100) {
+      if (picked <= sc.lights[mid].strengths.w) end = mid + 1;
+      else begin = mid;
+      mid = (begin + end) / 2;
+    }
+    l_strength = sc.lights[begin].strengths.w;
+    if (begin > 0) l_strength -= sc.lights[begin - 1].strengths.w;
+    i = begin;
+  } else {
+    i = (int)(rnd * (float)sc.light_count) - (int)rnd;
+  }
+  const DevLight L = sc.lights[i];
+  float3 ls = f3(L.col_ambient.x, L.col_ambient.y, L.col_ambient.z) + f3(L.col_diffuse.x, L.col_diffuse.y, L.col_diffuse.z) +
+              f3(L.col_specular.x, L.col_specular.y, L.col_specular.z);
+  float tmax = 1000.0f;
+  const int type = (int)L.v0_type.w;
+  const float3 v0 = f3(L.v0_type.x, L.v0_type.y, L.v0_type.z);
+  if (type == 1) {
+    float d = length(pos - v0);
+    float att = 1.0f / (L.strengths.x + L.strengths.y * d + L.strengths.z * d * d);
+    float3 ndir = -f3(L.dir_angle2.x, L.dir_angle2.y, L.dir_angle2.z);
+    ls = ls * (fmaxf(dot(n, ndir), 0.f) * att);
+    l = normalize(ndir);
+  } else if (type == 2) {
+    float d = length(pos - v0);
+    float att = 1.0f / (L.strengths.x + L.strengths.y * d + L.strengths.z * d * d);
+    float3 to = normalize(v0 - pos);
+    ls = ls * (fmaxf(dot(n, to), 0.f) * att);
+    l = to;
+  } else if (type == 5) {
+    float ux = rng_next(re), uy = rng_next(re);
+    float sq = sqrtf(ux);
+    float bx = 1.0f - sq, by = uy * sq;
+    const float3 p2 = f3(L.v1_strength.x, L.v1_strength.y, L.v1_strength.z);
+    const float3 p3 = f3(L.v2_angle.x, L.v2_angle.y, L.v2_angle.z);
+    float3 lp = v0 * (1.0f - bx - by) + p2 * bx + p3 * by;
+    float3 ldir = lp - pos;
+    float3 lnr = cross(p2 - v0, p3 - v0);
+    float area = .5f * length(lnr);
+    float3 ln = normalize(lnr);
+    float d = length(ldir);
+    ldir = ldir / d;
+    float att = 1.0f / (L.strengths.x + L.strengths.y * d + L.strengths.z * d * d);
+    ls = ls * (fmaxf(dot(n, ldir), 0.f) * fmaxf(dot(-ldir, ln), 0.f) * att * area);
+    l = ldir;
+    tmax = d - tmin;
+  }
+  if (length(ls) < 1e-6f) {
+    pdf = 0.f;
+    l = f3(0.f);
+    return f3(0.f);
+  }
+  pdf = 1.0f;
+  shadow_tmax = tmax;
+  traced = true;
+  if (mode == 1) return ls * sc.light_strength_sum / l_strength;
+  return ls * (float)sc.light_count;
+}
+
+// One bounce of shading for every entry of ray queue k&1.
+__global__ void __launch_bounds__(128) k_shade(SceneView sc, const FrameParams* __restrict__ fpp, Queues q,
+                                               Counters* c, GBufferOut g, int k) {
+  const FrameParams& fp = *fpp;
+  const uint32_t count = *((volatile uint32_t*)&c->ray[k & 1]);
+  const uint32_t* qpix = q.pix[k & 1];
+  const float4* qdir = q.dir[k & 1];
+  const int nq = (k + 1) & 1;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t n_round = (count + 31u) & ~31u;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_round; i += stride) {
+    bool push_ray = false, push_shadow = false;
+    float4 ray_o = make_float4(0, 0, 0, 0), ray_d = ray_o, sh_o = ray_o, sh_d = ray_o, sh_nee = ray_o, sh_add = ray_o;
+    uint32_t p = 0;
+    if (i < count) {
+      p = qpix[i];
+      const float4 d4 = qdir[i];
+      const float3 rdir = f3(d4.x, d4.y, d4.z);
+      const float4 h = q.hit[i];
+      const int tri = __float_as_int(h.w);
+      uint4 r4 = q.rng[p];
+      Rng re{r4.x, r4.y, r4.z, r4.w};
+      const float4 th4 = q.thr[p];
+      float3 thr = f3(th4.x, th4.y, th4.z);
+      float4 pv = q.prev[p], al = q.alb[p];
+      float3 prev = f3(pv.x, pv.y, pv.z);
+      int it = __float_as_int(pv.w), trans = __float_as_int(al.w);
+      SurfaceInfo si;
+      float3 position;
+      uint32_t category;
+      if (tri < 0) {
+        miss_payload(si, position, category);
+      } else {
+        const float4 t1 = sc.tris[3 * tri + 1], t2 = sc.tris[3 * tri + 2];
+        position = closest_hit(sc, rdir, __float_as_uint(t1.w), __float_as_uint(t2.w), h.y, h.z, si, category);
+      }
+      const bool miss = tri < 0;
+      // ---- next-event estimation at this vertex (lighting.glsl:246-261) ----
+      const float3 o = (k == 0) ? -normalize(rdir) : -rdir;
+      float3 nee = f3(0.f);
+      bool nee_pending = false;
+      float3 sl = f3(0.f);
+      float shadow_tmax = 0.f;
+      if (miss) {
+        nee = sky_color(-o) * thr;
+      } else {
+        float lpdf;
+        bool traced;
+        const float3 lcol = sample_light(sc, fp.light_mode, position, si.normal, re, sl, lpdf, shadow_tmax, traced);
+        if (traced && !(lcol.x == 0.f && lcol.y == 0.f && lcol.z == 0.f)) {
+          const float3 lh = normalize(sl + o);
+          const float3 brdf = brdf_eval(o, sl, lh, si);
+          const float bpdf = pdf_brdf(si, o, sl, lh);
+          const float w = power_heuristic(lpdf, bpdf);
+          const float3 light = f3(0.f) + lcol * brdf * w / lpdf;
+          nee = fmin3(thr * light, f3(kMaxRadiance));
+          nee_pending = true;
+        }
+      }
+      const float3 add = (k == 0) ? si.emissive : si.emissive * thr;
+      if (k == 0) {
+        // ---- G-buffer (ptRaygen.rgen:48-60) ----
+        const float3 alb = si.diffuse + si.specular;
+        al = make_float4(alb.x, alb.y, alb.z, al.w);
+        q.prim_key[p] = miss ? 0xffffffffu : __float_as_uint(sc.tris[3 * tri].w);
+        if (fp.write_gbuffer) {
+          g.depth[p] = length(position - prev);
+          g.normal[p] = make_float2(acosf(si.normal.z), atan2f(si.normal.y, si.normal.x));
+          const float cat = (float)category / 255.0f;
+          g.material[p] = make_uchar4(f2u8(cat), 0, 0, 0);
+          g.albedo[p] = make_uchar4(f2u8(alb.x), f2u8(alb.y), f2u8(alb.z), 255);
+        }
+      }
+      if (nee_pending) {
+        push_shadow = true;
+        sh_o = make_float4(position.x, position.y, position.z, 0.001f);
+        sh_d = make_float4(sl.x, sl.y, sl.z, shadow_tmax);
+        sh_nee = make_float4(nee.x, nee.y, nee.z, k == 0 ? 0.f : 1.f);
+        sh_add = make_float4(add.x, add.y, add.z, 0.f);
+      } else {
+        float4 rd = q.rad[p];
+        float3 rad = f3(rd.x, rd.y, rd.z);
+        rad = (k == 0) ? (f3(0.f) + nee) + add : rad + (nee + add);
+        q.rad[p] = make_float4(rad.x, rad.y, rad.z, rd.w);
+      }
+      // ---- next bounce (ptRaygen.rgen:66-75, lighting.glsl:263-283) ----
+      if (k > 0) it += 1;
+      if (!miss && (uint32_t)it < (uint32_t)fp.max_depth && trans < 10) {
+        if (si.illum == 7) {
+          it -= 1;
+          trans += 1;
+        }
+        const float3 v = normalize(prev - position);
+        prev = position;
+        float3 l;
+        float pdf;
+        const float3 brdf = sample_brdf(si, re, v, l, pdf);
+        if (!((brdf.x == 0.f && brdf.y == 0.f && brdf.z == 0.f) || pdf < kEpsilon)) {
+          float t = dot(l, si.normal);
+          if (si.illum == 7) t = 1.f;
+          float3 pt = thr * (brdf * t) / pdf;
+          bool alive = true;
+          if ((uint32_t)it > (uint32_t)fp.min_depth) {
+            if (rng_next(re) < kMinTermination) alive = false;
+            pt = pt / (1.0f - kMinTermination);
+          }
+          if (alive) {
+            thr = pt;
+            push_ray = true;
+            ray_o = make_float4(position.x, position.y, position.z, 0.001f);
+            ray_d = make_float4(l.x, l.y, l.z, 10000.0f);
+          }
+        }
+      }
+      q.rng[p] = make_uint4(re.x, re.y, re.z, re.w);
+      q.thr[p] = make_float4(thr.x, thr.y, thr.z, 0.f);
+      q.prev[p] = make_float4(prev.x, prev.y, prev.z, __int_as_float(it));
+      q.alb[p] = make_float4(al.x, al.y, al.z, __int_as_float(trans));
+    }
+    const int rs = warp_alloc(&c->ray[nq], push_ray);
+    if (rs >= 0) {
+      q.pix[nq][rs] = p;
+      q.org[nq][rs] = ray_o;
+      q.dir[nq][rs] = ray_d;
+    }
+    const int ss = warp_alloc(&c->shadow, push_shadow);
+    if (ss >= 0) {
+      q.spix[ss] = p;
+      q.sorg[ss] = sh_o;
+      q.sdir[ss] = sh_d;
+      q.snee[ss] = sh_nee;
+      q.sadd[ss] = sh_add;
+    }
+  }
+}
+
+// ptRaygen.rgen:81-103: clamp, then demodulate (DEMOD_ILLUMINATION_FLOAT) or
+// blend progressively in sRGB (FINAL_IMAGE).
+__global__ void k_finalize(const FrameParams* __restrict__ fpp, Queues q, float4* __restrict__ out) {
+  const FrameParams& fp = *fpp;
+  const int N = fp.W * fp.H;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) {
+    const float4 r = q.rad[p];
+    float3 fc = clamp3(f3(r.x, r.y, r.z), 0.f, kMaxRadiance);
+    if (!fp.final_image) {
+      const float4 a = q.alb[p];
+      float3 dm = fmin3(fc / (f3(a.x, a.y, a.z) + f3(kEpsilon)), f3(1e3f));
+      out[p] = make_float4(dm.x, dm.y, dm.z, 1.f);
+    } else {
+      if (fp.sample > 0) {
+        const float4 pr = out[p];
+        const float alpha = 1.0f / (float)(fp.sample + 1);
+        fc = mix3(srgb_to_linear(f3(pr.x, pr.y, pr.z)), fc, alpha);
+      }
+      fc = clamp3(linear_to_srgb(fc), 0.f, 1.f);
+      out[p] = make_float4(fc.x, fc.y, fc.z, 1.f);
+    }
+  }
+}
+
+// Standalone ray queries (no reference counterpart; used for traversal tests
+// and throughput measurement): hits[i] = (t, u, v, triangle key bits or -1).
+__global__ void __launch_bounds__(128) k_ray_query(SceneView sc, const float4* __restrict__ org,
+                                                   const float4* __restrict__ dir, float4* __restrict__ hits, uint32_t n,
+                                                   int any_hit, uint32_t* work, uint32_t* errflag) {
+  const int lane = threadIdx.x & 31;
+  int err = 0;
+  while (true) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(work, 32u);
+    base = __shfl_sync(kFullMask, base, 0);
+    if (base >= n) break;
+    const uint32_t i = base + lane;
+    if (i < n) {
+      const float4 o = org[i], d = dir[i];
+      RayPre r = ray_pre(f3(o.x, o.y, o.z), f3(d.x, d.y, d.z));
+      Hit h = any_hit ? traverse<true>(sc, r, o.w, d.w, &err) : traverse<false>(sc, r, o.w, d.w, &err);
+      const uint32_t key = h.tri >= 0 ? __float_as_uint(sc.tris[3 * h.tri].w) : 0xffffffffu;
+      hits[i] = make_float4(h.t, h.u, h.v, __uint_as_float(key));
+    }
+  }
+  if (err) atomicOr(errflag, 1u);
+}
+
+}  // namespace pbrt
+
+// ===========================================================================
+// Host objects.
+using namespace pbrt;
+
+namespace {
+
+template <class T> int dalloc(T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+  return PBRT_OK;
+}
+template <class T> int upload(T** p, const T* src, size_t count) {
+  int st = dalloc(p, count);
+  if (st) return st;
+  if (count) PBRT_CUDA(cudaMemcpy(*p, src, count * sizeof(T), cudaMemcpyHostToDevice));
+  return PBRT_OK;
+}
+
+float bits_f(uint32_t u) {
+  float f;
+  std::memcpy(&f, &u, 4);
+  return f;
+}
+
+// double-precision 4x4 inverse (column-major in/out), false if singular
+bool inverse4(const double* m, double* out) {
+  double a[4][8];
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 4; ++c) {
+      a[r][c] = m[c * 4 + r];
+      a[r][4 + c] = (r == c) ? 1.0 : 0.0;
+    }
+  for (int c = 0; c < 4; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < 4; ++r)
+      if (std::fabs(a[r][c]) > std::fabs(a[piv][c])) piv = r;
+    if (a[piv][c] == 0.0) return false;
+    for (int k = 0; k < 8; ++k) std::swap(a[c][k], a[piv][k]);
+    double d = a[c][c];
+    for (int k = 0; k < 8; ++k) a[c][k] /= d;
+    for (int r = 0; r < 4; ++r) {
+      if (r == c) continue;
+      double f = a[r][c];
+      for (int k = 0; k < 8; ++k) a[r][k] -= f * a[c][k];
+    }
+  }
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 4; ++c) out[c * 4 + r] = a[r][4 + c];
+  return true;
+}
+
+}  // namespace
+
+struct PbrtScene : pbrt::Object {
+  PbrtScene() : Object(pbrt::Kind::Scene) {}
+  ~PbrtScene() override {
+    for (void* p : allocs) cudaFree(p);
+  }
+  std::vector<void*> allocs;
+  SceneView view{};
+  Bvh8Stats stats;
+  uint32_t instance_count = 0, tri_count = 0;
+  bool transmissive = false;  // some material has illum 7 (refraction)
+  template <class T> int up(T** p, const T* src, size_t n) {
+    int st = upload(p, src, n);
+    if (!st) allocs.push_back((void*)*p);
+    return st;
+  }
+};
+
+struct PbrtPipeline : pbrt::Object {
+  PbrtPipeline() : Object(pbrt::Kind::Pipeline) {}
+  ~PbrtPipeline() override {
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    for (void* p : allocs) cudaFree(p);
+    if (host_fp) cudaFreeHost(host_fp);
+    release(scene);
+    release(gbuffer);
+    release(illumination);
+  }
+  PbrtScene* scene = nullptr;
+  PbrtGBuffer* gbuffer = nullptr;
+  PbrtIlluminationBuffer* illumination = nullptr;
+  bool write_gbuffer = false;
+  int W = 0, H = 0;
+  int light_mode = 0, min_depth = 0, max_depth = 2;
+  std::vector<void*> allocs;
+  Queues q{};
+  Counters* ctr = nullptr;
+  FrameParams* dev_fp = nullptr;
+  FrameParams* host_fp = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  int graph_depth = -1;
+  int grid_persistent = 0;
+  template <class T> int a(T** p, size_t n) {
+    int st = dalloc(p, n);
+    if (!st) allocs.push_back((void*)*p);
+    return st;
+  }
+};
+
+static int record_frame(PbrtPipeline* pp, cudaStream_t s) {
+  const int N = pp->W * pp->H;
+  const SceneView sc = pp->scene->view;
+  GBufferOut g{};
+  if (pp->gbuffer) {
+    g.depth = pp->gbuffer->depth.ptr<float>();
+    g.normal = pp->gbuffer->normal.ptr<float2>();
+    g.material = pp->gbuffer->material.ptr<uchar4>();
+    g.albedo = pp->gbuffer->albedo.ptr<uchar4>();
+  }
+  float4* out = pp->illumination->images[0].ptr<float4>();
+  const int blocks_px = std::min((N + 255) / 256, 152 * 8);
+  k_frame_begin<<<1, 1, 0, s>>>(pp->ctr, pp->dev_fp);
+  k_raygen<<<blocks_px, 256, 0, s>>>(pp->dev_fp, pp->q);
+  const int depth = pp->max_depth;
+  // Bounce k traces the rays that leave vertex k-1. Transmissive vertices do
+  // not count towards the depth (ptRaygen.rgen:69, up to 10 of them).
+  const int bounces = depth + 1 + (pp->scene->transmissive ? 10 : 0);
+  for (int k = 0; k < bounces; ++k) {
+    k_bounce_begin<<<1, 1, 0, s>>>(pp->ctr, k);
+    k_trace_closest<<<pp->grid_persistent, 128, 0, s>>>(sc, pp->q, pp->ctr, k);
+    k_shade<<<pp->grid_persistent, 128, 0, s>>>(sc, pp->dev_fp, pp->q, pp->ctr, g, k);
+    k_trace_shadow<<<pp->grid_persistent, 128, 0, s>>>(sc, pp->q, pp->ctr);
+    k_bounce_end<<<1, 1, 0, s>>>(pp->ctr);
+  }
+  k_finalize<<<blocks_px, 256, 0, s>>>(pp->dev_fp, pp->q, out);
+  return check_launch("path tracer frame");
+}
+
+extern "C" {
+
+PBRT_API int pbrt_scene_create(const PbrtSceneDesc* d, PbrtScene** out) {
+  if (!out || !d) return fail(PBRT_ERROR_INVALID_ARGUMENT, "scene: null argument");
+  *out = nullptr;
+  if (d->mesh_count == 0 || d->instance_count == 0 || !d->meshes || !d->instances || !d->materials)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "scene: needs meshes, instances and materials");
+  if (d->light_count > 0 && !d->lights) return fail(PBRT_ERROR_INVALID_ARGUMENT, "scene: lights missing");
+  if (d->texture_count == 0 || !d->textures || !d->mesh_textures)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "scene: needs a texture table (entry 0 = 1x1 white default)");
+  auto* sc = new (std::nothrow) PbrtScene();
+  if (!sc) return fail(PBRT_ERROR_OUT_OF_MEMORY, "scene: host allocation");
+  // --- mesh pools
+  std::vector<DevMesh> meshes(d->mesh_count);
+  std::vector<float> pos, nor, uv;
+  std::vector<uint32_t> idx;
+  for (uint32_t m = 0; m < d->mesh_count; ++m) {
+    const PbrtMeshDesc& md = d->meshes[m];
+    if (!md.positions || !md.normals || !md.uvs || !md.indices || md.index_count % 3 != 0 ||
+        (md.index_stride != 2 && md.index_stride != 4)) {
+      delete sc;
+      return fail(PBRT_ERROR_INVALID_ARGUMENT, "scene: mesh %u malformed (indices multiple of 3, stride 2 or 4)", m);
+    }
+    DevMesh& dm = meshes[m];
+    dm.vbase = (uint32_t)(pos.size() / 3);
+    dm.ibase = (uint32_t)idx.size();
+    dm.index_stride = md.index_stride;
+    for (int s = 0; s < 5; ++s) {
+      int t = d->mesh_textures[5 * m + s];
+      if (t < 0 || (uint32_t)t >= d->texture_count) {
+        delete sc;
+        return fail(PBRT_ERROR_INVALID_ARGUMENT, "scene: mesh %u texture slot %d -> %d out of range", m, s, t);
+      }
+      dm.tex[s] = t;
+    }
+    pos.insert(pos.end(), md.positions, md.positions + 3 * (size_t)md.vertex_count);
+    nor.insert(nor.end(), md.normals, md.normals + 3 * (size_t)md.vertex_count);
+    uv.insert(uv.end(), md.uvs, md.uvs + 2 * (size_t)md.vertex_count);
+    if (md.index_stride == 4) {
+      const uint32_t* ii = (const uint32_t*)md.indices;
+      for (uint32_t k = 0; k < md.index_count; ++k) {
+        if (ii[k] >= md.vertex_count) {
+          delete sc;
+          return fail(PBRT_ERROR_INVALID_ARGUMENT, "scene: mesh %u index %u out of range", m, ii[k]);
+        }
+      }
+      idx.insert(idx.end(), ii, ii + md.index_count);
+    } else {
+      const uint16_t* ii = (const uint16_t*)md.indices;
+      for (uint32_t k = 0; k < md.index_count; ++k)
+        if (ii[k] >= md.vertex_count) {
+          delete sc;
+          return fail(PBRT_ERROR_INVALID_ARGUMENT, "scene: mesh %u index %u out of range", m, ii[k]);
+        }
+      for (uint32_t k = 0; k < md.index_count; k += 2) {
+        uint32_t lo = ii[k], hi = (k + 1 < md.index_count) ? ii[k + 1] : 0u;
+        idx.push_back(lo | (hi << 16));
+      }
+      idx.push_back(0u);  // unpackIndex may read one word past an odd-length buffer
+    }
+  }
+  // --- instances: flatten to world-space triangles (instance-major order)
+  std::vector<DevInstance> inst(d->instance_count);
+  size_t total = 0;
+  for (uint32_t i = 0; i < d->instance_count; ++i) {
+    const PbrtObjectInstance& oi = d->instances[i];
+    if (oi.mesh_id < 0 || (uint32_t)oi.mesh_id >= d->mesh_count) {
+      delete sc;
+      return fail(PBRT_ERROR_INVALID_ARGUMENT, "scene: instance %u mesh %d out of range", i, oi.mesh_id);
+    }
+    total += d->meshes[oi.mesh_id].index_count / 3;
+  }
+  if (total == 0 || total > 0x7fffffffu) {
+    delete sc;
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "scene: %zu triangles", total);
+  }
+  std::vector<float> world(9 * total);
+  std::vector<uint32_t> tri_inst(total), tri_prim(total);
+  size_t t = 0;
+  bool any_alpha = false;
+  for (uint32_t i = 0; i < d->instance_count; ++i) {
+    const PbrtObjectInstance& oi = d->instances[i];
+    DevInstance& di = inst[i];
+    const float* M = oi.object_mat;
+    for (int c = 0; c < 4; ++c) di.obj.c[c] = make_float4(M[4 * c], M[4 * c + 1], M[4 * c + 2], M[4 * c + 3]);
+    double md[16], inv[16];
+    for (int k = 0; k < 16; ++k) md[k] = M[k];
+    if (!inverse4(md, inv)) {
+      delete sc;
+      return fail(PBRT_ERROR_INVALID_ARGUMENT, "scene: instance %u object matrix is singular", i);
+    }
+    // transpose(inverse(M)) columns: column c = row c of inverse(M)
+    for (int c = 0; c < 3; ++c)
+      di.nrm[c] = make_float4((float)inv[0 * 4 + c], (float)inv[1 * 4 + c], (float)inv[2 * 4 + c], 0.f);
+    di.mesh = oi.mesh_id;
+    di.index_stride = oi.index_stride;
+    di.opaque = d->instance_opaque ? (d->instance_opaque[i] ? 1u : 0u) : 1u;
+    di.pad = 0;
+    if (!di.opaque) any_alpha = true;
+    const PbrtMeshDesc& md_ = d->meshes[oi.mesh_id];
+    const uint32_t ntri = md_.index_count / 3;
+    for (uint32_t p = 0; p < ntri; ++p, ++t) {
+      for (int k = 0; k < 3; ++k) {
+        uint32_t vi = md_.index_stride == 4 ? ((const uint32_t*)md_.indices)[3 * p + k]
+                                            : ((const uint16_t*)md_.indices)[3 * p + k];
+        const float* v = md_.positions + 3 * (size_t)vi;
+        // (objectMat * vec4(v, 1)).xyz in FP32, GLSL column order
+        for (int a = 0; a < 3; ++a) {
+          float s = M[0 * 4 + a] * v[0];
+          s = s + M[1 * 4 + a] * v[1];
+          s = s + M[2 * 4 + a] * v[2];
+          s = s + M[3 * 4 + a] * 1.0f;
+          world[9 * t + 3 * k + a] = s;
+        }
+      }
+      tri_inst[t] = i;
+      tri_prim[t] = p;
+    }
+  }
+  std::vector<Node8> nodes;
+  std::vector<uint32_t> order;
+  build_bvh8(world.data(), total, nodes, order, &sc->stats);
+  if (sc->stats.depth >= kStackSize - 2) {
+    delete sc;
+    return fail(PBRT_ERROR_UNSUPPORTED, "scene: BVH depth %d exceeds the traversal stack", sc->stats.depth);
+  }
+  std::vector<float4> tris(3 * total);
+  for (size_t s = 0; s < total; ++s) {
+    const uint32_t o = order[s];
+    const float* w = &world[9 * (size_t)o];
+    tris[3 * s + 0] = make_float4(w[0], w[1], w[2], bits_f(o));
+    tris[3 * s + 1] = make_float4(w[3], w[4], w[5], bits_f(tri_inst[o]));
+    tris[3 * s + 2] = make_float4(w[6], w[7], w[8], bits_f(tri_prim[o]));
+  }
+  // --- textures
+  std::vector<DevTexture> texd(d->texture_count);
+  size_t texels = 0;
+  for (uint32_t i = 0; i < d->texture_count; ++i) {
+    const PbrtTextureDesc& td = d->textures[i];
+    if (!td.rgba8 || td.width == 0 || td.height == 0) {
+      delete sc;
+      return fail(PBRT_ERROR_INVALID_ARGUMENT, "scene: texture %u empty", i);
+    }
+    texd[i].offset = texels;
+    texd[i].w = td.width;
+    texd[i].h = td.height;
+    texels += (size_t)td.width * td.height;
+  }
+  int st = PBRT_OK;
+  uchar4* texpool = nullptr;
+  st = dalloc(&texpool, texels);
+  if (!st) sc->allocs.push_back(texpool);
+  for (uint32_t i = 0; !st && i < d->texture_count; ++i) {
+    cudaError_t e = cudaMemcpy(texpool + texd[i].offset, d->textures[i].rgba8,
+                               (size_t)d->textures[i].width * d->textures[i].height * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) st = cuda_fail(e, "texture upload");
+  }
+  std::vector<DevMaterial> mats(d->mesh_count);
+  std::memcpy(mats.data(), d->materials, sizeof(DevMaterial) * d->mesh_count);
+  for (const DevMaterial& m : mats)
+    if ((int)m.transmittance_illum.w == 7) sc->transmissive = true;
+  std::vector<DevLight> lights(std::max<uint32_t>(1, d->light_count));
+  if (d->light_count) std::memcpy(lights.data(), d->lights, sizeof(DevLight) * d->light_count);
+  SceneView& v = sc->view;
+  float4* dtris = nullptr;
+  Node8* dnodes = nullptr;
+  DevInstance* dinst = nullptr;
+  DevMesh* dmesh = nullptr;
+  DevMaterial* dmat = nullptr;
+  DevLight* dlight = nullptr;
+  float *dpos = nullptr, *dnor = nullptr, *duv = nullptr;
+  uint32_t* didx = nullptr;
+  DevTexture* dtex = nullptr;
+  if (!st) st = sc->up(&dtris, tris.data(), tris.size());
+  if (!st) st = sc->up(&dnodes, nodes.data(), nodes.size());
+  if (!st) st = sc->up(&dinst, inst.data(), inst.size());
+  if (!st) st = sc->up(&dmesh, meshes.data(), meshes.size());
+  if (!st) st = sc->up(&dmat, mats.data(), mats.size());
+  if (!st) st = sc->up(&dlight, lights.data(), lights.size());
+  if (!st) st = sc->up(&dpos, pos.data(), pos.size());
+  if (!st) st = sc->up(&dnor, nor.data(), nor.size());
+  if (!st) st = sc->up(&duv, uv.data(), uv.size());
+  if (!st) st = sc->up(&didx, idx.data(), idx.size());
+  if (!st) st = sc->up(&dtex, texd.data(), texd.size());
+  if (st) {
+    delete sc;
+    return st;
+  }
+  v.tris = dtris;
+  v.nodes = dnodes;
+  v.instances = dinst;
+  v.meshes = dmesh;
+  v.materials = dmat;
+  v.lights = dlight;
+  v.pos = dpos;
+  v.nor = dnor;
+  v.uv = duv;
+  v.idx = didx;
+  v.textures = dtex;
+  v.texels = texpool;
+  v.light_count = d->light_count;
+  v.light_strength_sum = d->light_count ? d->lights[d->light_count - 1].inclusive_strength : 0.f;
+  v.tri_count = (uint32_t)total;
+  v.any_alpha = any_alpha ? 1 : 0;
+  sc->instance_count = d->instance_count;
+  sc->tri_count = (uint32_t)total;
+  *out = sc;
+  return PBRT_OK;
+}
+
+PBRT_API int pbrt_scene_info(const PbrtScene* s, PbrtSceneInfo* info) {
+  if (!checked<const PbrtScene>((void*)s, Kind::Scene) || !info) return fail(PBRT_ERROR_INVALID_ARGUMENT, "not a scene");
+  info->triangle_count = s->tri_count;
+  info->instance_count = s->instance_count;
+  info->bvh_nodes = (uint32_t)s->stats.nodes;
+  info->bvh_depth = (uint32_t)s->stats.depth;
+  info->bvh_bytes = (uint64_t)s->stats.nodes * sizeof(Node8);
+  info->triangle_bytes = (uint64_t)s->tri_count * 48u;
+  info->build_ms = s->stats.build_ms;
+  info->light_count = s->view.light_count;
+  return PBRT_OK;
+}
+
+PBRT_API int pbrt_scene_trace_rays(PbrtScene* s, const void* origins_tmin, const void* directions_tmax, uint32_t n,
+                                   int32_t any_hit, void* hits_out, void* scratch_u32x2, pbrt_stream_t stream) {
+  if (!checked<PbrtScene>(s, Kind::Scene) || (n && (!origins_tmin || !directions_tmax || !hits_out || !scratch_u32x2)))
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "trace_rays: bad arguments");
+  if (n == 0) return PBRT_OK;
+  uint32_t* work = (uint32_t*)scratch_u32x2;
+  PBRT_CUDA(cudaMemsetAsync(work, 0, 2 * sizeof(uint32_t), stream));
+  int dev = 0, sms = 0;
+  PBRT_CUDA(cudaGetDevice(&dev));
+  PBRT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  k_ray_query<<<sms * 16, 128, 0, stream>>>(s->view, (const float4*)origins_tmin, (const float4*)directions_tmax,
+                                            (float4*)hits_out, n, any_hit, work, work + 1);
+  return check_launch("k_ray_query");
+}
+
+PBRT_API int pbrt_pipeline_create(PbrtScene* scene, PbrtGBuffer* g, PbrtIlluminationBuffer* illumination,
+                                  int32_t write_g_buffer, PbrtPipeline** out) {
+  if (!out) return fail(PBRT_ERROR_INVALID_ARGUMENT, "pipeline: null output");
+  *out = nullptr;
+  if (!checked<PbrtScene>(scene, Kind::Scene) || !checked<PbrtIlluminationBuffer>(illumination, Kind::Illumination))
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "pipeline: bad scene or illumination handle");
+  if (g && !checked<PbrtGBuffer>(g, Kind::GBuffer)) return fail(PBRT_ERROR_INVALID_ARGUMENT, "pipeline: bad GBuffer");
+  if (write_g_buffer && !g) return fail(PBRT_ERROR_INVALID_ARGUMENT, "pipeline: write_g_buffer needs a GBuffer");
+  if (illumination->type != PBRT_ILLUMINATION_DEMODULATED_FLOAT && illumination->type != PBRT_ILLUMINATION_FINAL_FLOAT)
+    return fail(PBRT_ERROR_UNSUPPORTED,
+                "pipeline: illumination must be DemodulatedFloat (DEMOD_ILLUMINATION_FLOAT) or FinalFloat (FINAL_IMAGE)");
+  if (g && (g->width != illumination->width || g->height != illumination->height))
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "pipeline: GBuffer and illumination sizes differ");
+  auto* pp = new (std::nothrow) PbrtPipeline();
+  if (!pp) return fail(PBRT_ERROR_OUT_OF_MEMORY, "pipeline: host allocation");
+  pp->scene = scene;
+  retain(scene);
+  pp->illumination = illumination;
+  retain(illumination);
+  if (g) {
+    pp->gbuffer = g;
+    retain(g);
+  }
+  pp->write_gbuffer = write_g_buffer != 0;
+  pp->W = (int)illumination->width;
+  pp->H = (int)illumination->height;
+  // PBRTPipeline.cpp:92-96: uniform light sampling above 800 lights
+  pp->light_mode = scene->view.light_count > 800 ? 2 : 0;
+  const size_t N = (size_t)pp->W * pp->H;
+  int st = PBRT_OK;
+  Queues& q = pp->q;
+  for (int i = 0; i < 2 && !st; ++i) {
+    st = pp->a(&q.pix[i], N);
+    if (!st) st = pp->a(&q.org[i], N);
+    if (!st) st = pp->a(&q.dir[i], N);
+  }
+  if (!st) st = pp->a(&q.hit, N);
+  if (!st) st = pp->a(&q.spix, N);
+  if (!st) st = pp->a(&q.sorg, N);
+  if (!st) st = pp->a(&q.sdir, N);
+  if (!st) st = pp->a(&q.snee, N);
+  if (!st) st = pp->a(&q.sadd, N);
+  if (!st) st = pp->a(&q.rng, N);
+  if (!st) st = pp->a(&q.thr, N);
+  if (!st) st = pp->a(&q.rad, N);
+  if (!st) st = pp->a(&q.prev, N);
+  if (!st) st = pp->a(&q.alb, N);
+  if (!st) st = pp->a(&q.prim_key, N);
+  if (!st) st = pp->a(&pp->ctr, 1);
+  if (!st) st = pp->a(&pp->dev_fp, 1);
+  if (!st) {
+    cudaError_t e = cudaMemset(pp->ctr, 0, sizeof(Counters));
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&pp->host_fp, sizeof(FrameParams));
+    if (e != cudaSuccess) st = cuda_fail(e, "pipeline state");
+  }
+  if (!st) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    pp->grid_persistent = sms * 12;
+  }
+  if (st) {
+    delete pp;
+    return st;
+  }
+  *out = pp;
+  return PBRT_OK;
+}
+
+PBRT_API int pbrt_pipeline_set_config(PbrtPipeline* pp, int32_t light_sampling, int32_t min_recursion_depth,
+                                      int32_t max_recursion_depth) {
+  if (!checked<PbrtPipeline>(pp, Kind::Pipeline)) return fail(PBRT_ERROR_INVALID_ARGUMENT, "not a pipeline");
+  if (light_sampling < 0 || light_sampling > 2 || min_recursion_depth < 0 || max_recursion_depth < 0 ||
+      max_recursion_depth > 64)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "pipeline config: light_sampling %d, depth [%d, %d]", light_sampling,
+                min_recursion_depth, max_recursion_depth);
+  pp->light_mode = light_sampling;
+  pp->min_depth = min_recursion_depth;
+  pp->max_depth = max_recursion_depth;
+  return PBRT_OK;
+}
+
+PBRT_API int pbrt_pipeline_trace(PbrtPipeline* pp, const PbrtPushConstants* pc, pbrt_stream_t stream) {
+  if (!checked<PbrtPipeline>(pp, Kind::Pipeline) || !pc) return fail(PBRT_ERROR_INVALID_ARGUMENT, "trace: bad arguments");
+  FrameParams& fp = *pp->host_fp;
+  // The previous frame's copy out of host_fp must be done before rewriting it.
+  PBRT_CUDA(cudaStreamSynchronize(stream));
+  for (int c = 0; c < 4; ++c) {
+    fp.inv_view.c[c] = make_float4(pc->view_inverse[4 * c], pc->view_inverse[4 * c + 1], pc->view_inverse[4 * c + 2],
+                                   pc->view_inverse[4 * c + 3]);
+    fp.inv_proj.c[c] = make_float4(pc->proj_inverse[4 * c], pc->proj_inverse[4 * c + 1], pc->proj_inverse[4 * c + 2],
+                                   pc->proj_inverse[4 * c + 3]);
+  }
+  fp.frame = pc->frame_number;
+  fp.sample = pc->sample_number;
+  fp.W = pp->W;
+  fp.H = pp->H;
+  fp.min_depth = pp->min_depth;
+  fp.max_depth = pp->max_depth;
+  fp.light_mode = pp->light_mode;
+  fp.final_image = pp->illumination->type == PBRT_ILLUMINATION_FINAL_FLOAT ? 1 : 0;
+  fp.write_gbuffer = pp->write_gbuffer ? 1 : 0;
+  PBRT_CUDA(cudaMemcpyAsync(pp->dev_fp, pp->host_fp, sizeof(FrameParams), cudaMemcpyHostToDevice, stream));
+  if (!pp->graph_exec || pp->graph_depth != pp->max_depth) {
+    if (pp->graph_exec) cudaGraphExecDestroy(pp->graph_exec);
+    pp->graph_exec = nullptr;
+    cudaStream_t cap;
+    PBRT_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    cudaGraph_t graph;
+    cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    int st = e == cudaSuccess ? record_frame(pp, cap) : cuda_fail(e, "begin capture");
+    cudaError_t e2 = cudaStreamEndCapture(cap, &graph);
+    cudaStreamDestroy(cap);
+    if (st) return st;
+    if (e2 != cudaSuccess) return cuda_fail(e2, "end capture");
+    e = cudaGraphInstantiate(&pp->graph_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(e, "graph instantiate");
+    pp->graph_depth = pp->max_depth;
+  }
+  PBRT_CUDA(cudaGraphLaunch(pp->graph_exec, stream));
+  return PBRT_OK;
+}
+
+PBRT_API int pbrt_pipeline_stats(PbrtPipeline* pp, pbrt_stream_t stream, PbrtTraceStats* out) {
+  if (!checked<PbrtPipeline>(pp, Kind::Pipeline) || !out) return fail(PBRT_ERROR_INVALID_ARGUMENT, "stats: bad arguments");
+  Counters c;
+  PBRT_CUDA(cudaMemcpyAsync(&c, pp->ctr, sizeof(Counters), cudaMemcpyDeviceToHost, stream));
+  PBRT_CUDA(cudaStreamSynchronize(stream));
+  out->frames = c.frames;
+  out->primary_rays = c.rays_primary;
+  out->extension_rays = c.rays_extension;
+  out->shadow_rays = c.rays_shadow;
+  out->error_flags = c.error;
+  return PBRT_OK;
+}
+
+PBRT_API int pbrt_pipeline_reset_stats(PbrtPipeline* pp, pbrt_stream_t stream) {
+  if (!checked<PbrtPipeline>(pp, Kind::Pipeline)) return fail(PBRT_ERROR_INVALID_ARGUMENT, "not a pipeline");
+  PBRT_CUDA(cudaMemsetAsync(pp->ctr, 0, sizeof(Counters), stream));
+  return PBRT_OK;
+}
+
+PBRT_API int pbrt_pipeline_debug_images(const PbrtPipeline* pp, PbrtImage* primary_hit_key) {
+  if (!checked<const PbrtPipeline>((void*)pp, Kind::Pipeline)) return fail(PBRT_ERROR_INVALID_ARGUMENT, "not a pipeline");
+  if (primary_hit_key) {
+    PbrtImage& im = *primary_hit_key;
+    im.data = pp->q.prim_key;
+    im.width = (uint32_t)pp->W;
+    im.height = (uint32_t)pp->H;
+    im.layers = 1;
+    im.format = PBRT_FORMAT_R32_UINT;
+    im.texel_bytes = 4;
+    im.row_bytes = (size_t)pp->W * 4;
+    im.layer_bytes = im.row_bytes * pp->H;
+  }
+  return PBRT_OK;
+}
+
+}  // extern "C"
