@@ -1,0 +1,413 @@
+#!/usr/bin/env python
+"""Benchmark of the per-frame path: 1080p denoised frames/s and Grays/s.
+
+A step is one frame of the reference's per-frame command list
+(source/VulkanPBRT.cpp:397-505): path-trace 1 spp (PBRTPipeline), temporal
+accumulation (Accumulator), BMFR denoise, copy-to-back -- on the full-size
+workload: 1920x1080, max depth 8 with Russian roulette after bounce 3, a
+seeded ~1M-triangle scene of 2000 instanced displaced icospheres and boxes
+(log-uniform scale .05-2) on a ground plane, per-mesh 1024^2 RGBA8
+value-noise textures, 5% alpha-masked meshes, 8 point lights + 1 area light,
+camera on a 16-frame orbit. Synthetic, seeded data stands in for the scenes
+the reference loads (no dataset is available).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the reference algorithm's CPU implementation (the
+project's C++ restatement; the reference's own shaders cannot run without a
+Vulkan stack) on this host's cores, on a bounded sample of the same frame.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "1080p denoised fps and Grays/s: neural vs BMFR at equal relMSE to 4096 spp"
+NODE_BYTES, TRI_BYTES = 80, 48  # Node8 and the 3-float4 triangle record
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=32)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--max-depth", type=int, default=8)
+    ap.add_argument("--min-depth", type=int, default=3)
+    ap.add_argument("--instances", type=int, default=2000)
+    ap.add_argument("--texture-size", type=int, default=1024)
+    ap.add_argument("--denoiser", default="bmfr", choices=["bmfr", "bfr"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def workload(args, seed_offset=0):
+    from vulkanpbrt_gb300 import scene as S
+
+    return S.instanced_field(seed=seed_offset, instances=args.instances, texture_size=args.texture_size)
+
+
+def orbit(sc, W, H, f, frames=16):
+    from vulkanpbrt_gb300.camera import Camera
+
+    eye0 = np.array(sc.camera_eye, np.float64)
+    c = np.array(sc.camera_center, np.float64)
+    r = math.hypot(eye0[0] - c[0], eye0[1] - c[1])
+    a0 = math.atan2(eye0[1] - c[1], eye0[0] - c[0])
+    a = a0 + 2 * math.pi * (f % frames) / frames / 16.0  # a slow orbit: 1/16 turn over 16 frames
+    eye = (c[0] + r * math.cos(a), c[1] + r * math.sin(a), eye0[2])
+    return Camera(eye, sc.camera_center, aspect=W / H)
+
+
+class ClockSampler:
+    """nvidia-smi SM clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 4 + i and r[4 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(kernel: str):
+    """dram bytes per launch of `kernel` from a committed ncu summary, if any."""
+    p = ROOT / "profiles" / "ncu_traffic.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get(kernel)
+    return None
+
+
+# ---------------------------------------------------------------------------
+def cpu_baseline(args, sc, sample_div=8, os_=None):
+    """The CPU restatement (FP32, all host threads) on a bounded sample: the
+    same scene and camera at 1/sample_div^2 of the pixels, trace + BMFR,
+    extrapolated to a full frame."""
+    from oracle import oracle as O
+    from vulkanpbrt_gb300.camera import col_major
+
+    W, H = args.width // sample_div, args.height // sample_div
+    cam = orbit(sc, W, H, 0)
+    os_ = os_ if os_ is not None else O.OracleScene(sc)
+    O.render(os_, 8, 8, col_major(cam.inv_view), col_major(cam.inv_proj), min_depth=args.min_depth,
+             max_depth=args.max_depth)  # builds and caches the oracle's BVH (not timed, like the GPU build)
+    t0 = time.perf_counter()
+    r = O.render(os_, W, H, col_major(cam.inv_view), col_major(cam.inv_proj), frame=1, min_depth=args.min_depth,
+                 max_depth=args.max_depth)
+    t1 = time.perf_counter()
+    den = np.zeros((2, H, W, 4), np.float16)
+    motion = np.full((H, W, 2), -1, np.float16)
+    spp = np.ones((H, W), np.uint8)
+    if W >= 66 and H >= 66:
+        O.bmfr(32, 256, 1, 0, col_major(cam.inv_view), col_major(cam.inv_proj), r["depth"], r["normal"], r["albedo"],
+               r["illum"].astype(np.float16), motion, spp, den)
+    t2 = time.perf_counter()
+    scale = (args.width * args.height) / (W * H)
+    frame_s = (t2 - t0) * scale
+    rays = float(r["rays"].sum())
+    return {
+        "value": 1.0 / frame_s,
+        "unit": "fps",
+        "cores": os.cpu_count(),
+        "kind": "port",
+        "sample": f"{W}x{H} frame (1/{sample_div * sample_div} of the pixels) of the same scene and camera, "
+                  f"trace + BMFR, FP32, scaled by pixel count",
+        "grays_per_s": rays / (t1 - t0) / 1e9,
+        "ms_per_frame": frame_s * 1e3,
+    }
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+
+    sc = workload(args)
+    os_ = O.OracleScene(sc)
+    steps = []
+    info = None
+    for i in range(args.warmup + args.steps):
+        info = cpu_baseline(args, sc, sample_div=16, os_=os_)
+        if i >= args.warmup:
+            steps.append(1.0 / info["value"])
+    per = float(np.mean(steps))
+    line = {
+        "metric": METRIC, "value": 1.0 / per, "unit": "fps", "impl": "reference", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+        "config": {"workload": "1080p 1spp depth8 RR>=3, 1M-tri instanced scene, BMFR 32x32",
+                   "width": args.width, "height": args.height, "max_depth": args.max_depth,
+                   "min_depth": args.min_depth, "instances": args.instances},
+        "cpu_baseline": {k: info[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": 1.0 / per, "unit": "fps", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "grays_per_s": info["grays_per_s"],
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+def run_gb300(args):
+    import torch
+
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from vulkanpbrt_gb300 import build as B
+
+    B.build()
+    import vulkanpbrt_gb300 as vp
+
+    W, H = args.width, args.height
+    sc = workload(args, seed_offset=0)  # every rank renders its own request stream of the same scene
+    sh = vp.SceneHandle(sc)
+    info = sh.info()
+    g = vp.GBuffer(W, H)
+    illu = vp.IlluminationBufferDemodulatedFloat(W, H)
+    pipe = vp.PBRTPipeline(sh, g, illu, True, max_recursion_depth=args.max_depth, min_recursion_depth=args.min_depth)
+    accu = vp.Accumulator(g, illu, separate_matrices=True)
+    acc_illu = accu.accumulated_illumination
+    abuf = accu.accumulation_buffer
+    if args.denoiser == "bmfr":
+        den = vp.BMFR(W, H, 32, 32, g, acc_illu, abuf, 256)
+    else:
+        den = vp.BFR(W, H, 16, 16, g, acc_illu, abuf)
+    pc = vp.PushConstants()
+    stream = torch.cuda.current_stream(dev)
+    cams = [orbit(sc, W, H, f) for f in range(16)]
+    state = {"prev": cams[0]}
+
+    def frame(f):
+        cam = cams[f % 16]
+        prev = state["prev"]
+        pc.set(view_inverse=cam.inv_view, proj_inverse=cam.inv_proj, prev_view=prev.view, frame_number=f)
+        accu.set_camera_matrices(f, vp.CameraMatrices(cam.view, cam.inv_view, cam.proj, cam.inv_proj),
+                                 vp.CameraMatrices(prev.view, prev.inv_view))
+        s = stream
+        pipe.trace(pc, s)
+        vp.lib().pbrt_accumulator_dispatch(accu.ptr, vp._abi.stream_handle(s))
+        den.dispatch(pc, s)
+        vp.lib().pbrt_accumulation_buffer_copy_to_back_images(abuf.ptr, g.ptr, acc_illu.ptr, vp._abi.stream_handle(s))
+        state["prev"] = cam
+
+    # warm-up (also builds the frame graph)
+    for f in range(args.warmup):
+        frame(f)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    st0 = pipe.stats(stream)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    tev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        ev[0].record(stream)
+        for i in range(args.steps):
+            f = args.warmup + i
+            cam = cams[f % 16]
+            prev = state["prev"]
+            pc.set(view_inverse=cam.inv_view, proj_inverse=cam.inv_proj, prev_view=prev.view, frame_number=f)
+            accu.set_camera_matrices(f, vp.CameraMatrices(cam.view, cam.inv_view, cam.proj, cam.inv_proj),
+                                     vp.CameraMatrices(prev.view, prev.inv_view))
+            tev[i][0].record(stream)
+            pipe.trace(pc, stream)
+            tev[i][1].record(stream)
+            vp.lib().pbrt_accumulator_dispatch(accu.ptr, vp._abi.stream_handle(stream))
+            den.dispatch(pc, stream)
+            vp.lib().pbrt_accumulation_buffer_copy_to_back_images(abuf.ptr, g.ptr, acc_illu.ptr,
+                                                                  vp._abi.stream_handle(stream))
+            state["prev"] = cam
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+    total_ms = ev[0].elapsed_time(ev[1])
+    trace_ms = sum(a.elapsed_time(b) for a, b in tev)
+    st1 = pipe.stats(stream)
+    rays = (st1.primary_rays - st0.primary_rays) + (st1.extension_rays - st0.extension_rays) + \
+        (st1.shadow_rays - st0.shadow_rays)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+
+    # ---- end to end through the public API: frame + read-back of the final image every step
+    final = den.get_final_descriptor_image().tensor()
+    host = torch.empty(final.shape, dtype=final.dtype, pin_memory=True)
+    for f in range(2):
+        frame(args.warmup + args.steps + f)
+        host.copy_(final, non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_steps = args.steps
+    t0 = time.perf_counter()
+    for i in range(e2e_steps):
+        frame(args.warmup + args.steps + 2 + i)
+        host.copy_(final, non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    # per-step host inputs: the push constants and two CameraMatrices, passed by value (kernel arguments)
+    h2d = C.sizeof(vp._abi.PbrtPushConstants) + 2 * C.sizeof(vp._abi.PbrtCameraMatrices)
+    d2h = final.numel() * final.element_size()
+
+    # ---- per-kernel profile of one frame (roofline of the dominant kernel)
+    prof = pipe.profile(pc, stream)
+    stages = {"trace_closest": prof.trace_closest_ms, "shade": prof.shade_ms, "trace_shadow": prof.trace_shadow_ms,
+              "raygen": prof.raygen_ms, "finalize": prof.finalize_ms}
+    # denoiser / accumulator kernels timed alone
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    vp.lib().pbrt_accumulator_dispatch(accu.ptr, vp._abi.stream_handle(stream))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    stages["accumulate"] = e0.elapsed_time(e1)
+    e0.record(stream)
+    den.dispatch(pc, stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    stages["bmfr" if args.denoiser == "bmfr" else "bfr"] = e0.elapsed_time(e1)
+    closest_bytes = prof.closest_nodes * NODE_BYTES + prof.closest_tris * TRI_BYTES
+    launches = max(1, prof.closest_launches)
+    per_launch_s = prof.trace_closest_ms / 1e3 / launches
+    achieved = closest_bytes / launches / per_launch_s / 1e9
+    peak, peak_kind = peaks()
+    traffic = profile_traffic("k_trace_closest")
+    dominant = max(stages, key=stages.get)
+    if rank == 0:
+        steps = args.steps
+        value = world * steps / (total_ms / 1e3)
+        clocks = clk.summary()
+        cpu = None
+        if not args.no_cpu_baseline:
+            try:
+                cpu = cpu_baseline(args, sc)
+            except Exception as e:  # the baseline must not sink the GPU line
+                cpu = {"value": None, "unit": "fps", "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {e}"}
+        line = {
+            "metric": METRIC,
+            "value": value,
+            "unit": "fps",
+            "n_gpus": world,
+            "steps": steps,
+            "warmup": args.warmup,
+            "ms_per_step": total_ms / steps,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32",
+            "data": "synthetic (seeded procedural scene; inputs larger than L2: 0.8 GB textures, 0.5 GB path state)",
+            "config": {
+                "workload": "1080p 1spp depth8 RR>=3, 1M-tri instanced scene, accumulate + BMFR 32x32 (16-frame orbit)",
+                "width": W, "height": H, "max_depth": args.max_depth, "min_depth": args.min_depth,
+                "triangles": int(info.triangle_count), "instances": int(info.instance_count),
+                "lights": int(info.light_count), "texture_size": args.texture_size, "denoiser": args.denoiser,
+                "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}",
+            },
+            "grays_per_s": rays / (trace_ms / 1e3) / 1e9 * world,
+            "rays_per_frame": rays / steps,
+            "trace_ms_per_frame": trace_ms / steps,
+            "stage_ms": {k: round(v, 4) for k, v in stages.items()},
+            "e2e": {"value": world * e2e_steps / e2e_s, "unit": "fps", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "roofline": {
+                "kernel": "k_trace_closest (BVH8 closest-hit traversal)",
+                "bound": "hbm",
+                "achieved": achieved,
+                "peak": peak,
+                "unit": "GB/s",
+                "frac": achieved / peak,
+                "peak_source": peak_kind,
+                "traffic": traffic,
+                "bytes_per_ray": closest_bytes / max(1, prof.closest_rays),
+                "nodes_per_ray": prof.closest_nodes / max(1, prof.closest_rays),
+                "tris_per_ray": prof.closest_tris / max(1, prof.closest_rays),
+                "dominant_kernel": dominant,
+            },
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "gpu_launches": steps * (3 + 5 * (args.max_depth + 1) + 1 + 2),
+            "bvh": {"nodes": int(info.bvh_nodes), "depth": int(info.bvh_depth), "build_ms": info.build_ms},
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

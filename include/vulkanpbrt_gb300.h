@@ -305,6 +305,18 @@ typedef struct PbrtTraceStats {
 /* BVH queries issued since creation / the last reset (stream-synchronising). */
 PBRT_API int pbrt_pipeline_stats(PbrtPipeline* p, pbrt_stream_t stream, PbrtTraceStats* out);
 PBRT_API int pbrt_pipeline_reset_stats(PbrtPipeline* p, pbrt_stream_t stream);
+/* One frame launched stage by stage with CUDA events around every launch
+ * (no graph), for per-kernel timing; counts BVH work. No reference
+ * counterpart (the reference writes two timestamps it never reads,
+ * source/VulkanPBRT.cpp:397-408). */
+typedef struct PbrtStageTimes {
+  float raygen_ms, trace_closest_ms, shade_ms, trace_shadow_ms, finalize_ms;
+  uint64_t closest_rays, shadow_rays;
+  uint64_t closest_nodes, closest_tris, shadow_nodes, shadow_tris; /* node / triangle visits */
+  uint32_t closest_launches;
+} PbrtStageTimes;
+PBRT_API int pbrt_pipeline_profile(PbrtPipeline* p, const PbrtPushConstants* pc, pbrt_stream_t stream,
+                                   PbrtStageTimes* out);
 /* R32_UINT per pixel: key of the primary ray's closest triangle (see
  * pbrt_scene_trace_rays), 0xffffffff on a miss. */
 PBRT_API int pbrt_pipeline_debug_images(const PbrtPipeline* p, PbrtImage* primary_hit_key);

@@ -865,13 +865,27 @@ template <class T> struct Tracer {
   }
 };
 
+// The last scene's world-space triangles and BVH are kept, keyed by the
+// scene arrays' identity, so repeated renders of one scene build them once.
+template <class T> World<T>& cached_world(const OrcScene* sc) {
+  static World<T> w;
+  static const void* key[4] = {nullptr, nullptr, nullptr, nullptr};
+  const void* k[4] = {sc->idx, sc->inst_mat, sc->pos, (const void*)(uintptr_t)sc->instance_count};
+  if (std::memcmp(k, key, sizeof(k)) != 0) {
+    w = World<T>();
+    w.build(sc);
+    std::memcpy(key, k, sizeof(k));
+  }
+  w.sc = sc;
+  return w;
+}
+
 template <class T>
 int render(const OrcScene* sc, int W, int H, const float* inv_view, const float* inv_proj, uint32_t frame,
            uint32_t sample_n, int min_depth, int max_depth, int light_mode, int final_image, int frames, float* illum,
            float* depth, float* normal, uint8_t* material, uint8_t* albedo, uint32_t* hit_key, uint64_t* ray_counts,
            int threads) {
-  World<T> w;
-  w.build(sc);
+  World<T>& w = cached_world<T>(sc);
   Tracer<T> tr{w, sc, light_mode, min_depth, max_depth,
                sc->light_count ? sc->lights[32 * (sc->light_count - 1) + 31] : 0.f};
   M4<T> iv, ip;
@@ -960,8 +974,7 @@ int oracle_trace_rays(const OrcScene* sc, const float* org_tmin, const float* di
                       float* hits, int precision, int threads) {
   auto run = [&](auto tag) {
     using T = decltype(tag);
-    World<T> w;
-    w.build(sc);
+    World<T>& w = cached_world<T>(sc);
     Tracer<T> tr{w, sc, 0, 0, 0, 0.f};
     parallel_rows((int)((n + 255) / 256), threads, [&](int blk) {
       uint64_t rays = 0;

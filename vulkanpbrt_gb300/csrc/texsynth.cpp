@@ -114,9 +114,10 @@ PBRT_API int pbrt_synth_texture(uint64_t seed, uint32_t size, int32_t kind, cons
       float u = ((float)x + .5f) * inv, v = ((float)y + .5f) * inv;
       uint8_t* o = out_rgba + 4 * ((size_t)y * W + x);
       if (kind == 0) {
-        float n = fbm(s0, u, v);
+        float n = fbm(s0, u, v), m = value_noise(s0 + 77u, u, v, 16);
+        const float hue[3] = {m, 1.f - m, 0.5f};
         for (int c = 0; c < 3; ++c) {
-          float t = 0.55f + 0.45f * fbm(s0 + 77u * (uint32_t)(c + 1), u, v) * 0.3f + 0.45f * 0.7f * n;
+          float t = 0.55f + 0.45f * (0.3f * hue[c] + 0.7f * n);
           o[c] = to_u8(std::pow(std::min(color[c] * t, 1.f), g));
         }
         o[3] = 255;

@@ -102,7 +102,8 @@ struct Hit {
 };
 
 template <bool ANY_HIT>
-PBRT_D Hit traverse(const SceneView& sc, const RayPre& r, float tmin, float tmax, int* err) {
+PBRT_D Hit traverse(const SceneView& sc, const RayPre& r, float tmin, float tmax, int* err, uint32_t& n_nodes,
+                    uint32_t& n_tris) {
   Hit best;
   best.tri = -1;
   best.t = tmax;
@@ -113,6 +114,7 @@ PBRT_D Hit traverse(const SceneView& sc, const RayPre& r, float tmin, float tmax
   uint32_t node = 0;
   const float4* nodes4 = reinterpret_cast<const float4*>(sc.nodes);
   while (true) {
+    ++n_nodes;
     const float4 n0 = __ldg(nodes4 + 5 * node + 0);
     const float4 n1 = __ldg(nodes4 + 5 * node + 1);
     const float4 n2 = __ldg(nodes4 + 5 * node + 2);
@@ -160,6 +162,7 @@ PBRT_D Hit traverse(const SceneView& sc, const RayPre& r, float tmin, float tmax
         for (uint32_t k = 0; k < cnt; ++k) {
           const uint32_t ti = tri_base + off + k;
           const float4 a = __ldg(sc.tris + 3 * ti), b = __ldg(sc.tris + 3 * ti + 1), c = __ldg(sc.tris + 3 * ti + 2);
+          ++n_tris;
           float t, u, v;
           if (!tri_intersect(r, a, b, c, tmin, t, u, v)) continue;
           const uint32_t key = __float_as_uint(a.w);
@@ -221,7 +224,16 @@ struct Counters {
   uint32_t error;        // traversal stack overflow
   uint32_t pad[2];
   unsigned long long rays_primary, rays_extension, rays_shadow, frames;
+  unsigned long long nodes_closest, tris_closest, nodes_shadow, tris_shadow;  // BVH work (node / triangle visits)
 };
+
+// Adds a per-thread count to a 64-bit total with one atomic per warp.
+PBRT_D void warp_add64(unsigned long long* dst, uint32_t v) {
+  unsigned long long x = v;
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  if ((threadIdx.x & 31) == 0 && x) atomicAdd(dst, x);
+}
 
 struct Queues {
   // ray queues (2, ping-pong): path index, origin|tmin, direction|tmax
@@ -266,6 +278,10 @@ PBRT_D int warp_alloc(uint32_t* counter, bool want) {
 }
 
 // ---------------------------------------------------------------------------
+// Per-frame parameters travel as this launch's argument: no host buffer has
+// to outlive the call, so consecutive frames need no host synchronisation.
+__global__ void k_set_params(FrameParams* dst, FrameParams fp) { *dst = fp; }
+
 __global__ void k_frame_begin(Counters* c, const FrameParams* fp) {
   c->ray[0] = (uint32_t)(fp->W * fp->H);
   c->ray[1] = 0;
@@ -325,6 +341,7 @@ __global__ void __launch_bounds__(128) k_trace_closest(SceneView sc, Queues q, C
   const float4* org = q.org[k & 1];
   const float4* dir = q.dir[k & 1];
   int err = 0;
+  uint32_t nn = 0, nt = 0;
   while (true) {
     uint32_t base = 0;
     if (lane == 0) base = atomicAdd(&c->work_trace, 32u);
@@ -334,10 +351,12 @@ __global__ void __launch_bounds__(128) k_trace_closest(SceneView sc, Queues q, C
     if (i < count) {
       const float4 o = org[i], d = dir[i];
       RayPre r = ray_pre(f3(o.x, o.y, o.z), f3(d.x, d.y, d.z));
-      Hit h = traverse<false>(sc, r, o.w, d.w, &err);
+      Hit h = traverse<false>(sc, r, o.w, d.w, &err, nn, nt);
       q.hit[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
     }
   }
+  warp_add64(&c->nodes_closest, nn);
+  warp_add64(&c->tris_closest, nt);
   if (err) atomicOr(&c->error, 1u);
 }
 
@@ -347,6 +366,7 @@ __global__ void __launch_bounds__(128) k_trace_shadow(SceneView sc, Queues q, Co
   const int lane = threadIdx.x & 31;
   const uint32_t count = *((volatile uint32_t*)&c->shadow);
   int err = 0;
+  uint32_t nn = 0, nt = 0;
   while (true) {
     uint32_t base = 0;
     if (lane == 0) base = atomicAdd(&c->work_shadow, 32u);
@@ -356,7 +376,7 @@ __global__ void __launch_bounds__(128) k_trace_shadow(SceneView sc, Queues q, Co
     if (i < count) {
       const float4 o = q.sorg[i], d = q.sdir[i];
       RayPre r = ray_pre(f3(o.x, o.y, o.z), f3(d.x, d.y, d.z));
-      Hit h = traverse<true>(sc, r, o.w, d.w, &err);
+      Hit h = traverse<true>(sc, r, o.w, d.w, &err, nn, nt);
       const uint32_t p = q.spix[i];
       const float4 nee4 = q.snee[i], add4 = q.sadd[i];
       const float3 nee = h.tri >= 0 ? f3(0.f) : f3(nee4.x, nee4.y, nee4.z);
@@ -371,6 +391,8 @@ __global__ void __launch_bounds__(128) k_trace_shadow(SceneView sc, Queues q, Co
       q.rad[p] = make_float4(rad.x, rad.y, rad.z, rd.w);
     }
   }
+  warp_add64(&c->nodes_shadow, nn);
+  warp_add64(&c->tris_shadow, nt);
   if (err) atomicOr(&c->error, 1u);
 }
 
@@ -683,6 +705,7 @@ __global__ void __launch_bounds__(128) k_ray_query(SceneView sc, const float4* _
                                                    int any_hit, uint32_t* work, uint32_t* errflag) {
   const int lane = threadIdx.x & 31;
   int err = 0;
+  uint32_t nn = 0, nt = 0;
   while (true) {
     uint32_t base = 0;
     if (lane == 0) base = atomicAdd(work, 32u);
@@ -692,7 +715,7 @@ __global__ void __launch_bounds__(128) k_ray_query(SceneView sc, const float4* _
     if (i < n) {
       const float4 o = org[i], d = dir[i];
       RayPre r = ray_pre(f3(o.x, o.y, o.z), f3(d.x, d.y, d.z));
-      Hit h = any_hit ? traverse<true>(sc, r, o.w, d.w, &err) : traverse<false>(sc, r, o.w, d.w, &err);
+      Hit h = any_hit ? traverse<true>(sc, r, o.w, d.w, &err, nn, nt) : traverse<false>(sc, r, o.w, d.w, &err, nn, nt);
       const uint32_t key = h.tri >= 0 ? __float_as_uint(sc.tris[3 * h.tri].w) : 0xffffffffu;
       hits[i] = make_float4(h.t, h.u, h.v, __uint_as_float(key));
     }
@@ -779,7 +802,6 @@ struct PbrtPipeline : pbrt::Object {
   ~PbrtPipeline() override {
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
     for (void* p : allocs) cudaFree(p);
-    if (host_fp) cudaFreeHost(host_fp);
     release(scene);
     release(gbuffer);
     release(illumination);
@@ -794,7 +816,6 @@ struct PbrtPipeline : pbrt::Object {
   Queues q{};
   Counters* ctr = nullptr;
   FrameParams* dev_fp = nullptr;
-  FrameParams* host_fp = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   int graph_depth = -1;
   int grid_persistent = 0;
@@ -805,7 +826,23 @@ struct PbrtPipeline : pbrt::Object {
   }
 };
 
-static int record_frame(PbrtPipeline* pp, cudaStream_t s) {
+// Optional per-stage timing (events summed over the frame's launches).
+struct StageEvents {
+  static constexpr int kCount = 5;  // raygen, closest, shade, shadow, finalize
+  cudaEvent_t ev[kCount][2];
+  float ms[kCount];
+  cudaStream_t stream;
+  void begin(int i) { cudaEventRecord(ev[i][0], stream); }
+  void end(int i) {
+    cudaEventRecord(ev[i][1], stream);
+    cudaEventSynchronize(ev[i][1]);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, ev[i][0], ev[i][1]);
+    ms[i] += t;
+  }
+};
+
+static int record_frame(PbrtPipeline* pp, cudaStream_t s, StageEvents* ev) {
   const int N = pp->W * pp->H;
   const SceneView sc = pp->scene->view;
   GBufferOut g{};
@@ -818,19 +855,28 @@ static int record_frame(PbrtPipeline* pp, cudaStream_t s) {
   float4* out = pp->illumination->images[0].ptr<float4>();
   const int blocks_px = std::min((N + 255) / 256, 152 * 8);
   k_frame_begin<<<1, 1, 0, s>>>(pp->ctr, pp->dev_fp);
+  if (ev) ev->begin(0);
   k_raygen<<<blocks_px, 256, 0, s>>>(pp->dev_fp, pp->q);
-  const int depth = pp->max_depth;
+  if (ev) ev->end(0);
   // Bounce k traces the rays that leave vertex k-1. Transmissive vertices do
   // not count towards the depth (ptRaygen.rgen:69, up to 10 of them).
-  const int bounces = depth + 1 + (pp->scene->transmissive ? 10 : 0);
+  const int bounces = pp->max_depth + 1 + (pp->scene->transmissive ? 10 : 0);
   for (int k = 0; k < bounces; ++k) {
     k_bounce_begin<<<1, 1, 0, s>>>(pp->ctr, k);
+    if (ev) ev->begin(1);
     k_trace_closest<<<pp->grid_persistent, 128, 0, s>>>(sc, pp->q, pp->ctr, k);
+    if (ev) ev->end(1);
+    if (ev) ev->begin(2);
     k_shade<<<pp->grid_persistent, 128, 0, s>>>(sc, pp->dev_fp, pp->q, pp->ctr, g, k);
+    if (ev) ev->end(2);
+    if (ev) ev->begin(3);
     k_trace_shadow<<<pp->grid_persistent, 128, 0, s>>>(sc, pp->q, pp->ctr);
+    if (ev) ev->end(3);
     k_bounce_end<<<1, 1, 0, s>>>(pp->ctr);
   }
+  if (ev) ev->begin(4);
   k_finalize<<<blocks_px, 256, 0, s>>>(pp->dev_fp, pp->q, out);
+  if (ev) ev->end(4);
   return check_launch("path tracer frame");
 }
 
@@ -1124,7 +1170,6 @@ PBRT_API int pbrt_pipeline_create(PbrtScene* scene, PbrtGBuffer* g, PbrtIllumina
   if (!st) st = pp->a(&pp->dev_fp, 1);
   if (!st) {
     cudaError_t e = cudaMemset(pp->ctr, 0, sizeof(Counters));
-    if (e == cudaSuccess) e = cudaMallocHost((void**)&pp->host_fp, sizeof(FrameParams));
     if (e != cudaSuccess) st = cuda_fail(e, "pipeline state");
   }
   if (!st) {
@@ -1154,11 +1199,8 @@ PBRT_API int pbrt_pipeline_set_config(PbrtPipeline* pp, int32_t light_sampling, 
   return PBRT_OK;
 }
 
-PBRT_API int pbrt_pipeline_trace(PbrtPipeline* pp, const PbrtPushConstants* pc, pbrt_stream_t stream) {
-  if (!checked<PbrtPipeline>(pp, Kind::Pipeline) || !pc) return fail(PBRT_ERROR_INVALID_ARGUMENT, "trace: bad arguments");
-  FrameParams& fp = *pp->host_fp;
-  // The previous frame's copy out of host_fp must be done before rewriting it.
-  PBRT_CUDA(cudaStreamSynchronize(stream));
+static FrameParams frame_params(const PbrtPipeline* pp, const PbrtPushConstants* pc) {
+  FrameParams fp;
   for (int c = 0; c < 4; ++c) {
     fp.inv_view.c[c] = make_float4(pc->view_inverse[4 * c], pc->view_inverse[4 * c + 1], pc->view_inverse[4 * c + 2],
                                    pc->view_inverse[4 * c + 3]);
@@ -1174,15 +1216,23 @@ PBRT_API int pbrt_pipeline_trace(PbrtPipeline* pp, const PbrtPushConstants* pc, 
   fp.light_mode = pp->light_mode;
   fp.final_image = pp->illumination->type == PBRT_ILLUMINATION_FINAL_FLOAT ? 1 : 0;
   fp.write_gbuffer = pp->write_gbuffer ? 1 : 0;
-  PBRT_CUDA(cudaMemcpyAsync(pp->dev_fp, pp->host_fp, sizeof(FrameParams), cudaMemcpyHostToDevice, stream));
-  if (!pp->graph_exec || pp->graph_depth != pp->max_depth) {
+  return fp;
+}
+
+PBRT_API int pbrt_pipeline_trace(PbrtPipeline* pp, const PbrtPushConstants* pc, pbrt_stream_t stream) {
+  if (!checked<PbrtPipeline>(pp, Kind::Pipeline) || !pc) return fail(PBRT_ERROR_INVALID_ARGUMENT, "trace: bad arguments");
+  k_set_params<<<1, 1, 0, stream>>>(pp->dev_fp, frame_params(pp, pc));
+  int st = check_launch("k_set_params");
+  if (st) return st;
+  const int bounces = pp->max_depth + 1 + (pp->scene->transmissive ? 10 : 0);
+  if (!pp->graph_exec || pp->graph_depth != bounces) {
     if (pp->graph_exec) cudaGraphExecDestroy(pp->graph_exec);
     pp->graph_exec = nullptr;
     cudaStream_t cap;
     PBRT_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
     cudaGraph_t graph;
     cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
-    int st = e == cudaSuccess ? record_frame(pp, cap) : cuda_fail(e, "begin capture");
+    st = e == cudaSuccess ? record_frame(pp, cap, nullptr) : cuda_fail(e, "begin capture");
     cudaError_t e2 = cudaStreamEndCapture(cap, &graph);
     cudaStreamDestroy(cap);
     if (st) return st;
@@ -1190,9 +1240,48 @@ PBRT_API int pbrt_pipeline_trace(PbrtPipeline* pp, const PbrtPushConstants* pc, 
     e = cudaGraphInstantiate(&pp->graph_exec, graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return cuda_fail(e, "graph instantiate");
-    pp->graph_depth = pp->max_depth;
+    pp->graph_depth = bounces;
   }
   PBRT_CUDA(cudaGraphLaunch(pp->graph_exec, stream));
+  return PBRT_OK;
+}
+
+PBRT_API int pbrt_pipeline_profile(PbrtPipeline* pp, const PbrtPushConstants* pc, pbrt_stream_t stream,
+                                   PbrtStageTimes* out) {
+  if (!checked<PbrtPipeline>(pp, Kind::Pipeline) || !pc || !out)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "profile: bad arguments");
+  StageEvents ev;
+  for (int i = 0; i < StageEvents::kCount; ++i) {
+    ev.ms[i] = 0.f;
+    PBRT_CUDA(cudaEventCreate(&ev.ev[i][0]));
+    PBRT_CUDA(cudaEventCreate(&ev.ev[i][1]));
+  }
+  ev.stream = stream;
+  k_set_params<<<1, 1, 0, stream>>>(pp->dev_fp, frame_params(pp, pc));
+  Counters before;
+  PBRT_CUDA(cudaMemcpyAsync(&before, pp->ctr, sizeof(Counters), cudaMemcpyDeviceToHost, stream));
+  PBRT_CUDA(cudaStreamSynchronize(stream));
+  int st = record_frame(pp, stream, &ev);
+  PBRT_CUDA(cudaStreamSynchronize(stream));
+  Counters after;
+  PBRT_CUDA(cudaMemcpy(&after, pp->ctr, sizeof(Counters), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < StageEvents::kCount; ++i) {
+    cudaEventDestroy(ev.ev[i][0]);
+    cudaEventDestroy(ev.ev[i][1]);
+  }
+  if (st) return st;
+  out->raygen_ms = ev.ms[0];
+  out->trace_closest_ms = ev.ms[1];
+  out->shade_ms = ev.ms[2];
+  out->trace_shadow_ms = ev.ms[3];
+  out->finalize_ms = ev.ms[4];
+  out->closest_rays = (after.rays_primary - before.rays_primary) + (after.rays_extension - before.rays_extension);
+  out->shadow_rays = after.rays_shadow - before.rays_shadow;
+  out->closest_nodes = after.nodes_closest - before.nodes_closest;
+  out->closest_tris = after.tris_closest - before.tris_closest;
+  out->shadow_nodes = after.nodes_shadow - before.nodes_shadow;
+  out->shadow_tris = after.tris_shadow - before.tris_shadow;
+  out->closest_launches = (uint32_t)(pp->graph_depth > 0 ? pp->graph_depth : pp->max_depth + 1);
   return PBRT_OK;
 }
 

@@ -45,6 +45,13 @@ class PbrtTraceStats(C.Structure):
                 ("shadow_rays", C.c_uint64), ("error_flags", C.c_uint32)]
 
 
+class PbrtStageTimes(C.Structure):
+    _fields_ = [("raygen_ms", C.c_float), ("trace_closest_ms", C.c_float), ("shade_ms", C.c_float),
+                ("trace_shadow_ms", C.c_float), ("finalize_ms", C.c_float), ("closest_rays", C.c_uint64),
+                ("shadow_rays", C.c_uint64), ("closest_nodes", C.c_uint64), ("closest_tris", C.c_uint64),
+                ("shadow_nodes", C.c_uint64), ("shadow_tris", C.c_uint64), ("closest_launches", C.c_uint32)]
+
+
 H, P = C.c_void_p, C.POINTER
 _abi.add_signatures({
     "pbrt_scene_create": (C.c_int32, [P(PbrtSceneDesc), P(H)]),
@@ -56,6 +63,7 @@ _abi.add_signatures({
     "pbrt_pipeline_stats": (C.c_int32, [H, H, P(PbrtTraceStats)]),
     "pbrt_pipeline_reset_stats": (C.c_int32, [H, H]),
     "pbrt_pipeline_debug_images": (C.c_int32, [H, P(PbrtImage)]),
+    "pbrt_pipeline_profile": (C.c_int32, [H, P(_abi.PbrtPushConstants), H, P(PbrtStageTimes)]),
 })
 
 
@@ -177,6 +185,12 @@ class PBRTPipeline(Handle):
         s = PbrtTraceStats()
         check(lib().pbrt_pipeline_stats(self.ptr, stream_handle(stream), C.byref(s)))
         return s
+
+    def profile(self, push_constants: PushConstants, stream=None) -> PbrtStageTimes:
+        """One frame launched stage by stage with CUDA events (per-kernel times, BVH work counts)."""
+        t = PbrtStageTimes()
+        check(lib().pbrt_pipeline_profile(self.ptr, C.byref(push_constants.value), stream_handle(stream), C.byref(t)))
+        return t
 
     def reset_stats(self, stream=None) -> None:
         check(lib().pbrt_pipeline_reset_stats(self.ptr, stream_handle(stream)))
