@@ -189,6 +189,42 @@ PBRT_API int pbrt_bmfr_images(const PbrtBMFR* b, PbrtImage* denoised, PbrtImage*
  * read; synchronises the stream). */
 PBRT_API int pbrt_bmfr_fp64_block_count(PbrtBMFR* b, pbrt_stream_t stream, uint32_t* count);
 
+/* BMFR for callers that cannot allocate device memory. No counterpart in the
+ * reference. Hosts that own the device-memory budget (an engine or compositor
+ * handing a plugin only its images), per-frame code that must not hit the
+ * device-wide synchronisation cudaMalloc / cudaFree can cause, and code that
+ * runs while its stream is being captured cannot create a PbrtBMFR (which
+ * allocates its weights and output images). This entry point runs the same
+ * fused BMFR kernel on images the caller provides and allocates nothing: the
+ * fit's per-block weights go to a fixed array inside the library, of
+ * PBRT_BMFR_NOALLOC_MAX_BLOCKS x 30 floats (1.9 MiB), which every GPU that
+ * loads the library holds until the process exits. Images whose block grid
+ * ((width/b + 2) x (height/b + 2) for block size b) exceeds that maximum are
+ * rejected with PBRT_ERROR_INVALID_ARGUMENT (1080p and 4K fit with 32x32 and
+ * 16x16 blocks, 1080p does not with 8x8). The first call on a device looks up
+ * that array's device address (cudaGetSymbolAddress) and sets the kernel's
+ * shared-memory limit, so make that first call before any stream capture.
+ * All calls share the one array: calls whose kernels can overlap on the GPU
+ * (different streams, no ordering between them) race on it; order them on
+ * one stream. Nothing in the array has to start at zero (each block writes
+ * its weights before reading them). The FP64 re-solve is not available here.
+ * Images: width x height, rows packed; denoised holds 2 RGBA16F layers (layer
+ * frame & 1 is read as the previous frame, layer (frame & 1) ^ 1 written). */
+#define PBRT_BMFR_NOALLOC_MAX_BLOCKS 16384
+typedef struct PbrtBmfrNoAllocImages {
+  const float* depth;    /* R32F */
+  const float* normal;   /* RG32F (theta, phi) */
+  const uint8_t* albedo; /* RGBA8 */
+  const void* noisy;     /* RGBA16F accumulated, demodulated illumination */
+  const void* motion;    /* RG16F */
+  const uint8_t* spp;    /* R8_UNORM */
+  void* denoised;        /* RGBA16F x 2 layers, read and written */
+  uint8_t* final_bgra;   /* B8G8R8A8, written */
+} PbrtBmfrNoAllocImages;
+PBRT_API int pbrt_bmfr_dispatch_noalloc(uint32_t width, uint32_t height, uint32_t block_size, int32_t position_type,
+                                        const PbrtBmfrNoAllocImages* images, const PbrtPushConstants* pc,
+                                        pbrt_stream_t stream);
+
 /* ---- BFR (source/renderModules/denoisers/BFR.hpp:8-45) ----------------- */
 PBRT_API int pbrt_bfr_create(uint32_t width, uint32_t height, uint32_t work_width, uint32_t work_height,
                              PbrtGBuffer* g, PbrtIlluminationBuffer* illumination, PbrtAccumulationBuffer* acc,

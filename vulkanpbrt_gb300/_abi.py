@@ -80,6 +80,11 @@ class PbrtAccumulationImages(C.Structure):
     _fields_ = [(n, PbrtImage) for n in ("prev_illu", "prev_illu_squared", "prev_depth", "prev_normal", "spp", "prev_spp", "motion")]
 
 
+class PbrtBmfrNoAllocImages(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in ("depth", "normal", "albedo", "noisy", "motion", "spp", "denoised",
+                                          "final_bgra")]
+
+
 _lib = None
 
 H = C.c_void_p
@@ -109,6 +114,7 @@ _SIGS = {
     "pbrt_bmfr_final_image": (i32, [H, P(PbrtImage)]),
     "pbrt_bmfr_images": (i32, [H, P(PbrtImage), P(PbrtImage)]),
     "pbrt_bmfr_fp64_block_count": (i32, [H, H, P(u32)]),
+    "pbrt_bmfr_dispatch_noalloc": (i32, [u32, u32, u32, i32, P(PbrtBmfrNoAllocImages), P(PbrtPushConstants), H]),
     "pbrt_bfr_create": (i32, [u32, u32, u32, u32, H, H, H, P(H)]),
     "pbrt_bfr_dispatch": (i32, [H, P(PbrtPushConstants), H]),
     "pbrt_bfr_final_image": (i32, [H, P(PbrtImage)]),

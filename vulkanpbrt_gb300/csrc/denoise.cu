@@ -11,6 +11,7 @@
 // shader rounding.
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <new>
 
 #include "device_common.cuh"
@@ -1188,3 +1189,102 @@ PBRT_API int pbrt_bfr_images(const PbrtBFR* b, PbrtImage* denoised) {
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// BMFR without device allocation.
+//
+// Some callers cannot call cudaMalloc: a host engine or compositor that owns
+// the device-memory budget and hands plugins only the images they work on,
+// per-frame code that must not run into the device-wide synchronisation
+// cudaMalloc / cudaFree can cause, or code that runs while its stream is being
+// captured. For them the fit's per-block weights -- the only memory the fused
+// kernel needs beyond its inputs and outputs -- live in the file-scope array
+// below, which every GPU that loads this library holds until the process
+// exits (kNoAllocMaxBlocks * 30 floats = 1.9 MiB).
+namespace pbrt {
+constexpr uint32_t kNoAllocMaxBlocks = PBRT_BMFR_NOALLOC_MAX_BLOCKS;
+static __device__ __align__(256) float g_bmfr_noalloc_weights[kNoAllocMaxBlocks * 30];
+
+// Device address of g_bmfr_noalloc_weights for each device, resolved once
+// with that device current (host code cannot use the symbol itself).
+static std::mutex g_noalloc_mutex;
+static float* g_noalloc_ptr[128] = {nullptr};
+
+static int noalloc_weights(float** out) {
+  int dev = 0;
+  PBRT_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 128) return fail(PBRT_ERROR_UNSUPPORTED, "BMFR no-alloc: device ordinal %d", dev);
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_bmfr_noalloc_weights);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_bmfr_noalloc_weights)");
+    for (int bw : {8, 16, 32}) {  // shared-memory opt-in of the kernel this entry point launches
+      size_t smem = bmfr_smem_bytes(bw);
+      cudaError_t a = bw == 8    ? cudaFuncSetAttribute(bmfr_fused_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                      : bw == 16 ? cudaFuncSetAttribute(bmfr_fused_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                                 : cudaFuncSetAttribute(bmfr_fused_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (a != cudaSuccess) return cuda_fail(a, "cudaFuncSetAttribute(bmfr_fused_kernel)");
+    }
+    g_noalloc_ptr[dev] = static_cast<float*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return PBRT_OK;
+}
+}  // namespace pbrt
+
+extern "C" PBRT_API int pbrt_bmfr_dispatch_noalloc(uint32_t width, uint32_t height, uint32_t block_size,
+                                                   int32_t position_type, const PbrtBmfrNoAllocImages* im,
+                                                   const PbrtPushConstants* pc, pbrt_stream_t stream) {
+  using namespace pbrt;
+  if (!im || !pc || !im->depth || !im->normal || !im->albedo || !im->noisy || !im->motion || !im->spp ||
+      !im->denoised || !im->final_bgra)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "BMFR no-alloc: null image pointer or push constants");
+  if (block_size != 8 && block_size != 16 && block_size != 32)
+    return fail(PBRT_ERROR_UNSUPPORTED, "BMFR no-alloc: block size %u (supported: 8, 16, 32)", block_size);
+  if (position_type < 0 || position_type > 2)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "BMFR no-alloc: POSITION_TYPE %d", position_type);
+  if (width < 2 * block_size + 2 || height < 2 * block_size + 2)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "BMFR no-alloc: image %ux%u smaller than the mirror padding allows",
+                width, height);
+  const uint64_t gw = width / block_size + 2, gh = height / block_size + 2;
+  if (gw * gh > kNoAllocMaxBlocks)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT,
+                "BMFR no-alloc: %ux%u with %ux%u blocks needs %llu blocks of weight scratch, above the fixed maximum "
+                "of %u (use pbrt_bmfr_create / pbrt_bmfr_dispatch, or larger blocks)",
+                width, height, block_size, block_size, (unsigned long long)(gw * gh), kNoAllocMaxBlocks);
+  float* weights = nullptr;
+  int st = noalloc_weights(&weights);
+  if (st) return st;
+  BmfrParams kp;
+  kp.inv_view = to_mat4(pc->view_inverse);
+  kp.inv_proj = to_mat4(pc->proj_inverse);
+  kp.W = (int)width;
+  kp.H = (int)height;
+  kp.gw = (int)gw;
+  kp.gh = (int)gh;
+  kp.frame = pc->frame_number;
+  kp.position_type = position_type;
+  kp.fp64_resolve = 0;
+  kp.depth = im->depth;
+  kp.normal = reinterpret_cast<const float2*>(im->normal);
+  kp.noisy_f16 = reinterpret_cast<const Half4*>(im->noisy);
+  kp.noisy_f32 = nullptr;
+  kp.weights = weights;  // every block writes all 30 of its weights before reading them back
+  kp.flagged = nullptr;
+  kp.post.motion = reinterpret_cast<const __half2*>(im->motion);
+  kp.post.spp = im->spp;
+  kp.post.albedo = im->albedo;
+  kp.post.denoised = reinterpret_cast<Half4*>(im->denoised);
+  kp.post.final_bgra = reinterpret_cast<uchar4*>(im->final_bgra);
+  kp.post.W = kp.W;
+  kp.post.H = kp.H;
+  kp.post.frame = kp.frame;
+  dim3 grid((unsigned)gw, (unsigned)gh);
+  switch (block_size) {
+    case 8: bmfr_fused_kernel<8><<<grid, BmfrShape<8>::NT, bmfr_smem_bytes(8), stream>>>(kp); break;
+    case 16: bmfr_fused_kernel<16><<<grid, BmfrShape<16>::NT, bmfr_smem_bytes(16), stream>>>(kp); break;
+    default: bmfr_fused_kernel<32><<<grid, BmfrShape<32>::NT, bmfr_smem_bytes(32), stream>>>(kp); break;
+  }
+  return check_launch("bmfr_fused_kernel (no-alloc)");
+}
