@@ -95,113 +95,132 @@ PBRT_D bool tri_intersect(const RayPre& r, float4 a, float4 b, float4 c, float t
   return true;
 }
 
-// Result of a traversal: BVH-order triangle slot (-1 = miss) and attributes.
-struct Hit {
-  int tri;
-  float t, u, v;
+// ptAlphaHit out of line: it runs rarely, and inlined into the node visit it
+// inflated the traversal loop (instruction-fetch stalls).
+__device__ __noinline__ bool alpha_accept_slow(const DevInstance* instances, const DevMesh* meshes,
+                                               const uint32_t* idx, const float* uvs, const DevTexture* textures,
+                                               const uchar4* texels, uint32_t inst_id, uint32_t prim, float bu,
+                                               float bv) {
+  SceneView sc{};
+  sc.instances = instances;
+  sc.meshes = meshes;
+  sc.idx = idx;
+  sc.uv = uvs;
+  sc.textures = textures;
+  sc.texels = texels;
+  return alpha_accept(sc, inst_id, prim, bu, bv);
+}
+PBRT_D bool alpha_accept_call(const SceneView& sc, uint32_t inst_id, uint32_t prim, float bu, float bv) {
+  if (__ldg(&sc.instances[inst_id].opaque)) return true;
+  return alpha_accept_slow(sc.instances, sc.meshes, sc.idx, sc.uv, sc.textures, sc.texels, inst_id, prim, bu, bv);
+}
+
+// Per-ray traversal state: the node to visit next, the short stack of node
+// groups (child base, inner mask << 8 | remaining hits) and the best hit.
+struct TravState {
+  uint32_t node;
+  int sp;
+  int best_tri;  // BVH-order triangle slot, -1 = miss
+  float tbest, bu, bv;
+  uint32_t best_key;
 };
 
+// Visits st.node: box-tests its children, intersects the triangles of the
+// leaf children that are hit, and moves to the nearest inner child (octant
+// order) or to the next entry of the stack. Returns false when the ray is
+// finished (stack empty, or -- for ANY_HIT -- an accepted hit).
 template <bool ANY_HIT>
-PBRT_D Hit traverse(const SceneView& sc, const RayPre& r, float tmin, float tmax, int* err, uint32_t& n_nodes,
-                    uint32_t& n_tris) {
-  Hit best;
-  best.tri = -1;
-  best.t = tmax;
-  best.u = best.v = 0.f;
-  uint32_t best_key = 0xffffffffu;
-  uint2 stack[kStackSize];
-  int sp = 0;
-  uint32_t node = 0;
+PBRT_D bool visit_node(const SceneView& sc, const RayPre& r, float tmin, TravState& st, uint2* stack, int& err,
+                       uint32_t& n_nodes, uint32_t& n_tris) {
   const float4* nodes4 = reinterpret_cast<const float4*>(sc.nodes);
-  while (true) {
-    ++n_nodes;
-    const float4 n0 = __ldg(nodes4 + 5 * node + 0);
-    const float4 n1 = __ldg(nodes4 + 5 * node + 1);
-    const float4 n2 = __ldg(nodes4 + 5 * node + 2);
-    const float4 n3 = __ldg(nodes4 + 5 * node + 3);
-    const float4 n4 = __ldg(nodes4 + 5 * node + 4);
-    const uint32_t emi = __float_as_uint(n0.w);
-    const float sx = __uint_as_float(((emi >> 0) & 0xffu) << 23);
-    const float sy = __uint_as_float(((emi >> 8) & 0xffu) << 23);
-    const float sz = __uint_as_float(((emi >> 16) & 0xffu) << 23);
-    const uint32_t imask = emi >> 24;
-    const uint32_t child_base = __float_as_uint(n1.x), tri_base = __float_as_uint(n1.y);
-    const uint32_t meta_lo = __float_as_uint(n1.z), meta_hi = __float_as_uint(n1.w);
-    // t = (p + scale * q - o) * inv = q * (scale * inv) + (p - o) * inv
-    const float adx = (n0.x - r.o.x) * r.inv.x, ady = (n0.y - r.o.y) * r.inv.y, adz = (n0.z - r.o.z) * r.inv.z;
-    const float scx = sx * r.inv.x, scy = sy * r.inv.y, scz = sz * r.inv.z;
-    const uint2 qlx = make_uint2(__float_as_uint(n2.x), __float_as_uint(n2.y));
-    const uint2 qly = make_uint2(__float_as_uint(n2.z), __float_as_uint(n2.w));
-    const uint2 qlz = make_uint2(__float_as_uint(n3.x), __float_as_uint(n3.y));
-    const uint2 qhx = make_uint2(__float_as_uint(n3.z), __float_as_uint(n3.w));
-    const uint2 qhy = make_uint2(__float_as_uint(n4.x), __float_as_uint(n4.y));
-    const uint2 qhz = make_uint2(__float_as_uint(n4.z), __float_as_uint(n4.w));
-    uint32_t inner = 0;
+  const uint32_t node = st.node;
+  ++n_nodes;
+  const float4 n0 = __ldg(nodes4 + 5 * node + 0);
+  const float4 n1 = __ldg(nodes4 + 5 * node + 1);
+  const float4 n2 = __ldg(nodes4 + 5 * node + 2);
+  const float4 n3 = __ldg(nodes4 + 5 * node + 3);
+  const float4 n4 = __ldg(nodes4 + 5 * node + 4);
+  const uint32_t emi = __float_as_uint(n0.w);
+  const uint32_t imask = emi >> 24;
+  const uint32_t child_base = __float_as_uint(n1.x), tri_base = __float_as_uint(n1.y);
+  const uint32_t meta_lo = __float_as_uint(n1.z), meta_hi = __float_as_uint(n1.w);
+  // t = (p + scale * q - o) * inv = q * (scale * inv) + (p - o) * inv
+  const float adx = (n0.x - r.o.x) * r.inv.x, ady = (n0.y - r.o.y) * r.inv.y, adz = (n0.z - r.o.z) * r.inv.z;
+  const float scx = __uint_as_float(((emi >> 0) & 0xffu) << 23) * r.inv.x;
+  const float scy = __uint_as_float(((emi >> 8) & 0xffu) << 23) * r.inv.y;
+  const float scz = __uint_as_float(((emi >> 16) & 0xffu) << 23) * r.inv.z;
+  uint32_t inner = 0, leaves = 0;
 #pragma unroll
-    for (int s = 0; s < 8; ++s) {
-      const uint32_t meta = ((s < 4 ? meta_lo : meta_hi) >> (8 * (s & 3))) & 0xffu;
-      if (meta == 0) continue;
-      const int sh = 8 * (s & 3);
-      float lx = (float)(((s < 4 ? qlx.x : qlx.y) >> sh) & 0xffu), hx = (float)(((s < 4 ? qhx.x : qhx.y) >> sh) & 0xffu);
-      float ly = (float)(((s < 4 ? qly.x : qly.y) >> sh) & 0xffu), hy = (float)(((s < 4 ? qhy.x : qhy.y) >> sh) & 0xffu);
-      float lz = (float)(((s < 4 ? qlz.x : qlz.y) >> sh) & 0xffu), hz = (float)(((s < 4 ? qhz.x : qhz.y) >> sh) & 0xffu);
-      float tx0 = fmaf(lx, scx, adx), tx1 = fmaf(hx, scx, adx);
-      float ty0 = fmaf(ly, scy, ady), ty1 = fmaf(hy, scy, ady);
-      float tz0 = fmaf(lz, scz, adz), tz1 = fmaf(hz, scz, adz);
-      float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
-      float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), best.t));
-      // widened by a few ulp: the quantised boxes are conservative, the
-      // slab arithmetic must not undo that
-      tn = tn - fabsf(tn) * 4e-7f;
-      tf = tf + fabsf(tf) * 4e-7f;
-      if (!(tn <= tf)) continue;
-      if (meta & 0x80u) {
-        inner |= 1u << (s ^ r.oct);
-      } else {
-        const uint32_t cnt = meta >> 5, off = meta & 31u;
-        for (uint32_t k = 0; k < cnt; ++k) {
-          const uint32_t ti = tri_base + off + k;
-          const float4 a = __ldg(sc.tris + 3 * ti), b = __ldg(sc.tris + 3 * ti + 1), c = __ldg(sc.tris + 3 * ti + 2);
-          ++n_tris;
-          float t, u, v;
-          if (!tri_intersect(r, a, b, c, tmin, t, u, v)) continue;
-          const uint32_t key = __float_as_uint(a.w);
-          if (!(t < best.t || (t == best.t && key < best_key))) continue;
-          if (sc.any_alpha && !alpha_accept(sc, __float_as_uint(b.w), __float_as_uint(c.w), u, v)) continue;
-          best.tri = (int)ti;
-          best.t = t;
-          best.u = u;
-          best.v = v;
-          best_key = key;
-          if (ANY_HIT) return best;
-        }
-      }
+  for (int s = 0; s < 8; ++s) {
+    const int sh = 8 * (s & 3);
+    const uint32_t meta = ((s < 4 ? meta_lo : meta_hi) >> sh) & 0xffu;
+    const float lx = (float)((__float_as_uint(s < 4 ? n2.x : n2.y) >> sh) & 0xffu);
+    const float ly = (float)((__float_as_uint(s < 4 ? n2.z : n2.w) >> sh) & 0xffu);
+    const float lz = (float)((__float_as_uint(s < 4 ? n3.x : n3.y) >> sh) & 0xffu);
+    const float hx = (float)((__float_as_uint(s < 4 ? n3.z : n3.w) >> sh) & 0xffu);
+    const float hy = (float)((__float_as_uint(s < 4 ? n4.x : n4.y) >> sh) & 0xffu);
+    const float hz = (float)((__float_as_uint(s < 4 ? n4.z : n4.w) >> sh) & 0xffu);
+    const float tx0 = fmaf(lx, scx, adx), tx1 = fmaf(hx, scx, adx);
+    const float ty0 = fmaf(ly, scy, ady), ty1 = fmaf(hy, scy, ady);
+    const float tz0 = fmaf(lz, scz, adz), tz1 = fmaf(hz, scz, adz);
+    float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
+    float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), st.tbest));
+    // widened by a few ulp: the quantised boxes are conservative, the slab
+    // arithmetic must not undo that
+    tn = tn - fabsf(tn) * 4e-7f;
+    tf = tf + fabsf(tf) * 4e-7f;
+    const bool hit = meta != 0 && tn <= tf;
+    if (hit) {
+      if (meta & 0x80u) inner |= 1u << (s ^ r.oct);
+      else leaves |= 1u << s;
     }
-    if (inner) {
-      const int k = __ffs(inner) - 1;
-      inner &= inner - 1;
-      const int s = k ^ r.oct;
-      if (inner) {
-        if (sp == kStackSize) {
-          *err = 1;
-          return best;
-        }
-        stack[sp++] = make_uint2(child_base, (imask << 8) | inner);
-      }
-      node = child_base + __popc(imask & ((1u << s) - 1u));
-      continue;
-    }
-    if (sp == 0) break;
-    uint2 g = stack[--sp];
-    uint32_t m = g.y & 0xffu;
-    const uint32_t im = g.y >> 8;
-    const int k = __ffs(m) - 1;
-    m &= m - 1;
-    const int s = k ^ r.oct;
-    if (m) stack[sp++] = make_uint2(g.x, (im << 8) | m);
-    node = g.x + __popc(im & ((1u << s) - 1u));
   }
-  return best;
+  while (leaves) {
+    const int s = __ffs(leaves) - 1;
+    leaves &= leaves - 1;
+    const uint32_t meta = ((s < 4 ? meta_lo : meta_hi) >> (8 * (s & 3))) & 0xffu;
+    const uint32_t cnt = meta >> 5, off = meta & 31u;
+    for (uint32_t k = 0; k < cnt; ++k) {
+      const uint32_t ti = tri_base + off + k;
+      const float4 a = __ldg(sc.tris + 3 * ti), b = __ldg(sc.tris + 3 * ti + 1), c = __ldg(sc.tris + 3 * ti + 2);
+      ++n_tris;
+      float t, u, v;
+      if (!tri_intersect(r, a, b, c, tmin, t, u, v)) continue;
+      const uint32_t key = __float_as_uint(a.w);
+      if (!(t < st.tbest || (t == st.tbest && key < st.best_key))) continue;
+      if (sc.any_alpha && !alpha_accept_call(sc, __float_as_uint(b.w), __float_as_uint(c.w), u, v)) continue;
+      st.best_tri = (int)ti;
+      st.tbest = t;
+      st.bu = u;
+      st.bv = v;
+      st.best_key = key;
+      if (ANY_HIT) return false;
+    }
+  }
+  if (inner) {
+    const int k = __ffs(inner) - 1;
+    inner &= inner - 1;
+    const int s = k ^ r.oct;
+    if (inner) {
+      if (st.sp == kStackSize) {
+        err = 1;
+        return false;
+      }
+      stack[st.sp++] = make_uint2(child_base, (imask << 8) | inner);
+    }
+    st.node = child_base + __popc(imask & ((1u << s) - 1u));
+    return true;
+  }
+  if (st.sp == 0) return false;
+  uint2 g = stack[--st.sp];
+  uint32_t m = g.y & 0xffu;
+  const uint32_t im = g.y >> 8;
+  const int k = __ffs(m) - 1;
+  m &= m - 1;
+  const int s = k ^ r.oct;
+  if (m) stack[st.sp++] = make_uint2(g.x, (im << 8) | m);
+  st.node = g.x + __popc(im & ((1u << s) - 1u));
+  return true;
 }
 
 // ---------------------------------------------------------------------------
@@ -332,68 +351,117 @@ __global__ void k_raygen(const FrameParams* __restrict__ fpp, Queues q) {
   }
 }
 
-// Closest-hit traversal of the ray queue by persistent warps.
-__global__ void __launch_bounds__(128) k_trace_closest(SceneView sc, Queues q, Counters* c, int k) {
-  const int lane = threadIdx.x & 31;
-  const uint32_t count = *((volatile uint32_t*)&c->ray[k & 1]);
-  const uint32_t* pix = q.pix[k & 1];
-  (void)pix;
-  const float4* org = q.org[k & 1];
-  const float4* dir = q.dir[k & 1];
-  int err = 0;
-  uint32_t nn = 0, nt = 0;
-  while (true) {
-    uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(&c->work_trace, 32u);
-    base = __shfl_sync(kFullMask, base, 0);
-    if (base >= count) break;
-    const uint32_t i = base + lane;
-    if (i < count) {
-      const float4 o = org[i], d = dir[i];
-      RayPre r = ray_pre(f3(o.x, o.y, o.z), f3(d.x, d.y, d.z));
-      Hit h = traverse<false>(sc, r, o.w, d.w, &err, nn, nt);
-      q.hit[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
-    }
-  }
-  warp_add64(&c->nodes_closest, nn);
-  warp_add64(&c->tris_closest, nt);
-  if (err) atomicOr(&c->error, 1u);
-}
+// Persistent traversal. Each lane holds one ray; when it finishes, the lane
+// takes the next ray of its warp's batch (32 ray indices fetched with one
+// atomic) at once, so a warp never waits for its slowest ray. MODE 0: closest
+// hit of the pipeline's ray queue; 1: any hit of the shadow queue, resolving
+// the pending NEE term; 2 / 3: closest / any hit of a ray-query batch.
+struct QueryIO {
+  const float4* org;
+  const float4* dir;
+  float4* hits;
+  uint32_t n;
+  uint32_t* work;
+  uint32_t* errflag;
+};
 
-// Any-hit traversal of the shadow queue, then the NEE term is resolved into
-// the path's radiance (lighting.glsl:252-260, 286; ptRaygen.rgen:43-44).
-__global__ void __launch_bounds__(128) k_trace_shadow(SceneView sc, Queues q, Counters* c) {
+template <int MODE>
+__global__ void __launch_bounds__(128, 8) k_traverse(SceneView sc, Queues q, Counters* c, int k, QueryIO io) {
+  constexpr bool ANY = (MODE == 1 || MODE == 3);
   const int lane = threadIdx.x & 31;
-  const uint32_t count = *((volatile uint32_t*)&c->shadow);
+  const unsigned lt_mask = (1u << lane) - 1u;
+  const float4* org;
+  const float4* dir;
+  uint32_t count;
+  uint32_t* work;
+  if (MODE == 0) {
+    count = *((volatile uint32_t*)&c->ray[k & 1]);
+    org = q.org[k & 1];
+    dir = q.dir[k & 1];
+    work = &c->work_trace;
+  } else if (MODE == 1) {
+    count = *((volatile uint32_t*)&c->shadow);
+    org = q.sorg;
+    dir = q.sdir;
+    work = &c->work_shadow;
+  } else {
+    count = io.n;
+    org = io.org;
+    dir = io.dir;
+    work = io.work;
+  }
+  uint2 stack[kStackSize];
+  TravState st;
+  RayPre r;
+  float tmin = 0.f;
+  int idx = -1;
+  uint32_t batch_next = 0, batch_end = 0;  // warp-uniform
+  bool drained = false;                     // warp-uniform: no more batches
   int err = 0;
   uint32_t nn = 0, nt = 0;
   while (true) {
-    uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(&c->work_shadow, 32u);
-    base = __shfl_sync(kFullMask, base, 0);
-    if (base >= count) break;
-    const uint32_t i = base + lane;
-    if (i < count) {
-      const float4 o = q.sorg[i], d = q.sdir[i];
-      RayPre r = ray_pre(f3(o.x, o.y, o.z), f3(d.x, d.y, d.z));
-      Hit h = traverse<true>(sc, r, o.w, d.w, &err, nn, nt);
-      const uint32_t p = q.spix[i];
-      const float4 nee4 = q.snee[i], add4 = q.sadd[i];
-      const float3 nee = h.tri >= 0 ? f3(0.f) : f3(nee4.x, nee4.y, nee4.z);
-      const float3 add = f3(add4.x, add4.y, add4.z);
-      float4 rd = q.rad[p];
-      float3 rad = f3(rd.x, rd.y, rd.z);
-      if (nee4.w == 0.f) {
-        rad = (f3(0.f) + nee) + add;  // finalColor = 0; += NEE; += emissive
-      } else {
-        rad = rad + (nee + add);  // finalColor += NEE + emissive * throughput
+    // ---- refill idle lanes from the warp's batch
+    unsigned need = __ballot_sync(kFullMask, idx < 0);
+    while (need && !drained) {
+      if (batch_next >= batch_end) {
+        uint32_t b = 0;
+        if (lane == 0) b = atomicAdd(work, 32u);
+        b = __shfl_sync(kFullMask, b, 0);
+        if (b >= count) {
+          drained = true;
+          break;
+        }
+        batch_next = b;
+        batch_end = min(b + 32u, count);
       }
-      q.rad[p] = make_float4(rad.x, rad.y, rad.z, rd.w);
+      const uint32_t avail = batch_end - batch_next;
+      const uint32_t rank = __popc(need & lt_mask);
+      if (((need >> lane) & 1u) && rank < avail) {
+        idx = (int)(batch_next + rank);
+        const float4 o = org[idx], d = dir[idx];
+        r = ray_pre(f3(o.x, o.y, o.z), f3(d.x, d.y, d.z));
+        tmin = o.w;
+        st.node = 0;
+        st.sp = 0;
+        st.best_tri = -1;
+        st.tbest = d.w;
+        st.bu = st.bv = 0.f;
+        st.best_key = 0xffffffffu;
+      }
+      batch_next += min((uint32_t)__popc(need), avail);
+      need = __ballot_sync(kFullMask, idx < 0);
     }
+    if (__all_sync(kFullMask, idx < 0)) break;
+    if (idx < 0) continue;
+    // ---- one node of this lane's ray
+    if (visit_node<ANY>(sc, r, tmin, st, stack, err, nn, nt)) continue;
+    // ---- ray finished
+    if (MODE == 0) {
+      q.hit[idx] = make_float4(st.tbest, st.bu, st.bv, __int_as_float(st.best_tri));
+    } else if (MODE == 1) {
+      const uint32_t p = q.spix[idx];
+      const float4 nee4 = q.snee[idx], add4 = q.sadd[idx];
+      const float3 nee = st.best_tri >= 0 ? f3(0.f) : f3(nee4.x, nee4.y, nee4.z);
+      const float3 add = f3(add4.x, add4.y, add4.z);
+      const float4 rd = q.rad[p];
+      float3 rad = f3(rd.x, rd.y, rd.z);
+      if (nee4.w == 0.f) rad = (f3(0.f) + nee) + add;  // finalColor = 0; += NEE; += emissive
+      else rad = rad + (nee + add);                    // finalColor += NEE + emissive * throughput
+      q.rad[p] = make_float4(rad.x, rad.y, rad.z, rd.w);
+    } else {
+      const uint32_t key = st.best_tri >= 0 ? __float_as_uint(sc.tris[3 * st.best_tri].w) : 0xffffffffu;
+      io.hits[idx] = make_float4(st.tbest, st.bu, st.bv, __uint_as_float(key));
+    }
+    idx = -1;
   }
-  warp_add64(&c->nodes_shadow, nn);
-  warp_add64(&c->tris_shadow, nt);
-  if (err) atomicOr(&c->error, 1u);
+  if (MODE == 0) {
+    warp_add64(&c->nodes_closest, nn);
+    warp_add64(&c->tris_closest, nt);
+  } else if (MODE == 1) {
+    warp_add64(&c->nodes_shadow, nn);
+    warp_add64(&c->tris_shadow, nt);
+  }
+  if (err) atomicOr(MODE <= 1 ? &c->error : io.errflag, 1u);
 }
 
 // sampleLight (lighting.glsl:19-227): returns the picked light's strength
@@ -698,31 +766,6 @@ __global__ void k_finalize(const FrameParams* __restrict__ fpp, Queues q, float4
   }
 }
 
-// Standalone ray queries (no reference counterpart; used for traversal tests
-// and throughput measurement): hits[i] = (t, u, v, triangle key bits or -1).
-__global__ void __launch_bounds__(128) k_ray_query(SceneView sc, const float4* __restrict__ org,
-                                                   const float4* __restrict__ dir, float4* __restrict__ hits, uint32_t n,
-                                                   int any_hit, uint32_t* work, uint32_t* errflag) {
-  const int lane = threadIdx.x & 31;
-  int err = 0;
-  uint32_t nn = 0, nt = 0;
-  while (true) {
-    uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(work, 32u);
-    base = __shfl_sync(kFullMask, base, 0);
-    if (base >= n) break;
-    const uint32_t i = base + lane;
-    if (i < n) {
-      const float4 o = org[i], d = dir[i];
-      RayPre r = ray_pre(f3(o.x, o.y, o.z), f3(d.x, d.y, d.z));
-      Hit h = any_hit ? traverse<true>(sc, r, o.w, d.w, &err, nn, nt) : traverse<false>(sc, r, o.w, d.w, &err, nn, nt);
-      const uint32_t key = h.tri >= 0 ? __float_as_uint(sc.tris[3 * h.tri].w) : 0xffffffffu;
-      hits[i] = make_float4(h.t, h.u, h.v, __uint_as_float(key));
-    }
-  }
-  if (err) atomicOr(errflag, 1u);
-}
-
 }  // namespace pbrt
 
 // ===========================================================================
@@ -864,13 +907,13 @@ static int record_frame(PbrtPipeline* pp, cudaStream_t s, StageEvents* ev) {
   for (int k = 0; k < bounces; ++k) {
     k_bounce_begin<<<1, 1, 0, s>>>(pp->ctr, k);
     if (ev) ev->begin(1);
-    k_trace_closest<<<pp->grid_persistent, 128, 0, s>>>(sc, pp->q, pp->ctr, k);
+    k_traverse<0><<<pp->grid_persistent, 128, 0, s>>>(sc, pp->q, pp->ctr, k, QueryIO{});
     if (ev) ev->end(1);
     if (ev) ev->begin(2);
     k_shade<<<pp->grid_persistent, 128, 0, s>>>(sc, pp->dev_fp, pp->q, pp->ctr, g, k);
     if (ev) ev->end(2);
     if (ev) ev->begin(3);
-    k_trace_shadow<<<pp->grid_persistent, 128, 0, s>>>(sc, pp->q, pp->ctr);
+    k_traverse<1><<<pp->grid_persistent, 128, 0, s>>>(sc, pp->q, pp->ctr, k, QueryIO{});
     if (ev) ev->end(3);
     k_bounce_end<<<1, 1, 0, s>>>(pp->ctr);
   }
@@ -1113,9 +1156,10 @@ PBRT_API int pbrt_scene_trace_rays(PbrtScene* s, const void* origins_tmin, const
   int dev = 0, sms = 0;
   PBRT_CUDA(cudaGetDevice(&dev));
   PBRT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  k_ray_query<<<sms * 16, 128, 0, stream>>>(s->view, (const float4*)origins_tmin, (const float4*)directions_tmax,
-                                            (float4*)hits_out, n, any_hit, work, work + 1);
-  return check_launch("k_ray_query");
+  QueryIO io{(const float4*)origins_tmin, (const float4*)directions_tmax, (float4*)hits_out, n, work, work + 1};
+  if (any_hit) k_traverse<3><<<sms * 8, 128, 0, stream>>>(s->view, Queues{}, nullptr, 0, io);
+  else k_traverse<2><<<sms * 8, 128, 0, stream>>>(s->view, Queues{}, nullptr, 0, io);
+  return check_launch("k_traverse (ray query)");
 }
 
 PBRT_API int pbrt_pipeline_create(PbrtScene* scene, PbrtGBuffer* g, PbrtIlluminationBuffer* illumination,
@@ -1176,7 +1220,7 @@ PBRT_API int pbrt_pipeline_create(PbrtScene* scene, PbrtGBuffer* g, PbrtIllumina
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    pp->grid_persistent = sms * 12;
+    pp->grid_persistent = sms * 8;  // 8 resident 128-thread CTAs per SM at <= 64 registers
   }
   if (st) {
     delete pp;
