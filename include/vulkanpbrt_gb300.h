@@ -364,6 +364,72 @@ PBRT_API int pbrt_pipeline_debug_images(const PbrtPipeline* p, PbrtImage* primar
 PBRT_API int pbrt_synth_texture(uint64_t seed, uint32_t size, int32_t kind, const float* color, int32_t alpha_mask,
                                 float rough_lo, float rough_hi, uint8_t* out_rgba);
 
+/* ---- kernel-predicting denoiser operators (no reference counterpart) ----
+ * Device pointers, NHWC layout, channel counts multiples of 16 for the
+ * convolutions. BF16 activations and weights, FP32 accumulation, FP32
+ * gradients and master weights. The network that strings them together is
+ * vulkanpbrt_gb300/kpunet.py. */
+/* y = relu?(conv3x3(concat(x1, upsample2(x2))) + bias), zero padding.
+ * w [cout][9][c1+c2] BF16 (tap = ky*3+kx); x2 may be null (c2 = 0).
+ * flags bit 0: ReLU; bit 1: add into y32 instead of storing. y (BF16) and
+ * y32 (FP32) are both optional, at least one is given. */
+PBRT_API int pbrt_nn_conv3x3(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* w, const float* bias,
+                             void* y, float* y32, int32_t n, int32_t h, int32_t w_px, int32_t cout, int32_t flags,
+                             pbrt_stream_t stream);
+/* dw [cout][9][c1+c2] FP32 += sum over pixels of dy (BF16) x im2col(input). */
+PBRT_API int pbrt_nn_conv3x3_wgrad(const void* dy, const void* x1, int32_t c1, const void* x2, int32_t c2, float* dw,
+                                   int32_t n, int32_t h, int32_t w_px, int32_t cout, pbrt_stream_t stream);
+/* [cout][9][cin] -> [cin][9][cout], taps reversed (backward-data weights). */
+PBRT_API int pbrt_nn_flip_weights(const void* w, void* wt, int32_t cout, int32_t cin, pbrt_stream_t stream);
+/* Network input: 16 BF16 channels per padded pixel (log1p radiance, albedo,
+ * normal, log1p depth / 8, zeros; edges replicated) and the noisy radiance
+ * (FP32 rgb) from an illumination image (RGBA32F, or RGBA16F when
+ * illum_is_half) and the G-buffer's albedo (RGBA8), normal (RG32F angles) and
+ * depth (R32F) images, n_img images of w x h each, packed. */
+PBRT_API int pbrt_nn_features(const void* illum, int32_t illum_is_half, const void* albedo, const void* normal,
+                              const void* depth, int32_t w, int32_t h, int32_t pw, int32_t ph, int32_t n_img,
+                              void* feat, float* rad, pbrt_stream_t stream);
+/* 2x2 average pooling (BF16 when is_f32 = 0, else FP32) and its backward (adds). */
+PBRT_API int pbrt_nn_avgpool2(const void* x, void* y, int32_t is_f32, int32_t n, int32_t h, int32_t w, int32_t c,
+                              pbrt_stream_t stream);
+PBRT_API int pbrt_nn_avgpool2_bwd_add(const float* dy, float* dx, int32_t n, int32_t h, int32_t w, int32_t c,
+                                      pbrt_stream_t stream);
+/* out = BF16(dy * (y > 0)); db (optional) += per-channel sums of out. */
+PBRT_API int pbrt_nn_relu_bwd(const float* dy, const void* y, void* out, float* db, int64_t pixels, int32_t c,
+                              pbrt_stream_t stream);
+/* Backward of concat(x1, upsample2(x2)): dx1 += dcat[:c1], dx2 += 2x2 sums of dcat[c1:]. */
+PBRT_API int pbrt_nn_split_upsum(const float* dcat, int32_t c1, int32_t c2, int32_t n, int32_t h, int32_t w,
+                                 float* dx1, float* dx2, pbrt_stream_t stream);
+/* Kernel-prediction head: logits = Wh . F + bh (k = 25, 26 or 27 outputs);
+ * softmax 5x5 kernel over R; with coarse, alpha = sigmoid(logit 25) blends
+ * the upsampled coarse result in; the last logit (k = 26 without coarse,
+ * 27 with) is the predicted log squared error written to var. */
+PBRT_API int pbrt_nn_kp_head(const void* F, const float* Wh, const float* bh, const float* R, const float* coarse,
+                             float* out, float* kw, float* filt, float* alpha, float* var, int32_t n, int32_t h,
+                             int32_t w, int32_t c, int32_t k, pbrt_stream_t stream);
+PBRT_API int pbrt_nn_kp_head_bwd(const void* F, const float* Wh, const float* bh, const float* R, const float* coarse,
+                                 float* kw, float* filt, float* alpha, int32_t n, int32_t h, int32_t w, int32_t c,
+                                 int32_t k, const float* dout, const float* dvar, float* dF, float* dWh, float* dbh,
+                                 float* dcoarse, pbrt_stream_t stream);
+/* relMSE of albedo x out against albedo x target over the unpadded w x h
+ * pixels, its gradient, and the variance head's regression on the
+ * per-pixel error; loss[0] += relMSE, loss[1] += variance loss. */
+PBRT_API int pbrt_nn_relmse_loss(const float* out, const float* target, const void* albedo, const float* var,
+                                 int32_t n, int32_t ph, int32_t pw, int32_t h, int32_t w, float var_weight, float* dout,
+                                 float* dvar, float* loss, pbrt_stream_t stream);
+/* Adam step on FP32 master weights (bias-corrected for step >= 1); refreshes
+ * the BF16 copy when w_bf16 is given. */
+PBRT_API int pbrt_nn_adam(float* w, const float* g, float* m, float* v, void* w_bf16, int64_t n, float lr, float b1,
+                          float b2, float eps, int32_t step, float grad_scale, pbrt_stream_t stream);
+/* Final image of the neural path, tone-mapped as BMFR's final image; with var
+ * and fallback_bgra, every tile x tile block whose mean predicted squared
+ * error exceeds threshold takes the fallback image (BMFR's final image) and
+ * is counted in fallback_tiles. */
+PBRT_API int pbrt_nn_compose(const float* out, int32_t pw, int32_t ph, int32_t w, int32_t h, const void* albedo,
+                             const float* var, float threshold, int32_t tile, const void* fallback_bgra,
+                             void* final_bgra, float* denoised_rgba32f, uint32_t* fallback_tiles,
+                             pbrt_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

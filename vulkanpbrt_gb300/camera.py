@@ -73,3 +73,24 @@ def orbit_camera(width: int, height: int, frame: int, frames: int, radius=12.0, 
 def col_major(m: np.ndarray) -> np.ndarray:
     """float32 [16] column-major (GLSL / vsg::mat4 memory order)."""
     return np.ascontiguousarray(np.asarray(m, dtype=np.float32).T).reshape(16)
+
+
+class CropCamera:
+    """The pixels [x0, x0 + w) x [y0, y0 + h) of a full_w x full_h frame of
+    `cam`, as a camera of its own: the inverse projection maps the crop's
+    NDC onto that window of the full frame's NDC, so a w x h render of it
+    matches the same pixels of the full render (same rays, same pixel
+    footprint)."""
+
+    def __init__(self, cam: Camera, full_w: int, full_h: int, x0: int, y0: int, w: int, h: int):
+        s = np.eye(4)
+        s[0, 0] = w / full_w
+        s[1, 1] = h / full_h
+        s[0, 3] = (2.0 * x0 + w) / full_w - 1.0
+        s[1, 3] = (2.0 * y0 + h) / full_h - 1.0
+        self.view64 = cam.view64
+        self.proj64 = np.linalg.inv(s) @ cam.proj64
+        self.view = cam.view
+        self.inv_view = cam.inv_view
+        self.proj = self.proj64.astype(np.float32)
+        self.inv_proj = (np.linalg.inv(cam.proj64) @ s).astype(np.float32)

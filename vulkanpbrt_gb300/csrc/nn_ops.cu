@@ -1,0 +1,501 @@
+// Non-convolution operators of the kernel-predicting denoiser (FP32 on the
+// CUDA cores): input features from the G-buffer, 2x2 pooling, the backward
+// helpers of the U-Net (ReLU mask, bias gradient, concat split and upsample
+// sum), the multi-scale kernel-prediction heads, the relMSE loss and Adam.
+// No reference counterpart: the reference's denoisers are BMFR and BFR.
+#include <cuda_bf16.h>
+
+#include <cstdint>
+
+#include "device_common.cuh"
+#include "internal.hpp"
+
+namespace pbrt {
+namespace nn {
+
+typedef __nv_bfloat16 bf16;
+constexpr int kKP = 25;  // 5x5 kernel taps
+
+#define GRID_STRIDE(i, n) for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < (n); i += (long)gridDim.x * blockDim.x)
+
+// Network input (16 BF16 channels at the padded size PH x PW; edge pixels
+// replicated): log1p(illumination rgb), albedo rgb, normal xyz (decoded from
+// the G-buffer's spherical angles), log1p(depth) / 8, zeros. Also the
+// noisy illumination itself (FP32 rgb) for the kernel-prediction heads.
+__global__ void features_kernel(const float4* __restrict__ illum32, const Half4* __restrict__ illum16,
+                                const uchar4* __restrict__ albedo, const float2* __restrict__ normal,
+                                const float* __restrict__ depth, int W, int H, int PW, int PH, int n_img,
+                                bf16* __restrict__ feat, float* __restrict__ rad) {
+  const long total = (long)n_img * PH * PW;
+  GRID_STRIDE(i, total) {
+    const int x = (int)(i % PW), y = (int)((i / PW) % PH), n = (int)(i / ((long)PW * PH));
+    const int sx = min(x, W - 1), sy = min(y, H - 1);
+    const size_t p = ((size_t)n * H + sy) * W + sx;
+    float4 c = illum32 ? illum32[p] : load_half4(illum16 + p);
+    c.x = fmaxf(c.x, 0.f);
+    c.y = fmaxf(c.y, 0.f);
+    c.z = fmaxf(c.z, 0.f);
+    const uchar4 a = albedo[p];
+    const float2 th = normal[p];
+    const float3 nn3 = decode_normal(th.x, th.y);
+    float f[16] = {log1pf(c.x), log1pf(c.y), log1pf(c.z), a.x / 255.f, a.y / 255.f, a.z / 255.f, nn3.x, nn3.y,
+                   nn3.z, log1pf(fmaxf(depth[p], 0.f)) * 0.125f, 0, 0, 0, 0, 0, 0};
+    bf16* o = feat + i * 16;
+#pragma unroll
+    for (int k = 0; k < 16; k += 2) *reinterpret_cast<__nv_bfloat162*>(o + k) = __floats2bfloat162_rn(f[k], f[k + 1]);
+    rad[i * 3 + 0] = c.x;
+    rad[i * 3 + 1] = c.y;
+    rad[i * 3 + 2] = c.z;
+  }
+}
+
+__global__ void avgpool2_bf16_kernel(const bf16* __restrict__ src, bf16* __restrict__ dst, int n_img, int H, int W,
+                                     int C) {
+  const int H2 = H / 2, W2 = W / 2;
+  const long total = (long)n_img * H2 * W2 * (C / 2);
+  GRID_STRIDE(i, total) {
+    const int c = (int)(i % (C / 2)) * 2;
+    const long q = i / (C / 2);
+    const int x = (int)(q % W2), yy = (int)((q / W2) % H2), n = (int)(q / ((long)W2 * H2));
+    float2 s = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int d = 0; d < 4; ++d) {
+      const size_t p = (((size_t)n * H + 2 * yy + (d >> 1)) * W + 2 * x + (d & 1)) * C + c;
+      float2 v = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(src + p));
+      s.x += v.x;
+      s.y += v.y;
+    }
+    *reinterpret_cast<__nv_bfloat162*>(dst + q * C + c) = __floats2bfloat162_rn(0.25f * s.x, 0.25f * s.y);
+  }
+}
+
+__global__ void avgpool2_f32_kernel(const float* __restrict__ src, float* __restrict__ dst, int n_img, int H, int W,
+                                    int C) {
+  const int H2 = H / 2, W2 = W / 2;
+  const long total = (long)n_img * H2 * W2 * C;
+  GRID_STRIDE(i, total) {
+    const int c = (int)(i % C);
+    const long q = i / C;
+    const int x = (int)(q % W2), yy = (int)((q / W2) % H2), n = (int)(q / ((long)W2 * H2));
+    float s = 0.f;
+#pragma unroll
+    for (int d = 0; d < 4; ++d) s += src[(((size_t)n * H + 2 * yy + (d >> 1)) * W + 2 * x + (d & 1)) * C + c];
+    dst[i] = 0.25f * s;
+  }
+}
+
+// dx[2i+a][2j+b] += dy[i][j] / 4   (FP32)
+__global__ void avgpool2_bwd_add_kernel(const float* __restrict__ dy, float* __restrict__ dx, int n_img, int H, int W,
+                                        int C) {
+  const long total = (long)n_img * H * W * C;
+  GRID_STRIDE(i, total) {
+    const int c = (int)(i % C);
+    const long p = i / C;
+    const int x = (int)(p % W), y = (int)((p / W) % H), n = (int)(p / ((long)W * H));
+    dx[i] += 0.25f * dy[(((size_t)n * (H / 2) + y / 2) * (W / 2) + x / 2) * C + c];
+  }
+}
+
+// out = bf16(dy * (y > 0)) and db[c] += sum of it (block partials, one
+// atomic per channel per block).
+__global__ void relu_bwd_kernel(const float* __restrict__ dy, const bf16* __restrict__ y, bf16* __restrict__ out,
+                                float* __restrict__ db, long P, int C) {
+  extern __shared__ float sdb[];
+  for (int c = threadIdx.x; c < C; c += blockDim.x) sdb[c] = 0.f;
+  __syncthreads();
+  const long total = P * C;
+  GRID_STRIDE(i, total) {
+    const int c = (int)(i % C);
+    float g = __bfloat162float(y[i]) > 0.f ? dy[i] : 0.f;
+    bf16 gb = __float2bfloat16_rn(g);
+    out[i] = gb;
+    if (db) atomicAdd(&sdb[c], __bfloat162float(gb));
+  }
+  __syncthreads();
+  if (db)
+    for (int c = threadIdx.x; c < C; c += blockDim.x) atomicAdd(&db[c], sdb[c]);
+}
+
+// Backward of "concat(x1, upsample2(x2))": dx1 += dcat[:, :c1];
+// dx2 += sum over each 2x2 of dcat[:, c1:].
+__global__ void split_upsum_kernel(const float* __restrict__ dcat, int c1, int c2, int n_img, int H, int W,
+                                   float* __restrict__ dx1, float* __restrict__ dx2) {
+  const int C = c1 + c2, H2 = H / 2, W2 = W / 2;
+  const long t1 = (long)n_img * H * W * c1;
+  GRID_STRIDE(i, t1) {
+    const int c = (int)(i % c1);
+    const long p = i / c1;
+    dx1[i] += dcat[p * C + c];
+  }
+  const long t2 = (long)n_img * H2 * W2 * c2;
+  GRID_STRIDE(i, t2) {
+    const int c = (int)(i % c2);
+    const long q = i / c2;
+    const int x = (int)(q % W2), y = (int)((q / W2) % H2), n = (int)(q / ((long)W2 * H2));
+    float s = 0.f;
+#pragma unroll
+    for (int d = 0; d < 4; ++d) s += dcat[((((size_t)n * H + 2 * y + (d >> 1)) * W + 2 * x + (d & 1))) * C + c1 + c];
+    dx2[i] += s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Kernel-prediction head at one scale. Per pixel: logits = Wh . F + bh;
+// 5x5 kernel = softmax(logits[0:25]) applied to the scale's noisy
+// illumination (edge-clamped); with a coarser result, alpha =
+// sigmoid(logits[25]) blends it in (o = (1 - a) f + a up(o_coarse)); at
+// scale 0 logits[26] is the predicted log squared error (variance gate).
+struct HeadArgs {
+  const bf16* F;       // [N][H][W][C]
+  const float* Wh;     // [K][C]
+  const float* bh;     // [K]
+  const float* R;      // [N][H][W][3]
+  const float* coarse; // [N][H/2][W/2][3] or null
+  float* out;          // [N][H][W][3]
+  float* kw;           // [N][H][W][25] softmax weights, saved for backward (optional)
+  float* filt;         // [N][H][W][3] filtered, before the blend (optional)
+  float* alpha;        // [N][H][W] blend weight (optional)
+  float* var;          // [N][H][W] or null (log squared-error prediction)
+  int N, H, W, C, K;
+};
+
+__global__ void kp_head_fwd_kernel(HeadArgs a) {
+  extern __shared__ float sW[];  // [K][C]
+  for (int i = threadIdx.x; i < a.K * a.C; i += blockDim.x) sW[i] = a.Wh[i];
+  __syncthreads();
+  const long P = (long)a.N * a.H * a.W;
+  GRID_STRIDE(p, P) {
+    const int x = (int)(p % a.W), y = (int)((p / a.W) % a.H), n = (int)(p / ((long)a.W * a.H));
+    float lg[27];
+    for (int k = 0; k < a.K; ++k) lg[k] = a.bh[k];
+    const bf16* f = a.F + p * a.C;
+    for (int c = 0; c < a.C; c += 2) {
+      float2 v = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(f + c));
+      for (int k = 0; k < a.K; ++k) lg[k] += sW[k * a.C + c] * v.x + sW[k * a.C + c + 1] * v.y;
+    }
+    float mx = lg[0];
+    for (int k = 1; k < kKP; ++k) mx = fmaxf(mx, lg[k]);
+    float s = 0.f;
+    for (int k = 0; k < kKP; ++k) {
+      lg[k] = __expf(lg[k] - mx);
+      s += lg[k];
+    }
+    const float inv = 1.f / s;
+    float3 acc = f3(0.f);
+    for (int k = 0; k < kKP; ++k) {
+      const float w = lg[k] * inv;
+      if (a.kw) a.kw[p * kKP + k] = w;
+      const int sx = min(max(x + k % 5 - 2, 0), a.W - 1), sy = min(max(y + k / 5 - 2, 0), a.H - 1);
+      const float* r = a.R + (((size_t)n * a.H + sy) * a.W + sx) * 3;
+      acc = acc + w * f3(r[0], r[1], r[2]);
+    }
+    if (a.filt) {
+      a.filt[p * 3 + 0] = acc.x;
+      a.filt[p * 3 + 1] = acc.y;
+      a.filt[p * 3 + 2] = acc.z;
+    }
+    float3 o = acc;
+    if (a.coarse) {
+      const float al = 1.f / (1.f + __expf(-lg[kKP]));
+      if (a.alpha) a.alpha[p] = al;
+      const float* cc = a.coarse + (((size_t)n * (a.H / 2) + y / 2) * (a.W / 2) + x / 2) * 3;
+      o = (1.f - al) * acc + al * f3(cc[0], cc[1], cc[2]);
+    }
+    if (a.var) a.var[p] = lg[a.coarse ? kKP + 1 : kKP];
+    a.out[p * 3 + 0] = o.x;
+    a.out[p * 3 + 1] = o.y;
+    a.out[p * 3 + 2] = o.z;
+  }
+}
+
+struct HeadBwdArgs {
+  HeadArgs f;
+  const float* dout;   // [N][H][W][3]
+  const float* dvar;   // [N][H][W] or null
+  float* dF;           // [N][H][W][C] accumulated
+  float* dWh;          // [K][C] accumulated
+  float* dbh;          // [K] accumulated
+  float* dcoarse;      // [N][H/2][W/2][3] accumulated, or null
+};
+
+__global__ void kp_head_bwd_kernel(HeadBwdArgs b) {
+  extern __shared__ float sm[];
+  const HeadArgs& a = b.f;
+  float* sW = sm;                  // [K][C]
+  float* sdW = sm + a.K * a.C;     // [K][C]
+  float* sdb = sdW + a.K * a.C;    // [K]
+  for (int i = threadIdx.x; i < a.K * a.C; i += blockDim.x) {
+    sW[i] = a.Wh[i];
+    sdW[i] = 0.f;
+  }
+  for (int i = threadIdx.x; i < a.K; i += blockDim.x) sdb[i] = 0.f;
+  __syncthreads();
+  const long P = (long)a.N * a.H * a.W;
+  GRID_STRIDE(p, P) {
+    const int x = (int)(p % a.W), y = (int)((p / a.W) % a.H), n = (int)(p / ((long)a.W * a.H));
+    float3 dout = f3(b.dout[p * 3], b.dout[p * 3 + 1], b.dout[p * 3 + 2]);
+    float dl[27];
+    for (int k = 0; k < a.K; ++k) dl[k] = 0.f;
+    float3 df = dout;
+    if (a.coarse) {
+      const float al = a.alpha[p];
+      const float* cc = a.coarse + (((size_t)n * (a.H / 2) + y / 2) * (a.W / 2) + x / 2) * 3;
+      const float3 fl = f3(a.filt[p * 3], a.filt[p * 3 + 1], a.filt[p * 3 + 2]);
+      const float da = dot(dout, f3(cc[0], cc[1], cc[2]) - fl);
+      dl[kKP] = da * al * (1.f - al);
+      df = (1.f - al) * dout;
+      if (b.dcoarse) {
+        float* dc = b.dcoarse + (((size_t)n * (a.H / 2) + y / 2) * (a.W / 2) + x / 2) * 3;
+        atomicAdd(dc + 0, al * dout.x);
+        atomicAdd(dc + 1, al * dout.y);
+        atomicAdd(dc + 2, al * dout.z);
+      }
+    }
+    if (b.dvar) dl[a.coarse ? kKP + 1 : kKP] = b.dvar[p];
+    // softmax backward
+    float dw[kKP], sum = 0.f;
+    for (int k = 0; k < kKP; ++k) {
+      const int sx = min(max(x + k % 5 - 2, 0), a.W - 1), sy = min(max(y + k / 5 - 2, 0), a.H - 1);
+      const float* r = a.R + (((size_t)n * a.H + sy) * a.W + sx) * 3;
+      dw[k] = dot(df, f3(r[0], r[1], r[2]));
+      sum += a.kw[p * kKP + k] * dw[k];
+    }
+    for (int k = 0; k < kKP; ++k) dl[k] = a.kw[p * kKP + k] * (dw[k] - sum);
+    const bf16* f = a.F + p * a.C;
+    float* dF = b.dF + p * a.C;
+    for (int c = 0; c < a.C; c += 2) {
+      float2 v = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(f + c));
+      float g0 = 0.f, g1 = 0.f;
+      for (int k = 0; k < a.K; ++k) {
+        g0 += sW[k * a.C + c] * dl[k];
+        g1 += sW[k * a.C + c + 1] * dl[k];
+        atomicAdd(&sdW[k * a.C + c], dl[k] * v.x);
+        atomicAdd(&sdW[k * a.C + c + 1], dl[k] * v.y);
+      }
+      dF[c] += g0;
+      dF[c + 1] += g1;
+    }
+    for (int k = 0; k < a.K; ++k) atomicAdd(&sdb[k], dl[k]);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < a.K * a.C; i += blockDim.x) atomicAdd(&b.dWh[i], sdW[i]);
+  for (int i = threadIdx.x; i < a.K; i += blockDim.x) atomicAdd(&b.dbh[i], sdb[i]);
+}
+
+// relMSE of the remodulated output against the remodulated target:
+// mean over valid pixels and channels of (A o - A t)^2 / ((A t)^2 + 0.01);
+// dout = dL/do. The predicted log squared error v (if given) is regressed on
+// log(e + 1e-4) of the pixel's error e with weight var_w. loss[0] += L,
+// loss[1] += variance loss.
+__global__ void relmse_loss_kernel(const float* __restrict__ out, const float* __restrict__ target,
+                                   const uchar4* __restrict__ albedo, const float* __restrict__ var, int N, int PH,
+                                   int PW, int H, int W, float var_w, float* __restrict__ dout,
+                                   float* __restrict__ dvar, float* __restrict__ loss) {
+  __shared__ float s_l[2];
+  if (threadIdx.x < 2) s_l[threadIdx.x] = 0.f;
+  __syncthreads();
+  const long P = (long)N * PH * PW;
+  const float norm = 1.f / (3.f * (float)N * H * W);
+  const float vnorm = 1.f / ((float)N * H * W);
+  GRID_STRIDE(p, P) {
+    const int x = (int)(p % PW), y = (int)((p / PW) % PH), n = (int)(p / ((long)PW * PH));
+    if (x >= W || y >= H) {
+      dout[p * 3] = dout[p * 3 + 1] = dout[p * 3 + 2] = 0.f;
+      if (dvar) dvar[p] = 0.f;
+      continue;
+    }
+    const uchar4 a4 = albedo[((size_t)n * H + y) * W + x];
+    const float A[3] = {a4.x / 255.f, a4.y / 255.f, a4.z / 255.f};
+    const float* t = target + (((size_t)n * H + y) * W + x) * 3;
+    float l = 0.f;
+    for (int c = 0; c < 3; ++c) {
+      const float r = A[c] * t[c], xo = A[c] * out[p * 3 + c];
+      const float den = r * r + 0.01f;
+      const float d = xo - r;
+      l += d * d / den;
+      dout[p * 3 + c] = norm * 2.f * d / den * A[c];
+    }
+    atomicAdd(&s_l[0], l * norm);
+    if (var) {
+      const float tgt = logf(l / 3.f + 1e-4f);
+      const float dv = var[p] - tgt;
+      dvar[p] = var_w * 2.f * dv * vnorm;
+      atomicAdd(&s_l[1], dv * dv * vnorm);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 2) atomicAdd(&loss[threadIdx.x], s_l[threadIdx.x]);
+}
+
+// Adam on FP32 master weights; writes the BF16 copy the convolutions read.
+__global__ void adam_kernel(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                            float* __restrict__ v, bf16* __restrict__ w16, long n, float lr, float b1, float b2,
+                            float eps, float c1, float c2, float grad_scale) {
+  GRID_STRIDE(i, n) {
+    const float gi = g[i] * grad_scale;
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    w[i] = wi;
+    if (w16) w16[i] = __float2bfloat16_rn(wi);
+  }
+}
+
+// Final image of the neural path: denoised illumination remodulated by the
+// albedo and tone mapped as bmfrPost does (shaders/bmfrPost.comp:211-214);
+// with a variance gate, tiles whose mean predicted error exceeds the
+// threshold take the fallback (BMFR) result instead.
+__global__ void compose_kernel(const float* __restrict__ out, int PW, int PH, int W, int H,
+                               const uchar4* __restrict__ albedo, const float* __restrict__ var, float threshold,
+                               int tile, const uchar4* __restrict__ fallback, uchar4* __restrict__ final_bgra,
+                               float4* __restrict__ denoised, uint32_t* __restrict__ fallback_tiles) {
+  const long P = (long)W * H;
+  GRID_STRIDE(i, P) {
+    const int x = (int)(i % W), y = (int)(i / W);
+    bool use_fallback = false;
+    if (var && fallback) {
+      // mean predicted log-error over the pixel's tile (recomputed per pixel; tiles are small)
+      const int tx0 = (x / tile) * tile, ty0 = (y / tile) * tile;
+      float s = 0.f;
+      int cnt = 0;
+      for (int yy = ty0; yy < min(ty0 + tile, H); yy += 4)
+        for (int xx = tx0; xx < min(tx0 + tile, W); xx += 4) {
+          s += __expf(var[(size_t)yy * PW + xx]);
+          ++cnt;
+        }
+      use_fallback = s / (float)cnt > threshold;
+      if (use_fallback && x == tx0 && y == ty0) atomicAdd(fallback_tiles, 1u);
+    }
+    if (use_fallback) {
+      final_bgra[i] = fallback[i];
+      continue;
+    }
+    const size_t p = (size_t)y * PW + x;
+    const float3 o = f3(out[p * 3], out[p * 3 + 1], out[p * 3 + 2]);
+    if (denoised) denoised[i] = make_float4(o.x, o.y, o.z, 1.f);
+    const uchar4 a = albedo[i];
+    float3 t = fmax3(f3(0.f), f3(a.x / 255.f + 1e-6f, a.y / 255.f + 1e-6f, a.z / 255.f + 1e-6f) * o);
+    t = clamp3(f3(powf(t.x, .454545f), powf(t.y, .454545f), powf(t.z, .454545f)), 0.f, 1.f);
+    final_bgra[i] = make_uchar4(f2u8(t.z), f2u8(t.y), f2u8(t.x), 255);
+  }
+}
+
+}  // namespace nn
+}  // namespace pbrt
+
+using namespace pbrt;
+using namespace pbrt::nn;
+
+namespace {
+inline int grid_for(long n, int block = 256) { return (int)std::min<long>((n + block - 1) / block, 152L * 16); }
+}  // namespace
+
+extern "C" {
+
+PBRT_API int pbrt_nn_features(const void* illum, int32_t illum_is_half, const void* albedo, const void* normal,
+                              const void* depth, int32_t w, int32_t h, int32_t pw, int32_t ph, int32_t n_img,
+                              void* feat, float* rad, pbrt_stream_t s) {
+  if (!illum || !albedo || !normal || !depth || !feat || !rad || pw < w || ph < h || w <= 0 || h <= 0 || n_img <= 0)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "nn features: bad arguments");
+  const long total = (long)n_img * ph * pw;
+  features_kernel<<<grid_for(total), 256, 0, s>>>(illum_is_half ? nullptr : (const float4*)illum,
+                                                  illum_is_half ? (const Half4*)illum : nullptr, (const uchar4*)albedo,
+                                                  (const float2*)normal, (const float*)depth, w, h, pw, ph, n_img,
+                                                  (bf16*)feat, rad);
+  return check_launch("features_kernel");
+}
+
+PBRT_API int pbrt_nn_avgpool2(const void* x, void* y, int32_t is_f32, int32_t n, int32_t h, int32_t w, int32_t c,
+                              pbrt_stream_t s) {
+  if (!x || !y || h % 2 || w % 2 || c <= 0 || (!is_f32 && c % 2)) return fail(PBRT_ERROR_INVALID_ARGUMENT, "avgpool2");
+  const long total = (long)n * (h / 2) * (w / 2) * c;
+  if (is_f32) avgpool2_f32_kernel<<<grid_for(total), 256, 0, s>>>((const float*)x, (float*)y, n, h, w, c);
+  else avgpool2_bf16_kernel<<<grid_for(total / 2), 256, 0, s>>>((const bf16*)x, (bf16*)y, n, h, w, c);
+  return check_launch("avgpool2");
+}
+
+PBRT_API int pbrt_nn_avgpool2_bwd_add(const float* dy, float* dx, int32_t n, int32_t h, int32_t w, int32_t c,
+                                      pbrt_stream_t s) {
+  if (!dy || !dx || h % 2 || w % 2) return fail(PBRT_ERROR_INVALID_ARGUMENT, "avgpool2 bwd");
+  avgpool2_bwd_add_kernel<<<grid_for((long)n * h * w * c), 256, 0, s>>>(dy, dx, n, h, w, c);
+  return check_launch("avgpool2_bwd_add");
+}
+
+PBRT_API int pbrt_nn_relu_bwd(const float* dy, const void* y, void* out, float* db, int64_t pixels, int32_t c,
+                              pbrt_stream_t s) {
+  if (!dy || !y || !out || c <= 0) return fail(PBRT_ERROR_INVALID_ARGUMENT, "relu bwd");
+  relu_bwd_kernel<<<grid_for(pixels * c), 256, c * sizeof(float), s>>>(dy, (const bf16*)y, (bf16*)out, db, pixels, c);
+  return check_launch("relu_bwd");
+}
+
+PBRT_API int pbrt_nn_split_upsum(const float* dcat, int32_t c1, int32_t c2, int32_t n, int32_t h, int32_t w,
+                                 float* dx1, float* dx2, pbrt_stream_t s) {
+  if (!dcat || !dx1 || !dx2 || h % 2 || w % 2) return fail(PBRT_ERROR_INVALID_ARGUMENT, "split upsum");
+  split_upsum_kernel<<<grid_for((long)n * h * w * c1), 256, 0, s>>>(dcat, c1, c2, n, h, w, dx1, dx2);
+  return check_launch("split_upsum");
+}
+
+PBRT_API int pbrt_nn_kp_head(const void* F, const float* Wh, const float* bh, const float* R, const float* coarse,
+                             float* out, float* kw, float* filt, float* alpha, float* var, int32_t n, int32_t h,
+                             int32_t w, int32_t c, int32_t k, pbrt_stream_t s) {
+  if (!F || !Wh || !bh || !R || !out || k < kKP || k > 27 || c % 2 || (size_t)k * c * sizeof(float) > 48 * 1024 ||
+      (var && k <= (coarse ? kKP + 1 : kKP)) || (coarse && k < kKP + 1))
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "kp head: bad arguments");
+  HeadArgs a{(const bf16*)F, Wh, bh, R, coarse, out, kw, filt, alpha, var, n, h, w, c, k};
+  kp_head_fwd_kernel<<<grid_for((long)n * h * w, 128), 128, k * c * sizeof(float), s>>>(a);
+  return check_launch("kp_head_fwd");
+}
+
+PBRT_API int pbrt_nn_kp_head_bwd(const void* F, const float* Wh, const float* bh, const float* R, const float* coarse,
+                                 float* kw, float* filt, float* alpha, int32_t n, int32_t h, int32_t w, int32_t c,
+                                 int32_t k, const float* dout, const float* dvar, float* dF, float* dWh, float* dbh,
+                                 float* dcoarse, pbrt_stream_t s) {
+  if (!F || !Wh || !R || !kw || !filt || (coarse && !alpha) || !dout || !dF || !dWh || !dbh || k < kKP || k > 27 ||
+      c % 2 || (2 * (size_t)k * c + k) * sizeof(float) > 48 * 1024 || (dvar && k <= (coarse ? kKP + 1 : kKP)) ||
+      (coarse && k < kKP + 1))
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "kp head bwd: bad arguments");
+  HeadBwdArgs b;
+  b.f = HeadArgs{(const bf16*)F, Wh, bh, R, coarse, nullptr, kw, filt, alpha, nullptr, n, h, w, c, k};
+  b.dout = dout;
+  b.dvar = dvar;
+  b.dF = dF;
+  b.dWh = dWh;
+  b.dbh = dbh;
+  b.dcoarse = dcoarse;
+  const size_t smem = (2 * (size_t)k * c + k) * sizeof(float);
+  kp_head_bwd_kernel<<<grid_for((long)n * h * w, 128), 128, smem, s>>>(b);
+  return check_launch("kp_head_bwd");
+}
+
+PBRT_API int pbrt_nn_relmse_loss(const float* out, const float* target, const void* albedo, const float* var,
+                                 int32_t n, int32_t ph, int32_t pw, int32_t h, int32_t w, float var_weight, float* dout,
+                                 float* dvar, float* loss, pbrt_stream_t s) {
+  if (!out || !target || !albedo || !dout || !loss || (var && !dvar))
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "relmse loss: bad arguments");
+  relmse_loss_kernel<<<grid_for((long)n * ph * pw), 256, 0, s>>>(out, target, (const uchar4*)albedo, var, n, ph, pw,
+                                                                h, w, var_weight, dout, dvar, loss);
+  return check_launch("relmse_loss");
+}
+
+PBRT_API int pbrt_nn_adam(float* w, const float* g, float* m, float* v, void* w_bf16, int64_t n, float lr, float b1,
+                          float b2, float eps, int32_t step, float grad_scale, pbrt_stream_t s) {
+  if (!w || !g || !m || !v || n <= 0 || step < 1) return fail(PBRT_ERROR_INVALID_ARGUMENT, "adam: bad arguments");
+  const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+  adam_kernel<<<grid_for(n), 256, 0, s>>>(w, g, m, v, (bf16*)w_bf16, n, lr, b1, b2, eps, c1, c2, grad_scale);
+  return check_launch("adam");
+}
+
+PBRT_API int pbrt_nn_compose(const float* out, int32_t pw, int32_t ph, int32_t w, int32_t h, const void* albedo,
+                             const float* var, float threshold, int32_t tile, const void* fallback_bgra,
+                             void* final_bgra, float* denoised_rgba32f, uint32_t* fallback_tiles, pbrt_stream_t s) {
+  if (!out || !albedo || !final_bgra || (var && fallback_bgra && (!fallback_tiles || tile <= 0)))
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "compose: bad arguments");
+  compose_kernel<<<grid_for((long)w * h), 256, 0, s>>>(out, pw, ph, w, h, (const uchar4*)albedo, var, threshold, tile,
+                                                      (const uchar4*)fallback_bgra, (uchar4*)final_bgra,
+                                                      (float4*)denoised_rgba32f, fallback_tiles);
+  return check_launch("compose");
+}
+
+}  // extern "C"
