@@ -51,7 +51,12 @@ def parse():
     ap.add_argument("--min-depth", type=int, default=3)
     ap.add_argument("--instances", type=int, default=2000)
     ap.add_argument("--texture-size", type=int, default=1024)
-    ap.add_argument("--denoiser", default="bmfr", choices=["bmfr", "bfr"])
+    ap.add_argument("--denoiser", default="neural", choices=["neural", "bmfr", "bfr"],
+                    help="neural: U-Net with BMFR as variance-gate fallback (BMFR runs every frame)")
+    ap.add_argument("--gate-threshold", type=float, default=1.0,
+                    help="neural path: tiles whose predicted relative squared error exceeds this show BMFR")
+    ap.add_argument("--weights", default=None, help="neural path: .npz of trained parameters (default: packaged)")
+    ap.add_argument("--ref-spp", type=int, default=4096, help="samples of the relMSE reference render (0: skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -213,6 +218,53 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------------------
+# kernels of one neural dispatch: features, 2 radiance poolings, 4 encoder
+# poolings, 18 convolutions, 3 heads, the gate and the compose
+NEURAL_LAUNCHES = 1 + 2 + 4 + 18 + 3 + 1 + 1
+
+
+def relmse_eval(args, vp, pipe, g, illu, bmfr, neural, pc, cams, stream, dev):
+    """relMSE of the last frame's outputs against an args.ref_spp-sample render
+    of the same camera (mean of the demodulated illumination; every image is
+    remodulated by the G-buffer albedo first): the 1-spp input, BMFR (after
+    the orbit's temporal accumulation) and the network (alone, and as shown:
+    gated tiles from BMFR)."""
+    import torch
+
+    f = pc.value.frame_number
+    img = illu.illumination_images[0].tensor()
+    noisy = img[..., :3].double().clone()
+    albedo = g.albedo.tensor()[..., :3].double() / 255.0
+    out = {"reference_spp": args.ref_spp, "frame": int(f)}
+    den = {"input_1spp": noisy}
+    if bmfr is not None:
+        den["bmfr"] = bmfr.denoised.tensor()[(f & 1) ^ 1][..., :3].double().clone()
+    if neural is not None:
+        nn_out = neural.denoised.tensor()[..., :3].double().clone()
+        den["neural"] = nn_out
+        if neural.fallback_mask is not None and bmfr is not None:
+            m = neural.fallback_mask.tensor()[..., 0].bool()
+            px = m.repeat_interleave(neural.tile, 0).repeat_interleave(neural.tile, 1)[:g.height, :g.width]
+            den["neural_gated"] = torch.where(px[..., None], den["bmfr"], nn_out)
+            out["fallback_tiles"] = int(m.sum().item())
+            out["tiles"] = int(m.numel())
+    torch.cuda.synchronize()
+    ref = torch.zeros_like(noisy)
+    t0 = time.perf_counter()
+    base = 1 << 24
+    for s_ in range(args.ref_spp):
+        pc.set(frame_number=base + s_)
+        pipe.trace(pc, stream)
+        ref += img[..., :3]
+    torch.cuda.synchronize()
+    out["reference_s"] = time.perf_counter() - t0
+    ref /= args.ref_spp
+    r = albedo * ref
+    for k, v in den.items():
+        out[k] = float((((albedo * v - r) ** 2) / (r * r + 0.01)).mean().item())
+    return out
+
+
 def run_gb300(args):
     import torch
 
@@ -238,16 +290,21 @@ def run_gb300(args):
     accu = vp.Accumulator(g, illu, separate_matrices=True)
     acc_illu = accu.accumulated_illumination
     abuf = accu.accumulation_buffer
-    if args.denoiser == "bmfr":
-        den = vp.BMFR(W, H, 32, 32, g, acc_illu, abuf, 256)
-    else:
+    if args.denoiser == "bfr":
         den = vp.BFR(W, H, 16, 16, g, acc_illu, abuf)
+        bmfr = None
+    else:
+        bmfr = den = vp.BMFR(W, H, 32, 32, g, acc_illu, abuf, 256)
+    neural = None
+    if args.denoiser == "neural":
+        neural = vp.NeuralDenoiser(W, H, g, illu, weights=args.weights, fallback=bmfr,
+                                   threshold=args.gate_threshold, tile=32)
     pc = vp.PushConstants()
     stream = torch.cuda.current_stream(dev)
     cams = [orbit(sc, W, H, f) for f in range(16)]
     state = {"prev": cams[0]}
 
-    def frame(f):
+    def frame(f, use_neural=True):
         cam = cams[f % 16]
         prev = state["prev"]
         pc.set(view_inverse=cam.inv_view, proj_inverse=cam.inv_proj, prev_view=prev.view, frame_number=f)
@@ -257,6 +314,8 @@ def run_gb300(args):
         pipe.trace(pc, s)
         vp.lib().pbrt_accumulator_dispatch(accu.ptr, vp._abi.stream_handle(s))
         den.dispatch(pc, s)
+        if neural is not None and use_neural:
+            neural.dispatch(pc, s)
         vp.lib().pbrt_accumulation_buffer_copy_to_back_images(abuf.ptr, g.ptr, acc_illu.ptr, vp._abi.stream_handle(s))
         state["prev"] = cam
 
@@ -284,6 +343,8 @@ def run_gb300(args):
             tev[i][1].record(stream)
             vp.lib().pbrt_accumulator_dispatch(accu.ptr, vp._abi.stream_handle(stream))
             den.dispatch(pc, stream)
+            if neural is not None:
+                neural.dispatch(pc, stream)
             vp.lib().pbrt_accumulation_buffer_copy_to_back_images(abuf.ptr, g.ptr, acc_illu.ptr,
                                                                   vp._abi.stream_handle(stream))
             state["prev"] = cam
@@ -299,8 +360,21 @@ def run_gb300(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(t.item())
 
+    # ---- the BMFR-only path (no network) over the same frames, for the neural-vs-BMFR comparison
+    bmfr_ms = None
+    if neural is not None:
+        for f in range(2):
+            frame(args.warmup + args.steps + f, use_neural=False)
+        torch.cuda.synchronize()
+        ev[0].record(stream)
+        for i in range(args.steps):
+            frame(args.warmup + args.steps + 2 + i, use_neural=False)
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+        bmfr_ms = ev[0].elapsed_time(ev[1]) / args.steps
+
     # ---- end to end through the public API: frame + read-back of the final image every step
-    final = den.get_final_descriptor_image().tensor()
+    final = (neural if neural is not None else den).get_final_descriptor_image().tensor()
     host = torch.empty(final.shape, dtype=final.dtype, pin_memory=True)
     for f in range(2):
         frame(args.warmup + args.steps + f)
@@ -332,7 +406,16 @@ def run_gb300(args):
     den.dispatch(pc, stream)
     e1.record(stream)
     torch.cuda.synchronize()
-    stages["bmfr" if args.denoiser == "bmfr" else "bfr"] = e0.elapsed_time(e1)
+    stages["bfr" if args.denoiser == "bfr" else "bmfr"] = e0.elapsed_time(e1)
+    if neural is not None:
+        e0.record(stream)
+        neural.dispatch(pc, stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        stages["neural"] = e0.elapsed_time(e1)
+    quality = None
+    if args.ref_spp > 0 and rank == 0:
+        quality = relmse_eval(args, vp, pipe, g, illu, bmfr, neural, pc, cams, stream, dev)
     closest_bytes = prof.closest_nodes * NODE_BYTES + prof.closest_tris * TRI_BYTES
     launches = max(1, prof.closest_launches)
     per_launch_s = prof.trace_closest_ms / 1e3 / launches
@@ -361,10 +444,12 @@ def run_gb300(args):
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f32",
+            "dtype": "f32 tracer / bf16 network" if neural is not None else "f32",
             "data": "synthetic (seeded procedural scene; inputs larger than L2: 0.8 GB textures, 0.5 GB path state)",
             "config": {
-                "workload": "1080p 1spp depth8 RR>=3, 1M-tri instanced scene, accumulate + BMFR 32x32 (16-frame orbit)",
+                "workload": ("1080p 1spp depth8 RR>=3, 1M-tri instanced scene, 16-frame orbit: accumulate + BMFR 32x32"
+                             + (" + kernel-predicting U-Net (BF16) with per-tile BMFR fallback gate"
+                                if neural is not None else "")),
                 "width": W, "height": H, "max_depth": args.max_depth, "min_depth": args.min_depth,
                 "triangles": int(info.triangle_count), "instances": int(info.instance_count),
                 "lights": int(info.light_count), "texture_size": args.texture_size, "denoiser": args.denoiser,
@@ -392,7 +477,9 @@ def run_gb300(args):
             },
             "cpu_baseline": cpu,
             "clocks": clocks,
-            "gpu_launches": steps * (3 + 5 * (args.max_depth + 1) + 1 + 2),
+            "gpu_launches": steps * (3 + 5 * (args.max_depth + 1) + 1 + 2 + (NEURAL_LAUNCHES if neural else 0)),
+            "bmfr_path": None if bmfr_ms is None else {"fps": world * 1e3 / bmfr_ms, "ms_per_step": bmfr_ms},
+            "relmse": quality,
             "bvh": {"nodes": int(info.bvh_nodes), "depth": int(info.bvh_depth), "build_ms": info.build_ms},
         }
         print(json.dumps(line), flush=True)

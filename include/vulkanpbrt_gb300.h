@@ -99,6 +99,8 @@ typedef struct PbrtBMFR PbrtBMFR;
 typedef struct PbrtBFR PbrtBFR;
 typedef struct PbrtScene PbrtScene;
 typedef struct PbrtPipeline PbrtPipeline;
+typedef struct PbrtNeural PbrtNeural;
+typedef struct PbrtTaa PbrtTaa;
 
 /* ---- library ---------------------------------------------------------- */
 PBRT_API const char* pbrt_version(void);
@@ -353,9 +355,40 @@ typedef struct PbrtStageTimes {
 } PbrtStageTimes;
 PBRT_API int pbrt_pipeline_profile(PbrtPipeline* p, const PbrtPushConstants* pc, pbrt_stream_t stream,
                                    PbrtStageTimes* out);
+/* Failure handling without a GPU fault (no reference counterpart; the
+ * reference has none). abort_flag: a pinned host word mapped into the
+ * device; writing nonzero makes frames in flight and later frames stop
+ * taking rays (checked every 64 warp batches) and shade nothing, until the
+ * host writes 0. set_budget: a frame whose traversal runs longer than
+ * budget_ns (0 = no budget, the default) stops the same way. status
+ * (stream-synchronising) gives PBRT_ERROR_ABORTED or PBRT_ERROR_TIMEOUT for a
+ * stopped frame since the last call, else PBRT_OK, and clears it; the
+ * pipeline stays usable. */
+PBRT_API int pbrt_pipeline_abort_flag(PbrtPipeline* p, uint32_t** host_flag);
+PBRT_API int pbrt_pipeline_set_budget(PbrtPipeline* p, uint64_t budget_ns);
+PBRT_API int pbrt_pipeline_status(PbrtPipeline* p, pbrt_stream_t stream, int32_t* frame_status);
 /* R32_UINT per pixel: key of the primary ray's closest triangle (see
  * pbrt_scene_trace_rays), 0xffffffff on a miss. */
 PBRT_API int pbrt_pipeline_debug_images(const PbrtPipeline* p, PbrtImage* primary_hit_key);
+
+/* ---- Taa (source/renderModules/Taa.hpp:9-35) ----------------------------
+ * Taa(width, height, work_width, work_height, g_buffer, acc_buffer, denoised)
+ * (Taa.cpp:4-91): denoised is the denoiser's final image (packed B8G8R8A8,
+ * e.g. pbrt_bmfr_final_image; it must outlive the Taa object); motion comes
+ * from acc_buffer. add_dispatch_to_command_graph (Taa.cpp:111-120) ->
+ * pbrt_taa_dispatch (frame_number from the push constants; the history copy
+ * of Taa.cpp:121-159 is part of the dispatch); get_final_descriptor_image ->
+ * pbrt_taa_final_image (B8G8R8A8). */
+PBRT_API int pbrt_taa_create(uint32_t width, uint32_t height, uint32_t work_width, uint32_t work_height,
+                             PbrtGBuffer* g_buffer, PbrtAccumulationBuffer* acc_buffer, const PbrtImage* denoised,
+                             PbrtTaa** out);
+PBRT_API int pbrt_taa_dispatch(PbrtTaa* taa, const PbrtPushConstants* pc, pbrt_stream_t stream);
+PBRT_API int pbrt_taa_final_image(const PbrtTaa* taa, PbrtImage* out);
+/* FormatConverter (source/renderModules/FormatConverter.hpp,
+ * shaders/formatConverter.comp:9-13): dst = src texel by texel, src
+ * RGBA32F / RGBA16F / RGBA8 / BGRA8, dst RGBA32F / RGBA8 / BGRA8 (UNORM
+ * stores clamp and round); same size. */
+PBRT_API int pbrt_format_convert(const PbrtImage* src, const PbrtImage* dst, pbrt_stream_t stream);
 
 /* ---- synthetic workloads (no reference counterpart) -------------------- */
 /* Procedural tileable value-noise RGBA8 texture: kind 0 albedo (sRGB-encoded
@@ -421,14 +454,49 @@ PBRT_API int pbrt_nn_relmse_loss(const float* out, const float* target, const vo
  * the BF16 copy when w_bf16 is given. */
 PBRT_API int pbrt_nn_adam(float* w, const float* g, float* m, float* v, void* w_bf16, int64_t n, float lr, float b1,
                           float b2, float eps, int32_t step, float grad_scale, pbrt_stream_t stream);
-/* Final image of the neural path, tone-mapped as BMFR's final image; with var
- * and fallback_bgra, every tile x tile block whose mean predicted squared
- * error exceeds threshold takes the fallback image (BMFR's final image) and
- * is counted in fallback_tiles. */
-PBRT_API int pbrt_nn_compose(const float* out, int32_t pw, int32_t ph, int32_t w, int32_t h, const void* albedo,
-                             const float* var, float threshold, int32_t tile, const void* fallback_bgra,
-                             void* final_bgra, float* denoised_rgba32f, uint32_t* fallback_tiles,
-                             pbrt_stream_t stream);
+/* Variance gate: mask[t] = 1 for every tile x tile block (row-major tiles
+ * over w x h) whose mean predicted relative squared error exp(var) exceeds
+ * threshold; count += the number of such tiles. */
+PBRT_API int pbrt_nn_gate(const float* var, int32_t pw, int32_t w, int32_t h, float threshold, int32_t tile,
+                          uint8_t* mask, uint32_t* count, pbrt_stream_t stream);
+/* Final image of the neural path, tone-mapped as BMFR's final image; pixels
+ * of masked tiles copy fallback_bgra (BMFR's final image). denoised_rgba32f
+ * (optional) always receives the network's output. */
+PBRT_API int pbrt_nn_compose(const float* out, int32_t pw, int32_t w, int32_t h, const void* albedo,
+                             const uint8_t* mask, int32_t tile, const void* fallback_bgra, void* final_bgra,
+                             float* denoised_rgba32f, pbrt_stream_t stream);
+
+/* ---- neural denoiser render module (no reference counterpart) ---------
+ * Reads the G-buffer and the 1-spp demodulated illumination image of
+ * `illumination` (RGBA32F or RGBA16F) and writes a denoised RGBA32F image and
+ * a B8G8R8A8 final image tone-mapped as BMFR's. Parameters: the flat FP32
+ * vector of vulkanpbrt_gb300/kpunet.py (convolution weights [cout][9][cin]
+ * in layer order, convolution biases, then per head weights [k][c] and
+ * biases), pbrt_neural_param_count floats. The forward pass is captured in
+ * a CUDA graph on the first dispatch. */
+PBRT_API int pbrt_neural_param_count(int64_t* count);
+PBRT_API int pbrt_neural_create(uint32_t width, uint32_t height, PbrtGBuffer* gbuffer,
+                                PbrtIlluminationBuffer* illumination, const float* params_host, int64_t count,
+                                PbrtNeural** out);
+PBRT_API int pbrt_neural_set_params(PbrtNeural* nd, const float* params_host, int64_t count);
+/* Variance gate: with bmfr given, every tile x tile block whose mean predicted
+ * per-pixel relative squared error exceeds threshold shows BMFR's final image
+ * in the final image (the denoised image keeps the network's output)
+ * (bmfr must be dispatched before the neural module each frame); null bmfr
+ * turns the gate off. */
+PBRT_API int pbrt_neural_set_fallback(PbrtNeural* nd, PbrtBMFR* bmfr, float threshold, int32_t tile);
+PBRT_API int pbrt_neural_dispatch(PbrtNeural* nd, pbrt_stream_t stream);
+/* The same launches without the graph (for per-kernel profiling). */
+PBRT_API int pbrt_neural_dispatch_direct(PbrtNeural* nd, pbrt_stream_t stream);
+PBRT_API int pbrt_neural_final_image(const PbrtNeural* nd, PbrtImage* out);
+/* denoised: RGBA32F width x height; variance: R32F predicted log relative
+ * squared error at the padded size (multiples of 16). */
+PBRT_API int pbrt_neural_images(const PbrtNeural* nd, PbrtImage* denoised, PbrtImage* variance);
+/* R8 image, one texel per gate tile (row-major): 1 where the last dispatch
+ * showed the fallback; empty (data null) while the gate is off. */
+PBRT_API int pbrt_neural_fallback_mask(const PbrtNeural* nd, PbrtImage* mask);
+/* Tiles of the last dispatch that took the fallback (stream-synchronising). */
+PBRT_API int pbrt_neural_fallback_tiles(const PbrtNeural* nd, pbrt_stream_t stream, uint32_t* count);
 
 #ifdef __cplusplus
 }

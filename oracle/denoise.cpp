@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <limits>
 #include <cstdint>
 #include <cstring>
 #include <thread>
@@ -626,6 +627,57 @@ int oracle_bfr(int W, int H, int bw, int bh, uint32_t frame, const float* depth,
         for (int j = 0; j < ASZ; ++j) dc = dc + feat[(size_t)i * ASZ + j] * alpha[j];
         post_store(W, H, frame, dc, ix[i], iy[i], albedo, motion, spp, denoised, final_bgra);
       }
+    }
+  }, threads);
+  return 0;
+}
+
+// TAA (shaders/taa.comp:48-103) with the history the reference keeps: the
+// previous final B8G8R8A8 image copied byte for byte into an R8G8B8A8 image
+// (source/renderModules/Taa.cpp:121-159), so the bilinear history sample
+// returns the previous frame's (b, g, r). denoised / final: B8G8R8A8 bytes;
+// history / history_next: the copied bytes; motion: RG16F.
+int oracle_taa(int W, int H, uint32_t frame, const uint16_t* motion, const uint8_t* denoised, const uint8_t* history,
+               uint8_t* final_bgra, uint8_t* history_next, int threads) {
+  auto fetch = [&](size_t p) { return vec3{u82f(denoised[4 * p + 2]), u82f(denoised[4 * p + 1]), u82f(denoised[4 * p])}; };
+  auto ycocg = [](vec3 c) {
+    return vec3{c.x * 1.f + c.y * 2.f + c.z * 1.f, c.x * 2.f + c.y * 0.f + c.z * -2.f,
+                c.x * -1.f + c.y * 2.f + c.z * -1.f};
+  };
+  parallel_for(H, [&](int y) {
+    for (int x = 0; x < W; ++x) {
+      const size_t p = (size_t)y * W + x;
+      const vec3 cur = fetch(p);
+      const vec2 uv{h2f(motion[2 * p]), h2f(motion[2 * p + 1])};
+      vec3 res = cur;
+      if (!(frame == 0 || uv.x < 0.f || uv.y < 0.f || uv.x > 1.f || uv.y > 1.f)) {
+        const float inf = std::numeric_limits<float>::infinity();
+        vec3 mn_box{inf, inf, inf}, mn_cross = mn_box, mx_box{-inf, -inf, -inf}, mx_cross = mx_box;
+        for (int dy = -1; dy <= 1; ++dy)
+          for (int dx = -1; dx <= 1; ++dx) {
+            const int sx = x + dx, sy = y + dy;
+            if (sx < 0 || sy < 0 || sx >= W || sy >= H) continue;
+            const vec3 c = ycocg((dx == 0 && dy == 0) ? cur : fetch((size_t)sy * W + sx));
+            if (dx == 0 || dy == 0) {
+              mn_cross = gmin(mn_cross, c);
+              mx_cross = gmax(mx_cross, c);
+            }
+            mn_box = gmin(mn_box, c);
+            mx_box = gmax(mx_box, c);
+          }
+        float h[4];
+        bilinear(W, H, uv, [&](int i, int j, float o[4]) {
+          const size_t q = 4 * ((size_t)j * W + i);
+          for (int k = 0; k < 4; ++k) o[k] = u82f(history[q + k]);
+        }, h);
+        const vec3 prev{h[0], h[1], h[2]};
+        const vec3 pc = ycocg(prev);
+        const vec3 mn = (mn_box + mn_cross) * .5f, mx = (mx_box + mx_cross) * .5f;
+        const bool inside = pc.x >= mn.x && pc.y >= mn.y && pc.z >= mn.z && pc.x <= mx.x && pc.y <= mx.y && pc.z <= mx.z;
+        if (inside) res = .4f * cur + (1.f - .4f) * prev;
+      }
+      const uint8_t o[4] = {f2u8(res.z), f2u8(res.y), f2u8(res.x), 255};
+      for (int k = 0; k < 4; ++k) final_bgra[4 * p + k] = history_next[4 * p + k] = o[k];
     }
   }, threads);
   return 0;

@@ -106,6 +106,18 @@ def bmfr_post(bw, frame, position_type, inv_view, inv_proj, depth, normal, albed
     return final
 
 
+def taa(frame, motion_f16, denoised_bgra, history, threads=None):
+    """taa.comp with the reference's byte-copied history. Returns (final BGRA8 [H,W,4], next history [H,W,4])."""
+    H, W = denoised_bgra.shape[:2]
+    final = np.zeros((H, W, 4), np.uint8)
+    nxt = np.zeros((H, W, 4), np.uint8)
+    rc = lib().oracle_taa(W, H, C.c_uint32(frame), _p(np.ascontiguousarray(motion_f16, np.float16)),
+                          _p(np.ascontiguousarray(denoised_bgra, np.uint8)), _p(np.ascontiguousarray(history, np.uint8)),
+                          _p(final), _p(nxt), threads_default() if threads is None else threads)
+    assert rc == 0
+    return final, nxt
+
+
 def bmfr(bw, fit_threads, frame, position_type, inv_view, inv_proj, depth, normal, albedo, noisy_f16, motion_f16, spp,
          denoised, threads=None):
     """bmfrPre -> bmfrFit -> bmfrPost. Returns (features, weights, final); `denoised` updated in place."""

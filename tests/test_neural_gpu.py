@@ -1,0 +1,153 @@
+"""The neural denoiser render module (pbrt_neural_*): its graph-captured
+native forward pass against the training-side forward of the same network
+(same kernels, so bit-identical), the variance gate at its extremes, and the
+ablation: on a held-out view the trained network must beat BMFR on the same
+1-spp frame, the untrained network and the raw 1-spp input, in relMSE
+against a many-sample render."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _random_frame(g, illu, seed):
+    import torch
+
+    gen = torch.Generator().manual_seed(seed)
+    H, W = g.height, g.width
+    g.depth.tensor().copy_(torch.rand(H, W, 1, generator=gen) * 20)
+    nrm = torch.rand(H, W, 2, generator=gen) * torch.tensor([3.14159, 6.28318])
+    g.normal.tensor().copy_(nrm)
+    g.albedo.tensor().copy_(torch.randint(10, 256, (H, W, 4), generator=gen, dtype=torch.uint8))
+    illu.illumination_images[0].tensor().copy_(torch.rand(H, W, 4, generator=gen) ** 4 * 8)
+
+
+def _params(seed):
+    from vulkanpbrt_gb300 import kpunet as K
+
+    p = K.init_params(seed)
+    lay, _ = K.param_layout()
+    rng = np.random.default_rng(seed)
+    for key, (off, shape) in lay.items():
+        if key.startswith("h") and key.endswith(".w"):
+            p[off:off + int(np.prod(shape))] = rng.standard_normal(int(np.prod(shape))).astype(np.float32) * 0.2
+    return p
+
+
+def test_native_forward_equals_training_forward(cuda):
+    import torch
+
+    import vulkanpbrt_gb300 as vp
+    from vulkanpbrt_gb300 import kpunet as K
+    from vulkanpbrt_gb300.neural import NeuralDenoiser, param_count
+
+    W, H = 200, 120
+    assert param_count() == K.param_layout()[1]
+    g = vp.GBuffer(W, H)
+    illu = vp.IlluminationBufferDemodulatedFloat(W, H)
+    _random_frame(g, illu, 1)
+    p = _params(3)
+    nd = NeuralDenoiser(W, H, g, illu, weights=p)
+    nd.dispatch()
+    nd.dispatch()  # graph replay
+    torch.cuda.synchronize()
+    got = nd.denoised.tensor()[..., :3].cpu()
+    net = K.KPUNet(cuda, params=p)
+    ws = net.workspace(1, 128, 208, training=False)
+    ws.set_input(illu.illumination_images[0].tensor()[None], g.albedo.tensor()[None], g.normal.tensor()[None],
+                 g.depth.tensor()[None, ..., 0])
+    want = ws.forward()[0, :H, :W].cpu()
+    torch.cuda.synchronize()
+    assert torch.equal(got, want)
+    assert torch.isfinite(got).all()
+
+
+def test_variance_gate_extremes(cuda):
+    import torch
+
+    import vulkanpbrt_gb300 as vp
+    from vulkanpbrt_gb300.neural import NeuralDenoiser
+
+    W, H = 200, 120
+    g = vp.GBuffer(W, H)
+    illu = vp.IlluminationBufferDemodulatedFloat(W, H)
+    _random_frame(g, illu, 2)
+    acc = vp.AccumulationBuffer(W, H)
+    bmfr = vp.BMFR(W, H, 32, 32, g, illu, acc, 256)
+    pc = vp.PushConstants()
+    bmfr.dispatch(pc)
+    nd = NeuralDenoiser(W, H, g, illu, weights=_params(4), fallback=bmfr, threshold=-1.0, tile=32)
+    nd.dispatch()
+    torch.cuda.synchronize()
+    tiles = ((W + 31) // 32) * ((H + 31) // 32)
+    assert nd.fallback_tiles() == tiles
+    assert torch.equal(nd.get_final_descriptor_image().tensor().cpu(), bmfr.get_final_descriptor_image().tensor().cpu())
+    assert int(nd.fallback_mask.tensor().sum()) == tiles
+    nd.set_fallback(bmfr, threshold=1e30, tile=32)
+    nd.dispatch()
+    torch.cuda.synchronize()
+    assert nd.fallback_tiles() == 0
+    plain = NeuralDenoiser(W, H, g, illu, weights=_params(4))
+    plain.dispatch()
+    torch.cuda.synchronize()
+    assert torch.equal(nd.get_final_descriptor_image().tensor().cpu(), plain.get_final_descriptor_image().tensor().cpu())
+
+
+def relmse(x, ref, albedo):
+    """mean of (A x - A r)^2 / ((A r)^2 + 0.01) over pixels and channels (A: the G-buffer albedo)."""
+    A = albedo[..., :3].double() / 255.0
+    r = A * ref[..., :3].double()
+    return (((A * x[..., :3].double() - r) ** 2) / (r * r + 0.01)).mean().item()
+
+
+def test_trained_network_beats_bmfr_and_untrained(cuda):
+    """Ablation on a view no training pair came from (the benchmark scene,
+    seed 0): 256 x 256 window of a 1080p frame, 1 spp, reference 1024 spp."""
+    import torch
+
+    import vulkanpbrt_gb300 as vp
+    from vulkanpbrt_gb300 import kpunet as K
+    from vulkanpbrt_gb300 import scene as S
+    from vulkanpbrt_gb300.camera import Camera, CropCamera
+    from vulkanpbrt_gb300.neural import WEIGHTS, NeuralDenoiser
+
+    if not WEIGHTS.exists():
+        pytest.skip("no trained weights in the package")
+    W = H = 256
+    sc = S.instanced_field(seed=0, texture_size=256)
+    sh = vp.SceneHandle(sc)
+    g = vp.GBuffer(W, H)
+    illu = vp.IlluminationBufferDemodulatedFloat(W, H)
+    pipe = vp.PBRTPipeline(sh, g, illu, True, max_recursion_depth=8, min_recursion_depth=3)
+    cam = Camera(sc.camera_eye, sc.camera_center, aspect=1920 / 1080)
+    cc = CropCamera(cam, 1920, 1080, 832, 412, W, H)
+    pc = vp.PushConstants()
+    pc.set(view_inverse=cc.inv_view, proj_inverse=cc.inv_proj, prev_view=cc.view, frame_number=0)
+    pipe.trace(pc)
+    img = illu.illumination_images[0].tensor()
+    noisy = img.clone()
+    acc = vp.AccumulationBuffer(W, H)
+    bmfr = vp.BMFR(W, H, 32, 32, g, illu, acc, 256)
+    bmfr.dispatch(pc)
+    trained = NeuralDenoiser(W, H, g, illu)
+    trained.dispatch()
+    untrained = NeuralDenoiser(W, H, g, illu, weights=K.init_params(0))
+    untrained.dispatch()
+    torch.cuda.synchronize()
+    den_bmfr = bmfr.denoised.tensor()[1].float().clone()  # frame 0 writes layer 1
+    den_nn = trained.denoised.tensor().clone()
+    den_un = untrained.denoised.tensor().clone()
+    albedo = g.albedo.tensor().clone()
+    ref = torch.zeros(H, W, 3, dtype=torch.float64, device=cuda)
+    spp = 1024
+    for s in range(spp):
+        pc.set(frame_number=1 + s)
+        pipe.trace(pc)
+        ref += img[..., :3]
+    ref /= spp
+    r = {k: relmse(v, ref, albedo) for k, v in
+         {"1spp": noisy, "bmfr": den_bmfr, "untrained": den_un, "trained": den_nn}.items()}
+    print("relMSE vs 1024 spp:", r)
+    assert r["trained"] < r["bmfr"]
+    assert r["trained"] < r["untrained"]
+    assert r["trained"] < r["1spp"]

@@ -199,26 +199,34 @@ def test_compose_and_variance_gate(cuda):
     from vulkanpbrt_gb300 import nn
 
     g = torch.Generator().manual_seed(9)
-    h, w, ph, pw = 70, 100, 80, 112
+    h, w, ph, pw, tile = 70, 100, 80, 112, 32
     out = torch.rand(ph, pw, 3, generator=g) * 2
     albedo = torch.randint(0, 256, (h, w, 4), generator=g, dtype=torch.uint8)
     fallback = torch.randint(0, 256, (h, w, 4), generator=g, dtype=torch.uint8)
     var = torch.full((ph, pw), -9.0)
-    var[:32, 32:64] = 3.0  # one tile over the threshold
+    var[:32, 32:64] = 3.0        # tile (1, 0): mean exp(3) > 1
+    var[64:70, 96:100] = 4.0     # tile (3, 2), partial 6 x 4 tile: over the threshold only if edges count
+    var[70:, :] = 50.0           # padding rows: must not count
+    tiles_x, tiles_y = (w + tile - 1) // tile, (h + tile - 1) // tile
+    mask = torch.zeros(tiles_x * tiles_y, dtype=torch.uint8, device=cuda)
+    count = torch.zeros(1, dtype=torch.int32, device=cuda)
+    nn.gate(var.to(cuda), w, h, 1.0, tile, mask, count)
     final = torch.empty(h, w, 4, dtype=torch.uint8, device=cuda)
     den = torch.empty(h, w, 4, device=cuda)
-    ntiles = torch.zeros(1, dtype=torch.int32, device=cuda)
-    nn.compose(out.to(cuda), albedo.to(cuda), final, var=var.to(cuda), threshold=1.0, tile=32,
-               fallback=fallback.to(cuda), denoised=den, fallback_tiles=ntiles)
+    nn.compose(out.to(cuda), albedo.to(cuda), final, mask=mask, tile=tile, fallback=fallback.to(cuda), denoised=den)
     torch.cuda.synchronize()
+    want = torch.zeros(tiles_y, tiles_x, dtype=torch.uint8)
+    for ty in range(tiles_y):
+        for tx in range(tiles_x):
+            blk = var[ty * tile:min(h, (ty + 1) * tile), tx * tile:min(w, (tx + 1) * tile)]
+            want[ty, tx] = int(blk.exp().mean().item() > 1.0)
+    assert torch.equal(mask.cpu().view(tiles_y, tiles_x), want)
+    assert int(count.item()) == int(want.sum())
     A = albedo[..., :3].float() / 255 + 1e-6
     t = (A * out[:h, :w]).clamp_min(0).pow(0.454545).clamp(0, 1)
     bgra = torch.floor(t * 255 + 0.5).to(torch.uint8).flip(-1)
+    gate_px = want.repeat_interleave(tile, 0).repeat_interleave(tile, 1)[:h, :w].bool()
     fc = final.cpu()
-    gate = torch.zeros(h, w, dtype=torch.bool)
-    gate[:32, 32:64] = True
-    assert torch.equal(fc[gate], fallback[gate])
-    diff = (fc[~gate][:, :3].int() - bgra[~gate].int()).abs().max().item()
-    assert diff <= 1
-    assert int(ntiles.item()) == 1
-    assert _rel(den[~gate][:, :3], out[:h, :w][~gate]) < 1e-6
+    assert torch.equal(fc[gate_px], fallback[gate_px])
+    assert (fc[~gate_px][:, :3].int() - bgra[~gate_px].int()).abs().max().item() <= 1
+    assert _rel(den[..., :3], out[:h, :w]) < 1e-6

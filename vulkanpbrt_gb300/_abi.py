@@ -119,6 +119,10 @@ _SIGS = {
     "pbrt_bfr_dispatch": (i32, [H, P(PbrtPushConstants), H]),
     "pbrt_bfr_final_image": (i32, [H, P(PbrtImage)]),
     "pbrt_bfr_images": (i32, [H, P(PbrtImage)]),
+    "pbrt_taa_create": (i32, [u32, u32, u32, u32, H, H, P(PbrtImage), P(H)]),
+    "pbrt_taa_dispatch": (i32, [H, P(PbrtPushConstants), H]),
+    "pbrt_taa_final_image": (i32, [H, P(PbrtImage)]),
+    "pbrt_format_convert": (i32, [P(PbrtImage), P(PbrtImage), H]),
 }
 
 

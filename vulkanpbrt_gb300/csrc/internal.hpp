@@ -21,7 +21,9 @@ enum class Kind : uint32_t {
   BMFR,
   BFR,
   Scene,
-  Pipeline
+  Pipeline,
+  Neural,
+  Taa
 };
 
 struct Object {

@@ -343,38 +343,48 @@ __global__ void adam_kernel(float* __restrict__ w, const float* __restrict__ g, 
   }
 }
 
-// Final image of the neural path: denoised illumination remodulated by the
-// albedo and tone mapped as bmfrPost does (shaders/bmfrPost.comp:211-214);
-// with a variance gate, tiles whose mean predicted error exceeds the
-// threshold take the fallback (BMFR) result instead.
-__global__ void compose_kernel(const float* __restrict__ out, int PW, int PH, int W, int H,
-                               const uchar4* __restrict__ albedo, const float* __restrict__ var, float threshold,
-                               int tile, const uchar4* __restrict__ fallback, uchar4* __restrict__ final_bgra,
-                               float4* __restrict__ denoised, uint32_t* __restrict__ fallback_tiles) {
+// Variance gate: one CTA per tile x tile block; the block falls back when
+// the mean over its pixels of the predicted relative squared error
+// (exp of the error head's log output) exceeds the threshold.
+__global__ void gate_kernel(const float* __restrict__ var, int PW, int W, int H, float threshold, int tile,
+                            uint8_t* __restrict__ mask, uint32_t* __restrict__ count) {
+  __shared__ float part[8];
+  const int tiles_x = (W + tile - 1) / tile;
+  const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+  const int x0 = tx * tile, y0 = ty * tile;
+  const int tw = min(tile, W - x0), th = min(tile, H - y0);
+  float s = 0.f;
+  for (int i = threadIdx.x; i < tw * th; i += blockDim.x) s += __expf(var[(size_t)(y0 + i / tw) * PW + x0 + i % tw]);
+  for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w];
+    const bool fb = t / (float)(tw * th) > threshold;
+    mask[blockIdx.x] = fb ? 1 : 0;
+    if (fb) atomicAdd(count, 1u);
+  }
+}
+
+// Final image of the neural path: the network's denoised illumination
+// (always written to `denoised`) remodulated by the albedo and tone mapped
+// as bmfrPost does (shaders/bmfrPost.comp:211-214); pixels of tiles the gate
+// marked take the fallback (BMFR) final image instead.
+__global__ void compose_kernel(const float* __restrict__ out, int PW, int W, int H, const uchar4* __restrict__ albedo,
+                               const uint8_t* __restrict__ mask, int tile, const uchar4* __restrict__ fallback,
+                               uchar4* __restrict__ final_bgra, float4* __restrict__ denoised) {
   const long P = (long)W * H;
+  const int tiles_x = mask ? (W + tile - 1) / tile : 1;
   GRID_STRIDE(i, P) {
     const int x = (int)(i % W), y = (int)(i / W);
-    bool use_fallback = false;
-    if (var && fallback) {
-      // mean predicted log-error over the pixel's tile (recomputed per pixel; tiles are small)
-      const int tx0 = (x / tile) * tile, ty0 = (y / tile) * tile;
-      float s = 0.f;
-      int cnt = 0;
-      for (int yy = ty0; yy < min(ty0 + tile, H); yy += 4)
-        for (int xx = tx0; xx < min(tx0 + tile, W); xx += 4) {
-          s += __expf(var[(size_t)yy * PW + xx]);
-          ++cnt;
-        }
-      use_fallback = s / (float)cnt > threshold;
-      if (use_fallback && x == tx0 && y == ty0) atomicAdd(fallback_tiles, 1u);
-    }
-    if (use_fallback) {
-      final_bgra[i] = fallback[i];
-      continue;
-    }
     const size_t p = (size_t)y * PW + x;
     const float3 o = f3(out[p * 3], out[p * 3 + 1], out[p * 3 + 2]);
     if (denoised) denoised[i] = make_float4(o.x, o.y, o.z, 1.f);
+    if (mask && mask[(y / tile) * tiles_x + x / tile]) {
+      final_bgra[i] = fallback[i];
+      continue;
+    }
     const uchar4 a = albedo[i];
     float3 t = fmax3(f3(0.f), f3(a.x / 255.f + 1e-6f, a.y / 255.f + 1e-6f, a.z / 255.f + 1e-6f) * o);
     t = clamp3(f3(powf(t.x, .454545f), powf(t.y, .454545f), powf(t.z, .454545f)), 0.f, 1.f);
@@ -487,14 +497,23 @@ PBRT_API int pbrt_nn_adam(float* w, const float* g, float* m, float* v, void* w_
   return check_launch("adam");
 }
 
-PBRT_API int pbrt_nn_compose(const float* out, int32_t pw, int32_t ph, int32_t w, int32_t h, const void* albedo,
-                             const float* var, float threshold, int32_t tile, const void* fallback_bgra,
-                             void* final_bgra, float* denoised_rgba32f, uint32_t* fallback_tiles, pbrt_stream_t s) {
-  if (!out || !albedo || !final_bgra || (var && fallback_bgra && (!fallback_tiles || tile <= 0)))
+PBRT_API int pbrt_nn_gate(const float* var, int32_t pw, int32_t w, int32_t h, float threshold, int32_t tile,
+                          uint8_t* mask, uint32_t* count, pbrt_stream_t s) {
+  if (!var || !mask || !count || tile < 4 || tile > 256 || w <= 0 || h <= 0 || pw < w)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "gate: bad arguments");
+  const int tiles = ((w + tile - 1) / tile) * ((h + tile - 1) / tile);
+  gate_kernel<<<tiles, 256, 0, s>>>(var, pw, w, h, threshold, tile, mask, count);
+  return check_launch("gate");
+}
+
+PBRT_API int pbrt_nn_compose(const float* out, int32_t pw, int32_t w, int32_t h, const void* albedo,
+                             const uint8_t* mask, int32_t tile, const void* fallback_bgra, void* final_bgra,
+                             float* denoised_rgba32f, pbrt_stream_t s) {
+  if (!out || !albedo || !final_bgra || pw < w || (mask && (!fallback_bgra || tile < 4 || tile > 256)))
     return fail(PBRT_ERROR_INVALID_ARGUMENT, "compose: bad arguments");
-  compose_kernel<<<grid_for((long)w * h), 256, 0, s>>>(out, pw, ph, w, h, (const uchar4*)albedo, var, threshold, tile,
+  compose_kernel<<<grid_for((long)w * h), 256, 0, s>>>(out, pw, w, h, (const uchar4*)albedo, mask, tile,
                                                       (const uchar4*)fallback_bgra, (uchar4*)final_bgra,
-                                                      (float4*)denoised_rgba32f, fallback_tiles);
+                                                      (float4*)denoised_rgba32f);
   return check_launch("compose");
 }
 

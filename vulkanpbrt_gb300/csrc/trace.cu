@@ -233,6 +233,8 @@ struct FrameParams {
   int light_mode;            // 0 surface strength, 1 light strength, 2 uniform
   int final_image;           // FINAL_IMAGE (progressive sRGB) instead of DEMOD_ILLUMINATION_FLOAT
   int write_gbuffer;
+  const volatile uint32_t* abort_flag;  // mapped host word, nonzero = stop (null: none)
+  unsigned long long budget_ns;         // frame time budget (0: none)
 };
 
 struct Counters {
@@ -240,8 +242,11 @@ struct Counters {
   uint32_t shadow;       // shadow queue size
   uint32_t work_trace;   // persistent-warp work index, closest hit
   uint32_t work_shadow;  // persistent-warp work index, any hit
-  uint32_t error;        // traversal stack overflow
-  uint32_t pad[2];
+  uint32_t error;        // bit 0 traversal stack overflow, bit 1 aborted, bit 2 budget exceeded
+  uint32_t stop;         // nonzero: the frame was stopped (abort flag or budget); no more work is taken
+  uint32_t pad;
+  unsigned long long t0, budget_ns;      // frame start (%globaltimer) and budget
+  const volatile uint32_t* abort_flag;
   unsigned long long rays_primary, rays_extension, rays_shadow, frames;
   unsigned long long nodes_closest, tris_closest, nodes_shadow, tris_shadow;  // BVH work (node / triangle visits)
 };
@@ -301,7 +306,35 @@ PBRT_D int warp_alloc(uint32_t* counter, bool want) {
 // to outlive the call, so consecutive frames need no host synchronisation.
 __global__ void k_set_params(FrameParams* dst, FrameParams fp) { *dst = fp; }
 
+PBRT_D unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Abort flag and frame budget: every traversal warp reads `stop` when it
+// takes a batch; one batch in 64 also polls the host's abort word and the
+// clock and raises `stop` (recording why in `error`). Stopped frames take no
+// more rays and shade nothing, so the frame ends early and the host reads
+// the reason with pbrt_pipeline_status; nothing waits on anything.
+constexpr uint32_t kPollBatches = 64;
+PBRT_D bool stop_requested(Counters* c, uint32_t batch) {
+  if (*((volatile uint32_t*)&c->stop)) return true;
+  if ((batch / 32u) % kPollBatches != 0) return false;
+  uint32_t why = 0;
+  if (c->abort_flag && *c->abort_flag) why = 2u;
+  else if (c->budget_ns && global_ns() - c->t0 > c->budget_ns) why = 4u;
+  if (!why) return false;
+  atomicOr(&c->stop, why);
+  atomicOr(&c->error, why);
+  return true;
+}
+
 __global__ void k_frame_begin(Counters* c, const FrameParams* fp) {
+  c->stop = 0;
+  c->t0 = global_ns();
+  c->budget_ns = fp->budget_ns;
+  c->abort_flag = fp->abort_flag;
   c->ray[0] = (uint32_t)(fp->W * fp->H);
   c->ray[1] = 0;
   c->shadow = 0;
@@ -405,7 +438,10 @@ __global__ void __launch_bounds__(128, 8) k_traverse(SceneView sc, Queues q, Cou
     while (need && !drained) {
       if (batch_next >= batch_end) {
         uint32_t b = 0;
-        if (lane == 0) b = atomicAdd(work, 32u);
+        if (lane == 0) {
+          b = atomicAdd(work, 32u);
+          if (MODE <= 1 && b < count && stop_requested(c, b)) b = count;
+        }
         b = __shfl_sync(kFullMask, b, 0);
         if (b >= count) {
           drained = true;
@@ -610,6 +646,7 @@ PBRT_D float3 sample_light(const SceneView& sc, int mode, float3 pos, float3 n, 
 __global__ void __launch_bounds__(128) k_shade(SceneView sc, const FrameParams* __restrict__ fpp, Queues q,
                                                Counters* c, GBufferOut g, int k) {
   const FrameParams& fp = *fpp;
+  if (*((volatile uint32_t*)&c->stop)) return;  // stopped frame: shade nothing, queue nothing
   const uint32_t count = *((volatile uint32_t*)&c->ray[k & 1]);
   const uint32_t* qpix = q.pix[k & 1];
   const float4* qdir = q.dir[k & 1];
@@ -845,6 +882,7 @@ struct PbrtPipeline : pbrt::Object {
   ~PbrtPipeline() override {
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
     for (void* p : allocs) cudaFree(p);
+    if (abort_host) cudaFreeHost(abort_host);
     release(scene);
     release(gbuffer);
     release(illumination);
@@ -862,6 +900,9 @@ struct PbrtPipeline : pbrt::Object {
   cudaGraphExec_t graph_exec = nullptr;
   int graph_depth = -1;
   int grid_persistent = 0;
+  uint32_t* abort_host = nullptr;  // mapped pinned word (pbrt_pipeline_abort_flag)
+  uint32_t* abort_dev = nullptr;
+  unsigned long long budget_ns = 0;
   template <class T> int a(T** p, size_t n) {
     int st = dalloc(p, n);
     if (!st) allocs.push_back((void*)*p);
@@ -1260,6 +1301,8 @@ static FrameParams frame_params(const PbrtPipeline* pp, const PbrtPushConstants*
   fp.light_mode = pp->light_mode;
   fp.final_image = pp->illumination->type == PBRT_ILLUMINATION_FINAL_FLOAT ? 1 : 0;
   fp.write_gbuffer = pp->write_gbuffer ? 1 : 0;
+  fp.abort_flag = pp->abort_dev;
+  fp.budget_ns = pp->budget_ns;
   return fp;
 }
 
@@ -1345,6 +1388,45 @@ PBRT_API int pbrt_pipeline_stats(PbrtPipeline* pp, pbrt_stream_t stream, PbrtTra
 PBRT_API int pbrt_pipeline_reset_stats(PbrtPipeline* pp, pbrt_stream_t stream) {
   if (!checked<PbrtPipeline>(pp, Kind::Pipeline)) return fail(PBRT_ERROR_INVALID_ARGUMENT, "not a pipeline");
   PBRT_CUDA(cudaMemsetAsync(pp->ctr, 0, sizeof(Counters), stream));
+  return PBRT_OK;
+}
+
+PBRT_API int pbrt_pipeline_abort_flag(PbrtPipeline* pp, uint32_t** host_flag) {
+  if (!checked<PbrtPipeline>(pp, Kind::Pipeline) || !host_flag)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "abort flag: bad arguments");
+  if (!pp->abort_host) {
+    void* h = nullptr;
+    PBRT_CUDA(cudaHostAlloc(&h, sizeof(uint32_t), cudaHostAllocMapped));
+    *(volatile uint32_t*)h = 0;
+    void* d = nullptr;
+    cudaError_t e = cudaHostGetDevicePointer(&d, h, 0);
+    if (e != cudaSuccess) {
+      cudaFreeHost(h);
+      return cuda_fail(e, "cudaHostGetDevicePointer");
+    }
+    pp->abort_host = (uint32_t*)h;
+    pp->abort_dev = (uint32_t*)d;
+  }
+  *host_flag = pp->abort_host;
+  return PBRT_OK;
+}
+
+PBRT_API int pbrt_pipeline_set_budget(PbrtPipeline* pp, uint64_t budget_ns) {
+  if (!checked<PbrtPipeline>(pp, Kind::Pipeline)) return fail(PBRT_ERROR_INVALID_ARGUMENT, "not a pipeline");
+  pp->budget_ns = budget_ns;
+  return PBRT_OK;
+}
+
+PBRT_API int pbrt_pipeline_status(PbrtPipeline* pp, pbrt_stream_t stream, int32_t* frame_status) {
+  if (!checked<PbrtPipeline>(pp, Kind::Pipeline) || !frame_status)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "status: bad arguments");
+  uint32_t err = 0;
+  PBRT_CUDA(cudaMemcpyAsync(&err, &pp->ctr->error, sizeof(err), cudaMemcpyDeviceToHost, stream));
+  PBRT_CUDA(cudaStreamSynchronize(stream));
+  *frame_status = (err & 2u) ? PBRT_ERROR_ABORTED : (err & 4u) ? PBRT_ERROR_TIMEOUT : PBRT_OK;
+  const uint32_t keep = err & 1u;  // the stack-overflow record stays for pbrt_pipeline_stats
+  PBRT_CUDA(cudaMemcpyAsync(&pp->ctr->error, &keep, sizeof(keep), cudaMemcpyHostToDevice, stream));
+  PBRT_CUDA(cudaStreamSynchronize(stream));
   return PBRT_OK;
 }
 

@@ -1,0 +1,102 @@
+"""NeuralDenoiser: the kernel-predicting U-Net as a render module beside BMFR
+and BFR (same construction from a G-buffer and an illumination buffer, same
+dispatch / final-image interface), over the pbrt_neural_* C ABI. No
+reference counterpart: the reference's denoisers are BMFR and BFR
+(source/renderModules/denoisers/)."""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import _abi
+from ._abi import PbrtImage, check, lib, stream_handle
+from .render_modules import BMFR, Commands, GBuffer, Handle, IlluminationBuffer, Image
+
+H = C.c_void_p
+_abi.add_signatures({
+    "pbrt_neural_param_count": (C.c_int32, [C.POINTER(C.c_int64)]),
+    "pbrt_neural_create": (C.c_int32, [C.c_uint32, C.c_uint32, H, H, H, C.c_int64, C.POINTER(H)]),
+    "pbrt_neural_set_params": (C.c_int32, [H, H, C.c_int64]),
+    "pbrt_neural_set_fallback": (C.c_int32, [H, H, C.c_float, C.c_int32]),
+    "pbrt_neural_dispatch": (C.c_int32, [H, H]),
+    "pbrt_neural_dispatch_direct": (C.c_int32, [H, H]),
+    "pbrt_neural_final_image": (C.c_int32, [H, C.POINTER(PbrtImage)]),
+    "pbrt_neural_images": (C.c_int32, [H, C.POINTER(PbrtImage), C.POINTER(PbrtImage)]),
+    "pbrt_neural_fallback_tiles": (C.c_int32, [H, H, C.POINTER(C.c_uint32)]),
+    "pbrt_neural_fallback_mask": (C.c_int32, [H, C.POINTER(PbrtImage)]),
+})
+
+WEIGHTS = Path(__file__).resolve().parent / "weights" / "kpunet.npz"
+
+
+def param_count() -> int:
+    n = C.c_int64()
+    check(lib().pbrt_neural_param_count(C.byref(n)))
+    return n.value
+
+
+def load_params(weights=None) -> np.ndarray:
+    """FP32 parameter vector from an .npz written by KPUNet.save (default:
+    the trained weights shipped with the package) or an array."""
+    if weights is None:
+        weights = WEIGHTS
+    if isinstance(weights, (str, Path)):
+        with np.load(weights) as d:
+            weights = d["params"]
+    p = np.ascontiguousarray(np.asarray(weights, dtype=np.float32))
+    if p.size != param_count():
+        raise ValueError(f"NeuralDenoiser: {p.size} parameters, the network has {param_count()}")
+    return p
+
+
+class NeuralDenoiser(Handle):
+    """Denoises the 1-spp demodulated illumination of `illu_buffer` with the
+    G-buffer's albedo, normal and depth. With `fallback` (a BMFR over the
+    same frame, dispatched first), tiles whose predicted error exceeds
+    `threshold` show BMFR's final image."""
+
+    def __init__(self, width: int, height: int, g_buffer: GBuffer, illu_buffer: IlluminationBuffer, weights=None,
+                 fallback: BMFR | None = None, threshold: float = 0.5, tile: int = 32):
+        p = load_params(weights)
+        h = C.c_void_p()
+        check(lib().pbrt_neural_create(width, height, g_buffer.ptr, illu_buffer.ptr, p.ctypes.data_as(H), p.size,
+                                       C.byref(h)))
+        super().__init__(h)
+        self._inputs = (g_buffer, illu_buffer)
+        self.width, self.height = width, height
+        d, v, f = PbrtImage(), PbrtImage(), PbrtImage()
+        check(lib().pbrt_neural_images(h, C.byref(d), C.byref(v)))
+        check(lib().pbrt_neural_final_image(h, C.byref(f)))
+        self.denoised, self.variance, self._final = Image(d, self), Image(v, self), Image(f, self)
+        self._fallback = None
+        self.set_fallback(fallback, threshold, tile)
+
+    def set_params(self, weights) -> None:
+        p = load_params(weights)
+        check(lib().pbrt_neural_set_params(self.ptr, p.ctypes.data_as(H), p.size))
+
+    def set_fallback(self, fallback: BMFR | None, threshold: float = 0.5, tile: int = 32) -> None:
+        check(lib().pbrt_neural_set_fallback(self.ptr, fallback.ptr if fallback is not None else None, threshold,
+                                             tile))
+        self._fallback = fallback
+        self.threshold, self.tile = threshold, tile
+        m = PbrtImage()
+        check(lib().pbrt_neural_fallback_mask(self.ptr, C.byref(m)))
+        self.fallback_mask = Image(m, self) if m.data else None
+
+    def dispatch(self, push_constants=None, stream=None, graph: bool = True) -> None:
+        fn = lib().pbrt_neural_dispatch if graph else lib().pbrt_neural_dispatch_direct
+        check(fn(self.ptr, stream_handle(stream)))
+
+    def add_dispatch_to_command_graph(self, commands: Commands, push_constants=None) -> None:
+        commands.add(lambda s: self.dispatch(push_constants, s))
+
+    def get_final_descriptor_image(self) -> Image:
+        return self._final
+
+    def fallback_tiles(self, stream=None) -> int:
+        n = C.c_uint32()
+        check(lib().pbrt_neural_fallback_tiles(self.ptr, stream_handle(stream), C.byref(n)))
+        return n.value

@@ -24,7 +24,8 @@ _abi.add_signatures({
     "pbrt_nn_kp_head_bwd": (i32, [H, H, H, H, H, H, H, H, i32, i32, i32, i32, i32, H, H, H, H, H, H, H]),
     "pbrt_nn_relmse_loss": (i32, [H, H, H, H, i32, i32, i32, i32, i32, f32, H, H, H, H]),
     "pbrt_nn_adam": (i32, [H, H, H, H, H, i64, f32, f32, f32, f32, i32, f32, H]),
-    "pbrt_nn_compose": (i32, [H, i32, i32, i32, i32, H, H, f32, i32, H, H, H, H, H]),
+    "pbrt_nn_gate": (i32, [H, i32, i32, i32, f32, i32, H, H, H]),
+    "pbrt_nn_compose": (i32, [H, i32, i32, i32, H, H, i32, H, H, H, H]),
 })
 
 RELU, ACCUMULATE = 1, 2
@@ -139,10 +140,14 @@ def adam(w, g, m, v, step, lr=1e-4, b1=0.9, b2=0.999, eps=1e-8, w_bf16=None, gra
                              grad_scale, _stream()))
 
 
-def compose(out, albedo, final_bgra, var=None, threshold=0.0, tile=32, fallback=None, denoised=None,
-            fallback_tiles=None):
-    """out [PH,PW,3] f32 -> final_bgra [h,w,4] u8 (tile-gated against fallback when var is given)."""
-    ph, pw = out.shape[-3:-1]
+def gate(var, w, h, threshold, tile, mask, count):
+    """mask [tiles] u8 = mean(exp(var)) over each tile x tile block of the w x h image > threshold."""
+    check(lib().pbrt_nn_gate(_ptr(var), var.shape[-1], w, h, threshold, tile, _ptr(mask), _ptr(count), _stream()))
+
+
+def compose(out, albedo, final_bgra, mask=None, tile=32, fallback=None, denoised=None):
+    """out [PH,PW,3] f32 -> final_bgra [h,w,4] u8; masked tiles copy fallback."""
+    pw = out.shape[-2]
     h, w = final_bgra.shape[:2]
-    check(lib().pbrt_nn_compose(_ptr(out), pw, ph, w, h, _ptr(albedo), _ptr(var), threshold, tile, _ptr(fallback),
-                                _ptr(final_bgra), _ptr(denoised), _ptr(fallback_tiles), _stream()))
+    check(lib().pbrt_nn_compose(_ptr(out), pw, w, h, _ptr(albedo), _ptr(mask), tile, _ptr(fallback),
+                                _ptr(final_bgra), _ptr(denoised), _stream()))

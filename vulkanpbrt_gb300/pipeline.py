@@ -64,6 +64,9 @@ _abi.add_signatures({
     "pbrt_pipeline_reset_stats": (C.c_int32, [H, H]),
     "pbrt_pipeline_debug_images": (C.c_int32, [H, P(PbrtImage)]),
     "pbrt_pipeline_profile": (C.c_int32, [H, P(_abi.PbrtPushConstants), H, P(PbrtStageTimes)]),
+    "pbrt_pipeline_abort_flag": (C.c_int32, [H, P(P(C.c_uint32))]),
+    "pbrt_pipeline_set_budget": (C.c_int32, [H, C.c_uint64]),
+    "pbrt_pipeline_status": (C.c_int32, [H, H, P(C.c_int32)]),
 })
 
 
@@ -194,3 +197,23 @@ class PBRTPipeline(Handle):
 
     def reset_stats(self, stream=None) -> None:
         check(lib().pbrt_pipeline_reset_stats(self.ptr, stream_handle(stream)))
+
+    def abort_flag(self):
+        """The pinned host word that stops frames while nonzero (ctypes uint32 view)."""
+        if getattr(self, "_abort", None) is None:
+            p = P(C.c_uint32)()
+            check(lib().pbrt_pipeline_abort_flag(self.ptr, C.byref(p)))
+            self._abort = p
+        return self._abort
+
+    def set_abort(self, on: bool) -> None:
+        self.abort_flag()[0] = 1 if on else 0
+
+    def set_budget(self, budget_ns: int) -> None:
+        check(lib().pbrt_pipeline_set_budget(self.ptr, int(budget_ns)))
+
+    def status(self, stream=None) -> int:
+        """PBRT_OK, or PBRT_ERROR_ABORTED / PBRT_ERROR_TIMEOUT for a frame stopped since the last call."""
+        st = C.c_int32()
+        check(lib().pbrt_pipeline_status(self.ptr, stream_handle(stream), C.byref(st)))
+        return st.value

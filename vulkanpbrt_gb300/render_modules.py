@@ -321,3 +321,39 @@ class BFR(Handle):
 
     def get_final_descriptor_image(self) -> Image:
         return self._final
+
+
+class Taa(Handle):
+    """Taa (source/renderModules/Taa.hpp): temporal anti-aliasing of a
+    denoiser's final image with the accumulation buffer's motion vectors."""
+
+    def __init__(self, width: int, height: int, work_width: int, work_height: int, g_buffer: GBuffer,
+                 acc_buffer: AccumulationBuffer, denoised: Image):
+        h = C.c_void_p()
+        check(lib().pbrt_taa_create(width, height, work_width, work_height, g_buffer.ptr, acc_buffer.ptr,
+                                    C.byref(denoised.view), C.byref(h)))
+        super().__init__(h)
+        self._inputs = (g_buffer, acc_buffer, denoised)  # the denoised image's owner must outlive this object
+        f = PbrtImage()
+        check(lib().pbrt_taa_final_image(h, C.byref(f)))
+        self._final = Image(f, self)
+
+    def compile(self, context=None) -> None:
+        pass
+
+    def update_image_layouts(self, context=None) -> None:
+        pass
+
+    def dispatch(self, push_constants: PushConstants, stream=None) -> None:
+        check(lib().pbrt_taa_dispatch(self.ptr, C.byref(push_constants.value), stream_handle(stream)))
+
+    def add_dispatch_to_command_graph(self, commands: Commands, push_constants: PushConstants) -> None:
+        commands.add(lambda s: self.dispatch(push_constants, s))
+
+    def get_final_descriptor_image(self) -> Image:
+        return self._final
+
+
+def format_convert(src: Image, dst: Image, stream=None) -> None:
+    """FormatConverter (source/renderModules/FormatConverter.cpp): dst = src texel by texel."""
+    check(lib().pbrt_format_convert(C.byref(src.view), C.byref(dst.view), stream_handle(stream)))
