@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--texture-size", type=int, default=1024)
     ap.add_argument("--denoiser", default="neural", choices=["neural", "bmfr", "bfr"],
                     help="neural: U-Net with BMFR as variance-gate fallback (BMFR runs every frame)")
-    ap.add_argument("--gate-threshold", type=float, default=1.0,
+    ap.add_argument("--gate-threshold", type=float, default=0.5,
                     help="neural path: tiles whose predicted relative squared error exceeds this show BMFR")
     ap.add_argument("--weights", default=None, help="neural path: .npz of trained parameters (default: packaged)")
     ap.add_argument("--ref-spp", type=int, default=4096, help="samples of the relMSE reference render (0: skip)")
@@ -248,6 +248,11 @@ def relmse_eval(args, vp, pipe, g, illu, bmfr, neural, pc, cams, stream, dev):
             den["neural_gated"] = torch.where(px[..., None], den["bmfr"], nn_out)
             out["fallback_tiles"] = int(m.sum().item())
             out["tiles"] = int(m.numel())
+        neural.set_precision(8)  # calibrated during the FP8 timing
+        neural.dispatch(pc, stream)
+        torch.cuda.synchronize()
+        den["neural_fp8"] = neural.denoised.tensor()[..., :3].double().clone()
+        neural.set_precision(16)
     torch.cuda.synchronize()
     ref = torch.zeros_like(noisy)
     t0 = time.perf_counter()
@@ -297,8 +302,9 @@ def run_gb300(args):
         bmfr = den = vp.BMFR(W, H, 32, 32, g, acc_illu, abuf, 256)
     neural = None
     if args.denoiser == "neural":
-        neural = vp.NeuralDenoiser(W, H, g, illu, weights=args.weights, fallback=bmfr,
-                                   threshold=args.gate_threshold, tile=32)
+        # the network reads what BMFR reads: the accumulator's output and its sample counts
+        neural = vp.NeuralDenoiser(W, H, g, acc_illu, weights=args.weights, fallback=bmfr,
+                                   threshold=args.gate_threshold, tile=32, acc_buffer=abuf)
     pc = vp.PushConstants()
     stream = torch.cuda.current_stream(dev)
     cams = [orbit(sc, W, H, f) for f in range(16)]
@@ -360,6 +366,28 @@ def run_gb300(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(t.item())
 
+    # ---- the same frames with FP8 (e4m3) convolutions, calibrated on the current frame
+    fp8_ms = None
+    if neural is not None:
+        neural.calibrate(stream)
+        neural.set_precision(8)
+        for f in range(2):
+            frame(args.warmup + args.steps + f)
+        torch.cuda.synchronize()
+        ev[0].record(stream)
+        for i in range(args.steps):
+            frame(args.warmup + args.steps + 2 + i)
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+        fp8_ms = ev[0].elapsed_time(ev[1]) / args.steps
+        e0f, e1f = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0f.record(stream)
+        neural.dispatch(pc, stream)
+        e1f.record(stream)
+        torch.cuda.synchronize()
+        fp8_neural_ms = e0f.elapsed_time(e1f)
+        neural.set_precision(16)
+
     # ---- the BMFR-only path (no network) over the same frames, for the neural-vs-BMFR comparison
     bmfr_ms = None
     if neural is not None:
@@ -413,6 +441,7 @@ def run_gb300(args):
         e1.record(stream)
         torch.cuda.synchronize()
         stages["neural"] = e0.elapsed_time(e1)
+        stages["neural_fp8"] = fp8_neural_ms
     quality = None
     if args.ref_spp > 0 and rank == 0:
         quality = relmse_eval(args, vp, pipe, g, illu, bmfr, neural, pc, cams, stream, dev)
@@ -479,6 +508,7 @@ def run_gb300(args):
             "clocks": clocks,
             "gpu_launches": steps * (3 + 5 * (args.max_depth + 1) + 1 + 2 + (NEURAL_LAUNCHES if neural else 0)),
             "bmfr_path": None if bmfr_ms is None else {"fps": world * 1e3 / bmfr_ms, "ms_per_step": bmfr_ms},
+            "neural_fp8_path": None if fp8_ms is None else {"fps": world * 1e3 / fp8_ms, "ms_per_step": fp8_ms},
             "relmse": quality,
             "bvh": {"nodes": int(info.bvh_nodes), "depth": int(info.bvh_depth), "build_ms": info.build_ms},
         }

@@ -101,6 +101,7 @@ typedef struct PbrtScene PbrtScene;
 typedef struct PbrtPipeline PbrtPipeline;
 typedef struct PbrtNeural PbrtNeural;
 typedef struct PbrtTaa PbrtTaa;
+typedef struct PbrtBatch PbrtBatch;
 
 /* ---- library ---------------------------------------------------------- */
 PBRT_API const char* pbrt_version(void);
@@ -355,6 +356,49 @@ typedef struct PbrtStageTimes {
 } PbrtStageTimes;
 PBRT_API int pbrt_pipeline_profile(PbrtPipeline* p, const PbrtPushConstants* pc, pbrt_stream_t stream,
                                    PbrtStageTimes* out);
+/* Launch shape of the tracer: persistent traversal CTAs and shading CTAs per
+ * SM (1..16 each; default 8 and 8). No reference counterpart. */
+PBRT_API int pbrt_pipeline_set_launch(PbrtPipeline* p, int32_t trace_blocks_per_sm, int32_t shade_blocks_per_sm);
+
+/* ---- batched requests (no reference counterpart) -----------------------
+ * Many independent renders in one CUDA graph launch: each request names its
+ * own pipeline (scene, resolution, depth, G-buffer, illumination buffer),
+ * renders spp frames from pc (frame numbers pc.frame_number ...
+ * pc.frame_number + spp - 1) and, optionally, accumulates them with its
+ * accumulator (static camera: `camera` for both current and previous) and
+ * denoises the result with its BMFR. Requests run as `branches` concurrent
+ * chains, assigned longest first to the least loaded chain. A pipeline may
+ * appear in one request of a batch only. */
+typedef struct PbrtBatchRequest {
+  PbrtPipeline* pipeline;
+  PbrtAccumulator* accumulator; /* optional */
+  PbrtBMFR* bmfr;               /* optional; reads the accumulator's output */
+  PbrtPushConstants pc;
+  PbrtCameraMatrices camera;    /* with proj, when accumulated */
+  uint32_t spp;
+} PbrtBatchRequest;
+typedef struct PbrtBatchTuning {
+  uint32_t branches;            /* concurrent chains (1..64) */
+  uint32_t trace_blocks_per_sm; /* persistent traversal CTAs per SM */
+  uint32_t shade_blocks_per_sm;
+  uint32_t order;               /* 0: as added, 1: longest first */
+} PbrtBatchTuning;
+PBRT_API int pbrt_batch_create(PbrtBatch** out);
+PBRT_API int pbrt_batch_add(PbrtBatch* b, const PbrtBatchRequest* request);
+PBRT_API int pbrt_batch_size(const PbrtBatch* b, uint32_t* count);
+PBRT_API int pbrt_batch_set_tuning(PbrtBatch* b, const PbrtBatchTuning* tuning);
+PBRT_API int pbrt_batch_get_tuning(const PbrtBatch* b, PbrtBatchTuning* tuning);
+/* One graph launch of every request (captured on first use or after a change). */
+PBRT_API int pbrt_batch_submit(PbrtBatch* b, pbrt_stream_t stream);
+/* Times each candidate tuning on this batch (median of `repeats` launches
+ * after one warm-up) and keeps the fastest (stream-synchronising). */
+PBRT_API int pbrt_batch_autotune(PbrtBatch* b, pbrt_stream_t stream, int32_t repeats, PbrtBatchTuning* best,
+                                 float* best_ms);
+/* The chain assignment the batch uses (host only): assign[i] in
+ * 0..branches-1 for request costs[i]; order 1 = longest first onto the least
+ * loaded chain, 0 = in the given order. */
+PBRT_API int pbrt_batch_plan(const double* costs, uint32_t n, uint32_t branches, uint32_t order, uint32_t* assign);
+
 /* Failure handling without a GPU fault (no reference counterpart; the
  * reference has none). abort_flag: a pinned host word mapped into the
  * device; writing nonzero makes frames in flight and later frames stop
@@ -409,19 +453,33 @@ PBRT_API int pbrt_synth_texture(uint64_t seed, uint32_t size, int32_t kind, cons
 PBRT_API int pbrt_nn_conv3x3(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* w, const float* bias,
                              void* y, float* y32, int32_t n, int32_t h, int32_t w_px, int32_t cout, int32_t flags,
                              pbrt_stream_t stream);
+/* FP8 (e4m3) variant for inference: w8 [cout][9][c1+c2] e4m3 with per-output-
+ * channel scales wscale and the per-input-channel activation scales folded
+ * in (pbrt_nn_quantize_weights_fp8); BF16 inputs are quantised on load with
+ * inv_xscale [c1+c2] (saturating); c1 + c2 <= 256; flags bit 0: ReLU. */
+PBRT_API int pbrt_nn_conv3x3_fp8(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* w8,
+                                 const float* wscale, const float* inv_xscale, const float* bias, void* y, int32_t n,
+                                 int32_t h, int32_t w_px, int32_t cout, int32_t flags, pbrt_stream_t stream);
+/* wscale[co] = max |w x xscale| / 448 over the channel, w8 = e4m3(w x xscale / wscale). */
+PBRT_API int pbrt_nn_quantize_weights_fp8(const float* w, const float* xscale, int32_t cout, int32_t cin, void* w8,
+                                          float* wscale, pbrt_stream_t stream);
+/* amax[c] = max(amax[c], max over pixels |x[p][c]|), x BF16 [pixels][c]. */
+PBRT_API int pbrt_nn_channel_amax(const void* x, int64_t pixels, int32_t c, float* amax, pbrt_stream_t stream);
 /* dw [cout][9][c1+c2] FP32 += sum over pixels of dy (BF16) x im2col(input). */
 PBRT_API int pbrt_nn_conv3x3_wgrad(const void* dy, const void* x1, int32_t c1, const void* x2, int32_t c2, float* dw,
                                    int32_t n, int32_t h, int32_t w_px, int32_t cout, pbrt_stream_t stream);
 /* [cout][9][cin] -> [cin][9][cout], taps reversed (backward-data weights). */
 PBRT_API int pbrt_nn_flip_weights(const void* w, void* wt, int32_t cout, int32_t cin, pbrt_stream_t stream);
 /* Network input: 16 BF16 channels per padded pixel (log1p radiance, albedo,
- * normal, log1p depth / 8, zeros; edges replicated) and the noisy radiance
- * (FP32 rgb) from an illumination image (RGBA32F, or RGBA16F when
- * illum_is_half) and the G-buffer's albedo (RGBA8), normal (RG32F angles) and
- * depth (R32F) images, n_img images of w x h each, packed. */
+ * normal, log1p depth / 8, min(spp, 16) / 16, zeros; edges replicated) and
+ * the radiance the heads filter (FP32 rgb, clamped to [0, 10]) from an
+ * illumination image (RGBA32F, or RGBA16F when illum_is_half), the
+ * G-buffer's albedo (RGBA8), normal (RG32F angles) and depth (R32F) images
+ * and, optionally, the accumulation buffer's spp image (R8, 1/256 steps;
+ * null = one sample); n_img images of w x h each, packed. */
 PBRT_API int pbrt_nn_features(const void* illum, int32_t illum_is_half, const void* albedo, const void* normal,
-                              const void* depth, int32_t w, int32_t h, int32_t pw, int32_t ph, int32_t n_img,
-                              void* feat, float* rad, pbrt_stream_t stream);
+                              const void* depth, const void* spp, int32_t w, int32_t h, int32_t pw, int32_t ph,
+                              int32_t n_img, void* feat, float* rad, pbrt_stream_t stream);
 /* 2x2 average pooling (BF16 when is_f32 = 0, else FP32) and its backward (adds). */
 PBRT_API int pbrt_nn_avgpool2(const void* x, void* y, int32_t is_f32, int32_t n, int32_t h, int32_t w, int32_t c,
                               pbrt_stream_t stream);
@@ -467,17 +525,20 @@ PBRT_API int pbrt_nn_compose(const float* out, int32_t pw, int32_t w, int32_t h,
                              float* denoised_rgba32f, pbrt_stream_t stream);
 
 /* ---- neural denoiser render module (no reference counterpart) ---------
- * Reads the G-buffer and the 1-spp demodulated illumination image of
- * `illumination` (RGBA32F or RGBA16F) and writes a denoised RGBA32F image and
+ * Reads the G-buffer and the demodulated illumination image of
+ * `illumination` (RGBA32F or RGBA16F: one sample, or the accumulator's
+ * output) and writes a denoised RGBA32F image and
  * a B8G8R8A8 final image tone-mapped as BMFR's. Parameters: the flat FP32
  * vector of vulkanpbrt_gb300/kpunet.py (convolution weights [cout][9][cin]
  * in layer order, convolution biases, then per head weights [k][c] and
  * biases), pbrt_neural_param_count floats. The forward pass is captured in
  * a CUDA graph on the first dispatch. */
 PBRT_API int pbrt_neural_param_count(int64_t* count);
+/* acc (optional): the accumulation buffer whose spp image counts the samples
+ * behind `illumination` (the accumulator's output); null for 1-spp input. */
 PBRT_API int pbrt_neural_create(uint32_t width, uint32_t height, PbrtGBuffer* gbuffer,
-                                PbrtIlluminationBuffer* illumination, const float* params_host, int64_t count,
-                                PbrtNeural** out);
+                                PbrtIlluminationBuffer* illumination, PbrtAccumulationBuffer* acc,
+                                const float* params_host, int64_t count, PbrtNeural** out);
 PBRT_API int pbrt_neural_set_params(PbrtNeural* nd, const float* params_host, int64_t count);
 /* Variance gate: with bmfr given, every tile x tile block whose mean predicted
  * per-pixel relative squared error exceeds threshold shows BMFR's final image
@@ -485,6 +546,13 @@ PBRT_API int pbrt_neural_set_params(PbrtNeural* nd, const float* params_host, in
  * (bmfr must be dispatched before the neural module each frame); null bmfr
  * turns the gate off. */
 PBRT_API int pbrt_neural_set_fallback(PbrtNeural* nd, PbrtBMFR* bmfr, float threshold, int32_t tile);
+/* FP8 inference: calibrate runs one BF16 pass on the current inputs
+ * (stream-synchronising) and derives per-input-channel activation scales
+ * (max |x| / 448) and per-output-channel e4m3 weights; set_precision(8)
+ * then runs every convolution as e4m3 x e4m3 -> FP32 on the tensor cores,
+ * set_precision(16) returns to BF16. New parameters drop the calibration. */
+PBRT_API int pbrt_neural_calibrate(PbrtNeural* nd, pbrt_stream_t stream);
+PBRT_API int pbrt_neural_set_precision(PbrtNeural* nd, int32_t bits);
 PBRT_API int pbrt_neural_dispatch(PbrtNeural* nd, pbrt_stream_t stream);
 /* The same launches without the graph (for per-kernel profiling). */
 PBRT_API int pbrt_neural_dispatch_direct(PbrtNeural* nd, pbrt_stream_t stream);

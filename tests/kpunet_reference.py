@@ -21,8 +21,9 @@ def decode_normal(th, ph):
     return torch.stack([torch.cos(ph) * st, torch.sin(ph) * st, torch.cos(th)], -1)
 
 
-def features(illum, albedo, normal, depth, ph, pw):
-    """illum [N,h,w,4] f32, albedo [N,h,w,4] u8, normal [N,h,w,2], depth [N,h,w] -> feat [N,ph,pw,16], rad."""
+def features(illum, albedo, normal, depth, ph, pw, spp=None):
+    """illum [N,h,w,4] f32, albedo [N,h,w,4] u8, normal [N,h,w,2], depth [N,h,w], spp [N,h,w] u8 (1/256 steps)
+    -> feat [N,ph,pw,16], rad (clamped to [0, 10])."""
     n, h, w = illum.shape[:3]
     yi = torch.clamp(torch.arange(ph), max=h - 1)
     xi = torch.clamp(torch.arange(pw), max=w - 1)
@@ -30,11 +31,13 @@ def features(illum, albedo, normal, depth, ph, pw):
     def pad(t):
         return t[:, yi][:, :, xi]
 
-    c = pad(illum[..., :3].float()).clamp_min(0)
+    c = pad(illum[..., :3].float()).clamp(0, 10)
     a = pad(albedo[..., :3].float()) / 255.0
     nrm = decode_normal(pad(normal[..., 0]), pad(normal[..., 1]))
     d = torch.log1p(pad(depth).clamp_min(0)) * 0.125
-    f = torch.cat([torch.log1p(c), a, nrm, d[..., None], torch.zeros(n, ph, pw, 6)], -1)
+    s = (torch.full((n, ph, pw), 1.0 / 16) if spp is None
+         else (pad(spp.float()) / 255.0 * 256.0).clamp(max=16.0) / 16.0)
+    f = torch.cat([torch.log1p(c), a, nrm, d[..., None], s[..., None], torch.zeros(n, ph, pw, 5)], -1)
     return bf16(f), c
 
 

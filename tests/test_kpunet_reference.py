@@ -20,7 +20,7 @@ def test_parameter_layout_is_dense_and_ordered():
     p = K.init_params(0)
     assert p.size == total and np.isfinite(p).all()
     off, shape = lay["e0a.w"]
-    assert not p[off:off + int(np.prod(shape))].reshape(shape)[:, :, 10:].any()
+    assert not p[off:off + int(np.prod(shape))].reshape(shape)[:, :, 11:].any()
 
 
 def test_reference_gradient_matches_finite_differences():
@@ -57,7 +57,7 @@ def test_reference_gradient_matches_finite_differences():
         off, shape = lay[key]
         size = int(np.prod(shape))
         cand = off + rng.choice(size, 3, replace=False)
-        idx.extend(int(i) for i in cand if key != "e0a.w" or (i - off) % K.IN_CH < 10)
+        idx.extend(int(i) for i in cand if key != "e0a.w" or (i - off) % K.IN_CH < 11)
     eps = 1e-6
     for i in idx:
         fp = flat.detach().clone()

@@ -147,7 +147,32 @@ def test_trained_network_beats_bmfr_and_untrained(cuda):
     ref /= spp
     r = {k: relmse(v, ref, albedo) for k, v in
          {"1spp": noisy, "bmfr": den_bmfr, "untrained": den_un, "trained": den_nn}.items()}
+    # the same comparison on the accumulator's output after 8 static frames
+    accu = vp.Accumulator(g, illu, separate_matrices=True)
+    acc_illu, abuf = accu.accumulated_illumination, accu.accumulation_buffer
+    bmfr8 = vp.BMFR(W, H, 32, 32, g, acc_illu, abuf, 256)
+    nn8 = NeuralDenoiser(W, H, g, acc_illu, acc_buffer=abuf)
+    cm = vp.CameraMatrices(cam.view, cam.inv_view, cc.proj, cc.inv_proj)
+    for f in range(8):
+        pc.set(frame_number=5000 + f)
+        pipe.trace(pc)
+        accu.set_camera_matrices(f, cm, cm)
+        vp.lib().pbrt_accumulator_dispatch(accu.ptr, None)
+        bmfr8.dispatch(pc)
+        nn8.dispatch()
+        vp.lib().pbrt_accumulation_buffer_copy_to_back_images(abuf.ptr, g.ptr, acc_illu.ptr, None)
+    torch.cuda.synchronize()
+    r["bmfr_8frames"] = relmse(bmfr8.denoised.tensor()[(5007 & 1) ^ 1].float(), ref, albedo)
+    r["trained_8frames"] = relmse(nn8.denoised.tensor(), ref, albedo)
+    r["accumulated_8frames"] = relmse(acc_illu.illumination_images[0].tensor().float(), ref, albedo)
+    nn8.calibrate()
+    nn8.set_precision(8)
+    nn8.dispatch()
+    torch.cuda.synchronize()
+    r["trained_8frames_fp8"] = relmse(nn8.denoised.tensor(), ref, albedo)
     print("relMSE vs 1024 spp:", r)
+    assert r["trained_8frames_fp8"] < 1.25 * r["trained_8frames"] + 1e-3
     assert r["trained"] < r["bmfr"]
     assert r["trained"] < r["untrained"]
     assert r["trained"] < r["1spp"]
+    assert r["trained_8frames"] < r["bmfr_8frames"]

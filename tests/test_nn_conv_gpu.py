@@ -28,9 +28,12 @@ def _close(got, want, tol=4e-3):
     return err / scale, err <= tol * scale
 
 
+@pytest.mark.parametrize("kernel", ["halo", "kstep"])
 @pytest.mark.parametrize("n,h,w,c1,c2,cout", [(2, 24, 40, 16, 0, 32), (1, 32, 32, 32, 0, 48), (1, 16, 48, 48, 32, 48),
-                                             (2, 20, 36, 64, 0, 160), (1, 18, 34, 96, 128, 96)])
-def test_conv3x3_forward(cuda, n, h, w, c1, c2, cout):
+                                             (2, 20, 36, 64, 0, 160), (1, 18, 34, 96, 128, 96),
+                                             (1, 10, 22, 48, 64, 48), (1, 12, 16, 32, 48, 32),
+                                             (1, 8, 16, 128, 0, 128), (1, 9, 17, 16, 0, 64)])
+def test_conv3x3_forward(cuda, n, h, w, c1, c2, cout, kernel):
     import torch
 
     from vulkanpbrt_gb300 import nn
@@ -41,7 +44,7 @@ def test_conv3x3_forward(cuda, n, h, w, c1, c2, cout):
     wt = (torch.randn(cout, 9, c1 + c2, generator=g) * 0.1).bfloat16().to(cuda)
     b = torch.randn(cout, generator=g).float().to(cuda)
     y32 = torch.empty(n, h, w, cout, device=cuda)
-    y = nn.conv3x3(x1, wt, b, x2=x2, relu=False, out32=y32)
+    y = nn.conv3x3(x1, wt, b, x2=x2, relu=False, out32=y32, kernel=kernel)
     torch.cuda.synchronize()
     ref = _ref_conv(x1, wt, b, x2)
     rel, ok = _close(y32, ref, 1e-4)
@@ -49,7 +52,7 @@ def test_conv3x3_forward(cuda, n, h, w, c1, c2, cout):
     assert ok
     rel, ok = _close(y, ref, 4e-3)
     assert ok
-    yr = nn.conv3x3(x1, wt, b, x2=x2, relu=True)
+    yr = nn.conv3x3(x1, wt, b, x2=x2, relu=True, kernel=kernel)
     torch.cuda.synchronize()
     assert _close(yr, ref.clamp_min(0), 4e-3)[1]
 

@@ -38,6 +38,7 @@ COMMON = [
 # FP32 arithmetic.
 EXTRA = {
     "denoise.cu": ["-fmad=false"],
+    "taa.cu": ["-fmad=false"],
 }
 
 

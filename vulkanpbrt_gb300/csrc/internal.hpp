@@ -23,7 +23,8 @@ enum class Kind : uint32_t {
   Scene,
   Pipeline,
   Neural,
-  Taa
+  Taa,
+  Batch
 };
 
 struct Object {

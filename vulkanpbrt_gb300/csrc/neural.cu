@@ -11,6 +11,7 @@
 
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "internal.hpp"
 
@@ -76,6 +77,7 @@ struct PbrtNeural : pbrt::Object {
   uint32_t width = 0, height = 0, pw = 0, ph = 0;
   PbrtGBuffer* gbuffer = nullptr;
   PbrtIlluminationBuffer* illumination = nullptr;
+  PbrtAccumulationBuffer* acc = nullptr;  // optional: samples per pixel of accumulated input
   PbrtBMFR* fallback = nullptr;
   float threshold = 0.f;
   int32_t tile = 32;
@@ -91,6 +93,14 @@ struct PbrtNeural : pbrt::Object {
   pbrt::DeviceImage mask;  // R8 per gate tile: 1 = fallback
   uint32_t* counter = nullptr;
   cudaGraphExec_t graph = nullptr;
+  // FP8 inference (pbrt_neural_calibrate / pbrt_neural_set_precision)
+  int precision = 16;
+  bool calibrated = false;
+  uint8_t* w8 = nullptr;      // e4m3 convolution weights, lay.conv_w_total
+  float* wscale = nullptr;    // per output channel, all convolutions
+  float* xscale = nullptr;    // per input channel, all convolutions
+  float* inv_xscale = nullptr;
+  size_t wsoff[kNumConvs] = {}, xsoff[kNumConvs] = {}, n_wscale = 0, n_xscale = 0;
 };
 
 namespace {
@@ -109,7 +119,8 @@ int record_forward(PbrtNeural* nd, cudaStream_t s) {
   const int is_half = illum.view.format == PBRT_FORMAT_R16G16B16A16_SFLOAT;
   int st;
   if ((st = pbrt_nn_features(illum.view.data, is_half, nd->gbuffer->albedo.view.data, nd->gbuffer->normal.view.data,
-                             nd->gbuffer->depth.view.data, nd->width, nd->height, PW, PH, n, nd->feat, nd->rad[0], s)))
+                             nd->gbuffer->depth.view.data, nd->acc ? nd->acc->spp.view.data : nullptr, nd->width,
+                             nd->height, PW, PH, n, nd->feat, nd->rad[0], s)))
     return st;
   if ((st = pbrt_nn_avgpool2(nd->rad[0], nd->rad[1], 1, n, PH, PW, 3, s))) return st;
   if ((st = pbrt_nn_avgpool2(nd->rad[1], nd->rad[2], 1, n, PH / 2, PW / 2, 3, s))) return st;
@@ -124,10 +135,13 @@ int record_forward(PbrtNeural* nd, cudaStream_t s) {
       if ((st = pbrt_nn_avgpool2(x, nd->pool[c.level], 0, n, h * 2, w * 2, kConvs[i - 1].cout, s))) return st;
       x = nd->pool[c.level];
     }
-    if (c.c2) {
-      st = pbrt_nn_conv3x3(nd->act[skip_of[c.level]], c.c1, x, c.c2, w16, b, nd->act[i], nullptr, n, h, w, c.cout, 1, s);
+    const bf16* in1 = c.c2 ? nd->act[skip_of[c.level]] : x;
+    const bf16* in2 = c.c2 ? x : nullptr;
+    if (nd->precision == 8) {
+      st = pbrt_nn_conv3x3_fp8(in1, c.c1, in2, c.c2, nd->w8 + nd->lay.conv_w[i], nd->wscale + nd->wsoff[i],
+                               nd->inv_xscale + nd->xsoff[i], b, nd->act[i], n, h, w, c.cout, 1, s);
     } else {
-      st = pbrt_nn_conv3x3(x, c.c1, nullptr, 0, w16, b, nd->act[i], nullptr, n, h, w, c.cout, 1, s);
+      st = pbrt_nn_conv3x3(in1, c.c1, in2, c.c2, w16, b, nd->act[i], nullptr, n, h, w, c.cout, 1, s);
     }
     if (st) return st;
     x = nd->act[i];
@@ -172,12 +186,17 @@ PbrtNeural::~PbrtNeural() {
   for (auto* p : rad) cudaFree(p);
   for (auto* p : out) cudaFree(p);
   cudaFree(counter);
+  cudaFree(w8);
+  cudaFree(wscale);
+  cudaFree(xscale);
+  cudaFree(inv_xscale);
   variance.free_();
   denoised.free_();
   final_image.free_();
   mask.free_();
   release(gbuffer);
   release(illumination);
+  release(acc);
   release(fallback);
 }
 
@@ -194,6 +213,11 @@ PBRT_API int pbrt_neural_set_params(PbrtNeural* nd, const float* params_host, in
     return fail(PBRT_ERROR_INVALID_ARGUMENT, "neural set params: expected %lld parameters, got %lld",
                 (long long)(nd ? nd->lay.total : 0), (long long)count);
   PBRT_CUDA(cudaMemcpy(nd->params, params_host, nd->lay.total * sizeof(float), cudaMemcpyHostToDevice));
+  nd->calibrated = false;
+  if (nd->precision == 8) {
+    nd->precision = 16;
+    drop_graph(nd);
+  }
   to_bf16_kernel<<<256, 256>>>(nd->params, nd->w16, nd->lay.conv_w_total);
   int st = check_launch("to_bf16_kernel");
   if (st) return st;
@@ -202,9 +226,13 @@ PBRT_API int pbrt_neural_set_params(PbrtNeural* nd, const float* params_host, in
 }
 
 PBRT_API int pbrt_neural_create(uint32_t width, uint32_t height, PbrtGBuffer* g, PbrtIlluminationBuffer* illu,
-                                const float* params_host, int64_t count, PbrtNeural** out) {
-  if (!out || !checked<PbrtGBuffer>(g, Kind::GBuffer) || !checked<PbrtIlluminationBuffer>(illu, Kind::Illumination))
+                                PbrtAccumulationBuffer* acc, const float* params_host, int64_t count,
+                                PbrtNeural** out) {
+  if (!out || !checked<PbrtGBuffer>(g, Kind::GBuffer) || !checked<PbrtIlluminationBuffer>(illu, Kind::Illumination) ||
+      (acc && !checked<PbrtAccumulationBuffer>(acc, Kind::Accumulation)))
     return fail(PBRT_ERROR_INVALID_ARGUMENT, "neural create: bad arguments");
+  if (acc && (acc->width != width || acc->height != height))
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "neural create: accumulation buffer size differs");
   *out = nullptr;
   if (g->width != width || g->height != height || illu->width != width || illu->height != height || width < 16 ||
       height < 16)
@@ -221,12 +249,22 @@ PBRT_API int pbrt_neural_create(uint32_t width, uint32_t height, PbrtGBuffer* g,
   nd->ph = (height + 15) / 16 * 16;
   retain(g);
   retain(illu);
+  if (acc) retain(acc);
   nd->gbuffer = g;
   nd->illumination = illu;
+  nd->acc = acc;
   const size_t P = (size_t)nd->pw * nd->ph;
   int st;
+  for (int i = 0; i < kNumConvs; ++i) {
+    nd->wsoff[i] = nd->n_wscale;
+    nd->n_wscale += kConvs[i].cout;
+    nd->xsoff[i] = nd->n_xscale;
+    nd->n_xscale += kConvs[i].c1 + kConvs[i].c2;
+  }
   if ((st = dalloc(&nd->params, nd->lay.total)) || (st = dalloc(&nd->w16, nd->lay.conv_w_total)) ||
-      (st = dalloc(&nd->feat, P * 16)) || (st = dalloc(&nd->counter, 1))) {
+      (st = dalloc(&nd->feat, P * 16)) || (st = dalloc(&nd->counter, 1)) ||
+      (st = dalloc(&nd->w8, nd->lay.conv_w_total)) || (st = dalloc(&nd->wscale, nd->n_wscale)) ||
+      (st = dalloc(&nd->xscale, nd->n_xscale)) || (st = dalloc(&nd->inv_xscale, nd->n_xscale))) {
     delete nd;
     return st;
   }
@@ -291,6 +329,66 @@ PBRT_API int pbrt_neural_dispatch(PbrtNeural* nd, pbrt_stream_t stream) {
 PBRT_API int pbrt_neural_dispatch_direct(PbrtNeural* nd, pbrt_stream_t stream) {
   if (!checked<PbrtNeural>(nd, Kind::Neural)) return fail(PBRT_ERROR_INVALID_ARGUMENT, "neural dispatch: not a handle");
   return record_forward(nd, stream);
+}
+
+// FP8 calibration: one BF16 forward pass on the current inputs, the
+// per-channel maximum |x| of every convolution's input, sx = amax / 448
+// (e4m3's largest finite value), then the per-output-channel FP8 weights
+// with sx folded in.
+PBRT_API int pbrt_neural_calibrate(PbrtNeural* nd, pbrt_stream_t stream) {
+  if (!checked<PbrtNeural>(nd, Kind::Neural)) return fail(PBRT_ERROR_INVALID_ARGUMENT, "neural calibrate: not a handle");
+  const int saved = nd->precision;
+  nd->precision = 16;
+  int st = record_forward(nd, stream);
+  nd->precision = saved;
+  if (st) return st;
+  PBRT_CUDA(cudaMemsetAsync(nd->xscale, 0, nd->n_xscale * sizeof(float), stream));
+  const size_t P = (size_t)nd->pw * nd->ph;
+  const int skip_of[4] = {1, 3, 5, 7};
+  for (int i = 0; i < kNumConvs && !st; ++i) {
+    const ConvSpec& c = kConvs[i];
+    const long px = (long)(P >> (2 * c.level));
+    const bf16* in1;
+    const bf16* in2 = nullptr;
+    if (i == 0) in1 = nd->feat;
+    else if (c.c2) {
+      in1 = nd->act[skip_of[c.level]];
+      in2 = nd->act[i - 1];
+    } else if (i < 10 && c.name[2] == 'a') in1 = nd->pool[c.level];
+    else in1 = nd->act[i - 1];
+    st = pbrt_nn_channel_amax(in1, px, c.c1, nd->xscale + nd->xsoff[i], stream);
+    if (!st && in2) st = pbrt_nn_channel_amax(in2, px / 4, c.c2, nd->xscale + nd->xsoff[i] + c.c1, stream);
+  }
+  if (st) return st;
+  std::vector<float> amax(nd->n_xscale), sx(nd->n_xscale), inv(nd->n_xscale);
+  PBRT_CUDA(cudaMemcpyAsync(amax.data(), nd->xscale, amax.size() * sizeof(float), cudaMemcpyDeviceToHost, stream));
+  PBRT_CUDA(cudaStreamSynchronize(stream));
+  for (size_t k = 0; k < amax.size(); ++k) {
+    sx[k] = amax[k] > 0.f ? amax[k] / 448.f : 1.f;
+    inv[k] = 1.f / sx[k];
+  }
+  PBRT_CUDA(cudaMemcpyAsync(nd->xscale, sx.data(), sx.size() * sizeof(float), cudaMemcpyHostToDevice, stream));
+  PBRT_CUDA(cudaMemcpyAsync(nd->inv_xscale, inv.data(), inv.size() * sizeof(float), cudaMemcpyHostToDevice, stream));
+  for (int i = 0; i < kNumConvs && !st; ++i)
+    st = pbrt_nn_quantize_weights_fp8(nd->params + nd->lay.conv_w[i], nd->xscale + nd->xsoff[i], kConvs[i].cout,
+                                      kConvs[i].c1 + kConvs[i].c2, nd->w8 + nd->lay.conv_w[i],
+                                      nd->wscale + nd->wsoff[i], stream);
+  if (st) return st;
+  PBRT_CUDA(cudaStreamSynchronize(stream));
+  nd->calibrated = true;
+  return PBRT_OK;
+}
+
+PBRT_API int pbrt_neural_set_precision(PbrtNeural* nd, int32_t bits) {
+  if (!checked<PbrtNeural>(nd, Kind::Neural) || (bits != 16 && bits != 8))
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "neural set precision: 16 (BF16) or 8 (FP8 e4m3)");
+  if (bits == 8 && !nd->calibrated)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "neural set precision: FP8 needs pbrt_neural_calibrate first");
+  if (nd->precision != bits) {
+    nd->precision = bits;
+    drop_graph(nd);
+  }
+  return PBRT_OK;
 }
 
 PBRT_API int pbrt_neural_final_image(const PbrtNeural* nd, PbrtImage* out) {

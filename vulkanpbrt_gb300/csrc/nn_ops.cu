@@ -20,26 +20,31 @@ constexpr int kKP = 25;  // 5x5 kernel taps
 
 // Network input (16 BF16 channels at the padded size PH x PW; edge pixels
 // replicated): log1p(illumination rgb), albedo rgb, normal xyz (decoded from
-// the G-buffer's spherical angles), log1p(depth) / 8, zeros. Also the
-// noisy illumination itself (FP32 rgb) for the kernel-prediction heads.
+// the G-buffer's spherical angles), log1p(depth) / 8, samples per pixel
+// (min(spp, 16) / 16, from the accumulation buffer's R8 spp image in the
+// accumulator's 1/256 steps; one sample without it), zeros. Also the
+// illumination the kernel-prediction heads filter (FP32 rgb), clamped to
+// [0, 10] as BMFR clamps its output (shaders/bmfrPost.comp:99).
+constexpr float kRadianceClamp = 10.f;
 __global__ void features_kernel(const float4* __restrict__ illum32, const Half4* __restrict__ illum16,
                                 const uchar4* __restrict__ albedo, const float2* __restrict__ normal,
-                                const float* __restrict__ depth, int W, int H, int PW, int PH, int n_img,
-                                bf16* __restrict__ feat, float* __restrict__ rad) {
+                                const float* __restrict__ depth, const uint8_t* __restrict__ spp, int W, int H, int PW,
+                                int PH, int n_img, bf16* __restrict__ feat, float* __restrict__ rad) {
   const long total = (long)n_img * PH * PW;
   GRID_STRIDE(i, total) {
     const int x = (int)(i % PW), y = (int)((i / PW) % PH), n = (int)(i / ((long)PW * PH));
     const int sx = min(x, W - 1), sy = min(y, H - 1);
     const size_t p = ((size_t)n * H + sy) * W + sx;
     float4 c = illum32 ? illum32[p] : load_half4(illum16 + p);
-    c.x = fmaxf(c.x, 0.f);
-    c.y = fmaxf(c.y, 0.f);
-    c.z = fmaxf(c.z, 0.f);
+    c.x = fminf(fmaxf(c.x, 0.f), kRadianceClamp);
+    c.y = fminf(fmaxf(c.y, 0.f), kRadianceClamp);
+    c.z = fminf(fmaxf(c.z, 0.f), kRadianceClamp);
     const uchar4 a = albedo[p];
     const float2 th = normal[p];
     const float3 nn3 = decode_normal(th.x, th.y);
+    const float s = spp ? fminf((float)spp[p] / 255.f * 256.f, 16.f) / 16.f : 1.f / 16.f;
     float f[16] = {log1pf(c.x), log1pf(c.y), log1pf(c.z), a.x / 255.f, a.y / 255.f, a.z / 255.f, nn3.x, nn3.y,
-                   nn3.z, log1pf(fmaxf(depth[p], 0.f)) * 0.125f, 0, 0, 0, 0, 0, 0};
+                   nn3.z, log1pf(fmaxf(depth[p], 0.f)) * 0.125f, s, 0, 0, 0, 0, 0};
     bf16* o = feat + i * 16;
 #pragma unroll
     for (int k = 0; k < 16; k += 2) *reinterpret_cast<__nv_bfloat162*>(o + k) = __floats2bfloat162_rn(f[k], f[k + 1]);
@@ -405,14 +410,15 @@ inline int grid_for(long n, int block = 256) { return (int)std::min<long>((n + b
 extern "C" {
 
 PBRT_API int pbrt_nn_features(const void* illum, int32_t illum_is_half, const void* albedo, const void* normal,
-                              const void* depth, int32_t w, int32_t h, int32_t pw, int32_t ph, int32_t n_img,
-                              void* feat, float* rad, pbrt_stream_t s) {
+                              const void* depth, const void* spp, int32_t w, int32_t h, int32_t pw, int32_t ph,
+                              int32_t n_img, void* feat, float* rad, pbrt_stream_t s) {
   if (!illum || !albedo || !normal || !depth || !feat || !rad || pw < w || ph < h || w <= 0 || h <= 0 || n_img <= 0)
     return fail(PBRT_ERROR_INVALID_ARGUMENT, "nn features: bad arguments");
   const long total = (long)n_img * ph * pw;
   features_kernel<<<grid_for(total), 256, 0, s>>>(illum_is_half ? nullptr : (const float4*)illum,
                                                   illum_is_half ? (const Half4*)illum : nullptr, (const uchar4*)albedo,
-                                                  (const float2*)normal, (const float*)depth, w, h, pw, ph, n_img,
+                                                  (const float2*)normal, (const float*)depth, (const uint8_t*)spp, w, h,
+                                                  pw, ph, n_img,
                                                   (bf16*)feat, rad);
   return check_launch("features_kernel");
 }

@@ -123,7 +123,19 @@ struct TravState {
   int best_tri;  // BVH-order triangle slot, -1 = miss
   float tbest, bu, bv;
   uint32_t best_key;
+  uint32_t tri_base, tri_mask;  // deferred triangles of the last node visited (kTraversalDeferTris)
 };
+constexpr uint32_t kNoNode = 0xffffffffu;
+
+// Traversal step shape. 0: a node visit tests the triangles of every hit
+// leaf child at once. 1: a node visit records them as a mask and the lane
+// tests one triangle per step until the mask is empty, so lanes of a warp
+// doing node visits and lanes doing triangle tests each do one unit per step
+// (the triangle/node separation of Ylitie, Karras & Laine, HPG 2017).
+#ifndef PBRT_TRAVERSAL_DEFER_TRIS
+#define PBRT_TRAVERSAL_DEFER_TRIS 1
+#endif
+constexpr int kTraversalDeferTris = PBRT_TRAVERSAL_DEFER_TRIS;
 
 // Visits st.node: box-tests its children, intersects the triangles of the
 // leaf children that are hit, and moves to the nearest inner child (octant
@@ -221,6 +233,125 @@ PBRT_D bool visit_node(const SceneView& sc, const RayPre& r, float tmin, TravSta
   if (m) stack[st.sp++] = make_uint2(g.x, (im << 8) | m);
   st.node = g.x + __popc(im & ((1u << s) - 1u));
   return true;
+}
+
+// Deferred form: box-tests st.node's children, records the triangles of the
+// hit leaf children in st.tri_mask and moves to the next node (kNoNode when
+// the stack is empty). The ray is finished when both are exhausted.
+template <bool POP>
+PBRT_D void visit_node_deferred(const SceneView& sc, const RayPre& r, float tmin, TravState& st, uint2* stack,
+                                int& err, uint32_t& n_nodes) {
+  const float4* nodes4 = reinterpret_cast<const float4*>(sc.nodes);
+  const uint32_t node = st.node;
+  ++n_nodes;
+  const float4 n0 = __ldg(nodes4 + 5 * node + 0);
+  const float4 n1 = __ldg(nodes4 + 5 * node + 1);
+  const float4 n2 = __ldg(nodes4 + 5 * node + 2);
+  const float4 n3 = __ldg(nodes4 + 5 * node + 3);
+  const float4 n4 = __ldg(nodes4 + 5 * node + 4);
+  const uint32_t emi = __float_as_uint(n0.w);
+  const uint32_t imask = emi >> 24;
+  const uint32_t child_base = __float_as_uint(n1.x), tri_base = __float_as_uint(n1.y);
+  const uint32_t meta_lo = __float_as_uint(n1.z), meta_hi = __float_as_uint(n1.w);
+  const float adx = (n0.x - r.o.x) * r.inv.x, ady = (n0.y - r.o.y) * r.inv.y, adz = (n0.z - r.o.z) * r.inv.z;
+  const float scx = __uint_as_float(((emi >> 0) & 0xffu) << 23) * r.inv.x;
+  const float scy = __uint_as_float(((emi >> 8) & 0xffu) << 23) * r.inv.y;
+  const float scz = __uint_as_float(((emi >> 16) & 0xffu) << 23) * r.inv.z;
+  uint32_t inner = 0, tris = 0;
+#pragma unroll
+  for (int s = 0; s < 8; ++s) {
+    const int sh = 8 * (s & 3);
+    const uint32_t meta = ((s < 4 ? meta_lo : meta_hi) >> sh) & 0xffu;
+    const float lx = (float)((__float_as_uint(s < 4 ? n2.x : n2.y) >> sh) & 0xffu);
+    const float ly = (float)((__float_as_uint(s < 4 ? n2.z : n2.w) >> sh) & 0xffu);
+    const float lz = (float)((__float_as_uint(s < 4 ? n3.x : n3.y) >> sh) & 0xffu);
+    const float hx = (float)((__float_as_uint(s < 4 ? n3.z : n3.w) >> sh) & 0xffu);
+    const float hy = (float)((__float_as_uint(s < 4 ? n4.x : n4.y) >> sh) & 0xffu);
+    const float hz = (float)((__float_as_uint(s < 4 ? n4.z : n4.w) >> sh) & 0xffu);
+    const float tx0 = fmaf(lx, scx, adx), tx1 = fmaf(hx, scx, adx);
+    const float ty0 = fmaf(ly, scy, ady), ty1 = fmaf(hy, scy, ady);
+    const float tz0 = fmaf(lz, scz, adz), tz1 = fmaf(hz, scz, adz);
+    float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
+    float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), st.tbest));
+    tn = tn - fabsf(tn) * 4e-7f;
+    tf = tf + fabsf(tf) * 4e-7f;
+    const bool hit = meta != 0 && tn <= tf;
+    if (hit) {
+      if (meta & 0x80u) inner |= 1u << (s ^ r.oct);
+      else tris |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);  // <= 8 leaves x 3 triangles: bits 0..23
+    }
+  }
+  st.tri_base = tri_base;
+  st.tri_mask = tris;
+  if (inner) {
+    const int k = __ffs(inner) - 1;
+    inner &= inner - 1;
+    const int s = k ^ r.oct;
+    if (inner) {
+      if (st.sp == kStackSize) {
+        err = 1;
+        st.node = kNoNode;
+        st.tri_mask = 0;
+        return;
+      }
+      stack[st.sp++] = make_uint2(child_base, (imask << 8) | inner);
+    }
+    st.node = child_base + __popc(imask & ((1u << s) - 1u));
+    return;
+  }
+  if (!POP || st.sp == 0) {
+    st.node = kNoNode;
+    return;
+  }
+  uint2 g = stack[--st.sp];
+  uint32_t m = g.y & 0xffu;
+  const uint32_t im = g.y >> 8;
+  const int k = __ffs(m) - 1;
+  m &= m - 1;
+  const int s = k ^ r.oct;
+  if (m) stack[st.sp++] = make_uint2(g.x, (im << 8) | m);
+  st.node = g.x + __popc(im & ((1u << s) - 1u));
+}
+
+// Postponing form (mode 2): a node visit leaves st.node = kNoNode when no
+// inner child is hit instead of popping; the pop is a step of its own, and a
+// stack entry with bit 31 set is a postponed triangle group.
+PBRT_D void pop_group(const RayPre& r, TravState& st, uint2* stack) {
+  uint2 g = stack[--st.sp];
+  if (g.y & 0x80000000u) {
+    st.tri_base = g.x;
+    st.tri_mask = g.y & 0x7fffffffu;
+    return;
+  }
+  uint32_t m = g.y & 0xffu;
+  const uint32_t im = g.y >> 8;
+  const int k = __ffs(m) - 1;
+  m &= m - 1;
+  const int s = k ^ r.oct;
+  if (m) stack[st.sp++] = make_uint2(g.x, (im << 8) | m);
+  st.node = g.x + __popc(im & ((1u << s) - 1u));
+}
+
+// Tests the lowest triangle of st.tri_mask. Returns true for an accepted
+// any-hit (the ray is finished).
+template <bool ANY_HIT>
+PBRT_D bool test_one_triangle(const SceneView& sc, const RayPre& r, float tmin, TravState& st, uint32_t& n_tris) {
+  const int b = __ffs(st.tri_mask) - 1;
+  st.tri_mask &= st.tri_mask - 1;
+  const uint32_t ti = st.tri_base + (uint32_t)b;
+  const float4 a = __ldg(sc.tris + 3 * ti), bb = __ldg(sc.tris + 3 * ti + 1), c = __ldg(sc.tris + 3 * ti + 2);
+  ++n_tris;
+  float t, u, v;
+  if (!tri_intersect(r, a, bb, c, tmin, t, u, v)) return false;
+  const uint32_t key = __float_as_uint(a.w);
+  if (!(t < st.tbest || (t == st.tbest && key < st.best_key))) return false;
+  if (sc.any_alpha && !alpha_accept_call(sc, __float_as_uint(bb.w), __float_as_uint(c.w), u, v)) return false;
+  st.best_tri = (int)ti;
+  st.tbest = t;
+  st.bu = u;
+  st.bv = v;
+  st.best_key = key;
+  return ANY_HIT;
 }
 
 // ---------------------------------------------------------------------------
@@ -463,14 +594,41 @@ __global__ void __launch_bounds__(128, 8) k_traverse(SceneView sc, Queues q, Cou
         st.tbest = d.w;
         st.bu = st.bv = 0.f;
         st.best_key = 0xffffffffu;
+        st.tri_mask = 0;
       }
       batch_next += min((uint32_t)__popc(need), avail);
       need = __ballot_sync(kFullMask, idx < 0);
     }
     if (__all_sync(kFullMask, idx < 0)) break;
-    if (idx < 0) continue;
-    // ---- one node of this lane's ray
-    if (visit_node<ANY>(sc, r, tmin, st, stack, err, nn, nt)) continue;
+    // ---- one step of this lane's ray
+    if (kTraversalDeferTris == 2) {
+      // postpone triangles while fewer than a quarter of the busy lanes have some
+      const bool busy = idx >= 0;
+      const unsigned act = __ballot_sync(kFullMask, busy);
+      const unsigned trl = __ballot_sync(kFullMask, busy && st.tri_mask != 0);
+      if (!busy) continue;
+      if (st.tri_mask && st.node != kNoNode && 4 * __popc(trl) < __popc(act) && st.sp < kStackSize) {
+        stack[st.sp++] = make_uint2(st.tri_base, st.tri_mask | 0x80000000u);
+        st.tri_mask = 0;
+      }
+      bool done = false;
+      if (st.tri_mask) done = test_one_triangle<ANY>(sc, r, tmin, st, nt);
+      else if (st.node != kNoNode) visit_node_deferred<false>(sc, r, tmin, st, stack, err, nn);
+      else pop_group(r, st, stack);
+      if (!done && (st.tri_mask || st.node != kNoNode || st.sp > 0)) continue;
+    } else if (kTraversalDeferTris == 1) {
+      if (idx < 0) continue;
+      if (st.tri_mask) {
+        if (!test_one_triangle<ANY>(sc, r, tmin, st, nt) && (st.tri_mask || st.node != kNoNode)) continue;
+      } else {
+        visit_node_deferred<true>(sc, r, tmin, st, stack, err, nn);
+        if (st.tri_mask || st.node != kNoNode) continue;
+      }
+    } else if (idx < 0) {
+      continue;
+    } else if (visit_node<ANY>(sc, r, tmin, st, stack, err, nn, nt)) {
+      continue;
+    }
     // ---- ray finished
     if (MODE == 0) {
       q.hit[idx] = make_float4(st.tbest, st.bu, st.bv, __int_as_float(st.best_tri));
@@ -643,7 +801,14 @@ PBRT_D float3 sample_light(const SceneView& sc, int mode, float3 pos, float3 n, 
 }
 
 // One bounce of shading for every entry of ray queue k&1.
-__global__ void __launch_bounds__(128) k_shade(SceneView sc, const FrameParams* __restrict__ fpp, Queues q,
+// Shading CTAs resident per SM the register allocation targets (a build
+// knob: more CTAs, fewer registers per thread).
+#ifdef PBRT_SHADE_MIN_BLOCKS
+#define PBRT_SHADE_BOUNDS __launch_bounds__(128, PBRT_SHADE_MIN_BLOCKS)
+#else
+#define PBRT_SHADE_BOUNDS __launch_bounds__(128)
+#endif
+__global__ void PBRT_SHADE_BOUNDS k_shade(SceneView sc, const FrameParams* __restrict__ fpp, Queues q,
                                                Counters* c, GBufferOut g, int k) {
   const FrameParams& fp = *fpp;
   if (*((volatile uint32_t*)&c->stop)) return;  // stopped frame: shade nothing, queue nothing
@@ -899,7 +1064,8 @@ struct PbrtPipeline : pbrt::Object {
   FrameParams* dev_fp = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   int graph_depth = -1;
-  int grid_persistent = 0;
+  int grid_persistent = 0;  // traversal CTAs (persistent warps)
+  int grid_shade = 0;       // shading CTAs (grid-stride)
   uint32_t* abort_host = nullptr;  // mapped pinned word (pbrt_pipeline_abort_flag)
   uint32_t* abort_dev = nullptr;
   unsigned long long budget_ns = 0;
@@ -951,7 +1117,7 @@ static int record_frame(PbrtPipeline* pp, cudaStream_t s, StageEvents* ev) {
     k_traverse<0><<<pp->grid_persistent, 128, 0, s>>>(sc, pp->q, pp->ctr, k, QueryIO{});
     if (ev) ev->end(1);
     if (ev) ev->begin(2);
-    k_shade<<<pp->grid_persistent, 128, 0, s>>>(sc, pp->dev_fp, pp->q, pp->ctr, g, k);
+    k_shade<<<pp->grid_shade, 128, 0, s>>>(sc, pp->dev_fp, pp->q, pp->ctr, g, k);
     if (ev) ev->end(2);
     if (ev) ev->begin(3);
     k_traverse<1><<<pp->grid_persistent, 128, 0, s>>>(sc, pp->q, pp->ctr, k, QueryIO{});
@@ -1262,6 +1428,7 @@ PBRT_API int pbrt_pipeline_create(PbrtScene* scene, PbrtGBuffer* g, PbrtIllumina
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     pp->grid_persistent = sms * 8;  // 8 resident 128-thread CTAs per SM at <= 64 registers
+    pp->grid_shade = sms * 8;
   }
   if (st) {
     delete pp;
@@ -1443,6 +1610,279 @@ PBRT_API int pbrt_pipeline_debug_images(const PbrtPipeline* pp, PbrtImage* prima
     im.row_bytes = (size_t)pp->W * 4;
     im.layer_bytes = im.row_bytes * pp->H;
   }
+  return PBRT_OK;
+}
+
+
+PBRT_API int pbrt_pipeline_set_launch(PbrtPipeline* pp, int32_t trace_blocks_per_sm, int32_t shade_blocks_per_sm) {
+  if (!checked<PbrtPipeline>(pp, Kind::Pipeline) || trace_blocks_per_sm < 1 || trace_blocks_per_sm > 16 ||
+      shade_blocks_per_sm < 1 || shade_blocks_per_sm > 16)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "set launch: blocks per SM must be in 1..16");
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (pp->grid_persistent != sms * trace_blocks_per_sm || pp->grid_shade != sms * shade_blocks_per_sm) {
+    pp->grid_persistent = sms * trace_blocks_per_sm;
+    pp->grid_shade = sms * shade_blocks_per_sm;
+    pp->graph_depth = -1;  // the frame graph is recaptured on the next trace
+  }
+  return PBRT_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Batched requests: many independent renders (own pipeline -- scene,
+// resolution, depth -- own sample count, optional accumulator and BMFR) in
+// one CUDA graph launch. The graph forks into `branches` concurrent chains;
+// requests are assigned to chains longest-first onto the least loaded chain
+// (cost = pixels x samples x (max depth + 1)), so small requests fill the GPU
+// beside large ones. Frame parameters are baked into the captured launches;
+// the graph is recaptured when the request list or the tuning changes.
+// No reference counterpart (the reference renders one view per frame).
+struct PbrtBatch : pbrt::Object {
+  PbrtBatch() : Object(pbrt::Kind::Batch) {}
+  ~PbrtBatch() override {
+    drop();
+    for (auto& r : reqs) {
+      release(r.pipeline);
+      release(r.accumulator);
+      release(r.bmfr);
+    }
+  }
+  std::vector<PbrtBatchRequest> reqs;
+  PbrtBatchTuning tuning{4, 8, 8, 1};
+  cudaGraphExec_t exec = nullptr;
+  void drop() {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+  }
+};
+
+namespace {
+
+double request_cost(const PbrtBatchRequest& r) {
+  return (double)r.pipeline->W * r.pipeline->H * (double)std::max<uint32_t>(r.spp, 1) *
+         (double)(r.pipeline->max_depth + 1);
+}
+
+// Requests of one request's frames: set params, trace, accumulate,
+// copy-to-back; then BMFR once.
+int record_request(const PbrtBatchRequest& r, cudaStream_t s) {
+  PbrtPipeline* pp = r.pipeline;
+  const uint32_t spp = std::max<uint32_t>(r.spp, 1);
+  int st = PBRT_OK;
+  for (uint32_t k = 0; k < spp && !st; ++k) {
+    PbrtPushConstants pc = r.pc;
+    pc.frame_number = r.pc.frame_number + k;
+    k_set_params<<<1, 1, 0, s>>>(pp->dev_fp, frame_params(pp, &pc));
+    if ((st = check_launch("k_set_params"))) break;
+    if ((st = record_frame(pp, s, nullptr))) break;
+    if (r.accumulator) {
+      if ((st = pbrt_accumulator_set_camera_matrices(r.accumulator, (int32_t)k, &r.camera, &r.camera))) break;
+      if ((st = pbrt_accumulator_dispatch(r.accumulator, s))) break;
+      PbrtIlluminationBuffer* acc_illu = nullptr;
+      PbrtAccumulationBuffer* ab = nullptr;
+      pbrt_accumulator_get_accumulated_illumination(r.accumulator, &acc_illu);
+      pbrt_accumulator_get_accumulation_buffer(r.accumulator, &ab);
+      if ((st = pbrt_accumulation_buffer_copy_to_back_images(ab, pp->gbuffer, acc_illu, s))) break;
+    }
+  }
+  if (!st && r.bmfr) {
+    PbrtPushConstants pc = r.pc;
+    pc.frame_number = r.pc.frame_number + spp - 1;
+    st = pbrt_bmfr_dispatch(r.bmfr, &pc, s);
+  }
+  return st;
+}
+
+int capture_batch(PbrtBatch* b) {
+  const uint32_t nb = std::max<uint32_t>(1, std::min<uint32_t>(b->tuning.branches, (uint32_t)b->reqs.size()));
+  std::vector<uint32_t> assign(b->reqs.size());
+  std::vector<double> costs(b->reqs.size());
+  for (size_t i = 0; i < b->reqs.size(); ++i) costs[i] = request_cost(b->reqs[i]);
+  int st = pbrt_batch_plan(costs.data(), (uint32_t)costs.size(), nb, b->tuning.order, assign.data());
+  if (st) return st;
+  for (auto& r : b->reqs) {
+    if ((st = pbrt_pipeline_set_launch(r.pipeline, (int32_t)b->tuning.trace_blocks_per_sm,
+                                       (int32_t)b->tuning.shade_blocks_per_sm)))
+      return st;
+  }
+  std::vector<cudaStream_t> br(nb, nullptr);
+  std::vector<cudaEvent_t> ev(nb + 1, nullptr);
+  cudaStream_t root = nullptr;
+  auto cleanup = [&]() {
+    for (auto s : br)
+      if (s) cudaStreamDestroy(s);
+    for (auto e : ev)
+      if (e) cudaEventDestroy(e);
+    if (root) cudaStreamDestroy(root);
+  };
+  cudaError_t e = cudaStreamCreateWithFlags(&root, cudaStreamNonBlocking);
+  for (uint32_t i = 0; i < nb && e == cudaSuccess; ++i) e = cudaStreamCreateWithFlags(&br[i], cudaStreamNonBlocking);
+  for (uint32_t i = 0; i <= nb && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    cleanup();
+    return cuda_fail(e, "batch streams");
+  }
+  cudaGraph_t graph = nullptr;
+  e = cudaStreamBeginCapture(root, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) e = cudaEventRecord(ev[nb], root);
+  for (uint32_t i = 0; i < nb && e == cudaSuccess; ++i) e = cudaStreamWaitEvent(br[i], ev[nb], 0);
+  st = e == cudaSuccess ? PBRT_OK : cuda_fail(e, "batch fork");
+  // order within a chain: as assigned (pbrt_batch_plan lists requests longest first)
+  std::vector<uint32_t> order(b->reqs.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = (uint32_t)i;
+  if (b->tuning.order == 1)
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return costs[x] > costs[y]; });
+  for (uint32_t i : order) {
+    if (st) break;
+    st = record_request(b->reqs[i], br[assign[i]]);
+  }
+  for (uint32_t i = 0; i < nb && !st; ++i) {
+    e = cudaEventRecord(ev[i], br[i]);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(root, ev[i], 0);
+    if (e != cudaSuccess) st = cuda_fail(e, "batch join");
+  }
+  cudaError_t e2 = cudaStreamEndCapture(root, &graph);
+  if (!st && e2 != cudaSuccess) st = cuda_fail(e2, "end capture (batch)");
+  if (!st) {
+    e = cudaGraphInstantiate(&b->exec, graph, 0);
+    if (e != cudaSuccess) st = cuda_fail(e, "graph instantiate (batch)");
+  }
+  if (graph) cudaGraphDestroy(graph);
+  cleanup();
+  return st;
+}
+
+}  // namespace
+
+extern "C" {
+
+PBRT_API int pbrt_batch_plan(const double* costs, uint32_t n, uint32_t branches, uint32_t order, uint32_t* assign) {
+  if ((n && (!costs || !assign)) || branches == 0 || order > 1)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "batch plan: bad arguments");
+  std::vector<uint32_t> idx(n);
+  for (uint32_t i = 0; i < n; ++i) idx[i] = i;
+  if (order == 1) std::stable_sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) { return costs[a] > costs[b]; });
+  std::vector<double> load(branches, 0.0);
+  for (uint32_t i : idx) {
+    uint32_t best = 0;
+    for (uint32_t k = 1; k < branches; ++k)
+      if (load[k] < load[best]) best = k;
+    assign[i] = best;
+    load[best] += costs[i];
+  }
+  return PBRT_OK;
+}
+
+PBRT_API int pbrt_batch_create(PbrtBatch** out) {
+  if (!out) return fail(PBRT_ERROR_INVALID_ARGUMENT, "batch create: null output");
+  *out = new (std::nothrow) PbrtBatch();
+  return *out ? PBRT_OK : fail(PBRT_ERROR_OUT_OF_MEMORY, "batch: host allocation");
+}
+
+PBRT_API int pbrt_batch_add(PbrtBatch* b, const PbrtBatchRequest* r) {
+  if (!checked<PbrtBatch>(b, Kind::Batch) || !r || !checked<PbrtPipeline>(r->pipeline, Kind::Pipeline) ||
+      (r->accumulator && !checked<PbrtAccumulator>(r->accumulator, Kind::Accumulator)) ||
+      (r->bmfr && !checked<PbrtBMFR>(r->bmfr, Kind::BMFR)) || r->spp == 0 || r->spp > 4096)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "batch add: bad request");
+  if (r->accumulator && !r->camera.has_proj)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "batch add: an accumulated request needs camera matrices with proj");
+  for (const auto& q : b->reqs)
+    if (q.pipeline == r->pipeline)
+      return fail(PBRT_ERROR_INVALID_ARGUMENT, "batch add: a pipeline may appear in one request only");
+  retain(r->pipeline);
+  if (r->accumulator) retain(r->accumulator);
+  if (r->bmfr) retain(r->bmfr);
+  b->reqs.push_back(*r);
+  b->drop();
+  return PBRT_OK;
+}
+
+PBRT_API int pbrt_batch_size(const PbrtBatch* b, uint32_t* count) {
+  if (!checked<const PbrtBatch>((void*)b, Kind::Batch) || !count) return fail(PBRT_ERROR_INVALID_ARGUMENT, "batch size");
+  *count = (uint32_t)b->reqs.size();
+  return PBRT_OK;
+}
+
+PBRT_API int pbrt_batch_set_tuning(PbrtBatch* b, const PbrtBatchTuning* t) {
+  if (!checked<PbrtBatch>(b, Kind::Batch) || !t || t->branches == 0 || t->branches > 64 || t->trace_blocks_per_sm < 1 ||
+      t->trace_blocks_per_sm > 16 || t->shade_blocks_per_sm < 1 || t->shade_blocks_per_sm > 16 || t->order > 1)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "batch tuning: out of range");
+  b->tuning = *t;
+  b->drop();
+  return PBRT_OK;
+}
+
+PBRT_API int pbrt_batch_get_tuning(const PbrtBatch* b, PbrtBatchTuning* t) {
+  if (!checked<const PbrtBatch>((void*)b, Kind::Batch) || !t) return fail(PBRT_ERROR_INVALID_ARGUMENT, "batch tuning");
+  *t = b->tuning;
+  return PBRT_OK;
+}
+
+PBRT_API int pbrt_batch_submit(PbrtBatch* b, pbrt_stream_t stream) {
+  if (!checked<PbrtBatch>(b, Kind::Batch)) return fail(PBRT_ERROR_INVALID_ARGUMENT, "batch submit: not a batch");
+  if (b->reqs.empty()) return PBRT_OK;
+  if (!b->exec) {
+    int st = capture_batch(b);
+    if (st) return st;
+  }
+  PBRT_CUDA(cudaGraphLaunch(b->exec, stream));
+  return PBRT_OK;
+}
+
+// Autotuner: times every candidate (chains x traversal CTAs/SM x shading
+// CTAs/SM, longest-first order) on the batch itself -- one warm-up launch,
+// then the median of `repeats` launches -- and keeps the fastest.
+PBRT_API int pbrt_batch_autotune(PbrtBatch* b, pbrt_stream_t stream, int32_t repeats, PbrtBatchTuning* best_out,
+                                 float* best_ms_out) {
+  if (!checked<PbrtBatch>(b, Kind::Batch) || repeats < 1 || repeats > 16)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "batch autotune: bad arguments");
+  if (b->reqs.empty()) return fail(PBRT_ERROR_INVALID_ARGUMENT, "batch autotune: empty batch");
+  const uint32_t chains[] = {1, 2, 4, 8, 16};
+  const uint32_t trace_bps[] = {4, 8};
+  const uint32_t shade_bps[] = {4, 8};
+  cudaEvent_t e0, e1;
+  PBRT_CUDA(cudaEventCreate(&e0));
+  PBRT_CUDA(cudaEventCreate(&e1));
+  PbrtBatchTuning best = b->tuning;
+  float best_ms = 1e30f;
+  int st = PBRT_OK;
+  for (uint32_t c : chains) {
+    if (c > b->reqs.size() && c != 1) continue;
+    for (uint32_t tb : trace_bps)
+      for (uint32_t sb : shade_bps) {
+        if (st) break;
+        PbrtBatchTuning t{c, tb, sb, 1};
+        if ((st = pbrt_batch_set_tuning(b, &t))) break;
+        if ((st = pbrt_batch_submit(b, stream))) break;  // capture + warm-up
+        std::vector<float> ms;
+        for (int r = 0; r < repeats && !st; ++r) {
+          cudaEventRecord(e0, stream);
+          st = pbrt_batch_submit(b, stream);
+          cudaEventRecord(e1, stream);
+          cudaError_t e = cudaEventSynchronize(e1);
+          if (!st && e != cudaSuccess) st = cuda_fail(e, "autotune timing");
+          float m = 0.f;
+          cudaEventElapsedTime(&m, e0, e1);
+          ms.push_back(m);
+        }
+        if (st) break;
+        std::sort(ms.begin(), ms.end());
+        const float med = ms[ms.size() / 2];
+        if (med < best_ms) {
+          best_ms = med;
+          best = t;
+        }
+      }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  if ((st = pbrt_batch_set_tuning(b, &best))) return st;
+  if (best_out) *best_out = best;
+  if (best_ms_out) *best_ms_out = best_ms;
   return PBRT_OK;
 }
 

@@ -9,7 +9,8 @@ the coarse ones); the two finer heads also predict the weight that blends
 the upsampled coarser result in, and the full-scale head predicts the log
 squared error of its pixel (the variance gate that hands tiles back to
 BMFR). Inputs are the 1-spp G-buffer and illumination: 16 BF16 channels
-(log1p radiance, albedo, normal, log1p depth / 8, six zero channels).
+(log1p radiance, albedo, normal, log1p depth / 8, samples per pixel, five
+zero channels).
 
 Activations and convolution weights are BF16 with FP32 accumulation; the
 master weights, gradients and Adam moments are FP32 in one flat buffer each,
@@ -74,7 +75,7 @@ def init_params(seed=0):
         off, shape = lay[name + ".w"]
         w = rng.standard_normal(shape).astype(np.float32) * np.sqrt(2.0 / (9 * (c1 + c2)))
         if name == "e0a":
-            w[:, :, 10:] = 0.0
+            w[:, :, 11:] = 0.0
         p[off:off + w.size] = w.ravel()
     for name, _, c, k, _ in HEADS:
         off, shape = lay[name + ".w"]
@@ -190,8 +191,8 @@ class Workspace:
         return flat[:n].view(self.n, self.ph >> level, self.pw >> level, c)
 
     # ---- forward ------------------------------------------------------------
-    def set_input(self, illum, albedo, normal, depth):
-        nn.features(illum, albedo, normal, depth, self.feat, self.rad[0])
+    def set_input(self, illum, albedo, normal, depth, spp=None):
+        nn.features(illum, albedo, normal, depth, self.feat, self.rad[0], spp=spp)
 
     def forward(self):
         net, a = self.net, self.act

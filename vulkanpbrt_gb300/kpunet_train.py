@@ -46,7 +46,7 @@ def _camera(kind, sc, rng, full_w, full_h):
     return Camera(eye, center, aspect=full_w / full_h)
 
 
-def render_views(views, window=512, crop=256, full=(1920, 1080), inputs=4, target_spp=4096, max_depth=8,
+def render_views(views, window=1024, crop=256, full=(1920, 1080), inputs=16, target_spp=4096, max_depth=8,
                  min_depth=3, texture_size=256, instances=2000, device="cuda", log=print):
     """views: list of (kind, scene_seed, camera_seed). Returns a dict of device
     tensors with one entry per crop: illum [M, inputs, crop, crop, 4] f32,
@@ -148,29 +148,42 @@ def augment(batch, rng):
     return batch
 
 
+SPP_CHOICES = (1, 1, 2, 4, 8, 16)  # samples averaged into one network input (1 spp twice as likely)
+
+
 def train(net, data, steps, batch=16, lr=1e-4, seed=0, log_every=100, var_weight=0.1, log=print,
           lr_floor=0.1):
-    """Adam steps over random crops (and random 1-spp inputs of each crop);
-    cosine learning-rate decay to lr * lr_floor. Returns the loss history."""
+    """Adam steps over random crops; each input is the mean of k of the
+    crop's one-sample frames (k from SPP_CHOICES, with the matching samples-
+    per-pixel channel, as the Accumulator's output carries it) -- so one
+    network serves raw 1-spp and accumulated input. Cosine learning-rate
+    decay to lr * lr_floor. Returns the loss history."""
     import torch
 
     from . import nn
 
     M, inputs, crop = data["illum"].shape[:3]
+    dev = data["illum"].device
     ws = net.workspace(batch, crop, crop)
     rng = np.random.default_rng(seed)
     hist = []
     t0 = time.time()
+    spp_u8 = torch.empty((batch, crop, crop), dtype=torch.uint8, device=dev)
     for it in range(steps):
-        idx = torch.from_numpy(rng.integers(0, M, batch)).to(data["illum"].device)
-        kin = torch.from_numpy(rng.integers(0, inputs, batch)).to(data["illum"].device)
-        b = {"illum": data["illum"][idx, kin], "albedo": data["albedo"][idx], "normal": data["normal"][idx],
-             "depth": data["depth"][idx], "target": data["target"][idx]}
-        b = {k: v[:, None] if k == "illum" else v for k, v in b.items()}
+        idx = rng.integers(0, M, batch)
+        ill = []
+        for j, m in enumerate(idx):
+            k = min(int(rng.choice(SPP_CHOICES)), inputs)
+            frames = torch.from_numpy(rng.permutation(inputs)[:k]).to(dev)
+            ill.append(data["illum"][int(m)][frames].mean(0))
+            spp_u8[j] = int(round(k / 256.0 * 255.0))  # the accumulator's R8 spp encoding
+        ti = torch.from_numpy(idx).to(dev)
+        b = {"illum": torch.stack(ill)[:, None], "albedo": data["albedo"][ti], "normal": data["normal"][ti],
+             "depth": data["depth"][ti], "target": data["target"][ti], "spp": spp_u8}
         b = augment(b, rng)
         illum = b["illum"][:, 0].contiguous()
         nn.features(illum, b["albedo"].contiguous(), b["normal"].contiguous(), b["depth"].contiguous(), ws.feat,
-                    ws.rad[0])
+                    ws.rad[0], spp=b["spp"].contiguous())
         cur = lr * (lr_floor + (1 - lr_floor) * 0.5 * (1 + math.cos(math.pi * it / max(steps, 1))))
         loss = ws.train_step(b["target"].contiguous(), b["albedo"].contiguous(), lr=cur, var_weight=var_weight)
         if it % log_every == 0 or it == steps - 1:
@@ -186,9 +199,9 @@ def main(argv=None):
 
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--views", type=int, default=24)
-    ap.add_argument("--window", type=int, default=512)
+    ap.add_argument("--window", type=int, default=1024)
     ap.add_argument("--crop", type=int, default=256)
-    ap.add_argument("--inputs", type=int, default=4)
+    ap.add_argument("--inputs", type=int, default=16)
     ap.add_argument("--target-spp", type=int, default=4096)
     ap.add_argument("--steps", type=int, default=3000)
     ap.add_argument("--batch", type=int, default=16)

@@ -17,7 +17,7 @@ from .render_modules import BMFR, Commands, GBuffer, Handle, IlluminationBuffer,
 H = C.c_void_p
 _abi.add_signatures({
     "pbrt_neural_param_count": (C.c_int32, [C.POINTER(C.c_int64)]),
-    "pbrt_neural_create": (C.c_int32, [C.c_uint32, C.c_uint32, H, H, H, C.c_int64, C.POINTER(H)]),
+    "pbrt_neural_create": (C.c_int32, [C.c_uint32, C.c_uint32, H, H, H, H, C.c_int64, C.POINTER(H)]),
     "pbrt_neural_set_params": (C.c_int32, [H, H, C.c_int64]),
     "pbrt_neural_set_fallback": (C.c_int32, [H, H, C.c_float, C.c_int32]),
     "pbrt_neural_dispatch": (C.c_int32, [H, H]),
@@ -26,6 +26,8 @@ _abi.add_signatures({
     "pbrt_neural_images": (C.c_int32, [H, C.POINTER(PbrtImage), C.POINTER(PbrtImage)]),
     "pbrt_neural_fallback_tiles": (C.c_int32, [H, H, C.POINTER(C.c_uint32)]),
     "pbrt_neural_fallback_mask": (C.c_int32, [H, C.POINTER(PbrtImage)]),
+    "pbrt_neural_calibrate": (C.c_int32, [H, H]),
+    "pbrt_neural_set_precision": (C.c_int32, [H, C.c_int32]),
 })
 
 WEIGHTS = Path(__file__).resolve().parent / "weights" / "kpunet.npz"
@@ -52,19 +54,21 @@ def load_params(weights=None) -> np.ndarray:
 
 
 class NeuralDenoiser(Handle):
-    """Denoises the 1-spp demodulated illumination of `illu_buffer` with the
-    G-buffer's albedo, normal and depth. With `fallback` (a BMFR over the
+    """Denoises the demodulated illumination of `illu_buffer` (one sample, or
+    the Accumulator's output with `acc_buffer` giving the sample counts) with
+    the G-buffer's albedo, normal and depth. With `fallback` (a BMFR over the
     same frame, dispatched first), tiles whose predicted error exceeds
     `threshold` show BMFR's final image."""
 
     def __init__(self, width: int, height: int, g_buffer: GBuffer, illu_buffer: IlluminationBuffer, weights=None,
-                 fallback: BMFR | None = None, threshold: float = 0.5, tile: int = 32):
+                 fallback: BMFR | None = None, threshold: float = 0.5, tile: int = 32, acc_buffer=None):
         p = load_params(weights)
         h = C.c_void_p()
-        check(lib().pbrt_neural_create(width, height, g_buffer.ptr, illu_buffer.ptr, p.ctypes.data_as(H), p.size,
-                                       C.byref(h)))
+        check(lib().pbrt_neural_create(width, height, g_buffer.ptr, illu_buffer.ptr,
+                                       acc_buffer.ptr if acc_buffer is not None else None, p.ctypes.data_as(H),
+                                       p.size, C.byref(h)))
         super().__init__(h)
-        self._inputs = (g_buffer, illu_buffer)
+        self._inputs = (g_buffer, illu_buffer, acc_buffer)
         self.width, self.height = width, height
         d, v, f = PbrtImage(), PbrtImage(), PbrtImage()
         check(lib().pbrt_neural_images(h, C.byref(d), C.byref(v)))
@@ -85,6 +89,14 @@ class NeuralDenoiser(Handle):
         m = PbrtImage()
         check(lib().pbrt_neural_fallback_mask(self.ptr, C.byref(m)))
         self.fallback_mask = Image(m, self) if m.data else None
+
+    def calibrate(self, stream=None) -> None:
+        """FP8 scales from one BF16 pass over the current inputs."""
+        check(lib().pbrt_neural_calibrate(self.ptr, stream_handle(stream)))
+
+    def set_precision(self, bits: int) -> None:
+        """16: BF16 convolutions; 8: FP8 e4m3 (after calibrate)."""
+        check(lib().pbrt_neural_set_precision(self.ptr, bits))
 
     def dispatch(self, push_constants=None, stream=None, graph: bool = True) -> None:
         fn = lib().pbrt_neural_dispatch if graph else lib().pbrt_neural_dispatch_direct

@@ -14,8 +14,11 @@ i32, i64, f32 = C.c_int32, C.c_int64, C.c_float
 _abi.add_signatures({
     "pbrt_nn_conv3x3": (i32, [H, i32, H, i32, H, H, H, H, i32, i32, i32, i32, i32, H]),
     "pbrt_nn_conv3x3_wgrad": (i32, [H, H, i32, H, i32, H, i32, i32, i32, i32, H]),
+    "pbrt_nn_conv3x3_fp8": (i32, [H, i32, H, i32, H, H, H, H, H, i32, i32, i32, i32, i32, H]),
+    "pbrt_nn_quantize_weights_fp8": (i32, [H, H, i32, i32, H, H, H]),
+    "pbrt_nn_channel_amax": (i32, [H, i64, i32, H, H]),
     "pbrt_nn_flip_weights": (i32, [H, H, i32, i32, H]),
-    "pbrt_nn_features": (i32, [H, i32, H, H, H, i32, i32, i32, i32, i32, H, H, H]),
+    "pbrt_nn_features": (i32, [H, i32, H, H, H, H, i32, i32, i32, i32, i32, H, H, H]),
     "pbrt_nn_avgpool2": (i32, [H, H, i32, i32, i32, i32, i32, H]),
     "pbrt_nn_avgpool2_bwd_add": (i32, [H, H, i32, i32, i32, i32, H]),
     "pbrt_nn_relu_bwd": (i32, [H, H, H, H, i64, i32, H]),
@@ -28,7 +31,7 @@ _abi.add_signatures({
     "pbrt_nn_compose": (i32, [H, i32, i32, i32, H, H, i32, H, H, H, H]),
 })
 
-RELU, ACCUMULATE = 1, 2
+RELU, ACCUMULATE, KSTEP = 1, 2, 4
 
 
 def _ptr(t):
@@ -41,10 +44,12 @@ def _stream():
     return C.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
-def conv3x3(x1, w, bias=None, x2=None, relu=False, out=None, out32=None, accumulate=False, store_bf16=True):
+def conv3x3(x1, w, bias=None, x2=None, relu=False, out=None, out32=None, accumulate=False, store_bf16=True,
+            kernel="halo"):
     """y = relu?(conv3x3(concat(x1, up2(x2))) + bias). x1 [N,H,W,C1] bf16, x2 [N,H/2,W/2,C2] bf16,
     w [Cout, 9, C1+C2] bf16, bias [Cout] f32. Returns the BF16 output [N,H,W,Cout] (None when
-    store_bf16 is False: only out32 is written, added to when accumulate is set)."""
+    store_bf16 is False: only out32 is written, added to when accumulate is set). kernel: "halo"
+    (input halo staged once per channel chunk) or "kstep" (pipelined per tap and 16 channels)."""
     import torch
 
     n, h, wd, c1 = x1.shape
@@ -52,10 +57,44 @@ def conv3x3(x1, w, bias=None, x2=None, relu=False, out=None, out32=None, accumul
     cout = w.shape[0]
     if out is None and store_bf16:
         out = torch.empty((n, h, wd, cout), dtype=torch.bfloat16, device=x1.device)
-    flags = (RELU if relu else 0) | (ACCUMULATE if accumulate else 0)
+    flags = (RELU if relu else 0) | (ACCUMULATE if accumulate else 0) | (KSTEP if kernel == "kstep" else 0)
     check(lib().pbrt_nn_conv3x3(_ptr(x1), c1, _ptr(x2), c2, _ptr(w), _ptr(bias), _ptr(out if store_bf16 else None),
                                 _ptr(out32), n, h, wd, cout, flags, _stream()))
     return out if store_bf16 else None
+
+
+def conv3x3_fp8(x1, w8, wscale, inv_xscale, bias=None, x2=None, relu=False, out=None):
+    """FP8 (e4m3) forward: w8 [Cout, 9, Cin] uint8 e4m3 with per-output-channel scales wscale [Cout] (activation
+    scales folded in), inv_xscale [Cin] quantises the BF16 input on load. Returns BF16 [N,H,W,Cout]."""
+    import torch
+
+    n, h, wd, c1 = x1.shape
+    c2 = 0 if x2 is None else x2.shape[3]
+    cout = w8.shape[0]
+    if out is None:
+        out = torch.empty((n, h, wd, cout), dtype=torch.bfloat16, device=x1.device)
+    check(lib().pbrt_nn_conv3x3_fp8(_ptr(x1), c1, _ptr(x2), c2, _ptr(w8), _ptr(wscale), _ptr(inv_xscale), _ptr(bias),
+                                    _ptr(out), n, h, wd, cout, RELU if relu else 0, _stream()))
+    return out
+
+
+def quantize_weights_fp8(w32, xscale, w8=None, wscale=None):
+    """w32 [Cout, 9, Cin] f32, xscale [Cin] -> (w8 uint8 e4m3, wscale [Cout])."""
+    import torch
+
+    cout, _, cin = w32.shape
+    if w8 is None:
+        w8 = torch.empty((cout, 9, cin), dtype=torch.uint8, device=w32.device)
+    if wscale is None:
+        wscale = torch.empty(cout, dtype=torch.float32, device=w32.device)
+    check(lib().pbrt_nn_quantize_weights_fp8(_ptr(w32), _ptr(xscale), cout, cin, _ptr(w8), _ptr(wscale), _stream()))
+    return w8, wscale
+
+
+def channel_amax(x, amax):
+    c = x.shape[-1]
+    check(lib().pbrt_nn_channel_amax(_ptr(x), x.numel() // c, c, _ptr(amax), _stream()))
+    return amax
 
 
 def conv3x3_wgrad(dy, x1, dw, x2=None):
@@ -78,15 +117,16 @@ def flip_weights(w, out=None):
     return out
 
 
-def features(illum, albedo, normal, depth, feat, rad):
-    """illum [N,h,w,4] f32|f16, albedo [N,h,w,4] u8, normal [N,h,w,2] f32, depth [N,h,w] f32 ->
-    feat [N,PH,PW,16] bf16 and rad [N,PH,PW,3] f32 (padded, edges replicated)."""
+def features(illum, albedo, normal, depth, feat, rad, spp=None):
+    """illum [N,h,w,4] f32|f16, albedo [N,h,w,4] u8, normal [N,h,w,2] f32, depth [N,h,w] f32, spp [N,h,w] u8
+    (accumulator steps of 1/256, optional) -> feat [N,PH,PW,16] bf16 and rad [N,PH,PW,3] f32 (padded, edges
+    replicated, clamped to [0, 10])."""
     import torch
 
     n, h, w = illum.shape[:3]
     ph, pw = feat.shape[1:3]
     check(lib().pbrt_nn_features(_ptr(illum), int(illum.dtype == torch.float16), _ptr(albedo), _ptr(normal),
-                                 _ptr(depth), w, h, pw, ph, n, _ptr(feat), _ptr(rad), _stream()))
+                                 _ptr(depth), _ptr(spp), w, h, pw, ph, n, _ptr(feat), _ptr(rad), _stream()))
 
 
 def avgpool2(x, out):
