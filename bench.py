@@ -265,9 +265,49 @@ def relmse_eval(args, vp, pipe, g, illu, bmfr, neural, pc, cams, stream, dev):
     out["reference_s"] = time.perf_counter() - t0
     ref /= args.ref_spp
     r = albedo * ref
+    err = {}
     for k, v in den.items():
-        out[k] = float((((albedo * v - r) ** 2) / (r * r + 0.01)).mean().item())
+        e = ((albedo * v - r) ** 2) / (r * r + 0.01)
+        err[k] = e.mean(-1)
+        out[k] = float(e.mean().item())
+    if neural is not None and bmfr is not None:
+        out["gate"] = gate_analysis(neural, err["neural"], err["bmfr"], g.width, g.height)
     return out
+
+
+def gate_analysis(neural, err_nn, err_bmfr, W, H, tile=32):
+    """How well the error head ranks 32x32 tiles: per tile, the predicted
+    relative squared error (mean exp of the head) against the measured
+    relMSE of the network and of BMFR; the composite relMSE if tiles whose
+    prediction exceeds each of several quantile thresholds showed BMFR."""
+    import torch
+
+    var = neural.variance.tensor()[..., 0][:H, :W].double().exp()
+    th, tw = (H + tile - 1) // tile, (W + tile - 1) // tile
+    ph, pw = th * tile - H, tw * tile - W
+
+    def tiles(x):
+        x = torch.nn.functional.pad(x[None, None], (0, pw, 0, ph))
+        cnt = torch.nn.functional.pad(torch.ones_like(x[0, 0])[:H, :W][None, None], (0, pw, 0, ph))
+        s = torch.nn.functional.avg_pool2d(x, tile, divisor_override=1)[0, 0]
+        n = torch.nn.functional.avg_pool2d(cnt, tile, divisor_override=1)[0, 0]
+        return (s / n).flatten(), n.flatten()
+
+    pred, n = tiles(var)
+    e_nn, _ = tiles(err_nn)
+    e_bm, _ = tiles(err_bmfr)
+    total = float(n.sum())
+    res = {"tiles": int(pred.numel()),
+           "corr_pred_vs_neural_err": float(torch.corrcoef(torch.stack([pred.log(), (e_nn + 1e-6).log()]))[0, 1]),
+           "best_possible": float(((torch.minimum(e_nn, e_bm) * n).sum() / total).item()),
+           "bmfr_better_tiles": int((e_bm < e_nn).sum().item())}
+    sweep = {}
+    for q in (0.5, 0.75, 0.9, 0.95, 0.99):
+        thr = float(torch.quantile(pred, q).item())
+        comp = torch.where(pred > thr, e_bm, e_nn)
+        sweep[f"q{q}"] = {"threshold": thr, "relmse": float(((comp * n).sum() / total).item())}
+    res["sweep"] = sweep
+    return res
 
 
 def run_gb300(args):
@@ -445,9 +485,13 @@ def run_gb300(args):
     quality = None
     if args.ref_spp > 0 and rank == 0:
         quality = relmse_eval(args, vp, pipe, g, illu, bmfr, neural, pc, cams, stream, dev)
-    closest_bytes = prof.closest_nodes * NODE_BYTES + prof.closest_tris * TRI_BYTES
-    launches = max(1, prof.closest_launches)
-    per_launch_s = prof.trace_closest_ms / 1e3 / launches
+    # traversal launches trace closest-hit and shadow rays together (bounce k's
+    # closest-hit rays with bounce k-1's shadow rays), so the roofline covers both
+    closest_bytes = (prof.closest_nodes + prof.shadow_nodes) * NODE_BYTES + \
+        (prof.closest_tris + prof.shadow_tris) * TRI_BYTES
+    trav_ms = prof.trace_closest_ms + prof.trace_shadow_ms
+    launches = max(1, prof.closest_launches + 1)
+    per_launch_s = trav_ms / 1e3 / launches
     achieved = closest_bytes / launches / per_launch_s / 1e9
     peak, peak_kind = peaks()
     traffic = profile_traffic("k_trace_closest")
@@ -491,7 +535,7 @@ def run_gb300(args):
             "e2e": {"value": world * e2e_steps / e2e_s, "unit": "fps", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "roofline": {
-                "kernel": "k_trace_closest (BVH8 closest-hit traversal)",
+                "kernel": "k_traverse (BVH8 traversal: closest-hit and shadow rays, merged launches)",
                 "bound": "hbm",
                 "achieved": achieved,
                 "peak": peak,
@@ -499,9 +543,9 @@ def run_gb300(args):
                 "frac": achieved / peak,
                 "peak_source": peak_kind,
                 "traffic": traffic,
-                "bytes_per_ray": closest_bytes / max(1, prof.closest_rays),
-                "nodes_per_ray": prof.closest_nodes / max(1, prof.closest_rays),
-                "tris_per_ray": prof.closest_tris / max(1, prof.closest_rays),
+                "bytes_per_ray": closest_bytes / max(1, prof.closest_rays + prof.shadow_rays),
+                "nodes_per_ray": (prof.closest_nodes + prof.shadow_nodes) / max(1, prof.closest_rays + prof.shadow_rays),
+                "tris_per_ray": (prof.closest_tris + prof.shadow_tris) / max(1, prof.closest_rays + prof.shadow_rays),
                 "dominant_kernel": dominant,
             },
             "cpu_baseline": cpu,

@@ -127,6 +127,26 @@ struct TravState {
 };
 constexpr uint32_t kNoNode = 0xffffffffu;
 
+// Traversal stack: the first kSmemStack entries of each lane live in shared
+// memory (a column per thread of a 128-thread CTA), deeper ones in local
+// memory. Typical depths stay in shared memory; with every entry in local
+// memory, 32 resident warps' stacks overflow L1 and each push and pop goes
+// to L2.
+#ifndef PBRT_SMEM_STACK
+#define PBRT_SMEM_STACK 0
+#endif
+constexpr int kSmemStack = PBRT_SMEM_STACK;
+constexpr int kTraverseThreads = 128;
+struct TravStack {
+  uint2* sm;  // this lane's column: sm[i * kTraverseThreads]
+  uint2 local[kStackSize - kSmemStack];
+  PBRT_D void put(int i, uint2 v) {
+    if (i < kSmemStack) sm[i * kTraverseThreads] = v;
+    else local[i - kSmemStack] = v;
+  }
+  PBRT_D uint2 get(int i) const { return i < kSmemStack ? sm[i * kTraverseThreads] : local[i - kSmemStack]; }
+};
+
 // Traversal step shape. 0: a node visit tests the triangles of every hit
 // leaf child at once. 1: a node visit records them as a mask and the lane
 // tests one triangle per step until the mask is empty, so lanes of a warp
@@ -142,7 +162,7 @@ constexpr int kTraversalDeferTris = PBRT_TRAVERSAL_DEFER_TRIS;
 // order) or to the next entry of the stack. Returns false when the ray is
 // finished (stack empty, or -- for ANY_HIT -- an accepted hit).
 template <bool ANY_HIT>
-PBRT_D bool visit_node(const SceneView& sc, const RayPre& r, float tmin, TravState& st, uint2* stack, int& err,
+PBRT_D bool visit_node(const SceneView& sc, const RayPre& r, float tmin, TravState& st, TravStack& stack, int& err,
                        uint32_t& n_nodes, uint32_t& n_tris) {
   const float4* nodes4 = reinterpret_cast<const float4*>(sc.nodes);
   const uint32_t node = st.node;
@@ -218,19 +238,19 @@ PBRT_D bool visit_node(const SceneView& sc, const RayPre& r, float tmin, TravSta
         err = 1;
         return false;
       }
-      stack[st.sp++] = make_uint2(child_base, (imask << 8) | inner);
+      stack.put(st.sp++, make_uint2(child_base, (imask << 8) | inner));
     }
     st.node = child_base + __popc(imask & ((1u << s) - 1u));
     return true;
   }
   if (st.sp == 0) return false;
-  uint2 g = stack[--st.sp];
+  uint2 g = stack.get(--st.sp);
   uint32_t m = g.y & 0xffu;
   const uint32_t im = g.y >> 8;
   const int k = __ffs(m) - 1;
   m &= m - 1;
   const int s = k ^ r.oct;
-  if (m) stack[st.sp++] = make_uint2(g.x, (im << 8) | m);
+  if (m) stack.put(st.sp++, make_uint2(g.x, (im << 8) | m));
   st.node = g.x + __popc(im & ((1u << s) - 1u));
   return true;
 }
@@ -239,7 +259,7 @@ PBRT_D bool visit_node(const SceneView& sc, const RayPre& r, float tmin, TravSta
 // hit leaf children in st.tri_mask and moves to the next node (kNoNode when
 // the stack is empty). The ray is finished when both are exhausted.
 template <bool POP>
-PBRT_D void visit_node_deferred(const SceneView& sc, const RayPre& r, float tmin, TravState& st, uint2* stack,
+PBRT_D void visit_node_deferred(const SceneView& sc, const RayPre& r, float tmin, TravState& st, TravStack& stack,
                                 int& err, uint32_t& n_nodes) {
   const float4* nodes4 = reinterpret_cast<const float4*>(sc.nodes);
   const uint32_t node = st.node;
@@ -294,7 +314,7 @@ PBRT_D void visit_node_deferred(const SceneView& sc, const RayPre& r, float tmin
         st.tri_mask = 0;
         return;
       }
-      stack[st.sp++] = make_uint2(child_base, (imask << 8) | inner);
+      stack.put(st.sp++, make_uint2(child_base, (imask << 8) | inner));
     }
     st.node = child_base + __popc(imask & ((1u << s) - 1u));
     return;
@@ -303,21 +323,21 @@ PBRT_D void visit_node_deferred(const SceneView& sc, const RayPre& r, float tmin
     st.node = kNoNode;
     return;
   }
-  uint2 g = stack[--st.sp];
+  uint2 g = stack.get(--st.sp);
   uint32_t m = g.y & 0xffu;
   const uint32_t im = g.y >> 8;
   const int k = __ffs(m) - 1;
   m &= m - 1;
   const int s = k ^ r.oct;
-  if (m) stack[st.sp++] = make_uint2(g.x, (im << 8) | m);
+  if (m) stack.put(st.sp++, make_uint2(g.x, (im << 8) | m));
   st.node = g.x + __popc(im & ((1u << s) - 1u));
 }
 
 // Postponing form (mode 2): a node visit leaves st.node = kNoNode when no
 // inner child is hit instead of popping; the pop is a step of its own, and a
 // stack entry with bit 31 set is a postponed triangle group.
-PBRT_D void pop_group(const RayPre& r, TravState& st, uint2* stack) {
-  uint2 g = stack[--st.sp];
+PBRT_D void pop_group(const RayPre& r, TravState& st, TravStack& stack) {
+  uint2 g = stack.get(--st.sp);
   if (g.y & 0x80000000u) {
     st.tri_base = g.x;
     st.tri_mask = g.y & 0x7fffffffu;
@@ -328,7 +348,7 @@ PBRT_D void pop_group(const RayPre& r, TravState& st, uint2* stack) {
   const int k = __ffs(m) - 1;
   m &= m - 1;
   const int s = k ^ r.oct;
-  if (m) stack[st.sp++] = make_uint2(g.x, (im << 8) | m);
+  if (m) stack.put(st.sp++, make_uint2(g.x, (im << 8) | m));
   st.node = g.x + __popc(im & ((1u << s) - 1u));
 }
 
@@ -409,7 +429,41 @@ struct Queues {
   float4* prev;  // previous vertex (worldSpacePos) xyz, w = loop index i (as int bits)
   float4* alb;   // primary albedo xyz (float, for demodulation), w = transDepth (int bits)
   uint32_t* prim_key;  // primary hit key per pixel (0xffffffff = miss), for parity tests
+  // ray sorting (kSortRays): shading appends to these, the sort scatters them
+  // into the ray queue / shadow queue ordered by (direction octant, origin cell)
+  uint32_t* pix_t;
+  float4* org_t;
+  float4* dir_t;
+  uint16_t* key_t;
+  uint32_t* spix_t;
+  float4* sorg_t;
+  float4* sdir_t;
+  float4* snee_t;
+  float4* sadd_t;
+  uint16_t* skey_t;
+  uint32_t* bins;  // [2][kSortBins]: extension rays, shadow rays
 };
+
+// Ray sorting: extension and shadow rays are reordered by a 12-bit key --
+// the direction octant (3 bits) over a 3-bit-per-axis Morton cell of the
+// origin in the scene box -- with a counting sort (histogram, scan,
+// warp-aggregated scatter) before they are traversed, so a warp's rays take
+// the same child order and start in the same region of the BVH. Results
+// are per pixel, so the order changes nothing but speed.
+#ifndef PBRT_SORT_RAYS
+#define PBRT_SORT_RAYS 0
+#endif
+constexpr int kSortRays = PBRT_SORT_RAYS;
+
+// Schedule: 1 traces bounce k's closest-hit rays and bounce k-1's shadow
+// rays in one persistent launch (fewer launch tails, more rays per launch);
+// per-pixel updates keep their order (shading of k-1, shadow resolve of
+// k-1, shading of k). 0: one launch per queue.
+#ifndef PBRT_MERGE_SHADOW
+#define PBRT_MERGE_SHADOW 1
+#endif
+constexpr int kMergeShadow = PBRT_MERGE_SHADOW;
+constexpr int kSortBits = 12, kSortBins = 1 << kSortBits;
 
 struct GBufferOut {
   float* depth;
@@ -486,6 +540,21 @@ __global__ void k_bounce_begin(Counters* c, int k) {
 
 __global__ void k_bounce_end(Counters* c) { c->rays_shadow += c->shadow; }
 
+// Merged schedule: bounce k's launch also traces the shadow rays of bounce
+// k-1, so the shadow queue is kept until that launch is done.
+__global__ void k_bounce_begin_merged(Counters* c, int k) {
+  if (k > 0) c->rays_extension += c->ray[k & 1];
+  c->ray[(k + 1) & 1] = 0;
+  c->work_trace = 0;
+  c->work_shadow = 0;
+  if (k == 0) c->shadow = 0;
+}
+__global__ void k_shadow_begin(Counters* c) { c->work_shadow = 0; }
+__global__ void k_shadow_consumed(Counters* c) {
+  c->rays_shadow += c->shadow;
+  c->shadow = 0;
+}
+
 // createRay (camera.glsl:6-16) and the RNG seeding of ptRaygen.rgen:28-40.
 __global__ void k_raygen(const FrameParams* __restrict__ fpp, Queues q) {
   const FrameParams& fp = *fpp;
@@ -531,14 +600,22 @@ struct QueryIO {
 
 template <int MODE>
 __global__ void __launch_bounds__(128, 8) k_traverse(SceneView sc, Queues q, Counters* c, int k, QueryIO io) {
+  // MODE 4: the closest-hit rays of queue k&1 followed by the shadow rays
+  // of the previous bounce, in one launch (one work counter over both)
   constexpr bool ANY = (MODE == 1 || MODE == 3);
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
   const float4* org;
   const float4* dir;
-  uint32_t count;
+  uint32_t count, count_c = 0;
   uint32_t* work;
-  if (MODE == 0) {
+  if (MODE == 4) {
+    count_c = *((volatile uint32_t*)&c->ray[k & 1]);
+    count = count_c + *((volatile uint32_t*)&c->shadow);
+    org = q.org[k & 1];
+    dir = q.dir[k & 1];
+    work = &c->work_trace;
+  } else if (MODE == 0) {
     count = *((volatile uint32_t*)&c->ray[k & 1]);
     org = q.org[k & 1];
     dir = q.dir[k & 1];
@@ -554,7 +631,9 @@ __global__ void __launch_bounds__(128, 8) k_traverse(SceneView sc, Queues q, Cou
     dir = io.dir;
     work = io.work;
   }
-  uint2 stack[kStackSize];
+  __shared__ uint2 s_stack[kSmemStack > 0 ? kSmemStack * kTraverseThreads : 1];
+  TravStack stack;
+  stack.sm = s_stack + threadIdx.x;
   TravState st;
   RayPre r;
   float tmin = 0.f;
@@ -562,7 +641,8 @@ __global__ void __launch_bounds__(128, 8) k_traverse(SceneView sc, Queues q, Cou
   uint32_t batch_next = 0, batch_end = 0;  // warp-uniform
   bool drained = false;                     // warp-uniform: no more batches
   int err = 0;
-  uint32_t nn = 0, nt = 0;
+  uint32_t nn = 0, nt = 0, nn_s = 0, nt_s = 0;
+  bool lane_any = ANY;
   while (true) {
     // ---- refill idle lanes from the warp's batch
     unsigned need = __ballot_sync(kFullMask, idx < 0);
@@ -571,7 +651,7 @@ __global__ void __launch_bounds__(128, 8) k_traverse(SceneView sc, Queues q, Cou
         uint32_t b = 0;
         if (lane == 0) {
           b = atomicAdd(work, 32u);
-          if (MODE <= 1 && b < count && stop_requested(c, b)) b = count;
+          if ((MODE <= 1 || MODE == 4) && b < count && stop_requested(c, b)) b = count;
         }
         b = __shfl_sync(kFullMask, b, 0);
         if (b >= count) {
@@ -585,7 +665,16 @@ __global__ void __launch_bounds__(128, 8) k_traverse(SceneView sc, Queues q, Cou
       const uint32_t rank = __popc(need & lt_mask);
       if (((need >> lane) & 1u) && rank < avail) {
         idx = (int)(batch_next + rank);
-        const float4 o = org[idx], d = dir[idx];
+        float4 o, d;
+        if (MODE == 4) {
+          lane_any = (uint32_t)idx >= count_c;
+          const uint32_t j = lane_any ? (uint32_t)idx - count_c : (uint32_t)idx;
+          o = lane_any ? q.sorg[j] : org[j];
+          d = lane_any ? q.sdir[j] : dir[j];
+        } else {
+          o = org[idx];
+          d = dir[idx];
+        }
         r = ray_pre(f3(o.x, o.y, o.z), f3(d.x, d.y, d.z));
         tmin = o.w;
         st.node = 0;
@@ -608,7 +697,7 @@ __global__ void __launch_bounds__(128, 8) k_traverse(SceneView sc, Queues q, Cou
       const unsigned trl = __ballot_sync(kFullMask, busy && st.tri_mask != 0);
       if (!busy) continue;
       if (st.tri_mask && st.node != kNoNode && 4 * __popc(trl) < __popc(act) && st.sp < kStackSize) {
-        stack[st.sp++] = make_uint2(st.tri_base, st.tri_mask | 0x80000000u);
+        stack.put(st.sp++, make_uint2(st.tri_base, st.tri_mask | 0x80000000u));
         st.tri_mask = 0;
       }
       bool done = false;
@@ -616,6 +705,16 @@ __global__ void __launch_bounds__(128, 8) k_traverse(SceneView sc, Queues q, Cou
       else if (st.node != kNoNode) visit_node_deferred<false>(sc, r, tmin, st, stack, err, nn);
       else pop_group(r, st, stack);
       if (!done && (st.tri_mask || st.node != kNoNode || st.sp > 0)) continue;
+    } else if (MODE == 4) {
+      if (idx < 0) continue;
+      if (st.tri_mask) {
+        const bool acc = lane_any ? test_one_triangle<true>(sc, r, tmin, st, nt_s)
+                                  : test_one_triangle<false>(sc, r, tmin, st, nt);
+        if (!acc && (st.tri_mask || st.node != kNoNode)) continue;
+      } else {
+        visit_node_deferred<true>(sc, r, tmin, st, stack, err, lane_any ? nn_s : nn);
+        if (st.tri_mask || st.node != kNoNode) continue;
+      }
     } else if (kTraversalDeferTris == 1) {
       if (idx < 0) continue;
       if (st.tri_mask) {
@@ -630,11 +729,12 @@ __global__ void __launch_bounds__(128, 8) k_traverse(SceneView sc, Queues q, Cou
       continue;
     }
     // ---- ray finished
-    if (MODE == 0) {
+    if (MODE == 0 || (MODE == 4 && !lane_any)) {
       q.hit[idx] = make_float4(st.tbest, st.bu, st.bv, __int_as_float(st.best_tri));
-    } else if (MODE == 1) {
-      const uint32_t p = q.spix[idx];
-      const float4 nee4 = q.snee[idx], add4 = q.sadd[idx];
+    } else if (MODE == 1 || MODE == 4) {
+      const uint32_t j = MODE == 4 ? (uint32_t)idx - count_c : (uint32_t)idx;
+      const uint32_t p = q.spix[j];
+      const float4 nee4 = q.snee[j], add4 = q.sadd[j];
       const float3 nee = st.best_tri >= 0 ? f3(0.f) : f3(nee4.x, nee4.y, nee4.z);
       const float3 add = f3(add4.x, add4.y, add4.z);
       const float4 rd = q.rad[p];
@@ -648,14 +748,19 @@ __global__ void __launch_bounds__(128, 8) k_traverse(SceneView sc, Queues q, Cou
     }
     idx = -1;
   }
-  if (MODE == 0) {
+  if (MODE == 4) {
+    warp_add64(&c->nodes_closest, nn);
+    warp_add64(&c->tris_closest, nt);
+    warp_add64(&c->nodes_shadow, nn_s);
+    warp_add64(&c->tris_shadow, nt_s);
+  } else if (MODE == 0) {
     warp_add64(&c->nodes_closest, nn);
     warp_add64(&c->tris_closest, nt);
   } else if (MODE == 1) {
     warp_add64(&c->nodes_shadow, nn);
     warp_add64(&c->tris_shadow, nt);
   }
-  if (err) atomicOr(MODE <= 1 ? &c->error : io.errflag, 1u);
+  if (err) atomicOr((MODE <= 1 || MODE == 4) ? &c->error : io.errflag, 1u);
 }
 
 // sampleLight (lighting.glsl:19-227): returns the picked light's strength
@@ -801,6 +906,104 @@ PBRT_D float3 sample_light(const SceneView& sc, int mode, float3 pos, float3 n, 
 }
 
 // One bounce of shading for every entry of ray queue k&1.
+PBRT_D uint32_t spread3(uint32_t v) {  // 3-bit value -> bits 0, 3, 6
+  return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4);
+}
+// Sort key of a ray: octant of its direction over the Morton cell of its
+// origin in the BVH root's box (8 cells per axis).
+PBRT_D uint16_t ray_key(const SceneView& sc, float3 o, float3 d) {
+  const float4 r0 = __ldg(reinterpret_cast<const float4*>(sc.nodes));
+  const uint32_t e = __float_as_uint(r0.w);
+  const float sx = __uint_as_float(((e >> 0) & 0xffu) << 23) * 255.f;
+  const float sy = __uint_as_float(((e >> 8) & 0xffu) << 23) * 255.f;
+  const float sz = __uint_as_float(((e >> 16) & 0xffu) << 23) * 255.f;
+  const uint32_t cx = (uint32_t)min(max((int)((o.x - r0.x) / sx * 8.f), 0), 7);
+  const uint32_t cy = (uint32_t)min(max((int)((o.y - r0.y) / sy * 8.f), 0), 7);
+  const uint32_t cz = (uint32_t)min(max((int)((o.z - r0.z) / sz * 8.f), 0), 7);
+  const uint32_t oct = (d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u);
+  return (uint16_t)((oct << 9) | spread3(cx) | (spread3(cy) << 1) | (spread3(cz) << 2));
+}
+
+__global__ void k_sort_hist(const uint32_t* __restrict__ count_ptr, const uint16_t* __restrict__ keys,
+                            uint32_t* __restrict__ bins) {
+  __shared__ uint32_t h[kSortBins];
+  for (int i = threadIdx.x; i < kSortBins; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  const uint32_t n = *((volatile const uint32_t*)count_ptr);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) atomicAdd(&h[keys[i]], 1u);
+  __syncthreads();
+  for (int i = threadIdx.x; i < kSortBins; i += blockDim.x)
+    if (h[i]) atomicAdd(&bins[i], h[i]);
+}
+
+// Exclusive scan of the kSortBins counts in place (one CTA of 1024 threads).
+__global__ void __launch_bounds__(1024) k_sort_scan(uint32_t* __restrict__ bins) {
+  __shared__ uint32_t warp_sums[32];
+  constexpr int kPer = kSortBins / 1024;
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  uint32_t v[kPer], sum = 0;
+#pragma unroll
+  for (int k = 0; k < kPer; ++k) {
+    v[k] = bins[t * kPer + k];
+    sum += v[k];
+  }
+  uint32_t incl = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) warp_sums[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    uint32_t ws = warp_sums[lane], wi = ws;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += y;
+    }
+    warp_sums[lane] = wi - ws;
+  }
+  __syncthreads();
+  uint32_t run = warp_sums[w] + incl - sum;
+#pragma unroll
+  for (int k = 0; k < kPer; ++k) {
+    bins[t * kPer + k] = run;
+    run += v[k];
+  }
+}
+
+// Scatter by key: lanes with equal keys reserve their slots with one atomic.
+template <bool SHADOW>
+__global__ void k_sort_scatter(const uint32_t* __restrict__ count_ptr, Queues q, int nq, uint32_t* __restrict__ offs) {
+  const uint32_t n = *((volatile const uint32_t*)count_ptr);
+  const uint32_t n_round = (n + 31u) & ~31u;
+  const int lane = threadIdx.x & 31;
+  const uint16_t* keys = SHADOW ? q.skey_t : q.key_t;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_round; i += gridDim.x * blockDim.x) {
+    const bool valid = i < n;
+    const uint32_t key = valid ? (uint32_t)keys[i] : 0xffffffffu;
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    const int leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (valid && lane == leader) base = atomicAdd(&offs[key], (uint32_t)__popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (!valid) continue;
+    const uint32_t dst = base + __popc(peers & ((1u << lane) - 1u));
+    if (SHADOW) {
+      q.spix[dst] = q.spix_t[i];
+      q.sorg[dst] = q.sorg_t[i];
+      q.sdir[dst] = q.sdir_t[i];
+      q.snee[dst] = q.snee_t[i];
+      q.sadd[dst] = q.sadd_t[i];
+    } else {
+      q.pix[nq][dst] = q.pix_t[i];
+      q.org[nq][dst] = q.org_t[i];
+      q.dir[nq][dst] = q.dir_t[i];
+    }
+  }
+}
+
 // Shading CTAs resident per SM the register allocation targets (a build
 // knob: more CTAs, fewer registers per thread).
 #ifdef PBRT_SHADE_MIN_BLOCKS
@@ -929,17 +1132,33 @@ __global__ void PBRT_SHADE_BOUNDS k_shade(SceneView sc, const FrameParams* __res
     }
     const int rs = warp_alloc(&c->ray[nq], push_ray);
     if (rs >= 0) {
-      q.pix[nq][rs] = p;
-      q.org[nq][rs] = ray_o;
-      q.dir[nq][rs] = ray_d;
+      if (kSortRays) {
+        q.pix_t[rs] = p;
+        q.org_t[rs] = ray_o;
+        q.dir_t[rs] = ray_d;
+        q.key_t[rs] = ray_key(sc, f3(ray_o.x, ray_o.y, ray_o.z), f3(ray_d.x, ray_d.y, ray_d.z));
+      } else {
+        q.pix[nq][rs] = p;
+        q.org[nq][rs] = ray_o;
+        q.dir[nq][rs] = ray_d;
+      }
     }
     const int ss = warp_alloc(&c->shadow, push_shadow);
     if (ss >= 0) {
-      q.spix[ss] = p;
-      q.sorg[ss] = sh_o;
-      q.sdir[ss] = sh_d;
-      q.snee[ss] = sh_nee;
-      q.sadd[ss] = sh_add;
+      if (kSortRays) {
+        q.spix_t[ss] = p;
+        q.sorg_t[ss] = sh_o;
+        q.sdir_t[ss] = sh_d;
+        q.snee_t[ss] = sh_nee;
+        q.sadd_t[ss] = sh_add;
+        q.skey_t[ss] = ray_key(sc, f3(sh_o.x, sh_o.y, sh_o.z), f3(sh_d.x, sh_d.y, sh_d.z));
+      } else {
+        q.spix[ss] = p;
+        q.sorg[ss] = sh_o;
+        q.sdir[ss] = sh_d;
+        q.snee[ss] = sh_nee;
+        q.sadd[ss] = sh_add;
+      }
     }
   }
 }
@@ -1112,17 +1331,44 @@ static int record_frame(PbrtPipeline* pp, cudaStream_t s, StageEvents* ev) {
   // not count towards the depth (ptRaygen.rgen:69, up to 10 of them).
   const int bounces = pp->max_depth + 1 + (pp->scene->transmissive ? 10 : 0);
   for (int k = 0; k < bounces; ++k) {
-    k_bounce_begin<<<1, 1, 0, s>>>(pp->ctr, k);
-    if (ev) ev->begin(1);
-    k_traverse<0><<<pp->grid_persistent, 128, 0, s>>>(sc, pp->q, pp->ctr, k, QueryIO{});
-    if (ev) ev->end(1);
+    if (kMergeShadow) {
+      k_bounce_begin_merged<<<1, 1, 0, s>>>(pp->ctr, k);
+      if (ev) ev->begin(1);
+      if (k == 0) k_traverse<0><<<pp->grid_persistent, 128, 0, s>>>(sc, pp->q, pp->ctr, k, QueryIO{});
+      else k_traverse<4><<<pp->grid_persistent, 128, 0, s>>>(sc, pp->q, pp->ctr, k, QueryIO{});
+      if (ev) ev->end(1);
+      k_shadow_consumed<<<1, 1, 0, s>>>(pp->ctr);
+    } else {
+      k_bounce_begin<<<1, 1, 0, s>>>(pp->ctr, k);
+      if (ev) ev->begin(1);
+      k_traverse<0><<<pp->grid_persistent, 128, 0, s>>>(sc, pp->q, pp->ctr, k, QueryIO{});
+      if (ev) ev->end(1);
+    }
     if (ev) ev->begin(2);
     k_shade<<<pp->grid_shade, 128, 0, s>>>(sc, pp->dev_fp, pp->q, pp->ctr, g, k);
+    if (kSortRays) {
+      const int nq = (k + 1) & 1;
+      uint32_t* bins_r = pp->q.bins;
+      uint32_t* bins_s = pp->q.bins + kSortBins;
+      const int sort_grid = std::min((N + 255) / 256, 152 * 4);
+      cudaMemsetAsync(pp->q.bins, 0, 2 * kSortBins * sizeof(uint32_t), s);
+      if (k + 1 < bounces) {
+        k_sort_hist<<<sort_grid, 256, 0, s>>>(&pp->ctr->ray[nq], pp->q.key_t, bins_r);
+        k_sort_scan<<<1, 1024, 0, s>>>(bins_r);
+        k_sort_scatter<false><<<sort_grid, 256, 0, s>>>(&pp->ctr->ray[nq], pp->q, nq, bins_r);
+      }
+      k_sort_hist<<<sort_grid, 256, 0, s>>>(&pp->ctr->shadow, pp->q.skey_t, bins_s);
+      k_sort_scan<<<1, 1024, 0, s>>>(bins_s);
+      k_sort_scatter<true><<<sort_grid, 256, 0, s>>>(&pp->ctr->shadow, pp->q, 0, bins_s);
+    }
     if (ev) ev->end(2);
-    if (ev) ev->begin(3);
-    k_traverse<1><<<pp->grid_persistent, 128, 0, s>>>(sc, pp->q, pp->ctr, k, QueryIO{});
-    if (ev) ev->end(3);
-    k_bounce_end<<<1, 1, 0, s>>>(pp->ctr);
+    if (!kMergeShadow || k + 1 == bounces) {  // merged: the last bounce's shadow rays go alone
+      if (ev) ev->begin(3);
+      if (kMergeShadow) k_shadow_begin<<<1, 1, 0, s>>>(pp->ctr);
+      k_traverse<1><<<pp->grid_persistent, 128, 0, s>>>(sc, pp->q, pp->ctr, k, QueryIO{});
+      if (ev) ev->end(3);
+      k_bounce_end<<<1, 1, 0, s>>>(pp->ctr);
+    }
   }
   if (ev) ev->begin(4);
   k_finalize<<<blocks_px, 256, 0, s>>>(pp->dev_fp, pp->q, out);
@@ -1417,6 +1663,19 @@ PBRT_API int pbrt_pipeline_create(PbrtScene* scene, PbrtGBuffer* g, PbrtIllumina
   if (!st) st = pp->a(&q.prev, N);
   if (!st) st = pp->a(&q.alb, N);
   if (!st) st = pp->a(&q.prim_key, N);
+  if (kSortRays) {
+    if (!st) st = pp->a(&q.pix_t, N);
+    if (!st) st = pp->a(&q.org_t, N);
+    if (!st) st = pp->a(&q.dir_t, N);
+    if (!st) st = pp->a(&q.key_t, N);
+    if (!st) st = pp->a(&q.spix_t, N);
+    if (!st) st = pp->a(&q.sorg_t, N);
+    if (!st) st = pp->a(&q.sdir_t, N);
+    if (!st) st = pp->a(&q.snee_t, N);
+    if (!st) st = pp->a(&q.sadd_t, N);
+    if (!st) st = pp->a(&q.skey_t, N);
+    if (!st) st = pp->a(&q.bins, 2 * kSortBins);
+  }
   if (!st) st = pp->a(&pp->ctr, 1);
   if (!st) st = pp->a(&pp->dev_fp, 1);
   if (!st) {
