@@ -53,12 +53,29 @@ def parse():
     ap.add_argument("--texture-size", type=int, default=1024)
     ap.add_argument("--denoiser", default="neural", choices=["neural", "bmfr", "bfr"],
                     help="neural: U-Net with BMFR as variance-gate fallback (BMFR runs every frame)")
-    ap.add_argument("--gate-threshold", type=float, default=0.5,
+    ap.add_argument("--gate-threshold", type=float, default=0.05,
                     help="neural path: tiles whose predicted relative squared error exceeds this show BMFR")
     ap.add_argument("--weights", default=None, help="neural path: .npz of trained parameters (default: packaged)")
     ap.add_argument("--ref-spp", type=int, default=4096, help="samples of the relMSE reference render (0: skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
+
+
+def max_over_ranks(ms: float, world: int, device=None) -> float:
+    """The job's time for a timed region: the slowest rank's (all ranks call this)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(world: int, steps: int, total_ms: float) -> float:
+    """Whole-job frames per second: every rank renders `steps` frames (weak scaling)."""
+    return world * steps / (total_ms / 1e3)
 
 
 def dist_env():
@@ -207,7 +224,8 @@ def run_reference(args):
         "metric": METRIC, "value": 1.0 / per, "unit": "fps", "impl": "reference", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-        "config": {"workload": "1080p 1spp depth8 RR>=3, 1M-tri instanced scene, BMFR 32x32",
+        "config": {"workload": "1080p 1spp depth8 RR>=3, 1M-tri instanced scene, BMFR 32x32 (the reference has "
+                               "no learned denoiser: its frame is trace + accumulate + BMFR)",
                    "width": args.width, "height": args.height, "max_depth": args.max_depth,
                    "min_depth": args.min_depth, "instances": args.instances},
         "cpu_baseline": {k: info[k] for k in ("value", "unit", "cores", "kind", "sample")},
@@ -401,10 +419,7 @@ def run_gb300(args):
     st1 = pipe.stats(stream)
     rays = (st1.primary_rays - st0.primary_rays) + (st1.extension_rays - st0.extension_rays) + \
         (st1.shadow_rays - st0.shadow_rays)
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, world, dev)
 
     # ---- the same frames with FP8 (e4m3) convolutions, calibrated on the current frame
     fp8_ms = None
@@ -498,7 +513,7 @@ def run_gb300(args):
     dominant = max(stages, key=stages.get)
     if rank == 0:
         steps = args.steps
-        value = world * steps / (total_ms / 1e3)
+        value = job_throughput(world, steps, total_ms)
         clocks = clk.summary()
         cpu = None
         if not args.no_cpu_baseline:

@@ -448,8 +448,10 @@ PBRT_API int pbrt_synth_texture(uint64_t seed, uint32_t size, int32_t kind, cons
  * vulkanpbrt_gb300/kpunet.py. */
 /* y = relu?(conv3x3(concat(x1, upsample2(x2))) + bias), zero padding.
  * w [cout][9][c1+c2] BF16 (tap = ky*3+kx); x2 may be null (c2 = 0).
- * flags bit 0: ReLU; bit 1: add into y32 instead of storing. y (BF16) and
- * y32 (FP32) are both optional, at least one is given. */
+ * flags bit 0: ReLU; bit 1: add into y32 instead of storing; bit 2: the
+ * per-(tap, 16-channel) pipelined kernel; bit 3: no 16 x 16-tile kernel for
+ * cout <= 48 (kernel choice only, same result). y (BF16) and y32 (FP32) are
+ * both optional, at least one is given. */
 PBRT_API int pbrt_nn_conv3x3(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* w, const float* bias,
                              void* y, float* y32, int32_t n, int32_t h, int32_t w_px, int32_t cout, int32_t flags,
                              pbrt_stream_t stream);

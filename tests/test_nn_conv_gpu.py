@@ -28,11 +28,12 @@ def _close(got, want, tol=4e-3):
     return err / scale, err <= tol * scale
 
 
-@pytest.mark.parametrize("kernel", ["halo", "kstep"])
+@pytest.mark.parametrize("kernel", ["halo", "halo4x2", "kstep"])
 @pytest.mark.parametrize("n,h,w,c1,c2,cout", [(2, 24, 40, 16, 0, 32), (1, 32, 32, 32, 0, 48), (1, 16, 48, 48, 32, 48),
                                              (2, 20, 36, 64, 0, 160), (1, 18, 34, 96, 128, 96),
                                              (1, 10, 22, 48, 64, 48), (1, 12, 16, 32, 48, 32),
-                                             (1, 8, 16, 128, 0, 128), (1, 9, 17, 16, 0, 64)])
+                                             (1, 8, 16, 128, 0, 128), (1, 9, 17, 16, 0, 64),
+                                             (2, 33, 47, 32, 0, 16), (1, 18, 30, 16, 16, 48)])
 def test_conv3x3_forward(cuda, n, h, w, c1, c2, cout, kernel):
     import torch
 

@@ -62,7 +62,8 @@ struct ConvArgs {
   bf16* y;             // [N][H][W][cout] (ldy = cout)
   float* y32;          // optional FP32 copy of the output
   int N, H, W, cout;
-  int relu;            // bit 0: ReLU; bit 1: add into y32 instead of overwriting; bit 2: k-step kernel
+  int relu;            // bit 0: ReLU; bit 1: add into y32 instead of overwriting; bit 2: k-step kernel;
+                       // bit 3: no wide-tile kernel
 };
 
 // Output tile: 8 rows x 16 columns = 128 pixels; BN output channels; K steps
@@ -309,6 +310,151 @@ __global__ void __launch_bounds__(256) conv3x3_halo_kernel(ConvArgs a) {
 #pragma unroll
       for (int j = 0; j < WN; ++j) {
         const int co = co0 + wn * (8 * WN) + j * 8 + 2 * (lane & 3);
+        if (co >= a.cout) continue;
+        float v0 = acc[i][j][2 * half], v1 = acc[i][j][2 * half + 1];
+        if (a.bias) {
+          v0 += a.bias[co];
+          v1 += a.bias[co + 1];
+        }
+        if (a.relu & 1) {
+          v0 = fmaxf(v0, 0.f);
+          v1 = fmaxf(v1, 0.f);
+        }
+        if (a.y) *reinterpret_cast<__nv_bfloat162*>(a.y + base + co) = __floats2bfloat162_rn(v0, v1);
+        if (a.y32) {
+          float2* d = reinterpret_cast<float2*>(a.y32 + base + co);
+          if (a.relu & 2) {
+            const float2 o = *d;
+            v0 += o.x;
+            v1 += o.y;
+          }
+          *d = make_float2(v0, v1);
+        }
+      }
+    }
+  }
+}
+
+// Wide-tile variant for narrow outputs (Cout <= 64): all eight warps split
+// the pixels of a 16 x 16 tile (32 each) and every warp computes all of the
+// CTA's output channels, so one A fragment feeds NT/2..NT MMAs and B
+// fragments come two n-tiles per ldmatrix.x4 (about half the ldmatrix
+// traffic per MMA of the 4 x 2 warp layout).
+constexpr int kMTH = 16;  // tile rows (x kTW = 16 columns)
+constexpr int kMHaloH = kMTH + 2, kMHaloPx = kMHaloH * kHaloW;
+
+template <int NT, int KC>
+struct HaloMCfg {
+  static constexpr int BN = 8 * NT;
+  static constexpr int kRowHalo = KC + (KC == 16 ? 0 : 8);
+  static constexpr int kRowW = 9 * KC + 8;
+  static constexpr int kStageElems = kMHaloPx * kRowHalo + BN * kRowW;
+  static constexpr size_t kSmem = 2 * (size_t)kStageElems * sizeof(bf16);
+};
+
+template <int NT, int KC>
+__global__ void __launch_bounds__(256) conv3x3_halo_m_kernel(ConvArgs a) {
+  typedef HaloMCfg<NT, KC> Cfg;
+  constexpr int BN = Cfg::BN, RH = Cfg::kRowHalo, RW = Cfg::kRowW;
+  extern __shared__ __align__(128) bf16 smem[];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tiles_x = (a.W + kTW - 1) / kTW;
+  const int x0 = (blockIdx.x % tiles_x) * kTW, y0 = (blockIdx.x / tiles_x) * kMTH;
+  const int n = blockIdx.y;
+  const int co0 = blockIdx.z * BN;
+  const int cin = a.c1 + a.c2;
+  const int nchunks = (cin + KC - 1) / KC;
+  const int H2 = a.H >> 1, W2 = a.W >> 1;
+  auto halo = [&](int st) { return smem + (size_t)st * Cfg::kStageElems; };
+  auto wts = [&](int st) { return smem + (size_t)st * Cfg::kStageElems + kMHaloPx * RH; };
+  auto load_chunk = [&](int st, int ch) {
+    const int c0 = ch * KC;
+    bf16* sh = halo(st);
+    constexpr int kPieces = KC / 8;
+    for (int i = tid; i < kMHaloPx * kPieces; i += 256) {
+      const int hp = i / kPieces, pc = i % kPieces;
+      const int yy = y0 - 1 + hp / kHaloW, xx = x0 - 1 + hp % kHaloW;
+      const int ci = c0 + pc * 8;
+      const bool ok = yy >= 0 && yy < a.H && xx >= 0 && xx < a.W && ci < cin;
+      const bf16* src = a.x1;
+      if (ok) {
+        if (ci < a.c1) src = a.x1 + (((size_t)n * a.H + yy) * a.W + xx) * a.c1 + ci;
+        else src = a.x2 + (((size_t)n * H2 + (yy >> 1)) * W2 + (xx >> 1)) * a.c2 + (ci - a.c1);
+      }
+      cp_async16(sh + hp * RH + pc * 8, src, ok);
+    }
+    bf16* sw = wts(st);
+    for (int i = tid; i < BN * 9 * kPieces; i += 256) {
+      const int row = i / (9 * kPieces), r = i % (9 * kPieces);
+      const int tap = r / kPieces, pc = r % kPieces;
+      const int co = co0 + row, ci = c0 + pc * 8;
+      const bool ok = co < a.cout && ci < cin;
+      const bf16* src = ok ? a.w + ((size_t)co * 9 + tap) * cin + ci : a.w;
+      cp_async16(sw + row * RW + tap * KC + pc * 8, src, ok);
+    }
+  };
+  float acc[2][NT][4];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < NT; ++j)
+#pragma unroll
+      for (int k = 0; k < 4; ++k) acc[i][j][k] = 0.f;
+  int pr[2], pcl[2];
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const int m = warp * 32 + i * 16 + (lane & 7) + 8 * ((lane >> 3) & 1);
+    pr[i] = m / kTW;
+    pcl[i] = m % kTW;
+  }
+  const int acol = 8 * (lane >> 4);
+  const int brow = (lane & 7) + 8 * (lane >> 4), bcol = 8 * ((lane >> 3) & 1);
+  load_chunk(0, 0);
+  cp_async_commit();
+  for (int ch = 0; ch < nchunks; ++ch) {
+    const int st = ch & 1;
+    if (ch + 1 < nchunks) load_chunk(st ^ 1, ch + 1);
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();
+    const uint32_t hbase = smem_u32(halo(st)), wbase = smem_u32(wts(st));
+#pragma unroll
+    for (int tap = 0; tap < 9; ++tap) {
+      const int dy = tap / 3, dx = tap % 3;
+#pragma unroll
+      for (int kk = 0; kk < KC; kk += 16) {
+        uint32_t af[2][4];
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+          const int hp = (pr[i] + dy) * kHaloW + pcl[i] + dx;
+          ldsm_x4(hbase + (uint32_t)((hp * RH + kk + acol) * 2), af[i][0], af[i][1], af[i][2], af[i][3]);
+        }
+#pragma unroll
+        for (int j = 0; j < NT; j += 2) {
+          uint32_t b0, b1, b2, b3;
+          ldsm_x4(wbase + (uint32_t)(((j * 8 + brow) * RW + tap * KC + kk + bcol) * 2), b0, b1, b2, b3);
+#pragma unroll
+          for (int i = 0; i < 2; ++i) {
+            mma_bf16(acc[i][j], af[i][0], af[i][1], af[i][2], af[i][3], b0, b1);
+            mma_bf16(acc[i][j + 1], af[i][0], af[i][1], af[i][2], af[i][3], b2, b3);
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  cp_async_wait<0>();
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const int p = warp * 32 + i * 16 + (lane >> 2) + 8 * half;
+      const int oy = y0 + p / kTW, ox = x0 + p % kTW;
+      if (oy >= a.H || ox >= a.W) continue;
+      const size_t base = (((size_t)n * a.H + oy) * a.W + ox) * a.cout;
+#pragma unroll
+      for (int j = 0; j < NT; ++j) {
+        const int co = co0 + j * 8 + 2 * (lane & 3);
         if (co >= a.cout) continue;
         float v0 = acc[i][j][2 * half], v1 = acc[i][j][2 * half + 1];
         if (a.bias) {
@@ -719,10 +865,27 @@ template <int WN, int KC> int launch_halo(const ConvArgs& a, cudaStream_t s) {
   conv3x3_halo_kernel<WN, KC><<<grid, 256, Cfg::kSmem, s>>>(a);
   return PBRT_OK;
 }
+template <int NT, int KC> int launch_halo_m(const ConvArgs& a, cudaStream_t s) {
+  typedef HaloMCfg<NT, KC> Cfg;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(conv3x3_halo_m_kernel<NT, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)Cfg::kSmem);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(conv3x3_halo_m_kernel)");
+    attr_set = true;
+  }
+  dim3 grid(((a.W + kTW - 1) / kTW) * ((a.H + kMTH - 1) / kMTH), a.N, (a.cout + Cfg::BN - 1) / Cfg::BN);
+  conv3x3_halo_m_kernel<NT, KC><<<grid, 256, Cfg::kSmem, s>>>(a);
+  return PBRT_OK;
+}
 // Wide channel chunks (fewer barriers) while the weight slab stays small.
 template <int WN> int launch_halo_for(const ConvArgs& a, cudaStream_t s) {
-  if constexpr (WN <= 4) return launch_halo<WN, 32>(a, s);
-  else return launch_halo<WN, 16>(a, s);
+  if constexpr (WN <= 4) {
+    if (a.c1 + a.c2 <= 16) return launch_halo<WN, 16>(a, s);  // one 16-channel chunk: no zero half
+    return launch_halo<WN, 32>(a, s);
+  } else {
+    return launch_halo<WN, 16>(a, s);
+  }
 }
 template <int WN> int launch_fp8(const Fp8ConvArgs& a, cudaStream_t s) {
   typedef Fp8Cfg<WN> Cfg;
@@ -767,6 +930,17 @@ PBRT_API int pbrt_nn_conv3x3(const void* x1, int32_t c1, const void* x2, int32_t
     return check_launch("conv3x3_fwd_kernel");
   }
   int st;
+  if ((relu & 8) == 0 && cout <= 48) {  // wide-tile kernel for narrow outputs (measured faster up to 48)
+    const bool k16 = c1 + c2 <= 16;
+    switch (cout / 16) {
+      case 1: st = k16 ? launch_halo_m<2, 16>(a, stream) : launch_halo_m<2, 32>(a, stream); break;
+      case 2: st = k16 ? launch_halo_m<4, 16>(a, stream) : launch_halo_m<4, 32>(a, stream); break;
+      case 3: st = k16 ? launch_halo_m<6, 16>(a, stream) : launch_halo_m<6, 32>(a, stream); break;
+      default: st = k16 ? launch_halo_m<8, 16>(a, stream) : launch_halo_m<8, 32>(a, stream); break;
+    }
+    if (st) return st;
+    return check_launch("conv3x3_halo_m_kernel");
+  }
   switch (bn / 16) {
     case 1: st = launch_halo_for<1>(a, stream); break;
     case 2: st = launch_halo_for<2>(a, stream); break;

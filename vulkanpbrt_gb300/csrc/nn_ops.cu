@@ -164,29 +164,47 @@ struct HeadArgs {
   int N, H, W, C, K;
 };
 
+// CT, KT > 0: channel and logit counts fixed at compile time (the network's
+// three heads), so the logits stay in registers; 0: any (runtime loops).
+template <int CT, int KT>
 __global__ void kp_head_fwd_kernel(HeadArgs a) {
   extern __shared__ float sW[];  // [K][C]
-  for (int i = threadIdx.x; i < a.K * a.C; i += blockDim.x) sW[i] = a.Wh[i];
+  const int C = CT > 0 ? CT : a.C, K = KT > 0 ? KT : a.K;
+  for (int i = threadIdx.x; i < K * C; i += blockDim.x) sW[i] = a.Wh[i];
   __syncthreads();
   const long P = (long)a.N * a.H * a.W;
   GRID_STRIDE(p, P) {
     const int x = (int)(p % a.W), y = (int)((p / a.W) % a.H), n = (int)(p / ((long)a.W * a.H));
     float lg[27];
-    for (int k = 0; k < a.K; ++k) lg[k] = a.bh[k];
-    const bf16* f = a.F + p * a.C;
-    for (int c = 0; c < a.C; c += 2) {
-      float2 v = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(f + c));
-      for (int k = 0; k < a.K; ++k) lg[k] += sW[k * a.C + c] * v.x + sW[k * a.C + c + 1] * v.y;
+#pragma unroll
+    for (int k = 0; k < 27; ++k)
+      if (k < K) lg[k] = a.bh[k];
+    const bf16* f = a.F + p * C;
+#pragma unroll 1
+    for (int c = 0; c < C; c += 8) {
+      const uint4 raw = *reinterpret_cast<const uint4*>(f + c);  // 8 channels
+      const uint32_t w4[4] = {raw.x, raw.y, raw.z, raw.w};
+#pragma unroll
+      for (int h = 0; h < 4; ++h) {
+        const float2 v = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w4[h]));
+        const int cc = c + 2 * h;
+#pragma unroll
+        for (int k = 0; k < 27; ++k)
+          if (k < K) lg[k] += sW[k * C + cc] * v.x + sW[k * C + cc + 1] * v.y;
+      }
     }
     float mx = lg[0];
+#pragma unroll
     for (int k = 1; k < kKP; ++k) mx = fmaxf(mx, lg[k]);
     float s = 0.f;
+#pragma unroll
     for (int k = 0; k < kKP; ++k) {
       lg[k] = __expf(lg[k] - mx);
       s += lg[k];
     }
     const float inv = 1.f / s;
     float3 acc = f3(0.f);
+#pragma unroll
     for (int k = 0; k < kKP; ++k) {
       const float w = lg[k] * inv;
       if (a.kw) a.kw[p * kKP + k] = w;
@@ -206,7 +224,7 @@ __global__ void kp_head_fwd_kernel(HeadArgs a) {
       const float* cc = a.coarse + (((size_t)n * (a.H / 2) + y / 2) * (a.W / 2) + x / 2) * 3;
       o = (1.f - al) * acc + al * f3(cc[0], cc[1], cc[2]);
     }
-    if (a.var) a.var[p] = lg[a.coarse ? kKP + 1 : kKP];
+    if (a.var) a.var[p] = a.coarse ? lg[kKP + 1] : lg[kKP];
     a.out[p * 3 + 0] = o.x;
     a.out[p * 3 + 1] = o.y;
     a.out[p * 3 + 2] = o.z;
@@ -460,7 +478,13 @@ PBRT_API int pbrt_nn_kp_head(const void* F, const float* Wh, const float* bh, co
       (var && k <= (coarse ? kKP + 1 : kKP)) || (coarse && k < kKP + 1))
     return fail(PBRT_ERROR_INVALID_ARGUMENT, "kp head: bad arguments");
   HeadArgs a{(const bf16*)F, Wh, bh, R, coarse, out, kw, filt, alpha, var, n, h, w, c, k};
-  kp_head_fwd_kernel<<<grid_for((long)n * h * w, 128), 128, k * c * sizeof(float), s>>>(a);
+  const int g = grid_for((long)n * h * w, 128);
+  const size_t sm = (size_t)k * c * sizeof(float);
+  if (c == 64 && k == 25) kp_head_fwd_kernel<64, 25><<<g, 128, sm, s>>>(a);
+  else if (c == 48 && k == 26) kp_head_fwd_kernel<48, 26><<<g, 128, sm, s>>>(a);
+  else if (c == 32 && k == 27) kp_head_fwd_kernel<32, 27><<<g, 128, sm, s>>>(a);
+  else if (c % 8 == 0) kp_head_fwd_kernel<0, 0><<<g, 128, sm, s>>>(a);
+  else return fail(PBRT_ERROR_INVALID_ARGUMENT, "kp head: channels must be a multiple of 8");
   return check_launch("kp_head_fwd");
 }
 

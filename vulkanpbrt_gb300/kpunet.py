@@ -284,3 +284,42 @@ class Workspace:
         net.step_count += 1
         nn.adam(net.w32, net.grad, net.m, net.v, net.step_count, lr=lr, w_bf16=net.w16)
         return self.loss
+
+
+def main(argv=None):
+    """Times the network's forward pass (and its layers) on random inputs:
+    python -m vulkanpbrt_gb300.kpunet [--height 1088 --width 1920 --iters 10]."""
+    import argparse
+    import json
+
+    import torch
+
+    ap = argparse.ArgumentParser(description="time the kernel-predicting U-Net forward pass")
+    ap.add_argument("--height", type=int, default=1088)
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--batch", type=int, default=1)
+    ap.add_argument("--iters", type=int, default=10)
+    a = ap.parse_args(argv)
+    from . import build
+
+    build.build()
+    dev = torch.device("cuda", 0)
+    net = KPUNet(dev, seed=0)
+    ws = net.workspace(a.batch, a.height, a.width, training=False)
+    ws.feat.normal_()
+    ws.rad[0].uniform_()
+    ws.forward()  # warm-up
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(a.iters):
+        ws.forward()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / a.iters
+    flop = sum(2 * 9 * (c1 + c2) * co * (a.height >> l) * (a.width >> l) for _, (c1, c2), co, l in CONVS) * a.batch
+    print(json.dumps({"forward_ms": ms, "conv_tflops_per_s": flop / ms / 1e9, "pixels": a.height * a.width * a.batch}))
+
+
+if __name__ == "__main__":
+    main()

@@ -31,7 +31,7 @@ _abi.add_signatures({
     "pbrt_nn_compose": (i32, [H, i32, i32, i32, H, H, i32, H, H, H, H]),
 })
 
-RELU, ACCUMULATE, KSTEP = 1, 2, 4
+RELU, ACCUMULATE, KSTEP, NO_WIDE = 1, 2, 4, 8
 
 
 def _ptr(t):
@@ -49,7 +49,8 @@ def conv3x3(x1, w, bias=None, x2=None, relu=False, out=None, out32=None, accumul
     """y = relu?(conv3x3(concat(x1, up2(x2))) + bias). x1 [N,H,W,C1] bf16, x2 [N,H/2,W/2,C2] bf16,
     w [Cout, 9, C1+C2] bf16, bias [Cout] f32. Returns the BF16 output [N,H,W,Cout] (None when
     store_bf16 is False: only out32 is written, added to when accumulate is set). kernel: "halo"
-    (input halo staged once per channel chunk) or "kstep" (pipelined per tap and 16 channels)."""
+    (input halo staged once per channel chunk; 16 x 16 tiles for Cout <= 48), "halo4x2" (8 x 16 tiles
+    only) or "kstep" (pipelined per tap and 16 channels)."""
     import torch
 
     n, h, wd, c1 = x1.shape
@@ -57,7 +58,8 @@ def conv3x3(x1, w, bias=None, x2=None, relu=False, out=None, out32=None, accumul
     cout = w.shape[0]
     if out is None and store_bf16:
         out = torch.empty((n, h, wd, cout), dtype=torch.bfloat16, device=x1.device)
-    flags = (RELU if relu else 0) | (ACCUMULATE if accumulate else 0) | (KSTEP if kernel == "kstep" else 0)
+    flags = (RELU if relu else 0) | (ACCUMULATE if accumulate else 0) | (KSTEP if kernel == "kstep" else 0) | \
+        (NO_WIDE if kernel == "halo4x2" else 0)
     check(lib().pbrt_nn_conv3x3(_ptr(x1), c1, _ptr(x2), c2, _ptr(w), _ptr(bias), _ptr(out if store_bf16 else None),
                                 _ptr(out32), n, h, wd, cout, flags, _stream()))
     return out if store_bf16 else None
