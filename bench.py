@@ -509,7 +509,7 @@ def run_gb300(args):
     per_launch_s = trav_ms / 1e3 / launches
     achieved = closest_bytes / launches / per_launch_s / 1e9
     peak, peak_kind = peaks()
-    traffic = profile_traffic("k_trace_closest")
+    traffic = profile_traffic("k_traverse")
     dominant = max(stages, key=stages.get)
     if rank == 0:
         steps = args.steps

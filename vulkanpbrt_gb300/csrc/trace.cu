@@ -598,8 +598,14 @@ struct QueryIO {
   uint32_t* errflag;
 };
 
+// Traversal CTAs resident per SM the register allocation targets (a build
+// knob; 8 x 128 threads at <= 64 registers).
+#ifndef PBRT_TRAVERSE_MIN_BLOCKS
+#define PBRT_TRAVERSE_MIN_BLOCKS 8
+#endif
 template <int MODE>
-__global__ void __launch_bounds__(128, 8) k_traverse(SceneView sc, Queues q, Counters* c, int k, QueryIO io) {
+__global__ void __launch_bounds__(128, PBRT_TRAVERSE_MIN_BLOCKS) k_traverse(SceneView sc, Queues q, Counters* c, int k,
+                                                                          QueryIO io) {
   // MODE 4: the closest-hit rays of queue k&1 followed by the shadow rays
   // of the previous bounce, in one launch (one work counter over both)
   constexpr bool ANY = (MODE == 1 || MODE == 3);

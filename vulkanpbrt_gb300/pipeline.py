@@ -209,6 +209,10 @@ class PBRTPipeline(Handle):
     def set_abort(self, on: bool) -> None:
         self.abort_flag()[0] = 1 if on else 0
 
+    def set_launch(self, trace_blocks_per_sm: int = 8, shade_blocks_per_sm: int = 8) -> None:
+        """Persistent traversal CTAs and shading CTAs per SM (1..16)."""
+        check(lib().pbrt_pipeline_set_launch(self.ptr, trace_blocks_per_sm, shade_blocks_per_sm))
+
     def set_budget(self, budget_ns: int) -> None:
         check(lib().pbrt_pipeline_set_budget(self.ptr, int(budget_ns)))
 
