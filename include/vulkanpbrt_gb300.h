@@ -462,6 +462,14 @@ PBRT_API int pbrt_nn_conv3x3(const void* x1, int32_t c1, const void* x2, int32_t
 PBRT_API int pbrt_nn_conv3x3_fp8(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* w8,
                                  const float* wscale, const float* inv_xscale, const float* bias, void* y, int32_t n,
                                  int32_t h, int32_t w_px, int32_t cout, int32_t flags, pbrt_stream_t stream);
+/* tcgen05 variant (5th-generation tensor cores, accumulator in tensor
+ * memory): BF16 output only, cout in {16, 32, ..., 128}, flags bit 0 ReLU. */
+PBRT_API int pbrt_nn_conv3x3_umma(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* w,
+                                  const float* bias, void* y, int32_t n, int32_t h, int32_t w_px, int32_t cout,
+                                  int32_t flags, pbrt_stream_t stream);
+/* Error flags of the tcgen05 kernels since the last call (bit 0: a bounded
+ * wait timed out), reset on read (stream-synchronising). */
+PBRT_API int pbrt_nn_umma_status(pbrt_stream_t stream, uint32_t* flags);
 /* wscale[co] = max |w x xscale| / 448 over the channel, w8 = e4m3(w x xscale / wscale). */
 PBRT_API int pbrt_nn_quantize_weights_fp8(const float* w, const float* xscale, int32_t cout, int32_t cin, void* w8,
                                           float* wscale, pbrt_stream_t stream);
@@ -555,6 +563,15 @@ PBRT_API int pbrt_neural_set_fallback(PbrtNeural* nd, PbrtBMFR* bmfr, float thre
  * set_precision(16) returns to BF16. New parameters drop the calibration. */
 PBRT_API int pbrt_neural_calibrate(PbrtNeural* nd, pbrt_stream_t stream);
 PBRT_API int pbrt_neural_set_precision(PbrtNeural* nd, int32_t bits);
+/* Per-layer convolution kernel: 0 = warp-level mma.sync kernels, 1 =
+ * tcgen05 (tensor memory, TMA). autotune (run by the first dispatch when no
+ * choice was set) times both for every layer on the current inputs and
+ * keeps the faster (stream-synchronising); conv_kernels reads the choice
+ * (18 entries, layer order of vulkanpbrt_gb300/kpunet.py), set_conv_kernels
+ * fixes it. */
+PBRT_API int pbrt_neural_autotune(PbrtNeural* nd, pbrt_stream_t stream);
+PBRT_API int pbrt_neural_conv_kernels(const PbrtNeural* nd, int32_t* kinds, int32_t count);
+PBRT_API int pbrt_neural_set_conv_kernels(PbrtNeural* nd, const int32_t* kinds, int32_t count);
 PBRT_API int pbrt_neural_dispatch(PbrtNeural* nd, pbrt_stream_t stream);
 /* The same launches without the graph (for per-kernel profiling). */
 PBRT_API int pbrt_neural_dispatch_direct(PbrtNeural* nd, pbrt_stream_t stream);

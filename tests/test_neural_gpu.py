@@ -48,17 +48,24 @@ def test_native_forward_equals_training_forward(cuda):
     _random_frame(g, illu, 1)
     p = _params(3)
     nd = NeuralDenoiser(W, H, g, illu, weights=p)
-    nd.dispatch()
+    nd.dispatch()  # tunes the per-layer kernel choice, then captures the graph
     nd.dispatch()  # graph replay
     torch.cuda.synchronize()
     got = nd.denoised.tensor()[..., :3].cpu()
+    kinds = nd.conv_kernels()
     net = K.KPUNet(cuda, params=p)
     ws = net.workspace(1, 128, 208, training=False)
     ws.set_input(illu.illumination_images[0].tensor()[None], g.albedo.tensor()[None], g.normal.tensor()[None],
                  g.depth.tensor()[None, ..., 0])
-    want = ws.forward()[0, :H, :W].cpu()
+    want = ws.forward(kinds)[0, :H, :W].cpu()
     torch.cuda.synchronize()
     assert torch.equal(got, want)
+    # a fixed choice: every layer on the tcgen05 kernel, then every layer on mma.sync
+    for kind in ("umma", "mma"):
+        nd.set_conv_kernels([kind] * 18)
+        nd.dispatch()
+        torch.cuda.synchronize()
+        assert torch.equal(nd.denoised.tensor()[..., :3].cpu(), ws.forward(kind)[0, :H, :W].cpu())
     assert torch.isfinite(got).all()
 
 
@@ -88,6 +95,7 @@ def test_variance_gate_extremes(cuda):
     torch.cuda.synchronize()
     assert nd.fallback_tiles() == 0
     plain = NeuralDenoiser(W, H, g, illu, weights=_params(4))
+    plain.set_conv_kernels(nd.conv_kernels())  # the same per-layer kernels, so the same bits
     plain.dispatch()
     torch.cuda.synchronize()
     assert torch.equal(nd.get_final_descriptor_image().tensor().cpu(), plain.get_final_descriptor_image().tensor().cpu())

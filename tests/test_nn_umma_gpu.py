@@ -1,0 +1,36 @@
+"""The tcgen05 convolutions (accumulator in tensor memory; the per-tile
+form, and the persistent form with its input halo from a TMA load or from
+cp.async gathers) against torch's FP32 conv2d on the same BF16 operands:
+within one BF16 ulp (4e-3) of the output scale, no error flag from their
+bounded waits. Larger images exercise the persistent form's tile loop."""
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("n,h,w,c1,c2,cout", [(1, 16, 8, 16, 0, 32), (2, 24, 40, 16, 0, 32), (1, 32, 32, 32, 0, 48),
+                                             (1, 16, 48, 48, 32, 48), (1, 20, 36, 64, 0, 64),
+                                             (1, 18, 34, 96, 128, 96), (1, 9, 17, 128, 0, 128),
+                                             (1, 34, 46, 32, 48, 32), (2, 136, 240, 32, 48, 32),
+                                             (1, 128, 200, 16, 0, 32)])
+@pytest.mark.parametrize("mode", ["tma", "persistent", "tile"])
+def test_conv3x3_umma_forward(cuda, n, h, w, c1, c2, cout, mode):
+    import torch
+
+    from tests.test_nn_conv_gpu import _close, _ref_conv
+    from vulkanpbrt_gb300 import nn
+
+    g = torch.Generator().manual_seed(n * 100 + c1 + c2 + cout + h)
+    x1 = torch.randn(n, h, w, c1, generator=g).bfloat16().to(cuda)
+    x2 = torch.randn(n, h // 2, w // 2, c2, generator=g).bfloat16().to(cuda) if c2 else None
+    wt = (torch.randn(cout, 9, c1 + c2, generator=g) * 0.1).bfloat16().to(cuda)
+    b = torch.randn(cout, generator=g).float().to(cuda)
+    kw = dict(persistent=mode != "tile", tma=mode == "tma")
+    y = nn.conv3x3_umma(x1, wt, b, x2=x2, relu=False, **kw)
+    yr = nn.conv3x3_umma(x1, wt, b, x2=x2, relu=True, **kw)
+    assert nn.umma_status() == 0
+    ref = _ref_conv(x1, wt, b, x2)
+    rel, ok = _close(y, ref, 4e-3)
+    print(f"umma conv rel err {rel:.2e}")
+    assert ok
+    assert _close(yr, ref.clamp_min(0), 4e-3)[1]

@@ -9,6 +9,7 @@
 // (source/renderModules/BMFR.cpp, source/renderModules/BFR.cpp).
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -93,6 +94,9 @@ struct PbrtNeural : pbrt::Object {
   pbrt::DeviceImage mask;  // R8 per gate tile: 1 = fallback
   uint32_t* counter = nullptr;
   cudaGraphExec_t graph = nullptr;
+  // per layer: 0 = mma.sync kernels, 1 = tcgen05 kernel (chosen by timing both on the first dispatch)
+  int32_t conv_kernel[kNumConvs] = {};
+  bool tuned = false;
   // FP8 inference (pbrt_neural_calibrate / pbrt_neural_set_precision)
   int precision = 16;
   bool calibrated = false;
@@ -140,6 +144,8 @@ int record_forward(PbrtNeural* nd, cudaStream_t s) {
     if (nd->precision == 8) {
       st = pbrt_nn_conv3x3_fp8(in1, c.c1, in2, c.c2, nd->w8 + nd->lay.conv_w[i], nd->wscale + nd->wsoff[i],
                                nd->inv_xscale + nd->xsoff[i], b, nd->act[i], n, h, w, c.cout, 1, s);
+    } else if (nd->conv_kernel[i] == 1) {
+      st = pbrt_nn_conv3x3_umma(in1, c.c1, in2, c.c2, w16, b, nd->act[i], n, h, w, c.cout, 1, s);
     } else {
       st = pbrt_nn_conv3x3(in1, c.c1, in2, c.c2, w16, b, nd->act[i], nullptr, n, h, w, c.cout, 1, s);
     }
@@ -306,8 +312,93 @@ PBRT_API int pbrt_neural_set_fallback(PbrtNeural* nd, PbrtBMFR* bmfr, float thre
   return PBRT_OK;
 }
 
+// Per-layer kernel choice: one forward pass to have every layer's input,
+// then each convolution timed with both kernels (median of 3 after a
+// warm-up, CUDA events) and the faster kept. Stream-synchronising.
+PBRT_API int pbrt_neural_autotune(PbrtNeural* nd, pbrt_stream_t stream) {
+  if (!checked<PbrtNeural>(nd, Kind::Neural)) return fail(PBRT_ERROR_INVALID_ARGUMENT, "neural autotune: not a handle");
+  for (int i = 0; i < kNumConvs; ++i) nd->conv_kernel[i] = 0;
+  const int saved = nd->precision;
+  nd->precision = 16;
+  int st = record_forward(nd, stream);
+  nd->precision = saved;
+  if (st) return st;
+  cudaEvent_t e0, e1;
+  PBRT_CUDA(cudaEventCreate(&e0));
+  PBRT_CUDA(cudaEventCreate(&e1));
+  const int skip_of[4] = {1, 3, 5, 7};
+  for (int i = 0; i < kNumConvs && !st; ++i) {
+    const ConvSpec& c = kConvs[i];
+    const int h = nd->ph >> c.level, w = nd->pw >> c.level;
+    const bf16* in1;
+    const bf16* in2 = nullptr;
+    if (i == 0) in1 = nd->feat;
+    else if (c.c2) {
+      in1 = nd->act[skip_of[c.level]];
+      in2 = nd->act[i - 1];
+    } else if (i < 10 && c.name[2] == 'a') in1 = nd->pool[c.level];
+    else in1 = nd->act[i - 1];
+    const bf16* w16 = nd->w16 + nd->lay.conv_w[i];
+    const float* b = nd->params + nd->lay.conv_b[i];
+    float best[2] = {1e30f, 1e30f};
+    for (int k = 0; k < 2 && !st; ++k) {
+      float ms[3];
+      for (int r = 0; r < 4 && !st; ++r) {
+        cudaEventRecord(e0, stream);
+        st = k ? pbrt_nn_conv3x3_umma(in1, c.c1, in2, c.c2, w16, b, nd->act[i], 1, h, w, c.cout, 1, stream)
+               : pbrt_nn_conv3x3(in1, c.c1, in2, c.c2, w16, b, nd->act[i], nullptr, 1, h, w, c.cout, 1, stream);
+        cudaEventRecord(e1, stream);
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (!st && e != cudaSuccess) st = cuda_fail(e, "neural autotune");
+        if (r > 0) cudaEventElapsedTime(&ms[r - 1], e0, e1);
+      }
+      if (!st) {
+        std::sort(ms, ms + 3);
+        best[k] = ms[1];
+      }
+    }
+    nd->conv_kernel[i] = best[1] < best[0] ? 1 : 0;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  uint32_t flags = 0;
+  if ((st = pbrt_nn_umma_status(stream, &flags))) return st;
+  if (flags) {  // a tcgen05 wait ran out: keep the mma.sync kernels
+    for (int i = 0; i < kNumConvs; ++i) nd->conv_kernel[i] = 0;
+    return fail(PBRT_ERROR_TIMEOUT, "neural autotune: a tcgen05 convolution timed out; using mma.sync");
+  }
+  nd->tuned = true;
+  drop_graph(nd);
+  return PBRT_OK;
+}
+
+PBRT_API int pbrt_neural_conv_kernels(const PbrtNeural* nd, int32_t* kinds, int32_t count) {
+  if (!checked<const PbrtNeural>((void*)nd, Kind::Neural) || !kinds || count < kNumConvs)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "neural conv kernels: bad arguments");
+  for (int i = 0; i < kNumConvs; ++i) kinds[i] = nd->conv_kernel[i];
+  return PBRT_OK;
+}
+
+PBRT_API int pbrt_neural_set_conv_kernels(PbrtNeural* nd, const int32_t* kinds, int32_t count) {
+  if (!checked<PbrtNeural>(nd, Kind::Neural) || !kinds || count != kNumConvs)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "neural set conv kernels: bad arguments");
+  for (int i = 0; i < kNumConvs; ++i) {
+    if (kinds[i] != 0 && kinds[i] != 1) return fail(PBRT_ERROR_INVALID_ARGUMENT, "neural set conv kernels: 0 or 1");
+    nd->conv_kernel[i] = kinds[i];
+  }
+  nd->tuned = true;
+  drop_graph(nd);
+  return PBRT_OK;
+}
+
 PBRT_API int pbrt_neural_dispatch(PbrtNeural* nd, pbrt_stream_t stream) {
   if (!checked<PbrtNeural>(nd, Kind::Neural)) return fail(PBRT_ERROR_INVALID_ARGUMENT, "neural dispatch: not a handle");
+  if (!nd->tuned) {
+    nd->tuned = true;  // once, whatever the outcome
+    int st = pbrt_neural_autotune(nd, stream);
+    if (st && st != PBRT_ERROR_TIMEOUT) return st;
+  }
   if (!nd->graph) {
     cudaStream_t cap;
     PBRT_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));

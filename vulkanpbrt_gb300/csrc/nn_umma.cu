@@ -1,0 +1,624 @@
+// 3x3 convolution forward on the 5th-generation tensor cores (tcgen05): an
+// implicit GEMM with the accumulator in tensor memory. One CTA (4 warps)
+// computes a 16 x 8-pixel output tile (M = 128) for N = Cout <= 128 output
+// channels. Per chunk of up to 32 input channels the CTA stages, with
+// cp.async, the 18 x 10 input halo and the 9 x chunk x N weight slab in
+// shared memory in the K-major "interleaved" layout of the MMA's matrix
+// descriptors (8 x 16-byte core matrices): the halo is stored as planes of
+// 8 channels, pixel rows of the halo 10 pixels apart, so the A operand of
+// every tap is the same descriptor with its start address shifted by the
+// tap's pixel offset (stride between 8-pixel row groups = one halo row).
+// Thread 0 issues 9 x chunk/16 MMAs (kind::f16, BF16 x BF16 -> FP32) per
+// chunk and commits them to an mbarrier, which gates the reuse of the
+// stage two chunks later; the epilogue reads the accumulator with
+// tcgen05.ld (each warp its 32 TMEM lanes = 32 pixels), adds the bias,
+// applies ReLU and stores BF16. Every wait is bounded: on a timeout the
+// kernel records an error (pbrt_nn_umma_status), waits again for its own
+// MMAs, frees its tensor memory and returns.
+#include <cuda.h>  // CUtensorMap (the encoder is fetched through the runtime)
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+
+#include "internal.hpp"
+
+namespace pbrt {
+namespace nn {
+
+typedef __nv_bfloat16 bf16;
+
+__device__ uint32_t g_umma_error = 0;
+
+namespace umma {
+
+constexpr int kTileH = 16, kTileW = 8, kM = kTileH * kTileW;  // 128 pixels
+constexpr int kHaloH = kTileH + 2, kHaloW = kTileW + 2, kHaloPx = kHaloH * kHaloW;  // 180
+constexpr int kKC = 32;                    // input channels per chunk
+constexpr int kPlanes = kKC / 8;           // 8-channel planes per chunk
+constexpr int kPlaneBytes = kHaloPx * 16;  // one plane of the halo: 2880 B
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void cp16(uint32_t dst, const void* src, bool valid) {
+  const int n = valid ? 16 : 0;
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(n));
+}
+
+// Shared-memory matrix descriptor, K-major, no swizzle: start address,
+// leading (K-direction) and stride (M/N-direction) core-matrix offsets, in
+// 16-byte units; version 1.
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo_bytes, uint32_t sbo_bytes) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3fffu);
+  d |= (uint64_t)((lbo_bytes >> 4) & 0x3fffu) << 16;
+  d |= (uint64_t)((sbo_bytes >> 4) & 0x3fffu) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// Instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, M = 128, N = n.
+__host__ __device__ constexpr uint32_t idesc_bf16(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t addr, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(addr), "r"(count));
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t addr, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(addr), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ unsigned long long now_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait for an mbarrier phase: false after ~2 s.
+__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
+  if (mbar_try_wait(addr, parity)) return true;
+  const unsigned long long t0 = now_ns();
+  while (true) {
+    if (mbar_try_wait(addr, parity)) return true;
+    if (now_ns() - t0 > 2000000000ull) return false;
+  }
+}
+
+}  // namespace umma
+
+struct UmmaConvArgs {
+  const bf16* x1;
+  const bf16* x2;
+  int c1, c2;
+  const bf16* w;       // [cout][9][c1 + c2]
+  const float* bias;   // [cout] or null
+  bf16* y;             // [N][H][W][cout]
+  int N, H, W, cout;
+  int relu;
+};
+
+template <int NC>  // output channels (= MMA N), multiple of 16, <= 128
+__global__ void __launch_bounds__(128) conv3x3_umma_kernel(UmmaConvArgs a) {
+  using namespace umma;
+  constexpr int kWBytes = 9 * kPlanes * NC * 16;          // weight slab per stage
+  constexpr int kStage = kPlanes * kPlaneBytes + kWBytes;  // halo + weights
+  constexpr uint32_t kCols = NC <= 32 ? 32 : (NC <= 64 ? 64 : 128);
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ __align__(8) uint64_t mbar[2];
+  __shared__ uint32_t tmem_base_slot;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tiles_x = (a.W + kTileW - 1) / kTileW;
+  const int x0 = (blockIdx.x % tiles_x) * kTileW, y0 = (blockIdx.x / tiles_x) * kTileH;
+  const int n = blockIdx.y;
+  const int cin = a.c1 + a.c2;
+  const int nchunks = (cin + kKC - 1) / kKC;
+  const int H2 = a.H >> 1, W2 = a.W >> 1;
+  const uint32_t sbase = smem_addr(smem);
+  const uint32_t mb0 = smem_addr(&mbar[0]), mb1 = smem_addr(&mbar[1]);
+
+  if (tid == 0) {
+    umma::mbar_init(mb0, 1);
+    umma::mbar_init(mb1, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                     smem_addr(&tmem_base_slot)),
+                 "r"(kCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = tmem_base_slot;
+
+  auto load_chunk = [&](int st, int ch) {
+    const uint32_t hb = sbase + st * kStage, wb = hb + kPlanes * kPlaneBytes;
+    const int c0 = ch * kKC;
+    for (int i = tid; i < kHaloPx * kPlanes; i += 128) {
+      const int hp = i % kHaloPx, p = i / kHaloPx;
+      const int yy = y0 - 1 + hp / kHaloW, xx = x0 - 1 + hp % kHaloW;
+      const int ci = c0 + p * 8;
+      const bool ok = yy >= 0 && yy < a.H && xx >= 0 && xx < a.W && ci < cin;
+      const bf16* src = a.x1;
+      if (ok) {
+        if (ci < a.c1) src = a.x1 + (((size_t)n * a.H + yy) * a.W + xx) * a.c1 + ci;
+        else src = a.x2 + (((size_t)n * H2 + (yy >> 1)) * W2 + (xx >> 1)) * a.c2 + (ci - a.c1);
+      }
+      umma::cp16(hb + p * kPlaneBytes + hp * 16, src, ok);
+    }
+    for (int i = tid; i < NC * 9 * kPlanes; i += 128) {
+      const int co = i % NC, r = i / NC;
+      const int p = r % kPlanes, tap = r / kPlanes;
+      const int ci = c0 + p * 8;
+      const bool ok = co < a.cout && ci < cin;
+      const bf16* src = ok ? a.w + ((size_t)co * 9 + tap) * cin + ci : a.w;
+      umma::cp16(wb + ((tap * kPlanes + p) * NC + co) * 16, src, ok);
+    }
+  };
+
+  bool failed = false;
+  load_chunk(0, 0);
+  asm volatile("cp.async.commit_group;\n" ::);
+  for (int ch = 0; ch < nchunks && !failed; ++ch) {
+    const int st = ch & 1;
+    if (ch + 1 < nchunks) {
+      const int s1 = (ch + 1) & 1;
+      bool ok = true;
+      if (ch + 1 >= 2) ok = umma::mbar_wait(s1 ? mb1 : mb0, (uint32_t)(((ch - 1) >> 1) & 1));
+      if (__syncthreads_or(!ok)) {  // the same decision in every thread
+        failed = true;
+        break;
+      }
+      load_chunk(s1, ch + 1);
+    }
+    asm volatile("cp.async.commit_group;\n" ::);
+    asm volatile("cp.async.wait_group 1;\n" ::);
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      const uint32_t hb = sbase + st * kStage, wb = hb + kPlanes * kPlaneBytes;
+      const int kc = cin - ch * kKC < kKC ? cin - ch * kKC : kKC;  // 16 or 32
+      constexpr uint32_t idesc = umma::idesc_bf16(NC);
+#pragma unroll 1
+      for (int tap = 0; tap < 9; ++tap) {
+        const int dy = tap / 3, dx = tap % 3;
+        for (int ks = 0; ks < kc / 16; ++ks) {
+          const uint64_t da =
+              umma::sdesc(hb + (2 * ks) * kPlaneBytes + (dy * kHaloW + dx) * 16, kPlaneBytes, kHaloW * 16);
+          const uint64_t db = umma::sdesc(wb + ((tap * kPlanes + 2 * ks) * NC) * 16, NC * 16, 8 * 16);
+          const uint32_t acc = (ch > 0 || tap > 0 || ks > 0) ? 1u : 0u;
+          asm volatile(
+              "{\n\t.reg .pred p;\n\t"
+              "setp.ne.b32 p, %4, 0;\n\t"
+              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+              "l"(da), "l"(db), "r"(idesc), "r"(acc));
+        }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                       st ? mb1 : mb0)
+                   : "memory");
+    }
+  }
+  asm volatile("cp.async.wait_group 0;\n" ::);
+  // all MMAs issued so far complete before the accumulator is read or freed
+  const int last = nchunks - 1;
+  bool done = umma::mbar_wait((last & 1) ? mb1 : mb0, (uint32_t)((last >> 1) & 1));
+  if (!done) done = umma::mbar_wait((last & 1) ? mb1 : mb0, (uint32_t)((last >> 1) & 1));  // once more, bounded
+  failed = __syncthreads_or(failed || !done);
+  if (failed) {
+    if (tid == 0) atomicOr(&g_umma_error, 1u);
+  } else {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const int m = warp * 32 + lane;  // TMEM lane = pixel of the tile
+    const int oy = y0 + m / kTileW, ox = x0 + m % kTileW;
+    const bool inside = oy < a.H && ox < a.W;
+    bf16* dst = a.y + (((size_t)n * a.H + (inside ? oy : 0)) * a.W + (inside ? ox : 0)) * a.cout;
+#pragma unroll
+    for (int c0 = 0; c0 < NC; c0 += 16) {
+      uint32_t v[16];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+            "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+      if (inside) {
+        uint32_t packed[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          float f0 = __uint_as_float(v[2 * j]), f1 = __uint_as_float(v[2 * j + 1]);
+          if (a.bias) {
+            f0 += a.bias[c0 + 2 * j];
+            f1 += a.bias[c0 + 2 * j + 1];
+          }
+          if (a.relu & 1) {
+            f0 = fmaxf(f0, 0.f);
+            f1 = fmaxf(f1, 0.f);
+          }
+          const __nv_bfloat162 b2 = __floats2bfloat162_rn(f0, f1);
+          packed[j] = *reinterpret_cast<const uint32_t*>(&b2);
+        }
+        uint4* d4 = reinterpret_cast<uint4*>(dst + c0);
+        d4[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+        d4[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kCols));
+  }
+}
+
+// Persistent form for the large-image layers: the whole weight tensor
+// (9 x Cin x N) stays in shared memory for the CTA's lifetime, and the CTA
+// walks output tiles with a two-deep pipeline: while the tensor cores work
+// on tile i (accumulator buffer i&1 in tensor memory), the CTA loads tile
+// i+1's halo (all Cin channels) into the other halo buffer and drains tile
+// i-1's accumulator (bias, ReLU, BF16 stores). Used when the weights and two
+// halos fit in shared memory.
+// With use_tma, the x1 part of each halo comes in one TMA load (x1 viewed as
+// a 5-D tensor [8 channels][x][y][channel group][image], box
+// [8][10][18][c1/8][1]: exactly the plane layout, out-of-image pixels filled
+// with zeros) that completes on a per-buffer mbarrier; the upsampled x2 part
+// is still gathered with cp.async.
+template <int NC>
+__global__ void __launch_bounds__(128) conv3x3_umma_persistent_kernel(UmmaConvArgs a, int tiles_per_image,
+                                                                      const __grid_constant__ CUtensorMap x1map,
+                                                                      int use_tma) {
+  using namespace umma;
+  constexpr uint32_t kCols = 2 * NC <= 64 ? 64 : (2 * NC <= 128 ? 128 : 256);
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ __align__(8) uint64_t mbar[2];
+  __shared__ __align__(8) uint64_t tbar[2];  // TMA arrival per halo buffer
+  __shared__ uint32_t tmem_base_slot;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int cin = a.c1 + a.c2, planes = cin / 8;
+  const int halo_bytes = planes * kPlaneBytes;
+  const int tiles_x = (a.W + kTileW - 1) / kTileW;
+  const int total_tiles = tiles_per_image * a.N;
+  const int H2 = a.H >> 1, W2 = a.W >> 1;
+  const uint32_t sbase = smem_addr(smem);
+  const uint32_t wbase = sbase;
+  const uint32_t hbase0 = (sbase + 9 * planes * NC * 16 + 1023u) & ~1023u;
+  const uint32_t hbase1 = (hbase0 + halo_bytes + 1023u) & ~1023u;
+  const uint32_t mb0 = smem_addr(&mbar[0]), mb1 = smem_addr(&mbar[1]);
+  const uint32_t tb0 = smem_addr(&tbar[0]), tb1 = smem_addr(&tbar[1]);
+  const int x1_planes = use_tma ? a.c1 / 8 : 0;  // planes the TMA load fills
+  if (tid == 0) {
+    umma::mbar_init(mb0, 1);
+    umma::mbar_init(mb1, 1);
+    umma::mbar_init(tb0, 1);
+    umma::mbar_init(tb1, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                     smem_addr(&tmem_base_slot)),
+                 "r"(kCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = tmem_base_slot;
+
+  // weights, once: [tap][plane][n][8 channels]
+  for (int i = tid; i < NC * 9 * planes; i += 128) {
+    const int co = i % NC, r = i / NC;
+    const int p = r % planes, tap = r / planes;
+    umma::cp16(wbase + ((tap * planes + p) * NC + co) * 16, a.w + ((size_t)co * 9 + tap) * cin + p * 8, true);
+  }
+  auto tile_origin = [&](int t, int& img, int& x0, int& y0) {
+    img = t / tiles_per_image;
+    const int r = t % tiles_per_image;
+    x0 = (r % tiles_x) * kTileW;
+    y0 = (r / tiles_x) * kTileH;
+  };
+  auto load_halo = [&](uint32_t hb, int t) {
+    int img, x0, y0;
+    tile_origin(t, img, x0, y0);
+    if (x1_planes && tid == 0) {
+      const uint32_t tb = hb == hbase0 ? tb0 : tb1;
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(tb),
+                   "r"((uint32_t)(x1_planes * kPlaneBytes))
+                   : "memory");
+      asm volatile(
+          "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
+          "%6}], [%7];\n" ::"r"(hb),
+          "l"(reinterpret_cast<uint64_t>(&x1map)), "r"(0), "r"(x0 - 1), "r"(y0 - 1), "r"(0), "r"(img), "r"(tb)
+          : "memory");
+    }
+    for (int i = tid + x1_planes * kHaloPx; i < kHaloPx * planes; i += 128) {
+      const int hp = i % kHaloPx, p = i / kHaloPx;
+      const int yy = y0 - 1 + hp / kHaloW, xx = x0 - 1 + hp % kHaloW;
+      const int ci = p * 8;
+      const bool ok = yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
+      const bf16* src = a.x1;
+      if (ok) {
+        if (ci < a.c1) src = a.x1 + (((size_t)img * a.H + yy) * a.W + xx) * a.c1 + ci;
+        else src = a.x2 + (((size_t)img * H2 + (yy >> 1)) * W2 + (xx >> 1)) * a.c2 + (ci - a.c1);
+      }
+      umma::cp16(hb + p * kPlaneBytes + hp * 16, src, ok);
+    }
+  };
+  auto epilogue = [&](int t, uint32_t buf) {
+    int img, x0, y0;
+    tile_origin(t, img, x0, y0);
+    const int m = warp * 32 + lane;
+    const int oy = y0 + m / kTileW, ox = x0 + m % kTileW;
+    const bool inside = oy < a.H && ox < a.W;
+    bf16* dst = a.y + (((size_t)img * a.H + (inside ? oy : 0)) * a.W + (inside ? ox : 0)) * a.cout;
+#pragma unroll
+    for (int c0 = 0; c0 < NC; c0 += 16) {
+      uint32_t v[16];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + buf * NC + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+            "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+      if (inside) {
+        uint32_t packed[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          float f0 = __uint_as_float(v[2 * j]), f1 = __uint_as_float(v[2 * j + 1]);
+          if (a.bias) {
+            f0 += a.bias[c0 + 2 * j];
+            f1 += a.bias[c0 + 2 * j + 1];
+          }
+          if (a.relu & 1) {
+            f0 = fmaxf(f0, 0.f);
+            f1 = fmaxf(f1, 0.f);
+          }
+          const __nv_bfloat162 b2 = __floats2bfloat162_rn(f0, f1);
+          packed[j] = *reinterpret_cast<const uint32_t*>(&b2);
+        }
+        uint4* d4 = reinterpret_cast<uint4*>(dst + c0);
+        d4[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+        d4[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+      }
+    }
+  };
+
+  bool failed = false;
+  int i = 0, mma_issued = -1;  // index of the last tile whose MMAs were issued
+  int t = blockIdx.x;
+  if (t < total_tiles) load_halo(hbase0, t);
+  asm volatile("cp.async.commit_group;\n" ::);  // weights + first halo
+  for (; t < total_tiles; t += gridDim.x, ++i) {
+    const uint32_t b = (uint32_t)(i & 1);
+    const uint32_t hb = b ? hbase1 : hbase0;
+    asm volatile("cp.async.wait_group 0;\n" ::);
+    if (x1_planes) {  // halo i's TMA load: the (i >> 1)-th completion on this buffer's barrier
+      const bool ok = umma::mbar_wait(b ? tb1 : tb0, (uint32_t)((i >> 1) & 1));
+      if (__syncthreads_or(!ok)) {
+        umma::mbar_wait(b ? tb1 : tb0, (uint32_t)((i >> 1) & 1));  // the copy in flight, once more
+        failed = true;
+        break;
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();  // halo i in place; accumulator buffer b drained (epilogue of tile i-2)
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      constexpr uint32_t idesc = umma::idesc_bf16(NC);
+      const uint32_t d = tmem + b * NC;
+#pragma unroll 1
+      for (int tap = 0; tap < 9; ++tap) {
+        const int dy = tap / 3, dx = tap % 3;
+        for (int ks = 0; ks < planes / 2; ++ks) {
+          const uint64_t da = umma::sdesc(hb + (2 * ks) * kPlaneBytes + (dy * kHaloW + dx) * 16, kPlaneBytes,
+                                          kHaloW * 16);
+          const uint64_t db = umma::sdesc(wbase + ((tap * planes + 2 * ks) * NC) * 16, NC * 16, 8 * 16);
+          const uint32_t acc = (tap > 0 || ks > 0) ? 1u : 0u;
+          asm volatile(
+              "{\n\t.reg .pred p;\n\t"
+              "setp.ne.b32 p, %4, 0;\n\t"
+              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+              "l"(da), "l"(db), "r"(idesc), "r"(acc));
+        }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                       b ? mb1 : mb0)
+                   : "memory");
+    }
+    mma_issued = i;
+    // tile i-1's MMAs (which read the other halo buffer) must be done before
+    // that buffer is refilled and before its accumulator is drained
+    if (i >= 1) {
+      const uint32_t pb = b ^ 1u;
+      const bool ok = umma::mbar_wait(pb ? mb1 : mb0, (uint32_t)(((i - 1) >> 1) & 1));
+      if (__syncthreads_or(!ok)) {
+        failed = true;
+        break;
+      }
+    }
+    const int tn = t + gridDim.x;
+    if (tn < total_tiles) load_halo(b ? hbase0 : hbase1, tn);
+    asm volatile("cp.async.commit_group;\n" ::);
+    if (i >= 1) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      epilogue(t - (int)gridDim.x, b ^ 1u);
+    }
+  }
+  asm volatile("cp.async.wait_group 0;\n" ::);
+  if (failed && mma_issued > i - 1) {  // tile i's MMAs were issued and not waited for: once more, bounded
+    umma::mbar_wait((i & 1) ? mb1 : mb0, (uint32_t)((i >> 1) & 1));
+    __syncthreads();
+  }
+  if (!failed && i >= 1) {  // the last tile
+    const int last = i - 1;
+    bool ok = umma::mbar_wait((last & 1) ? mb1 : mb0, (uint32_t)((last >> 1) & 1));
+    if (!ok) ok = umma::mbar_wait((last & 1) ? mb1 : mb0, (uint32_t)((last >> 1) & 1));
+    failed = __syncthreads_or(!ok);
+    if (!failed) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      epilogue(blockIdx.x + last * (int)gridDim.x, (uint32_t)(last & 1));
+    }
+  }
+  if (failed && tid == 0) atomicOr(&g_umma_error, 1u);
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kCols));
+  }
+}
+
+}  // namespace nn
+}  // namespace pbrt
+
+using namespace pbrt;
+using namespace pbrt::nn;
+
+namespace {
+template <int NC> int launch_umma(const UmmaConvArgs& a, cudaStream_t s) {
+  constexpr int kStage = umma::kPlanes * umma::kPlaneBytes + 9 * umma::kPlanes * NC * 16;
+  constexpr size_t kSmem = 2 * (size_t)kStage + 1024;  // two stages (+ alignment of the dynamic base)
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(conv3x3_umma_kernel<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kSmem);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(conv3x3_umma_kernel)");
+    attr_set = true;
+  }
+  dim3 grid(((a.W + umma::kTileW - 1) / umma::kTileW) * ((a.H + umma::kTileH - 1) / umma::kTileH), a.N, 1);
+  conv3x3_umma_kernel<NC><<<grid, 128, kSmem, s>>>(a);
+  return PBRT_OK;
+}
+// Shared memory of the persistent form: the weights and two halos (each
+// 1024-byte aligned for the TMA destination).
+size_t persistent_smem(int cin, int nc) { return (size_t)9 * cin * nc * 2 + 2 * (size_t)cin * 360 + 3 * 1024; }
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+
+// x1 [N][H][W][c1] BF16 as [8][W][H][c1/8][N] with box [8][10][18][c1/8][1].
+bool make_x1_map(CUtensorMap* m, const void* x1, int n, int h, int w, int c1) {
+  EncodeTiledFn enc = encode_tiled();
+  if (!enc || ((uintptr_t)x1 & 15) || c1 % 8 || c1 / 8 > 256) return false;
+  const cuuint64_t dims[5] = {8, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)(c1 / 8), (cuuint64_t)n};
+  const cuuint64_t strides[4] = {(cuuint64_t)c1 * 2, (cuuint64_t)w * c1 * 2, 16, (cuuint64_t)h * w * c1 * 2};
+  const cuuint32_t box[5] = {8, (cuuint32_t)umma::kHaloW, (cuuint32_t)umma::kHaloH, (cuuint32_t)(c1 / 8), 1};
+  const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void*>(x1), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+constexpr size_t kPersistentSmemMax = 200 * 1024;
+
+template <int NC> int launch_umma_persistent(const UmmaConvArgs& a, cudaStream_t s, bool use_tma_flag) {
+  const size_t smem = persistent_smem(a.c1 + a.c2, NC);
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(conv3x3_umma_persistent_kernel<NC>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPersistentSmemMax);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(conv3x3_umma_persistent_kernel)");
+    attr_set = true;
+  }
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  constexpr int kCols = 2 * NC <= 64 ? 64 : (2 * NC <= 128 ? 128 : 256);  // tensor memory per CTA
+  const int per_sm = std::max(1, std::min({4, (int)((227 * 1024) / smem), 512 / kCols}));
+  const int tiles_per_image = ((a.W + umma::kTileW - 1) / umma::kTileW) * ((a.H + umma::kTileH - 1) / umma::kTileH);
+  const int grid = std::min(tiles_per_image * a.N, sms * per_sm);
+  CUtensorMap map;
+  memset(&map, 0, sizeof(map));
+  const int use_tma = use_tma_flag && make_x1_map(&map, a.x1, a.N, a.H, a.W, a.c1) ? 1 : 0;
+  conv3x3_umma_persistent_kernel<NC><<<grid, 128, smem, s>>>(a, tiles_per_image, map, use_tma);
+  return PBRT_OK;
+}
+}  // namespace
+
+extern "C" {
+
+// tcgen05 forward convolution (BF16 output only): Cout in {16, 32, 48, 64,
+// 80, 96, 112, 128}, channel counts multiples of 16; flags bit 0: ReLU,
+// bit 1: the per-tile kernel only, bit 2: no TMA (cp.async gathers).
+PBRT_API int pbrt_nn_conv3x3_umma(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* w,
+                                  const float* bias, void* y, int32_t n, int32_t h, int32_t wd, int32_t cout,
+                                  int32_t flags, pbrt_stream_t stream) {
+  if (!x1 || !w || !y || c1 <= 0 || c1 % 16 || c2 < 0 || c2 % 16 || (c2 && !x2) || cout < 16 || cout > 128 ||
+      cout % 16 || n <= 0 || h <= 0 || wd <= 0 || (c2 && (h % 2 || wd % 2)))
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "nn conv3x3 umma: bad arguments (c1 %d, c2 %d, cout %d)", c1, c2, cout);
+  UmmaConvArgs a{(const bf16*)x1, (const bf16*)x2, c1, c2, (const bf16*)w, bias, (bf16*)y, n, h, wd, cout, flags};
+  int st;
+  if (!(flags & 2) && persistent_smem(c1 + c2, cout) <= kPersistentSmemMax) {
+    switch (cout) {
+      case 16: st = launch_umma_persistent<16>(a, stream, !(flags & 4)); break;
+      case 32: st = launch_umma_persistent<32>(a, stream, !(flags & 4)); break;
+      case 48: st = launch_umma_persistent<48>(a, stream, !(flags & 4)); break;
+      case 64: st = launch_umma_persistent<64>(a, stream, !(flags & 4)); break;
+      case 80: st = launch_umma_persistent<80>(a, stream, !(flags & 4)); break;
+      case 96: st = launch_umma_persistent<96>(a, stream, !(flags & 4)); break;
+      case 112: st = launch_umma_persistent<112>(a, stream, !(flags & 4)); break;
+      default: st = launch_umma_persistent<128>(a, stream, !(flags & 4)); break;
+    }
+    if (st) return st;
+    return check_launch("conv3x3_umma_persistent_kernel");
+  }
+  switch (cout) {
+    case 16: st = launch_umma<16>(a, stream); break;
+    case 32: st = launch_umma<32>(a, stream); break;
+    case 48: st = launch_umma<48>(a, stream); break;
+    case 64: st = launch_umma<64>(a, stream); break;
+    case 80: st = launch_umma<80>(a, stream); break;
+    case 96: st = launch_umma<96>(a, stream); break;
+    case 112: st = launch_umma<112>(a, stream); break;
+    default: st = launch_umma<128>(a, stream); break;
+  }
+  if (st) return st;
+  return check_launch("conv3x3_umma_kernel");
+}
+
+// Error flags of the tcgen05 kernels since the last call (bit 0: an
+// mbarrier wait timed out); resets them (stream-synchronising).
+PBRT_API int pbrt_nn_umma_status(pbrt_stream_t stream, uint32_t* flags) {
+  if (!flags) return fail(PBRT_ERROR_INVALID_ARGUMENT, "umma status: null output");
+  PBRT_CUDA(cudaStreamSynchronize(stream));
+  PBRT_CUDA(cudaMemcpyFromSymbol(flags, g_umma_error, sizeof(uint32_t)));
+  const uint32_t zero = 0;
+  PBRT_CUDA(cudaMemcpyToSymbol(g_umma_error, &zero, sizeof(uint32_t)));
+  return PBRT_OK;
+}
+
+}  // extern "C"

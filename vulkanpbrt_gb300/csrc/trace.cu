@@ -156,6 +156,12 @@ struct TravStack {
 #define PBRT_TRAVERSAL_DEFER_TRIS 1
 #endif
 constexpr int kTraversalDeferTris = PBRT_TRAVERSAL_DEFER_TRIS;
+// L1 prefetch of the next node and of the first deferred triangle at the
+// end of a node visit (build knob).
+#ifndef PBRT_TRAVERSE_PREFETCH
+#define PBRT_TRAVERSE_PREFETCH 0
+#endif
+constexpr int kTraversePrefetch = PBRT_TRAVERSE_PREFETCH;
 
 // Visits st.node: box-tests its children, intersects the triangles of the
 // leaf children that are hit, and moves to the nearest inner child (octant
@@ -303,6 +309,10 @@ PBRT_D void visit_node_deferred(const SceneView& sc, const RayPre& r, float tmin
   }
   st.tri_base = tri_base;
   st.tri_mask = tris;
+  if (kTraversePrefetch && tris) {  // the first triangle this lane tests next
+    const float4* t = sc.tris + 3 * (tri_base + (uint32_t)(__ffs(tris) - 1));
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(t));
+  }
   if (inner) {
     const int k = __ffs(inner) - 1;
     inner &= inner - 1;
@@ -317,6 +327,11 @@ PBRT_D void visit_node_deferred(const SceneView& sc, const RayPre& r, float tmin
       stack.put(st.sp++, make_uint2(child_base, (imask << 8) | inner));
     }
     st.node = child_base + __popc(imask & ((1u << s) - 1u));
+    if (kTraversePrefetch) {  // the next node's 80 bytes, while the triangles are tested
+      const char* nd = reinterpret_cast<const char*>(sc.nodes) + (size_t)st.node * 80;
+      asm volatile("prefetch.global.L1 [%0];" ::"l"(nd));
+      asm volatile("prefetch.global.L1 [%0];" ::"l"(nd + 64));
+    }
     return;
   }
   if (!POP || st.sp == 0) {

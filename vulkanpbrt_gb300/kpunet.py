@@ -194,8 +194,12 @@ class Workspace:
     def set_input(self, illum, albedo, normal, depth, spp=None):
         nn.features(illum, albedo, normal, depth, self.feat, self.rad[0], spp=spp)
 
-    def forward(self):
+    def forward(self, kernel="mma"):
+        """kernel: "mma" (warp-level mma.sync convolutions, the training path), "umma" (tcgen05), or a
+        list with one of the two per convolution (layer order of CONVS)."""
         net, a = self.net, self.act
+        kinds = list(kernel) if isinstance(kernel, (list, tuple)) else [kernel] * len(CONVS)
+        layer = {name: (nn.conv3x3_umma if k == "umma" else nn.conv3x3) for (name, _, _, _), k in zip(CONVS, kinds)}
         nn.avgpool2(self.rad[0], self.rad[1])
         nn.avgpool2(self.rad[1], self.rad[2])
         x = self.feat
@@ -203,14 +207,14 @@ class Workspace:
             if name.endswith("a") and lvl > 0:
                 nn.avgpool2(x, self.pool[lvl])
                 x = self.pool[lvl]
-            nn.conv3x3(x, net.conv_w(name), net.conv_b(name), relu=True, out=a[name])
+            layer[name](x, net.conv_w(name), net.conv_b(name), relu=True, out=a[name])
             x = a[name]
         skips = {0: a["e0b"], 1: a["e1b"], 2: a["e2b"], 3: a["e3b"]}
         for name, (c1, c2), cout, lvl in DECODER:
             if name.endswith("a"):
-                nn.conv3x3(skips[lvl], net.conv_w(name), net.conv_b(name), x2=x, relu=True, out=a[name])
+                layer[name](skips[lvl], net.conv_w(name), net.conv_b(name), x2=x, relu=True, out=a[name])
             else:
-                nn.conv3x3(x, net.conv_w(name), net.conv_b(name), relu=True, out=a[name])
+                layer[name](x, net.conv_w(name), net.conv_b(name), relu=True, out=a[name])
             x = a[name]
         tr = self.training
         for hname, fname, c, k, s in HEADS:
@@ -299,6 +303,7 @@ def main(argv=None):
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--batch", type=int, default=1)
     ap.add_argument("--iters", type=int, default=10)
+    ap.add_argument("--kernel", default="mma", choices=["mma", "umma"], help="convolutions: mma.sync or tcgen05")
     a = ap.parse_args(argv)
     from . import build
 
@@ -308,12 +313,12 @@ def main(argv=None):
     ws = net.workspace(a.batch, a.height, a.width, training=False)
     ws.feat.normal_()
     ws.rad[0].uniform_()
-    ws.forward()  # warm-up
+    ws.forward(a.kernel)  # warm-up
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(a.iters):
-        ws.forward()
+        ws.forward(a.kernel)
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / a.iters

@@ -28,6 +28,9 @@ _abi.add_signatures({
     "pbrt_neural_fallback_mask": (C.c_int32, [H, C.POINTER(PbrtImage)]),
     "pbrt_neural_calibrate": (C.c_int32, [H, H]),
     "pbrt_neural_set_precision": (C.c_int32, [H, C.c_int32]),
+    "pbrt_neural_autotune": (C.c_int32, [H, H]),
+    "pbrt_neural_conv_kernels": (C.c_int32, [H, C.POINTER(C.c_int32), C.c_int32]),
+    "pbrt_neural_set_conv_kernels": (C.c_int32, [H, C.POINTER(C.c_int32), C.c_int32]),
 })
 
 WEIGHTS = Path(__file__).resolve().parent / "weights" / "kpunet.npz"
@@ -97,6 +100,21 @@ class NeuralDenoiser(Handle):
     def set_precision(self, bits: int) -> None:
         """16: BF16 convolutions; 8: FP8 e4m3 (after calibrate)."""
         check(lib().pbrt_neural_set_precision(self.ptr, bits))
+
+    def autotune(self, stream=None) -> list:
+        """Times the mma.sync and tcgen05 kernels for every convolution on the current inputs; keeps the faster."""
+        check(lib().pbrt_neural_autotune(self.ptr, stream_handle(stream)))
+        return self.conv_kernels()
+
+    def conv_kernels(self) -> list:
+        """Per-layer convolution kernel: "mma" or "umma" (tcgen05)."""
+        k = (C.c_int32 * 18)()
+        check(lib().pbrt_neural_conv_kernels(self.ptr, k, 18))
+        return ["umma" if v else "mma" for v in k]
+
+    def set_conv_kernels(self, kinds) -> None:
+        k = (C.c_int32 * 18)(*[1 if x == "umma" else 0 for x in kinds])
+        check(lib().pbrt_neural_set_conv_kernels(self.ptr, k, 18))
 
     def dispatch(self, push_constants=None, stream=None, graph: bool = True) -> None:
         fn = lib().pbrt_neural_dispatch if graph else lib().pbrt_neural_dispatch_direct

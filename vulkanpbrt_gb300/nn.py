@@ -17,6 +17,8 @@ _abi.add_signatures({
     "pbrt_nn_conv3x3_fp8": (i32, [H, i32, H, i32, H, H, H, H, H, i32, i32, i32, i32, i32, H]),
     "pbrt_nn_quantize_weights_fp8": (i32, [H, H, i32, i32, H, H, H]),
     "pbrt_nn_channel_amax": (i32, [H, i64, i32, H, H]),
+    "pbrt_nn_conv3x3_umma": (i32, [H, i32, H, i32, H, H, H, i32, i32, i32, i32, i32, H]),
+    "pbrt_nn_umma_status": (i32, [H, C.POINTER(C.c_uint32)]),
     "pbrt_nn_flip_weights": (i32, [H, H, i32, i32, H]),
     "pbrt_nn_features": (i32, [H, i32, H, H, H, H, i32, i32, i32, i32, i32, H, H, H]),
     "pbrt_nn_avgpool2": (i32, [H, H, i32, i32, i32, i32, i32, H]),
@@ -97,6 +99,30 @@ def channel_amax(x, amax):
     c = x.shape[-1]
     check(lib().pbrt_nn_channel_amax(_ptr(x), x.numel() // c, c, _ptr(amax), _stream()))
     return amax
+
+
+def conv3x3_umma(x1, w, bias=None, x2=None, relu=False, out=None, persistent=True, tma=True):
+    """tcgen05 forward (BF16 out): as conv3x3, Cout in {16, ..., 128}. persistent=False forces the
+    per-tile kernel (the persistent one is used when the weights and two input halos fit in shared memory);
+    tma=False gathers the persistent kernel's input halo with cp.async instead of a TMA load."""
+    import torch
+
+    n, h, wd, c1 = x1.shape
+    c2 = 0 if x2 is None else x2.shape[3]
+    cout = w.shape[0]
+    if out is None:
+        out = torch.empty((n, h, wd, cout), dtype=torch.bfloat16, device=x1.device)
+    flags = (RELU if relu else 0) | (0 if persistent else 2) | (0 if tma else 4)
+    check(lib().pbrt_nn_conv3x3_umma(_ptr(x1), c1, _ptr(x2), c2, _ptr(w), _ptr(bias), _ptr(out), n, h, wd, cout,
+                                     flags, _stream()))
+    return out
+
+
+def umma_status() -> int:
+    """Error flags of the tcgen05 kernels since the last call (0 = none); synchronises."""
+    f = C.c_uint32()
+    check(lib().pbrt_nn_umma_status(_stream(), C.byref(f)))
+    return f.value
 
 
 def conv3x3_wgrad(dy, x1, dw, x2=None):
