@@ -13,7 +13,7 @@ pytestmark = pytest.mark.gpu
                                              (1, 18, 34, 96, 128, 96), (1, 9, 17, 128, 0, 128),
                                              (1, 34, 46, 32, 48, 32), (2, 136, 240, 32, 48, 32),
                                              (1, 128, 200, 16, 0, 32)])
-@pytest.mark.parametrize("mode", ["tma", "persistent", "tile"])
+@pytest.mark.parametrize("mode", ["ws", "ws_gather", "tma", "persistent", "tile"])
 def test_conv3x3_umma_forward(cuda, n, h, w, c1, c2, cout, mode):
     import torch
 
@@ -25,7 +25,7 @@ def test_conv3x3_umma_forward(cuda, n, h, w, c1, c2, cout, mode):
     x2 = torch.randn(n, h // 2, w // 2, c2, generator=g).bfloat16().to(cuda) if c2 else None
     wt = (torch.randn(cout, 9, c1 + c2, generator=g) * 0.1).bfloat16().to(cuda)
     b = torch.randn(cout, generator=g).float().to(cuda)
-    kw = dict(persistent=mode != "tile", tma=mode == "tma")
+    kw = dict(persistent=mode != "tile", tma=mode in ("ws", "tma"), specialised=mode.startswith("ws"))
     y = nn.conv3x3_umma(x1, wt, b, x2=x2, relu=False, **kw)
     yr = nn.conv3x3_umma(x1, wt, b, x2=x2, relu=True, **kw)
     assert nn.umma_status() == 0

@@ -485,6 +485,237 @@ __global__ void __launch_bounds__(128) conv3x3_umma_persistent_kernel(UmmaConvAr
   }
 }
 
+// Warp-specialised persistent form. Warp 0 produces input halos into a
+// ring of shared-memory stages (x1 by TMA; the upsampled x2 part by cp.async
+// gathers, after which each lane waits for its copies, fences them for the
+// tensor cores and arrives on the same "full" barrier); warp 1
+// allocates tensor memory and, from one lane, issues each tile's MMAs into
+// one of two accumulator buffers, committing to the stage's "empty" barrier
+// (the producer may refill it) and to the buffer's "full" barrier; warps
+// 2-5 drain finished accumulators (bias, ReLU, BF16 stores) and release the
+// buffer. No block-wide barrier inside the tile loop. Every wait is bounded
+// (2 s); a timeout raises a shared abort flag that ends every role's loop.
+constexpr int kWsThreads = 192;
+
+__device__ __forceinline__ void mbar_arrive(uint32_t addr) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(addr) : "memory");
+}
+
+template <int NC>
+__global__ void __launch_bounds__(kWsThreads) conv3x3_umma_ws_kernel(UmmaConvArgs a, int tiles_per_image,
+                                                                     const __grid_constant__ CUtensorMap x1map,
+                                                                     int use_tma, int stages) {
+  using namespace umma;
+  constexpr uint32_t kCols = 2 * NC <= 64 ? 64 : (2 * NC <= 128 ? 128 : 256);
+  constexpr int kMaxStages = 6;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ __align__(8) uint64_t full_bar[kMaxStages], empty_bar[kMaxStages], tfull_bar[2], tempty_bar[2];
+  __shared__ uint32_t tmem_base_slot;
+  __shared__ volatile int abort_flag;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int cin = a.c1 + a.c2, planes = cin / 8;
+  const int halo_bytes = planes * kPlaneBytes;
+  const int halo_pitch = (halo_bytes + 1023) & ~1023;
+  const int tiles_x = (a.W + kTileW - 1) / kTileW;
+  const int total_tiles = tiles_per_image * a.N;
+  const int H2 = a.H >> 1, W2 = a.W >> 1;
+  const int x1_planes = use_tma ? a.c1 / 8 : 0;
+  const bool gather = planes > x1_planes;  // cp.async part present
+  const uint32_t sbase = smem_addr(smem);
+  const uint32_t wbase = sbase;
+  const uint32_t hbase = (sbase + 9 * planes * NC * 16 + 1023u) & ~1023u;
+  auto fb = [&](int st) { return smem_addr(&full_bar[st]); };
+  auto eb = [&](int st) { return smem_addr(&empty_bar[st]); };
+  auto tfb = [&](int b) { return smem_addr(&tfull_bar[b]); };
+  auto teb = [&](int b) { return smem_addr(&tempty_bar[b]); };
+  if (tid == 0) {
+    for (int st = 0; st < stages; ++st) {
+      umma::mbar_init(fb(st), (x1_planes ? 1u : 0u) + (gather ? 32u : 0u));
+      umma::mbar_init(eb(st), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      umma::mbar_init(tfb(b), 1);
+      umma::mbar_init(teb(b), 128);
+    }
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                     smem_addr(&tmem_base_slot)),
+                 "r"(kCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+  }
+  // weights, once, by every thread
+  for (int i = tid; i < NC * 9 * planes; i += kWsThreads) {
+    const int co = i % NC, r = i / NC;
+    const int p = r % planes, tap = r / planes;
+    umma::cp16(wbase + ((tap * planes + p) * NC + co) * 16, a.w + ((size_t)co * 9 + tap) * cin + p * 8, true);
+  }
+  asm volatile("cp.async.commit_group;\n" ::);
+  asm volatile("cp.async.wait_group 0;\n" ::);
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = tmem_base_slot;
+  auto tile_origin = [&](int t, int& img, int& x0, int& y0) {
+    img = t / tiles_per_image;
+    const int r = t % tiles_per_image;
+    x0 = (r % tiles_x) * kTileW;
+    y0 = (r / tiles_x) * kTileH;
+  };
+  auto wait = [&](uint32_t bar, uint32_t parity) {
+    if (umma::mbar_wait(bar, parity)) return true;
+    abort_flag = 1;
+    return false;
+  };
+
+  if (warp == 0) {
+    // ---- producer
+    int i = 0;
+    for (int t = blockIdx.x; t < total_tiles && !abort_flag; t += gridDim.x, ++i) {
+      const int st = i % stages, k = i / stages;
+      if (!wait(eb(st), (uint32_t)((k & 1) ^ 1))) break;  // the MMAs of the stage's previous tile are done
+      const uint32_t hb = hbase + st * halo_pitch;
+      int img, x0, y0;
+      tile_origin(t, img, x0, y0);
+      if (x1_planes && lane == 0) {
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb(st)),
+                     "r"((uint32_t)(x1_planes * kPlaneBytes))
+                     : "memory");
+        asm volatile(
+            "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+            "%5, %6}], [%7];\n" ::"r"(hb),
+            "l"(reinterpret_cast<uint64_t>(&x1map)), "r"(0), "r"(x0 - 1), "r"(y0 - 1), "r"(0), "r"(img), "r"(fb(st))
+            : "memory");
+      }
+      if (gather) {
+        for (int q = lane + x1_planes * kHaloPx; q < kHaloPx * planes; q += 32) {
+          const int hp = q % kHaloPx, p = q / kHaloPx;
+          const int yy = y0 - 1 + hp / kHaloW, xx = x0 - 1 + hp % kHaloW;
+          const int ci = p * 8;
+          const bool ok = yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
+          const bf16* src = a.x1;
+          if (ok) {
+            if (ci < a.c1) src = a.x1 + (((size_t)img * a.H + yy) * a.W + xx) * a.c1 + ci;
+            else src = a.x2 + (((size_t)img * H2 + (yy >> 1)) * W2 + (xx >> 1)) * a.c2 + (ci - a.c1);
+          }
+          umma::cp16(hb + p * kPlaneBytes + hp * 16, src, ok);
+        }
+        // this lane's copies landed and made visible to the tensor cores, then one arrival
+        asm volatile("cp.async.commit_group;\n" ::);
+        asm volatile("cp.async.wait_group 0;\n" ::);
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        mbar_arrive(fb(st));
+      }
+    }
+    asm volatile("cp.async.wait_group 0;\n" ::);
+  } else if (warp == 1) {
+    // ---- MMA issue (one lane)
+    if (lane == 0) {
+      constexpr uint32_t idesc = umma::idesc_bf16(NC);
+      int i = 0;
+      for (int t = blockIdx.x; t < total_tiles && !abort_flag; t += gridDim.x, ++i) {
+        const int st = i % stages, k = i / stages, b = i & 1, kb = i >> 1;
+        if (!wait(fb(st), (uint32_t)(k & 1))) break;           // halo in place
+        if (!wait(teb(b), (uint32_t)((kb & 1) ^ 1))) break;    // accumulator buffer drained
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const uint32_t hb = hbase + st * halo_pitch, d = tmem + (uint32_t)b * NC;
+        for (int tap = 0; tap < 9; ++tap) {
+          const int dy = tap / 3, dx = tap % 3;
+          for (int ks = 0; ks < planes / 2; ++ks) {
+            const uint64_t da = umma::sdesc(hb + (2 * ks) * kPlaneBytes + (dy * kHaloW + dx) * 16, kPlaneBytes,
+                                            kHaloW * 16);
+            const uint64_t db = umma::sdesc(wbase + ((tap * planes + 2 * ks) * NC) * 16, NC * 16, 8 * 16);
+            const uint32_t acc = (tap > 0 || ks > 0) ? 1u : 0u;
+            asm volatile(
+                "{\n\t.reg .pred p;\n\t"
+                "setp.ne.b32 p, %4, 0;\n\t"
+                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+                "l"(da), "l"(db), "r"(idesc), "r"(acc));
+          }
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(eb(st))
+                     : "memory");
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(tfb(b))
+                     : "memory");
+      }
+    }
+    __syncwarp();
+  } else {
+    // ---- epilogue (warps 2-5: tensor-memory subpartitions 2, 3, 0, 1)
+    const int sub = warp & 3;
+    int i = 0;
+    for (int t = blockIdx.x; t < total_tiles; t += gridDim.x, ++i) {
+      const int b = i & 1, kb = i >> 1;
+      const bool ok = umma::mbar_wait(tfb(b), (uint32_t)(kb & 1));
+      if (__any_sync(0xffffffffu, !ok) || abort_flag) {
+        abort_flag = 1;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      int img, x0, y0;
+      tile_origin(t, img, x0, y0);
+      const int m = sub * 32 + lane;
+      const int oy = y0 + m / kTileW, ox = x0 + m % kTileW;
+      const bool inside = oy < a.H && ox < a.W;
+      bf16* dst = a.y + (((size_t)img * a.H + (inside ? oy : 0)) * a.W + (inside ? ox : 0)) * a.cout;
+#pragma unroll
+      for (int c0 = 0; c0 < NC; c0 += 16) {
+        uint32_t v[16];
+        const uint32_t taddr = tmem + ((uint32_t)(sub * 32) << 16) + (uint32_t)b * NC + (uint32_t)c0;
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+            "[%16];\n"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        if (inside) {
+          uint32_t packed[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            float f0 = __uint_as_float(v[2 * j]), f1 = __uint_as_float(v[2 * j + 1]);
+            if (a.bias) {
+              f0 += a.bias[c0 + 2 * j];
+              f1 += a.bias[c0 + 2 * j + 1];
+            }
+            if (a.relu & 1) {
+              f0 = fmaxf(f0, 0.f);
+              f1 = fmaxf(f1, 0.f);
+            }
+            const __nv_bfloat162 b2 = __floats2bfloat162_rn(f0, f1);
+            packed[j] = *reinterpret_cast<const uint32_t*>(&b2);
+          }
+          uint4* d4 = reinterpret_cast<uint4*>(dst + c0);
+          d4[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+          d4[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+      mbar_arrive(teb(b));
+    }
+  }
+  // every role is past its loop; the epilogue has waited for the last MMAs
+  // (or a role gave up: then wait once more, bounded, for MMAs in flight)
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (abort_flag) {
+    if (tid == 0) atomicOr(&g_umma_error, 1u);
+    const int n_mine = (total_tiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+    if (n_mine > 0 && warp == 1 && lane == 0) {  // the last tile's accumulator commit, bounded
+      const int last = n_mine - 1;
+      umma::mbar_wait(tfb(last & 1), (uint32_t)((last >> 1) & 1));
+    }
+    __syncthreads();
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kCols));
+  }
+}
+
 }  // namespace nn
 }  // namespace pbrt
 
@@ -545,6 +776,39 @@ bool make_x1_map(CUtensorMap* m, const void* x1, int n, int h, int w, int c1) {
 }
 constexpr size_t kPersistentSmemMax = 200 * 1024;
 
+// Warp-specialised form: weights + `stages` halo buffers (1024-aligned).
+size_t ws_smem(int cin, int nc, int stages) {
+  const size_t halo = ((size_t)cin * 360 + 1023) & ~(size_t)1023;
+  return (size_t)9 * cin * nc * 2 + 1024 + stages * halo + 1024;
+}
+constexpr size_t kWsSmemMax = 200 * 1024;
+
+template <int NC> int launch_umma_ws(const UmmaConvArgs& a, cudaStream_t s, bool use_tma_flag) {
+  const int cin = a.c1 + a.c2;
+  int stages = 6;
+  while (stages > 2 && ws_smem(cin, NC, stages) > kWsSmemMax) --stages;
+  const size_t smem = ws_smem(cin, NC, stages);
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(conv3x3_umma_ws_kernel<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kWsSmemMax);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(conv3x3_umma_ws_kernel)");
+    attr_set = true;
+  }
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  constexpr int kCols = 2 * NC <= 64 ? 64 : (2 * NC <= 128 ? 128 : 256);
+  const int per_sm = std::max(1, std::min({4, (int)((227 * 1024) / smem), 512 / kCols}));
+  const int tiles_per_image = ((a.W + umma::kTileW - 1) / umma::kTileW) * ((a.H + umma::kTileH - 1) / umma::kTileH);
+  const int grid = std::min(tiles_per_image * a.N, sms * per_sm);
+  CUtensorMap map;
+  memset(&map, 0, sizeof(map));
+  const int use_tma = use_tma_flag && make_x1_map(&map, a.x1, a.N, a.H, a.W, a.c1) ? 1 : 0;
+  conv3x3_umma_ws_kernel<NC><<<grid, kWsThreads, smem, s>>>(a, tiles_per_image, map, use_tma, stages);
+  return PBRT_OK;
+}
+
 template <int NC> int launch_umma_persistent(const UmmaConvArgs& a, cudaStream_t s, bool use_tma_flag) {
   const size_t smem = persistent_smem(a.c1 + a.c2, NC);
   static bool attr_set = false;
@@ -573,7 +837,8 @@ extern "C" {
 
 // tcgen05 forward convolution (BF16 output only): Cout in {16, 32, 48, 64,
 // 80, 96, 112, 128}, channel counts multiples of 16; flags bit 0: ReLU,
-// bit 1: the per-tile kernel only, bit 2: no TMA (cp.async gathers).
+// bit 1: the per-tile kernel only, bit 2: no TMA (cp.async gathers), bit 3:
+// the single-role persistent kernel instead of the warp-specialised one.
 PBRT_API int pbrt_nn_conv3x3_umma(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* w,
                                   const float* bias, void* y, int32_t n, int32_t h, int32_t wd, int32_t cout,
                                   int32_t flags, pbrt_stream_t stream) {
@@ -582,6 +847,22 @@ PBRT_API int pbrt_nn_conv3x3_umma(const void* x1, int32_t c1, const void* x2, in
     return fail(PBRT_ERROR_INVALID_ARGUMENT, "nn conv3x3 umma: bad arguments (c1 %d, c2 %d, cout %d)", c1, c2, cout);
   UmmaConvArgs a{(const bf16*)x1, (const bf16*)x2, c1, c2, (const bf16*)w, bias, (bf16*)y, n, h, wd, cout, flags};
   int st;
+  // warp-specialised form for single inputs (its one producer warp would
+  // have to gather the upsampled second input alone)
+  if (!(flags & 10) && (c2 == 0 || (flags & 4)) && ws_smem(c1 + c2, cout, 2) <= kWsSmemMax) {
+    switch (cout) {
+      case 16: st = launch_umma_ws<16>(a, stream, !(flags & 4)); break;
+      case 32: st = launch_umma_ws<32>(a, stream, !(flags & 4)); break;
+      case 48: st = launch_umma_ws<48>(a, stream, !(flags & 4)); break;
+      case 64: st = launch_umma_ws<64>(a, stream, !(flags & 4)); break;
+      case 80: st = launch_umma_ws<80>(a, stream, !(flags & 4)); break;
+      case 96: st = launch_umma_ws<96>(a, stream, !(flags & 4)); break;
+      case 112: st = launch_umma_ws<112>(a, stream, !(flags & 4)); break;
+      default: st = launch_umma_ws<128>(a, stream, !(flags & 4)); break;
+    }
+    if (st) return st;
+    return check_launch("conv3x3_umma_ws_kernel");
+  }
   if (!(flags & 2) && persistent_smem(c1 + c2, cout) <= kPersistentSmemMax) {
     switch (cout) {
       case 16: st = launch_umma_persistent<16>(a, stream, !(flags & 4)); break;

@@ -101,10 +101,11 @@ def channel_amax(x, amax):
     return amax
 
 
-def conv3x3_umma(x1, w, bias=None, x2=None, relu=False, out=None, persistent=True, tma=True):
+def conv3x3_umma(x1, w, bias=None, x2=None, relu=False, out=None, persistent=True, tma=True, specialised=True):
     """tcgen05 forward (BF16 out): as conv3x3, Cout in {16, ..., 128}. persistent=False forces the
     per-tile kernel (the persistent one is used when the weights and two input halos fit in shared memory);
-    tma=False gathers the persistent kernel's input halo with cp.async instead of a TMA load."""
+    tma=False gathers the persistent kernel's input halo with cp.async instead of a TMA load; specialised=False
+    uses the single-role persistent kernel instead of the warp-specialised one."""
     import torch
 
     n, h, wd, c1 = x1.shape
@@ -112,7 +113,7 @@ def conv3x3_umma(x1, w, bias=None, x2=None, relu=False, out=None, persistent=Tru
     cout = w.shape[0]
     if out is None:
         out = torch.empty((n, h, wd, cout), dtype=torch.bfloat16, device=x1.device)
-    flags = (RELU if relu else 0) | (0 if persistent else 2) | (0 if tma else 4)
+    flags = (RELU if relu else 0) | (0 if persistent else 2) | (0 if tma else 4) | (0 if specialised else 8)
     check(lib().pbrt_nn_conv3x3_umma(_ptr(x1), c1, _ptr(x2), c2, _ptr(w), _ptr(bias), _ptr(out), n, h, wd, cout,
                                      flags, _stream()))
     return out
