@@ -101,6 +101,7 @@ typedef struct PbrtScene PbrtScene;
 typedef struct PbrtPipeline PbrtPipeline;
 typedef struct PbrtNeural PbrtNeural;
 typedef struct PbrtTaa PbrtTaa;
+typedef struct PbrtBFRBlender PbrtBFRBlender;
 typedef struct PbrtBatch PbrtBatch;
 
 /* ---- library ---------------------------------------------------------- */
@@ -110,6 +111,14 @@ PBRT_API int pbrt_last_error(char* buffer, size_t size);
 /* Reference counting for every handle type above. */
 PBRT_API int pbrt_retain(void* handle);
 PBRT_API int pbrt_release(void* handle);
+/* Host <-> device copies of a whole image (all layers), stream ordered:
+ * the staging-buffer copies of the reference's offline replay
+ * (OfflineGBuffer / OfflineIllumination upload_* / download_*,
+ * source/io/RenderIO.cpp:372-391, 718-1008). host rows are host_row_bytes
+ * apart (>= width * texel bytes). */
+PBRT_API int pbrt_image_upload(const PbrtImage* dst, const void* host, size_t host_row_bytes, pbrt_stream_t stream);
+PBRT_API int pbrt_image_download(const PbrtImage* src, void* host, size_t host_row_bytes, pbrt_stream_t stream);
+PBRT_API int pbrt_stream_synchronize(pbrt_stream_t stream);
 
 /* ---- GBuffer (source/buffers/GBuffer.hpp:9-26) -------------------------
  * Public images depth R32F, normal RG32F (theta, phi), material RGBA8,
@@ -428,6 +437,23 @@ PBRT_API int pbrt_taa_create(uint32_t width, uint32_t height, uint32_t work_widt
                              PbrtTaa** out);
 PBRT_API int pbrt_taa_dispatch(PbrtTaa* taa, const PbrtPushConstants* pc, pbrt_stream_t stream);
 PBRT_API int pbrt_taa_final_image(const PbrtTaa* taa, PbrtImage* out);
+/* ---- BFRBlender (source/renderModules/denoisers/BFRBlender.hpp:6-27) ----
+ * BFRBlender(width, height, average_image, average_squared_image, denoised0,
+ * denoised1, denoised2, work_width = 16, work_height = 16, filter_radius = 2)
+ * (BFRBlender.cpp:5-70, shaders/bfrBlender.comp): blends the 8x8, 16x16 and
+ * 32x32 denoisers' final images (denoised0/1/2: packed 8-bit RGBA or BGRA,
+ * blended byte for byte) by the local standard deviation of the average
+ * image's luminance. average / average_squared: RGBA16F (the accumulated
+ * IlluminationBufferDemodulated's images 0 and 1) or RGBA32F. The images
+ * must outlive the blender. add_dispatch_to_command_graph
+ * (BFRBlender.cpp:84-91) -> pbrt_bfr_blender_dispatch;
+ * get_final_descriptor_image -> pbrt_bfr_blender_final_image (B8G8R8A8). */
+PBRT_API int pbrt_bfr_blender_create(uint32_t width, uint32_t height, const PbrtImage* average_image,
+                                     const PbrtImage* average_squared_image, const PbrtImage* denoised0,
+                                     const PbrtImage* denoised1, const PbrtImage* denoised2, uint32_t work_width,
+                                     uint32_t work_height, uint32_t filter_radius, PbrtBFRBlender** out);
+PBRT_API int pbrt_bfr_blender_dispatch(PbrtBFRBlender* blender, pbrt_stream_t stream);
+PBRT_API int pbrt_bfr_blender_final_image(const PbrtBFRBlender* blender, PbrtImage* out);
 /* FormatConverter (source/renderModules/FormatConverter.hpp,
  * shaders/formatConverter.comp:9-13): dst = src texel by texel, src
  * RGBA32F / RGBA16F / RGBA8 / BGRA8, dst RGBA32F / RGBA8 / BGRA8 (UNORM

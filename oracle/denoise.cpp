@@ -683,6 +683,64 @@ int oracle_taa(int W, int H, uint32_t frame, const uint16_t* motion, const uint8
   return 0;
 }
 
+// BFRBlender (shaders/bfrBlender.comp:31-68): blend of the 8x8 / 16x16 /
+// 32x32 denoisers' 8-bit final images (den8 / den16 / den32, blended byte for
+// byte) by the standard deviation of the average image's luminance over a
+// (2 radius + 1)^2 window, each running mean blended 1:1 with the pixel's own
+// average / average-square luminance. avg / avg_sq: RGBA16F (is_float32 = 0)
+// or RGBA32F (1). Window taps outside the image read zero and still count
+// (robust-access imageLoad); min(t, 1) of a NaN deviation is 1, the GPU's
+// IEEE minNum. out: 8-bit, alpha 255.
+int oracle_bfr_blend(int W, int H, int radius, int is_float32, const void* avg, const void* avg_sq,
+                     const uint8_t* den8, const uint8_t* den16, const uint8_t* den32, uint8_t* out, int threads) {
+  auto load = [&](const void* im, int x, int y) {
+    const size_t p = (size_t)y * W + x;
+    if (is_float32) {
+      const float* f = (const float*)im + 4 * p;
+      return vec3{f[0], f[1], f[2]};
+    }
+    const uint16_t* h = (const uint16_t*)im + 4 * p;
+    return vec3{h2f(h[0]), h2f(h[1]), h2f(h[2])};
+  };
+  auto lum = [](vec3 c) {
+    const float k = 1.0f / 3.0f;
+    return (c.x * k + c.y * k) + c.z * k;
+  };
+  auto mix3 = [](float a, float b, float c, float t) {
+    const float mid = .5f, max_dev = 1.f;
+    t = t / max_dev;
+    t = std::fmin(t, 1.f);
+    const float af = std::fmax(1.0f - (t / mid), 0.f);
+    const float bf = (t < mid) ? t / mid : 1.f - (t - mid) / (1.0f - mid);
+    const float cf = (1.0f - af) - bf;
+    return (af * a + bf * b) + cf * c;
+  };
+  parallel_for(H, [&](int y) {
+    for (int x = 0; x < W; ++x) {
+      float sq = 0.f, av = 0.f;
+      int count = 0;
+      for (int dy = -radius; dy <= radius; ++dy)
+        for (int dx = -radius; dx <= radius; ++dx) {
+          const int sx = x + dx, sy = y + dy;
+          const bool in = sx >= 0 && sy >= 0 && sx < W && sy < H;
+          const float cur = in ? lum(load(avg, sx, sy)) : 0.f;
+          ++count;
+          const float w = 1.0f / (float)count;
+          sq = mix(sq, cur * cur, w);
+          av = mix(av, cur, w);
+        }
+      av = mix(av, lum(load(avg, x, y)), .5f);
+      sq = mix(sq, lum(load(avg_sq, x, y)), .5f);
+      const float sd = std::sqrt(sq - av * av);
+      const size_t p = 4 * ((size_t)y * W + x);
+      for (int c = 0; c < 3; ++c)
+        out[p + c] = f2u8(mix3(u82f(den32[p + c]), u82f(den16[p + c]), u82f(den8[p + c]), sd));
+      out[p + 3] = 255;
+    }
+  }, threads);
+  return 0;
+}
+
 // Known-answer helpers for the tests.
 float oracle_bmfr_random(uint32_t a) { return bmfr_random(a); }
 uint16_t oracle_f2h(float f) { return f2h(f); }

@@ -118,6 +118,20 @@ def taa(frame, motion_f16, denoised_bgra, history, threads=None):
     return final, nxt
 
 
+def bfr_blend(avg, avg_sq, den8, den16, den32, radius=2, threads=None):
+    """bfrBlender.comp. avg / avg_sq: [H,W,4] float16 or float32; den*: [H,W,4] u8. Returns [H,W,4] u8."""
+    H, W = den8.shape[:2]
+    f32 = avg.dtype == np.float32
+    dt = np.float32 if f32 else np.float16
+    out = np.zeros((H, W, 4), np.uint8)
+    rc = lib().oracle_bfr_blend(W, H, radius, int(f32), _p(np.ascontiguousarray(avg, dt)),
+                                _p(np.ascontiguousarray(avg_sq, dt)), _p(np.ascontiguousarray(den8, np.uint8)),
+                                _p(np.ascontiguousarray(den16, np.uint8)), _p(np.ascontiguousarray(den32, np.uint8)),
+                                _p(out), threads_default() if threads is None else threads)
+    assert rc == 0
+    return out
+
+
 def bmfr(bw, fit_threads, frame, position_type, inv_view, inv_proj, depth, normal, albedo, noisy_f16, motion_f16, spp,
          denoised, threads=None):
     """bmfrPre -> bmfrFit -> bmfrPost. Returns (features, weights, final); `denoised` updated in place."""

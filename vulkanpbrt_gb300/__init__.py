@@ -7,6 +7,7 @@ reference's render-module classes over that ABI.
 from ._abi import PbrtError, declared_symbols, lib  # noqa: F401
 from .render_modules import (  # noqa: F401
     BFR,
+    BFRBlender,
     BMFR,
     AccumulationBuffer,
     Accumulator,
@@ -30,5 +31,6 @@ from . import texsynth  # noqa: F401,E402  (registers pbrt_synth_texture)
 from . import nn  # noqa: F401,E402  (registers the neural-denoiser operators)
 from .neural import NeuralDenoiser  # noqa: F401,E402
 from .batch import Batch  # noqa: F401,E402
+from .denoiser_utils import DenoisingBlockSize, DenoisingType, add_denoiser_to_commands  # noqa: F401,E402
 
 __version__ = "0.1.0"

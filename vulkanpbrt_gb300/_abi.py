@@ -122,6 +122,13 @@ _SIGS = {
     "pbrt_taa_create": (i32, [u32, u32, u32, u32, H, H, P(PbrtImage), P(H)]),
     "pbrt_taa_dispatch": (i32, [H, P(PbrtPushConstants), H]),
     "pbrt_taa_final_image": (i32, [H, P(PbrtImage)]),
+    "pbrt_image_upload": (i32, [P(PbrtImage), H, C.c_size_t, H]),
+    "pbrt_image_download": (i32, [P(PbrtImage), H, C.c_size_t, H]),
+    "pbrt_stream_synchronize": (i32, [H]),
+    "pbrt_bfr_blender_create": (i32, [u32, u32, P(PbrtImage), P(PbrtImage), P(PbrtImage), P(PbrtImage), P(PbrtImage),
+                                      u32, u32, u32, P(H)]),
+    "pbrt_bfr_blender_dispatch": (i32, [H, H]),
+    "pbrt_bfr_blender_final_image": (i32, [H, P(PbrtImage)]),
     "pbrt_format_convert": (i32, [P(PbrtImage), P(PbrtImage), H]),
 }
 

@@ -39,6 +39,7 @@ COMMON = [
 EXTRA = {
     "denoise.cu": ["-fmad=false"],
     "taa.cu": ["-fmad=false"],
+    "blend.cu": ["-fmad=false"],
 }
 
 

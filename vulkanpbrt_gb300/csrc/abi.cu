@@ -121,6 +121,31 @@ PBRT_API int pbrt_release(void* handle) {
   return PBRT_OK;
 }
 
+PBRT_API int pbrt_image_upload(const PbrtImage* dst, const void* host, size_t host_row_bytes, pbrt_stream_t stream) {
+  if (!dst || !dst->data || !host || host_row_bytes < (size_t)dst->width * dst->texel_bytes)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "image upload: bad arguments");
+  const size_t rows = (size_t)dst->height * (dst->layers ? dst->layers : 1);
+  cudaError_t e = cudaMemcpy2DAsync(dst->data, dst->row_bytes, host, host_row_bytes,
+                                    (size_t)dst->width * dst->texel_bytes, rows, cudaMemcpyHostToDevice,
+                                    (cudaStream_t)stream);
+  return e == cudaSuccess ? PBRT_OK : cuda_fail(e, "image upload");
+}
+
+PBRT_API int pbrt_image_download(const PbrtImage* src, void* host, size_t host_row_bytes, pbrt_stream_t stream) {
+  if (!src || !src->data || !host || host_row_bytes < (size_t)src->width * src->texel_bytes)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "image download: bad arguments");
+  const size_t rows = (size_t)src->height * (src->layers ? src->layers : 1);
+  cudaError_t e = cudaMemcpy2DAsync(host, host_row_bytes, src->data, src->row_bytes,
+                                    (size_t)src->width * src->texel_bytes, rows, cudaMemcpyDeviceToHost,
+                                    (cudaStream_t)stream);
+  return e == cudaSuccess ? PBRT_OK : cuda_fail(e, "image download");
+}
+
+PBRT_API int pbrt_stream_synchronize(pbrt_stream_t stream) {
+  cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+  return e == cudaSuccess ? PBRT_OK : cuda_fail(e, "stream synchronize");
+}
+
 PBRT_API int pbrt_gbuffer_create(uint32_t width, uint32_t height, PbrtGBuffer** out) {
   if (!out || width == 0 || height == 0) return fail(PBRT_ERROR_INVALID_ARGUMENT, "gbuffer: bad size or output");
   *out = nullptr;

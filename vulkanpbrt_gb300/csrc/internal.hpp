@@ -24,7 +24,8 @@ enum class Kind : uint32_t {
   Pipeline,
   Neural,
   Taa,
-  Batch
+  Batch,
+  BfrBlender
 };
 
 struct Object {

@@ -323,6 +323,42 @@ class BFR(Handle):
         return self._final
 
 
+class BFRBlender(Handle):
+    """BFRBlender (source/renderModules/denoisers/BFRBlender.hpp): blends
+    the final images of the 8x8, 16x16 and 32x32 denoisers by the local
+    standard deviation of the average image."""
+
+    def __init__(self, width: int, height: int, average_image: Image, average_squared_image: Image, denoised0: Image,
+                 denoised1: Image, denoised2: Image, work_width: int = 16, work_height: int = 16,
+                 filter_radius: int = 2):
+        h = C.c_void_p()
+        check(lib().pbrt_bfr_blender_create(width, height, C.byref(average_image.view),
+                                            C.byref(average_squared_image.view), C.byref(denoised0.view),
+                                            C.byref(denoised1.view), C.byref(denoised2.view), work_width, work_height,
+                                            filter_radius, C.byref(h)))
+        super().__init__(h)
+        # the images' owners must outlive this object
+        self._inputs = (average_image, average_squared_image, denoised0, denoised1, denoised2)
+        f = PbrtImage()
+        check(lib().pbrt_bfr_blender_final_image(h, C.byref(f)))
+        self._final = Image(f, self)
+
+    def compile(self, context=None) -> None:
+        pass
+
+    def update_image_layouts(self, context=None) -> None:
+        pass
+
+    def dispatch(self, stream=None) -> None:
+        check(lib().pbrt_bfr_blender_dispatch(self.ptr, stream_handle(stream)))
+
+    def add_dispatch_to_command_graph(self, commands: Commands) -> None:
+        commands.add(lambda s: self.dispatch(s))
+
+    def get_final_descriptor_image(self) -> Image:
+        return self._final
+
+
 class Taa(Handle):
     """Taa (source/renderModules/Taa.hpp): temporal anti-aliasing of a
     denoiser's final image with the accumulation buffer's motion vectors."""
