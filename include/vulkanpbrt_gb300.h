@@ -320,6 +320,17 @@ typedef struct PbrtSceneInfo {
   double build_ms;
 } PbrtSceneInfo;
 PBRT_API int pbrt_scene_create(const PbrtSceneDesc* desc, PbrtScene** out);
+/* Mesh preparation the visitor applies before it hands a mesh on
+ * (RayTracingVisitor.cpp:52-127, 133-166), host side: area-weighted running
+ * average of face normals into normals[3 * vertex_count] (not normalised,
+ * as there; the visitor does this when the mesh's first normal is zero),
+ * and texture coordinates (0,0), (0,1), (1,0) per triangle corner, later
+ * triangles overwriting earlier ones, into uvs[2 * vertex_count] (when the
+ * mesh has none). index_stride: 2 (uint16) or 4 (uint32). */
+PBRT_API int pbrt_mesh_generate_normals(const float* positions, uint32_t vertex_count, const void* indices,
+                                        uint32_t index_count, uint32_t index_stride, float* normals);
+PBRT_API int pbrt_mesh_fill_uvs(uint32_t vertex_count, const void* indices, uint32_t index_count,
+                                uint32_t index_stride, float* uvs);
 PBRT_API int pbrt_scene_info(const PbrtScene* scene, PbrtSceneInfo* info);
 /* Ray queries against the scene (no reference counterpart; the path tracer's
  * traversal exposed for tests and throughput measurement). Device arrays of n

@@ -122,6 +122,8 @@ _SIGS = {
     "pbrt_taa_create": (i32, [u32, u32, u32, u32, H, H, P(PbrtImage), P(H)]),
     "pbrt_taa_dispatch": (i32, [H, P(PbrtPushConstants), H]),
     "pbrt_taa_final_image": (i32, [H, P(PbrtImage)]),
+    "pbrt_mesh_generate_normals": (i32, [H, u32, H, u32, u32, H]),
+    "pbrt_mesh_fill_uvs": (i32, [u32, H, u32, u32, H]),
     "pbrt_image_upload": (i32, [P(PbrtImage), H, C.c_size_t, H]),
     "pbrt_image_download": (i32, [P(PbrtImage), H, C.c_size_t, H]),
     "pbrt_stream_synchronize": (i32, [H]),

@@ -104,7 +104,13 @@ class Scene:
             self.lights.append(packed_light(LIGHT_AREA, vs[0], vs[1], vs[2], emission, (0.0, 0.0, 1.0)))
 
     def finalize_lights(self) -> None:
-        """Inclusive strength prefix sums (RayTracingVisitor.cpp:428-441)."""
+        """Inclusive strength prefix sums (RayTracingVisitor.cpp:428-441),
+        after adding the default directional light to a scene without
+        lights (RayTracingVisitor.cpp:409-423)."""
+        if not self.lights:
+            from .scene_import import default_light
+
+            self.lights.append(default_light())
         acc = np.float32(0)
         for l in self.lights:
             s = np.float32(0)
