@@ -261,6 +261,58 @@ PBRT_D bool visit_node(const SceneView& sc, const RayPre& r, float tmin, TravSta
   return true;
 }
 
+// Slab-test shape (build knobs). PBRT_NEARFAR: pick each axis's near and
+// far quantised planes once per node by the sign of the ray's reciprocal
+// direction (the fma of a smaller plane gives the smaller t for a positive
+// scale, so this is the min / max of the pair, bit for bit), instead of a
+// min and a max per axis and child. PBRT_MINMAX3: the entry / exit
+// distances with three-input min / max.
+#ifndef PBRT_NEARFAR
+#define PBRT_NEARFAR 1
+#endif
+#ifndef PBRT_MINMAX3
+#define PBRT_MINMAX3 0
+#endif
+// PBRT_HITMASK: collect the children's box hits as an 8-bit mask and
+// classify it once per node (inner children: the node's inner mask, moved
+// to octant order by three conditional bit swaps; leaves: a mask made from
+// the meta bytes' triangle-count fields) instead of per child.
+#ifndef PBRT_HITMASK
+#define PBRT_HITMASK 1
+#endif
+// Bits 0, 8, 16, 24 of x -> bits 0..3.
+PBRT_D uint32_t gather_byte_lsbs(uint32_t x) { return ((x * 0x204081u) >> 21) & 0xFu; }
+// 8-bit mask of the slots whose meta byte is a leaf (triangle count 1..3 in bits 5-6).
+PBRT_D uint32_t leaf_slots(uint32_t meta_lo, uint32_t meta_hi) {
+  const uint32_t c0 = (meta_lo >> 5) & 0x03030303u, c1 = (meta_hi >> 5) & 0x03030303u;
+  return gather_byte_lsbs((c0 | (c0 >> 1)) & 0x01010101u) | (gather_byte_lsbs((c1 | (c1 >> 1)) & 0x01010101u) << 4);
+}
+// Moves bit s of an 8-bit mask to bit s ^ oct.
+PBRT_D uint32_t octant_permute(uint32_t m, int oct) {
+  if (oct & 1) m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
+  if (oct & 2) m = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
+  if (oct & 4) m = ((m & 0x0Fu) << 4) | ((m >> 4) & 0x0Fu);
+  return m;
+}
+PBRT_D float fmax3f(float a, float b, float c) {
+#if PBRT_MINMAX3
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+#else
+  return fmaxf(fmaxf(a, b), c);
+#endif
+}
+PBRT_D float fmin3f(float a, float b, float c) {
+#if PBRT_MINMAX3
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+#else
+  return fminf(fminf(a, b), c);
+#endif
+}
+
 // Deferred form: box-tests st.node's children, records the triangles of the
 // hit leaf children in st.tri_mask and moves to the next node (kNoNode when
 // the stack is empty). The ray is finished when both are exhausted.
@@ -283,11 +335,32 @@ PBRT_D void visit_node_deferred(const SceneView& sc, const RayPre& r, float tmin
   const float scx = __uint_as_float(((emi >> 0) & 0xffu) << 23) * r.inv.x;
   const float scy = __uint_as_float(((emi >> 8) & 0xffu) << 23) * r.inv.y;
   const float scz = __uint_as_float(((emi >> 16) & 0xffu) << 23) * r.inv.z;
-  uint32_t inner = 0, tris = 0;
+  uint32_t inner = 0, tris = 0, hitm = 0;
+#if PBRT_NEARFAR
+  // near / far plane words: lo for a positive reciprocal, hi for a negative one
+  const bool sx = scx < 0.f, sy = scy < 0.f, sz = scz < 0.f;
+  const uint32_t lx0 = __float_as_uint(n2.x), lx1 = __float_as_uint(n2.y), ly0 = __float_as_uint(n2.z),
+                 ly1 = __float_as_uint(n2.w), lz0 = __float_as_uint(n3.x), lz1 = __float_as_uint(n3.y);
+  const uint32_t hx0 = __float_as_uint(n3.z), hx1 = __float_as_uint(n3.w), hy0 = __float_as_uint(n4.x),
+                 hy1 = __float_as_uint(n4.y), hz0 = __float_as_uint(n4.z), hz1 = __float_as_uint(n4.w);
+  const uint32_t nx0 = sx ? hx0 : lx0, nx1 = sx ? hx1 : lx1, fx0 = sx ? lx0 : hx0, fx1 = sx ? lx1 : hx1;
+  const uint32_t ny0 = sy ? hy0 : ly0, ny1 = sy ? hy1 : ly1, fy0 = sy ? ly0 : hy0, fy1 = sy ? ly1 : hy1;
+  const uint32_t nz0 = sz ? hz0 : lz0, nz1 = sz ? hz1 : lz1, fz0 = sz ? lz0 : hz0, fz1 = sz ? lz1 : hz1;
+#endif
 #pragma unroll
   for (int s = 0; s < 8; ++s) {
     const int sh = 8 * (s & 3);
     const uint32_t meta = ((s < 4 ? meta_lo : meta_hi) >> sh) & 0xffu;
+#if PBRT_NEARFAR
+    const float tnx = fmaf((float)(((s < 4 ? nx0 : nx1) >> sh) & 0xffu), scx, adx);
+    const float tny = fmaf((float)(((s < 4 ? ny0 : ny1) >> sh) & 0xffu), scy, ady);
+    const float tnz = fmaf((float)(((s < 4 ? nz0 : nz1) >> sh) & 0xffu), scz, adz);
+    const float tfx = fmaf((float)(((s < 4 ? fx0 : fx1) >> sh) & 0xffu), scx, adx);
+    const float tfy = fmaf((float)(((s < 4 ? fy0 : fy1) >> sh) & 0xffu), scy, ady);
+    const float tfz = fmaf((float)(((s < 4 ? fz0 : fz1) >> sh) & 0xffu), scz, adz);
+    float tn = fmaxf(fmax3f(tnx, tny, tnz), tmin);
+    float tf = fminf(fmin3f(tfx, tfy, tfz), st.tbest);
+#else
     const float lx = (float)((__float_as_uint(s < 4 ? n2.x : n2.y) >> sh) & 0xffu);
     const float ly = (float)((__float_as_uint(s < 4 ? n2.z : n2.w) >> sh) & 0xffu);
     const float lz = (float)((__float_as_uint(s < 4 ? n3.x : n3.y) >> sh) & 0xffu);
@@ -299,14 +372,30 @@ PBRT_D void visit_node_deferred(const SceneView& sc, const RayPre& r, float tmin
     const float tz0 = fmaf(lz, scz, adz), tz1 = fmaf(hz, scz, adz);
     float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
     float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), st.tbest));
+#endif
     tn = tn - fabsf(tn) * 4e-7f;
     tf = tf + fabsf(tf) * 4e-7f;
+#if PBRT_HITMASK
+    hitm |= (tn <= tf ? 1u : 0u) << s;
+    (void)meta;
+#else
     const bool hit = meta != 0 && tn <= tf;
     if (hit) {
       if (meta & 0x80u) inner |= 1u << (s ^ r.oct);
       else tris |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);  // <= 8 leaves x 3 triangles: bits 0..23
     }
+#endif
   }
+#if PBRT_HITMASK
+  inner = octant_permute(hitm & imask, r.oct);
+  uint32_t lh = hitm & leaf_slots(meta_lo, meta_hi);
+  while (lh) {
+    const int s = __ffs(lh) - 1;
+    lh &= lh - 1;
+    const uint32_t meta = ((s < 4 ? meta_lo : meta_hi) >> (8 * (s & 3))) & 0xffu;
+    tris |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);  // <= 8 leaves x 3 triangles: bits 0..23
+  }
+#endif
   st.tri_base = tri_base;
   st.tri_mask = tris;
   if (kTraversePrefetch && tris) {  // the first triangle this lane tests next
@@ -1032,6 +1121,11 @@ __global__ void k_sort_scatter(const uint32_t* __restrict__ count_ptr, Queues q,
 #else
 #define PBRT_SHADE_BOUNDS __launch_bounds__(128)
 #endif
+// LM: the light-sampling mode (FrameParams::light_mode) and FIRST: the
+// primary bounce, both fixed per instantiation so each launch carries only
+// the code of its own mode and bounce (a smaller loop body: fewer
+// instruction-fetch stalls).
+template <int LM, bool FIRST>
 __global__ void PBRT_SHADE_BOUNDS k_shade(SceneView sc, const FrameParams* __restrict__ fpp, Queues q,
                                                Counters* c, GBufferOut g, int k) {
   const FrameParams& fp = *fpp;
@@ -1070,7 +1164,7 @@ __global__ void PBRT_SHADE_BOUNDS k_shade(SceneView sc, const FrameParams* __res
       }
       const bool miss = tri < 0;
       // ---- next-event estimation at this vertex (lighting.glsl:246-261) ----
-      const float3 o = (k == 0) ? -normalize(rdir) : -rdir;
+      const float3 o = FIRST ? -normalize(rdir) : -rdir;
       float3 nee = f3(0.f);
       bool nee_pending = false;
       float3 sl = f3(0.f);
@@ -1080,7 +1174,7 @@ __global__ void PBRT_SHADE_BOUNDS k_shade(SceneView sc, const FrameParams* __res
       } else {
         float lpdf;
         bool traced;
-        const float3 lcol = sample_light(sc, fp.light_mode, position, si.normal, re, sl, lpdf, shadow_tmax, traced);
+        const float3 lcol = sample_light(sc, LM, position, si.normal, re, sl, lpdf, shadow_tmax, traced);
         if (traced && !(lcol.x == 0.f && lcol.y == 0.f && lcol.z == 0.f)) {
           const float3 lh = normalize(sl + o);
           const float3 brdf = brdf_eval(o, sl, lh, si);
@@ -1091,8 +1185,8 @@ __global__ void PBRT_SHADE_BOUNDS k_shade(SceneView sc, const FrameParams* __res
           nee_pending = true;
         }
       }
-      const float3 add = (k == 0) ? si.emissive : si.emissive * thr;
-      if (k == 0) {
+      const float3 add = FIRST ? si.emissive : si.emissive * thr;
+      if (FIRST) {
         // ---- G-buffer (ptRaygen.rgen:48-60) ----
         const float3 alb = si.diffuse + si.specular;
         al = make_float4(alb.x, alb.y, alb.z, al.w);
@@ -1109,16 +1203,16 @@ __global__ void PBRT_SHADE_BOUNDS k_shade(SceneView sc, const FrameParams* __res
         push_shadow = true;
         sh_o = make_float4(position.x, position.y, position.z, 0.001f);
         sh_d = make_float4(sl.x, sl.y, sl.z, shadow_tmax);
-        sh_nee = make_float4(nee.x, nee.y, nee.z, k == 0 ? 0.f : 1.f);
+        sh_nee = make_float4(nee.x, nee.y, nee.z, FIRST ? 0.f : 1.f);
         sh_add = make_float4(add.x, add.y, add.z, 0.f);
       } else {
         float4 rd = q.rad[p];
         float3 rad = f3(rd.x, rd.y, rd.z);
-        rad = (k == 0) ? (f3(0.f) + nee) + add : rad + (nee + add);
+        rad = FIRST ? (f3(0.f) + nee) + add : rad + (nee + add);
         q.rad[p] = make_float4(rad.x, rad.y, rad.z, rd.w);
       }
       // ---- next bounce (ptRaygen.rgen:66-75, lighting.glsl:263-283) ----
-      if (k > 0) it += 1;
+      if (!FIRST) it += 1;
       if (!miss && (uint32_t)it < (uint32_t)fp.max_depth && trans < 10) {
         if (si.illum == 7) {
           it -= 1;
@@ -1304,6 +1398,7 @@ struct PbrtPipeline : pbrt::Object {
   FrameParams* dev_fp = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   int graph_depth = -1;
+  int graph_light_mode = -1;  // the light-sampling mode the captured graph's shading kernels were built for
   int grid_persistent = 0;  // traversal CTAs (persistent warps)
   int grid_shade = 0;       // shading CTAs (grid-stride)
   uint32_t* abort_host = nullptr;  // mapped pinned word (pbrt_pipeline_abort_flag)
@@ -1331,6 +1426,20 @@ struct StageEvents {
     ms[i] += t;
   }
 };
+
+static void launch_shade(int grid, cudaStream_t s, const SceneView& sc, const FrameParams* fp, const Queues& q,
+                         Counters* c, const GBufferOut& g, int k, int light_mode) {
+  if (light_mode == 1) {
+    if (k == 0) k_shade<1, true><<<grid, 128, 0, s>>>(sc, fp, q, c, g, k);
+    else k_shade<1, false><<<grid, 128, 0, s>>>(sc, fp, q, c, g, k);
+  } else if (light_mode == 2) {
+    if (k == 0) k_shade<2, true><<<grid, 128, 0, s>>>(sc, fp, q, c, g, k);
+    else k_shade<2, false><<<grid, 128, 0, s>>>(sc, fp, q, c, g, k);
+  } else {
+    if (k == 0) k_shade<0, true><<<grid, 128, 0, s>>>(sc, fp, q, c, g, k);
+    else k_shade<0, false><<<grid, 128, 0, s>>>(sc, fp, q, c, g, k);
+  }
+}
 
 static int record_frame(PbrtPipeline* pp, cudaStream_t s, StageEvents* ev) {
   const int N = pp->W * pp->H;
@@ -1366,7 +1475,7 @@ static int record_frame(PbrtPipeline* pp, cudaStream_t s, StageEvents* ev) {
       if (ev) ev->end(1);
     }
     if (ev) ev->begin(2);
-    k_shade<<<pp->grid_shade, 128, 0, s>>>(sc, pp->dev_fp, pp->q, pp->ctr, g, k);
+    launch_shade(pp->grid_shade, s, sc, pp->dev_fp, pp->q, pp->ctr, g, k, pp->light_mode);
     if (kSortRays) {
       const int nq = (k + 1) & 1;
       uint32_t* bins_r = pp->q.bins;
@@ -1759,7 +1868,7 @@ PBRT_API int pbrt_pipeline_trace(PbrtPipeline* pp, const PbrtPushConstants* pc, 
   int st = check_launch("k_set_params");
   if (st) return st;
   const int bounces = pp->max_depth + 1 + (pp->scene->transmissive ? 10 : 0);
-  if (!pp->graph_exec || pp->graph_depth != bounces) {
+  if (!pp->graph_exec || pp->graph_depth != bounces || pp->graph_light_mode != pp->light_mode) {
     if (pp->graph_exec) cudaGraphExecDestroy(pp->graph_exec);
     pp->graph_exec = nullptr;
     cudaStream_t cap;
@@ -1775,6 +1884,7 @@ PBRT_API int pbrt_pipeline_trace(PbrtPipeline* pp, const PbrtPushConstants* pc, 
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return cuda_fail(e, "graph instantiate");
     pp->graph_depth = bounces;
+    pp->graph_light_mode = pp->light_mode;
   }
   PBRT_CUDA(cudaGraphLaunch(pp->graph_exec, stream));
   return PBRT_OK;
