@@ -6,7 +6,8 @@
 //                                in BVH leaf order (48 B per triangle);
 //                                key = instance-major flat index (tie breaks)
 //   nodes     Node8[nnodes]     80 B compressed 8-wide nodes, root at 0
-//   instances DevInstance[]     object matrix, normal matrix, mesh, flags
+//   instances DevInstance[]     object matrix, normal matrix, mesh, flags, the
+//                                mesh's pool offsets and texture ids
 //   meshes    DevMesh[]         offsets into the vertex / index pools
 //   pos/nor/uv float pools      non-interleaved as the reference's SSBOs
 //   idx       uint32 pool        u32 indices, or u16 pairs packed per word
@@ -38,6 +39,11 @@ struct alignas(16) DevInstance {
   uint32_t index_stride;
   uint32_t opaque;  // 0: run the any-hit alpha test
   uint32_t pad;
+  // the mesh's pool offsets and texture ids, copied here so a hit reaches
+  // its vertices and textures one dependent load sooner
+  uint32_t vbase, ibase;
+  int32_t tex[5];
+  uint32_t pad2;
 };
 struct alignas(16) DevMaterial {
   float4 ambient_roughness, diffuse_ior, specular_dissolve, transmittance_illum, emission_texture_id;

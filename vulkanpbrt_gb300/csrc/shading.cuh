@@ -50,7 +50,18 @@ PBRT_D Rng rng_init(uint32_t x, uint32_t y, uint32_t frame) {
 // ---------------------------------------------------------------------------
 // color.glsl
 PBRT_D float luminance(float3 c) { return dot(c, f3(0.2126f, 0.7152f, 0.0722f)); }
-PBRT_D float3 srgb_to_linear(float3 c) { return f3(powf(c.x, 2.2f), powf(c.y, 2.2f), powf(c.z, 2.2f)); }
+// normalize() of the shading code: the hardware reciprocal square root
+// (2 ulp) instead of three correctly rounded divisions; ray generation, the
+// surface normal (stored in the G-buffer as angles) and the denoisers keep
+// the exact form.
+PBRT_D float3 nrmz(float3 a) { return a * rsqrtf(dot(a, a)); }
+// pow(c, 2.2) with the hardware exp2 / log2 (c >= 0: filtered texel values;
+// relative error ~1e-6, GLSL's own pow precision is exp2(y * log2(x))'s)
+PBRT_D float3 srgb_to_linear(float3 c) { return f3(__powf(c.x, 2.2f), __powf(c.y, 2.2f), __powf(c.z, 2.2f)); }
+PBRT_D float pow5(float x) {  // pow(x, 5.0)
+  const float x2 = x * x;
+  return x2 * x2 * x;
+}
 PBRT_D float3 linear_to_srgb(float3 c) {
   const float g = 1.0f / 2.2f;
   return f3(powf(c.x, g), powf(c.y, g), powf(c.z, g));
@@ -111,7 +122,7 @@ PBRT_D float3 brdf_eval(float3 v, float3 l, float3 h, const SurfaceInfo& s) {
   // BRDF_Diffuse_Disney (brdf.glsl:61-69)
   float fd90 = 0.5f + 2.0f * s.perceptual_roughness * VdotH * VdotH;
   float dim = 0.9f;  // min over (1 - 0.1) per channel
-  float dis = ((1.0f + (fd90 - 1.0f) * powf(1.0f - NdotL, 5.0f)) * (1.0f + (fd90 - 1.0f) * powf(1.0f - NdotV, 5.0f))) *
+  float dis = ((1.0f + (fd90 - 1.0f) * pow5(1.0f - NdotL)) * (1.0f + (fd90 - 1.0f) * pow5(1.0f - NdotV))) *
               kRecipPI * dim;
   float3 diffuse_c = (f3(1.f) - F) * (s.diffuse * dis);
   float3 spec = F * G * D / (4.0f * NdotL * NdotV);
@@ -124,12 +135,16 @@ PBRT_D float3 sample_ggx(float rx, float ry, float alpha2) {
   float phi = 2.f * kPI * rx;
   float cos_h = sqrtf((1.0f - ry) / (1.0f + (alpha2 - 1.0f) * ry));
   float sin_h = sqrtf(1.0f - cos_h * cos_h);
-  return f3(sin_h * cosf(phi), sin_h * sinf(phi), cos_h);
+  float sp, cp;
+  __sincosf(phi, &sp, &cp);  // phi in [0, 2 pi): the hardware sine / cosine
+  return f3(sin_h * cp, sin_h * sp, cos_h);
 }
 PBRT_D float3 sample_hemisphere(float rx, float ry) {
   float t = 2.f * kPI * ry;
   float sr = sqrtf(rx);
-  float dx = sr * cosf(t), dy = sr * sinf(t);
+  float st, ct;
+  __sincosf(t, &st, &ct);
+  float dx = sr * ct, dy = sr * st;
   return f3(dx, dy, sqrtf(fmaxf(0.f, 1.0f - dx * dx - dy * dy)));
 }
 
@@ -149,13 +164,13 @@ PBRT_D float3 sample_brdf(const SurfaceInfo& s, Rng re, float3 v, float3& l, flo
   } else {
     float3 hs = sample_hemisphere(ux, uy);
     l = s.basis0 * hs.x + s.basis1 * hs.y + b2 * hs.z;
-    h = normalize(v + l);
+    h = nrmz(v + l);
   }
   pdf = pdf_brdf(s, v, l, h);
   float3 brdf = brdf_eval(v, l, h, s);
   if (s.illum == 7) {
     float vh = dot(v, h);
-    float fr = 1.f + (0.f - 1.f) * powf(clampf(1.0f - vh, 0.0f, 1.0f), 5.0f);  // specularReflection(vec3(1), vec3(0), VdotH).x
+    float fr = 1.f + (0.f - 1.f) * pow5(clampf(1.0f - vh, 0.0f, 1.0f));  // specularReflection(vec3(1), vec3(0), VdotH).x
     if (rng_next(re) < fr || !entering) {
       float t = !entering ? s.ior : 1.f / s.ior;
       float cos_i = dot(b2, l);
@@ -204,8 +219,8 @@ PBRT_D float4 tex_sample(const SceneView& sc, int tex, float u, float v) {
 PBRT_D bool tex_is_1x1(const SceneView& sc, int tex) { return sc.textures[tex].w == 1 && sc.textures[tex].h == 1; }
 
 // unpackIndex (geometry.glsl:4-26)
-PBRT_D uint3 unpack_index(const SceneView& sc, const DevMesh& m, uint32_t prim, uint32_t stride) {
-  const uint32_t* ind = sc.idx + m.ibase;
+PBRT_D uint3 unpack_index(const SceneView& sc, uint32_t ibase, uint32_t prim, uint32_t stride) {
+  const uint32_t* ind = sc.idx + ibase;
   if (stride == 4) return make_uint3(ind[3 * prim], ind[3 * prim + 1], ind[3 * prim + 2]);
   int full = 3 * (int)prim;
   uint32_t p = (uint32_t)((float)full * .5f);
@@ -230,13 +245,13 @@ PBRT_D float2 vload2(const float* pool, uint32_t v) { return make_float2(pool[2 
 PBRT_D bool alpha_accept(const SceneView& sc, uint32_t inst_id, uint32_t prim, float bu, float bv) {
   const DevInstance& inst = sc.instances[inst_id];
   if (inst.opaque) return true;
-  const DevMesh m = sc.meshes[inst.mesh];
-  uint3 ix = unpack_index(sc, m, prim, inst.index_stride);
-  float2 t0 = vload2(sc.uv, m.vbase + ix.x), t1 = vload2(sc.uv, m.vbase + ix.y), t2 = vload2(sc.uv, m.vbase + ix.z);
+  const uint32_t vb = inst.vbase;
+  uint3 ix = unpack_index(sc, inst.ibase, prim, inst.index_stride);
+  float2 t0 = vload2(sc.uv, vb + ix.x), t1 = vload2(sc.uv, vb + ix.y), t2 = vload2(sc.uv, vb + ix.z);
   float b0 = 1.0f - bu - bv;
   float u = t0.x * b0 + t1.x * bu + t2.x * bv;
   float v = t0.y * b0 + t1.y * bu + t2.y * bv;
-  float4 d = tex_sample(sc, m.tex[0], u, v);
+  float4 d = tex_sample(sc, inst.tex[0], u, v);
   return !(d.w < .01f);
 }
 
@@ -258,21 +273,22 @@ PBRT_D float3 closest_hit(const SceneView& sc, float3 ray_dir, uint32_t inst_id,
   const float eps = 1e-6f;
   const DevInstance& inst = sc.instances[inst_id];
   const int obj = inst.mesh;
-  const DevMesh m = sc.meshes[obj];
-  uint3 ix = unpack_index(sc, m, prim, inst.index_stride);
-  float3 p0 = vload3(sc.pos, m.vbase + ix.x), p1 = vload3(sc.pos, m.vbase + ix.y), p2 = vload3(sc.pos, m.vbase + ix.z);
-  float3 n0 = vload3(sc.nor, m.vbase + ix.x), n1 = vload3(sc.nor, m.vbase + ix.y), n2 = vload3(sc.nor, m.vbase + ix.z);
-  float2 t0 = vload2(sc.uv, m.vbase + ix.x), t1 = vload2(sc.uv, m.vbase + ix.y), t2 = vload2(sc.uv, m.vbase + ix.z);
+  const uint32_t vb = inst.vbase;
+  const int32_t* mtex = inst.tex;
+  uint3 ix = unpack_index(sc, inst.ibase, prim, inst.index_stride);
+  float3 p0 = vload3(sc.pos, vb + ix.x), p1 = vload3(sc.pos, vb + ix.y), p2 = vload3(sc.pos, vb + ix.z);
+  float3 n0 = vload3(sc.nor, vb + ix.x), n1 = vload3(sc.nor, vb + ix.y), n2 = vload3(sc.nor, vb + ix.z);
+  float2 t0 = vload2(sc.uv, vb + ix.x), t1 = vload2(sc.uv, vb + ix.y), t2 = vload2(sc.uv, vb + ix.z);
   const float b0 = 1.0f - bu - bv, b1 = bu, b2 = bv;
   float2 tc = make_float2(t0.x * b0 + t1.x * b1 + t2.x * b2, t0.y * b0 + t1.y * b1 + t2.y * b2);
-  float4 dm = tex_sample(sc, m.tex[0], tc.x, tc.y);
+  float4 dm = tex_sample(sc, mtex[0], tc.x, tc.y);
   float3 diffuse = srgb_to_linear(f3(dm.x, dm.y, dm.z));
   float diffuse_a = dm.w;
   diffuse = diffuse * diffuse_a;
   float3 position = p0 * b0 + p1 * b1 + p2 * b2;
   float4 wp = mul(inst.obj, make_float4(position.x, position.y, position.z, 1.f));
   position = f3(wp.x, wp.y, wp.z);
-  float3 normal = normalize(n0 * b0 + n1 * b1 + n2 * b2);
+  float3 normal = normalize(n0 * b0 + n1 * b1 + n2 * b2);  // exact: the G-buffer stores it
   if (isinf(normal.x) || isnan(normal.x)) normal = f3(0.f, 1.f, 0.f);
   const float3 c0 = f3(inst.nrm[0].x, inst.nrm[0].y, inst.nrm[0].z);
   const float3 c1 = f3(inst.nrm[1].x, inst.nrm[1].y, inst.nrm[1].z);
@@ -291,12 +307,12 @@ PBRT_D float3 closest_hit(const SceneView& sc, float3 ray_dir, uint32_t inst_id,
   // gramSchmidt (geometry.glsl:78-82)
   float3 tt = T - project(T, normal);
   float3 bb = B - project(B, tt) - project(B, normal);
-  si.basis0 = normalize(tt);
-  si.basis1 = normalize(bb);
+  si.basis0 = nrmz(tt);
+  si.basis1 = nrmz(bb);
   si.basis2 = normal;
   // getNormal (geometry.glsl:84-92)
-  if (!tex_is_1x1(sc, m.tex[2])) {
-    float4 nm = tex_sample(sc, m.tex[2], tc.x, tc.y);
+  if (!tex_is_1x1(sc, mtex[2])) {
+    float4 nm = tex_sample(sc, mtex[2], tc.x, tc.y);
     float3 tn = f3(nm.x * 2.0f - 1.0f, nm.y * 2.0f - 1.0f, nm.z * 2.0f - 1.0f);
     normal = normalize(si.basis0 * tn.x + si.basis1 * tn.y + si.basis2 * tn.z);
   }
@@ -304,11 +320,11 @@ PBRT_D float3 closest_hit(const SceneView& sc, float3 ray_dir, uint32_t inst_id,
   diffuse = diffuse * f3(mat.diffuse_ior.x, mat.diffuse_ior.y, mat.diffuse_ior.z);
   float3 spec;
   float pr;
-  if (tex_is_1x1(sc, m.tex[4])) {
+  if (tex_is_1x1(sc, mtex[4])) {
     spec = f3(mat.specular_dissolve.x, mat.specular_dissolve.y, mat.specular_dissolve.z);
     pr = mat.ambient_roughness.w;
   } else {
-    float4 sm = tex_sample(sc, m.tex[4], tc.x, tc.y);
+    float4 sm = tex_sample(sc, mtex[4], tc.x, tc.y);
     spec = srgb_to_linear(f3(sm.x, sm.y, sm.z));
     pr = sm.w;
   }
@@ -322,8 +338,8 @@ PBRT_D float3 closest_hit(const SceneView& sc, float3 ray_dir, uint32_t inst_id,
   float3 scol = mix3(f3(0.04f), base, metallic);
   float refl = fmaxf(fmaxf(scol.x, scol.y), scol.z);
   float r90 = clampf(refl * 25.f, 0.f, 1.f);
-  float3 v = normalize(-ray_dir);
-  float4 em = tex_sample(sc, m.tex[3], tc.x, tc.y);
+  float3 v = nrmz(-ray_dir);
+  float4 em = tex_sample(sc, mtex[3], tc.x, tc.y);
   float3 emissive = f3(mat.emission_texture_id.x, mat.emission_texture_id.y, mat.emission_texture_id.z) *
                     srgb_to_linear(f3(em.x, em.y, em.z));
   if (dot(v, normal) < 0.f) emissive = f3(0.f);

@@ -280,6 +280,10 @@ PBRT_D bool visit_node(const SceneView& sc, const RayPre& r, float tmin, TravSta
 #ifndef PBRT_HITMASK
 #define PBRT_HITMASK 1
 #endif
+// byte k of w as a float (k is a constant once the child loop is unrolled;
+// measured faster than building 2^23 + byte with a byte permute and
+// subtracting 2^23)
+PBRT_D float byte_to_float(uint32_t w, int k) { return (float)((w >> (8 * k)) & 0xffu); }
 // Bits 0, 8, 16, 24 of x -> bits 0..3.
 PBRT_D uint32_t gather_byte_lsbs(uint32_t x) { return ((x * 0x204081u) >> 21) & 0xFu; }
 // 8-bit mask of the slots whose meta byte is a leaf (triangle count 1..3 in bits 5-6).
@@ -352,12 +356,13 @@ PBRT_D void visit_node_deferred(const SceneView& sc, const RayPre& r, float tmin
     const int sh = 8 * (s & 3);
     const uint32_t meta = ((s < 4 ? meta_lo : meta_hi) >> sh) & 0xffu;
 #if PBRT_NEARFAR
-    const float tnx = fmaf((float)(((s < 4 ? nx0 : nx1) >> sh) & 0xffu), scx, adx);
-    const float tny = fmaf((float)(((s < 4 ? ny0 : ny1) >> sh) & 0xffu), scy, ady);
-    const float tnz = fmaf((float)(((s < 4 ? nz0 : nz1) >> sh) & 0xffu), scz, adz);
-    const float tfx = fmaf((float)(((s < 4 ? fx0 : fx1) >> sh) & 0xffu), scx, adx);
-    const float tfy = fmaf((float)(((s < 4 ? fy0 : fy1) >> sh) & 0xffu), scy, ady);
-    const float tfz = fmaf((float)(((s < 4 ? fz0 : fz1) >> sh) & 0xffu), scz, adz);
+    const int K = s & 3;
+    const float tnx = fmaf(byte_to_float(s < 4 ? nx0 : nx1, K), scx, adx);
+    const float tny = fmaf(byte_to_float(s < 4 ? ny0 : ny1, K), scy, ady);
+    const float tnz = fmaf(byte_to_float(s < 4 ? nz0 : nz1, K), scz, adz);
+    const float tfx = fmaf(byte_to_float(s < 4 ? fx0 : fx1, K), scx, adx);
+    const float tfy = fmaf(byte_to_float(s < 4 ? fy0 : fy1, K), scy, ady);
+    const float tfz = fmaf(byte_to_float(s < 4 ? fz0 : fz1, K), scz, adz);
     float tn = fmaxf(fmax3f(tnx, tny, tnz), tmin);
     float tf = fminf(fmin3f(tfx, tfy, tfz), st.tbest);
 #else
@@ -519,7 +524,8 @@ struct Queues {
   uint32_t* pix[2];
   float4* org[2];
   float4* dir[2];
-  float4* hit;  // t, u, v, triangle slot (bits; -1 miss)
+  float4* hit;    // t, u, v, key of the closest triangle (bits; 0xffffffff miss)
+  uint2* hit_ip;  // instance and primitive of the closest triangle
   // shadow queue: path index, origin|tmin, direction|tmax, pending NEE, add term
   uint32_t* spix;
   float4* sorg;
@@ -840,7 +846,14 @@ __global__ void __launch_bounds__(128, PBRT_TRAVERSE_MIN_BLOCKS) k_traverse(Scen
     }
     // ---- ray finished
     if (MODE == 0 || (MODE == 4 && !lane_any)) {
-      q.hit[idx] = make_float4(st.tbest, st.bu, st.bv, __int_as_float(st.best_tri));
+      // the hit's instance and primitive, read here where the triangle was
+      // just tested (L1), so shading starts one dependent load later in the chain
+      uint2 ip = make_uint2(0xffffffffu, 0u);
+      if (st.best_tri >= 0)
+        ip = make_uint2(__float_as_uint(__ldg(&sc.tris[3 * st.best_tri + 1].w)),
+                        __float_as_uint(__ldg(&sc.tris[3 * st.best_tri + 2].w)));
+      q.hit[idx] = make_float4(st.tbest, st.bu, st.bv, __uint_as_float(st.best_tri >= 0 ? st.best_key : 0xffffffffu));
+      q.hit_ip[idx] = ip;
     } else if (MODE == 1 || MODE == 4) {
       const uint32_t j = MODE == 4 ? (uint32_t)idx - count_c : (uint32_t)idx;
       const uint32_t p = q.spix[j];
@@ -875,7 +888,9 @@ __global__ void __launch_bounds__(128, PBRT_TRAVERSE_MIN_BLOCKS) k_traverse(Scen
 
 // sampleLight (lighting.glsl:19-227): returns the picked light's strength
 // (lightStrength), fills the direction, the pick pdf and the shadow ray's
-// tmax; traced = false when no shadow ray is cast.
+// tmax; traced = false when no shadow ray is cast. The per-light
+// attenuation, direction and pick-probability divisions use the hardware
+// reciprocal (GLSL's own division is only 2.5 ulp).
 PBRT_D float3 sample_light(const SceneView& sc, int mode, float3 pos, float3 n, Rng& re, float3& l, float& pdf,
                            float& shadow_tmax, bool& traced) {
   const float tmin = 0.001f;
@@ -902,15 +917,15 @@ PBRT_D float3 sample_light(const SceneView& sc, int mode, float3 pos, float3 n, 
       const float3 v0 = f3(L.v0_type.x, L.v0_type.y, L.v0_type.z);
       if (type == 1) {  // directional
         float d = length(pos - v0);
-        float att = 1.0f / (L.strengths.x + L.strengths.y * d + L.strengths.z * d * d);
+        float att = __fdividef(1.0f, L.strengths.x + L.strengths.y * d + L.strengths.z * d * d);
         float3 ndir = -f3(L.dir_angle2.x, L.dir_angle2.y, L.dir_angle2.z);
         strength = fmaxf(dot(n, ndir), 0.f) * power * att;
         ls = ls * (dot(n, ndir) * att);
-        cur_l = normalize(ndir);
+        cur_l = nrmz(ndir);
       } else if (type == 2) {  // point
         float d = length(pos - v0);
-        float att = 1.0f / (L.strengths.x + L.strengths.y * d + L.strengths.z * d * d);
-        float3 to = normalize(v0 - pos);
+        float att = __fdividef(1.0f, L.strengths.x + L.strengths.y * d + L.strengths.z * d * d);
+        float3 to = nrmz(v0 - pos);
         strength = fmaxf(dot(n, to), 0.f) * power * att;
         ls = ls * (dot(n, to) * att);
         cur_l = to;
@@ -922,17 +937,17 @@ PBRT_D float3 sample_light(const SceneView& sc, int mode, float3 pos, float3 n, 
         const float3 p3 = f3(L.v2_angle.x, L.v2_angle.y, L.v2_angle.z);
         float3 lp = v0 * (1.0f - bx - by) + p2 * bx + p3 * by;  // blerp
         float3 ldir = lp - pos;
-        float3 ln = normalize(cross(p2 - v0, p3 - v0));
+        float3 ln = nrmz(cross(p2 - v0, p3 - v0));
         float d = length(ldir);
-        ldir = ldir / d;
-        float att = 1.0f / (L.strengths.x + L.strengths.y * d + L.strengths.z * d * d);
+        ldir = ldir * __fdividef(1.0f, d);
+        float att = __fdividef(1.0f, L.strengths.x + L.strengths.y * d + L.strengths.z * d * d);
         strength = fmaxf(dot(n, ldir), 0.f) * fmaxf(dot(-ldir, ln), 0.f) * power * att;
         ls = ls * (fmaxf(dot(n, ldir), 0.f) * fmaxf(dot(-ldir, ln), 0.f) * att);
         cur_l = ldir;
         cur_tmax = d - tmin;
       }
       strength_sum += strength;
-      if (rng_next(re) < strength / strength_sum) {
+      if (rng_next(re) < __fdividef(strength, strength_sum)) {
         picked_strength = strength;
         picked_ls = ls;
         tmax = cur_tmax;
@@ -975,14 +990,14 @@ PBRT_D float3 sample_light(const SceneView& sc, int mode, float3 pos, float3 n, 
   const float3 v0 = f3(L.v0_type.x, L.v0_type.y, L.v0_type.z);
   if (type == 1) {
     float d = length(pos - v0);
-    float att = 1.0f / (L.strengths.x + L.strengths.y * d + L.strengths.z * d * d);
+    float att = __fdividef(1.0f, L.strengths.x + L.strengths.y * d + L.strengths.z * d * d);
     float3 ndir = -f3(L.dir_angle2.x, L.dir_angle2.y, L.dir_angle2.z);
     ls = ls * (fmaxf(dot(n, ndir), 0.f) * att);
-    l = normalize(ndir);
+    l = nrmz(ndir);
   } else if (type == 2) {
     float d = length(pos - v0);
-    float att = 1.0f / (L.strengths.x + L.strengths.y * d + L.strengths.z * d * d);
-    float3 to = normalize(v0 - pos);
+    float att = __fdividef(1.0f, L.strengths.x + L.strengths.y * d + L.strengths.z * d * d);
+    float3 to = nrmz(v0 - pos);
     ls = ls * (fmaxf(dot(n, to), 0.f) * att);
     l = to;
   } else if (type == 5) {
@@ -995,10 +1010,10 @@ PBRT_D float3 sample_light(const SceneView& sc, int mode, float3 pos, float3 n, 
     float3 ldir = lp - pos;
     float3 lnr = cross(p2 - v0, p3 - v0);
     float area = .5f * length(lnr);
-    float3 ln = normalize(lnr);
+    float3 ln = nrmz(lnr);
     float d = length(ldir);
-    ldir = ldir / d;
-    float att = 1.0f / (L.strengths.x + L.strengths.y * d + L.strengths.z * d * d);
+    ldir = ldir * __fdividef(1.0f, d);
+    float att = __fdividef(1.0f, L.strengths.x + L.strengths.y * d + L.strengths.z * d * d);
     ls = ls * (fmaxf(dot(n, ldir), 0.f) * fmaxf(dot(-ldir, ln), 0.f) * att * area);
     l = ldir;
     tmax = d - tmin;
@@ -1145,7 +1160,8 @@ __global__ void PBRT_SHADE_BOUNDS k_shade(SceneView sc, const FrameParams* __res
       const float4 d4 = qdir[i];
       const float3 rdir = f3(d4.x, d4.y, d4.z);
       const float4 h = q.hit[i];
-      const int tri = __float_as_int(h.w);
+      const uint32_t hit_key = __float_as_uint(h.w);
+      const uint2 hit_ip = q.hit_ip[i];
       uint4 r4 = q.rng[p];
       Rng re{r4.x, r4.y, r4.z, r4.w};
       const float4 th4 = q.thr[p];
@@ -1156,15 +1172,11 @@ __global__ void PBRT_SHADE_BOUNDS k_shade(SceneView sc, const FrameParams* __res
       SurfaceInfo si;
       float3 position;
       uint32_t category;
-      if (tri < 0) {
-        miss_payload(si, position, category);
-      } else {
-        const float4 t1 = sc.tris[3 * tri + 1], t2 = sc.tris[3 * tri + 2];
-        position = closest_hit(sc, rdir, __float_as_uint(t1.w), __float_as_uint(t2.w), h.y, h.z, si, category);
-      }
-      const bool miss = tri < 0;
+      const bool miss = hit_key == 0xffffffffu;
+      if (miss) miss_payload(si, position, category);
+      else position = closest_hit(sc, rdir, hit_ip.x, hit_ip.y, h.y, h.z, si, category);
       // ---- next-event estimation at this vertex (lighting.glsl:246-261) ----
-      const float3 o = FIRST ? -normalize(rdir) : -rdir;
+      const float3 o = FIRST ? -nrmz(rdir) : -rdir;
       float3 nee = f3(0.f);
       bool nee_pending = false;
       float3 sl = f3(0.f);
@@ -1176,7 +1188,7 @@ __global__ void PBRT_SHADE_BOUNDS k_shade(SceneView sc, const FrameParams* __res
         bool traced;
         const float3 lcol = sample_light(sc, LM, position, si.normal, re, sl, lpdf, shadow_tmax, traced);
         if (traced && !(lcol.x == 0.f && lcol.y == 0.f && lcol.z == 0.f)) {
-          const float3 lh = normalize(sl + o);
+          const float3 lh = nrmz(sl + o);
           const float3 brdf = brdf_eval(o, sl, lh, si);
           const float bpdf = pdf_brdf(si, o, sl, lh);
           const float w = power_heuristic(lpdf, bpdf);
@@ -1190,7 +1202,7 @@ __global__ void PBRT_SHADE_BOUNDS k_shade(SceneView sc, const FrameParams* __res
         // ---- G-buffer (ptRaygen.rgen:48-60) ----
         const float3 alb = si.diffuse + si.specular;
         al = make_float4(alb.x, alb.y, alb.z, al.w);
-        q.prim_key[p] = miss ? 0xffffffffu : __float_as_uint(sc.tris[3 * tri].w);
+        q.prim_key[p] = hit_key;
         if (fp.write_gbuffer) {
           g.depth[p] = length(position - prev);
           g.normal[p] = make_float2(acosf(si.normal.z), atan2f(si.normal.y, si.normal.x));
@@ -1218,7 +1230,7 @@ __global__ void PBRT_SHADE_BOUNDS k_shade(SceneView sc, const FrameParams* __res
           it -= 1;
           trans += 1;
         }
-        const float3 v = normalize(prev - position);
+        const float3 v = nrmz(prev - position);
         prev = position;
         float3 l;
         float pdf;
@@ -1602,6 +1614,9 @@ PBRT_API int pbrt_scene_create(const PbrtSceneDesc* d, PbrtScene** out) {
       di.nrm[c] = make_float4((float)inv[0 * 4 + c], (float)inv[1 * 4 + c], (float)inv[2 * 4 + c], 0.f);
     di.mesh = oi.mesh_id;
     di.index_stride = oi.index_stride;
+    di.vbase = meshes[oi.mesh_id].vbase;
+    di.ibase = meshes[oi.mesh_id].ibase;
+    for (int s = 0; s < 5; ++s) di.tex[s] = meshes[oi.mesh_id].tex[s];
     di.opaque = d->instance_opaque ? (d->instance_opaque[i] ? 1u : 0u) : 1u;
     di.pad = 0;
     if (!di.opaque) any_alpha = true;
@@ -1782,6 +1797,7 @@ PBRT_API int pbrt_pipeline_create(PbrtScene* scene, PbrtGBuffer* g, PbrtIllumina
     if (!st) st = pp->a(&q.dir[i], N);
   }
   if (!st) st = pp->a(&q.hit, N);
+  if (!st) st = pp->a(&q.hit_ip, N);
   if (!st) st = pp->a(&q.spix, N);
   if (!st) st = pp->a(&q.sorg, N);
   if (!st) st = pp->a(&q.sdir, N);
