@@ -53,7 +53,8 @@ PBRT_D float luminance(float3 c) { return dot(c, f3(0.2126f, 0.7152f, 0.0722f));
 // normalize() of the shading code: the hardware reciprocal square root
 // (2 ulp) instead of three correctly rounded divisions; ray generation, the
 // surface normal (stored in the G-buffer as angles) and the denoisers keep
-// the exact form.
+// the exact form. The BRDF, sampling and tangent-frame divisions below use
+// the hardware reciprocal too (__fdividef); GLSL's own x / y is 2.5 ulp.
 PBRT_D float3 nrmz(float3 a) { return a * rsqrtf(dot(a, a)); }
 // pow(c, 2.2) with the hardware exp2 / log2 (c >= 0: filtered texel values;
 // relative error ~1e-6, GLSL's own pow precision is exp2(y * log2(x))'s)
@@ -92,14 +93,14 @@ PBRT_D float3 basis_mul(const SurfaceInfo& s, float3 v) { return s.basis0 * v.x 
 PBRT_D float specular_sample_weight(const SurfaceInfo& s) {
   float wd = mixf(luminance(s.diffuse), 0.f, s.metalness);
   float ws = luminance(s.specular);
-  return fminf(1.f, ws / (wd + wd));
+  return fminf(1.f, __fdividef(ws, wd + wd));
 }
 PBRT_D float pdf_brdf(const SurfaceInfo& s, float3 v, float3 l, float3 h) {
   float pdf_d = kRecipPI * dot(l, s.normal);
   float a2 = s.alpha_roughness * s.alpha_roughness;
   float nh = dot(h, s.normal);
   float q = nh * nh * (a2 - 1.0f) + 1.0f;
-  float pdf_s = a2 / (kPI * (q * q));
+  float pdf_s = __fdividef(a2, kPI * (q * q));
   pdf_s *= nh;
   return mixf(pdf_d, pdf_s, specular_sample_weight(s));
 }
@@ -113,19 +114,19 @@ PBRT_D float3 brdf_eval(float3 v, float3 l, float3 h, const SurfaceInfo& s) {
   float3 F = s.r0 + (s.r90 - s.r90 * s.r0) * exp2f((-5.55473f * VdotH - 6.98316f) * VdotH);
   // geometricOcclusion (brdf.glsl:104-112)
   float r = s.alpha_roughness * s.alpha_roughness;
-  float aL = 2.0f * NdotL / (NdotL + sqrtf(r + (1.0f - r) * (NdotL * NdotL)));
-  float aV = 2.0f * NdotV / (NdotV + sqrtf(r + (1.0f - r) * (NdotV * NdotV)));
+  float aL = __fdividef(2.0f * NdotL, NdotL + sqrtf(r + (1.0f - r) * (NdotL * NdotL)));
+  float aV = __fdividef(2.0f * NdotV, NdotV + sqrtf(r + (1.0f - r) * (NdotV * NdotV)));
   float G = aL * aV;
   // microfacetDistribution (brdf.glsl:125-130)
   float f = (NdotH * r - NdotH) * NdotH + 1.0f;
-  float D = r / (kPI * f * f);
+  float D = __fdividef(r, kPI * f * f);
   // BRDF_Diffuse_Disney (brdf.glsl:61-69)
   float fd90 = 0.5f + 2.0f * s.perceptual_roughness * VdotH * VdotH;
   float dim = 0.9f;  // min over (1 - 0.1) per channel
   float dis = ((1.0f + (fd90 - 1.0f) * pow5(1.0f - NdotL)) * (1.0f + (fd90 - 1.0f) * pow5(1.0f - NdotV))) *
               kRecipPI * dim;
   float3 diffuse_c = (f3(1.f) - F) * (s.diffuse * dis);
-  float3 spec = F * G * D / (4.0f * NdotL * NdotV);
+  float3 spec = F * (G * D * __fdividef(1.0f, 4.0f * NdotL * NdotV));
   if (dot(n, l) <= 0.f) spec = f3(0.f);
   return diffuse_c + spec;
 }
@@ -133,7 +134,7 @@ PBRT_D float3 brdf_eval(float3 v, float3 l, float3 h, const SurfaceInfo& s) {
 // sampling.glsl:11-27
 PBRT_D float3 sample_ggx(float rx, float ry, float alpha2) {
   float phi = 2.f * kPI * rx;
-  float cos_h = sqrtf((1.0f - ry) / (1.0f + (alpha2 - 1.0f) * ry));
+  float cos_h = sqrtf(__fdividef(1.0f - ry, 1.0f + (alpha2 - 1.0f) * ry));
   float sin_h = sqrtf(1.0f - cos_h * cos_h);
   float sp, cp;
   __sincosf(phi, &sp, &cp);  // phi in [0, 2 pi): the hardware sine / cosine
@@ -193,7 +194,7 @@ PBRT_D float3 sample_brdf(const SurfaceInfo& s, Rng re, float3 v, float3& l, flo
 // lighting.glsl:6-10
 PBRT_D float power_heuristic(float a, float b) {
   float f = a * a, g = b * b;
-  return f / (f + g);
+  return __fdividef(f, f + g);
 }
 
 // lighting.glsl:233-240
@@ -258,13 +259,13 @@ PBRT_D bool alpha_accept(const SceneView& sc, uint32_t inst_id, uint32_t prim, f
 // geometry.glsl:59-82
 PBRT_D float3 get_tangent(float3 A, float3 B, float3 C, float2 Auv, float2 Buv, float2 Cuv) {
   float bv_cv = Buv.y - Cuv.y;
-  if (bv_cv == 0.0f) return (B - C) / (Buv.x - Cuv.x);
-  float q = (Auv.y - Cuv.y) / bv_cv;
+  if (bv_cv == 0.0f) return (B - C) * __fdividef(1.0f, Buv.x - Cuv.x);
+  float q = __fdividef(Auv.y - Cuv.y, bv_cv);
   float3 D = C + (B - C) * q;
   float2 Duv = make_float2(Cuv.x + (Buv.x - Cuv.x) * q, Cuv.y + (Buv.y - Cuv.y) * q);
-  return (D - A) / (Duv.x - Auv.x);
+  return (D - A) * __fdividef(1.0f, Duv.x - Auv.x);
 }
-PBRT_D float3 project(float3 a, float3 b) { return dot(a, b) / dot(b, b) * b; }
+PBRT_D float3 project(float3 a, float3 b) { return __fdividef(dot(a, b), dot(b, b)) * b; }
 
 // ptClosesthit.rchit:18-92 (plus the payload written by ptMiss.rmiss for
 // misses). Returns the hit position; fills si and the material category.
