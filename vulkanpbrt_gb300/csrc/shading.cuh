@@ -72,10 +72,10 @@ PBRT_D float convert_metallic(float3 diffuse, float3 specular, float max_specula
   float ps = sqrtf(0.299f * specular.x * specular.x + 0.587f * specular.y * specular.y + 0.114f * specular.z * specular.z);
   if (ps < kMinRoughness) return 0.f;
   float a = kMinRoughness;
-  float b = pd * (1.0f - max_specular) / (1.0f - kMinRoughness) + ps - 2.0f * kMinRoughness;
+  float b = __fdividef(pd * (1.0f - max_specular), 1.0f - kMinRoughness) + ps - 2.0f * kMinRoughness;
   float c = kMinRoughness - ps;
   float D = fmaxf(b * b - 4.0f * a * c, 0.0f);
-  return clampf((-b + sqrtf(D)) / (2.0f * a), 0.0f, 1.0f);
+  return clampf(__fdividef(-b + sqrtf(D), 2.0f * a), 0.0f, 1.0f);
 }
 
 // ---------------------------------------------------------------------------
@@ -331,8 +331,8 @@ PBRT_D float3 closest_hit(const SceneView& sc, float3 ray_dir, uint32_t inst_id,
   }
   float max_spec = fmaxf(fmaxf(spec.x, spec.y), spec.z);
   float metallic = convert_metallic(diffuse, spec, max_spec);
-  float3 bc_diff = diffuse * ((1.0f - max_spec) / (1 - kMinRoughness) / fmaxf(1 - metallic, eps));
-  float3 bc_spec = spec - (f3(kMinRoughness) * (1 - metallic) * (1 / fmaxf(metallic, eps)));
+  float3 bc_diff = diffuse * __fdividef(__fdividef(1.0f - max_spec, 1 - kMinRoughness), fmaxf(1 - metallic, eps));
+  float3 bc_spec = spec - (f3(kMinRoughness) * (1 - metallic) * __fdividef(1.0f, fmaxf(metallic, eps)));
   float3 base = mix3(bc_diff, bc_spec, metallic * metallic);
   float3 dcol = base * (f3(1.0f) - f3(0.04f));
   dcol = dcol * (1.0f - metallic);

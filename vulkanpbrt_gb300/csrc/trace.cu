@@ -1192,7 +1192,7 @@ __global__ void PBRT_SHADE_BOUNDS k_shade(SceneView sc, const FrameParams* __res
           const float3 brdf = brdf_eval(o, sl, lh, si);
           const float bpdf = pdf_brdf(si, o, sl, lh);
           const float w = power_heuristic(lpdf, bpdf);
-          const float3 light = f3(0.f) + lcol * brdf * w / lpdf;
+          const float3 light = f3(0.f) + lcol * brdf * __fdividef(w, lpdf);
           nee = fmin3(thr * light, f3(kMaxRadiance));
           nee_pending = true;
         }
@@ -1238,11 +1238,11 @@ __global__ void PBRT_SHADE_BOUNDS k_shade(SceneView sc, const FrameParams* __res
         if (!((brdf.x == 0.f && brdf.y == 0.f && brdf.z == 0.f) || pdf < kEpsilon)) {
           float t = dot(l, si.normal);
           if (si.illum == 7) t = 1.f;
-          float3 pt = thr * (brdf * t) / pdf;
+          float3 pt = thr * (brdf * t) * __fdividef(1.0f, pdf);
           bool alive = true;
           if ((uint32_t)it > (uint32_t)fp.min_depth) {
             if (rng_next(re) < kMinTermination) alive = false;
-            pt = pt / (1.0f - kMinTermination);
+            pt = pt * __fdividef(1.0f, 1.0f - kMinTermination);
           }
           if (alive) {
             thr = pt;
