@@ -156,6 +156,11 @@ struct TravStack {
 #define PBRT_TRAVERSAL_DEFER_TRIS 1
 #endif
 constexpr int kTraversalDeferTris = PBRT_TRAVERSAL_DEFER_TRIS;
+// Shape 2: a lane postpones its triangles while fewer than 1 / PBRT_DEFER_SHARE
+// of the busy lanes have triangles to test.
+#ifndef PBRT_DEFER_SHARE
+#define PBRT_DEFER_SHARE 4
+#endif
 // L1 prefetch of the next node and of the first deferred triangle at the
 // end of a node visit (build knob).
 #ifndef PBRT_TRAVERSE_PREFETCH
@@ -812,14 +817,20 @@ __global__ void __launch_bounds__(128, PBRT_TRAVERSE_MIN_BLOCKS) k_traverse(Scen
       const unsigned act = __ballot_sync(kFullMask, busy);
       const unsigned trl = __ballot_sync(kFullMask, busy && st.tri_mask != 0);
       if (!busy) continue;
-      if (st.tri_mask && st.node != kNoNode && 4 * __popc(trl) < __popc(act) && st.sp < kStackSize) {
+      if (st.tri_mask && st.node != kNoNode && PBRT_DEFER_SHARE * __popc(trl) < __popc(act) && st.sp < kStackSize) {
         stack.put(st.sp++, make_uint2(st.tri_base, st.tri_mask | 0x80000000u));
         st.tri_mask = 0;
       }
       bool done = false;
-      if (st.tri_mask) done = test_one_triangle<ANY>(sc, r, tmin, st, nt);
-      else if (st.node != kNoNode) visit_node_deferred<false>(sc, r, tmin, st, stack, err, nn);
-      else pop_group(r, st, stack);
+      if (st.tri_mask) {
+        if (MODE == 4) done = lane_any ? test_one_triangle<true>(sc, r, tmin, st, nt_s)
+                                       : test_one_triangle<false>(sc, r, tmin, st, nt);
+        else done = test_one_triangle<ANY>(sc, r, tmin, st, nt);
+      } else if (st.node != kNoNode) {
+        visit_node_deferred<false>(sc, r, tmin, st, stack, err, (MODE == 4 && lane_any) ? nn_s : nn);
+      } else {
+        pop_group(r, st, stack);
+      }
       if (!done && (st.tri_mask || st.node != kNoNode || st.sp > 0)) continue;
     } else if (MODE == 4) {
       if (idx < 0) continue;
