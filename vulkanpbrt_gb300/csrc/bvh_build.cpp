@@ -3,6 +3,7 @@
 #include <atomic>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <future>
 #include <limits>
@@ -13,7 +14,12 @@
 namespace pbrt {
 namespace {
 
-constexpr int kBins = 32;
+constexpr int kMaxBins = 128;
+int bins_from_env() {  // binned-SAH bins (PBRT_BVH_BINS, default 32)
+  const char* e = std::getenv("PBRT_BVH_BINS");
+  const int v = e ? std::atoi(e) : 32;
+  return std::min(kMaxBins, std::max(4, v));
+}
 constexpr int kMaxLeaf = 3;
 constexpr uint32_t kParallelCutoff = 1u << 15;
 
@@ -49,6 +55,7 @@ struct BNode {
 };
 
 struct Builder {
+  int kBins = bins_from_env();
   std::vector<Box> pbox;
   std::vector<float> cent;  // 3 per prim
   std::vector<uint32_t> idx;
@@ -74,8 +81,8 @@ struct Builder {
     for (int a = 0; a < 3; ++a) {
       float ext = cb.hi[a] - cb.lo[a];
       if (!(ext > 0.f)) continue;
-      Box bb[kBins];
-      uint32_t bc[kBins] = {0};
+      Box bb[kMaxBins];
+      uint32_t bc[kMaxBins] = {0};
       float k = (float)kBins / ext;
       for (uint32_t i = begin; i < begin + count; ++i) {
         uint32_t p = idx[i];
@@ -83,8 +90,8 @@ struct Builder {
         bb[b].grow(pbox[p]);
         bc[b]++;
       }
-      double ra[kBins];
-      uint32_t rc[kBins];
+      double ra[kMaxBins];
+      uint32_t rc[kMaxBins];
       Box acc;
       uint32_t n = 0;
       for (int b = kBins - 1; b > 0; --b) {
@@ -134,11 +141,117 @@ struct Builder {
   }
 };
 
+// SAH-optimal collapse of the binary tree into 8-wide nodes (the dynamic
+// programme of Ylitie, Karras & Laine, HPG 2017, section 3.1): for every
+// binary node n and i = 1..8, cost[n][i] is the cheapest way to represent
+// n's subtree as at most i child slots of a wide node, a slot being a leaf
+// (<= 3 triangles, cost area x kPrim x count) or a wide node (cost
+// area x kNode + its best 8-slot distribution).
+struct WideDP {
+  static constexpr float kNode = 1.0f;
+  float kPrim = 0.3f;  // triangle test vs node visit cost (PBRT_BVH_PRIM_COST)
+  static constexpr float kInf = std::numeric_limits<float>::infinity();
+  const Builder& b;
+  std::vector<float> cost;      // [node][9], index 1..8
+  std::vector<int8_t> split;    // [node][9]: left share k of a distribution, 0 = take i - 1, -1 = single slot
+  std::vector<uint8_t> is_leaf; // slot type when the node is one slot
+  std::vector<int8_t> wide_split;  // left share of the 8-slot distribution of a wide node
+  explicit WideDP(const Builder& bb) : b(bb) {}
+
+  void solve(uint32_t root) {
+    const size_t n = b.next.load();
+    cost.assign(n * 9, kInf);
+    split.assign(n * 9, -1);
+    is_leaf.assign(n, 0);
+    wide_split.assign(n, 1);
+    // post-order with an explicit stack
+    std::vector<std::pair<uint32_t, bool>> stk{{root, false}};
+    while (!stk.empty()) {
+      auto [ni, done] = stk.back();
+      stk.pop_back();
+      const BNode& nd = b.nodes[ni];
+      if (nd.left >= 0 && !done) {
+        stk.push_back({ni, true});
+        stk.push_back({(uint32_t)nd.left, false});
+        stk.push_back({(uint32_t)nd.right, false});
+        continue;
+      }
+      node(ni);
+    }
+  }
+
+  void node(uint32_t ni) {
+    const BNode& nd = b.nodes[ni];
+    float* c = &cost[9 * (size_t)ni];
+    int8_t* sp = &split[9 * (size_t)ni];
+    const float area = (float)nd.box.area();
+    const float leafc = nd.count <= (uint32_t)kMaxLeaf ? area * kPrim * (float)nd.count : kInf;
+    if (nd.left < 0) {
+      for (int i = 1; i <= 8; ++i) c[i] = leafc;
+      is_leaf[ni] = 1;
+      return;
+    }
+    const float* cl = &cost[9 * (size_t)nd.left];
+    const float* cr = &cost[9 * (size_t)nd.right];
+    float dist[9];
+    int8_t arg[9];
+    for (int j = 2; j <= 8; ++j) {
+      dist[j] = kInf;
+      arg[j] = 1;
+      for (int k = 1; k < j; ++k) {
+        const float v = cl[k] + cr[j - k];
+        if (v < dist[j]) {
+          dist[j] = v;
+          arg[j] = (int8_t)k;
+        }
+      }
+    }
+    const float internal = area * kNode + dist[8];
+    is_leaf[ni] = leafc <= internal ? 1 : 0;
+    c[1] = std::min(leafc, internal);
+    sp[1] = -1;
+    for (int i = 2; i <= 8; ++i) {
+      if (dist[i] < c[i - 1]) {
+        c[i] = dist[i];
+        sp[i] = arg[i];
+      } else {
+        c[i] = c[i - 1];
+        sp[i] = 0;
+      }
+    }
+    wide_split[ni] = arg[8];
+  }
+
+  // the slots representing node ni with at most i of them
+  void slots(uint32_t ni, int i, std::vector<uint32_t>& out) const {
+    const int8_t s = split[9 * (size_t)ni + i];
+    if (i == 1 || s < 0) {
+      out.push_back(ni);
+      return;
+    }
+    if (s == 0) {
+      slots(ni, i - 1, out);
+      return;
+    }
+    const BNode& nd = b.nodes[ni];
+    slots((uint32_t)nd.left, s, out);
+    slots((uint32_t)nd.right, i - s, out);
+  }
+  // children slots of the wide node made from binary node ni
+  void children(uint32_t ni, std::vector<uint32_t>& out) const {
+    const BNode& nd = b.nodes[ni];
+    const int k = wide_split[ni];
+    slots((uint32_t)nd.left, k, out);
+    slots((uint32_t)nd.right, 8 - k, out);
+  }
+};
+
 struct Collapser {
   const Builder& b;
   std::vector<Node8>& out;
   std::vector<uint32_t>& tri_order;
   Bvh8Stats st;
+  const WideDP* dp = nullptr;  // SAH collapse (else: open the largest child)
 
   static uint8_t exponent_for(double extent) {
     // smallest power of two s with extent / s <= 255 (extent taken in double)
@@ -155,6 +268,8 @@ struct Collapser {
     const BNode& root = b.nodes[bnode];
     if (root.left < 0) {
       ch.push_back(bnode);  // single leaf under this node
+    } else if (dp) {
+      dp->children(bnode, ch);
     } else {
       ch.push_back((uint32_t)root.left);
       ch.push_back((uint32_t)root.right);
@@ -235,13 +350,14 @@ struct Collapser {
     for (int s = 0; s < 8; ++s) {
       if (!slot_used[s]) continue;
       const BNode& c = b.nodes[slot_child[s]];
+      const bool leaf_slot = c.left < 0 || (dp && dp->is_leaf[slot_child[s]]);
       for (int a = 0; a < 3; ++a) {
         double lo = std::floor(((double)c.box.lo[a] - p[a]) / scale[a]);
         double hi = std::ceil(((double)c.box.hi[a] - p[a]) / scale[a]);
         n.qlo[a][s] = (uint8_t)std::min(255.0, std::max(0.0, lo));
         n.qhi[a][s] = (uint8_t)std::min(255.0, std::max(0.0, hi));
       }
-      if (c.left >= 0) {
+      if (!leaf_slot) {
         n.imask |= (uint8_t)(1u << s);
         n.meta[s] = 0x80;
         inner.push_back({(uint32_t)s, slot_child[s]});
@@ -285,7 +401,16 @@ void build_bvh8(const float* v, size_t n, std::vector<Node8>& nodes, std::vector
   tri_order.clear();
   tri_order.reserve(n);
   nodes.resize(1);
+  // PBRT_BVH_COLLAPSE=greedy: open the largest child until 8 (the default is
+  // the SAH-optimal collapse)
+  const char* mode = std::getenv("PBRT_BVH_COLLAPSE");
+  WideDP dp(b);
+  if (const char* pc = std::getenv("PBRT_BVH_PRIM_COST")) dp.kPrim = (float)std::atof(pc);
   Collapser c{b, nodes, tri_order, {}};
+  if (!(mode && std::strcmp(mode, "greedy") == 0) && b.nodes[root].left >= 0) {
+    dp.solve(root);
+    c.dp = &dp;
+  }
   c.encode(0, root, 0);
   if (stats) {
     *stats = c.st;
