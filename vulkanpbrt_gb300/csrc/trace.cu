@@ -1141,12 +1141,13 @@ __global__ void k_sort_scatter(const uint32_t* __restrict__ count_ptr, Queues q,
 }
 
 // Shading CTAs resident per SM the register allocation targets (a build
-// knob: more CTAs, fewer registers per thread).
-#ifdef PBRT_SHADE_MIN_BLOCKS
-#define PBRT_SHADE_BOUNDS __launch_bounds__(128, PBRT_SHADE_MIN_BLOCKS)
-#else
-#define PBRT_SHADE_BOUNDS __launch_bounds__(128)
+// knob: more CTAs, fewer registers per thread). Measured at 1080p: 8 (64
+// registers, a few spills) 1.58 ms per frame; 4-5 (unbounded, ~110
+// registers) 1.90; 6 1.96; 10 1.79; 12 1.95; 16 2.38.
+#ifndef PBRT_SHADE_MIN_BLOCKS
+#define PBRT_SHADE_MIN_BLOCKS 8
 #endif
+#define PBRT_SHADE_BOUNDS __launch_bounds__(128, PBRT_SHADE_MIN_BLOCKS)
 // LM: the light-sampling mode (FrameParams::light_mode) and FIRST: the
 // primary bounce, both fixed per instantiation so each launch carries only
 // the code of its own mode and bounce (a smaller loop body: fewer
