@@ -467,7 +467,25 @@ PBRT_D void pop_group(const RayPre& r, TravState& st, TravStack& stack) {
 }
 
 // Tests the lowest triangle of st.tri_mask. Returns true for an accepted
-// any-hit (the ray is finished).
+// any-hit (the ray is finished). The runtime form (any_hit a lane flag) lets
+// a warp holding closest-hit and shadow rays run one copy of the test.
+PBRT_D bool test_one_triangle_rt(const SceneView& sc, const RayPre& r, float tmin, TravState& st, bool any_hit) {
+  const int b = __ffs(st.tri_mask) - 1;
+  st.tri_mask &= st.tri_mask - 1;
+  const uint32_t ti = st.tri_base + (uint32_t)b;
+  const float4 a = __ldg(sc.tris + 3 * ti), bb = __ldg(sc.tris + 3 * ti + 1), c = __ldg(sc.tris + 3 * ti + 2);
+  float t, u, v;
+  if (!tri_intersect(r, a, bb, c, tmin, t, u, v)) return false;
+  const uint32_t key = __float_as_uint(a.w);
+  if (!(t < st.tbest || (t == st.tbest && key < st.best_key))) return false;
+  if (sc.any_alpha && !alpha_accept_call(sc, __float_as_uint(bb.w), __float_as_uint(c.w), u, v)) return false;
+  st.best_tri = (int)ti;
+  st.tbest = t;
+  st.bu = u;
+  st.bv = v;
+  st.best_key = key;
+  return any_hit;
+}
 template <bool ANY_HIT>
 PBRT_D bool test_one_triangle(const SceneView& sc, const RayPre& r, float tmin, TravState& st, uint32_t& n_tris) {
   const int b = __ffs(st.tri_mask) - 1;
@@ -835,8 +853,9 @@ __global__ void __launch_bounds__(128, PBRT_TRAVERSE_MIN_BLOCKS) k_traverse(Scen
     } else if (MODE == 4) {
       if (idx < 0) continue;
       if (st.tri_mask) {
-        const bool acc = lane_any ? test_one_triangle<true>(sc, r, tmin, st, nt_s)
-                                  : test_one_triangle<false>(sc, r, tmin, st, nt);
+        nt += lane_any ? 0u : 1u;
+        nt_s += lane_any ? 1u : 0u;
+        const bool acc = test_one_triangle_rt(sc, r, tmin, st, lane_any);
         if (!acc && (st.tri_mask || st.node != kNoNode)) continue;
       } else {
         visit_node_deferred<true>(sc, r, tmin, st, stack, err, lane_any ? nn_s : nn);
