@@ -504,6 +504,14 @@ PBRT_API int pbrt_nn_conv3x3_fp8(const void* x1, int32_t c1, const void* x2, int
 PBRT_API int pbrt_nn_conv3x3_umma(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* w,
                                   const float* bias, void* y, int32_t n, int32_t h, int32_t w_px, int32_t cout,
                                   int32_t flags, pbrt_stream_t stream);
+/* The warp-specialised tcgen05 convolution of a single input (x1, c1) that
+ * also writes the 2x2 average pooling of its BF16 output y into pooled
+ * ([n][h/2][wd/2][cout], the same bits as pbrt_nn_avgpool2 of y): the
+ * encoder's pooling fused into the producing convolution's epilogue. Needs
+ * h % 16 == 0 and wd % 8 == 0 (else PBRT_ERROR_UNSUPPORTED). */
+PBRT_API int pbrt_nn_conv3x3_umma_pooled(const void* x1, int32_t c1, const void* w, const float* bias, void* y,
+                                         void* pooled, int32_t n, int32_t h, int32_t wd, int32_t cout, int32_t flags,
+                                         pbrt_stream_t stream);
 /* Error flags of the tcgen05 kernels since the last call (bit 0: a bounded
  * wait timed out), reset on read (stream-synchronising). */
 PBRT_API int pbrt_nn_umma_status(pbrt_stream_t stream, uint32_t* flags);

@@ -34,3 +34,27 @@ def test_conv3x3_umma_forward(cuda, n, h, w, c1, c2, cout, mode):
     print(f"umma conv rel err {rel:.2e}")
     assert ok
     assert _close(yr, ref.clamp_min(0), 4e-3)[1]
+
+
+@pytest.mark.parametrize("n,h,w,c1,cout", [(1, 32, 48, 16, 32), (2, 64, 40, 32, 48), (1, 48, 64, 48, 64),
+                                          (1, 272, 480, 48, 64)])
+def test_conv3x3_umma_pooled(cuda, n, h, w, c1, cout):
+    """The warp-specialised convolution with the next level's 2x2 average
+    pooling in its epilogue: the same output bits as without it, and the
+    same pooled bits as the stand-alone pooling kernel on that output."""
+    import torch
+
+    from vulkanpbrt_gb300 import nn
+
+    g = torch.Generator().manual_seed(h + w + c1)
+    x1 = torch.randn(n, h, w, c1, generator=g).bfloat16().to(cuda)
+    wt = (torch.randn(cout, 9, c1, generator=g) * 0.1).bfloat16().to(cuda)
+    b = torch.randn(cout, generator=g).float().to(cuda)
+    y, pooled = nn.conv3x3_umma_pooled(x1, wt, b, relu=True)
+    y_plain = nn.conv3x3_umma(x1, wt, b, relu=True)
+    p_ref = torch.empty_like(pooled)
+    nn.avgpool2(y_plain, p_ref)
+    torch.cuda.synchronize()
+    assert nn.umma_status() == 0
+    assert torch.equal(y, y_plain)
+    assert torch.equal(pooled, p_ref)

@@ -130,20 +130,29 @@ int record_forward(PbrtNeural* nd, cudaStream_t s) {
   if ((st = pbrt_nn_avgpool2(nd->rad[1], nd->rad[2], 1, n, PH / 2, PW / 2, 3, s))) return st;
   const bf16* x = nd->feat;
   const int skip_of[4] = {1, 3, 5, 7};  // e0b, e1b, e2b, e3b
+  bool pooled = false;  // the previous convolution also wrote the next level's pooled input
   for (int i = 0; i < kNumConvs; ++i) {
     const ConvSpec& c = kConvs[i];
     const int h = PH >> c.level, w = PW >> c.level;
     const bf16* w16 = nd->w16 + nd->lay.conv_w[i];
     const float* b = nd->params + nd->lay.conv_b[i];
     if (i < 10 && c.name[2] == 'a' && c.level > 0) {  // encoder: pool the previous level's output first
-      if ((st = pbrt_nn_avgpool2(x, nd->pool[c.level], 0, n, h * 2, w * 2, kConvs[i - 1].cout, s))) return st;
+      if (!pooled && (st = pbrt_nn_avgpool2(x, nd->pool[c.level], 0, n, h * 2, w * 2, kConvs[i - 1].cout, s)))
+        return st;
       x = nd->pool[c.level];
     }
+    pooled = false;
     const bf16* in1 = c.c2 ? nd->act[skip_of[c.level]] : x;
     const bf16* in2 = c.c2 ? x : nullptr;
+    // an encoder level's second convolution on the tcgen05 kernel pools its
+    // output in the epilogue (levels 0-2; the frame must divide into tiles)
+    const bool pool_here = i < 8 && (i & 1) && c.c2 == 0 && nd->conv_kernel[i] == 1 && nd->precision != 8;
     if (nd->precision == 8) {
       st = pbrt_nn_conv3x3_fp8(in1, c.c1, in2, c.c2, nd->w8 + nd->lay.conv_w[i], nd->wscale + nd->wsoff[i],
                                nd->inv_xscale + nd->xsoff[i], b, nd->act[i], n, h, w, c.cout, 1, s);
+    } else if (pool_here && (st = pbrt_nn_conv3x3_umma_pooled(in1, c.c1, w16, b, nd->act[i], nd->pool[c.level + 1],
+                                                              n, h, w, c.cout, 1, s)) != PBRT_ERROR_UNSUPPORTED) {
+      pooled = st == PBRT_OK;
     } else if (nd->conv_kernel[i] == 1) {
       st = pbrt_nn_conv3x3_umma(in1, c.c1, in2, c.c2, w16, b, nd->act[i], n, h, w, c.cout, 1, s);
     } else {

@@ -107,6 +107,7 @@ struct UmmaConvArgs {
   bf16* y;             // [N][H][W][cout]
   int N, H, W, cout;
   int relu;
+  bf16* pooled = nullptr;  // [N][H/2][W/2][cout]: 2x2 average of y (warp-specialised kernel only)
 };
 
 template <int NC>  // output channels (= MMA N), multiple of 16, <= 128
@@ -691,6 +692,37 @@ __global__ void __launch_bounds__(kWsThreads) conv3x3_umma_ws_kernel(UmmaConvArg
           uint4* d4 = reinterpret_cast<uint4*>(dst + c0);
           d4[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
           d4[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+          if (a.pooled) {
+            // 2x2 average of the stored BF16 values (the frame divides into
+            // tiles, so every lane is inside): a warp holds four 8-pixel rows
+            // of the tile (lane = 8 row + column), so a pooled pixel's window
+            // is lanes lane, lane ^ 1, lane ^ 8, lane ^ 9, summed in the
+            // order of the stand-alone pooling kernel: the same bits
+            uint32_t q1[8], q8[8], q9[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              q1[j] = __shfl_xor_sync(0xffffffffu, packed[j], 1);
+              q8[j] = __shfl_xor_sync(0xffffffffu, packed[j], 8);
+              q9[j] = __shfl_xor_sync(0xffffffffu, packed[j], 9);
+            }
+            if ((lane & 9) == 0) {
+              uint32_t po[8];
+#pragma unroll
+              for (int j = 0; j < 8; ++j) {
+                const float2 v0 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&packed[j]));
+                const float2 v1 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&q1[j]));
+                const float2 v2 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&q8[j]));
+                const float2 v3 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&q9[j]));
+                const float sx = ((v0.x + v1.x) + v2.x) + v3.x, sy = ((v0.y + v1.y) + v2.y) + v3.y;
+                const __nv_bfloat162 b2 = __floats2bfloat162_rn(0.25f * sx, 0.25f * sy);
+                po[j] = *reinterpret_cast<const uint32_t*>(&b2);
+              }
+              bf16* pd = a.pooled + (((size_t)img * (a.H >> 1) + (oy >> 1)) * (a.W >> 1) + (ox >> 1)) * a.cout + c0;
+              uint4* p4 = reinterpret_cast<uint4*>(pd);
+              p4[0] = make_uint4(po[0], po[1], po[2], po[3]);
+              p4[1] = make_uint4(po[4], po[5], po[6], po[7]);
+            }
+          }
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -889,6 +921,36 @@ PBRT_API int pbrt_nn_conv3x3_umma(const void* x1, int32_t c1, const void* x2, in
   }
   if (st) return st;
   return check_launch("conv3x3_umma_kernel");
+}
+
+// The warp-specialised convolution of a single input that also writes the
+// 2x2 average pooling of its output (the next encoder level's input; the
+// same bits as pbrt_nn_avgpool2 of y). Needs h % 16 == 0, wd % 8 == 0 and
+// the warp-specialised kernel's shared memory; PBRT_ERROR_UNSUPPORTED
+// otherwise (the caller pools separately).
+PBRT_API int pbrt_nn_conv3x3_umma_pooled(const void* x1, int32_t c1, const void* w, const float* bias, void* y,
+                                         void* pooled, int32_t n, int32_t h, int32_t wd, int32_t cout, int32_t flags,
+                                         pbrt_stream_t stream) {
+  if (!x1 || !w || !y || !pooled || c1 <= 0 || c1 % 16 || cout < 16 || cout > 128 || cout % 16 || n <= 0 || h <= 0 ||
+      wd <= 0)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "nn conv3x3 umma pooled: bad arguments (c1 %d, cout %d)", c1, cout);
+  if (h % umma::kTileH || wd % umma::kTileW || ws_smem(c1, cout, 2) > kWsSmemMax)
+    return fail(PBRT_ERROR_UNSUPPORTED, "nn conv3x3 umma pooled: %dx%d, c1 %d, cout %d", wd, h, c1, cout);
+  UmmaConvArgs a{(const bf16*)x1, nullptr, c1, 0, (const bf16*)w, bias, (bf16*)y, n, h, wd, cout, flags};
+  a.pooled = (bf16*)pooled;
+  int st;
+  switch (cout) {
+    case 16: st = launch_umma_ws<16>(a, stream, true); break;
+    case 32: st = launch_umma_ws<32>(a, stream, true); break;
+    case 48: st = launch_umma_ws<48>(a, stream, true); break;
+    case 64: st = launch_umma_ws<64>(a, stream, true); break;
+    case 80: st = launch_umma_ws<80>(a, stream, true); break;
+    case 96: st = launch_umma_ws<96>(a, stream, true); break;
+    case 112: st = launch_umma_ws<112>(a, stream, true); break;
+    default: st = launch_umma_ws<128>(a, stream, true); break;
+  }
+  if (st) return st;
+  return check_launch("conv3x3_umma_ws_kernel (pooled)");
 }
 
 // Error flags of the tcgen05 kernels since the last call (bit 0: an

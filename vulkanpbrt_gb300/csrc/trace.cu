@@ -858,7 +858,10 @@ __global__ void __launch_bounds__(128, PBRT_TRAVERSE_MIN_BLOCKS) k_traverse(Scen
         const bool acc = test_one_triangle_rt(sc, r, tmin, st, lane_any);
         if (!acc && (st.tri_mask || st.node != kNoNode)) continue;
       } else {
-        visit_node_deferred<true>(sc, r, tmin, st, stack, err, lane_any ? nn_s : nn);
+        uint32_t one = 0;
+        visit_node_deferred<true>(sc, r, tmin, st, stack, err, one);
+        nn += lane_any ? 0u : one;
+        nn_s += lane_any ? one : 0u;
         if (st.tri_mask || st.node != kNoNode) continue;
       }
     } else if (kTraversalDeferTris == 1) {

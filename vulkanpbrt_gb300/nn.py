@@ -18,6 +18,7 @@ _abi.add_signatures({
     "pbrt_nn_quantize_weights_fp8": (i32, [H, H, i32, i32, H, H, H]),
     "pbrt_nn_channel_amax": (i32, [H, i64, i32, H, H]),
     "pbrt_nn_conv3x3_umma": (i32, [H, i32, H, i32, H, H, H, i32, i32, i32, i32, i32, H]),
+    "pbrt_nn_conv3x3_umma_pooled": (i32, [H, i32, H, H, H, H, i32, i32, i32, i32, i32, H]),
     "pbrt_nn_umma_status": (i32, [H, C.POINTER(C.c_uint32)]),
     "pbrt_nn_flip_weights": (i32, [H, H, i32, i32, H]),
     "pbrt_nn_features": (i32, [H, i32, H, H, H, H, i32, i32, i32, i32, i32, H, H, H]),
@@ -117,6 +118,20 @@ def conv3x3_umma(x1, w, bias=None, x2=None, relu=False, out=None, persistent=Tru
     check(lib().pbrt_nn_conv3x3_umma(_ptr(x1), c1, _ptr(x2), c2, _ptr(w), _ptr(bias), _ptr(out), n, h, wd, cout,
                                      flags, _stream()))
     return out
+
+
+def conv3x3_umma_pooled(x1, w, bias=None, relu=False):
+    """conv3x3_umma of a single input that also returns the 2x2 average pooling of its output
+    (the same bits as avgpool2 of it), from the warp-specialised kernel's epilogue."""
+    import torch
+
+    n, h, wd, c1 = x1.shape
+    cout = w.shape[0]
+    out = torch.empty((n, h, wd, cout), dtype=torch.bfloat16, device=x1.device)
+    pooled = torch.empty((n, h // 2, wd // 2, cout), dtype=torch.bfloat16, device=x1.device)
+    check(lib().pbrt_nn_conv3x3_umma_pooled(_ptr(x1), c1, _ptr(w), _ptr(bias), _ptr(out), _ptr(pooled), n, h, wd,
+                                            cout, RELU if relu else 0, _stream()))
+    return out, pooled
 
 
 def umma_status() -> int:
