@@ -513,6 +513,7 @@ __global__ void __launch_bounds__(kWsThreads) conv3x3_umma_ws_kernel(UmmaConvArg
   __shared__ __align__(8) uint64_t full_bar[kMaxStages], empty_bar[kMaxStages], tfull_bar[2], tempty_bar[2];
   __shared__ uint32_t tmem_base_slot;
   __shared__ volatile int abort_flag;
+  __shared__ __align__(16) float s_bias[NC];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int cin = a.c1 + a.c2, planes = cin / 8;
   const int halo_bytes = planes * kPlaneBytes;
@@ -547,6 +548,7 @@ __global__ void __launch_bounds__(kWsThreads) conv3x3_umma_ws_kernel(UmmaConvArg
                  "r"(kCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
   }
+  for (int i = tid; i < NC; i += kWsThreads) s_bias[i] = a.bias ? a.bias[i] : 0.f;
   // weights, once, by every thread
   for (int i = tid; i < NC * 9 * planes; i += kWsThreads) {
     const int co = i % NC, r = i / NC;
@@ -662,25 +664,37 @@ __global__ void __launch_bounds__(kWsThreads) conv3x3_umma_ws_kernel(UmmaConvArg
       const int oy = y0 + m / kTileW, ox = x0 + m % kTileW;
       const bool inside = oy < a.H && ox < a.W;
       bf16* dst = a.y + (((size_t)img * a.H + (inside ? oy : 0)) * a.W + (inside ? ox : 0)) * a.cout;
+      // two 16-column loads in flight before one wait (fewer tensor-memory round trips)
 #pragma unroll
-      for (int c0 = 0; c0 < NC; c0 += 16) {
-        uint32_t v[16];
-        const uint32_t taddr = tmem + ((uint32_t)(sub * 32) << 16) + (uint32_t)b * NC + (uint32_t)c0;
+      for (int c00 = 0; c00 < NC; c00 += 32) {
+      uint32_t vv[2][16];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        if (c00 + 16 * h >= NC) break;
+        const uint32_t taddr = tmem + ((uint32_t)(sub * 32) << 16) + (uint32_t)b * NC + (uint32_t)(c00 + 16 * h);
+        uint32_t* v = vv[h];
         asm volatile(
             "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
             "[%16];\n"
             : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
               "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
             : "r"(taddr));
-        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+      }
+      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int c0 = c00 + 16 * h;
+        if (c0 >= NC) break;
+        const uint32_t* v = vv[h];
         if (inside) {
           uint32_t packed[8];
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
             float f0 = __uint_as_float(v[2 * j]), f1 = __uint_as_float(v[2 * j + 1]);
             if (a.bias) {
-              f0 += a.bias[c0 + 2 * j];
-              f1 += a.bias[c0 + 2 * j + 1];
+              const float2 bb = *reinterpret_cast<const float2*>(&s_bias[c0 + 2 * j]);
+              f0 += bb.x;
+              f1 += bb.y;
             }
             if (a.relu & 1) {
               f0 = fmaxf(f0, 0.f);
@@ -724,6 +738,7 @@ __global__ void __launch_bounds__(kWsThreads) conv3x3_umma_ws_kernel(UmmaConvArg
             }
           }
         }
+      }
       }
       asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
       mbar_arrive(teb(b));
