@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 
 #include "internal.hpp"
@@ -832,7 +833,12 @@ constexpr size_t kWsSmemMax = 200 * 1024;
 
 template <int NC> int launch_umma_ws(const UmmaConvArgs& a, cudaStream_t s, bool use_tma_flag) {
   const int cin = a.c1 + a.c2;
-  int stages = 6;
+  // input stages in flight (PBRT_WS_STAGES, 2..6, default 4; fewer stages, more resident CTAs)
+  static const int max_stages = [] {
+    const char* e = std::getenv("PBRT_WS_STAGES");
+    return e ? std::min(6, std::max(2, std::atoi(e))) : 4;  // 4 measured best at 1080p (3 and 6 slower)
+  }();
+  int stages = max_stages;
   while (stages > 2 && ws_smem(cin, NC, stages) > kWsSmemMax) --stages;
   const size_t smem = ws_smem(cin, NC, stages);
   static bool attr_set = false;
