@@ -12,6 +12,7 @@ pytestmark = pytest.mark.gpu
                                              (1, 16, 48, 48, 32, 48), (1, 20, 36, 64, 0, 64),
                                              (1, 18, 34, 96, 128, 96), (1, 9, 17, 128, 0, 128),
                                              (1, 34, 46, 32, 48, 32), (2, 136, 240, 32, 48, 32),
+                                             (2, 128, 256, 48, 64, 48),
                                              (1, 128, 200, 16, 0, 32)])
 @pytest.mark.parametrize("mode", ["ws", "ws_gather", "tma", "persistent", "tile"])
 def test_conv3x3_umma_forward(cuda, n, h, w, c1, c2, cout, mode):

@@ -497,7 +497,12 @@ __global__ void __launch_bounds__(128) conv3x3_umma_persistent_kernel(UmmaConvAr
 // 2-5 drain finished accumulators (bias, ReLU, BF16 stores) and release the
 // buffer. No block-wide barrier inside the tile loop. Every wait is bounded
 // (2 s); a timeout raises a shared abort flag that ends every role's loop.
-constexpr int kWsThreads = 192;
+// warp 0: TMA producer; 1: MMA issue; 2-5: epilogue; 6-9: cp.async gather of
+// the halo planes the TMA does not load (the upsampled second input), each
+// stage owned by one gather warp, so a warp's wait for its own copies does
+// not hold up the other stages
+constexpr int kWsGatherWarps = 4;
+constexpr int kWsThreads = 192 + 32 * kWsGatherWarps;
 
 __device__ __forceinline__ void mbar_arrive(uint32_t addr) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(addr) : "memory");
@@ -549,9 +554,9 @@ __global__ void __launch_bounds__(kWsThreads) conv3x3_umma_ws_kernel(UmmaConvArg
                  "r"(kCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
   }
-  for (int i = tid; i < NC; i += kWsThreads) s_bias[i] = a.bias ? a.bias[i] : 0.f;
+  for (int i = tid; i < NC; i += (int)blockDim.x) s_bias[i] = a.bias ? a.bias[i] : 0.f;
   // weights, once, by every thread
-  for (int i = tid; i < NC * 9 * planes; i += kWsThreads) {
+  for (int i = tid; i < NC * 9 * planes; i += (int)blockDim.x) {
     const int co = i % NC, r = i / NC;
     const int p = r % planes, tap = r / planes;
     umma::cp16(wbase + ((tap * planes + p) * NC + co) * 16, a.w + ((size_t)co * 9 + tap) * cin + p * 8, true);
@@ -576,15 +581,15 @@ __global__ void __launch_bounds__(kWsThreads) conv3x3_umma_ws_kernel(UmmaConvArg
   };
 
   if (warp == 0) {
-    // ---- producer
+    // ---- producer (TMA of the x1 planes)
     int i = 0;
-    for (int t = blockIdx.x; t < total_tiles && !abort_flag; t += gridDim.x, ++i) {
+    for (int t = blockIdx.x; t < total_tiles && !abort_flag && x1_planes; t += gridDim.x, ++i) {
       const int st = i % stages, k = i / stages;
       if (!wait(eb(st), (uint32_t)((k & 1) ^ 1))) break;  // the MMAs of the stage's previous tile are done
       const uint32_t hb = hbase + st * halo_pitch;
       int img, x0, y0;
       tile_origin(t, img, x0, y0);
-      if (x1_planes && lane == 0) {
+      if (lane == 0) {
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb(st)),
                      "r"((uint32_t)(x1_planes * kPlaneBytes))
                      : "memory");
@@ -594,7 +599,22 @@ __global__ void __launch_bounds__(kWsThreads) conv3x3_umma_ws_kernel(UmmaConvArg
             "l"(reinterpret_cast<uint64_t>(&x1map)), "r"(0), "r"(x0 - 1), "r"(y0 - 1), "r"(0), "r"(img), "r"(fb(st))
             : "memory");
       }
-      if (gather) {
+    }
+  } else if (warp >= 6) {
+    // ---- gather (cp.async of the planes after the TMA's). Stage st belongs
+    // to warp st % kWsGatherWarps alone, so each stage's fills and arrivals
+    // come in phase order from one warp: a warp cannot wait on a stage's
+    // empty barrier two phases late (its parity would then read as done).
+    const int gw = warp - 6;
+    int i = 0;
+    for (int t = blockIdx.x; t < total_tiles && !abort_flag && gather; t += gridDim.x, ++i) {
+      if ((i % stages) % kWsGatherWarps != gw) continue;
+      const int st = i % stages, k = i / stages;
+      if (!wait(eb(st), (uint32_t)((k & 1) ^ 1))) break;
+      const uint32_t hb = hbase + st * halo_pitch;
+      int img, x0, y0;
+      tile_origin(t, img, x0, y0);
+      {
         for (int q = lane + x1_planes * kHaloPx; q < kHaloPx * planes; q += 32) {
           const int hp = q % kHaloPx, p = q / kHaloPx;
           const int yy = y0 - 1 + hp / kHaloW, xx = x0 - 1 + hp % kHaloW;
@@ -852,13 +872,16 @@ template <int NC> int launch_umma_ws(const UmmaConvArgs& a, cudaStream_t s, bool
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   constexpr int kCols = 2 * NC <= 64 ? 64 : (2 * NC <= 128 ? 128 : 256);
-  const int per_sm = std::max(1, std::min({4, (int)((227 * 1024) / smem), 512 / kCols}));
-  const int tiles_per_image = ((a.W + umma::kTileW - 1) / umma::kTileW) * ((a.H + umma::kTileH - 1) / umma::kTileH);
-  const int grid = std::min(tiles_per_image * a.N, sms * per_sm);
   CUtensorMap map;
   memset(&map, 0, sizeof(map));
   const int use_tma = use_tma_flag && make_x1_map(&map, a.x1, a.N, a.H, a.W, a.c1) ? 1 : 0;
-  conv3x3_umma_ws_kernel<NC><<<grid, kWsThreads, smem, s>>>(a, tiles_per_image, map, use_tma, stages);
+  // the gather warps only when some planes are not loaded by the TMA
+  const bool gather = !use_tma || a.c2 > 0;
+  const int threads = gather ? kWsThreads : kWsThreads - 32 * kWsGatherWarps;
+  const int per_sm = std::max(1, std::min({4, (int)((227 * 1024) / smem), 512 / kCols, 65536 / (threads * 80)}));
+  const int tiles_per_image = ((a.W + umma::kTileW - 1) / umma::kTileW) * ((a.H + umma::kTileH - 1) / umma::kTileH);
+  const int grid = std::min(tiles_per_image * a.N, sms * per_sm);
+  conv3x3_umma_ws_kernel<NC><<<grid, threads, smem, s>>>(a, tiles_per_image, map, use_tma, stages);
   return PBRT_OK;
 }
 
@@ -900,9 +923,8 @@ PBRT_API int pbrt_nn_conv3x3_umma(const void* x1, int32_t c1, const void* x2, in
     return fail(PBRT_ERROR_INVALID_ARGUMENT, "nn conv3x3 umma: bad arguments (c1 %d, c2 %d, cout %d)", c1, c2, cout);
   UmmaConvArgs a{(const bf16*)x1, (const bf16*)x2, c1, c2, (const bf16*)w, bias, (bf16*)y, n, h, wd, cout, flags};
   int st;
-  // warp-specialised form for single inputs (its one producer warp would
-  // have to gather the upsampled second input alone)
-  if (!(flags & 10) && (c2 == 0 || (flags & 4)) && ws_smem(c1 + c2, cout, 2) <= kWsSmemMax) {
+  // warp-specialised form (the upsampled second input comes from its gather warps)
+  if (!(flags & 10) && ws_smem(c1 + c2, cout, 2) <= kWsSmemMax) {
     switch (cout) {
       case 16: st = launch_umma_ws<16>(a, stream, !(flags & 4)); break;
       case 32: st = launch_umma_ws<32>(a, stream, !(flags & 4)); break;
