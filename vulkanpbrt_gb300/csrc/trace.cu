@@ -919,6 +919,159 @@ __global__ void __launch_bounds__(128, PBRT_TRAVERSE_MIN_BLOCKS) k_traverse(Scen
   if (err) atomicOr((MODE <= 1 || MODE == 4) ? &c->error : io.errflag, 1u);
 }
 
+// Packet traversal of the primary rays (bounce 0): a warp takes 32
+// consecutive queue entries (a 32-pixel row segment) and walks the BVH
+// together: every lane box-tests the same node's children against its own
+// ray (its own t range), the warp follows the union of the hits (octant
+// order of the warp's first ray) on one shared stack, and each lane tests
+// the triangles of the union's leaves that its own ray hit. All lanes run the
+// same node visit (a single ray's traversal keeps about half of them busy on
+// primary rays); the closest hit is the same, as it depends only on which
+// triangles a ray tests, never on the order. Node visits are counted once
+// per warp (one fetch serves the 32 rays), triangle tests per ray.
+#ifndef PBRT_PACKET_PRIMARY
+#define PBRT_PACKET_PRIMARY 1
+#endif
+__global__ void __launch_bounds__(128, PBRT_TRAVERSE_MIN_BLOCKS) k_traverse_packet(SceneView sc, Queues q, Counters* c) {
+  __shared__ uint2 s_stack[kTraverseThreads / 32][kStackSize];
+  const int lane = threadIdx.x & 31;
+  uint2* stk = s_stack[threadIdx.x >> 5];
+  const uint32_t count = *((volatile uint32_t*)&c->ray[0]);
+  const float4* nodes4 = reinterpret_cast<const float4*>(sc.nodes);
+  uint32_t nn = 0, nt = 0;
+  int err = 0;
+  while (true) {
+    uint32_t base = 0;
+    if (lane == 0) {
+      base = atomicAdd(&c->work_trace, 32u);
+      if (base < count && stop_requested(c, base)) base = count;
+    }
+    base = __shfl_sync(kFullMask, base, 0);
+    if (base >= count) break;
+    const uint32_t idx = base + (uint32_t)lane;
+    const bool valid = idx < count;
+    float4 o = make_float4(0.f, 0.f, 0.f, 0.f), d = make_float4(0.f, 0.f, 1.f, -1.f);
+    if (valid) {
+      o = q.org[0][idx];
+      d = q.dir[0][idx];
+    }
+    const RayPre r = ray_pre(f3(o.x, o.y, o.z), f3(d.x, d.y, d.z));
+    const float tmin = o.w;
+    TravState st;
+    st.best_tri = -1;
+    st.tbest = d.w;  // invalid lanes: -1, so no box is ever hit
+    st.bu = st.bv = 0.f;
+    st.best_key = 0xffffffffu;
+    const int oct = __shfl_sync(kFullMask, r.oct, 0);
+    uint32_t node = 0;
+    int sp = 0;  // warp-uniform
+    while (true) {
+      // ---- box tests of node's children, per lane (the deferred visit's slab code)
+      ++nn;
+      const float4 n0 = __ldg(nodes4 + 5 * node + 0), n1 = __ldg(nodes4 + 5 * node + 1);
+      const float4 n2 = __ldg(nodes4 + 5 * node + 2), n3 = __ldg(nodes4 + 5 * node + 3);
+      const float4 n4 = __ldg(nodes4 + 5 * node + 4);
+      const uint32_t emi = __float_as_uint(n0.w), imask = emi >> 24;
+      const uint32_t child_base = __float_as_uint(n1.x), tri_base = __float_as_uint(n1.y);
+      const uint32_t meta_lo = __float_as_uint(n1.z), meta_hi = __float_as_uint(n1.w);
+      const float adx = (n0.x - r.o.x) * r.inv.x, ady = (n0.y - r.o.y) * r.inv.y, adz = (n0.z - r.o.z) * r.inv.z;
+      const float scx = __uint_as_float(((emi >> 0) & 0xffu) << 23) * r.inv.x;
+      const float scy = __uint_as_float(((emi >> 8) & 0xffu) << 23) * r.inv.y;
+      const float scz = __uint_as_float(((emi >> 16) & 0xffu) << 23) * r.inv.z;
+      const bool sx = scx < 0.f, sy = scy < 0.f, sz = scz < 0.f;
+      const uint32_t lx0 = __float_as_uint(n2.x), lx1 = __float_as_uint(n2.y), ly0 = __float_as_uint(n2.z),
+                     ly1 = __float_as_uint(n2.w), lz0 = __float_as_uint(n3.x), lz1 = __float_as_uint(n3.y);
+      const uint32_t hx0 = __float_as_uint(n3.z), hx1 = __float_as_uint(n3.w), hy0 = __float_as_uint(n4.x),
+                     hy1 = __float_as_uint(n4.y), hz0 = __float_as_uint(n4.z), hz1 = __float_as_uint(n4.w);
+      const uint32_t nx0 = sx ? hx0 : lx0, nx1 = sx ? hx1 : lx1, fx0 = sx ? lx0 : hx0, fx1 = sx ? lx1 : hx1;
+      const uint32_t ny0 = sy ? hy0 : ly0, ny1 = sy ? hy1 : ly1, fy0 = sy ? ly0 : hy0, fy1 = sy ? ly1 : hy1;
+      const uint32_t nz0 = sz ? hz0 : lz0, nz1 = sz ? hz1 : lz1, fz0 = sz ? lz0 : hz0, fz1 = sz ? lz1 : hz1;
+      uint32_t hitm = 0;
+#pragma unroll
+      for (int s = 0; s < 8; ++s) {
+        const int K = s & 3;
+        const float tnx = fmaf(byte_to_float(s < 4 ? nx0 : nx1, K), scx, adx);
+        const float tny = fmaf(byte_to_float(s < 4 ? ny0 : ny1, K), scy, ady);
+        const float tnz = fmaf(byte_to_float(s < 4 ? nz0 : nz1, K), scz, adz);
+        const float tfx = fmaf(byte_to_float(s < 4 ? fx0 : fx1, K), scx, adx);
+        const float tfy = fmaf(byte_to_float(s < 4 ? fy0 : fy1, K), scy, ady);
+        const float tfz = fmaf(byte_to_float(s < 4 ? fz0 : fz1, K), scz, adz);
+        float tn = fmaxf(fmax3f(tnx, tny, tnz), tmin);
+        float tf = fminf(fmin3f(tfx, tfy, tfz), st.tbest);
+        tn = tn - fabsf(tn) * 4e-7f;
+        tf = tf + fabsf(tf) * 4e-7f;
+        hitm |= (tn <= tf ? 1u : 0u) << s;
+      }
+      uint32_t tris = 0;
+      uint32_t lh = hitm & leaf_slots(meta_lo, meta_hi);
+      while (lh) {
+        const int s = __ffs(lh) - 1;
+        lh &= lh - 1;
+        const uint32_t meta = ((s < 4 ? meta_lo : meta_hi) >> (8 * (s & 3))) & 0xffu;
+        tris |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
+      }
+      // ---- triangles of the union's leaves, each lane those its ray reached
+      uint32_t utris = __reduce_or_sync(kFullMask, tris);
+      while (utris) {
+        const int b = __ffs(utris) - 1;
+        utris &= utris - 1;
+        if ((tris >> b) & 1u) {
+          st.tri_base = tri_base;
+          st.tri_mask = 1u << b;
+          ++nt;
+          test_one_triangle_rt(sc, r, tmin, st, false);
+        }
+      }
+      // ---- next node: nearest inner child of the union (warp octant order), rest on the stack
+      const uint32_t uinner = octant_permute(__reduce_or_sync(kFullMask, hitm & imask), oct);
+      if (uinner) {
+        const int k = __ffs(uinner) - 1;
+        const uint32_t rest = uinner & (uinner - 1);
+        if (rest) {
+          if (sp == kStackSize) {
+            err = 1;
+            break;
+          }
+          if (lane == 0) stk[sp] = make_uint2(child_base, (imask << 8) | rest);
+          ++sp;
+        }
+        const int s = k ^ oct;
+        node = child_base + __popc(imask & ((1u << s) - 1u));
+        __syncwarp();
+        continue;
+      }
+      if (sp == 0) break;
+      __syncwarp();
+      const uint2 g = stk[sp - 1];
+      uint32_t m = g.y & 0xffu;
+      const uint32_t im = g.y >> 8;
+      const int k = __ffs(m) - 1;
+      m &= m - 1;
+      __syncwarp();
+      if (m) {
+        if (lane == 0) stk[sp - 1] = make_uint2(g.x, (im << 8) | m);
+      } else {
+        --sp;
+      }
+      const int s = k ^ oct;
+      node = g.x + __popc(im & ((1u << s) - 1u));
+      __syncwarp();
+    }
+    if (valid) {
+      uint2 ip = make_uint2(0xffffffffu, 0u);
+      if (st.best_tri >= 0)
+        ip = make_uint2(__float_as_uint(__ldg(&sc.tris[3 * st.best_tri + 1].w)),
+                        __float_as_uint(__ldg(&sc.tris[3 * st.best_tri + 2].w)));
+      q.hit[idx] = make_float4(st.tbest, st.bu, st.bv, __uint_as_float(st.best_tri >= 0 ? st.best_key : 0xffffffffu));
+      q.hit_ip[idx] = ip;
+    }
+  }
+  // nodes counted per warp (lane 0's count), triangles per ray
+  warp_add64(&c->nodes_closest, lane == 0 ? nn : 0u);
+  warp_add64(&c->tris_closest, nt);
+  if (err) atomicOr(&c->error, 1u);
+}
+
 // sampleLight (lighting.glsl:19-227): returns the picked light's strength
 // (lightStrength), fills the direction, the pick pdf and the shadow ray's
 // tmax; traced = false when no shadow ray is cast. The per-light
@@ -1510,7 +1663,8 @@ static int record_frame(PbrtPipeline* pp, cudaStream_t s, StageEvents* ev) {
     if (kMergeShadow) {
       k_bounce_begin_merged<<<1, 1, 0, s>>>(pp->ctr, k);
       if (ev) ev->begin(1);
-      if (k == 0) k_traverse<0><<<pp->grid_persistent, 128, 0, s>>>(sc, pp->q, pp->ctr, k, QueryIO{});
+      if (k == 0 && PBRT_PACKET_PRIMARY) k_traverse_packet<<<pp->grid_persistent, 128, 0, s>>>(sc, pp->q, pp->ctr);
+      else if (k == 0) k_traverse<0><<<pp->grid_persistent, 128, 0, s>>>(sc, pp->q, pp->ctr, k, QueryIO{});
       else k_traverse<4><<<pp->grid_persistent, 128, 0, s>>>(sc, pp->q, pp->ctr, k, QueryIO{});
       if (ev) ev->end(1);
       k_shadow_consumed<<<1, 1, 0, s>>>(pp->ctr);
