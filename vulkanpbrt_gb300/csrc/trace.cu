@@ -689,11 +689,27 @@ __global__ void k_shadow_consumed(Counters* c) {
 }
 
 // createRay (camera.glsl:6-16) and the RNG seeding of ptRaygen.rgen:28-40.
+// Primary rays enter the queue in 8x4-pixel tiles when the frame divides
+// into them: the 32 rays a packet-traversal warp takes then cover a compact
+// patch of the image (a smaller union of nodes than a 32-pixel row).
+#ifndef PBRT_TILE_RAYGEN
+#define PBRT_TILE_RAYGEN 1
+#endif
 __global__ void k_raygen(const FrameParams* __restrict__ fpp, Queues q) {
   const FrameParams& fp = *fpp;
   const int N = fp.W * fp.H;
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) {
-    const int x = p % fp.W, y = p / fp.W;
+  const bool tiled = PBRT_TILE_RAYGEN && fp.W % 8 == 0 && fp.H % 4 == 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    int x, y;
+    if (tiled) {
+      const int tile = i >> 5, l = i & 31, tiles_x = fp.W >> 3;
+      x = (tile % tiles_x) * 8 + (l & 7);
+      y = (tile / tiles_x) * 4 + (l >> 3);
+    } else {
+      x = i % fp.W;
+      y = i / fp.W;
+    }
+    const int p = y * fp.W + x;
     Rng re = rng_init((uint32_t)x, (uint32_t)y, fp.frame);
     float pcx = (float)x + .5f, pcy = (float)y + .5f;
     if (fp.final_image && fp.sample > 0) {  // antiAlias: only FINAL_IMAGE after the first sample
@@ -706,9 +722,9 @@ __global__ void k_raygen(const FrameParams* __restrict__ fpp, Queues q) {
     float4 d = mul(fp.inv_proj, make_float4(cx, cy, 1.f, 1.f));
     float3 nd = normalize(f3(d.x, d.y, d.z));
     d = mul(fp.inv_view, make_float4(nd.x, nd.y, nd.z, 0.f));
-    q.pix[0][p] = (uint32_t)p;
-    q.org[0][p] = make_float4(org.x, org.y, org.z, 0.001f);
-    q.dir[0][p] = make_float4(d.x, d.y, d.z, 10000.0f);
+    q.pix[0][i] = (uint32_t)p;
+    q.org[0][i] = make_float4(org.x, org.y, org.z, 0.001f);
+    q.dir[0][i] = make_float4(d.x, d.y, d.z, 10000.0f);
     q.rng[p] = make_uint4(re.x, re.y, re.z, re.w);
     q.thr[p] = make_float4(1.f, 1.f, 1.f, 0.f);
     q.rad[p] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -920,7 +936,7 @@ __global__ void __launch_bounds__(128, PBRT_TRAVERSE_MIN_BLOCKS) k_traverse(Scen
 }
 
 // Packet traversal of the primary rays (bounce 0): a warp takes 32
-// consecutive queue entries (a 32-pixel row segment) and walks the BVH
+// consecutive queue entries (an 8x4-pixel tile, see k_raygen) and walks the BVH
 // together: every lane box-tests the same node's children against its own
 // ray (its own t range), the warp follows the union of the hits (octant
 // order of the warp's first ray) on one shared stack, and each lane tests
