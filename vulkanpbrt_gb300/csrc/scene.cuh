@@ -63,6 +63,7 @@ struct SceneView {
   const DevMesh* meshes;
   const DevMaterial* materials;
   const DevLight* lights;
+  const float4* light_sum;  // per light: ambient + diffuse + specular colour (xyz), w = its power (sampleLight's sums)
   const float* pos;
   const float* nor;
   const float* uv;

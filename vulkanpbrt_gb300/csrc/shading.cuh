@@ -215,6 +215,8 @@ PBRT_D float4 tex_fetch(const SceneView& sc, const DevTexture& t, int x, int y) 
 }
 PBRT_D float4 tex_sample(const SceneView& sc, int tex, float u, float v) {
   const DevTexture t = sc.textures[tex];
+  // a constant (1x1) texture: the texel itself (the bilinear weights sum to one)
+  if (t.w == 1 && t.h == 1) return tex_fetch(sc, t, 0, 0);
   return bilinear((int)t.w, (int)t.h, u, v, [&](int i, int j) { return tex_fetch(sc, t, i, j); });
 }
 PBRT_D bool tex_is_1x1(const SceneView& sc, int tex) { return sc.textures[tex].w == 1 && sc.textures[tex].h == 1; }

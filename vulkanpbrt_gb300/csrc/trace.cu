@@ -1105,12 +1105,9 @@ PBRT_D float3 sample_light(const SceneView& sc, int mode, float3 pos, float3 n, 
     float tmax = 1000.0f;
     for (uint32_t i = 0; i < sc.light_count; ++i) {
       const DevLight L = sc.lights[i];
-      const float3 ca = f3(L.col_ambient.x, L.col_ambient.y, L.col_ambient.z);
-      const float3 cd = f3(L.col_diffuse.x, L.col_diffuse.y, L.col_diffuse.z);
-      const float3 cs = f3(L.col_specular.x, L.col_specular.y, L.col_specular.z);
-      const float3 csum = ca + cd + cs;
-      const float csw = L.col_ambient.w + L.col_diffuse.w + L.col_specular.w;
-      const float power = ((csum.x + csum.y) + csum.z) + csw;  // dot(colA + colD + colS, vec4(1))
+      const float4 lsum = sc.light_sum[i];  // colA + colD + colS, and dot(colA + colD + colS, vec4(1))
+      const float3 csum = f3(lsum.x, lsum.y, lsum.z);
+      const float power = lsum.w;
       float strength = 0.f;
       float3 ls = csum;
       float cur_tmax = 1000.0f;
@@ -1185,8 +1182,8 @@ PBRT_D float3 sample_light(const SceneView& sc, int mode, float3 pos, float3 n, 
     i = (int)(rnd * (float)sc.light_count) - (int)rnd;
   }
   const DevLight L = sc.lights[i];
-  float3 ls = f3(L.col_ambient.x, L.col_ambient.y, L.col_ambient.z) + f3(L.col_diffuse.x, L.col_diffuse.y, L.col_diffuse.z) +
-              f3(L.col_specular.x, L.col_specular.y, L.col_specular.z);
+  const float4 lsum = sc.light_sum[i];
+  float3 ls = f3(lsum.x, lsum.y, lsum.z);
   float tmax = 1000.0f;
   const int type = (int)L.v0_type.w;
   const float3 v0 = f3(L.v0_type.x, L.v0_type.y, L.v0_type.z);
@@ -1888,6 +1885,16 @@ PBRT_API int pbrt_scene_create(const PbrtSceneDesc* d, PbrtScene** out) {
     if ((int)m.transmittance_illum.w == 7) sc->transmissive = true;
   std::vector<DevLight> lights(std::max<uint32_t>(1, d->light_count));
   if (d->light_count) std::memcpy(lights.data(), d->lights, sizeof(DevLight) * d->light_count);
+  // sampleLight's per-light colour sum and power, once (same FP32 order as the shader's expressions)
+  std::vector<float4> light_sum(lights.size());
+  for (size_t i = 0; i < lights.size(); ++i) {
+    const DevLight& L = lights[i];
+    const float sx = (L.col_ambient.x + L.col_diffuse.x) + L.col_specular.x;
+    const float sy = (L.col_ambient.y + L.col_diffuse.y) + L.col_specular.y;
+    const float sz = (L.col_ambient.z + L.col_diffuse.z) + L.col_specular.z;
+    const float sw = (L.col_ambient.w + L.col_diffuse.w) + L.col_specular.w;
+    light_sum[i] = make_float4(sx, sy, sz, ((sx + sy) + sz) + sw);
+  }
   SceneView& v = sc->view;
   float4* dtris = nullptr;
   Node8* dnodes = nullptr;
@@ -1895,6 +1902,7 @@ PBRT_API int pbrt_scene_create(const PbrtSceneDesc* d, PbrtScene** out) {
   DevMesh* dmesh = nullptr;
   DevMaterial* dmat = nullptr;
   DevLight* dlight = nullptr;
+  float4* dlsum = nullptr;
   float *dpos = nullptr, *dnor = nullptr, *duv = nullptr;
   uint32_t* didx = nullptr;
   DevTexture* dtex = nullptr;
@@ -1904,6 +1912,7 @@ PBRT_API int pbrt_scene_create(const PbrtSceneDesc* d, PbrtScene** out) {
   if (!st) st = sc->up(&dmesh, meshes.data(), meshes.size());
   if (!st) st = sc->up(&dmat, mats.data(), mats.size());
   if (!st) st = sc->up(&dlight, lights.data(), lights.size());
+  if (!st) st = sc->up(&dlsum, light_sum.data(), light_sum.size());
   if (!st) st = sc->up(&dpos, pos.data(), pos.size());
   if (!st) st = sc->up(&dnor, nor.data(), nor.size());
   if (!st) st = sc->up(&duv, uv.data(), uv.size());
@@ -1919,6 +1928,7 @@ PBRT_API int pbrt_scene_create(const PbrtSceneDesc* d, PbrtScene** out) {
   v.meshes = dmesh;
   v.materials = dmat;
   v.lights = dlight;
+  v.light_sum = dlsum;
   v.pos = dpos;
   v.nor = dnor;
   v.uv = duv;
