@@ -495,7 +495,9 @@ PBRT_API int pbrt_nn_conv3x3(const void* x1, int32_t c1, const void* x2, int32_t
 /* FP8 (e4m3) variant for inference: w8 [cout][9][c1+c2] e4m3 with per-output-
  * channel scales wscale and the per-input-channel activation scales folded
  * in (pbrt_nn_quantize_weights_fp8); BF16 inputs are quantised on load with
- * inv_xscale [c1+c2] (saturating); c1 + c2 <= 256; flags bit 0: ReLU. */
+ * inv_xscale [c1+c2] (saturating); c1 + c2 <= 256; flags bit 0: ReLU,
+ * bit 3: the mma.sync kernel only (default: pbrt_nn_conv3x3_fp8_umma where
+ * it applies, this kernel otherwise). */
 PBRT_API int pbrt_nn_conv3x3_fp8(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* w8,
                                  const float* wscale, const float* inv_xscale, const float* bias, void* y, int32_t n,
                                  int32_t h, int32_t w_px, int32_t cout, int32_t flags, pbrt_stream_t stream);
@@ -512,6 +514,16 @@ PBRT_API int pbrt_nn_conv3x3_umma(const void* x1, int32_t c1, const void* x2, in
 PBRT_API int pbrt_nn_conv3x3_umma_pooled(const void* x1, int32_t c1, const void* w, const float* bias, void* y,
                                          void* pooled, int32_t n, int32_t h, int32_t wd, int32_t cout, int32_t flags,
                                          pbrt_stream_t stream);
+/* The FP8 convolution on the tcgen05 tensor cores (kind::f8f6f4, K = 32 per
+ * instruction): the arguments and quantisation of pbrt_nn_conv3x3_fp8, cout
+ * in {16, 32, ..., 128}, plus an optional pooled output as in
+ * pbrt_nn_conv3x3_umma_pooled (x2 must then be NULL). PBRT_ERROR_UNSUPPORTED
+ * when the weights and two input stages do not fit in shared memory, an
+ * operand is not 16-byte aligned, or (pooled) h % 16 or wd % 8 is not 0. */
+PBRT_API int pbrt_nn_conv3x3_fp8_umma(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* w8,
+                                      const float* wscale, const float* inv_xscale, const float* bias, void* y,
+                                      void* pooled, int32_t n, int32_t h, int32_t w_px, int32_t cout, int32_t flags,
+                                      pbrt_stream_t stream);
 /* Error flags of the tcgen05 kernels since the last call (bit 0: a bounded
  * wait timed out), reset on read (stream-synchronising). */
 PBRT_API int pbrt_nn_umma_status(pbrt_stream_t stream, uint32_t* flags);
@@ -604,8 +616,11 @@ PBRT_API int pbrt_neural_set_fallback(PbrtNeural* nd, PbrtBMFR* bmfr, float thre
 /* FP8 inference: calibrate runs one BF16 pass on the current inputs
  * (stream-synchronising) and derives per-input-channel activation scales
  * (max |x| / 448) and per-output-channel e4m3 weights; set_precision(8)
- * then runs every convolution as e4m3 x e4m3 -> FP32 on the tensor cores,
- * set_precision(16) returns to BF16. New parameters drop the calibration. */
+ * then runs every convolution but the first (16 input channels, which stays
+ * BF16) as e4m3 x e4m3 -> FP32 on the tensor cores (tcgen05 kind::f8f6f4
+ * where the layer fits in shared memory, mma.sync otherwise), with the
+ * encoder's pooling fused as in BF16; set_precision(16) returns to BF16.
+ * New parameters drop the calibration. */
 PBRT_API int pbrt_neural_calibrate(PbrtNeural* nd, pbrt_stream_t stream);
 PBRT_API int pbrt_neural_set_precision(PbrtNeural* nd, int32_t bits);
 /* Per-layer convolution kernel: 0 = warp-level mma.sync kernels, 1 =

@@ -1,6 +1,8 @@
-"""FP8 (e4m3) inference path of the neural denoiser: the FP8 convolution
-against a plain PyTorch FP32 convolution of the same e4m3-quantised operands
-(one BF16 ulp, 4e-3 of the output scale), the weight quantiser against
+"""FP8 (e4m3) inference path of the neural denoiser: the FP8 convolutions
+(the tcgen05 kind::f8f6f4 form and the mma.sync kernel) against a plain
+PyTorch FP32 convolution of the same e4m3-quantised operands (one BF16 ulp,
+4e-3 of the output scale), the fused pooling of the tcgen05 form against the
+stand-alone pooling kernel (bit-exact), the weight quantiser against
 torch's own e4m3 rounding (byte-exact), and the calibrated FP8 network
 against the BF16 network on the same frame."""
 import pytest
@@ -8,14 +10,14 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("n,h,w,c1,c2,cout", [(1, 24, 40, 16, 0, 32), (2, 16, 32, 48, 64, 48), (1, 20, 36, 96, 128, 96),
-                                             (1, 9, 17, 32, 0, 128)])
-def test_conv3x3_fp8_matches_quantised_reference(cuda, n, h, w, c1, c2, cout):
+def _fp8_case(n, h, w, c1, c2, cout):
+    """Seeded inputs, device-quantised weights and the FP32 reference convolution of the same e4m3 operands."""
     import torch
     import torch.nn.functional as F
 
     from vulkanpbrt_gb300 import nn
 
+    cuda = torch.device("cuda:0")
     g = torch.Generator().manual_seed(c1 + c2 + cout)
     x1 = (torch.randn(n, h, w, c1, generator=g).abs() * 3).bfloat16()
     x2 = (torch.randn(n, h // 2, w // 2, c2, generator=g).abs()).bfloat16() if c2 else None
@@ -26,25 +28,83 @@ def test_conv3x3_fp8_matches_quantised_reference(cuda, n, h, w, c1, c2, cout):
     xc = torch.cat([x1.float(), up], -1) if c2 else x1.float()
     amax = xc.abs().amax((0, 1, 2))
     xs = torch.where(amax > 0, amax / 448.0, torch.ones_like(amax))
-    # device-side quantisation and convolution
-    amax_d = torch.zeros(c1, device=cuda)
-    nn.channel_amax(x1.to(cuda), amax_d)
-    assert torch.equal(amax_d.cpu(), x1.float().abs().amax((0, 1, 2)))
     w8, ws = nn.quantize_weights_fp8(w32.to(cuda), xs.to(cuda))
-    y = nn.conv3x3_fp8(x1.to(cuda), w8, ws, (1.0 / xs).to(cuda), bias.to(cuda), x2=x2.to(cuda) if c2 else None)
-    torch.cuda.synchronize()
-    # reference: the same e4m3 operands in FP32
     wsc = (w32 * xs).abs().amax((1, 2)) / 448.0
     w8_ref = (w32 * xs / wsc[:, None, None]).to(torch.float8_e4m3fn)
     assert torch.equal(w8.cpu(), w8_ref.view(torch.uint8))
     assert torch.allclose(ws.cpu(), wsc, rtol=1e-6)
     xq = (xc * (1.0 / xs)).to(torch.float8_e4m3fn).float()
     wt = w8_ref.float().reshape(cout, 3, 3, cin).permute(0, 3, 1, 2)
-    ref = F.conv2d(xq.permute(0, 3, 1, 2), wt, padding=1).permute(0, 2, 3, 1) * wsc + bias
+    ref = F.conv2d(xq.permute(0, 3, 1, 2).to(cuda), wt.to(cuda), padding=1).permute(0, 2, 3, 1).cpu() * wsc + bias
+    args = dict(x1=x1.to(cuda), w8=w8, wscale=ws, inv_xscale=(1.0 / xs).to(cuda), bias=bias.to(cuda),
+                x2=x2.to(cuda) if c2 else None)
+    return args, ref
+
+
+def _check(y, ref, what):
     scale = ref.abs().max().item()
     err = (y.float().cpu() - ref).abs().max().item()
-    print(f"fp8 conv max err / scale = {err / scale:.2e}")
+    print(f"{what}: fp8 conv max err / scale = {err / scale:.2e}")
     assert err <= 4e-3 * scale
+
+
+@pytest.mark.parametrize("kernel", ["auto", "mma"])
+@pytest.mark.parametrize("n,h,w,c1,c2,cout", [(1, 24, 40, 16, 0, 32), (2, 16, 32, 48, 64, 48), (1, 20, 36, 96, 128, 96),
+                                             (1, 9, 17, 32, 0, 128)])
+def test_conv3x3_fp8_matches_quantised_reference(cuda, n, h, w, c1, c2, cout, kernel):
+    import torch
+
+    from vulkanpbrt_gb300 import nn
+
+    x1 = (torch.randn(n, h, w, c1, generator=torch.Generator().manual_seed(c1 + c2 + cout)).abs() * 3).bfloat16()
+    amax_d = torch.zeros(c1, device=cuda)
+    nn.channel_amax(x1.to(cuda), amax_d)
+    assert torch.equal(amax_d.cpu(), x1.float().abs().amax((0, 1, 2)))
+    args, ref = _fp8_case(n, h, w, c1, c2, cout)
+    y = nn.conv3x3_fp8(**args, kernel=kernel)
+    torch.cuda.synchronize()
+    _check(y, ref, kernel)
+
+
+# the tcgen05 form alone: the padded 16-channel input, the upsampled second
+# input, Cout 128, 160 input channels (two stages in 204 KB of shared
+# memory), and a frame of more tiles than resident CTAs (every input stage
+# and accumulator buffer reused several times)
+@pytest.mark.parametrize("n,h,w,c1,c2,cout", [(1, 24, 40, 16, 0, 32), (2, 32, 64, 48, 64, 48), (1, 9, 17, 32, 0, 128),
+                                             (1, 40, 24, 80, 0, 96), (1, 48, 64, 64, 96, 64),
+                                             (4, 256, 256, 32, 0, 32)])
+def test_conv3x3_fp8_umma(cuda, n, h, w, c1, c2, cout):
+    import torch
+
+    from vulkanpbrt_gb300 import nn
+
+    args, ref = _fp8_case(n, h, w, c1, c2, cout)
+    y = nn.conv3x3_fp8(**args, kernel="umma")
+    assert nn.umma_status() == 0
+    _check(y, ref, "umma")
+    # the same operands on the mma.sync kernel: the two agree to the BF16 rounding of the output
+    y_mma = nn.conv3x3_fp8(**args, kernel="mma")
+    torch.cuda.synchronize()
+    d = (y.float() - y_mma.float()).abs().max().item()
+    assert d <= 8e-3 * ref.abs().max().item()
+
+
+def test_conv3x3_fp8_umma_pooled(cuda):
+    import torch
+
+    from vulkanpbrt_gb300 import nn
+
+    args, _ = _fp8_case(2, 64, 48, 32, 0, 48)
+    y0 = nn.conv3x3_fp8(**args, relu=True, kernel="umma")
+    y, pooled = nn.conv3x3_fp8(**args, relu=True, pooled=True)
+    assert nn.umma_status() == 0
+    assert torch.equal(y, y0)
+    assert torch.equal(pooled, nn.avgpool2(y, torch.empty_like(pooled)))
+    import vulkanpbrt_gb300 as vp
+
+    a2, _ = _fp8_case(1, 24, 40, 16, 0, 32)  # a frame that does not divide into 16 x 8 tiles
+    with pytest.raises(vp.PbrtError):
+        nn.conv3x3_fp8(**a2, pooled=True)
 
 
 def test_fp8_network_close_to_bf16(cuda):

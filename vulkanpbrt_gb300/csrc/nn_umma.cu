@@ -17,6 +17,7 @@
 // MMAs, frees its tensor memory and returns.
 #include <cuda.h>  // CUtensorMap (the encoder is fetched through the runtime)
 #include <cuda_bf16.h>
+#include <cuda_fp8.h>
 
 #include <algorithm>
 #include <cstdint>
@@ -65,6 +66,12 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kM >> 4) << 24);
 }
 
+// Instruction descriptor, kind::f8f6f4: FP32 accumulator, E4M3 A and B
+// (format code 0), both K-major, M = 128, N = n. K = 32 per instruction.
+__host__ __device__ constexpr uint32_t idesc_e4m3(int n) {
+  return (1u << 4) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kM >> 4) << 24);
+}
+
 __device__ __forceinline__ void mbar_init(uint32_t addr, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(addr), "r"(count));
 }
@@ -109,6 +116,12 @@ struct UmmaConvArgs {
   int N, H, W, cout;
   int relu;
   bf16* pooled = nullptr;  // [N][H/2][W/2][cout]: 2x2 average of y (warp-specialised kernel only)
+  // FP8 form of the warp-specialised kernel: e4m3 weights [cout][9][c1 + c2]
+  // with one scale per output channel, and the per-input-channel scales
+  // that quantise the BF16 activations on their way into shared memory
+  const uint8_t* w8 = nullptr;
+  const float* wscale = nullptr;      // [cout]
+  const float* inv_xscale = nullptr;  // [c1 + c2]
 };
 
 template <int NC>  // output channels (= MMA N), multiple of 16, <= 128
@@ -501,6 +514,16 @@ __global__ void __launch_bounds__(128) conv3x3_umma_persistent_kernel(UmmaConvAr
 // the halo planes the TMA does not load (the upsampled second input), each
 // stage owned by one gather warp, so a warp's wait for its own copies does
 // not hold up the other stages
+//
+// FP8 form (kF8): a stage receives the BF16 halo planes as above (the TMA
+// completes on a separate per-stage barrier); the stage's gather warp waits
+// for them, quantises them in place with the per-input-channel scales
+// (e4m3, saturating) into planes of 16 e4m3 channels (16 bytes a pixel:
+// the plane geometry of 8 BF16 channels), zeros past the input channels up
+// to a multiple of 32, and only then arrives on the "full" barrier; the MMA
+// warp issues kind::f8f6f4 with K = 32 (two planes) per instruction, half
+// the BF16 instruction count; the epilogue multiplies by the per-output-
+// channel weight scale before the bias.
 constexpr int kWsGatherWarps = 4;
 constexpr int kWsThreads = 192 + 32 * kWsGatherWarps;
 
@@ -508,8 +531,23 @@ __device__ __forceinline__ void mbar_arrive(uint32_t addr) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(addr) : "memory");
 }
 
-template <int NC>
-__global__ void __launch_bounds__(kWsThreads) conv3x3_umma_ws_kernel(UmmaConvArgs a, int tiles_per_image,
+// e4m3 codes (saturating) of four BF16 values (two packed pairs) scaled by
+// s[0..3], in channel order from the low byte: the quantisation of the
+// mma.sync FP8 kernel.
+__device__ __forceinline__ uint32_t quant4_e4m3(uint32_t lo2, uint32_t hi2, const float* s) {
+  const float2 f0 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&lo2));
+  const float2 f1 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&hi2));
+  const __nv_fp8x2_storage_t q0 = __nv_cvt_float2_to_fp8x2(make_float2(f0.x * s[0], f0.y * s[1]), __NV_SATFINITE,
+                                                           __NV_E4M3);
+  const __nv_fp8x2_storage_t q1 = __nv_cvt_float2_to_fp8x2(make_float2(f1.x * s[2], f1.y * s[3]), __NV_SATFINITE,
+                                                           __NV_E4M3);
+  return (uint32_t)q0 | ((uint32_t)q1 << 16);
+}
+
+// FP8: at most 64 registers, three CTAs an SM (the full-resolution layers
+// run out of CTAs in flight with two); BF16: the compiler's allocation.
+template <int NC, bool kF8>
+__global__ void __launch_bounds__(kWsThreads, kF8 ? 3 : 0) conv3x3_umma_ws_kernel(UmmaConvArgs a, int tiles_per_image,
                                                                      const __grid_constant__ CUtensorMap x1map,
                                                                      int use_tma, int stages) {
   using namespace umma;
@@ -517,18 +555,26 @@ __global__ void __launch_bounds__(kWsThreads) conv3x3_umma_ws_kernel(UmmaConvArg
   constexpr int kMaxStages = 6;
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t full_bar[kMaxStages], empty_bar[kMaxStages], tfull_bar[2], tempty_bar[2];
+  __shared__ __align__(8) uint64_t tma_bar[kF8 ? kMaxStages : 1];  // FP8: the TMA's arrival per stage
   __shared__ uint32_t tmem_base_slot;
   __shared__ volatile int abort_flag;
   __shared__ __align__(16) float s_bias[NC];
+  __shared__ __align__(16) float s_wsc[kF8 ? NC : 1];    // FP8: weight scale per output channel
+  __shared__ __align__(16) float s_inv[kF8 ? 256 : 4];   // FP8: 1 / activation scale per input channel, 0 past cin
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int cin = a.c1 + a.c2, planes = cin / 8;
-  const int halo_bytes = planes * kPlaneBytes;
+  const int cin = a.c1 + a.c2;
+  // MMA planes: 8 BF16 channels, or 16 e4m3 channels (input padded to a multiple of 32)
+  const int planes = kF8 ? ((cin + 31) & ~31) / 16 : cin / 8;
+  // BF16 planes a stage receives (8 channels each); the FP8 form quantises
+  // them in place into its e4m3 planes (at most the same bytes)
+  const int in_planes = cin / 8;
+  const int halo_bytes = in_planes * kPlaneBytes;
   const int halo_pitch = (halo_bytes + 1023) & ~1023;
   const int tiles_x = (a.W + kTileW - 1) / kTileW;
   const int total_tiles = tiles_per_image * a.N;
   const int H2 = a.H >> 1, W2 = a.W >> 1;
   const int x1_planes = use_tma ? a.c1 / 8 : 0;
-  const bool gather = planes > x1_planes;  // cp.async part present
+  const bool gather = kF8 || in_planes > x1_planes;  // cp.async part present (FP8: the quantising warps)
   const uint32_t sbase = smem_addr(smem);
   const uint32_t wbase = sbase;
   const uint32_t hbase = (sbase + 9 * planes * NC * 16 + 1023u) & ~1023u;
@@ -536,10 +582,12 @@ __global__ void __launch_bounds__(kWsThreads) conv3x3_umma_ws_kernel(UmmaConvArg
   auto eb = [&](int st) { return smem_addr(&empty_bar[st]); };
   auto tfb = [&](int b) { return smem_addr(&tfull_bar[b]); };
   auto teb = [&](int b) { return smem_addr(&tempty_bar[b]); };
+  auto tmb = [&](int st) { return smem_addr(&tma_bar[kF8 ? st : 0]); };
   if (tid == 0) {
     for (int st = 0; st < stages; ++st) {
-      umma::mbar_init(fb(st), (x1_planes ? 1u : 0u) + (gather ? 32u : 0u));
+      umma::mbar_init(fb(st), kF8 ? 32u : (x1_planes ? 1u : 0u) + (gather ? 32u : 0u));
       umma::mbar_init(eb(st), 1);
+      if (kF8) umma::mbar_init(tmb(st), 1);
     }
     for (int b = 0; b < 2; ++b) {
       umma::mbar_init(tfb(b), 1);
@@ -555,11 +603,21 @@ __global__ void __launch_bounds__(kWsThreads) conv3x3_umma_ws_kernel(UmmaConvArg
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
   }
   for (int i = tid; i < NC; i += (int)blockDim.x) s_bias[i] = a.bias ? a.bias[i] : 0.f;
-  // weights, once, by every thread
+  if constexpr (kF8) {
+    for (int i = tid; i < NC; i += (int)blockDim.x) s_wsc[i] = a.wscale[i];
+    for (int i = tid; i < 256; i += (int)blockDim.x) s_inv[i] = i < cin ? a.inv_xscale[i] : 0.f;
+  }
+  // weights, once, by every thread: [tap][plane][n][16 bytes]
   for (int i = tid; i < NC * 9 * planes; i += (int)blockDim.x) {
     const int co = i % NC, r = i / NC;
     const int p = r % planes, tap = r / planes;
-    umma::cp16(wbase + ((tap * planes + p) * NC + co) * 16, a.w + ((size_t)co * 9 + tap) * cin + p * 8, true);
+    if constexpr (kF8) {  // e4m3, zeros for the padding channels
+      const bool ok = p * 16 < cin;
+      umma::cp16(wbase + ((tap * planes + p) * NC + co) * 16, ok ? a.w8 + ((size_t)co * 9 + tap) * cin + p * 16 : a.w8,
+                 ok);
+    } else {
+      umma::cp16(wbase + ((tap * planes + p) * NC + co) * 16, a.w + ((size_t)co * 9 + tap) * cin + p * 8, true);
+    }
   }
   asm volatile("cp.async.commit_group;\n" ::);
   asm volatile("cp.async.wait_group 0;\n" ::);
@@ -590,13 +648,14 @@ __global__ void __launch_bounds__(kWsThreads) conv3x3_umma_ws_kernel(UmmaConvArg
       int img, x0, y0;
       tile_origin(t, img, x0, y0);
       if (lane == 0) {
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb(st)),
+        const uint32_t bar = kF8 ? tmb(st) : fb(st);  // FP8: the quantising warp waits for the load
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar),
                      "r"((uint32_t)(x1_planes * kPlaneBytes))
                      : "memory");
         asm volatile(
             "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
             "%5, %6}], [%7];\n" ::"r"(hb),
-            "l"(reinterpret_cast<uint64_t>(&x1map)), "r"(0), "r"(x0 - 1), "r"(y0 - 1), "r"(0), "r"(img), "r"(fb(st))
+            "l"(reinterpret_cast<uint64_t>(&x1map)), "r"(0), "r"(x0 - 1), "r"(y0 - 1), "r"(0), "r"(img), "r"(bar)
             : "memory");
       }
     }
@@ -615,7 +674,7 @@ __global__ void __launch_bounds__(kWsThreads) conv3x3_umma_ws_kernel(UmmaConvArg
       int img, x0, y0;
       tile_origin(t, img, x0, y0);
       {
-        for (int q = lane + x1_planes * kHaloPx; q < kHaloPx * planes; q += 32) {
+        for (int q = lane + x1_planes * kHaloPx; q < kHaloPx * in_planes; q += 32) {
           const int hp = q % kHaloPx, p = q / kHaloPx;
           const int yy = y0 - 1 + hp / kHaloW, xx = x0 - 1 + hp % kHaloW;
           const int ci = p * 8;
@@ -630,6 +689,37 @@ __global__ void __launch_bounds__(kWsThreads) conv3x3_umma_ws_kernel(UmmaConvArg
         // this lane's copies landed and made visible to the tensor cores, then one arrival
         asm volatile("cp.async.commit_group;\n" ::);
         asm volatile("cp.async.wait_group 0;\n" ::);
+        if constexpr (kF8) {
+          // every BF16 plane in place (the TMA's and the warp's copies), then
+          // each 16-channel pair quantised into e4m3 plane p at the offset of
+          // BF16 plane p: a lane rewrites only its own pixels, and plane p's
+          // BF16 source planes 2p, 2p + 1 are not yet overwritten
+          if (x1_planes && !wait(tmb(st), (uint32_t)(k & 1))) break;
+          __syncwarp();
+          for (int p = 0; p < planes; ++p) {
+            const float* sc = s_inv + p * 16;
+            const bool lo_in = 2 * p < in_planes, hi_in = 2 * p + 1 < in_planes;  // else padding channels
+            for (int hp = lane; hp < kHaloPx; hp += 32) {
+              uint4 lo = make_uint4(0u, 0u, 0u, 0u), hi = lo;
+              const uint32_t src = hb + (2 * p) * kPlaneBytes + hp * 16;
+              if (lo_in)
+                asm volatile("ld.shared.v4.b32 {%0, %1, %2, %3}, [%4];\n"
+                             : "=r"(lo.x), "=r"(lo.y), "=r"(lo.z), "=r"(lo.w)
+                             : "r"(src)
+                             : "memory");
+              if (hi_in)
+                asm volatile("ld.shared.v4.b32 {%0, %1, %2, %3}, [%4];\n"
+                             : "=r"(hi.x), "=r"(hi.y), "=r"(hi.z), "=r"(hi.w)
+                             : "r"(src + kPlaneBytes)
+                             : "memory");
+              const uint32_t o0 = quant4_e4m3(lo.x, lo.y, sc), o1 = quant4_e4m3(lo.z, lo.w, sc + 4);
+              const uint32_t o2 = quant4_e4m3(hi.x, hi.y, sc + 8), o3 = quant4_e4m3(hi.z, hi.w, sc + 12);
+              asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};\n" ::"r"(hb + p * kPlaneBytes + hp * 16),
+                           "r"(o0), "r"(o1), "r"(o2), "r"(o3)
+                           : "memory");
+            }
+          }
+        }
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         mbar_arrive(fb(st));
       }
@@ -638,7 +728,7 @@ __global__ void __launch_bounds__(kWsThreads) conv3x3_umma_ws_kernel(UmmaConvArg
   } else if (warp == 1) {
     // ---- MMA issue (one lane)
     if (lane == 0) {
-      constexpr uint32_t idesc = umma::idesc_bf16(NC);
+      constexpr uint32_t idesc = kF8 ? umma::idesc_e4m3(NC) : umma::idesc_bf16(NC);
       int i = 0;
       for (int t = blockIdx.x; t < total_tiles && !abort_flag; t += gridDim.x, ++i) {
         const int st = i % stages, k = i / stages, b = i & 1, kb = i >> 1;
@@ -653,11 +743,18 @@ __global__ void __launch_bounds__(kWsThreads) conv3x3_umma_ws_kernel(UmmaConvArg
                                             kHaloW * 16);
             const uint64_t db = umma::sdesc(wbase + ((tap * planes + 2 * ks) * NC) * 16, NC * 16, 8 * 16);
             const uint32_t acc = (tap > 0 || ks > 0) ? 1u : 0u;
-            asm volatile(
-                "{\n\t.reg .pred p;\n\t"
-                "setp.ne.b32 p, %4, 0;\n\t"
-                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
-                "l"(da), "l"(db), "r"(idesc), "r"(acc));
+            if constexpr (kF8)
+              asm volatile(
+                  "{\n\t.reg .pred p;\n\t"
+                  "setp.ne.b32 p, %4, 0;\n\t"
+                  "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+                  "l"(da), "l"(db), "r"(idesc), "r"(acc));
+            else
+              asm volatile(
+                  "{\n\t.reg .pred p;\n\t"
+                  "setp.ne.b32 p, %4, 0;\n\t"
+                  "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+                  "l"(da), "l"(db), "r"(idesc), "r"(acc));
           }
         }
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(eb(st))
@@ -712,6 +809,11 @@ __global__ void __launch_bounds__(kWsThreads) conv3x3_umma_ws_kernel(UmmaConvArg
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
             float f0 = __uint_as_float(v[2 * j]), f1 = __uint_as_float(v[2 * j + 1]);
+            if constexpr (kF8) {
+              const float2 sw = *reinterpret_cast<const float2*>(&s_wsc[c0 + 2 * j]);
+              f0 *= sw.x;
+              f1 *= sw.y;
+            }
             if (a.bias) {
               const float2 bb = *reinterpret_cast<const float2*>(&s_bias[c0 + 2 * j]);
               f0 += bb.x;
@@ -850,21 +952,33 @@ size_t ws_smem(int cin, int nc, int stages) {
   return (size_t)9 * cin * nc * 2 + 1024 + stages * halo + 1024;
 }
 constexpr size_t kWsSmemMax = 200 * 1024;
+// the FP8 form (at most 3 KB of static shared memory): up to the 227 KB a CTA may hold
+constexpr size_t kWsSmemMaxF8 = 220 * 1024;
 
-template <int NC> int launch_umma_ws(const UmmaConvArgs& a, cudaStream_t s, bool use_tma_flag) {
+// The FP8 form holds e4m3 planes of 16 channels, the input padded to a
+// multiple of 32: the shared memory of the BF16 form at half the (padded)
+// channel count.
+size_t ws_smem_f8(int cin, int nc, int stages) {
+  const size_t halo = ((size_t)cin * 360 + 1023) & ~(size_t)1023;  // BF16 planes, quantised in place
+  return (size_t)9 * ((cin + 31) & ~31) * nc + 1024 + stages * halo + 1024;
+}
+
+template <int NC, bool kF8> int launch_umma_ws(const UmmaConvArgs& a, cudaStream_t s, bool use_tma_flag) {
   const int cin = a.c1 + a.c2;
+  auto smem_for = [&](int st) { return kF8 ? ws_smem_f8(cin, NC, st) : ws_smem(cin, NC, st); };
   // input stages in flight (PBRT_WS_STAGES, 2..6, default 4; fewer stages, more resident CTAs)
   static const int max_stages = [] {
     const char* e = std::getenv("PBRT_WS_STAGES");
     return e ? std::min(6, std::max(2, std::atoi(e))) : 4;  // 4 measured best at 1080p (3 and 6 slower)
   }();
   int stages = max_stages;
-  while (stages > 2 && ws_smem(cin, NC, stages) > kWsSmemMax) --stages;
-  const size_t smem = ws_smem(cin, NC, stages);
+  const size_t smem_max = kF8 ? kWsSmemMaxF8 : kWsSmemMax;
+  while (stages > 2 && smem_for(stages) > smem_max) --stages;
+  const size_t smem = smem_for(stages);
   static bool attr_set = false;
   if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(conv3x3_umma_ws_kernel<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)kWsSmemMax);
+    cudaError_t e = cudaFuncSetAttribute(conv3x3_umma_ws_kernel<NC, kF8>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(conv3x3_umma_ws_kernel)");
     attr_set = true;
   }
@@ -875,13 +989,25 @@ template <int NC> int launch_umma_ws(const UmmaConvArgs& a, cudaStream_t s, bool
   CUtensorMap map;
   memset(&map, 0, sizeof(map));
   const int use_tma = use_tma_flag && make_x1_map(&map, a.x1, a.N, a.H, a.W, a.c1) ? 1 : 0;
-  // the gather warps only when some planes are not loaded by the TMA
-  const bool gather = !use_tma || a.c2 > 0;
+  // the gather warps only when some planes are not loaded by the TMA (FP8: always, they quantise)
+  const bool gather = kF8 || !use_tma || a.c2 > 0;
   const int threads = gather ? kWsThreads : kWsThreads - 32 * kWsGatherWarps;
-  const int per_sm = std::max(1, std::min({4, (int)((227 * 1024) / smem), 512 / kCols, 65536 / (threads * 80)}));
+  int per_sm = std::max(1, std::min({4, (int)((227 * 1024) / smem), 512 / kCols, 65536 / (threads * 80)}));
+  if (kF8) {  // resident CTAs from the kernel's registers (warp granules of 256) and shared memory
+    cudaFuncAttributes fa;
+    int fit = 1;
+    if (cudaFuncGetAttributes(&fa, conv3x3_umma_ws_kernel<NC, kF8>) == cudaSuccess && fa.numRegs > 0) {
+      const int regs_cta = (threads / 32) * ((fa.numRegs * 32 + 255) / 256 * 256);
+      const size_t smem_cta = smem + fa.sharedSizeBytes + 1024;  // + the system's reservation per CTA
+      fit = std::min(65536 / regs_cta, (int)((228 * 1024) / smem_cta));
+    } else {
+      cudaGetLastError();
+    }
+    per_sm = std::max(1, std::min({4, fit, 512 / kCols}));
+  }
   const int tiles_per_image = ((a.W + umma::kTileW - 1) / umma::kTileW) * ((a.H + umma::kTileH - 1) / umma::kTileH);
   const int grid = std::min(tiles_per_image * a.N, sms * per_sm);
-  conv3x3_umma_ws_kernel<NC><<<grid, threads, smem, s>>>(a, tiles_per_image, map, use_tma, stages);
+  conv3x3_umma_ws_kernel<NC, kF8><<<grid, threads, smem, s>>>(a, tiles_per_image, map, use_tma, stages);
   return PBRT_OK;
 }
 
@@ -926,14 +1052,14 @@ PBRT_API int pbrt_nn_conv3x3_umma(const void* x1, int32_t c1, const void* x2, in
   // warp-specialised form (the upsampled second input comes from its gather warps)
   if (!(flags & 10) && ws_smem(c1 + c2, cout, 2) <= kWsSmemMax) {
     switch (cout) {
-      case 16: st = launch_umma_ws<16>(a, stream, !(flags & 4)); break;
-      case 32: st = launch_umma_ws<32>(a, stream, !(flags & 4)); break;
-      case 48: st = launch_umma_ws<48>(a, stream, !(flags & 4)); break;
-      case 64: st = launch_umma_ws<64>(a, stream, !(flags & 4)); break;
-      case 80: st = launch_umma_ws<80>(a, stream, !(flags & 4)); break;
-      case 96: st = launch_umma_ws<96>(a, stream, !(flags & 4)); break;
-      case 112: st = launch_umma_ws<112>(a, stream, !(flags & 4)); break;
-      default: st = launch_umma_ws<128>(a, stream, !(flags & 4)); break;
+      case 16: st = launch_umma_ws<16, false>(a, stream, !(flags & 4)); break;
+      case 32: st = launch_umma_ws<32, false>(a, stream, !(flags & 4)); break;
+      case 48: st = launch_umma_ws<48, false>(a, stream, !(flags & 4)); break;
+      case 64: st = launch_umma_ws<64, false>(a, stream, !(flags & 4)); break;
+      case 80: st = launch_umma_ws<80, false>(a, stream, !(flags & 4)); break;
+      case 96: st = launch_umma_ws<96, false>(a, stream, !(flags & 4)); break;
+      case 112: st = launch_umma_ws<112, false>(a, stream, !(flags & 4)); break;
+      default: st = launch_umma_ws<128, false>(a, stream, !(flags & 4)); break;
     }
     if (st) return st;
     return check_launch("conv3x3_umma_ws_kernel");
@@ -983,17 +1109,55 @@ PBRT_API int pbrt_nn_conv3x3_umma_pooled(const void* x1, int32_t c1, const void*
   a.pooled = (bf16*)pooled;
   int st;
   switch (cout) {
-    case 16: st = launch_umma_ws<16>(a, stream, true); break;
-    case 32: st = launch_umma_ws<32>(a, stream, true); break;
-    case 48: st = launch_umma_ws<48>(a, stream, true); break;
-    case 64: st = launch_umma_ws<64>(a, stream, true); break;
-    case 80: st = launch_umma_ws<80>(a, stream, true); break;
-    case 96: st = launch_umma_ws<96>(a, stream, true); break;
-    case 112: st = launch_umma_ws<112>(a, stream, true); break;
-    default: st = launch_umma_ws<128>(a, stream, true); break;
+    case 16: st = launch_umma_ws<16, false>(a, stream, true); break;
+    case 32: st = launch_umma_ws<32, false>(a, stream, true); break;
+    case 48: st = launch_umma_ws<48, false>(a, stream, true); break;
+    case 64: st = launch_umma_ws<64, false>(a, stream, true); break;
+    case 80: st = launch_umma_ws<80, false>(a, stream, true); break;
+    case 96: st = launch_umma_ws<96, false>(a, stream, true); break;
+    case 112: st = launch_umma_ws<112, false>(a, stream, true); break;
+    default: st = launch_umma_ws<128, false>(a, stream, true); break;
   }
   if (st) return st;
   return check_launch("conv3x3_umma_ws_kernel (pooled)");
+}
+
+// FP8 (e4m3) convolution on the tensor cores (kind::f8f6f4): the arguments
+// and quantisation of pbrt_nn_conv3x3_fp8, plus the optional fused 2x2
+// pooling of pbrt_nn_conv3x3_umma_pooled (single input only).
+// PBRT_ERROR_UNSUPPORTED when the weights and two input stages do not fit
+// in shared memory, an operand is not 16-byte aligned, or (pooled) the
+// frame does not divide into 16 x 8 tiles.
+PBRT_API int pbrt_nn_conv3x3_fp8_umma(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* w8,
+                                      const float* wscale, const float* inv_xscale, const float* bias, void* y,
+                                      void* pooled, int32_t n, int32_t h, int32_t wd, int32_t cout, int32_t flags,
+                                      pbrt_stream_t stream) {
+  if (!x1 || !w8 || !wscale || !inv_xscale || !y || c1 <= 0 || c1 % 16 || c2 < 0 || c2 % 16 || (c2 && !x2) ||
+      c1 + c2 > 256 || cout < 16 || cout > 128 || cout % 16 || n <= 0 || h <= 0 || wd <= 0 ||
+      (c2 && (h % 2 || wd % 2)) || (pooled && c2))
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "nn conv3x3 fp8 umma: bad arguments (c1 %d, c2 %d, cout %d)", c1, c2,
+                cout);
+  if (ws_smem_f8(c1 + c2, cout, 2) > kWsSmemMaxF8 || ((uintptr_t)x1 & 15) || ((uintptr_t)x2 & 15) ||
+      ((uintptr_t)w8 & 15) || (pooled && (h % umma::kTileH || wd % umma::kTileW)))
+    return fail(PBRT_ERROR_UNSUPPORTED, "nn conv3x3 fp8 umma: %dx%d, c1 %d, c2 %d, cout %d", wd, h, c1, c2, cout);
+  UmmaConvArgs a{(const bf16*)x1, (const bf16*)x2, c1, c2, nullptr, bias, (bf16*)y, n, h, wd, cout, flags};
+  a.pooled = (bf16*)pooled;
+  a.w8 = (const uint8_t*)w8;
+  a.wscale = wscale;
+  a.inv_xscale = inv_xscale;
+  int st;
+  switch (cout) {
+    case 16: st = launch_umma_ws<16, true>(a, stream, true); break;
+    case 32: st = launch_umma_ws<32, true>(a, stream, true); break;
+    case 48: st = launch_umma_ws<48, true>(a, stream, true); break;
+    case 64: st = launch_umma_ws<64, true>(a, stream, true); break;
+    case 80: st = launch_umma_ws<80, true>(a, stream, true); break;
+    case 96: st = launch_umma_ws<96, true>(a, stream, true); break;
+    case 112: st = launch_umma_ws<112, true>(a, stream, true); break;
+    default: st = launch_umma_ws<128, true>(a, stream, true); break;
+  }
+  if (st) return st;
+  return check_launch("conv3x3_umma_ws_kernel (fp8)");
 }
 
 // Error flags of the tcgen05 kernels since the last call (bit 0: an

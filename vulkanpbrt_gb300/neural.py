@@ -98,7 +98,8 @@ class NeuralDenoiser(Handle):
         check(lib().pbrt_neural_calibrate(self.ptr, stream_handle(stream)))
 
     def set_precision(self, bits: int) -> None:
-        """16: BF16 convolutions; 8: FP8 e4m3 (after calibrate)."""
+        """16: BF16 convolutions; 8: FP8 e4m3 for every convolution but the 16-channel input one (after
+        calibrate)."""
         check(lib().pbrt_neural_set_precision(self.ptr, bits))
 
     def autotune(self, stream=None) -> list:

@@ -19,6 +19,7 @@ _abi.add_signatures({
     "pbrt_nn_channel_amax": (i32, [H, i64, i32, H, H]),
     "pbrt_nn_conv3x3_umma": (i32, [H, i32, H, i32, H, H, H, i32, i32, i32, i32, i32, H]),
     "pbrt_nn_conv3x3_umma_pooled": (i32, [H, i32, H, H, H, H, i32, i32, i32, i32, i32, H]),
+    "pbrt_nn_conv3x3_fp8_umma": (i32, [H, i32, H, i32, H, H, H, H, H, H, i32, i32, i32, i32, i32, H]),
     "pbrt_nn_umma_status": (i32, [H, C.POINTER(C.c_uint32)]),
     "pbrt_nn_flip_weights": (i32, [H, H, i32, i32, H]),
     "pbrt_nn_features": (i32, [H, i32, H, H, H, H, i32, i32, i32, i32, i32, H, H, H]),
@@ -68,9 +69,13 @@ def conv3x3(x1, w, bias=None, x2=None, relu=False, out=None, out32=None, accumul
     return out if store_bf16 else None
 
 
-def conv3x3_fp8(x1, w8, wscale, inv_xscale, bias=None, x2=None, relu=False, out=None):
+def conv3x3_fp8(x1, w8, wscale, inv_xscale, bias=None, x2=None, relu=False, out=None, kernel="auto",
+                pooled=False):
     """FP8 (e4m3) forward: w8 [Cout, 9, Cin] uint8 e4m3 with per-output-channel scales wscale [Cout] (activation
-    scales folded in), inv_xscale [Cin] quantises the BF16 input on load. Returns BF16 [N,H,W,Cout]."""
+    scales folded in), inv_xscale [Cin] quantises the BF16 input on load. Returns BF16 [N,H,W,Cout].
+    kernel: "auto" (tcgen05 where it applies), "mma" (the mma.sync kernel) or "umma" (tcgen05 only: raises
+    PbrtError where it does not apply). pooled=True (tcgen05, single input) also returns the 2x2 average
+    pooling of the output, from the epilogue."""
     import torch
 
     n, h, wd, c1 = x1.shape
@@ -78,8 +83,15 @@ def conv3x3_fp8(x1, w8, wscale, inv_xscale, bias=None, x2=None, relu=False, out=
     cout = w8.shape[0]
     if out is None:
         out = torch.empty((n, h, wd, cout), dtype=torch.bfloat16, device=x1.device)
+    flags = RELU if relu else 0
+    if kernel == "umma" or pooled:
+        pool = torch.empty((n, h // 2, wd // 2, cout), dtype=torch.bfloat16, device=x1.device) if pooled else None
+        check(lib().pbrt_nn_conv3x3_fp8_umma(_ptr(x1), c1, _ptr(x2), c2, _ptr(w8), _ptr(wscale), _ptr(inv_xscale),
+                                             _ptr(bias), _ptr(out), _ptr(pool), n, h, wd, cout, flags, _stream()))
+        return (out, pool) if pooled else out
+    flags |= 8 if kernel == "mma" else 0
     check(lib().pbrt_nn_conv3x3_fp8(_ptr(x1), c1, _ptr(x2), c2, _ptr(w8), _ptr(wscale), _ptr(inv_xscale), _ptr(bias),
-                                    _ptr(out), n, h, wd, cout, RELU if relu else 0, _stream()))
+                                    _ptr(out), n, h, wd, cout, flags, _stream()))
     return out
 
 
