@@ -89,6 +89,19 @@ def test_conv3x3_fp8_umma(cuda, n, h, w, c1, c2, cout):
     assert d <= 8e-3 * ref.abs().max().item()
 
 
+def test_conv3x3_fp8_umma_full_frame(cuda):
+    """The decoder's full-resolution concatenated layer (32 + 48 -> 32) at
+    1088x1920: the FP8 form with two stages and two CTAs an SM."""
+    import torch
+
+    from vulkanpbrt_gb300 import nn
+
+    args, ref = _fp8_case(1, 1088, 1920, 32, 48, 32)
+    y = nn.conv3x3_fp8(**args, kernel="umma")
+    assert nn.umma_status() == 0
+    _check(y, ref, "umma full frame")
+
+
 def test_conv3x3_fp8_umma_pooled(cuda):
     import torch
 

@@ -37,6 +37,29 @@ def test_conv3x3_umma_forward(cuda, n, h, w, c1, c2, cout, mode):
     assert _close(yr, ref.clamp_min(0), 4e-3)[1]
 
 
+@pytest.mark.parametrize("c1,c2", [(32, 48), (32, 0)])
+def test_conv3x3_umma_full_frame(cuda, c1, c2):
+    """The full-resolution decoder / encoder shapes at 1088x1920, where the
+    warp-specialised form trades stages for resident CTAs (two stages: two
+    CTAs an SM with the upsampled input, four without)."""
+    import torch
+
+    from tests.test_nn_conv_gpu import _close, _ref_conv
+    from vulkanpbrt_gb300 import nn
+
+    g = torch.Generator(device=cuda).manual_seed(c1 + c2)
+    h, w, cout = 1088, 1920, 32
+    x1 = torch.randn(1, h, w, c1, device=cuda, generator=g).bfloat16()
+    x2 = torch.randn(1, h // 2, w // 2, c2, device=cuda, generator=g).bfloat16() if c2 else None
+    wt = (torch.randn(cout, 9, c1 + c2, device=cuda, generator=g) * 0.1).bfloat16()
+    b = torch.randn(cout, device=cuda, generator=g)
+    y = nn.conv3x3_umma(x1, wt, b, x2=x2)
+    assert nn.umma_status() == 0
+    rel, ok = _close(y, _ref_conv(x1, wt, b, x2), 4e-3)
+    print(f"full-frame umma conv rel err {rel:.2e}")
+    assert ok
+
+
 @pytest.mark.parametrize("n,h,w,c1,cout", [(1, 32, 48, 16, 32), (2, 64, 40, 32, 48), (1, 48, 64, 48, 64),
                                           (1, 272, 480, 48, 64)])
 def test_conv3x3_umma_pooled(cuda, n, h, w, c1, cout):

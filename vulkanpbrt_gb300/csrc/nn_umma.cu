@@ -966,15 +966,17 @@ size_t ws_smem_f8(int cin, int nc, int stages) {
 template <int NC, bool kF8> int launch_umma_ws(const UmmaConvArgs& a, cudaStream_t s, bool use_tma_flag) {
   const int cin = a.c1 + a.c2;
   auto smem_for = [&](int st) { return kF8 ? ws_smem_f8(cin, NC, st) : ws_smem(cin, NC, st); };
-  // input stages in flight (PBRT_WS_STAGES, 2..6, default 4; fewer stages, more resident CTAs)
-  static const int max_stages = [] {
+  // input stages in flight: PBRT_WS_STAGES (2..6) fixes the count; by
+  // default the count of 2..4 with the most resident CTAs, the deeper ring
+  // among equals, and a shallower one only while every CTA still walks 16
+  // tiles or more (d0a, 80 channels at 1080p: two CTAs an SM with two
+  // stages, 245 us, against one with four, 302 us; e1a, 4080 tiles: four
+  // stages and two CTAs, 36 us, against two and four, 42 us)
+  static const int env_stages = [] {
     const char* e = std::getenv("PBRT_WS_STAGES");
-    return e ? std::min(6, std::max(2, std::atoi(e))) : 4;  // 4 measured best at 1080p (3 and 6 slower)
+    return e ? std::min(6, std::max(2, std::atoi(e))) : 0;
   }();
-  int stages = max_stages;
   const size_t smem_max = kF8 ? kWsSmemMaxF8 : kWsSmemMax;
-  while (stages > 2 && smem_for(stages) > smem_max) --stages;
-  const size_t smem = smem_for(stages);
   static bool attr_set = false;
   if (!attr_set) {
     cudaError_t e = cudaFuncSetAttribute(conv3x3_umma_ws_kernel<NC, kF8>,
@@ -992,21 +994,38 @@ template <int NC, bool kF8> int launch_umma_ws(const UmmaConvArgs& a, cudaStream
   // the gather warps only when some planes are not loaded by the TMA (FP8: always, they quantise)
   const bool gather = kF8 || !use_tma || a.c2 > 0;
   const int threads = gather ? kWsThreads : kWsThreads - 32 * kWsGatherWarps;
-  int per_sm = std::max(1, std::min({4, (int)((227 * 1024) / smem), 512 / kCols, 65536 / (threads * 80)}));
-  if (kF8) {  // resident CTAs from the kernel's registers (warp granules of 256) and shared memory
+  // resident CTAs an SM at a given dynamic shared-memory size, from the
+  // kernel's registers (warp granules of 256), its static shared memory and
+  // the 1 KB the system reserves per CTA, within 228 KB an SM
+  int regs_cta = 0, static_smem = 0;
+  {
     cudaFuncAttributes fa;
-    int fit = 1;
     if (cudaFuncGetAttributes(&fa, conv3x3_umma_ws_kernel<NC, kF8>) == cudaSuccess && fa.numRegs > 0) {
-      const int regs_cta = (threads / 32) * ((fa.numRegs * 32 + 255) / 256 * 256);
-      const size_t smem_cta = smem + fa.sharedSizeBytes + 1024;  // + the system's reservation per CTA
-      fit = std::min(65536 / regs_cta, (int)((228 * 1024) / smem_cta));
+      regs_cta = (threads / 32) * ((fa.numRegs * 32 + 255) / 256 * 256);
+      static_smem = (int)fa.sharedSizeBytes;
     } else {
       cudaGetLastError();
     }
-    per_sm = std::max(1, std::min({4, fit, 512 / kCols}));
   }
+  auto resident = [&](size_t smem) {
+    const int fit = regs_cta ? std::min(65536 / regs_cta, (int)((228 * 1024) / (smem + static_smem + 1024))) : 1;
+    return std::max(1, std::min({4, fit, 512 / kCols}));
+  };
   const int tiles_per_image = ((a.W + umma::kTileW - 1) / umma::kTileW) * ((a.H + umma::kTileH - 1) / umma::kTileH);
-  const int grid = std::min(tiles_per_image * a.N, sms * per_sm);
+  const long total_tiles = (long)tiles_per_image * a.N;
+  int stages = env_stages ? env_stages : 4;
+  while (stages > 2 && smem_for(stages) > smem_max) --stages;
+  if (!env_stages) {
+    int best = stages, best_r = resident(smem_for(stages));
+    for (int st = stages - 1; st >= 2; --st) {
+      const int r = resident(smem_for(st));
+      if (r > best_r && total_tiles >= 16L * sms * r) best = st, best_r = r;
+    }
+    stages = best;
+  }
+  const size_t smem = smem_for(stages);
+  const int per_sm = resident(smem);
+  const int grid = (int)std::min(total_tiles, (long)sms * per_sm);
   conv3x3_umma_ws_kernel<NC, kF8><<<grid, threads, smem, s>>>(a, tiles_per_image, map, use_tma, stages);
   return PBRT_OK;
 }
