@@ -102,6 +102,29 @@ def test_conv3x3_fp8_umma_full_frame(cuda):
     _check(y, ref, "umma full frame")
 
 
+def test_conv3x3_fp8_fallback_records_no_error(cuda):
+    """A layer the tcgen05 form does not take (224 input channels) runs on
+    the mma.sync kernel without leaving an error message behind."""
+    import torch
+
+    import vulkanpbrt_gb300 as vp
+    from vulkanpbrt_gb300 import nn
+    from vulkanpbrt_gb300._abi import last_error
+
+    bad = torch.zeros(1, 4, 4, 8, dtype=torch.bfloat16, device=cuda)  # 8 channels: rejected
+    w8 = torch.zeros(16, 9, 8, dtype=torch.uint8, device=cuda)
+    one = torch.ones(16, device=cuda)
+    with pytest.raises(vp.PbrtError):
+        nn.conv3x3_fp8(bad, w8, one, one[:8])
+    msg = last_error()
+    assert "bad arguments" in msg
+    args, ref = _fp8_case(1, 20, 36, 96, 128, 96)
+    y = nn.conv3x3_fp8(**args)
+    torch.cuda.synchronize()
+    _check(y, ref, "auto (mma.sync)")
+    assert last_error() == msg
+
+
 def test_conv3x3_fp8_umma_pooled(cuda):
     import torch
 

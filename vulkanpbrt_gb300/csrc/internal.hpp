@@ -47,6 +47,14 @@ int cuda_fail(cudaError_t e, const char* what);
   } while (0)
 // Checks the launch just issued on this thread.
 int check_launch(const char* what);
+// Whether the FP8 tcgen05 convolution (pbrt_nn_conv3x3_fp8_umma) takes
+// these operands: shared memory for the weights and two input stages,
+// 16-byte alignment, and (pooled) a frame of whole 16 x 8 tiles.
+bool nn_fp8_umma_fits(const void* x1, int c1, const void* x2, int c2, const void* w8, int cout, int h, int w,
+                      bool pooled);
+// Whether pbrt_nn_conv3x3_umma_pooled takes this layer (whole 16 x 8 tiles,
+// the weights and two input stages in shared memory).
+bool nn_umma_pooled_fits(int c1, int cout, int h, int w);
 
 void retain(Object* o);
 void release(Object* o);

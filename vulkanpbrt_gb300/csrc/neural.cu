@@ -146,21 +146,22 @@ int record_forward(PbrtNeural* nd, cudaStream_t s) {
     const bf16* in2 = c.c2 ? x : nullptr;
     // an encoder level's second convolution on the tcgen05 kernel pools its
     // output in the epilogue (levels 0-2; the frame must divide into tiles)
-    const bool pool_here = i < 8 && (i & 1) && c.c2 == 0 && nd->conv_kernel[i] == 1 && nd->precision != 8;
+    const bool pool_here = i < 8 && (i & 1) && c.c2 == 0 && nd->conv_kernel[i] == 1 && nd->precision != 8 &&
+                           nn_umma_pooled_fits(c.c1, c.cout, h, w);
     // FP8 inference quantises every convolution but the first: its 16 input
     // channels pad to 32 in e4m3, the BF16 instruction count, so it stays BF16
     if (nd->precision == 8 && i > 0) {
       const uint8_t* w8 = nd->w8 + nd->lay.conv_w[i];
       const float* wsc = nd->wscale + nd->wsoff[i];
       const float* ixs = nd->inv_xscale + nd->xsoff[i];
-      st = PBRT_ERROR_UNSUPPORTED;
-      if (i < 8 && (i & 1) && c.c2 == 0) {  // the encoder's pooling in the FP8 convolution's epilogue
+      if (i < 8 && (i & 1) && c.c2 == 0 && nn_fp8_umma_fits(in1, c.c1, nullptr, 0, w8, c.cout, h, w, true)) {
+        // the encoder's pooling in the FP8 convolution's epilogue
         st = pbrt_nn_conv3x3_fp8_umma(in1, c.c1, nullptr, 0, w8, wsc, ixs, b, nd->act[i], nd->pool[c.level + 1], n, h,
                                       w, c.cout, 1, s);
         pooled = st == PBRT_OK;
-      }
-      if (st == PBRT_ERROR_UNSUPPORTED)
+      } else {
         st = pbrt_nn_conv3x3_fp8(in1, c.c1, in2, c.c2, w8, wsc, ixs, b, nd->act[i], n, h, w, c.cout, 1, s);
+      }
     } else if (pool_here && (st = pbrt_nn_conv3x3_umma_pooled(in1, c.c1, w16, b, nd->act[i], nd->pool[c.level + 1],
                                                               n, h, w, c.cout, 1, s)) != PBRT_ERROR_UNSUPPORTED) {
       pooled = st == PBRT_OK;

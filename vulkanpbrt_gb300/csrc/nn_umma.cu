@@ -1054,6 +1054,16 @@ template <int NC> int launch_umma_persistent(const UmmaConvArgs& a, cudaStream_t
 }
 }  // namespace
 
+bool pbrt::nn_fp8_umma_fits(const void* x1, int c1, const void* x2, int c2, const void* w8, int cout, int h, int w,
+                            bool pooled) {
+  return ws_smem_f8(c1 + c2, cout, 2) <= kWsSmemMaxF8 && !((uintptr_t)x1 & 15) && !((uintptr_t)x2 & 15) &&
+         !((uintptr_t)w8 & 15) && !(pooled && (h % umma::kTileH || w % umma::kTileW));
+}
+
+bool pbrt::nn_umma_pooled_fits(int c1, int cout, int h, int w) {
+  return h % umma::kTileH == 0 && w % umma::kTileW == 0 && ws_smem(c1, cout, 2) <= kWsSmemMax;
+}
+
 extern "C" {
 
 // tcgen05 forward convolution (BF16 output only): Cout in {16, 32, 48, 64,
@@ -1122,7 +1132,7 @@ PBRT_API int pbrt_nn_conv3x3_umma_pooled(const void* x1, int32_t c1, const void*
   if (!x1 || !w || !y || !pooled || c1 <= 0 || c1 % 16 || cout < 16 || cout > 128 || cout % 16 || n <= 0 || h <= 0 ||
       wd <= 0)
     return fail(PBRT_ERROR_INVALID_ARGUMENT, "nn conv3x3 umma pooled: bad arguments (c1 %d, cout %d)", c1, cout);
-  if (h % umma::kTileH || wd % umma::kTileW || ws_smem(c1, cout, 2) > kWsSmemMax)
+  if (!nn_umma_pooled_fits(c1, cout, h, wd))
     return fail(PBRT_ERROR_UNSUPPORTED, "nn conv3x3 umma pooled: %dx%d, c1 %d, cout %d", wd, h, c1, cout);
   UmmaConvArgs a{(const bf16*)x1, nullptr, c1, 0, (const bf16*)w, bias, (bf16*)y, n, h, wd, cout, flags};
   a.pooled = (bf16*)pooled;
@@ -1156,8 +1166,7 @@ PBRT_API int pbrt_nn_conv3x3_fp8_umma(const void* x1, int32_t c1, const void* x2
       (c2 && (h % 2 || wd % 2)) || (pooled && c2))
     return fail(PBRT_ERROR_INVALID_ARGUMENT, "nn conv3x3 fp8 umma: bad arguments (c1 %d, c2 %d, cout %d)", c1, c2,
                 cout);
-  if (ws_smem_f8(c1 + c2, cout, 2) > kWsSmemMaxF8 || ((uintptr_t)x1 & 15) || ((uintptr_t)x2 & 15) ||
-      ((uintptr_t)w8 & 15) || (pooled && (h % umma::kTileH || wd % umma::kTileW)))
+  if (!nn_fp8_umma_fits(x1, c1, x2, c2, w8, cout, h, wd, pooled != nullptr))
     return fail(PBRT_ERROR_UNSUPPORTED, "nn conv3x3 fp8 umma: %dx%d, c1 %d, c2 %d, cout %d", wd, h, c1, c2, cout);
   UmmaConvArgs a{(const bf16*)x1, (const bf16*)x2, c1, c2, nullptr, bias, (bf16*)y, n, h, wd, cout, flags};
   a.pooled = (bf16*)pooled;
