@@ -638,6 +638,7 @@ __global__ void __launch_bounds__(kWsThreads, kF8 ? 3 : 0) conv3x3_umma_ws_kerne
     return false;
   };
 
+  int tma_issued = 0;  // producer: TMA loads issued (the abort path waits for the last one per stage)
   if (warp == 0) {
     // ---- producer (TMA of the x1 planes)
     int i = 0;
@@ -658,6 +659,7 @@ __global__ void __launch_bounds__(kWsThreads, kF8 ? 3 : 0) conv3x3_umma_ws_kerne
             "l"(reinterpret_cast<uint64_t>(&x1map)), "r"(0), "r"(x0 - 1), "r"(y0 - 1), "r"(0), "r"(img), "r"(bar)
             : "memory");
       }
+      ++tma_issued;
     }
   } else if (warp >= 6) {
     // ---- gather (cp.async of the planes after the TMA's). Stage st belongs
@@ -877,6 +879,16 @@ __global__ void __launch_bounds__(kWsThreads, kF8 ? 3 : 0) conv3x3_umma_ws_kerne
     if (n_mine > 0 && warp == 1 && lane == 0) {  // the last tile's accumulator commit, bounded
       const int last = n_mine - 1;
       umma::mbar_wait(tfb(last & 1), (uint32_t)((last >> 1) & 1));
+    }
+    if (x1_planes && warp == 0 && lane == 0) {
+      // TMA loads still in flight land before the CTA's shared memory is
+      // released: the last load into each stage, bounded (FP8: the load's own
+      // barrier; BF16: the stage's full barrier, which with gather warps also
+      // waits for their arrivals and may give up at the bound)
+      for (int st = 0; st < stages && st < tma_issued; ++st) {
+        const int j = tma_issued - 1 - (tma_issued - 1 - st) % stages;  // last tile loaded into stage st
+        umma::mbar_wait(kF8 ? tmb(st) : fb(st), (uint32_t)((j / stages) & 1));
+      }
     }
     __syncthreads();
   }
