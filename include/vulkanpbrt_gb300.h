@@ -471,13 +471,6 @@ PBRT_API int pbrt_bfr_blender_final_image(const PbrtBFRBlender* blender, PbrtIma
  * stores clamp and round); same size. */
 PBRT_API int pbrt_format_convert(const PbrtImage* src, const PbrtImage* dst, pbrt_stream_t stream);
 
-/* ---- synthetic workloads (no reference counterpart) -------------------- */
-/* Procedural tileable value-noise RGBA8 texture: kind 0 albedo (sRGB-encoded
- * colour, optional alpha holes), 1 specular (colour + roughness in alpha),
- * 2 tangent-space normal map. out_rgba: size * size * 4 bytes of host memory. */
-PBRT_API int pbrt_synth_texture(uint64_t seed, uint32_t size, int32_t kind, const float* color, int32_t alpha_mask,
-                                float rough_lo, float rough_hi, uint8_t* out_rgba);
-
 /* ---- kernel-predicting denoiser operators (no reference counterpart) ----
  * Device pointers, NHWC layout, channel counts multiples of 16 for the
  * convolutions. BF16 activations and weights, FP32 accumulation, FP32

@@ -27,7 +27,6 @@ from .render_modules import (  # noqa: F401
 )
 
 from .pipeline import PBRTPipeline, SceneHandle  # noqa: F401,E402
-from . import texsynth  # noqa: F401,E402  (registers pbrt_synth_texture)
 from . import nn  # noqa: F401,E402  (registers the neural-denoiser operators)
 from .neural import NeuralDenoiser  # noqa: F401,E402
 from .batch import Batch  # noqa: F401,E402

@@ -25,7 +25,9 @@ ambient_roughness.w (or the specular map's alpha).
 """
 from __future__ import annotations
 
+import concurrent.futures
 import math
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -335,12 +337,21 @@ def instanced_field(seed: int = 0, instances: int = 2000, unique_meshes: int = 6
     sc = Scene(camera_eye=(0.0, -radius * 0.6, radius * 0.2), camera_center=(0.0, 0.0, 1.0))
     if synth is None:
         from .texsynth import synth_texture as synth
+    # textures are generated on a thread pool (numpy releases the GIL in its
+    # array passes); ids are assigned in submission order
+    pool = concurrent.futures.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1))
+    jobs = []
+    base = len(sc.textures)  # the 1x1 white default comes first
+
+    def texture(*args) -> int:
+        jobs.append(pool.submit(synth, *args))
+        return base + len(jobs) - 1
 
     def textures(mesh_seed: int, albedo, metal: bool, alpha: bool, rough_lo: float, rough_hi: float):
-        d = sc.add_texture(synth(mesh_seed, texture_size, "albedo", tuple(0 if metal else a for a in albedo), alpha))
-        s = sc.add_texture(synth(mesh_seed + 1, texture_size, "specular", tuple(albedo if metal else (0, 0, 0)), False,
-                                 rough_lo, rough_hi))
-        n = sc.add_texture(synth(mesh_seed + 2, texture_size, "normal", (0, 0, 0), False))
+        d = texture(mesh_seed, texture_size, "albedo", tuple(0 if metal else a for a in albedo), alpha)
+        s = texture(mesh_seed + 1, texture_size, "specular", tuple(albedo if metal else (0, 0, 0)), False,
+                    rough_lo, rough_hi)
+        n = texture(mesh_seed + 2, texture_size, "normal", (0, 0, 0), False)
         return [d, 0, n, 0, s]
 
     # ground plane (u32 indices: exercises the full-index path)
@@ -394,4 +405,8 @@ def instanced_field(seed: int = 0, instances: int = 2000, unique_meshes: int = 6
     sc.add_instance(lid, np.eye(4))
     sc.add_emissive_lights(lid, np.eye(4), e)
     sc.finalize_lights()
+    assert len(sc.textures) == base, "texture ids are assigned in submission order"
+    for j in jobs:
+        sc.add_texture(j.result())
+    pool.shutdown()
     return sc
