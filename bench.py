@@ -58,8 +58,16 @@ def parse():
     ap.add_argument("--weights", default=None, help="neural path: .npz of trained parameters (default: packaged)")
     ap.add_argument("--ref-spp", type=int, default=4096, help="samples of the relMSE reference render (0: skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="frame1080p", choices=["frame1080p", "batch64"],
-                    help="batch64: 64 uneven render requests in one graph launch (not the headline line)")
+    ap.add_argument("--sort-rays", action="store_true", help="sort extension / shadow rays before traversal")
+    ap.add_argument("--separate-shadow", action="store_true",
+                    help="trace shadow rays in their own launch (default: merged into the next bounce's launch)")
+    ap.add_argument("--workload", default="frame1080p", choices=["frame1080p", "batch64", "unet_layers"],
+                    help="batch64: 64 uneven render requests in one graph launch; unet_layers: per-convolution "
+                         "times of the U-Net (neither is the headline line)")
+    ap.add_argument("--layers", default="", help="unet_layers: comma-separated layer names (default: all 18)")
+    ap.add_argument("--kernels", default="bf16_tcgen05,bf16_mma,fp8_tcgen05,fp8_mma",
+                    help="unet_layers: comma-separated subset of bf16_tcgen05,bf16_mma,fp8_tcgen05,fp8_mma")
+    ap.add_argument("--reps", type=int, default=20, help="unet_layers: timed launches per layer and kernel")
     return ap.parse_args()
 
 
@@ -389,6 +397,7 @@ def run_gb300(args):
     g = vp.GBuffer(W, H)
     illu = vp.IlluminationBufferDemodulatedFloat(W, H)
     pipe = vp.PBRTPipeline(sh, g, illu, True, max_recursion_depth=args.max_depth, min_recursion_depth=args.min_depth)
+    pipe.set_schedule(sort_rays=args.sort_rays, merge_shadow=not args.separate_shadow)
     accu = vp.Accumulator(g, illu, separate_matrices=True)
     acc_illu = accu.accumulated_illumination
     abuf = accu.accumulation_buffer
@@ -581,6 +590,7 @@ def run_gb300(args):
                 "triangles": int(info.triangle_count), "instances": int(info.instance_count),
                 "lights": int(info.light_count), "texture_size": args.texture_size, "denoiser": args.denoiser,
                 "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}",
+                "schedule": {"sort_rays": bool(args.sort_rays), "merge_shadow": not args.separate_shadow},
             },
             "grays_per_s": rays / (trace_ms / 1e3) / 1e9 * world,
             "rays_per_frame": rays / steps,
@@ -694,11 +704,110 @@ def run_batch(args):
                        "denoiser": "accumulate + BMFR 32x32 per request"}}
     print(json.dumps(line), flush=True)
 
+UNET_KERNELS = ("bf16_tcgen05", "bf16_mma", "fp8_tcgen05", "fp8_mma")
+
+
+def _event_time_us(fn, reps):
+    import torch
+
+    for _ in range(3):
+        fn()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps * 1e3
+
+
+def unet_layer_times(width, height, reps, layers, kernels):
+    """Per-convolution device times of the kernel-predicting U-Net: each of its
+    18 3x3 convolutions (kpunet's layer table) timed alone with CUDA events on
+    random BF16 inputs at its level of the padded frame, on the BF16 tcgen05
+    kernels, the BF16 mma.sync kernel, the FP8 tcgen05 form and the FP8
+    mma.sync kernel. Returns [(name, c1, c2, cout, level, {kernel: us or None})]."""
+    import torch
+
+    from vulkanpbrt_gb300 import build as B
+
+    B.build()
+    from vulkanpbrt_gb300 import nn
+    from vulkanpbrt_gb300._abi import PbrtError
+    from vulkanpbrt_gb300.kpunet import CONVS
+
+    dev = torch.device("cuda:0")
+    g = torch.Generator(device=dev).manual_seed(0)
+    rows = []
+    for name, (c1, c2), cout, lvl in CONVS:
+        if layers and name not in layers:
+            continue
+        h, w = height >> lvl, width >> lvl
+        x1 = torch.rand(1, h, w, c1, device=dev, generator=g).bfloat16()
+        x2 = torch.rand(1, h // 2, w // 2, c2, device=dev, generator=g).bfloat16() if c2 else None
+        cin = c1 + c2
+        w32 = torch.randn(cout, 9, cin, device=dev, generator=g) * 0.05
+        wb = w32.bfloat16()
+        b = torch.zeros(cout, device=dev)
+        xs = torch.ones(cin, device=dev)
+        w8, ws = nn.quantize_weights_fp8(w32, xs)
+        out = torch.empty(1, h, w, cout, device=dev, dtype=torch.bfloat16)
+        run = {
+            "bf16_tcgen05": lambda: nn.conv3x3_umma(x1, wb, b, x2=x2, relu=True, out=out),
+            "bf16_mma": lambda: nn.conv3x3(x1, wb, b, x2=x2, relu=True, out=out),
+            "fp8_tcgen05": lambda: nn.conv3x3_fp8(x1, w8, ws, xs, b, x2=x2, relu=True, out=out, kernel="umma"),
+            "fp8_mma": lambda: nn.conv3x3_fp8(x1, w8, ws, xs, b, x2=x2, relu=True, out=out, kernel="mma"),
+        }
+        t = {}
+        for k in UNET_KERNELS:
+            if k not in kernels:
+                t[k] = None
+                continue
+            try:
+                t[k] = _event_time_us(run[k], reps)
+            except PbrtError:  # the FP8 tcgen05 form: weights and two input stages do not fit in shared memory
+                t[k] = None
+        rows.append((name, c1, c2, cout, lvl, t))
+    if nn.umma_status():
+        raise RuntimeError("a tcgen05 convolution reported a timed-out wait")
+    return rows
+
+
+def run_unet_layers(args):
+    """Markdown table of per-convolution times (microseconds per launch) at
+    --width x --height rounded up to the network's padded frame (multiples of
+    16). Inputs are larger than L2 for the full-resolution layers only, so the
+    deeper levels' times are L2-warm."""
+    layers = [x for x in args.layers.split(",") if x]
+    keys = [x for x in args.kernels.split(",") if x]
+    bad = [k for k in keys if k not in UNET_KERNELS]
+    if bad:
+        raise SystemExit(f"unknown kernels {bad}; choose from {','.join(UNET_KERNELS)}")
+    W, H = (args.width + 15) // 16 * 16, (args.height + 15) // 16 * 16
+    rows = unet_layer_times(W, H, args.reps, layers, keys)
+    print("| layer | c1+c2 -> cout | size | " + " | ".join(keys) + " |")
+    print("|---|---|---|" + "---|" * len(keys))
+    tot = {k: 0.0 for k in keys}
+    for name, c1, c2, cout, lvl, t in rows:
+        cells = []
+        for k in keys:
+            v = t[k]
+            cells.append("-" if v is None else f"{v:.1f}")
+            tot[k] += 0.0 if v is None else v
+        print(f"| {name} | {c1}+{c2} -> {cout} | {W >> lvl}x{H >> lvl} | " + " | ".join(cells) + " |")
+    print("| sum | | | " + " | ".join(f"{tot[k]:.1f}" for k in keys) + " |")
+    if "fp8_tcgen05" in keys and "fp8_mma" in keys:  # the FP8 path as dispatched: tcgen05 where it fits
+        fp8_net = sum((t["fp8_tcgen05"] if t["fp8_tcgen05"] is not None else t["fp8_mma"]) or 0.0 for *_, t in rows)
+        print(f"\nFP8 as dispatched (tcgen05 where it fits): {fp8_net:.1f} us")
+
 
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "unet_layers":
+        run_unet_layers(args)
     elif args.workload == "batch64":
         run_batch(args)
     else:

@@ -200,6 +200,14 @@ PBRT_API int pbrt_bmfr_images(const PbrtBMFR* b, PbrtImage* denoised, PbrtImage*
 /* Number of blocks re-solved in FP64 by the last dispatch (stream-ordered
  * read; synchronises the stream). */
 PBRT_API int pbrt_bmfr_fp64_block_count(PbrtBMFR* b, pbrt_stream_t stream, uint32_t* count);
+/* R-diagonal ratio above which a block is re-solved in FP64 (default 1e6;
+ * finite, >= 1). No reference counterpart. */
+PBRT_API int pbrt_bmfr_set_condition_limit(PbrtBMFR* b, float limit);
+/* Of the last dispatch with fp64_resolve on: the number of blocks re-solved
+ * in FP64 and the largest R-diagonal ratio max|R_ii| / min|R_ii| of any
+ * block's FP32 fit (infinite for a zero or NaN diagonal). Stream-ordered
+ * read; synchronises the stream. No reference counterpart. */
+PBRT_API int pbrt_bmfr_condition_stats(PbrtBMFR* b, pbrt_stream_t stream, uint32_t* flagged, float* max_ratio);
 
 /* BMFR for callers that cannot allocate device memory. No counterpart in the
  * reference. Hosts that own the device-memory budget (an engine or compositor
@@ -212,16 +220,22 @@ PBRT_API int pbrt_bmfr_fp64_block_count(PbrtBMFR* b, pbrt_stream_t stream, uint3
  * PBRT_BMFR_NOALLOC_MAX_BLOCKS x 30 floats (1.9 MiB), which every GPU that
  * loads the library holds until the process exits. Images whose block grid
  * ((width/b + 2) x (height/b + 2) for block size b) exceeds that maximum are
- * rejected with PBRT_ERROR_INVALID_ARGUMENT (1080p and 4K fit with 32x32 and
- * 16x16 blocks, 1080p does not with 8x8). The first call on a device looks up
- * that array's device address (cudaGetSymbolAddress) and sets the kernel's
- * shared-memory limit, so make that first call before any stream capture.
- * All calls share the one array: calls whose kernels can overlap on the GPU
- * (different streams, no ordering between them) race on it; order them on
- * one stream. Nothing in the array has to start at zero (each block writes
- * its weights before reading them). The FP64 re-solve is not available here.
+ * rejected with PBRT_ERROR_INVALID_ARGUMENT: 1080p fits with 16x16 and 32x32
+ * blocks (8,418 and 2,170 blocks), 4K (3840x2160) only with 32x32 blocks
+ * (8,418; at 16x16 it needs 33,154), and 1080p with 8x8 blocks (33,154) does
+ * not. The first call on a device (and the first after that device's
+ * context changes, e.g. after cudaDeviceReset) looks up that array's device
+ * address (cudaGetSymbolAddress) and sets the kernel's shared-memory limit,
+ * so make that first call before any stream capture. All calls share the one
+ * array: calls whose kernels can overlap on the GPU (different streams, no
+ * ordering between them) race on it; order them on one stream. Nothing in
+ * the array has to start at zero (each block writes its weights before
+ * reading them). The FP64 re-solve is not available here.
  * Images: width x height, rows packed; denoised holds 2 RGBA16F layers (layer
- * frame & 1 is read as the previous frame, layer (frame & 1) ^ 1 written). */
+ * frame & 1 is read as the previous frame, layer (frame & 1) ^ 1 written).
+ * Alignment (device addresses): noisy, denoised and normal 8 bytes; depth,
+ * motion, albedo and final_bgra 4 bytes; a misaligned pointer is rejected
+ * with PBRT_ERROR_INVALID_ARGUMENT. */
 #define PBRT_BMFR_NOALLOC_MAX_BLOCKS 16384
 typedef struct PbrtBmfrNoAllocImages {
   const float* depth;    /* R32F */
@@ -379,6 +393,14 @@ PBRT_API int pbrt_pipeline_profile(PbrtPipeline* p, const PbrtPushConstants* pc,
 /* Launch shape of the tracer: persistent traversal CTAs and shading CTAs per
  * SM (1..16 each; default 8 and 8). No reference counterpart. */
 PBRT_API int pbrt_pipeline_set_launch(PbrtPipeline* p, int32_t trace_blocks_per_sm, int32_t shade_blocks_per_sm);
+/* Frame schedule (no reference counterpart; the results are the same either
+ * way). sort_rays = 1: extension and shadow rays are reordered by direction
+ * octant and origin cell (a counting sort on the GPU) before they are
+ * traversed; its staging queues are allocated on first use. merge_shadow =
+ * 1 (default): bounce k's closest-hit rays and bounce k-1's shadow rays are
+ * traced in one launch; 0: one launch per queue. The frame graph is
+ * recaptured on the next trace after a change. */
+PBRT_API int pbrt_pipeline_set_schedule(PbrtPipeline* p, int32_t sort_rays, int32_t merge_shadow);
 
 /* ---- batched requests (no reference counterpart) -----------------------
  * Many independent renders in one CUDA graph launch: each request names its

@@ -1,0 +1,87 @@
+"""The small plain-method configuration as one chain, GPU against oracle:
+a Cornell-style box of 24 triangles with 8 icospheres of 1280 triangles and
+a 0.2 x 0.2 area light of radiance 20, 640x360, 1 spp, depth 4 without
+Russian roulette, four frames from a static camera traced, accumulated and
+denoised by BMFR with 32x32 blocks -- the reference's frame
+(source/VulkanPBRT.cpp:397-445: TraceRays, Accumulator, BMFR, copy to the
+back images), run through the render modules on the GPU and through the
+oracle's ptRaygen / accumulator.comp / bmfrPre-Fit-Post restatement on the
+CPU, each chain feeding its own outputs forward.
+
+Tolerances. Traced radiance agrees within 1e-4 on >= 99.8% of pixels per
+frame; the rest are paths that branched differently after a last-bit
+difference. Those pixels enter the accumulation and, through the per-block
+least-squares fit, move their whole block's denoised output slightly, so
+the chain's output is compared as an image: relMSE between the two
+denoised frames below 1e-4 (the denoiser's own error against a converged
+render is ~1e-2), >= 95% of pixels within 1e-3, the accumulated sample
+counts identical, and the final BGRA8 images within 2 LSB on >= 99% of
+pixels.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("position_type", [0, 2])
+def test_cornell_four_frame_chain_matches_oracle(cuda, oracle, position_type):
+    import torch
+
+    import vulkanpbrt_gb300 as vp
+    from vulkanpbrt_gb300 import scene as S
+    from vulkanpbrt_gb300.camera import Camera, col_major
+
+    W, H, depth = 640, 360, 4
+    sc = S.cornell_spheres(seed=2, spheres=8, subdiv=3)
+    assert sc.tri_count == 24 + 8 * 1280 + 2
+    cam = Camera(sc.camera_eye, sc.camera_center, aspect=W / H)
+    sh = vp.SceneHandle(sc)
+    g = vp.GBuffer(W, H)
+    illu = vp.IlluminationBufferDemodulatedFloat(W, H)
+    pipe = vp.PBRTPipeline(sh, g, illu, True, max_recursion_depth=depth, min_recursion_depth=depth)
+    accu = vp.Accumulator(g, illu, separate_matrices=True)
+    bm = vp.BMFR(W, H, 32, 32, g, accu.accumulated_illumination, accu.accumulation_buffer, 256,
+                 position_type=position_type)
+    os_ = oracle.OracleScene(sc)
+    iv, ip = col_major(cam.inv_view), col_major(cam.inv_proj)
+    prev_origin = np.linalg.inv(cam.view.astype(np.float64))[:3, 3].tolist() + [1.0]
+    prev_depth = np.zeros((H, W), np.float32)
+    prev_spp = np.zeros((H, W), np.uint8)
+    prev_out = np.zeros((H, W, 4), np.float16)
+    den_ref = np.zeros((2, H, W, 4), np.float16)
+    cm = vp.CameraMatrices(cam.view, cam.inv_view, cam.proj, cam.inv_proj)
+    for f in range(4):
+        pc = vp.PushConstants(view_inverse=cam.inv_view, proj_inverse=cam.inv_proj, prev_view=cam.view, frame_number=f)
+        accu.set_camera_matrices(f, cm, vp.CameraMatrices(cam.view, cam.inv_view))
+        pipe.trace(pc)
+        vp.lib().pbrt_accumulator_dispatch(accu.ptr, None)
+        bm.dispatch(pc)
+        vp.lib().pbrt_accumulation_buffer_copy_to_back_images(accu.accumulation_buffer.ptr, g.ptr,
+                                                              accu.accumulated_illumination.ptr, None)
+        torch.cuda.synchronize()
+        r = oracle.render(os_, W, H, iv, ip, frame=f, min_depth=depth, max_depth=depth)
+        motion, spp, acc_il = oracle.accumulate(f, 1, ip, iv, col_major(cam.view), prev_origin, r["illum"], r["depth"],
+                                                prev_depth, prev_spp, prev_out)
+        _, _, fin_ref = oracle.bmfr(32, 256, f, position_type, iv, ip, r["depth"], r["normal"], r["albedo"], acc_il,
+                                    motion, spp, den_ref)
+        prev_depth, prev_spp, prev_out = r["depth"], spp, acc_il
+
+        il = illu.illumination_images[0].tensor().cpu().numpy()[..., :3].astype(np.float64)
+        ri = r["illum"][..., :3].astype(np.float64)
+        traced_ok = (np.abs(il - ri) <= 1e-4 * np.maximum(np.abs(il), np.abs(ri)) + 1e-6).all(-1).mean()
+        spp_gpu = accu.accumulation_buffer.spp.tensor().cpu().numpy()[..., 0]
+        den = bm.denoised.tensor().cpu().numpy()[(f & 1) ^ 1][..., :3].astype(np.float64)
+        dr = den_ref[(f & 1) ^ 1][..., :3].astype(np.float64)
+        rel = float((((den - dr) ** 2) / (dr * dr + 0.01)).mean())
+        close = (np.abs(den - dr) <= 1e-3 * np.maximum(np.abs(den), np.abs(dr)) + 1e-4).all(-1).mean()
+        fin = bm.get_final_descriptor_image().tensor().cpu().numpy().astype(int)
+        lsb = (np.abs(fin - fin_ref.astype(int)) <= 2).all(-1).mean()
+        print(f"pt={position_type} frame {f}: traced within 1e-4 {traced_ok * 100:.3f}%, spp equal "
+              f"{(spp_gpu == spp).mean() * 100:.3f}%, denoised relMSE(gpu, oracle) {rel:.3g}, within 1e-3 "
+              f"{close * 100:.2f}%, final within 2 LSB {lsb * 100:.3f}%")
+        assert traced_ok >= 0.998
+        assert (spp_gpu == spp).all()
+        assert rel < 1e-4
+        assert close >= 0.95
+        assert lsb >= 0.99

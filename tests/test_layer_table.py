@@ -1,7 +1,7 @@
 """The U-Net's layer table in Python (`kpunet.CONVS`, used by training and
-by the per-layer timing tool) against the native network's table
-(`kConvs` in csrc/neural.cu), and the timing tool's argument checks. CPU
-only."""
+by the benchmark's per-layer timing) against the native network's table
+(`kConvs` in csrc/neural.cu), and the timing workload's argument checks.
+CPU only."""
 import re
 from pathlib import Path
 
@@ -22,8 +22,12 @@ def test_python_layer_table_matches_native():
     assert native == [(name, c1, c2, cout, lvl) for name, (c1, c2), cout, lvl in CONVS]
 
 
-def test_layer_times_rejects_unknown_kernels():
-    from vulkanpbrt_gb300 import layer_times
+def test_unet_layer_workload_rejects_unknown_kernels(monkeypatch):
+    import sys
 
-    with pytest.raises(SystemExit):
-        layer_times.main(["--kernels", "bf16_tcgen05,int4"])
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--workload", "unet_layers", "--kernels", "bf16_tcgen05,int4"])
+    with pytest.raises(SystemExit, match="unknown kernels"):
+        bench.main()

@@ -18,16 +18,18 @@ from denoise_cases import close_fraction, get, inputs, put
 pytestmark = pytest.mark.gpu
 
 
-def _noalloc(vp, W, H, bw, s_dev, den, fin, pc):
+def _noalloc(vp, W, H, bw, s_dev, den, fin, pc, position_type=0):
     from vulkanpbrt_gb300._abi import PbrtBmfrNoAllocImages, check, lib
 
     im = PbrtBmfrNoAllocImages(*[t.data_ptr() for t in (s_dev["depth"], s_dev["normal"], s_dev["albedo"],
                                                         s_dev["noisy"], s_dev["motion"], s_dev["spp"], den, fin)])
-    check(lib().pbrt_bmfr_dispatch_noalloc(W, H, bw, 0, C.byref(im), C.byref(pc.value), None))
+    check(lib().pbrt_bmfr_dispatch_noalloc(W, H, bw, position_type, C.byref(im), C.byref(pc.value), None))
 
 
-@pytest.mark.parametrize("bw,fk", [(32, 256), (16, 256)])
-def test_noalloc_matches_allocating_bmfr_on_two_calls(cuda, bw, fk):
+# block size, fitting threads of the allocating BMFR, POSITION_TYPE (0: the
+# reference's default screen-space position feature; 1, 2: world-space forms)
+@pytest.mark.parametrize("bw,fk,ptype", [(32, 256, 0), (16, 256, 0), (8, 64, 0), (32, 256, 1), (32, 256, 2)])
+def test_noalloc_matches_allocating_bmfr_on_two_calls(cuda, bw, fk, ptype):
     import torch
 
     import vulkanpbrt_gb300 as vp
@@ -36,7 +38,7 @@ def test_noalloc_matches_allocating_bmfr_on_two_calls(cuda, bw, fk):
     g = vp.GBuffer(W, H)
     illu = vp.IlluminationBufferDemodulated(W, H)
     acc = vp.AccumulationBuffer(W, H)
-    ref = vp.BMFR(W, H, bw, bw, g, illu, acc, fk)
+    ref = vp.BMFR(W, H, bw, bw, g, illu, acc, fk, position_type=ptype)
     den = torch.zeros((2, H, W, 4), dtype=torch.float16, device=cuda)
     fin = torch.zeros((H, W, 4), dtype=torch.uint8, device=cuda)
     for frame in (0, 1):  # two calls in a row: the second reads the first's denoised layer
@@ -57,7 +59,7 @@ def test_noalloc_matches_allocating_bmfr_on_two_calls(cuda, bw, fk):
             "motion": torch.from_numpy(s["motion"]).to(cuda),
             "spp": torch.from_numpy(s["spp"]).to(cuda),
         }
-        _noalloc(vp, W, H, bw, s_dev, den, fin, pc)
+        _noalloc(vp, W, H, bw, s_dev, den, fin, pc, ptype)
         torch.cuda.synchronize()
         want_den = get(ref.denoised)
         want_fin = get(ref.get_final_descriptor_image())
@@ -80,3 +82,20 @@ def test_noalloc_rejects_grids_beyond_its_scratch(cuda):
     pc = vp.PushConstants()
     with pytest.raises(PbrtError, match="fixed maximum"):
         check(lib().pbrt_bmfr_dispatch_noalloc(W, H, 8, 0, C.byref(im), C.byref(pc.value), None))
+
+
+def test_noalloc_rejects_misaligned_images(cuda):
+    import torch
+
+    import vulkanpbrt_gb300 as vp
+    from vulkanpbrt_gb300._abi import PbrtBmfrNoAllocImages, PbrtError, check, lib
+
+    W, H = 320, 180
+    buf = torch.zeros(W * H * 16 + 64, dtype=torch.uint8, device=cuda)
+    p = buf.data_ptr()
+    pc = vp.PushConstants()
+    for field, off in (("noisy", 4), ("denoised", 2), ("normal", 4), ("depth", 2), ("final_bgra", 1)):
+        im = PbrtBmfrNoAllocImages(p, p, p, p, p, p, p, p)
+        setattr(im, field, p + off)
+        with pytest.raises(PbrtError, match=f"{field} pointer .* aligned"):
+            check(lib().pbrt_bmfr_dispatch_noalloc(W, H, 32, 0, C.byref(im), C.byref(pc.value), None))

@@ -114,6 +114,8 @@ _SIGS = {
     "pbrt_bmfr_final_image": (i32, [H, P(PbrtImage)]),
     "pbrt_bmfr_images": (i32, [H, P(PbrtImage), P(PbrtImage)]),
     "pbrt_bmfr_fp64_block_count": (i32, [H, H, P(u32)]),
+    "pbrt_bmfr_set_condition_limit": (i32, [H, C.c_float]),
+    "pbrt_bmfr_condition_stats": (i32, [H, H, P(u32), P(C.c_float)]),
     "pbrt_bmfr_dispatch_noalloc": (i32, [u32, u32, u32, i32, P(PbrtBmfrNoAllocImages), P(PbrtPushConstants), H]),
     "pbrt_bfr_create": (i32, [u32, u32, u32, u32, H, H, H, P(H)]),
     "pbrt_bfr_dispatch": (i32, [H, P(PbrtPushConstants), H]),

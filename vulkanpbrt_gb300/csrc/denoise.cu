@@ -9,6 +9,8 @@
 // arithmetic is restated operation by operation, and none of these kernels is
 // bound by FP32 issue, so contraction would only move results away from the
 // shader rounding.
+#include <cuda.h>
+
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -201,12 +203,13 @@ struct BmfrParams {
   uint32_t frame;
   int position_type;
   int fp64_resolve;
+  float cond_limit;  // R-diagonal ratio above which a block is re-solved in FP64
   const float* depth;
   const float2* normal;
   const Half4* noisy_f16;
   const float4* noisy_f32;
   float* weights;  // 30 layers x gh x gw
-  uint32_t* flagged;  // [0] = count, [1..] = block ids needing the FP64 re-solve
+  uint32_t* flagged;  // [0] = count, [1] = largest R-diagonal ratio (float bits), [2..] = block ids to re-solve
   PostArgs post;
 };
 
@@ -493,9 +496,11 @@ __global__ void __launch_bounds__(BmfrShape<BW>::NT, BW == 8 ? 8 : 3) bmfr_fused
       dmax = fmaxf(dmax, a);
       dmin = fminf(dmin, a);
     }
-    if (!(dmax <= 1e6f * dmin)) {
+    const float ratio = dmax <= 3.0e38f * dmin ? dmax / dmin : INFINITY;  // dmin = 0 or NaN: infinite
+    atomicMax(p.flagged + 1, __float_as_uint(ratio));  // non-negative floats order as their bits
+    if (!(dmax <= p.cond_limit * dmin)) {
       uint32_t slot = atomicAdd(p.flagged, 1u);
-      p.flagged[1 + slot] = (uint32_t)(gy * p.gw + gx);
+      p.flagged[2 + slot] = (uint32_t)(gy * p.gw + gx);
     }
   }
   __syncthreads();
@@ -536,7 +541,7 @@ __global__ void __launch_bounds__(256) bmfr_fp64_kernel(BmfrParams p) {
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const uint32_t nflag = p.flagged[0];
   for (uint32_t k = blockIdx.x; k < nflag; k += gridDim.x) {
-    const int bid = (int)p.flagged[1 + k];
+    const int bid = (int)p.flagged[2 + k];
     const int gx = bid % p.gw, gy = bid / p.gw;
     const int offx = (int)((float)BW * c_bmfr_offsets[p.frame % 16][0]);
     const int offy = (int)((float)BW * c_bmfr_offsets[p.frame % 16][1]);
@@ -863,13 +868,14 @@ PbrtBFR::~PbrtBFR() {
 
 template <int BW> static int launch_bmfr(PbrtBMFR* b, const BmfrParams& kp, pbrt_stream_t stream) {
   size_t smem = bmfr_smem_bytes(BW);
-  static bool attr_set = false;
-  if (!attr_set) {
+  static PerDeviceOnce attrs;
+  int ast = once_per_device(attrs, [&]() -> int {
     PBRT_CUDA(cudaFuncSetAttribute(bmfr_fused_kernel<BW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     PBRT_CUDA(cudaFuncSetAttribute(bmfr_fp64_kernel<BW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)(sizeof(double) * (13 * BW * BW + 8 * 14))));
-    attr_set = true;
-  }
+    return PBRT_OK;
+  });
+  if (ast) return ast;
   dim3 grid(kp.gw, kp.gh);
   bmfr_fused_kernel<BW><<<grid, BmfrShape<BW>::NT, smem, stream>>>(kp);
   int st = check_launch("bmfr_fused_kernel");
@@ -1036,7 +1042,7 @@ PBRT_API int pbrt_bmfr_create(uint32_t width, uint32_t height, uint32_t work_wid
   if ((st = b->denoised.alloc(width, height, 2, PBRT_FORMAT_R16G16B16A16_SFLOAT)) ||
       (st = b->final_image.alloc(width, height, 1, PBRT_FORMAT_B8G8R8A8_UNORM)) ||
       (st = b->weights.alloc(gw, gh, 30, PBRT_FORMAT_R32_SFLOAT)) ||
-      (st = b->flags.alloc(gw * gh + 1, 1, 1, PBRT_FORMAT_R32_SFLOAT))) {
+      (st = b->flags.alloc(gw * gh + 2, 1, 1, PBRT_FORMAT_R32_SFLOAT))) {
     delete b;
     return st;
   }
@@ -1067,6 +1073,7 @@ PBRT_API int pbrt_bmfr_dispatch(PbrtBMFR* b, const PbrtPushConstants* pc, pbrt_s
   kp.frame = pc->frame_number;
   kp.position_type = b->position_type;
   kp.fp64_resolve = b->fp64_resolve;
+  kp.cond_limit = b->cond_limit;
   kp.depth = b->gbuffer->depth.ptr<float>();
   kp.normal = b->gbuffer->normal.ptr<float2>();
   const DeviceImage& noisy = b->illumination->images[0];
@@ -1083,7 +1090,7 @@ PBRT_API int pbrt_bmfr_dispatch(PbrtBMFR* b, const PbrtPushConstants* pc, pbrt_s
   kp.post.W = kp.W;
   kp.post.H = kp.H;
   kp.post.frame = kp.frame;
-  if (b->fp64_resolve) PBRT_CUDA(cudaMemsetAsync(b->counter, 0, sizeof(uint32_t), stream));
+  if (b->fp64_resolve) PBRT_CUDA(cudaMemsetAsync(b->counter, 0, 2 * sizeof(uint32_t), stream));
   switch (b->bw) {
     case 8: return launch_bmfr<8>(b, kp, stream);
     case 16: return launch_bmfr<16>(b, kp, stream);
@@ -1110,6 +1117,28 @@ PBRT_API int pbrt_bmfr_fp64_block_count(PbrtBMFR* b, pbrt_stream_t stream, uint3
   if (!b->fp64_resolve) return PBRT_OK;
   PBRT_CUDA(cudaMemcpyAsync(count, b->counter, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
   PBRT_CUDA(cudaStreamSynchronize(stream));
+  return PBRT_OK;
+}
+
+PBRT_API int pbrt_bmfr_set_condition_limit(PbrtBMFR* b, float limit) {
+  if (!checked<PbrtBMFR>(b, Kind::BMFR)) return fail(PBRT_ERROR_INVALID_ARGUMENT, "not a BMFR");
+  if (!(limit >= 1.f) || !std::isfinite(limit))
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "BMFR: condition limit %g (finite, >= 1)", (double)limit);
+  b->cond_limit = limit;
+  return PBRT_OK;
+}
+
+PBRT_API int pbrt_bmfr_condition_stats(PbrtBMFR* b, pbrt_stream_t stream, uint32_t* flagged, float* max_ratio) {
+  if (!checked<PbrtBMFR>(b, Kind::BMFR) || !flagged || !max_ratio)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "bad arguments");
+  *flagged = 0;
+  *max_ratio = 0.f;
+  if (!b->fp64_resolve) return fail(PBRT_ERROR_INVALID_ARGUMENT, "BMFR: condition statistics need fp64_resolve");
+  uint32_t w[2];
+  PBRT_CUDA(cudaMemcpyAsync(w, b->counter, sizeof(w), cudaMemcpyDeviceToHost, stream));
+  PBRT_CUDA(cudaStreamSynchronize(stream));
+  *flagged = w[0];
+  std::memcpy(max_ratio, &w[1], sizeof(float));
   return PBRT_OK;
 }
 
@@ -1205,18 +1234,46 @@ namespace pbrt {
 constexpr uint32_t kNoAllocMaxBlocks = PBRT_BMFR_NOALLOC_MAX_BLOCKS;
 static __device__ __align__(256) float g_bmfr_noalloc_weights[kNoAllocMaxBlocks * 30];
 
-// Device address of g_bmfr_noalloc_weights for each device, resolved once
-// with that device current (host code cannot use the symbol itself).
+// Device address of g_bmfr_noalloc_weights for each device, resolved with
+// that device current (host code cannot use the symbol itself), together
+// with the id of the context it was resolved in: after cudaDeviceReset the
+// device's next context loads the module anew, so the address and the
+// kernel attributes are resolved again.
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
 static std::mutex g_noalloc_mutex;
-static float* g_noalloc_ptr[128] = {nullptr};
+static float* g_noalloc_ptr[kMaxDevices] = {nullptr};
+static unsigned long long g_noalloc_ctx[kMaxDevices] = {0};
+
+// Unique id of the calling thread's current context (0 if unavailable).
+static unsigned long long current_context_id() {
+  static const std::pair<CtxGetCurrentFn, CtxGetIdFn> fns = []() {
+    void* a = nullptr;
+    void* b = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+        q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      return std::pair<CtxGetCurrentFn, CtxGetIdFn>(nullptr, nullptr);
+    }
+    return std::pair<CtxGetCurrentFn, CtxGetIdFn>((CtxGetCurrentFn)a, (CtxGetIdFn)b);
+  }();
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (!fns.first || !fns.second || fns.first(&ctx) != CUDA_SUCCESS || !ctx || fns.second(ctx, &id) != CUDA_SUCCESS)
+    return 0;
+  return id;
+}
 
 static int noalloc_weights(float** out) {
   int dev = 0;
   PBRT_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 128) return fail(PBRT_ERROR_UNSUPPORTED, "BMFR no-alloc: device ordinal %d", dev);
+  if (dev < 0 || dev >= kMaxDevices) return fail(PBRT_ERROR_UNSUPPORTED, "BMFR no-alloc: device ordinal %d", dev);
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_ptr[dev]) {
+  if (!g_noalloc_ptr[dev] || current_context_id() != g_noalloc_ctx[dev]) {
     void* p = nullptr;
+    // (also makes the device's primary context current on a thread's first call)
     cudaError_t e = cudaGetSymbolAddress(&p, g_bmfr_noalloc_weights);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_bmfr_noalloc_weights)");
     for (int bw : {8, 16, 32}) {  // shared-memory opt-in of the kernel this entry point launches
@@ -1227,6 +1284,7 @@ static int noalloc_weights(float** out) {
       if (a != cudaSuccess) return cuda_fail(a, "cudaFuncSetAttribute(bmfr_fused_kernel)");
     }
     g_noalloc_ptr[dev] = static_cast<float*>(p);
+    g_noalloc_ctx[dev] = current_context_id();
   }
   *out = g_noalloc_ptr[dev];
   return PBRT_OK;
@@ -1240,6 +1298,17 @@ extern "C" PBRT_API int pbrt_bmfr_dispatch_noalloc(uint32_t width, uint32_t heig
   if (!im || !pc || !im->depth || !im->normal || !im->albedo || !im->noisy || !im->motion || !im->spp ||
       !im->denoised || !im->final_bgra)
     return fail(PBRT_ERROR_INVALID_ARGUMENT, "BMFR no-alloc: null image pointer or push constants");
+  {
+    // the kernel reads noisy / denoised as 8-byte half4, normal as float2, motion
+    // as half2, depth as float and albedo / final as 4-byte texels
+    const struct { const void* p; unsigned align; const char* name; } req[] = {
+        {im->noisy, 8, "noisy"}, {im->denoised, 8, "denoised"}, {im->normal, 8, "normal"}, {im->depth, 4, "depth"},
+        {im->motion, 4, "motion"}, {im->albedo, 4, "albedo"}, {im->final_bgra, 4, "final_bgra"}};
+    for (const auto& r : req)
+      if (reinterpret_cast<uintptr_t>(r.p) % r.align)
+        return fail(PBRT_ERROR_INVALID_ARGUMENT, "BMFR no-alloc: %s pointer %p is not %u-byte aligned", r.name, r.p,
+                    r.align);
+  }
   if (block_size != 8 && block_size != 16 && block_size != 32)
     return fail(PBRT_ERROR_UNSUPPORTED, "BMFR no-alloc: block size %u (supported: 8, 16, 32)", block_size);
   if (position_type < 0 || position_type > 2)

@@ -6,6 +6,7 @@
 #include <atomic>
 #include <cstdarg>
 #include <cstdint>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -55,6 +56,28 @@ bool nn_fp8_umma_fits(const void* x1, int c1, const void* x2, int c2, const void
 // Whether pbrt_nn_conv3x3_umma_pooled takes this layer (whole 16 x 8 tiles,
 // the weights and two input stages in shared memory).
 bool nn_umma_pooled_fits(int c1, int cout, int h, int w);
+
+// One-time setup per device (kernel attributes such as the dynamic
+// shared-memory opt-in are recorded per device, not per process):
+// once_per_device(flag, f) runs f() with the caller's current device the
+// first time it is called on that device, and again after a failed f().
+// Thread-safe.
+constexpr int kMaxDevices = 64;
+struct PerDeviceOnce {
+  std::mutex m;
+  bool done[kMaxDevices] = {};
+};
+template <class F> int once_per_device(PerDeviceOnce& o, F&& f) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) return fail(PBRT_ERROR_UNSUPPORTED, "device ordinal %d beyond %d", dev, kMaxDevices);
+  std::lock_guard<std::mutex> lock(o.m);
+  if (o.done[dev]) return PBRT_OK;
+  int st = f();
+  if (st == PBRT_OK) o.done[dev] = true;
+  return st;
+}
 
 void retain(Object* o);
 void release(Object* o);
@@ -130,12 +153,13 @@ struct PbrtBMFR : pbrt::Object {
   ~PbrtBMFR() override;
   uint32_t width = 0, height = 0, bw = 32, fitting_kernel = 256;
   int32_t position_type = 0, fp64_resolve = 0;
+  float cond_limit = 1e6f;  // FP64 re-solve above this R-diagonal ratio
   PbrtGBuffer* gbuffer = nullptr;
   PbrtIlluminationBuffer* illumination = nullptr;
   PbrtAccumulationBuffer* acc = nullptr;
   pbrt::DeviceImage denoised, final_image, weights;
   pbrt::DeviceImage flags;  // per block: condition estimate exceeded (FP64 re-solve list)
-  uint32_t* counter = nullptr;  // device: [0] = number of flagged blocks
+  uint32_t* counter = nullptr;  // device: [0] = number of flagged blocks, [1] = largest ratio (float bits)
 };
 
 struct PbrtBFR : pbrt::Object {

@@ -854,26 +854,28 @@ template <int WN> void launch_fwd(const ConvArgs& a, cudaStream_t s) {
 }
 template <int WN, int KC> int launch_halo(const ConvArgs& a, cudaStream_t s) {
   typedef HaloCfg<WN, KC> Cfg;
-  static bool attr_set = false;  // per process; the attribute is per function
-  if (!attr_set) {
+  static PerDeviceOnce attrs;
+  int ast = once_per_device(attrs, [&]() -> int {
     cudaError_t e = cudaFuncSetAttribute(conv3x3_halo_kernel<WN, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)Cfg::kSmem);
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(conv3x3_halo_kernel)");
-    attr_set = true;
-  }
+    return PBRT_OK;
+  });
+  if (ast) return ast;
   dim3 grid(((a.W + kTW - 1) / kTW) * ((a.H + kTH - 1) / kTH), a.N, (a.cout + Cfg::BN - 1) / Cfg::BN);
   conv3x3_halo_kernel<WN, KC><<<grid, 256, Cfg::kSmem, s>>>(a);
   return PBRT_OK;
 }
 template <int NT, int KC> int launch_halo_m(const ConvArgs& a, cudaStream_t s) {
   typedef HaloMCfg<NT, KC> Cfg;
-  static bool attr_set = false;
-  if (!attr_set) {
+  static PerDeviceOnce attrs;
+  int ast = once_per_device(attrs, [&]() -> int {
     cudaError_t e = cudaFuncSetAttribute(conv3x3_halo_m_kernel<NT, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)Cfg::kSmem);
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(conv3x3_halo_m_kernel)");
-    attr_set = true;
-  }
+    return PBRT_OK;
+  });
+  if (ast) return ast;
   dim3 grid(((a.W + kTW - 1) / kTW) * ((a.H + kMTH - 1) / kMTH), a.N, (a.cout + Cfg::BN - 1) / Cfg::BN);
   conv3x3_halo_m_kernel<NT, KC><<<grid, 256, Cfg::kSmem, s>>>(a);
   return PBRT_OK;
@@ -889,13 +891,14 @@ template <int WN> int launch_halo_for(const ConvArgs& a, cudaStream_t s) {
 }
 template <int WN> int launch_fp8(const Fp8ConvArgs& a, cudaStream_t s) {
   typedef Fp8Cfg<WN> Cfg;
-  static bool attr_set = false;
-  if (!attr_set) {
+  static PerDeviceOnce attrs;
+  int ast = once_per_device(attrs, [&]() -> int {
     cudaError_t e = cudaFuncSetAttribute(conv3x3_halo_fp8_kernel<WN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)Cfg::kSmem);
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(conv3x3_halo_fp8_kernel)");
-    attr_set = true;
-  }
+    return PBRT_OK;
+  });
+  if (ast) return ast;
   dim3 grid(((a.W + kTW - 1) / kTW) * ((a.H + kTH - 1) / kTH), a.N, (a.cout + Cfg::BN - 1) / Cfg::BN);
   conv3x3_halo_fp8_kernel<WN><<<grid, 256, Cfg::kSmem, s>>>(a);
   return PBRT_OK;

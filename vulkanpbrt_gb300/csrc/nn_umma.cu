@@ -908,13 +908,14 @@ namespace {
 template <int NC> int launch_umma(const UmmaConvArgs& a, cudaStream_t s) {
   constexpr int kStage = umma::kPlanes * umma::kPlaneBytes + 9 * umma::kPlanes * NC * 16;
   constexpr size_t kSmem = 2 * (size_t)kStage + 1024;  // two stages (+ alignment of the dynamic base)
-  static bool attr_set = false;
-  if (!attr_set) {
+  static PerDeviceOnce attrs;
+  int ast = once_per_device(attrs, [&]() -> int {
     cudaError_t e = cudaFuncSetAttribute(conv3x3_umma_kernel<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)kSmem);
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(conv3x3_umma_kernel)");
-    attr_set = true;
-  }
+    return PBRT_OK;
+  });
+  if (ast) return ast;
   dim3 grid(((a.W + umma::kTileW - 1) / umma::kTileW) * ((a.H + umma::kTileH - 1) / umma::kTileH), a.N, 1);
   conv3x3_umma_kernel<NC><<<grid, 128, kSmem, s>>>(a);
   return PBRT_OK;
@@ -929,18 +930,16 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 EncodeTiledFn encode_tiled() {
-  static EncodeTiledFn fn = nullptr;
-  static bool tried = false;
-  if (!tried) {
-    tried = true;
+  // the driver entry point is process-wide; resolved once (thread-safe static)
+  static const EncodeTiledFn fn = []() -> EncodeTiledFn {
     void* p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = (EncodeTiledFn)p;
-    else
-      cudaGetLastError();
-  }
+      return (EncodeTiledFn)p;
+    cudaGetLastError();
+    return nullptr;
+  }();
   return fn;
 }
 
@@ -989,13 +988,14 @@ template <int NC, bool kF8> int launch_umma_ws(const UmmaConvArgs& a, cudaStream
     return e ? std::min(6, std::max(2, std::atoi(e))) : 0;
   }();
   const size_t smem_max = kF8 ? kWsSmemMaxF8 : kWsSmemMax;
-  static bool attr_set = false;
-  if (!attr_set) {
+  static PerDeviceOnce attrs;
+  int ast = once_per_device(attrs, [&]() -> int {
     cudaError_t e = cudaFuncSetAttribute(conv3x3_umma_ws_kernel<NC, kF8>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(conv3x3_umma_ws_kernel)");
-    attr_set = true;
-  }
+    return PBRT_OK;
+  });
+  if (ast) return ast;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1044,13 +1044,14 @@ template <int NC, bool kF8> int launch_umma_ws(const UmmaConvArgs& a, cudaStream
 
 template <int NC> int launch_umma_persistent(const UmmaConvArgs& a, cudaStream_t s, bool use_tma_flag) {
   const size_t smem = persistent_smem(a.c1 + a.c2, NC);
-  static bool attr_set = false;
-  if (!attr_set) {
+  static PerDeviceOnce attrs;
+  int ast = once_per_device(attrs, [&]() -> int {
     cudaError_t e = cudaFuncSetAttribute(conv3x3_umma_persistent_kernel<NC>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPersistentSmemMax);
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(conv3x3_umma_persistent_kernel)");
-    attr_set = true;
-  }
+    return PBRT_OK;
+  });
+  if (ast) return ast;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

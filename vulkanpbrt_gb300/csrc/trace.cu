@@ -562,7 +562,7 @@ struct Queues {
   float4* prev;  // previous vertex (worldSpacePos) xyz, w = loop index i (as int bits)
   float4* alb;   // primary albedo xyz (float, for demodulation), w = transDepth (int bits)
   uint32_t* prim_key;  // primary hit key per pixel (0xffffffff = miss), for parity tests
-  // ray sorting (kSortRays): shading appends to these, the sort scatters them
+  // ray sorting (sort_rays schedule): shading appends to these, the sort scatters them
   // into the ray queue / shadow queue ordered by (direction octant, origin cell)
   uint32_t* pix_t;
   float4* org_t;
@@ -577,25 +577,18 @@ struct Queues {
   uint32_t* bins;  // [2][kSortBins]: extension rays, shadow rays
 };
 
+// Schedule options of a pipeline (pbrt_pipeline_set_schedule).
 // Ray sorting: extension and shadow rays are reordered by a 12-bit key --
 // the direction octant (3 bits) over a 3-bit-per-axis Morton cell of the
 // origin in the scene box -- with a counting sort (histogram, scan,
 // warp-aggregated scatter) before they are traversed, so a warp's rays take
 // the same child order and start in the same region of the BVH. Results
-// are per pixel, so the order changes nothing but speed.
-#ifndef PBRT_SORT_RAYS
-#define PBRT_SORT_RAYS 0
-#endif
-constexpr int kSortRays = PBRT_SORT_RAYS;
-
-// Schedule: 1 traces bounce k's closest-hit rays and bounce k-1's shadow
-// rays in one persistent launch (fewer launch tails, more rays per launch);
+// are per pixel, so the order changes nothing but speed. Shading appends to
+// the staging queues (pix_t ... skey_t) when Queues::key_t is set.
+// Merged schedule: bounce k's closest-hit rays and bounce k-1's shadow rays
+// in one persistent launch (fewer launch tails, more rays per launch);
 // per-pixel updates keep their order (shading of k-1, shadow resolve of
-// k-1, shading of k). 0: one launch per queue.
-#ifndef PBRT_MERGE_SHADOW
-#define PBRT_MERGE_SHADOW 1
-#endif
-constexpr int kMergeShadow = PBRT_MERGE_SHADOW;
+// k-1, shading of k). Otherwise one launch per queue.
 constexpr int kSortBits = 12, kSortBins = 1 << kSortBits;
 
 struct GBufferOut {
@@ -945,9 +938,6 @@ __global__ void __launch_bounds__(128, PBRT_TRAVERSE_MIN_BLOCKS) k_traverse(Scen
 // primary rays); the closest hit is the same, as it depends only on which
 // triangles a ray tests, never on the order. Node visits are counted once
 // per warp (one fetch serves the 32 rays), triangle tests per ray.
-#ifndef PBRT_PACKET_PRIMARY
-#define PBRT_PACKET_PRIMARY 1
-#endif
 __global__ void __launch_bounds__(128, PBRT_TRAVERSE_MIN_BLOCKS) k_traverse_packet(SceneView sc, Queues q, Counters* c) {
   __shared__ uint2 s_stack[kTraverseThreads / 32][kStackSize];
   const int lane = threadIdx.x & 31;
@@ -1459,7 +1449,7 @@ __global__ void PBRT_SHADE_BOUNDS k_shade(SceneView sc, const FrameParams* __res
     }
     const int rs = warp_alloc(&c->ray[nq], push_ray);
     if (rs >= 0) {
-      if (kSortRays) {
+      if (q.key_t) {
         q.pix_t[rs] = p;
         q.org_t[rs] = ray_o;
         q.dir_t[rs] = ray_d;
@@ -1472,7 +1462,7 @@ __global__ void PBRT_SHADE_BOUNDS k_shade(SceneView sc, const FrameParams* __res
     }
     const int ss = warp_alloc(&c->shadow, push_shadow);
     if (ss >= 0) {
-      if (kSortRays) {
+      if (q.skey_t) {
         q.spix_t[ss] = p;
         q.sorg_t[ss] = sh_o;
         q.sdir_t[ss] = sh_d;
@@ -1611,6 +1601,8 @@ struct PbrtPipeline : pbrt::Object {
   cudaGraphExec_t graph_exec = nullptr;
   int graph_depth = -1;
   int graph_light_mode = -1;  // the light-sampling mode the captured graph's shading kernels were built for
+  int sort_rays = 0;        // schedule: counting sort of the ray and shadow queues before traversal
+  int merge_shadow = 1;     // schedule: shadow rays of bounce k-1 traced in bounce k's launch
   int grid_persistent = 0;  // traversal CTAs (persistent warps)
   int grid_shade = 0;       // shading CTAs (grid-stride)
   uint32_t* abort_host = nullptr;  // mapped pinned word (pbrt_pipeline_abort_flag)
@@ -1656,6 +1648,12 @@ static void launch_shade(int grid, cudaStream_t s, const SceneView& sc, const Fr
 static int record_frame(PbrtPipeline* pp, cudaStream_t s, StageEvents* ev) {
   const int N = pp->W * pp->H;
   const SceneView sc = pp->scene->view;
+  Queues q = pp->q;
+  if (!pp->sort_rays) {  // shading writes the queues directly
+    q.key_t = nullptr;
+    q.skey_t = nullptr;
+  }
+  const bool merge = pp->merge_shadow != 0;
   GBufferOut g{};
   if (pp->gbuffer) {
     g.depth = pp->gbuffer->depth.ptr<float>();
@@ -1667,54 +1665,54 @@ static int record_frame(PbrtPipeline* pp, cudaStream_t s, StageEvents* ev) {
   const int blocks_px = std::min((N + 255) / 256, 152 * 8);
   k_frame_begin<<<1, 1, 0, s>>>(pp->ctr, pp->dev_fp);
   if (ev) ev->begin(0);
-  k_raygen<<<blocks_px, 256, 0, s>>>(pp->dev_fp, pp->q);
+  k_raygen<<<blocks_px, 256, 0, s>>>(pp->dev_fp, q);
   if (ev) ev->end(0);
   // Bounce k traces the rays that leave vertex k-1. Transmissive vertices do
   // not count towards the depth (ptRaygen.rgen:69, up to 10 of them).
   const int bounces = pp->max_depth + 1 + (pp->scene->transmissive ? 10 : 0);
   for (int k = 0; k < bounces; ++k) {
-    if (kMergeShadow) {
+    if (merge) {
       k_bounce_begin_merged<<<1, 1, 0, s>>>(pp->ctr, k);
       if (ev) ev->begin(1);
-      if (k == 0 && PBRT_PACKET_PRIMARY) k_traverse_packet<<<pp->grid_persistent, 128, 0, s>>>(sc, pp->q, pp->ctr);
-      else if (k == 0) k_traverse<0><<<pp->grid_persistent, 128, 0, s>>>(sc, pp->q, pp->ctr, k, QueryIO{});
-      else k_traverse<4><<<pp->grid_persistent, 128, 0, s>>>(sc, pp->q, pp->ctr, k, QueryIO{});
+      if (k == 0) k_traverse_packet<<<pp->grid_persistent, 128, 0, s>>>(sc, q, pp->ctr);
+      else k_traverse<4><<<pp->grid_persistent, 128, 0, s>>>(sc, q, pp->ctr, k, QueryIO{});
       if (ev) ev->end(1);
       k_shadow_consumed<<<1, 1, 0, s>>>(pp->ctr);
     } else {
       k_bounce_begin<<<1, 1, 0, s>>>(pp->ctr, k);
       if (ev) ev->begin(1);
-      k_traverse<0><<<pp->grid_persistent, 128, 0, s>>>(sc, pp->q, pp->ctr, k, QueryIO{});
+      if (k == 0) k_traverse_packet<<<pp->grid_persistent, 128, 0, s>>>(sc, q, pp->ctr);
+      else k_traverse<0><<<pp->grid_persistent, 128, 0, s>>>(sc, q, pp->ctr, k, QueryIO{});
       if (ev) ev->end(1);
     }
     if (ev) ev->begin(2);
-    launch_shade(pp->grid_shade, s, sc, pp->dev_fp, pp->q, pp->ctr, g, k, pp->light_mode);
-    if (kSortRays) {
+    launch_shade(pp->grid_shade, s, sc, pp->dev_fp, q, pp->ctr, g, k, pp->light_mode);
+    if (pp->sort_rays) {
       const int nq = (k + 1) & 1;
-      uint32_t* bins_r = pp->q.bins;
-      uint32_t* bins_s = pp->q.bins + kSortBins;
+      uint32_t* bins_r = q.bins;
+      uint32_t* bins_s = q.bins + kSortBins;
       const int sort_grid = std::min((N + 255) / 256, 152 * 4);
-      cudaMemsetAsync(pp->q.bins, 0, 2 * kSortBins * sizeof(uint32_t), s);
+      cudaMemsetAsync(q.bins, 0, 2 * kSortBins * sizeof(uint32_t), s);
       if (k + 1 < bounces) {
-        k_sort_hist<<<sort_grid, 256, 0, s>>>(&pp->ctr->ray[nq], pp->q.key_t, bins_r);
+        k_sort_hist<<<sort_grid, 256, 0, s>>>(&pp->ctr->ray[nq], q.key_t, bins_r);
         k_sort_scan<<<1, 1024, 0, s>>>(bins_r);
-        k_sort_scatter<false><<<sort_grid, 256, 0, s>>>(&pp->ctr->ray[nq], pp->q, nq, bins_r);
+        k_sort_scatter<false><<<sort_grid, 256, 0, s>>>(&pp->ctr->ray[nq], q, nq, bins_r);
       }
-      k_sort_hist<<<sort_grid, 256, 0, s>>>(&pp->ctr->shadow, pp->q.skey_t, bins_s);
+      k_sort_hist<<<sort_grid, 256, 0, s>>>(&pp->ctr->shadow, q.skey_t, bins_s);
       k_sort_scan<<<1, 1024, 0, s>>>(bins_s);
-      k_sort_scatter<true><<<sort_grid, 256, 0, s>>>(&pp->ctr->shadow, pp->q, 0, bins_s);
+      k_sort_scatter<true><<<sort_grid, 256, 0, s>>>(&pp->ctr->shadow, q, 0, bins_s);
     }
     if (ev) ev->end(2);
-    if (!kMergeShadow || k + 1 == bounces) {  // merged: the last bounce's shadow rays go alone
+    if (!merge || k + 1 == bounces) {  // merged: the last bounce's shadow rays go alone
       if (ev) ev->begin(3);
-      if (kMergeShadow) k_shadow_begin<<<1, 1, 0, s>>>(pp->ctr);
-      k_traverse<1><<<pp->grid_persistent, 128, 0, s>>>(sc, pp->q, pp->ctr, k, QueryIO{});
+      if (merge) k_shadow_begin<<<1, 1, 0, s>>>(pp->ctr);
+      k_traverse<1><<<pp->grid_persistent, 128, 0, s>>>(sc, q, pp->ctr, k, QueryIO{});
       if (ev) ev->end(3);
       k_bounce_end<<<1, 1, 0, s>>>(pp->ctr);
     }
   }
   if (ev) ev->begin(4);
-  k_finalize<<<blocks_px, 256, 0, s>>>(pp->dev_fp, pp->q, out);
+  k_finalize<<<blocks_px, 256, 0, s>>>(pp->dev_fp, q, out);
   if (ev) ev->end(4);
   return check_launch("path tracer frame");
 }
@@ -2023,19 +2021,6 @@ PBRT_API int pbrt_pipeline_create(PbrtScene* scene, PbrtGBuffer* g, PbrtIllumina
   if (!st) st = pp->a(&q.prev, N);
   if (!st) st = pp->a(&q.alb, N);
   if (!st) st = pp->a(&q.prim_key, N);
-  if (kSortRays) {
-    if (!st) st = pp->a(&q.pix_t, N);
-    if (!st) st = pp->a(&q.org_t, N);
-    if (!st) st = pp->a(&q.dir_t, N);
-    if (!st) st = pp->a(&q.key_t, N);
-    if (!st) st = pp->a(&q.spix_t, N);
-    if (!st) st = pp->a(&q.sorg_t, N);
-    if (!st) st = pp->a(&q.sdir_t, N);
-    if (!st) st = pp->a(&q.snee_t, N);
-    if (!st) st = pp->a(&q.sadd_t, N);
-    if (!st) st = pp->a(&q.skey_t, N);
-    if (!st) st = pp->a(&q.bins, 2 * kSortBins);
-  }
   if (!st) st = pp->a(&pp->ctr, 1);
   if (!st) st = pp->a(&pp->dev_fp, 1);
   if (!st) {
@@ -2233,6 +2218,34 @@ PBRT_API int pbrt_pipeline_debug_images(const PbrtPipeline* pp, PbrtImage* prima
   return PBRT_OK;
 }
 
+
+PBRT_API int pbrt_pipeline_set_schedule(PbrtPipeline* pp, int32_t sort_rays, int32_t merge_shadow) {
+  if (!checked<PbrtPipeline>(pp, Kind::Pipeline)) return fail(PBRT_ERROR_INVALID_ARGUMENT, "not a pipeline");
+  if (sort_rays && !pp->q.key_t) {  // staging queues of the sort, allocated on first use
+    Queues& q = pp->q;
+    const size_t N = (size_t)pp->W * pp->H;
+    int st = PBRT_OK;
+    if (!st) st = pp->a(&q.pix_t, N);
+    if (!st) st = pp->a(&q.org_t, N);
+    if (!st) st = pp->a(&q.dir_t, N);
+    if (!st) st = pp->a(&q.spix_t, N);
+    if (!st) st = pp->a(&q.sorg_t, N);
+    if (!st) st = pp->a(&q.sdir_t, N);
+    if (!st) st = pp->a(&q.snee_t, N);
+    if (!st) st = pp->a(&q.sadd_t, N);
+    if (!st) st = pp->a(&q.skey_t, N);
+    if (!st) st = pp->a(&q.bins, 2 * kSortBins);
+    if (!st) st = pp->a(&q.key_t, N);  // last: key_t marks the staging queues as allocated
+    if (st) return st;
+  }
+  const int sr = sort_rays ? 1 : 0, ms = merge_shadow ? 1 : 0;
+  if (sr != pp->sort_rays || ms != pp->merge_shadow) {
+    pp->sort_rays = sr;
+    pp->merge_shadow = ms;
+    pp->graph_depth = -1;  // the frame graph is recaptured on the next trace
+  }
+  return PBRT_OK;
+}
 
 PBRT_API int pbrt_pipeline_set_launch(PbrtPipeline* pp, int32_t trace_blocks_per_sm, int32_t shade_blocks_per_sm) {
   if (!checked<PbrtPipeline>(pp, Kind::Pipeline) || trace_blocks_per_sm < 1 || trace_blocks_per_sm > 16 ||

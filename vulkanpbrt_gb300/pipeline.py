@@ -67,6 +67,7 @@ _abi.add_signatures({
     "pbrt_pipeline_abort_flag": (C.c_int32, [H, P(P(C.c_uint32))]),
     "pbrt_pipeline_set_budget": (C.c_int32, [H, C.c_uint64]),
     "pbrt_pipeline_status": (C.c_int32, [H, H, P(C.c_int32)]),
+    "pbrt_pipeline_set_schedule": (C.c_int32, [H, C.c_int32, C.c_int32]),
 })
 
 
@@ -212,6 +213,10 @@ class PBRTPipeline(Handle):
     def set_launch(self, trace_blocks_per_sm: int = 8, shade_blocks_per_sm: int = 8) -> None:
         """Persistent traversal CTAs and shading CTAs per SM (1..16)."""
         check(lib().pbrt_pipeline_set_launch(self.ptr, trace_blocks_per_sm, shade_blocks_per_sm))
+
+    def set_schedule(self, sort_rays: bool = False, merge_shadow: bool = True) -> None:
+        """Frame schedule: ray sorting before traversal; shadow rays merged into the next bounce's launch."""
+        check(lib().pbrt_pipeline_set_schedule(self.ptr, int(sort_rays), int(merge_shadow)))
 
     def set_budget(self, budget_ns: int) -> None:
         check(lib().pbrt_pipeline_set_budget(self.ptr, int(budget_ns)))

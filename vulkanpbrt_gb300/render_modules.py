@@ -291,6 +291,16 @@ class BMFR(Handle):
         check(lib().pbrt_bmfr_fp64_block_count(self.ptr, stream_handle(stream), C.byref(n)))
         return n.value
 
+    def set_condition_limit(self, limit: float) -> None:
+        """R-diagonal ratio above which a block is re-solved in FP64 (default 1e6)."""
+        check(lib().pbrt_bmfr_set_condition_limit(self.ptr, float(limit)))
+
+    def condition_stats(self, stream=None):
+        """(blocks re-solved in FP64, largest R-diagonal ratio) of the last dispatch (needs fp64_resolve)."""
+        n, r = C.c_uint32(), C.c_float()
+        check(lib().pbrt_bmfr_condition_stats(self.ptr, stream_handle(stream), C.byref(n), C.byref(r)))
+        return n.value, r.value
+
 
 class BFR(Handle):
     """BFR (source/renderModules/denoisers/BFR.hpp)."""
