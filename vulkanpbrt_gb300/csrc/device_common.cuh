@@ -40,12 +40,32 @@ PBRT_D float3 mix3(float3 x, float3 y, float a) { return x * (1.f - a) + y * a; 
 struct Mat4 {
   float4 c[4];
 };
+// Unfused forms (each product and sum rounded on its own, in the shader's
+// left-to-right order): the hit position, the ray origins built from it and
+// the G-buffer depth come out bit-identical to an unfused FP32 evaluation.
+PBRT_D float3 mul_rn(float3 a, float s) { return f3(__fmul_rn(a.x, s), __fmul_rn(a.y, s), __fmul_rn(a.z, s)); }
+PBRT_D float3 add_rn(float3 a, float3 b) { return f3(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z)); }
+PBRT_D float length_rn(float3 a) {
+  return sqrtf(__fadd_rn(__fadd_rn(__fmul_rn(a.x, a.x), __fmul_rn(a.y, a.y)), __fmul_rn(a.z, a.z)));
+}
+PBRT_D float3 normalize_rn(float3 a) {
+  const float l = length_rn(a);
+  return f3(__fdiv_rn(a.x, l), __fdiv_rn(a.y, l), __fdiv_rn(a.z, l));
+}
 PBRT_D float4 mul(const Mat4& m, float4 v) {
   float4 r;
   r.x = m.c[0].x * v.x + m.c[1].x * v.y + m.c[2].x * v.z + m.c[3].x * v.w;
   r.y = m.c[0].y * v.x + m.c[1].y * v.y + m.c[2].y * v.z + m.c[3].y * v.w;
   r.z = m.c[0].z * v.x + m.c[1].z * v.y + m.c[2].z * v.z + m.c[3].z * v.w;
   r.w = m.c[0].w * v.x + m.c[1].w * v.y + m.c[2].w * v.z + m.c[3].w * v.w;
+  return r;
+}
+// m * (p, 1), xyz, unfused: ((c0 p.x + c1 p.y) + c2 p.z) + c3.
+PBRT_D float3 mul_point_rn(const Mat4& m, float3 p) {
+  float3 r;
+  r.x = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m.c[0].x, p.x), __fmul_rn(m.c[1].x, p.y)), __fmul_rn(m.c[2].x, p.z)), m.c[3].x);
+  r.y = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m.c[0].y, p.x), __fmul_rn(m.c[1].y, p.y)), __fmul_rn(m.c[2].y, p.z)), m.c[3].y);
+  r.z = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m.c[0].z, p.x), __fmul_rn(m.c[1].z, p.y)), __fmul_rn(m.c[2].z, p.z)), m.c[3].z);
   return r;
 }
 

@@ -288,15 +288,15 @@ PBRT_D float3 closest_hit(const SceneView& sc, float3 ray_dir, uint32_t inst_id,
   float3 diffuse = srgb_to_linear(f3(dm.x, dm.y, dm.z));
   float diffuse_a = dm.w;
   diffuse = diffuse * diffuse_a;
-  float3 position = p0 * b0 + p1 * b1 + p2 * b2;
-  float4 wp = mul(inst.obj, make_float4(position.x, position.y, position.z, 1.f));
-  position = f3(wp.x, wp.y, wp.z);
-  float3 normal = normalize(n0 * b0 + n1 * b1 + n2 * b2);  // exact: the G-buffer stores it
+  // unfused: the next rays start from this point and the G-buffer stores its distance
+  const float3 position = mul_point_rn(inst.obj, add_rn(add_rn(mul_rn(p0, b0), mul_rn(p1, b1)), mul_rn(p2, b2)));
+  // unfused, in the shader's order: the G-buffer stores this normal
+  float3 normal = normalize_rn(add_rn(add_rn(mul_rn(n0, b0), mul_rn(n1, b1)), mul_rn(n2, b2)));
   if (isinf(normal.x) || isnan(normal.x)) normal = f3(0.f, 1.f, 0.f);
   const float3 c0 = f3(inst.nrm[0].x, inst.nrm[0].y, inst.nrm[0].z);
   const float3 c1 = f3(inst.nrm[1].x, inst.nrm[1].y, inst.nrm[1].z);
   const float3 c2 = f3(inst.nrm[2].x, inst.nrm[2].y, inst.nrm[2].z);
-  normal = normalize(c0 * normal.x + c1 * normal.y + c2 * normal.z);
+  normal = normalize_rn(add_rn(add_rn(mul_rn(c0, normal.x), mul_rn(c1, normal.y)), mul_rn(c2, normal.z)));
   if (t0.x == t1.x && t0.y == t1.y) t1.x += eps;
   if (t0.x == t2.x && t0.y == t2.y) t2.y += eps;
   if (t1.x == t2.x && t1.y == t2.y) {

@@ -1394,7 +1394,7 @@ __global__ void PBRT_SHADE_BOUNDS k_shade(SceneView sc, const FrameParams* __res
         al = make_float4(alb.x, alb.y, alb.z, al.w);
         q.prim_key[p] = hit_key;
         if (fp.write_gbuffer) {
-          g.depth[p] = length(position - prev);
+          g.depth[p] = length_rn(position - prev);
           g.normal[p] = make_float2(acosf(si.normal.z), atan2f(si.normal.y, si.normal.x));
           const float cat = (float)category / 255.0f;
           g.material[p] = make_uchar4(f2u8(cat), 0, 0, 0);
