@@ -116,65 +116,58 @@ PBRT_D bool alpha_accept_call(const SceneView& sc, uint32_t inst_id, uint32_t pr
 }
 
 // Per-ray traversal state: the node to visit next, the short stack of node
-// groups (child base, inner mask << 8 | remaining hits) and the best hit.
+// groups (child base, inner mask << 8 | remaining hits), the triangles of the
+// last node visited that wait for their test, and the best hit.
 struct TravState {
   uint32_t node;
   int sp;
   int best_tri;  // BVH-order triangle slot, -1 = miss
   float tbest, bu, bv;
   uint32_t best_key;
-  uint32_t tri_base, tri_mask;  // deferred triangles of the last node visited (kTraversalDeferTris)
+  uint32_t tri_base, tri_mask;  // pending triangles: slots tri_base + bit of tri_mask
 };
 constexpr uint32_t kNoNode = 0xffffffffu;
 
-// Traversal stack: the first kSmemStack entries of each lane live in shared
-// memory (a column per thread of a 128-thread CTA), deeper ones in local
-// memory. Typical depths stay in shared memory; with every entry in local
-// memory, 32 resident warps' stacks overflow L1 and each push and pop goes
-// to L2.
-#ifndef PBRT_SMEM_STACK
-#define PBRT_SMEM_STACK 0
-#endif
-constexpr int kSmemStack = PBRT_SMEM_STACK;
+// Traversal stack in local memory (per lane; interleaved across lanes by the
+// hardware). Shallow at the depths of these trees: pushes and pops hit L1.
 constexpr int kTraverseThreads = 128;
 struct TravStack {
-  uint2* sm;  // this lane's column: sm[i * kTraverseThreads]
-  uint2 local[kStackSize - kSmemStack];
-  PBRT_D void put(int i, uint2 v) {
-    if (i < kSmemStack) sm[i * kTraverseThreads] = v;
-    else local[i - kSmemStack] = v;
-  }
-  PBRT_D uint2 get(int i) const { return i < kSmemStack ? sm[i * kTraverseThreads] : local[i - kSmemStack]; }
+  uint2 local[kStackSize];
+  PBRT_D void put(int i, uint2 v) { local[i] = v; }
+  PBRT_D uint2 get(int i) const { return local[i]; }
 };
 
-// Traversal step shape. 0: a node visit tests the triangles of every hit
-// leaf child at once. 1: a node visit records them as a mask and the lane
-// tests one triangle per step until the mask is empty, so lanes of a warp
-// doing node visits and lanes doing triangle tests each do one unit per step
-// (the triangle/node separation of Ylitie, Karras & Laine, HPG 2017).
-#ifndef PBRT_TRAVERSAL_DEFER_TRIS
-#define PBRT_TRAVERSAL_DEFER_TRIS 1
-#endif
-constexpr int kTraversalDeferTris = PBRT_TRAVERSAL_DEFER_TRIS;
-// Shape 2: a lane postpones its triangles while fewer than 1 / PBRT_DEFER_SHARE
-// of the busy lanes have triangles to test.
-#ifndef PBRT_DEFER_SHARE
-#define PBRT_DEFER_SHARE 4
-#endif
-// L1 prefetch of the next node and of the first deferred triangle at the
-// end of a node visit (build knob).
-#ifndef PBRT_TRAVERSE_PREFETCH
-#define PBRT_TRAVERSE_PREFETCH 0
-#endif
-constexpr int kTraversePrefetch = PBRT_TRAVERSE_PREFETCH;
+// The entry / exit distances of the three slabs; three-input min / max.
+PBRT_D float fmax3f(float a, float b, float c) { return fmaxf(fmaxf(a, b), c); }
+PBRT_D float fmin3f(float a, float b, float c) { return fminf(fminf(a, b), c); }
+// byte k of w as a float (k is a constant once the child loop is unrolled)
+PBRT_D float byte_to_float(uint32_t w, int k) { return (float)((w >> (8 * k)) & 0xffu); }
+// Bits 0, 8, 16, 24 of x -> bits 0..3.
+PBRT_D uint32_t gather_byte_lsbs(uint32_t x) { return ((x * 0x204081u) >> 21) & 0xFu; }
+// 8-bit mask of the slots whose meta byte is a leaf (triangle count 1..3 in bits 5-6).
+PBRT_D uint32_t leaf_slots(uint32_t meta_lo, uint32_t meta_hi) {
+  const uint32_t c0 = (meta_lo >> 5) & 0x03030303u, c1 = (meta_hi >> 5) & 0x03030303u;
+  return gather_byte_lsbs((c0 | (c0 >> 1)) & 0x01010101u) | (gather_byte_lsbs((c1 | (c1 >> 1)) & 0x01010101u) << 4);
+}
+// Moves bit s of an 8-bit mask to bit s ^ oct.
+PBRT_D uint32_t octant_permute(uint32_t m, int oct) {
+  if (oct & 1) m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
+  if (oct & 2) m = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
+  if (oct & 4) m = ((m & 0x0Fu) << 4) | ((m >> 4) & 0x0Fu);
+  return m;
+}
 
-// Visits st.node: box-tests its children, intersects the triangles of the
-// leaf children that are hit, and moves to the nearest inner child (octant
-// order) or to the next entry of the stack. Returns false when the ray is
-// finished (stack empty, or -- for ANY_HIT -- an accepted hit).
-template <bool ANY_HIT>
-PBRT_D bool visit_node(const SceneView& sc, const RayPre& r, float tmin, TravState& st, TravStack& stack, int& err,
-                       uint32_t& n_nodes, uint32_t& n_tris) {
+// Node visit: box-tests st.node's children, records the triangles of the hit
+// leaf children in st.tri_mask and moves to the next node -- the nearest hit
+// inner child (octant order), else the next entry of the stack, else kNoNode.
+// Each axis's near and far quantised plane words are chosen once per node by
+// the sign of the ray's reciprocal direction (for a positive scale the fma of
+// the smaller plane is the smaller t, so this is the per-child min / max, bit
+// for bit); the hits are collected as an 8-bit mask and classified once per
+// node (inner children: the node's inner mask moved to octant order; leaves:
+// a mask built from the meta bytes' count fields).
+PBRT_D void visit_node(const SceneView& sc, const RayPre& r, float tmin, TravState& st, TravStack& stack, int& err,
+                       uint32_t& n_nodes) {
   const float4* nodes4 = reinterpret_cast<const float4*>(sc.nodes);
   const uint32_t node = st.node;
   ++n_nodes;
@@ -192,160 +185,6 @@ PBRT_D bool visit_node(const SceneView& sc, const RayPre& r, float tmin, TravSta
   const float scx = __uint_as_float(((emi >> 0) & 0xffu) << 23) * r.inv.x;
   const float scy = __uint_as_float(((emi >> 8) & 0xffu) << 23) * r.inv.y;
   const float scz = __uint_as_float(((emi >> 16) & 0xffu) << 23) * r.inv.z;
-  uint32_t inner = 0, leaves = 0;
-#pragma unroll
-  for (int s = 0; s < 8; ++s) {
-    const int sh = 8 * (s & 3);
-    const uint32_t meta = ((s < 4 ? meta_lo : meta_hi) >> sh) & 0xffu;
-    const float lx = (float)((__float_as_uint(s < 4 ? n2.x : n2.y) >> sh) & 0xffu);
-    const float ly = (float)((__float_as_uint(s < 4 ? n2.z : n2.w) >> sh) & 0xffu);
-    const float lz = (float)((__float_as_uint(s < 4 ? n3.x : n3.y) >> sh) & 0xffu);
-    const float hx = (float)((__float_as_uint(s < 4 ? n3.z : n3.w) >> sh) & 0xffu);
-    const float hy = (float)((__float_as_uint(s < 4 ? n4.x : n4.y) >> sh) & 0xffu);
-    const float hz = (float)((__float_as_uint(s < 4 ? n4.z : n4.w) >> sh) & 0xffu);
-    const float tx0 = fmaf(lx, scx, adx), tx1 = fmaf(hx, scx, adx);
-    const float ty0 = fmaf(ly, scy, ady), ty1 = fmaf(hy, scy, ady);
-    const float tz0 = fmaf(lz, scz, adz), tz1 = fmaf(hz, scz, adz);
-    float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
-    float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), st.tbest));
-    // widened by a few ulp: the quantised boxes are conservative, the slab
-    // arithmetic must not undo that
-    tn = tn - fabsf(tn) * 4e-7f;
-    tf = tf + fabsf(tf) * 4e-7f;
-    const bool hit = meta != 0 && tn <= tf;
-    if (hit) {
-      if (meta & 0x80u) inner |= 1u << (s ^ r.oct);
-      else leaves |= 1u << s;
-    }
-  }
-  while (leaves) {
-    const int s = __ffs(leaves) - 1;
-    leaves &= leaves - 1;
-    const uint32_t meta = ((s < 4 ? meta_lo : meta_hi) >> (8 * (s & 3))) & 0xffu;
-    const uint32_t cnt = meta >> 5, off = meta & 31u;
-    for (uint32_t k = 0; k < cnt; ++k) {
-      const uint32_t ti = tri_base + off + k;
-      const float4 a = __ldg(sc.tris + 3 * ti), b = __ldg(sc.tris + 3 * ti + 1), c = __ldg(sc.tris + 3 * ti + 2);
-      ++n_tris;
-      float t, u, v;
-      if (!tri_intersect(r, a, b, c, tmin, t, u, v)) continue;
-      const uint32_t key = __float_as_uint(a.w);
-      if (!(t < st.tbest || (t == st.tbest && key < st.best_key))) continue;
-      if (sc.any_alpha && !alpha_accept_call(sc, __float_as_uint(b.w), __float_as_uint(c.w), u, v)) continue;
-      st.best_tri = (int)ti;
-      st.tbest = t;
-      st.bu = u;
-      st.bv = v;
-      st.best_key = key;
-      if (ANY_HIT) return false;
-    }
-  }
-  if (inner) {
-    const int k = __ffs(inner) - 1;
-    inner &= inner - 1;
-    const int s = k ^ r.oct;
-    if (inner) {
-      if (st.sp == kStackSize) {
-        err = 1;
-        return false;
-      }
-      stack.put(st.sp++, make_uint2(child_base, (imask << 8) | inner));
-    }
-    st.node = child_base + __popc(imask & ((1u << s) - 1u));
-    return true;
-  }
-  if (st.sp == 0) return false;
-  uint2 g = stack.get(--st.sp);
-  uint32_t m = g.y & 0xffu;
-  const uint32_t im = g.y >> 8;
-  const int k = __ffs(m) - 1;
-  m &= m - 1;
-  const int s = k ^ r.oct;
-  if (m) stack.put(st.sp++, make_uint2(g.x, (im << 8) | m));
-  st.node = g.x + __popc(im & ((1u << s) - 1u));
-  return true;
-}
-
-// Slab-test shape (build knobs). PBRT_NEARFAR: pick each axis's near and
-// far quantised planes once per node by the sign of the ray's reciprocal
-// direction (the fma of a smaller plane gives the smaller t for a positive
-// scale, so this is the min / max of the pair, bit for bit), instead of a
-// min and a max per axis and child. PBRT_MINMAX3: the entry / exit
-// distances with three-input min / max.
-#ifndef PBRT_NEARFAR
-#define PBRT_NEARFAR 1
-#endif
-#ifndef PBRT_MINMAX3
-#define PBRT_MINMAX3 0
-#endif
-// PBRT_HITMASK: collect the children's box hits as an 8-bit mask and
-// classify it once per node (inner children: the node's inner mask, moved
-// to octant order by three conditional bit swaps; leaves: a mask made from
-// the meta bytes' triangle-count fields) instead of per child.
-#ifndef PBRT_HITMASK
-#define PBRT_HITMASK 1
-#endif
-// byte k of w as a float (k is a constant once the child loop is unrolled;
-// measured faster than building 2^23 + byte with a byte permute and
-// subtracting 2^23)
-PBRT_D float byte_to_float(uint32_t w, int k) { return (float)((w >> (8 * k)) & 0xffu); }
-// Bits 0, 8, 16, 24 of x -> bits 0..3.
-PBRT_D uint32_t gather_byte_lsbs(uint32_t x) { return ((x * 0x204081u) >> 21) & 0xFu; }
-// 8-bit mask of the slots whose meta byte is a leaf (triangle count 1..3 in bits 5-6).
-PBRT_D uint32_t leaf_slots(uint32_t meta_lo, uint32_t meta_hi) {
-  const uint32_t c0 = (meta_lo >> 5) & 0x03030303u, c1 = (meta_hi >> 5) & 0x03030303u;
-  return gather_byte_lsbs((c0 | (c0 >> 1)) & 0x01010101u) | (gather_byte_lsbs((c1 | (c1 >> 1)) & 0x01010101u) << 4);
-}
-// Moves bit s of an 8-bit mask to bit s ^ oct.
-PBRT_D uint32_t octant_permute(uint32_t m, int oct) {
-  if (oct & 1) m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
-  if (oct & 2) m = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
-  if (oct & 4) m = ((m & 0x0Fu) << 4) | ((m >> 4) & 0x0Fu);
-  return m;
-}
-PBRT_D float fmax3f(float a, float b, float c) {
-#if PBRT_MINMAX3
-  float r;
-  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
-  return r;
-#else
-  return fmaxf(fmaxf(a, b), c);
-#endif
-}
-PBRT_D float fmin3f(float a, float b, float c) {
-#if PBRT_MINMAX3
-  float r;
-  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
-  return r;
-#else
-  return fminf(fminf(a, b), c);
-#endif
-}
-
-// Deferred form: box-tests st.node's children, records the triangles of the
-// hit leaf children in st.tri_mask and moves to the next node (kNoNode when
-// the stack is empty). The ray is finished when both are exhausted.
-template <bool POP>
-PBRT_D void visit_node_deferred(const SceneView& sc, const RayPre& r, float tmin, TravState& st, TravStack& stack,
-                                int& err, uint32_t& n_nodes) {
-  const float4* nodes4 = reinterpret_cast<const float4*>(sc.nodes);
-  const uint32_t node = st.node;
-  ++n_nodes;
-  const float4 n0 = __ldg(nodes4 + 5 * node + 0);
-  const float4 n1 = __ldg(nodes4 + 5 * node + 1);
-  const float4 n2 = __ldg(nodes4 + 5 * node + 2);
-  const float4 n3 = __ldg(nodes4 + 5 * node + 3);
-  const float4 n4 = __ldg(nodes4 + 5 * node + 4);
-  const uint32_t emi = __float_as_uint(n0.w);
-  const uint32_t imask = emi >> 24;
-  const uint32_t child_base = __float_as_uint(n1.x), tri_base = __float_as_uint(n1.y);
-  const uint32_t meta_lo = __float_as_uint(n1.z), meta_hi = __float_as_uint(n1.w);
-  const float adx = (n0.x - r.o.x) * r.inv.x, ady = (n0.y - r.o.y) * r.inv.y, adz = (n0.z - r.o.z) * r.inv.z;
-  const float scx = __uint_as_float(((emi >> 0) & 0xffu) << 23) * r.inv.x;
-  const float scy = __uint_as_float(((emi >> 8) & 0xffu) << 23) * r.inv.y;
-  const float scz = __uint_as_float(((emi >> 16) & 0xffu) << 23) * r.inv.z;
-  uint32_t inner = 0, tris = 0, hitm = 0;
-#if PBRT_NEARFAR
   // near / far plane words: lo for a positive reciprocal, hi for a negative one
   const bool sx = scx < 0.f, sy = scy < 0.f, sz = scz < 0.f;
   const uint32_t lx0 = __float_as_uint(n2.x), lx1 = __float_as_uint(n2.y), ly0 = __float_as_uint(n2.z),
@@ -355,12 +194,9 @@ PBRT_D void visit_node_deferred(const SceneView& sc, const RayPre& r, float tmin
   const uint32_t nx0 = sx ? hx0 : lx0, nx1 = sx ? hx1 : lx1, fx0 = sx ? lx0 : hx0, fx1 = sx ? lx1 : hx1;
   const uint32_t ny0 = sy ? hy0 : ly0, ny1 = sy ? hy1 : ly1, fy0 = sy ? ly0 : hy0, fy1 = sy ? ly1 : hy1;
   const uint32_t nz0 = sz ? hz0 : lz0, nz1 = sz ? hz1 : lz1, fz0 = sz ? lz0 : hz0, fz1 = sz ? lz1 : hz1;
-#endif
+  uint32_t hitm = 0;
 #pragma unroll
   for (int s = 0; s < 8; ++s) {
-    const int sh = 8 * (s & 3);
-    const uint32_t meta = ((s < 4 ? meta_lo : meta_hi) >> sh) & 0xffu;
-#if PBRT_NEARFAR
     const int K = s & 3;
     const float tnx = fmaf(byte_to_float(s < 4 ? nx0 : nx1, K), scx, adx);
     const float tny = fmaf(byte_to_float(s < 4 ? ny0 : ny1, K), scy, ady);
@@ -370,34 +206,14 @@ PBRT_D void visit_node_deferred(const SceneView& sc, const RayPre& r, float tmin
     const float tfz = fmaf(byte_to_float(s < 4 ? fz0 : fz1, K), scz, adz);
     float tn = fmaxf(fmax3f(tnx, tny, tnz), tmin);
     float tf = fminf(fmin3f(tfx, tfy, tfz), st.tbest);
-#else
-    const float lx = (float)((__float_as_uint(s < 4 ? n2.x : n2.y) >> sh) & 0xffu);
-    const float ly = (float)((__float_as_uint(s < 4 ? n2.z : n2.w) >> sh) & 0xffu);
-    const float lz = (float)((__float_as_uint(s < 4 ? n3.x : n3.y) >> sh) & 0xffu);
-    const float hx = (float)((__float_as_uint(s < 4 ? n3.z : n3.w) >> sh) & 0xffu);
-    const float hy = (float)((__float_as_uint(s < 4 ? n4.x : n4.y) >> sh) & 0xffu);
-    const float hz = (float)((__float_as_uint(s < 4 ? n4.z : n4.w) >> sh) & 0xffu);
-    const float tx0 = fmaf(lx, scx, adx), tx1 = fmaf(hx, scx, adx);
-    const float ty0 = fmaf(ly, scy, ady), ty1 = fmaf(hy, scy, ady);
-    const float tz0 = fmaf(lz, scz, adz), tz1 = fmaf(hz, scz, adz);
-    float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
-    float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), st.tbest));
-#endif
+    // widened by a few ulp: the quantised boxes are conservative, the slab
+    // arithmetic must not undo that
     tn = tn - fabsf(tn) * 4e-7f;
     tf = tf + fabsf(tf) * 4e-7f;
-#if PBRT_HITMASK
     hitm |= (tn <= tf ? 1u : 0u) << s;
-    (void)meta;
-#else
-    const bool hit = meta != 0 && tn <= tf;
-    if (hit) {
-      if (meta & 0x80u) inner |= 1u << (s ^ r.oct);
-      else tris |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);  // <= 8 leaves x 3 triangles: bits 0..23
-    }
-#endif
   }
-#if PBRT_HITMASK
-  inner = octant_permute(hitm & imask, r.oct);
+  uint32_t inner = octant_permute(hitm & imask, r.oct);
+  uint32_t tris = 0;
   uint32_t lh = hitm & leaf_slots(meta_lo, meta_hi);
   while (lh) {
     const int s = __ffs(lh) - 1;
@@ -405,13 +221,8 @@ PBRT_D void visit_node_deferred(const SceneView& sc, const RayPre& r, float tmin
     const uint32_t meta = ((s < 4 ? meta_lo : meta_hi) >> (8 * (s & 3))) & 0xffu;
     tris |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);  // <= 8 leaves x 3 triangles: bits 0..23
   }
-#endif
   st.tri_base = tri_base;
   st.tri_mask = tris;
-  if (kTraversePrefetch && tris) {  // the first triangle this lane tests next
-    const float4* t = sc.tris + 3 * (tri_base + (uint32_t)(__ffs(tris) - 1));
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(t));
-  }
   if (inner) {
     const int k = __ffs(inner) - 1;
     inner &= inner - 1;
@@ -426,14 +237,9 @@ PBRT_D void visit_node_deferred(const SceneView& sc, const RayPre& r, float tmin
       stack.put(st.sp++, make_uint2(child_base, (imask << 8) | inner));
     }
     st.node = child_base + __popc(imask & ((1u << s) - 1u));
-    if (kTraversePrefetch) {  // the next node's 80 bytes, while the triangles are tested
-      const char* nd = reinterpret_cast<const char*>(sc.nodes) + (size_t)st.node * 80;
-      asm volatile("prefetch.global.L1 [%0];" ::"l"(nd));
-      asm volatile("prefetch.global.L1 [%0];" ::"l"(nd + 64));
-    }
     return;
   }
-  if (!POP || st.sp == 0) {
+  if (st.sp == 0) {
     st.node = kNoNode;
     return;
   }
@@ -447,28 +253,8 @@ PBRT_D void visit_node_deferred(const SceneView& sc, const RayPre& r, float tmin
   st.node = g.x + __popc(im & ((1u << s) - 1u));
 }
 
-// Postponing form (mode 2): a node visit leaves st.node = kNoNode when no
-// inner child is hit instead of popping; the pop is a step of its own, and a
-// stack entry with bit 31 set is a postponed triangle group.
-PBRT_D void pop_group(const RayPre& r, TravState& st, TravStack& stack) {
-  uint2 g = stack.get(--st.sp);
-  if (g.y & 0x80000000u) {
-    st.tri_base = g.x;
-    st.tri_mask = g.y & 0x7fffffffu;
-    return;
-  }
-  uint32_t m = g.y & 0xffu;
-  const uint32_t im = g.y >> 8;
-  const int k = __ffs(m) - 1;
-  m &= m - 1;
-  const int s = k ^ r.oct;
-  if (m) stack.put(st.sp++, make_uint2(g.x, (im << 8) | m));
-  st.node = g.x + __popc(im & ((1u << s) - 1u));
-}
-
-// Tests the lowest triangle of st.tri_mask. Returns true for an accepted
-// any-hit (the ray is finished). The runtime form (any_hit a lane flag) lets
-// a warp holding closest-hit and shadow rays run one copy of the test.
+// Tests the lowest triangle of st.tri_mask (the packet traversal's form).
+// Returns true for an accepted any-hit (the ray is finished).
 PBRT_D bool test_one_triangle_rt(const SceneView& sc, const RayPre& r, float tmin, TravState& st, bool any_hit) {
   const int b = __ffs(st.tri_mask) - 1;
   st.tri_mask &= st.tri_mask - 1;
@@ -486,24 +272,135 @@ PBRT_D bool test_one_triangle_rt(const SceneView& sc, const RayPre& r, float tmi
   st.best_key = key;
   return any_hit;
 }
-template <bool ANY_HIT>
-PBRT_D bool test_one_triangle(const SceneView& sc, const RayPre& r, float tmin, TravState& st, uint32_t& n_tris) {
-  const int b = __ffs(st.tri_mask) - 1;
-  st.tri_mask &= st.tri_mask - 1;
-  const uint32_t ti = st.tri_base + (uint32_t)b;
-  const float4 a = __ldg(sc.tris + 3 * ti), bb = __ldg(sc.tris + 3 * ti + 1), c = __ldg(sc.tris + 3 * ti + 2);
-  ++n_tris;
-  float t, u, v;
-  if (!tri_intersect(r, a, bb, c, tmin, t, u, v)) return false;
-  const uint32_t key = __float_as_uint(a.w);
-  if (!(t < st.tbest || (t == st.tbest && key < st.best_key))) return false;
-  if (sc.any_alpha && !alpha_accept_call(sc, __float_as_uint(bb.w), __float_as_uint(c.w), u, v)) return false;
-  st.best_tri = (int)ti;
-  st.tbest = t;
-  st.bu = u;
-  st.bv = v;
-  st.best_key = key;
-  return ANY_HIT;
+
+// Cooperative triangle tests. A lane's node visit leaves 0 to 24 triangles
+// to test, and only about a quarter of a warp's lanes have some at any step,
+// so a per-lane triangle step runs with most lanes idle. Instead, after each
+// step of node visits the warp lists every pending (ray, triangle) pair --
+// lane i's pairs are numbers excl_i .. excl_i + count_i - 1 of an exclusive
+// scan of the per-lane counts -- and tests them 32 at a time, lane j taking
+// pair j of each pass: its owner is the largest i with excl_i <= j (a binary
+// search over the scan, held in registers and read with shuffles), the
+// triangle the owner's (j - excl_i)-th pending bit. The owner's ray (origin,
+// the watertight test's shear and axis permutation, tmin, any-hit flag) is
+// read from its record in shared memory; an accepted hit lowers the owner's
+// best (t bits << 32 | triangle key) with a 64-bit shared-memory atomicMin --
+// the nearest hit, ties to the lowest key, as the serial order gives -- and
+// the lane holding the winning pair writes its u, v and triangle slot. The
+// closest hit depends only on which triangles are tested, so the result is
+// the serial traversal's, bit for bit.
+struct TriRay {
+  float ox, oy, oz, tmin;
+  float sx, sy, sz;
+  uint32_t perm;  // kx | ky << 2 | kz << 4 | any-hit << 6
+};
+struct TriBest {
+  unsigned long long best;  // (t bits << 32) | key of the nearest accepted triangle
+  float u, v;
+  uint32_t tri;  // its BVH-order slot
+  uint32_t pad;
+};
+PBRT_D unsigned long long pack_hit(float t, uint32_t key) {
+  return ((unsigned long long)__float_as_uint(t) << 32) | key;  // t > 0: the bits order as the values
+}
+PBRT_D TriRay make_tri_ray(const RayPre& r, float tmin, bool any) {
+  TriRay t;
+  t.ox = r.o.x;
+  t.oy = r.o.y;
+  t.oz = r.o.z;
+  t.tmin = tmin;
+  t.sx = r.Sx;
+  t.sy = r.Sy;
+  t.sz = r.Sz;
+  t.perm = (uint32_t)r.kx | ((uint32_t)r.ky << 2) | ((uint32_t)r.kz << 4) | (any ? 64u : 0u);
+  return t;
+}
+// The watertight test (tri_intersect) with the ray read from its record.
+PBRT_D bool tri_intersect_rec(const TriRay& q, float4 a, float4 b, float4 c, float& t, float& u, float& v) {
+  RayPre r;
+  r.o = f3(q.ox, q.oy, q.oz);
+  r.kx = (int)(q.perm & 3u);
+  r.ky = (int)((q.perm >> 2) & 3u);
+  r.kz = (int)((q.perm >> 4) & 3u);
+  r.Sx = q.sx;
+  r.Sy = q.sy;
+  r.Sz = q.sz;
+  return tri_intersect(r, a, b, c, q.tmin, t, u, v);
+}
+// Tests every pending triangle of the warp's rays (all 32 lanes call it).
+// Returns, per lane, whether its any-hit ray found an accepted triangle.
+PBRT_D bool coop_triangles(const SceneView& sc, TravState& st, const TriRay* rays, TriBest* best, int lane,
+                           uint32_t& n_tris, uint32_t& n_tris_any) {
+  const uint32_t cnt = __popc(st.tri_mask);
+  uint32_t incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(kFullMask, incl, o);
+    if (lane >= o) incl += y;
+  }
+  const uint32_t total = __shfl_sync(kFullMask, incl, 31);
+  if (total == 0) return false;
+  const uint32_t excl = incl - cnt;
+  const unsigned long long start = pack_hit(st.tbest, st.best_key);
+  if (cnt) best[lane].best = start;
+  __syncwarp();
+  for (uint32_t base = 0; base < total; base += 32) {
+    const uint32_t j = base + (uint32_t)lane;
+    int owner = 0;  // the largest lane i with excl_i <= j
+#pragma unroll
+    for (int step = 16; step >= 1; step >>= 1) {
+      const uint32_t e = __shfl_sync(kFullMask, excl, owner + step);
+      if (e <= j) owner += step;
+    }
+    const uint32_t omask = __shfl_sync(kFullMask, st.tri_mask, owner);
+    const uint32_t obase = __shfl_sync(kFullMask, st.tri_base, owner);
+    const uint32_t oexcl = __shfl_sync(kFullMask, excl, owner);
+    bool won = false;
+    unsigned long long cand = 0;
+    float cu = 0.f, cv = 0.f;
+    uint32_t ti = 0;
+    if (j < total) {
+      ti = obase + __fns(omask, 0, (int)(j - oexcl) + 1);
+      const TriRay q = rays[owner];
+      const bool any = (q.perm & 64u) != 0;
+      n_tris += any ? 0u : 1u;
+      n_tris_any += any ? 1u : 0u;
+      const float4 a = __ldg(sc.tris + 3 * ti), b = __ldg(sc.tris + 3 * ti + 1), c = __ldg(sc.tris + 3 * ti + 2);
+      float t, u, v;
+      if (tri_intersect_rec(q, a, b, c, t, u, v)) {
+        cand = pack_hit(t, __float_as_uint(a.w));
+        if (cand < *((volatile unsigned long long*)&best[owner].best) &&
+            (!sc.any_alpha || alpha_accept_call(sc, __float_as_uint(b.w), __float_as_uint(c.w), u, v))) {
+          atomicMin(&best[owner].best, cand);
+          won = true;
+          cu = u;
+          cv = v;
+        }
+      }
+    }
+    __syncwarp();
+    if (won && best[owner].best == cand) {  // the keys are distinct: one winner per owner
+      best[owner].u = cu;
+      best[owner].v = cv;
+      best[owner].tri = ti;
+    }
+    __syncwarp();
+  }
+  bool accepted = false;
+  if (cnt) {
+    const TriBest b = best[lane];
+    if (b.best != start) {
+      st.tbest = __uint_as_float((uint32_t)(b.best >> 32));
+      st.best_key = (uint32_t)b.best;
+      st.bu = b.u;
+      st.bv = b.v;
+      st.best_tri = (int)b.tri;
+      accepted = (rays[lane].perm & 64u) != 0;
+    }
+    st.tri_mask = 0;
+  }
+  __syncwarp();
+  return accepted;
 }
 
 // ---------------------------------------------------------------------------
@@ -740,14 +637,12 @@ struct QueryIO {
   uint32_t* errflag;
 };
 
-// Traversal CTAs resident per SM the register allocation targets (a build
-// knob; 8 x 128 threads at <= 64 registers).
-#ifndef PBRT_TRAVERSE_MIN_BLOCKS
-#define PBRT_TRAVERSE_MIN_BLOCKS 8
-#endif
+// Traversal CTAs resident per SM the register allocation targets (8 x 128
+// threads at <= 64 registers).
+constexpr int kTraverseMinBlocks = 8;
 template <int MODE>
-__global__ void __launch_bounds__(128, PBRT_TRAVERSE_MIN_BLOCKS) k_traverse(SceneView sc, Queues q, Counters* c, int k,
-                                                                          QueryIO io) {
+__global__ void __launch_bounds__(128, kTraverseMinBlocks) k_traverse(SceneView sc, Queues q, Counters* c, int k,
+                                                                    QueryIO io) {
   // MODE 4: the closest-hit rays of queue k&1 followed by the shadow rays
   // of the previous bounce, in one launch (one work counter over both)
   constexpr bool ANY = (MODE == 1 || MODE == 3);
@@ -779,9 +674,12 @@ __global__ void __launch_bounds__(128, PBRT_TRAVERSE_MIN_BLOCKS) k_traverse(Scen
     dir = io.dir;
     work = io.work;
   }
-  __shared__ uint2 s_stack[kSmemStack > 0 ? kSmemStack * kTraverseThreads : 1];
+  // per-lane ray records and best hits of the cooperative triangle tests
+  __shared__ TriRay s_rays[kTraverseThreads];
+  __shared__ TriBest s_best[kTraverseThreads];
+  TriRay* const w_rays = s_rays + (threadIdx.x & ~31);
+  TriBest* const w_best = s_best + (threadIdx.x & ~31);
   TravStack stack;
-  stack.sm = s_stack + threadIdx.x;
   TravState st;
   RayPre r;
   float tmin = 0.f;
@@ -791,6 +689,7 @@ __global__ void __launch_bounds__(128, PBRT_TRAVERSE_MIN_BLOCKS) k_traverse(Scen
   int err = 0;
   uint32_t nn = 0, nt = 0, nn_s = 0, nt_s = 0;
   bool lane_any = ANY;
+  st.tri_mask = 0;
   while (true) {
     // ---- refill idle lanes from the warp's batch
     unsigned need = __ballot_sync(kFullMask, idx < 0);
@@ -825,6 +724,7 @@ __global__ void __launch_bounds__(128, PBRT_TRAVERSE_MIN_BLOCKS) k_traverse(Scen
         }
         r = ray_pre(f3(o.x, o.y, o.z), f3(d.x, d.y, d.z));
         tmin = o.w;
+        w_rays[lane] = make_tri_ray(r, tmin, lane_any);
         st.node = 0;
         st.sp = 0;
         st.best_tri = -1;
@@ -837,55 +737,11 @@ __global__ void __launch_bounds__(128, PBRT_TRAVERSE_MIN_BLOCKS) k_traverse(Scen
       need = __ballot_sync(kFullMask, idx < 0);
     }
     if (__all_sync(kFullMask, idx < 0)) break;
-    // ---- one step of this lane's ray
-    if (kTraversalDeferTris == 2) {
-      // postpone triangles while fewer than a quarter of the busy lanes have some
-      const bool busy = idx >= 0;
-      const unsigned act = __ballot_sync(kFullMask, busy);
-      const unsigned trl = __ballot_sync(kFullMask, busy && st.tri_mask != 0);
-      if (!busy) continue;
-      if (st.tri_mask && st.node != kNoNode && PBRT_DEFER_SHARE * __popc(trl) < __popc(act) && st.sp < kStackSize) {
-        stack.put(st.sp++, make_uint2(st.tri_base, st.tri_mask | 0x80000000u));
-        st.tri_mask = 0;
-      }
-      bool done = false;
-      if (st.tri_mask) {
-        if (MODE == 4) done = lane_any ? test_one_triangle<true>(sc, r, tmin, st, nt_s)
-                                       : test_one_triangle<false>(sc, r, tmin, st, nt);
-        else done = test_one_triangle<ANY>(sc, r, tmin, st, nt);
-      } else if (st.node != kNoNode) {
-        visit_node_deferred<false>(sc, r, tmin, st, stack, err, (MODE == 4 && lane_any) ? nn_s : nn);
-      } else {
-        pop_group(r, st, stack);
-      }
-      if (!done && (st.tri_mask || st.node != kNoNode || st.sp > 0)) continue;
-    } else if (MODE == 4) {
-      if (idx < 0) continue;
-      if (st.tri_mask) {
-        nt += lane_any ? 0u : 1u;
-        nt_s += lane_any ? 1u : 0u;
-        const bool acc = test_one_triangle_rt(sc, r, tmin, st, lane_any);
-        if (!acc && (st.tri_mask || st.node != kNoNode)) continue;
-      } else {
-        uint32_t one = 0;
-        visit_node_deferred<true>(sc, r, tmin, st, stack, err, one);
-        nn += lane_any ? 0u : one;
-        nn_s += lane_any ? one : 0u;
-        if (st.tri_mask || st.node != kNoNode) continue;
-      }
-    } else if (kTraversalDeferTris == 1) {
-      if (idx < 0) continue;
-      if (st.tri_mask) {
-        if (!test_one_triangle<ANY>(sc, r, tmin, st, nt) && (st.tri_mask || st.node != kNoNode)) continue;
-      } else {
-        visit_node_deferred<true>(sc, r, tmin, st, stack, err, nn);
-        if (st.tri_mask || st.node != kNoNode) continue;
-      }
-    } else if (idx < 0) {
-      continue;
-    } else if (visit_node<ANY>(sc, r, tmin, st, stack, err, nn, nt)) {
-      continue;
-    }
+    // ---- the triangles of the last node visits, the warp's lanes sharing them out
+    const bool accepted = coop_triangles(sc, st, w_rays, w_best, lane, nt, nt_s);
+    // ---- one node visit per busy lane
+    if (idx >= 0 && !accepted && st.node != kNoNode) visit_node(sc, r, tmin, st, stack, err, lane_any ? nn_s : nn);
+    if (idx < 0 || (!accepted && (st.node != kNoNode || st.tri_mask != 0))) continue;
     // ---- ray finished
     if (MODE == 0 || (MODE == 4 && !lane_any)) {
       // the hit's instance and primitive, read here where the triangle was
@@ -912,6 +768,7 @@ __global__ void __launch_bounds__(128, PBRT_TRAVERSE_MIN_BLOCKS) k_traverse(Scen
       io.hits[idx] = make_float4(st.tbest, st.bu, st.bv, __uint_as_float(key));
     }
     idx = -1;
+    st.tri_mask = 0;
   }
   if (MODE == 4) {
     warp_add64(&c->nodes_closest, nn);
@@ -922,8 +779,8 @@ __global__ void __launch_bounds__(128, PBRT_TRAVERSE_MIN_BLOCKS) k_traverse(Scen
     warp_add64(&c->nodes_closest, nn);
     warp_add64(&c->tris_closest, nt);
   } else if (MODE == 1) {
-    warp_add64(&c->nodes_shadow, nn);
-    warp_add64(&c->tris_shadow, nt);
+    warp_add64(&c->nodes_shadow, nn_s);
+    warp_add64(&c->tris_shadow, nt_s);
   }
   if (err) atomicOr((MODE <= 1 || MODE == 4) ? &c->error : io.errflag, 1u);
 }
@@ -938,7 +795,7 @@ __global__ void __launch_bounds__(128, PBRT_TRAVERSE_MIN_BLOCKS) k_traverse(Scen
 // primary rays); the closest hit is the same, as it depends only on which
 // triangles a ray tests, never on the order. Node visits are counted once
 // per warp (one fetch serves the 32 rays), triangle tests per ray.
-__global__ void __launch_bounds__(128, PBRT_TRAVERSE_MIN_BLOCKS) k_traverse_packet(SceneView sc, Queues q, Counters* c) {
+__global__ void __launch_bounds__(128, kTraverseMinBlocks) k_traverse_packet(SceneView sc, Queues q, Counters* c) {
   __shared__ uint2 s_stack[kTraverseThreads / 32][kStackSize];
   const int lane = threadIdx.x & 31;
   uint2* stk = s_stack[threadIdx.x >> 5];
