@@ -61,9 +61,14 @@ def parse():
     ap.add_argument("--sort-rays", action="store_true", help="sort extension / shadow rays before traversal")
     ap.add_argument("--separate-shadow", action="store_true",
                     help="trace shadow rays in their own launch (default: merged into the next bounce's launch)")
-    ap.add_argument("--workload", default="frame1080p", choices=["frame1080p", "batch64", "unet_layers"],
+    ap.add_argument("--workload", default="frame1080p", choices=["frame1080p", "batch64", "unet_layers", "full"],
                     help="batch64: 64 uneven render requests in one graph launch; unet_layers: per-convolution "
-                         "times of the U-Net (neither is the headline line)")
+                         "times of the U-Net; full: 4K 4 spp frames of a 4M-triangle scene (FP8 network, gate, "
+                         "BMFR with the FP64 re-solve) beside 16 concurrent 1080p requests (none of these is the "
+                         "headline line)")
+    ap.add_argument("--frames", type=int, default=60, help="full: frames of the camera path")
+    ap.add_argument("--relmse-frames", default="59", help="full: comma-separated frames whose relMSE is measured")
+    ap.add_argument("--full-ref-spp", type=int, default=1024, help="full: samples of each 4K relMSE reference")
     ap.add_argument("--layers", default="", help="unet_layers: comma-separated layer names (default: all 18)")
     ap.add_argument("--kernels", default="bf16_tcgen05,bf16_mma,fp8_tcgen05,fp8_mma",
                     help="unet_layers: comma-separated subset of bf16_tcgen05,bf16_mma,fp8_tcgen05,fp8_mma")
@@ -167,13 +172,15 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic(kernel: str):
-    """dram bytes per launch of `kernel` from a committed ncu summary, if any."""
+def profile_counters(kernel: str) -> dict:
+    """Per-launch ncu figures of `kernel` from the committed summary (DRAM and
+    L2 bytes, issue-slot use, lanes per instruction), if any."""
     p = ROOT / "profiles" / "ncu_traffic.json"
     if p.exists():
-        d = json.loads(p.read_text())
-        return d.get(kernel)
-    return None
+        d = json.loads(p.read_text()).get(kernel)
+        if isinstance(d, dict):
+            return d
+    return {}
 
 
 # ---------------------------------------------------------------------------
@@ -557,7 +564,8 @@ def run_gb300(args):
     per_launch_s = trav_ms / 1e3 / launches
     achieved = closest_bytes / launches / per_launch_s / 1e9
     peak, peak_kind = peaks()
-    traffic = profile_traffic("k_traverse")
+    counters = profile_counters("k_traverse")
+    traffic = counters.get("dram_bytes_per_launch")
     dominant = max(stages, key=stages.get)
     if rank == 0:
         steps = args.steps
@@ -593,6 +601,9 @@ def run_gb300(args):
                 "schedule": {"sort_rays": bool(args.sort_rays), "merge_shadow": not args.separate_shadow},
             },
             "grays_per_s": rays / (trace_ms / 1e3) / 1e9 * world,
+            # the same queries over the traversal kernels' time alone (packet,
+            # merged closest + shadow, last shadow launches of one profiled frame)
+            "traversal_grays_per_s": (prof.closest_rays + prof.shadow_rays) / (trav_ms / 1e3) / 1e9 * world,
             "rays_per_frame": rays / steps,
             "trace_ms_per_frame": trace_ms / steps,
             "stage_ms": {k: round(v, 4) for k, v in stages.items()},
@@ -607,6 +618,14 @@ def run_gb300(args):
                 "frac": achieved / peak,
                 "peak_source": peak_kind,
                 "traffic": traffic,
+                # the roof the traversal actually meets: instruction issue
+                # (ncu, per launch of one frame's traversal); the BVH and most
+                # triangle records stay in L2
+                "issue_active_pct": counters.get("issue_active_pct"),
+                "lanes_per_instruction": counters.get("lanes_per_instruction"),
+                "l2_bytes_per_launch": counters.get("l2_bytes_per_launch"),
+                "l2_pct_of_peak": counters.get("l2_pct_of_peak"),
+                "counters_source": counters.get("source"),
                 "bytes_per_ray": closest_bytes / max(1, prof.closest_rays + prof.shadow_rays),
                 "nodes_per_ray": (prof.closest_nodes + prof.shadow_nodes) / max(1, prof.closest_rays + prof.shadow_rays),
                 "tris_per_ray": (prof.closest_tris + prof.shadow_tris) / max(1, prof.closest_rays + prof.shadow_rays),
@@ -703,6 +722,163 @@ def run_batch(args):
                        "resolution": "log-uniform 256^2..1080p", "spp": "uniform {1,2,4,8,16}", "depth": "4-8",
                        "denoiser": "accumulate + BMFR 32x32 per request"}}
     print(json.dumps(line), flush=True)
+
+def run_full(args):
+    """The full chosen form: 3840x2160, 4 samples per pixel, max depth 8 with
+    Russian roulette after bounce 3, a seeded ~4M-triangle instanced field
+    with 32 lights, a 60-frame camera path; every frame traced 4 times and
+    accumulated, then BMFR 32x32 (FP64 re-solve on) and the kernel-predicting
+    network in FP8 with the per-tile gate falling back to BMFR; beside each
+    4K frame, 16 independent 1080p requests (own seeded scene, 1 spp,
+    accumulator + BMFR each) in one graph launch on a second stream. A step
+    is one 4K frame plus one submission of the 16 requests. relMSE of the
+    listed frames against an --full-ref-spp render of the same camera
+    (remodulated by the G-buffer albedo), beside BMFR's."""
+    import torch
+
+    from vulkanpbrt_gb300 import build as B
+
+    B.build()
+    import vulkanpbrt_gb300 as vp
+    from vulkanpbrt_gb300 import scene as S
+    from vulkanpbrt_gb300.camera import default_camera
+
+    W, H, spp = 3840, 2160, 4
+    t0 = time.perf_counter()
+    sc = S.instanced_field(seed=0, instances=8000, point_lights=30)
+    sh = vp.SceneHandle(sc)
+    info = sh.info()
+    g = vp.GBuffer(W, H)
+    illu = vp.IlluminationBufferDemodulatedFloat(W, H)
+    pipe = vp.PBRTPipeline(sh, g, illu, True, max_recursion_depth=args.max_depth, min_recursion_depth=args.min_depth)
+    accu = vp.Accumulator(g, illu, separate_matrices=True)
+    abuf, acc_illu = accu.accumulation_buffer, accu.accumulated_illumination
+    bmfr = vp.BMFR(W, H, 32, 32, g, acc_illu, abuf, 256, fp64_resolve=True)
+    neural = vp.NeuralDenoiser(W, H, g, acc_illu, fallback=bmfr, threshold=args.gate_threshold, tile=32,
+                               acc_buffer=abuf)
+    # the 16 concurrent 1080p requests
+    rng = np.random.default_rng(77)
+    batch, keep = vp.Batch(), []
+    for i in range(16):
+        rsc = batch_scene(rng, 9000 + i)
+        rsh = vp.SceneHandle(rsc)
+        rg, ri = vp.GBuffer(1920, 1080), vp.IlluminationBufferDemodulatedFloat(1920, 1080)
+        rp = vp.PBRTPipeline(rsh, rg, ri, True, max_recursion_depth=args.max_depth, min_recursion_depth=args.min_depth)
+        ra = vp.Accumulator(rg, ri, separate_matrices=True)
+        rb = vp.BMFR(1920, 1080, 32, 32, rg, ra.accumulated_illumination, ra.accumulation_buffer, 256)
+        cam = default_camera(1920, 1080)
+        rpc = vp.PushConstants(view_inverse=cam.inv_view, proj_inverse=cam.inv_proj, prev_view=cam.view,
+                               frame_number=1 + 37 * i)
+        batch.add(rp, rpc, spp=1, accumulator=ra, bmfr=rb,
+                  camera=vp.CameraMatrices(cam.view, cam.inv_view, cam.proj, cam.inv_proj))
+        keep.append((rsc, rsh, rg, ri, rp, ra, rb, rpc))
+    setup_s = time.perf_counter() - t0
+    main_s = torch.cuda.current_stream()
+    side_s = torch.cuda.Stream()
+    pc = vp.PushConstants()
+    cams = [orbit(sc, W, H, f, frames=args.frames) for f in range(args.frames)]
+    state = {"prev": cams[0]}
+
+    def frame(f, stream):
+        cam, prev = cams[f % args.frames], state["prev"]
+        sh_ = vp._abi.stream_handle(stream)
+        for s_ in range(spp):
+            pc.set(view_inverse=cam.inv_view, proj_inverse=cam.inv_proj, prev_view=(prev if s_ == 0 else cam).view,
+                   frame_number=f * spp + s_)
+            p_ = prev if s_ == 0 else cam
+            accu.set_camera_matrices(f * spp + s_, vp.CameraMatrices(cam.view, cam.inv_view, cam.proj, cam.inv_proj),
+                                     vp.CameraMatrices(p_.view, p_.inv_view))
+            pipe.trace(pc, stream)
+            vp.lib().pbrt_accumulator_dispatch(accu.ptr, sh_)
+            if s_ == spp - 1:
+                bmfr.dispatch(pc, stream)
+                neural.dispatch(pc, stream)
+            vp.lib().pbrt_accumulation_buffer_copy_to_back_images(abuf.ptr, g.ptr, acc_illu.ptr, sh_)
+        state["prev"] = cam
+
+    # warm-up: graphs, autotune of the network's kernels, FP8 calibration
+    frame(0, main_s)
+    neural.calibrate(main_s)
+    neural.set_precision(8)
+    batch.submit(side_s)
+    for f in range(1, 1 + max(1, args.warmup)):
+        frame(f, main_s)
+    torch.cuda.synchronize()
+    measure = {int(x) for x in args.relmse_frames.split(",") if x}
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    st0 = pipe.stats()
+    total_ms, per_frame, fp64_blocks, ratios, fallback = 0.0, [], [], [], []
+    quality = []
+    state["prev"] = cams[0]
+    for f in range(args.frames):
+        torch.cuda.synchronize()
+        ev0.record(main_s)
+        side_s.wait_event(ev0)
+        batch.submit(side_s)
+        frame(f, main_s)
+        done = torch.cuda.Event()
+        done.record(side_s)
+        main_s.wait_event(done)
+        ev1.record(main_s)
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        total_ms += ms
+        per_frame.append(ms)
+        n, r = bmfr.condition_stats(main_s)
+        fp64_blocks.append(n)
+        ratios.append(r)
+        fallback.append(neural.fallback_tiles(main_s))
+        if f in measure:
+            quality.append(dict(frame=f, **full_relmse(args, vp, pipe, g, illu, bmfr, neural, pc, main_s)))
+    st1 = pipe.stats()
+    rays = (st1.primary_rays - st0.primary_rays) + (st1.extension_rays - st0.extension_rays) + \
+        (st1.shadow_rays - st0.shadow_rays)
+    line = {
+        "metric": "4K 4spp denoised frames/s with 16 concurrent 1080p requests", "value": args.frames / (total_ms / 1e3),
+        "unit": "fps", "frames": args.frames, "ms_per_step": total_ms / args.frames,
+        "ms_per_step_max": max(per_frame), "requests_per_s": 16 * args.frames / (total_ms / 1e3),
+        "grays_per_s_4k": rays / (total_ms / 1e3) / 1e9,
+        "config": {"workload": "full chosen form", "width": W, "height": H, "spp": spp, "max_depth": args.max_depth,
+                   "min_depth": args.min_depth, "triangles": int(info.triangle_count), "lights": int(info.light_count),
+                   "instances": int(info.instance_count), "network": "FP8 e4m3 (input layer BF16)",
+                   "gate_threshold": args.gate_threshold, "bmfr": "32x32, FP64 re-solve above R-ratio 1e6",
+                   "requests": "16 x 1080p, 1 spp, accumulate + BMFR, own seeded scene each, one graph launch on a "
+                               "second stream beside each 4K frame"},
+        "fp64_blocks_per_frame_max": max(fp64_blocks), "largest_r_ratio": max(ratios),
+        "fallback_tiles_per_frame": {"min": min(fallback), "max": max(fallback), "tiles": int(
+            ((W + 31) // 32) * ((H + 31) // 32))},
+        "relmse": quality, "setup_s": setup_s,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def full_relmse(args, vp, pipe, g, illu, bmfr, neural, pc, stream):
+    """relMSE of the current frame's outputs (network as shown with the gate,
+    network alone, BMFR) against an --full-ref-spp render of the same camera."""
+    import torch
+
+    f = pc.value.frame_number
+    albedo = g.albedo.tensor()[..., :3].double() / 255.0
+    outs = {"bmfr": bmfr.denoised.tensor()[(f & 1) ^ 1][..., :3].double().clone(),
+            "neural": neural.denoised.tensor()[..., :3].double().clone()}
+    m = neural.fallback_mask.tensor()[..., 0].bool()
+    px = m.repeat_interleave(neural.tile, 0).repeat_interleave(neural.tile, 1)[:g.height, :g.width]
+    outs["neural_gated"] = torch.where(px[..., None], outs["bmfr"], outs["neural"])
+    img = illu.illumination_images[0].tensor()
+    ref = torch.zeros_like(outs["bmfr"])
+    for s_ in range(args.full_ref_spp):
+        pc.set(frame_number=(1 << 24) + s_)
+        pipe.trace(pc, stream)
+        ref += img[..., :3]
+    torch.cuda.synchronize()
+    pc.set(frame_number=f)
+    ref /= args.full_ref_spp
+    r = albedo * ref
+    res = {"reference_spp": args.full_ref_spp}
+    for k, v in outs.items():
+        res[k] = float((((albedo * v - r) ** 2) / (r * r + 0.01)).mean().item())
+    return res
+
 
 UNET_KERNELS = ("bf16_tcgen05", "bf16_mma", "fp8_tcgen05", "fp8_mma")
 
@@ -808,6 +984,8 @@ def main():
         run_reference(args)
     elif args.workload == "unet_layers":
         run_unet_layers(args)
+    elif args.workload == "full":
+        run_full(args)
     elif args.workload == "batch64":
         run_batch(args)
     else:
