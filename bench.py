@@ -53,8 +53,11 @@ def parse():
     ap.add_argument("--texture-size", type=int, default=1024)
     ap.add_argument("--denoiser", default="neural", choices=["neural", "bmfr", "bfr"],
                     help="neural: U-Net with BMFR as variance-gate fallback (BMFR runs every frame)")
+    ap.add_argument("--gate", default="learned", choices=["learned", "threshold"],
+                    help="neural path: the learned tile gate (weights/gate.json) or the threshold rule")
     ap.add_argument("--gate-threshold", type=float, default=0.05,
-                    help="neural path: tiles whose predicted relative squared error exceeds this show BMFR")
+                    help="neural path, threshold rule: tiles whose predicted relative squared error exceeds this "
+                         "show BMFR")
     ap.add_argument("--weights", default=None, help="neural path: .npz of trained parameters (default: packaged)")
     ap.add_argument("--ref-spp", type=int, default=4096, help="samples of the relMSE reference render (0: skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -417,7 +420,8 @@ def run_gb300(args):
     if args.denoiser == "neural":
         # the network reads what BMFR reads: the accumulator's output and its sample counts
         neural = vp.NeuralDenoiser(W, H, g, acc_illu, weights=args.weights, fallback=bmfr,
-                                   threshold=args.gate_threshold, tile=32, acc_buffer=abuf)
+                                   threshold=args.gate_threshold, tile=32, acc_buffer=abuf,
+                                   gate_model="default" if args.gate == "learned" else None)
     pc = vp.PushConstants()
     stream = torch.cuda.current_stream(dev)
     cams = [orbit(sc, W, H, f) for f in range(16)]
@@ -592,11 +596,11 @@ def run_gb300(args):
             "data": "synthetic (seeded procedural scene; inputs larger than L2: 0.8 GB textures, 0.5 GB path state)",
             "config": {
                 "workload": ("1080p 1spp depth8 RR>=3, 1M-tri instanced scene, 16-frame orbit: accumulate + BMFR 32x32"
-                             + (" + kernel-predicting U-Net (BF16) with per-tile BMFR fallback gate"
+                             + (" + kernel-predicting U-Net (BF16) with the learned per-tile BMFR fallback gate"
                                 if neural is not None else "")),
                 "width": W, "height": H, "max_depth": args.max_depth, "min_depth": args.min_depth,
                 "triangles": int(info.triangle_count), "instances": int(info.instance_count),
-                "lights": int(info.light_count), "texture_size": args.texture_size, "denoiser": args.denoiser,
+                "lights": int(info.light_count), "texture_size": args.texture_size, "denoiser": args.denoiser, "gate": args.gate,
                 "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}",
                 "schedule": {"sort_rays": bool(args.sort_rays), "merge_shadow": not args.separate_shadow},
             },
@@ -755,6 +759,7 @@ def run_full(args):
     abuf, acc_illu = accu.accumulation_buffer, accu.accumulated_illumination
     bmfr = vp.BMFR(W, H, 32, 32, g, acc_illu, abuf, 256, fp64_resolve=True)
     neural = vp.NeuralDenoiser(W, H, g, acc_illu, fallback=bmfr, threshold=args.gate_threshold, tile=32,
+                               gate_model="default" if args.gate == "learned" else None,
                                acc_buffer=abuf)
     # the 16 concurrent 1080p requests
     rng = np.random.default_rng(77)

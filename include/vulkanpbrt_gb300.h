@@ -599,6 +599,19 @@ PBRT_API int pbrt_nn_adam(float* w, const float* g, float* m, float* v, void* w_
  * threshold; count += the number of such tiles. */
 PBRT_API int pbrt_nn_gate(const float* var, int32_t pw, int32_t w, int32_t h, float threshold, int32_t tile,
                           uint8_t* mask, uint32_t* count, pbrt_stream_t stream);
+/* Learned tile gate (no reference counterpart): per tile, eight features
+ * (log of: the mean predicted relative squared error exp(var), the mean
+ * squared difference between final_bgra -- the network's final image -- and
+ * bmfr_final_bgra in [0,1] units, the mean spp byte, the variance of
+ * log(1 + luminance) of the noisy input, the mean |d log depth| (forward
+ * differences), 1 - |mean normal|, the mean noisy luminance, the mean
+ * albedo) score coef[8] + sum coef[k] * feature[k]; tiles scoring above 0
+ * get mask 1, are counted, and take bmfr_final_bgra's pixels in
+ * final_bgra. noisy: RGBA16F (noisy_is_half) or RGBA32F; spp may be NULL. */
+PBRT_API int pbrt_nn_gate_model(const float* var, int32_t pw, int32_t w, int32_t h, int32_t tile,
+                                const void* bmfr_final_bgra, const uint8_t* spp, const void* noisy, int32_t noisy_is_half,
+                                const float* depth, const void* normal, const void* albedo, const float* coef,
+                                uint8_t* mask, uint32_t* count, void* final_bgra, pbrt_stream_t s);
 /* Final image of the neural path, tone-mapped as BMFR's final image; pixels
  * of masked tiles copy fallback_bgra (BMFR's final image). denoised_rgba32f
  * (optional) always receives the network's output. */
@@ -628,6 +641,12 @@ PBRT_API int pbrt_neural_set_params(PbrtNeural* nd, const float* params_host, in
  * (bmfr must be dispatched before the neural module each frame); null bmfr
  * turns the gate off. */
 PBRT_API int pbrt_neural_set_fallback(PbrtNeural* nd, PbrtBMFR* bmfr, float threshold, int32_t tile);
+/* Learned tile gate in place of the threshold (no reference counterpart):
+ * coef = 8 weights and a bias of the linear score pbrt_nn_gate_model
+ * describes (fitted offline; vulkanpbrt_gb300/weights/gate.json), n = 9; a
+ * tile scoring above 0 shows BMFR's final image. NULL returns to the
+ * threshold rule. Needs a fallback BMFR (pbrt_neural_set_fallback). */
+PBRT_API int pbrt_neural_set_gate_model(PbrtNeural* nd, const float* coef, int32_t n);
 /* FP8 inference: calibrate runs one BF16 pass on the current inputs
  * (stream-synchronising) and derives per-input-channel activation scales
  * (max |x| / 448) and per-output-channel e4m3 weights; set_precision(8)

@@ -82,6 +82,8 @@ struct PbrtNeural : pbrt::Object {
   PbrtBMFR* fallback = nullptr;
   float threshold = 0.f;
   int32_t tile = 32;
+  bool gate_model = false;  // the learned tile gate instead of the threshold on the predicted error
+  float gate_coef[9] = {};
   Layout lay;
   float* params = nullptr;  // FP32, lay.total
   bf16* w16 = nullptr;      // BF16 convolution weights, lay.conv_w_total
@@ -183,17 +185,26 @@ int record_forward(PbrtNeural* nd, cudaStream_t s) {
                               hs.c, hs.k, s)))
       return st;
   }
-  const bool gate = nd->fallback != nullptr;
+  const bool gate = nd->fallback != nullptr && !nd->gate_model;
+  if (nd->fallback) PBRT_CUDA(cudaMemsetAsync(nd->counter, 0, sizeof(uint32_t), s));
   if (gate) {
-    PBRT_CUDA(cudaMemsetAsync(nd->counter, 0, sizeof(uint32_t), s));
     if ((st = pbrt_nn_gate(nd->variance.ptr<float>(), PW, nd->width, nd->height, nd->threshold, nd->tile,
                            nd->mask.ptr<uint8_t>(), nd->counter, s)))
       return st;
   }
-  return pbrt_nn_compose(nd->out[0], PW, nd->width, nd->height, nd->gbuffer->albedo.view.data,
-                         gate ? nd->mask.ptr<uint8_t>() : nullptr, nd->tile,
-                         gate ? nd->fallback->final_image.view.data : nullptr, nd->final_image.view.data,
-                         nd->denoised.ptr<float>(), s);
+  if ((st = pbrt_nn_compose(nd->out[0], PW, nd->width, nd->height, nd->gbuffer->albedo.view.data,
+                            gate ? nd->mask.ptr<uint8_t>() : nullptr, nd->tile,
+                            gate ? nd->fallback->final_image.view.data : nullptr, nd->final_image.view.data,
+                            nd->denoised.ptr<float>(), s)))
+    return st;
+  if (!nd->fallback || !nd->gate_model) return PBRT_OK;
+  // the learned gate reads the composed network image and BMFR's and overwrites the tiles it hands to BMFR
+  return pbrt_nn_gate_model(nd->variance.ptr<float>(), PW, nd->width, nd->height, nd->tile,
+                            nd->fallback->final_image.view.data, nd->acc ? nd->acc->spp.ptr<uint8_t>() : nullptr,
+                            illum.view.data, is_half,
+                            nd->gbuffer->depth.ptr<float>(), nd->gbuffer->normal.view.data,
+                            nd->gbuffer->albedo.view.data, nd->gate_coef, nd->mask.ptr<uint8_t>(), nd->counter,
+                            nd->final_image.view.data, s);
 }
 
 void drop_graph(PbrtNeural* nd) {
@@ -308,6 +319,15 @@ PBRT_API int pbrt_neural_create(uint32_t width, uint32_t height, PbrtGBuffer* g,
     return st;
   }
   *out = nd;
+  return PBRT_OK;
+}
+
+PBRT_API int pbrt_neural_set_gate_model(PbrtNeural* nd, const float* coef, int32_t n) {
+  if (!checked<PbrtNeural>(nd, Kind::Neural) || (coef && n != 9))
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "neural gate model: 9 coefficients (8 weights, bias) or null");
+  nd->gate_model = coef != nullptr;
+  for (int k = 0; k < 9; ++k) nd->gate_coef[k] = coef ? coef[k] : 0.f;
+  drop_graph(nd);  // the coefficients are baked into the captured launch
   return PBRT_OK;
 }
 

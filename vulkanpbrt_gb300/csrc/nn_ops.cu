@@ -390,6 +390,106 @@ __global__ void gate_kernel(const float* __restrict__ var, int PW, int W, int H,
   }
 }
 
+// Learned tile gate (no reference counterpart). Per tile of the frame, eight
+// features that need no reference image -- the error head's mean predicted
+// relative squared error, the mean squared difference between the
+// network's and BMFR's final images, the mean accumulated sample count, the
+// variance of log(1 + luminance) and the mean luminance of the noisy input,
+// the mean depth gradient |d log depth|, the normals' spread 1 - |mean n|,
+// the mean albedo -- each as a logarithm, enter a linear score (a logistic
+// classifier fitted offline to tiles of held-out frames, labelled by which
+// denoiser is nearer a converged render); a tile whose score is above zero
+// shows BMFR's final image. Runs after the network's final image is
+// composed and overwrites the chosen tiles with BMFR's pixels.
+struct GateModelArgs {
+  const float* var;  // padded (PW) log predicted relative squared error
+  int PW, W, H, tile;
+  const uchar4* nn_final;  // network final image, B8G8R8A8, overwritten in fallback tiles
+  const uchar4* bm_final;  // BMFR final image
+  const uint8_t* spp;      // accumulated samples (null: 1)
+  const Half4* noisy16;    // noisy demodulated input (one of the two)
+  const float4* noisy32;
+  const float* depth;
+  const float2* normal;    // (theta, phi)
+  const uchar4* albedo;
+  float coef[9];           // 8 weights, then the bias
+  uint8_t* mask;
+  uint32_t* count;
+  uchar4* final_out;
+};
+constexpr int kGateSums = 11;
+__global__ void __launch_bounds__(256) gate_model_kernel(GateModelArgs a) {
+  __shared__ float part[8][kGateSums];
+  __shared__ int fallback;
+  const int tiles_x = (a.W + a.tile - 1) / a.tile;
+  const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+  const int x0 = tx * a.tile, y0 = ty * a.tile;
+  const int tw = min(a.tile, a.W - x0), th = min(a.tile, a.H - y0);
+  float acc[kGateSums];
+#pragma unroll
+  for (int k = 0; k < kGateSums; ++k) acc[k] = 0.f;
+  for (int i = threadIdx.x; i < tw * th; i += blockDim.x) {
+    const int x = x0 + i % tw, y = y0 + i / tw;
+    const size_t p = (size_t)y * a.W + x;
+    acc[0] += expf(a.var[(size_t)y * a.PW + x]);
+    const uchar4 n = a.nn_final[p], b = a.bm_final[p];
+    const float dx = ((float)b.x - (float)n.x) / 255.f, dy = ((float)b.y - (float)n.y) / 255.f,
+                dz = ((float)b.z - (float)n.z) / 255.f;
+    acc[1] += (dx * dx + dy * dy + dz * dz) / 3.f;
+    acc[2] += a.spp ? (float)a.spp[p] : 1.f;
+    const float4 c = a.noisy32 ? a.noisy32[p] : load_half4(a.noisy16 + p);
+    const float lum = 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z;
+    const float ll = log1pf(fmaxf(lum, 0.f));
+    acc[3] += ll;
+    acc[4] += ll * ll;
+    const float ld = logf(fminf(fmaxf(a.depth[p], 1e-3f), 1e4f));
+    float g = 0.f;
+    if (x + 1 < a.W) g += fabsf(logf(fminf(fmaxf(a.depth[p + 1], 1e-3f), 1e4f)) - ld);
+    if (y + 1 < a.H) g += fabsf(logf(fminf(fmaxf(a.depth[p + a.W], 1e-3f), 1e4f)) - ld);
+    acc[5] += g;
+    const float2 tp = a.normal[p];
+    float st, ct, sp, cp;
+    sincosf(tp.x, &st, &ct);
+    sincosf(tp.y, &sp, &cp);
+    acc[6] += st * cp;
+    acc[7] += st * sp;
+    acc[8] += ct;
+    acc[9] += lum;
+    const uchar4 al = a.albedo[p];
+    acc[10] += ((float)al.x + (float)al.y + (float)al.z) / (3.f * 255.f);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < kGateSums; ++k) {
+    for (int o = 16; o; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+    if (lane == 0) part[warp][k] = acc[k];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float m[kGateSums];
+    for (int k = 0; k < kGateSums; ++k) {
+      m[k] = 0.f;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m[k] += part[w][k];
+      m[k] /= (float)(tw * th);
+    }
+    const float e = 1e-8f;
+    const float nl = sqrtf(m[6] * m[6] + m[7] * m[7] + m[8] * m[8]);
+    const float f[8] = {logf(m[0] + e), logf(m[1] + e), logf(m[2] + e), logf(fmaxf(m[4] - m[3] * m[3], 0.f) + e),
+                        logf(m[5] + e), logf(fmaxf(1.f - nl, 0.f) + e), logf(m[9] + e), logf(m[10] + e)};
+    float score = a.coef[8];
+    for (int k = 0; k < 8; ++k) score += a.coef[k] * f[k];
+    fallback = score > 0.f;
+    a.mask[blockIdx.x] = fallback ? 1 : 0;
+    if (fallback) atomicAdd(a.count, 1u);
+  }
+  __syncthreads();
+  if (!fallback) return;
+  for (int i = threadIdx.x; i < tw * th; i += blockDim.x) {
+    const size_t p = (size_t)(y0 + i / tw) * a.W + x0 + i % tw;
+    a.final_out[p] = a.bm_final[p];
+  }
+}
+
 // Final image of the neural path: the network's denoised illumination
 // (always written to `denoised`) remodulated by the albedo and tone mapped
 // as bmfrPost does (shaders/bmfrPost.comp:211-214); pixels of tiles the gate
@@ -534,6 +634,36 @@ PBRT_API int pbrt_nn_gate(const float* var, int32_t pw, int32_t w, int32_t h, fl
   const int tiles = ((w + tile - 1) / tile) * ((h + tile - 1) / tile);
   gate_kernel<<<tiles, 256, 0, s>>>(var, pw, w, h, threshold, tile, mask, count);
   return check_launch("gate");
+}
+
+PBRT_API int pbrt_nn_gate_model(const float* var, int32_t pw, int32_t w, int32_t h, int32_t tile,
+                                const void* bmfr_final_bgra, const uint8_t* spp, const void* noisy, int32_t noisy_is_half,
+                                const float* depth, const void* normal, const void* albedo, const float* coef,
+                                uint8_t* mask, uint32_t* count, void* final_bgra, pbrt_stream_t s) {
+  if (!var || !bmfr_final_bgra || !noisy || !depth || !normal || !albedo || !coef || !mask || !count ||
+      !final_bgra || tile < 4 || tile > 256 || w <= 0 || h <= 0 || pw < w)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "gate model: bad arguments");
+  GateModelArgs a;
+  a.var = var;
+  a.PW = pw;
+  a.W = w;
+  a.H = h;
+  a.tile = tile;
+  a.nn_final = (const uchar4*)final_bgra;
+  a.bm_final = (const uchar4*)bmfr_final_bgra;
+  a.spp = spp;
+  a.noisy16 = noisy_is_half ? (const Half4*)noisy : nullptr;
+  a.noisy32 = noisy_is_half ? nullptr : (const float4*)noisy;
+  a.depth = depth;
+  a.normal = (const float2*)normal;
+  a.albedo = (const uchar4*)albedo;
+  for (int k = 0; k < 9; ++k) a.coef[k] = coef[k];
+  a.mask = mask;
+  a.count = count;
+  a.final_out = (uchar4*)final_bgra;
+  const int tiles = ((w + tile - 1) / tile) * ((h + tile - 1) / tile);
+  gate_model_kernel<<<tiles, 256, 0, s>>>(a);
+  return check_launch("gate model");
 }
 
 PBRT_API int pbrt_nn_compose(const float* out, int32_t pw, int32_t w, int32_t h, const void* albedo,

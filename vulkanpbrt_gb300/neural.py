@@ -20,6 +20,7 @@ _abi.add_signatures({
     "pbrt_neural_create": (C.c_int32, [C.c_uint32, C.c_uint32, H, H, H, H, C.c_int64, C.POINTER(H)]),
     "pbrt_neural_set_params": (C.c_int32, [H, H, C.c_int64]),
     "pbrt_neural_set_fallback": (C.c_int32, [H, H, C.c_float, C.c_int32]),
+    "pbrt_neural_set_gate_model": (C.c_int32, [H, C.POINTER(C.c_float), C.c_int32]),
     "pbrt_neural_dispatch": (C.c_int32, [H, H]),
     "pbrt_neural_dispatch_direct": (C.c_int32, [H, H]),
     "pbrt_neural_final_image": (C.c_int32, [H, C.POINTER(PbrtImage)]),
@@ -34,6 +35,15 @@ _abi.add_signatures({
 })
 
 WEIGHTS = Path(__file__).resolve().parent / "weights" / "kpunet.npz"
+GATE = Path(__file__).resolve().parent / "weights" / "gate.json"
+
+
+def gate_coefficients(path=None) -> np.ndarray:
+    """The learned tile gate's 8 weights and bias (default: the packaged fit)."""
+    import json
+
+    d = json.loads(Path(path or GATE).read_text())
+    return np.asarray(d["coef"], np.float32)
 
 
 def param_count() -> int:
@@ -60,11 +70,14 @@ class NeuralDenoiser(Handle):
     """Denoises the demodulated illumination of `illu_buffer` (one sample, or
     the Accumulator's output with `acc_buffer` giving the sample counts) with
     the G-buffer's albedo, normal and depth. With `fallback` (a BMFR over the
-    same frame, dispatched first), tiles whose predicted error exceeds
-    `threshold` show BMFR's final image."""
+    same frame, dispatched first), tiles the learned gate scores above zero
+    (gate_model "default": the packaged coefficients; or 9 numbers) show
+    BMFR's final image; with gate_model None the rule is the mean predicted
+    error of the tile above `threshold`."""
 
     def __init__(self, width: int, height: int, g_buffer: GBuffer, illu_buffer: IlluminationBuffer, weights=None,
-                 fallback: BMFR | None = None, threshold: float = 0.5, tile: int = 32, acc_buffer=None):
+                 fallback: BMFR | None = None, threshold: float = 0.5, tile: int = 32, acc_buffer=None,
+                 gate_model="default"):
         p = load_params(weights)
         h = C.c_void_p()
         check(lib().pbrt_neural_create(width, height, g_buffer.ptr, illu_buffer.ptr,
@@ -79,6 +92,18 @@ class NeuralDenoiser(Handle):
         self.denoised, self.variance, self._final = Image(d, self), Image(v, self), Image(f, self)
         self._fallback = None
         self.set_fallback(fallback, threshold, tile)
+        if fallback is not None and gate_model is not None:
+            self.set_gate_model(gate_coefficients() if isinstance(gate_model, str) else gate_model)
+
+    def set_gate_model(self, coef) -> None:
+        """Learned tile gate (8 weights, bias; see pbrt_nn_gate_model) or None for the threshold rule."""
+        if coef is None:
+            check(lib().pbrt_neural_set_gate_model(self.ptr, None, 0))
+            self.gate_coef = None
+            return
+        c = np.ascontiguousarray(np.asarray(coef, np.float32))
+        check(lib().pbrt_neural_set_gate_model(self.ptr, c.ctypes.data_as(C.POINTER(C.c_float)), c.size))
+        self.gate_coef = c
 
     def set_params(self, weights) -> None:
         p = load_params(weights)
