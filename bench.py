@@ -781,6 +781,7 @@ def run_full(args):
     main_s = torch.cuda.current_stream()
     side_s = torch.cuda.Stream()
     pc = vp.PushConstants()
+    pc_den = vp.PushConstants()  # the denoisers' frame number counts frames, not samples (BMFR's layer parity)
     cams = [orbit(sc, W, H, f, frames=args.frames) for f in range(args.frames)]
     state = {"prev": cams[0]}
 
@@ -796,8 +797,9 @@ def run_full(args):
             pipe.trace(pc, stream)
             vp.lib().pbrt_accumulator_dispatch(accu.ptr, sh_)
             if s_ == spp - 1:
-                bmfr.dispatch(pc, stream)
-                neural.dispatch(pc, stream)
+                pc_den.set(view_inverse=cam.inv_view, proj_inverse=cam.inv_proj, prev_view=prev.view, frame_number=f)
+                bmfr.dispatch(pc_den, stream)
+                neural.dispatch(pc_den, stream)
             vp.lib().pbrt_accumulation_buffer_copy_to_back_images(abuf.ptr, g.ptr, acc_illu.ptr, sh_)
         state["prev"] = cam
 
@@ -834,7 +836,7 @@ def run_full(args):
         ratios.append(r)
         fallback.append(neural.fallback_tiles(main_s))
         if f in measure:
-            quality.append(dict(frame=f, **full_relmse(args, vp, pipe, g, illu, bmfr, neural, pc, main_s)))
+            quality.append(dict(frame=f, **full_relmse(args, vp, pipe, g, illu, bmfr, neural, pc, pc_den, main_s)))
     st1 = pipe.stats()
     rays = (st1.primary_rays - st0.primary_rays) + (st1.extension_rays - st0.extension_rays) + \
         (st1.shadow_rays - st0.shadow_rays)
@@ -857,12 +859,12 @@ def run_full(args):
     print(json.dumps(line), flush=True)
 
 
-def full_relmse(args, vp, pipe, g, illu, bmfr, neural, pc, stream):
+def full_relmse(args, vp, pipe, g, illu, bmfr, neural, pc, pc_den, stream):
     """relMSE of the current frame's outputs (network as shown with the gate,
     network alone, BMFR) against an --full-ref-spp render of the same camera."""
     import torch
 
-    f = pc.value.frame_number
+    f = pc_den.value.frame_number
     albedo = g.albedo.tensor()[..., :3].double() / 255.0
     outs = {"bmfr": bmfr.denoised.tensor()[(f & 1) ^ 1][..., :3].double().clone(),
             "neural": neural.denoised.tensor()[..., :3].double().clone()}
@@ -876,7 +878,6 @@ def full_relmse(args, vp, pipe, g, illu, bmfr, neural, pc, stream):
         pipe.trace(pc, stream)
         ref += img[..., :3]
     torch.cuda.synchronize()
-    pc.set(frame_number=f)
     ref /= args.full_ref_spp
     r = albedo * ref
     res = {"reference_spp": args.full_ref_spp}
