@@ -315,19 +315,42 @@ def relmse_eval(args, vp, pipe, g, illu, bmfr, neural, pc, cams, stream, dev):
     if bmfr is not None:
         den["bmfr"] = bmfr.denoised.tensor()[(f & 1) ^ 1][..., :3].double().clone()
     if neural is not None:
-        nn_out = neural.denoised.tensor()[..., :3].double().clone()
-        den["neural"] = nn_out
-        if neural.fallback_mask is not None and bmfr is not None:
-            m = neural.fallback_mask.tensor()[..., 0].bool()
-            px = m.repeat_interleave(neural.tile, 0).repeat_interleave(neural.tile, 1)[:g.height, :g.width]
-            den["neural_gated"] = torch.where(px[..., None], den["bmfr"], nn_out)
-            out["fallback_tiles"] = int(m.sum().item())
+        coef = getattr(neural, "gate_coef", None)
+        if coef is not None and bmfr is not None:
+            # the learned gate: `denoised` is what the module shows (per-tile blends of the network and BMFR);
+            # the network alone comes from one more dispatch with the gate off
+            m = neural.fallback_mask.tensor()[..., 0].long()
+            den["neural_gated"] = neural.denoised.tensor()[..., :3].double().clone()
+            out["fallback_tiles"] = int((m > 0).sum().item())
             out["tiles"] = int(m.numel())
-        neural.set_precision(8)  # calibrated during the FP8 timing
-        neural.dispatch(pc, stream)
-        torch.cuda.synchronize()
-        den["neural_fp8"] = neural.denoised.tensor()[..., :3].double().clone()
-        neural.set_precision(16)
+            out["gate_tiles_by_alpha"] = dict(zip(("1", "0.75", "0.5", "0.25", "0"),
+                                                  torch.bincount(m.flatten(), minlength=5).tolist()))
+            neural.set_gate_model(None)
+            neural.set_fallback(bmfr, threshold=1e30, tile=neural.tile)
+            neural.dispatch(pc, stream)
+            torch.cuda.synchronize()
+            den["neural"] = neural.denoised.tensor()[..., :3].double().clone()
+            neural.set_precision(8)  # calibrated during the FP8 timing; the network alone
+            neural.dispatch(pc, stream)
+            torch.cuda.synchronize()
+            den["neural_fp8"] = neural.denoised.tensor()[..., :3].double().clone()
+            neural.set_precision(16)
+            neural.set_fallback(bmfr, threshold=args.gate_threshold, tile=neural.tile)
+            neural.set_gate_model(coef)
+        else:
+            nn_out = neural.denoised.tensor()[..., :3].double().clone()
+            den["neural"] = nn_out
+            if neural.fallback_mask is not None and bmfr is not None:
+                m = neural.fallback_mask.tensor()[..., 0].bool()
+                px = m.repeat_interleave(neural.tile, 0).repeat_interleave(neural.tile, 1)[:g.height, :g.width]
+                den["neural_gated"] = torch.where(px[..., None], den["bmfr"], nn_out)
+                out["fallback_tiles"] = int(m.sum().item())
+                out["tiles"] = int(m.numel())
+            neural.set_precision(8)  # calibrated during the FP8 timing
+            neural.dispatch(pc, stream)
+            torch.cuda.synchronize()
+            den["neural_fp8"] = neural.denoised.tensor()[..., :3].double().clone()
+            neural.set_precision(16)
     torch.cuda.synchronize()
     ref = torch.zeros_like(noisy)
     t0 = time.perf_counter()
@@ -730,9 +753,10 @@ def run_batch(args):
 def run_full(args):
     """The full chosen form: 3840x2160, 4 samples per pixel, max depth 8 with
     Russian roulette after bounce 3, a seeded ~4M-triangle instanced field
-    with 32 lights, a 60-frame camera path; every frame traced 4 times and
-    accumulated, then BMFR 32x32 (FP64 re-solve on) and the kernel-predicting
-    network in FP8 with the per-tile gate falling back to BMFR; beside each
+    with 32 lights, a 60-frame camera path; every frame traced 4 times (the
+    samples averaged), accumulated, then BMFR 32x32 (FP64 re-solve on) and
+    the kernel-predicting network in FP8 with the learned per-tile gate
+    blending in BMFR; beside each
     4K frame, 16 independent 1080p requests (own seeded scene, 1 spp,
     accumulator + BMFR each) in one graph launch on a second stream. A step
     is one 4K frame plus one submission of the 16 requests. relMSE of the
@@ -785,22 +809,28 @@ def run_full(args):
     cams = [orbit(sc, W, H, f, frames=args.frames) for f in range(args.frames)]
     state = {"prev": cams[0]}
 
+    img = illu.illumination_images[0].tensor()
+    sample_sum = torch.zeros_like(img)
+
     def frame(f, stream):
+        # the frame's 4 samples are traced and averaged into the illumination
+        # buffer, then accumulated once with the frame's own camera motion
         cam, prev = cams[f % args.frames], state["prev"]
         sh_ = vp._abi.stream_handle(stream)
+        sample_sum.zero_()
         for s_ in range(spp):
-            pc.set(view_inverse=cam.inv_view, proj_inverse=cam.inv_proj, prev_view=(prev if s_ == 0 else cam).view,
+            pc.set(view_inverse=cam.inv_view, proj_inverse=cam.inv_proj, prev_view=prev.view,
                    frame_number=f * spp + s_)
-            p_ = prev if s_ == 0 else cam
-            accu.set_camera_matrices(f * spp + s_, vp.CameraMatrices(cam.view, cam.inv_view, cam.proj, cam.inv_proj),
-                                     vp.CameraMatrices(p_.view, p_.inv_view))
             pipe.trace(pc, stream)
-            vp.lib().pbrt_accumulator_dispatch(accu.ptr, sh_)
-            if s_ == spp - 1:
-                pc_den.set(view_inverse=cam.inv_view, proj_inverse=cam.inv_proj, prev_view=prev.view, frame_number=f)
-                bmfr.dispatch(pc_den, stream)
-                neural.dispatch(pc_den, stream)
-            vp.lib().pbrt_accumulation_buffer_copy_to_back_images(abuf.ptr, g.ptr, acc_illu.ptr, sh_)
+            sample_sum.add_(img)
+        img.copy_(sample_sum / spp)
+        accu.set_camera_matrices(f, vp.CameraMatrices(cam.view, cam.inv_view, cam.proj, cam.inv_proj),
+                                 vp.CameraMatrices(prev.view, prev.inv_view))
+        vp.lib().pbrt_accumulator_dispatch(accu.ptr, sh_)
+        pc_den.set(view_inverse=cam.inv_view, proj_inverse=cam.inv_proj, prev_view=prev.view, frame_number=f)
+        bmfr.dispatch(pc_den, stream)
+        neural.dispatch(pc_den, stream)
+        vp.lib().pbrt_accumulation_buffer_copy_to_back_images(abuf.ptr, g.ptr, acc_illu.ptr, sh_)
         state["prev"] = cam
 
     # warm-up: graphs, autotune of the network's kernels, FP8 calibration
@@ -867,10 +897,15 @@ def full_relmse(args, vp, pipe, g, illu, bmfr, neural, pc, pc_den, stream):
     f = pc_den.value.frame_number
     albedo = g.albedo.tensor()[..., :3].double() / 255.0
     outs = {"bmfr": bmfr.denoised.tensor()[(f & 1) ^ 1][..., :3].double().clone(),
-            "neural": neural.denoised.tensor()[..., :3].double().clone()}
-    m = neural.fallback_mask.tensor()[..., 0].bool()
-    px = m.repeat_interleave(neural.tile, 0).repeat_interleave(neural.tile, 1)[:g.height, :g.width]
-    outs["neural_gated"] = torch.where(px[..., None], outs["bmfr"], outs["neural"])
+            "neural_gated": neural.denoised.tensor()[..., :3].double().clone()}  # as shown (learned gate)
+    coef = neural.gate_coef
+    neural.set_gate_model(None)
+    neural.set_fallback(bmfr, threshold=1e30, tile=neural.tile)
+    neural.dispatch(pc_den, stream)  # the network alone
+    torch.cuda.synchronize()
+    outs["neural"] = neural.denoised.tensor()[..., :3].double().clone()
+    neural.set_fallback(bmfr, threshold=args.gate_threshold, tile=neural.tile)
+    neural.set_gate_model(coef)
     img = illu.illumination_images[0].tensor()
     ref = torch.zeros_like(outs["bmfr"])
     for s_ in range(args.full_ref_spp):

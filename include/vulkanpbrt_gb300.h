@@ -601,17 +601,26 @@ PBRT_API int pbrt_nn_gate(const float* var, int32_t pw, int32_t w, int32_t h, fl
                           uint8_t* mask, uint32_t* count, pbrt_stream_t stream);
 /* Learned tile gate (no reference counterpart): per tile, eight features
  * (log of: the mean predicted relative squared error exp(var), the mean
- * squared difference between final_bgra -- the network's final image -- and
- * bmfr_final_bgra in [0,1] units, the mean spp byte, the variance of
- * log(1 + luminance) of the noisy input, the mean |d log depth| (forward
- * differences), 1 - |mean normal|, the mean noisy luminance, the mean
- * albedo) score coef[8] + sum coef[k] * feature[k]; tiles scoring above 0
- * get mask 1, are counted, and take bmfr_final_bgra's pixels in
- * final_bgra. noisy: RGBA16F (noisy_is_half) or RGBA32F; spp may be NULL. */
-PBRT_API int pbrt_nn_gate_model(const float* var, int32_t pw, int32_t w, int32_t h, int32_t tile,
-                                const void* bmfr_final_bgra, const uint8_t* spp, const void* noisy, int32_t noisy_is_half,
-                                const float* depth, const void* normal, const void* albedo, const float* coef,
-                                uint8_t* mask, uint32_t* count, void* final_bgra, pbrt_stream_t s);
+ * squared difference between final_bgra -- the network's composed final
+ * image -- and bmfr_final_bgra in [0,1] units, the mean spp byte, the
+ * variance of log(1 + luminance) of the noisy input, the mean |d log depth|
+ * (forward differences), 1 - |mean normal|, the mean noisy luminance, the
+ * mean albedo) give four predictions coef[9c + 8] + sum_k coef[9c + k] *
+ * feature[k] of the change in relative squared error from showing alpha *
+ * network + (1 - alpha) * BMFR, alpha = 0.75, 0.5, 0.25, 0 (c = 0..3); the
+ * tile takes the lowest prediction below zero, else the network alone.
+ * mask: 0 network, 1..4 the chosen alpha; count: tiles with alpha < 1. In
+ * those tiles denoised_rgba32f gets the blend of nn_out (padded rows of pw
+ * pixels, 3 floats each) and BMFR's denoised layer *bmfr_layer (RGBA16F,
+ * two layers of w x h), and final_bgra its remodulated, tone-mapped value
+ * (alpha 0: bmfr_final_bgra's pixels). noisy: RGBA16F (noisy_is_half) or
+ * RGBA32F; spp may be NULL. */
+PBRT_API int pbrt_nn_gate_model(const float* var, const float* nn_out, int32_t pw, int32_t w, int32_t h,
+                                int32_t tile, const void* bmfr_final_bgra, const void* bmfr_denoised,
+                                const uint32_t* bmfr_layer, const uint8_t* spp, const void* noisy,
+                                int32_t noisy_is_half, const float* depth, const void* normal, const void* albedo,
+                                const float* coef, uint8_t* mask, uint32_t* count, void* final_bgra,
+                                float* denoised_rgba32f, pbrt_stream_t s);
 /* Final image of the neural path, tone-mapped as BMFR's final image; pixels
  * of masked tiles copy fallback_bgra (BMFR's final image). denoised_rgba32f
  * (optional) always receives the network's output. */
@@ -642,10 +651,12 @@ PBRT_API int pbrt_neural_set_params(PbrtNeural* nd, const float* params_host, in
  * turns the gate off. */
 PBRT_API int pbrt_neural_set_fallback(PbrtNeural* nd, PbrtBMFR* bmfr, float threshold, int32_t tile);
 /* Learned tile gate in place of the threshold (no reference counterpart):
- * coef = 8 weights and a bias of the linear score pbrt_nn_gate_model
- * describes (fitted offline; vulkanpbrt_gb300/weights/gate.json), n = 9; a
- * tile scoring above 0 shows BMFR's final image. NULL returns to the
- * threshold rule. Needs a fallback BMFR (pbrt_neural_set_fallback). */
+ * coef = the 4 x 9 coefficients of the predictions pbrt_nn_gate_model
+ * describes (fitted offline; vulkanpbrt_gb300/weights/gate.json), n = 36;
+ * tiles show alpha * network + (1 - alpha) * BMFR with the alpha in {1,
+ * 0.75, 0.5, 0.25, 0} predicted best, in the final and the denoised images.
+ * NULL returns to the threshold rule. Needs a fallback BMFR
+ * (pbrt_neural_set_fallback), dispatched before the neural module. */
 PBRT_API int pbrt_neural_set_gate_model(PbrtNeural* nd, const float* coef, int32_t n);
 /* FP8 inference: calibrate runs one BF16 pass on the current inputs
  * (stream-synchronising) and derives per-input-channel activation scales

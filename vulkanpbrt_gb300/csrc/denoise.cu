@@ -210,6 +210,7 @@ struct BmfrParams {
   const float4* noisy_f32;
   float* weights;  // 30 layers x gh x gw
   uint32_t* flagged;  // [0] = count, [1] = largest R-diagonal ratio (float bits), [2..] = block ids to re-solve
+  uint32_t* last_layer;  // device word: the denoised layer this dispatch writes (null: not recorded)
   PostArgs post;
 };
 
@@ -277,6 +278,7 @@ __global__ void __launch_bounds__(BmfrShape<BW>::NT, BW == 8 ? 8 : 3) bmfr_fused
 
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const int gx = blockIdx.x, gy = blockIdx.y;
+  if (p.last_layer && gx == 0 && gy == 0 && t == 0) *p.last_layer = (p.frame & 1u) ^ 1u;
   const int offx = (int)((float)BW * c_bmfr_offsets[p.frame % 16][0]);
   const int offy = (int)((float)BW * c_bmfr_offsets[p.frame % 16][1]);
   const float EPS = 1e-6f;
@@ -1042,11 +1044,12 @@ PBRT_API int pbrt_bmfr_create(uint32_t width, uint32_t height, uint32_t work_wid
   if ((st = b->denoised.alloc(width, height, 2, PBRT_FORMAT_R16G16B16A16_SFLOAT)) ||
       (st = b->final_image.alloc(width, height, 1, PBRT_FORMAT_B8G8R8A8_UNORM)) ||
       (st = b->weights.alloc(gw, gh, 30, PBRT_FORMAT_R32_SFLOAT)) ||
-      (st = b->flags.alloc(gw * gh + 2, 1, 1, PBRT_FORMAT_R32_SFLOAT))) {
+      (st = b->flags.alloc(gw * gh + 3, 1, 1, PBRT_FORMAT_R32_SFLOAT))) {
     delete b;
     return st;
   }
   b->counter = b->flags.ptr<uint32_t>();
+  b->last_layer = b->counter + gw * gh + 2;
   *out = b;
   return PBRT_OK;
 }
@@ -1082,6 +1085,7 @@ PBRT_API int pbrt_bmfr_dispatch(PbrtBMFR* b, const PbrtPushConstants* pc, pbrt_s
   kp.noisy_f32 = f32 ? noisy.ptr<float4>() : nullptr;
   kp.weights = b->weights.ptr<float>();
   kp.flagged = b->counter;
+  kp.last_layer = b->last_layer;
   kp.post.motion = b->acc->motion.ptr<__half2>();
   kp.post.spp = b->acc->spp.ptr<uint8_t>();
   kp.post.albedo = b->gbuffer->albedo.ptr<uint8_t>();
@@ -1341,6 +1345,7 @@ extern "C" PBRT_API int pbrt_bmfr_dispatch_noalloc(uint32_t width, uint32_t heig
   kp.noisy_f32 = nullptr;
   kp.weights = weights;  // every block writes all 30 of its weights before reading them back
   kp.flagged = nullptr;
+  kp.last_layer = nullptr;
   kp.post.motion = reinterpret_cast<const __half2*>(im->motion);
   kp.post.spp = im->spp;
   kp.post.albedo = im->albedo;

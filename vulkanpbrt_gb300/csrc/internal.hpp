@@ -160,6 +160,7 @@ struct PbrtBMFR : pbrt::Object {
   pbrt::DeviceImage denoised, final_image, weights;
   pbrt::DeviceImage flags;  // per block: condition estimate exceeded (FP64 re-solve list)
   uint32_t* counter = nullptr;  // device: [0] = number of flagged blocks, [1] = largest ratio (float bits)
+  uint32_t* last_layer = nullptr;  // device: the denoised layer the last dispatch wrote (0 or 1)
 };
 
 struct PbrtBFR : pbrt::Object {

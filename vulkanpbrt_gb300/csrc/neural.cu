@@ -83,7 +83,7 @@ struct PbrtNeural : pbrt::Object {
   float threshold = 0.f;
   int32_t tile = 32;
   bool gate_model = false;  // the learned tile gate instead of the threshold on the predicted error
-  float gate_coef[9] = {};
+  float gate_coef[36] = {};
   Layout lay;
   float* params = nullptr;  // FP32, lay.total
   bf16* w16 = nullptr;      // BF16 convolution weights, lay.conv_w_total
@@ -199,12 +199,13 @@ int record_forward(PbrtNeural* nd, cudaStream_t s) {
     return st;
   if (!nd->fallback || !nd->gate_model) return PBRT_OK;
   // the learned gate reads the composed network image and BMFR's and overwrites the tiles it hands to BMFR
-  return pbrt_nn_gate_model(nd->variance.ptr<float>(), PW, nd->width, nd->height, nd->tile,
-                            nd->fallback->final_image.view.data, nd->acc ? nd->acc->spp.ptr<uint8_t>() : nullptr,
-                            illum.view.data, is_half,
-                            nd->gbuffer->depth.ptr<float>(), nd->gbuffer->normal.view.data,
-                            nd->gbuffer->albedo.view.data, nd->gate_coef, nd->mask.ptr<uint8_t>(), nd->counter,
-                            nd->final_image.view.data, s);
+  return pbrt_nn_gate_model(nd->variance.ptr<float>(), nd->out[0], PW, nd->width, nd->height, nd->tile,
+                            nd->fallback->final_image.view.data, nd->fallback->denoised.view.data,
+                            nd->fallback->last_layer, nd->acc ? nd->acc->spp.ptr<uint8_t>() : nullptr,
+                            illum.view.data, is_half, nd->gbuffer->depth.ptr<float>(),
+                            nd->gbuffer->normal.view.data, nd->gbuffer->albedo.view.data, nd->gate_coef,
+                            nd->mask.ptr<uint8_t>(), nd->counter, nd->final_image.view.data,
+                            nd->denoised.ptr<float>(), s);
 }
 
 void drop_graph(PbrtNeural* nd) {
@@ -323,10 +324,10 @@ PBRT_API int pbrt_neural_create(uint32_t width, uint32_t height, PbrtGBuffer* g,
 }
 
 PBRT_API int pbrt_neural_set_gate_model(PbrtNeural* nd, const float* coef, int32_t n) {
-  if (!checked<PbrtNeural>(nd, Kind::Neural) || (coef && n != 9))
-    return fail(PBRT_ERROR_INVALID_ARGUMENT, "neural gate model: 9 coefficients (8 weights, bias) or null");
+  if (!checked<PbrtNeural>(nd, Kind::Neural) || (coef && n != 36))
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "neural gate model: 36 coefficients (4 x (8 weights, bias)) or null");
   nd->gate_model = coef != nullptr;
-  for (int k = 0; k < 9; ++k) nd->gate_coef[k] = coef ? coef[k] : 0.f;
+  for (int k = 0; k < 36; ++k) nd->gate_coef[k] = coef ? coef[k] : 0.f;
   drop_graph(nd);  // the coefficients are baked into the captured launch
   return PBRT_OK;
 }

@@ -396,31 +396,40 @@ __global__ void gate_kernel(const float* __restrict__ var, int PW, int W, int H,
 // network's and BMFR's final images, the mean accumulated sample count, the
 // variance of log(1 + luminance) and the mean luminance of the noisy input,
 // the mean depth gradient |d log depth|, the normals' spread 1 - |mean n|,
-// the mean albedo -- each as a logarithm, enter a linear score (a logistic
-// classifier fitted offline to tiles of held-out frames, labelled by which
-// denoiser is nearer a converged render); a tile whose score is above zero
-// shows BMFR's final image. Runs after the network's final image is
-// composed and overwrites the chosen tiles with BMFR's pixels.
+// the mean albedo -- each as a logarithm, enter four linear predictions of
+// how much the tile's relative squared error changes when the shown
+// illumination is alpha * network + (1 - alpha) * BMFR for alpha = 0.75,
+// 0.5, 0.25 and 0 instead of the network alone (regressions fitted offline
+// on tiles of held-out frames against converged renders). The tile takes the
+// alpha with the lowest prediction (alpha 1, the network, when none is
+// below zero). Runs after the network's final image is composed: tiles with
+// alpha < 1 get the blend of the network's FP32 output and BMFR's denoised
+// (RGBA16F) illumination in `denoised` and, remodulated and tone mapped as
+// the compose pass does, in the final image (alpha 0: BMFR's own final
+// pixels).
 struct GateModelArgs {
   const float* var;  // padded (PW) log predicted relative squared error
+  const float* nn_out;  // padded (PW) network output, 3 floats a pixel
   int PW, W, H, tile;
-  const uchar4* nn_final;  // network final image, B8G8R8A8, overwritten in fallback tiles
   const uchar4* bm_final;  // BMFR final image
+  const Half4* bm_denoised;  // BMFR denoised, 2 layers of W x H
+  const uint32_t* bm_layer;  // device word: the layer BMFR wrote this frame
   const uint8_t* spp;      // accumulated samples (null: 1)
   const Half4* noisy16;    // noisy demodulated input (one of the two)
   const float4* noisy32;
   const float* depth;
   const float2* normal;    // (theta, phi)
   const uchar4* albedo;
-  float coef[9];           // 8 weights, then the bias
-  uint8_t* mask;
-  uint32_t* count;
-  uchar4* final_out;
+  float coef[36];          // per alpha 0.75, 0.5, 0.25, 0: 8 weights, then the bias
+  uint8_t* mask;           // per tile: 0 network, 1..4 alpha 0.75 .. 0
+  uint32_t* count;         // tiles with alpha < 1
+  uchar4* final_out;       // the composed network image, rewritten in blended tiles
+  float4* denoised;        // the network's output image, rewritten in blended tiles
 };
 constexpr int kGateSums = 11;
 __global__ void __launch_bounds__(256) gate_model_kernel(GateModelArgs a) {
   __shared__ float part[8][kGateSums];
-  __shared__ int fallback;
+  __shared__ int choice;
   const int tiles_x = (a.W + a.tile - 1) / a.tile;
   const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
   const int x0 = tx * a.tile, y0 = ty * a.tile;
@@ -432,7 +441,7 @@ __global__ void __launch_bounds__(256) gate_model_kernel(GateModelArgs a) {
     const int x = x0 + i % tw, y = y0 + i / tw;
     const size_t p = (size_t)y * a.W + x;
     acc[0] += expf(a.var[(size_t)y * a.PW + x]);
-    const uchar4 n = a.nn_final[p], b = a.bm_final[p];
+    const uchar4 n = a.final_out[p], b = a.bm_final[p];
     const float dx = ((float)b.x - (float)n.x) / 255.f, dy = ((float)b.y - (float)n.y) / 255.f,
                 dz = ((float)b.z - (float)n.z) / 255.f;
     acc[1] += (dx * dx + dy * dy + dz * dz) / 3.f;
@@ -476,17 +485,39 @@ __global__ void __launch_bounds__(256) gate_model_kernel(GateModelArgs a) {
     const float nl = sqrtf(m[6] * m[6] + m[7] * m[7] + m[8] * m[8]);
     const float f[8] = {logf(m[0] + e), logf(m[1] + e), logf(m[2] + e), logf(fmaxf(m[4] - m[3] * m[3], 0.f) + e),
                         logf(m[5] + e), logf(fmaxf(1.f - nl, 0.f) + e), logf(m[9] + e), logf(m[10] + e)};
-    float score = a.coef[8];
-    for (int k = 0; k < 8; ++k) score += a.coef[k] * f[k];
-    fallback = score > 0.f;
-    a.mask[blockIdx.x] = fallback ? 1 : 0;
-    if (fallback) atomicAdd(a.count, 1u);
+    int best = 0;
+    float best_d = 0.f;  // the network alone
+    for (int c = 0; c < 4; ++c) {
+      float d = a.coef[9 * c + 8];
+      for (int k = 0; k < 8; ++k) d += a.coef[9 * c + k] * f[k];
+      if (d < best_d) {
+        best_d = d;
+        best = c + 1;
+      }
+    }
+    choice = best;
+    a.mask[blockIdx.x] = (uint8_t)best;
+    if (best) atomicAdd(a.count, 1u);
   }
   __syncthreads();
-  if (!fallback) return;
+  if (!choice) return;
+  const float alpha = 1.f - 0.25f * (float)choice;
+  const Half4* bm = a.bm_denoised + (size_t)(*a.bm_layer & 1u) * a.W * a.H;
   for (int i = threadIdx.x; i < tw * th; i += blockDim.x) {
-    const size_t p = (size_t)(y0 + i / tw) * a.W + x0 + i % tw;
-    a.final_out[p] = a.bm_final[p];
+    const int x = x0 + i % tw, y = y0 + i / tw;
+    const size_t p = (size_t)y * a.W + x, q = (size_t)y * a.PW + x;
+    const float4 b = load_half4(bm + p);
+    const float3 o = f3(a.nn_out[q * 3], a.nn_out[q * 3 + 1], a.nn_out[q * 3 + 2]);
+    const float3 c = o * alpha + f3(b.x, b.y, b.z) * (1.f - alpha);
+    a.denoised[p] = make_float4(c.x, c.y, c.z, 1.f);
+    if (choice == 4) {
+      a.final_out[p] = a.bm_final[p];
+      continue;
+    }
+    const uchar4 al = a.albedo[p];
+    float3 t = fmax3(f3(0.f), f3(al.x / 255.f + 1e-6f, al.y / 255.f + 1e-6f, al.z / 255.f + 1e-6f) * c);
+    t = clamp3(f3(powf(t.x, .454545f), powf(t.y, .454545f), powf(t.z, .454545f)), 0.f, 1.f);
+    a.final_out[p] = make_uchar4(f2u8(t.z), f2u8(t.y), f2u8(t.x), 255);
   }
 }
 
@@ -636,31 +667,37 @@ PBRT_API int pbrt_nn_gate(const float* var, int32_t pw, int32_t w, int32_t h, fl
   return check_launch("gate");
 }
 
-PBRT_API int pbrt_nn_gate_model(const float* var, int32_t pw, int32_t w, int32_t h, int32_t tile,
-                                const void* bmfr_final_bgra, const uint8_t* spp, const void* noisy, int32_t noisy_is_half,
-                                const float* depth, const void* normal, const void* albedo, const float* coef,
-                                uint8_t* mask, uint32_t* count, void* final_bgra, pbrt_stream_t s) {
-  if (!var || !bmfr_final_bgra || !noisy || !depth || !normal || !albedo || !coef || !mask || !count ||
-      !final_bgra || tile < 4 || tile > 256 || w <= 0 || h <= 0 || pw < w)
+PBRT_API int pbrt_nn_gate_model(const float* var, const float* nn_out, int32_t pw, int32_t w, int32_t h,
+                                int32_t tile, const void* bmfr_final_bgra, const void* bmfr_denoised,
+                                const uint32_t* bmfr_layer, const uint8_t* spp, const void* noisy,
+                                int32_t noisy_is_half, const float* depth, const void* normal, const void* albedo,
+                                const float* coef, uint8_t* mask, uint32_t* count, void* final_bgra,
+                                float* denoised_rgba32f, pbrt_stream_t s) {
+  if (!var || !nn_out || !bmfr_final_bgra || !bmfr_denoised || !bmfr_layer || !noisy || !depth || !normal ||
+      !albedo || !coef || !mask || !count || !final_bgra || !denoised_rgba32f || tile < 4 || tile > 256 || w <= 0 ||
+      h <= 0 || pw < w)
     return fail(PBRT_ERROR_INVALID_ARGUMENT, "gate model: bad arguments");
   GateModelArgs a;
   a.var = var;
+  a.nn_out = nn_out;
   a.PW = pw;
   a.W = w;
   a.H = h;
   a.tile = tile;
-  a.nn_final = (const uchar4*)final_bgra;
   a.bm_final = (const uchar4*)bmfr_final_bgra;
+  a.bm_denoised = (const Half4*)bmfr_denoised;
+  a.bm_layer = bmfr_layer;
   a.spp = spp;
   a.noisy16 = noisy_is_half ? (const Half4*)noisy : nullptr;
   a.noisy32 = noisy_is_half ? nullptr : (const float4*)noisy;
   a.depth = depth;
   a.normal = (const float2*)normal;
   a.albedo = (const uchar4*)albedo;
-  for (int k = 0; k < 9; ++k) a.coef[k] = coef[k];
+  for (int k = 0; k < 36; ++k) a.coef[k] = coef[k];
   a.mask = mask;
   a.count = count;
   a.final_out = (uchar4*)final_bgra;
+  a.denoised = (float4*)denoised_rgba32f;
   const int tiles = ((w + tile - 1) / tile) * ((h + tile - 1) / tile);
   gate_model_kernel<<<tiles, 256, 0, s>>>(a);
   return check_launch("gate model");

@@ -1,8 +1,11 @@
 """Fitting the neural denoiser's learned tile gate (no reference counterpart).
 
-The gate (pbrt_nn_gate_model) hands a 32x32 tile of the network's output to
-BMFR when a linear score of eight per-tile log features is above zero. This
-module makes the training data and fits the score:
+The gate (pbrt_nn_gate_model) shows, per 32x32 tile, alpha * network +
+(1 - alpha) * BMFR with alpha in {1, 0.75, 0.5, 0.25, 0}: four linear
+functions of eight per-tile log features predict how much each blend
+changes the tile's relative squared error against the network alone, and
+the tile takes the lowest prediction below zero. This module makes the
+training data and fits the predictions:
 
     python -m vulkanpbrt_gb300.gate_fit collect --out gate_data.npz   # GPU
     python -m vulkanpbrt_gb300.gate_fit fit gate_data.npz --out gate.json
@@ -10,13 +13,12 @@ module makes the training data and fits the score:
 collect renders held-out seeded instanced fields (never the benchmark's seed
 0) through the benchmark's frame -- trace, accumulate, BMFR 32x32, the
 network -- along the benchmark's 16-frame orbit and, at a few frames, the
-features the gate kernel computes, plus each denoiser's per-tile relMSE
-against a many-sample render of the same camera (remodulated by the
-G-buffer albedo, as the benchmark measures). fit is a cost-weighted L2
-logistic regression (label: BMFR nearer the reference; weight: the
-difference of the two errors) by Newton's method on standardised features,
-with the regularisation chosen by leave-one-scene-out error, written back as
-coefficients on the raw features.
+features the gate kernel computes, plus the per-tile relMSE of the network,
+of BMFR and of the three blends against a many-sample render of the same
+camera (remodulated by the G-buffer albedo, as the benchmark measures). fit
+is a ridge regression per blend of the error change on standardised
+features, with the regularisation chosen by leave-one-scene-out error of
+the resulting choice, written back as coefficients on the raw features.
 """
 from __future__ import annotations
 
@@ -66,7 +68,7 @@ def tile_features(var, nn_fin, bm_fin, spp, noisy, depth, nrm, alb8):
     return torch.stack([f0, f1, f2, f3, f4, f5, f6, f7], 1), n
 
 
-def collect(out: str, seeds=(21, 22, 23, 24), frames=(15, 30, 46), ref_spp=1024, width=1920, height=1080):
+def collect(out: str, seeds=(21, 22, 23, 24, 25, 26), frames=(15, 30, 46), ref_spp=2048, width=1920, height=1080):
     """Renders the training frames on cuda:0 and saves features and errors to `out` (.npz)."""
     import sys
 
@@ -81,7 +83,7 @@ def collect(out: str, seeds=(21, 22, 23, 24), frames=(15, 30, 46), ref_spp=1024,
 
     W, H = width, height
     stream = torch.cuda.current_stream()
-    rec = {k: [] for k in ("err_nn", "err_bm", "f", "scene", "frame")}
+    rec = {k: [] for k in ("err_nn", "err_b75", "err_b50", "err_b25", "err_bm", "f", "scene", "frame")}
     for si, seed in enumerate(seeds):
         sc = S.instanced_field(seed=seed)
         sh = vp.SceneHandle(sc)
@@ -92,7 +94,7 @@ def collect(out: str, seeds=(21, 22, 23, 24), frames=(15, 30, 46), ref_spp=1024,
         acc_illu, abuf = accu.accumulated_illumination, accu.accumulation_buffer
         bm = vp.BMFR(W, H, 32, 32, g, acc_illu, abuf, 256)
         nd = vp.NeuralDenoiser(W, H, g, acc_illu, fallback=bm, threshold=1e30, tile=TILE, acc_buffer=abuf,
-                               gate_model=None)
+                               gate_model=None)  # the network alone
         pc = vp.PushConstants()
         prev = bench.orbit(sc, W, H, 0)
         hs = vp._abi.stream_handle(stream)
@@ -139,6 +141,8 @@ def collect(out: str, seeds=(21, 22, 23, 24), frames=(15, 30, 46), ref_spp=1024,
 
             rec["err_nn"].append(err(nn_o).cpu().numpy())
             rec["err_bm"].append(err(bm_o).cpu().numpy())
+            for a_, k_ in ((0.75, "err_b75"), (0.5, "err_b50"), (0.25, "err_b25")):
+                rec[k_].append(err(a_ * nn_o + (1 - a_) * bm_o).cpu().numpy())
             rec["f"].append(feats.cpu().numpy())
             rec["scene"].append(np.full(feats.shape[0], si))
             rec["frame"].append(np.full(feats.shape[0], f))
@@ -147,56 +151,56 @@ def collect(out: str, seeds=(21, 22, 23, 24), frames=(15, 30, 46), ref_spp=1024,
     np.savez(out, **{k: np.concatenate(v) for k, v in rec.items()}, seeds=np.array(seeds), ref_spp=ref_spp)
 
 
-def logistic(X, y, w, C, iters=50):
-    """Weighted L2 logistic regression (Newton's method): (coef, bias) on the given features."""
-    A = np.concatenate([X, np.ones((len(X), 1))], 1)
-    beta = np.zeros(A.shape[1])
-    reg = np.full(A.shape[1], 1.0 / C)
-    reg[-1] = 0.0  # no penalty on the bias
-    for _ in range(iters):
-        p = 1.0 / (1.0 + np.exp(-(A @ beta)))
-        g = A.T @ (w * (p - y)) + reg * beta
-        Hs = (A * (w * p * (1 - p))[:, None]).T @ A + np.diag(reg)
-        step = np.linalg.solve(Hs, g)
-        beta -= step
-        if np.abs(step).max() < 1e-10:
-            break
-    return beta[:-1], beta[-1]
+BLENDS = ("err_b75", "err_b50", "err_b25", "err_bm")  # alpha 0.75, 0.5, 0.25, 0 on the network
 
 
-def fit(data: str, out: str, Cs=(0.3, 1.0, 3.0)):
+def fit(data: str, out: str, lams=(0.1, 1.0, 10.0)):
     d = np.load(data)
-    en, eb, X, scene = d["err_nn"], d["err_bm"], d["f"], d["scene"]
-    ok = np.isfinite(X).all(1) & np.isfinite(en) & np.isfinite(eb)
-    en, eb, X, scene = en[ok], eb[ok], X[ok], scene[ok]
-    y = (eb < en).astype(float)
-    w = np.abs(en - eb)
+    X, scene = d["f"], d["scene"]
+    E = np.stack([d["err_nn"]] + [d[k] for k in BLENDS], 1)
+    ok = np.isfinite(X).all(1) & np.isfinite(E).all(1)
+    X, E, scene = X[ok], E[ok], scene[ok]
 
-    def train(sel, C):
+    def train(sel, lam):
         mu, sd = X[sel].mean(0), X[sel].std(0) + 1e-9
-        c, b = logistic((X[sel] - mu) / sd, y[sel], w[sel] / w[sel].mean(), C)
-        return c / sd, b - (c * mu / sd).sum()
+        A = np.concatenate([(X[sel] - mu) / sd, np.ones((int(sel.sum()), 1))], 1)
+        coef = []
+        for k in range(1, 5):
+            b = np.linalg.solve(A.T @ A + lam * np.eye(9), A.T @ (E[sel, k] - E[sel, 0]))
+            coef.append(np.concatenate([b[:8] / sd, [b[8] - (b[:8] * mu / sd).sum()]]))
+        return np.stack(coef)
+
+    def choose(C, Xs):
+        pred = np.concatenate([np.zeros((len(Xs), 1)), Xs @ C[:, :8].T + C[:, 8]], 1)
+        return pred.argmin(1)
 
     best = None
-    for C in Cs:
-        tot = np.zeros(3)
+    for lam in lams:
+        tot, picks = np.zeros(2), np.zeros(5)
         for s in np.unique(scene):
-            c, b = train(scene != s, C)
             te = scene == s
-            pick = X[te] @ c + b > 0
-            tot += [np.where(pick, eb[te], en[te]).sum(), en[te].sum(), pick.sum()]
-        res = tot / len(en)
-        print(f"C {C}: leave-one-scene-out relMSE gated {res[0]:.5f}, network {res[1]:.5f}, tiles to BMFR {res[2]:.3f}")
+            ch = choose(train(scene != s, lam), X[te])
+            tot += [E[te][np.arange(int(te.sum())), ch].sum(), E[te, 0].sum()]
+            picks += np.bincount(ch, minlength=5)
+        res = tot / len(E)
+        print(f"ridge {lam}: leave-one-scene-out relMSE gated {res[0]:.5f}, network {res[1]:.5f}, "
+              f"alpha 1/.75/.5/.25/0 on {np.round(picks / picks.sum(), 3).tolist()} of the tiles")
         if best is None or res[0] < best[1][0]:
-            best = (C, res)
-    C, res = best
-    c, b = train(np.ones(len(en), bool), C)
-    doc = {"coef": [float(v) for v in c] + [float(b)], "features": FEATURES,
-           "fit": {"tiles": int(len(en)), "scenes": int(len(np.unique(scene))), "C": C,
+            best = (lam, res, picks / picks.sum())
+    lam, res, picks = best
+    C = train(np.ones(len(E), bool), lam)
+    doc = {"coef": [float(v) for v in C.reshape(-1)], "features": FEATURES,
+           "data": "held-out seeded instanced fields (never the benchmark's seed 0), 1920x1080, depth 8 with Russian "
+                   "roulette after bounce 3, the benchmark's 16-frame orbit with accumulation, BMFR 32x32 and the "
+                   "network; 2040 tiles of 32x32 a frame; per-tile relMSE against a many-sample render of the same "
+                   "camera, remodulated by the G-buffer albedo",
+           "blends": "rows: alpha 0.75, 0.5, 0.25, 0 on the network (1 - alpha on BMFR); 8 weights, then the bias",
+           "fit": {"tiles": int(len(E)), "scenes": int(len(np.unique(scene))), "ridge": lam,
                    "seeds": [int(v) for v in d["seeds"]] if "seeds" in d.files else None,
                    "reference_spp": int(d["ref_spp"]) if "ref_spp" in d.files else None,
-                   "leave_one_scene_out": {"gated": float(res[0]), "network": float(res[1]), "bmfr_tiles": float(res[2])},
-                   "best_possible": float(np.minimum(en, eb).mean()), "bmfr": float(eb.mean())}}
+                   "leave_one_scene_out": {"gated": float(res[0]), "network": float(res[1]),
+                                           "alpha_share": [float(v) for v in picks]},
+                   "per_tile_best_of_the_five": float(E.min(1).mean()), "bmfr": float(E[:, 4].mean())}}
     Path(out).write_text(json.dumps(doc, indent=1))
     return doc
 
@@ -206,7 +210,7 @@ def main(argv=None):
     sub = ap.add_subparsers(dest="cmd", required=True)
     c = sub.add_parser("collect")
     c.add_argument("--out", default="gate_data.npz")
-    c.add_argument("--ref-spp", type=int, default=1024)
+    c.add_argument("--ref-spp", type=int, default=2048)
     f = sub.add_parser("fit")
     f.add_argument("data")
     f.add_argument("--out", default=str(Path(__file__).resolve().parent / "weights" / "gate.json"))

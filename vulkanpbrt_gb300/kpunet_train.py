@@ -199,6 +199,7 @@ def main(argv=None):
 
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--views", type=int, default=24)
+    ap.add_argument("--views-per-scene", type=int, default=2, help="views (windows) rendered from each seeded scene")
     ap.add_argument("--window", type=int, default=1024)
     ap.add_argument("--crop", type=int, default=256)
     ap.add_argument("--inputs", type=int, default=16)
@@ -222,7 +223,7 @@ def main(argv=None):
 
     dev = torch.device("cuda", 0)
     t0 = time.time()
-    views = default_views(a.views)
+    views = default_views(a.views, views_per_scene=a.views_per_scene)
     data = render_views(views, a.window, a.crop, inputs=a.inputs, target_spp=a.target_spp, max_depth=a.max_depth,
                         min_depth=a.min_depth, texture_size=a.texture_size, instances=a.instances, device=dev)
     t_data = time.time() - t0
@@ -232,7 +233,8 @@ def main(argv=None):
     torch.cuda.synchronize()
     t_train = time.time() - t1
     net.save(a.out)
-    rec = {"views": len(views), "crops": int(data["illum"].shape[0]), "inputs_per_crop": a.inputs,
+    rec = {"views": len(views), "scene_count": len({(k, s) for k, s, _ in views}), "window": a.window,
+           "crops": int(data["illum"].shape[0]), "inputs_per_crop": a.inputs,
            "target_spp": a.target_spp, "steps": a.steps, "batch": a.batch, "lr": a.lr, "data_s": t_data,
            "train_s": t_train, "loss": hist, "scenes": sorted({(k, s) for k, s, _ in views})}
     if a.log:

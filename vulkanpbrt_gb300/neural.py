@@ -39,7 +39,7 @@ GATE = Path(__file__).resolve().parent / "weights" / "gate.json"
 
 
 def gate_coefficients(path=None) -> np.ndarray:
-    """The learned tile gate's 8 weights and bias (default: the packaged fit)."""
+    """The learned tile gate's 4 x 9 coefficients (default: the packaged fit)."""
     import json
 
     d = json.loads(Path(path or GATE).read_text())
@@ -70,10 +70,11 @@ class NeuralDenoiser(Handle):
     """Denoises the demodulated illumination of `illu_buffer` (one sample, or
     the Accumulator's output with `acc_buffer` giving the sample counts) with
     the G-buffer's albedo, normal and depth. With `fallback` (a BMFR over the
-    same frame, dispatched first), tiles the learned gate scores above zero
-    (gate_model "default": the packaged coefficients; or 9 numbers) show
-    BMFR's final image; with gate_model None the rule is the mean predicted
-    error of the tile above `threshold`."""
+    same frame, dispatched first), the learned gate shows per tile the blend
+    of the network's and BMFR's outputs it predicts best (gate_model
+    "default": the packaged coefficients; or 36 numbers); with gate_model
+    None, tiles whose mean predicted error exceeds `threshold` show BMFR's
+    final image."""
 
     def __init__(self, width: int, height: int, g_buffer: GBuffer, illu_buffer: IlluminationBuffer, weights=None,
                  fallback: BMFR | None = None, threshold: float = 0.5, tile: int = 32, acc_buffer=None,
@@ -91,12 +92,13 @@ class NeuralDenoiser(Handle):
         check(lib().pbrt_neural_final_image(h, C.byref(f)))
         self.denoised, self.variance, self._final = Image(d, self), Image(v, self), Image(f, self)
         self._fallback = None
+        self.gate_coef = None
         self.set_fallback(fallback, threshold, tile)
         if fallback is not None and gate_model is not None:
             self.set_gate_model(gate_coefficients() if isinstance(gate_model, str) else gate_model)
 
     def set_gate_model(self, coef) -> None:
-        """Learned tile gate (8 weights, bias; see pbrt_nn_gate_model) or None for the threshold rule."""
+        """Learned tile gate (4 x 9 coefficients; see pbrt_nn_gate_model) or None for the threshold rule."""
         if coef is None:
             check(lib().pbrt_neural_set_gate_model(self.ptr, None, 0))
             self.gate_coef = None

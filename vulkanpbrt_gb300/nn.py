@@ -32,7 +32,7 @@ _abi.add_signatures({
     "pbrt_nn_relmse_loss": (i32, [H, H, H, H, i32, i32, i32, i32, i32, f32, H, H, H, H]),
     "pbrt_nn_adam": (i32, [H, H, H, H, H, i64, f32, f32, f32, f32, i32, f32, H]),
     "pbrt_nn_gate": (i32, [H, i32, i32, i32, f32, i32, H, H, H]),
-    "pbrt_nn_gate_model": (i32, [H, i32, i32, i32, i32, H, H, H, i32, H, H, H, H, H, H, H, H]),
+    "pbrt_nn_gate_model": (i32, [H, H, i32, i32, i32, i32, H, H, H, H, H, i32, H, H, H, H, H, H, H, H, H]),
     "pbrt_nn_compose": (i32, [H, i32, i32, i32, H, H, i32, H, H, H, H]),
 })
 
