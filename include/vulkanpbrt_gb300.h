@@ -529,6 +529,23 @@ PBRT_API int pbrt_nn_conv3x3_umma(const void* x1, int32_t c1, const void* x2, in
 PBRT_API int pbrt_nn_conv3x3_umma_pooled(const void* x1, int32_t c1, const void* w, const float* bias, void* y,
                                          void* pooled, int32_t n, int32_t h, int32_t wd, int32_t cout, int32_t flags,
                                          pbrt_stream_t stream);
+/* Backward weights on tcgen05: the arguments of pbrt_nn_conv3x3_wgrad (dw
+ * [cout][9][c1+c2] FP32, added to), cout <= 128, c1 + c2 <= 256, 16-byte
+ * aligned inputs. One CTA a (pixel run, tap): dY and the shifted input are
+ * the MMA's MN-major operands as stored, the sum over the run in tensor
+ * memory, then atomics into dw. */
+PBRT_API int pbrt_nn_conv3x3_wgrad_umma(const void* dy, const void* x1, int32_t c1, const void* x2, int32_t c2,
+                                        float* dw, int32_t n, int32_t h, int32_t w_px, int32_t cout,
+                                        pbrt_stream_t stream);
+/* tcgen05 convolution of a single input with an FP32 output y32
+ * [n][h][wd][cout] (16-byte aligned operands): the backward-data pass of
+ * training (dY with pbrt_nn_flip_weights' weights). Any cout that is a
+ * multiple of 16: the output channels run in slices whose weights fit in
+ * shared memory, one launch a slice. flags bit 0: ReLU, bit 2: no TMA.
+ * PBRT_ERROR_UNSUPPORTED when no slice fits (c1 too large). */
+PBRT_API int pbrt_nn_conv3x3_umma_f32(const void* x1, int32_t c1, const void* w, const float* bias, float* y32,
+                                      int32_t n, int32_t h, int32_t wd, int32_t cout, int32_t flags,
+                                      pbrt_stream_t stream);
 /* The FP8 convolution on the tcgen05 tensor cores (kind::f8f6f4, K = 32 per
  * instruction): the arguments and quantisation of pbrt_nn_conv3x3_fp8, cout
  * in {16, 32, ..., 128}, plus an optional pooled output as in

@@ -6,7 +6,8 @@ the training path), then a short training run that must lower the loss.
 Tolerances: outputs and losses within 2e-2 relative (BF16 activations
 rounded at the same points, FP32 accumulation in a different order); each
 parameter gradient within 6e-2 relative L2 error and cosine similarity above
-0.995 (the GPU also rounds the ReLU-masked gradients to BF16)."""
+0.995 (the GPU also rounds the ReLU-masked gradients to BF16). Checked with
+the forward and backward-data convolutions on mma.sync and on tcgen05."""
 import numpy as np
 import pytest
 
@@ -40,7 +41,8 @@ def _params(seed):
     return p
 
 
-def test_forward_loss_and_gradients_match_reference(cuda):
+@pytest.mark.parametrize("kernel", ["mma", "umma"])
+def test_forward_loss_and_gradients_match_reference(cuda, kernel):
     import torch
 
     from tests import kpunet_reference as ref
@@ -52,9 +54,9 @@ def test_forward_loss_and_gradients_match_reference(cuda):
     net = K.KPUNet(cuda, params=p)
     ws = net.workspace(n, h, w)
     ws.set_input(illum.to(cuda), albedo.to(cuda), normal.to(cuda), depth.to(cuda))
-    out = ws.forward()
+    out = ws.forward(kernel)
     net.grad.zero_()
-    ws.loss_and_grad(target.to(cuda), albedo.to(cuda), var_weight=0.1)
+    ws.loss_and_grad(target.to(cuda), albedo.to(cuda), var_weight=0.1, kernel=kernel)
     torch.cuda.synchronize()
 
     feat, rad = ref.features(illum, albedo, normal, depth, h, w)

@@ -58,8 +58,12 @@ def test_conv3x3_forward(cuda, n, h, w, c1, c2, cout, kernel):
     assert _close(yr, ref.clamp_min(0), 4e-3)[1]
 
 
-@pytest.mark.parametrize("n,h,w,cin,cout", [(2, 24, 40, 16, 32), (1, 32, 32, 48, 64), (2, 16, 24, 64, 32)])
-def test_conv3x3_backward_data_and_weight(cuda, n, h, w, cin, cout):
+@pytest.mark.parametrize("wkernel", ["mma", "umma"])
+@pytest.mark.parametrize("n,h,w,cin,cout", [(2, 24, 40, 16, 32), (1, 32, 32, 48, 64), (2, 16, 24, 64, 32),
+                                             (1, 18, 34, 224, 96), (2, 64, 96, 32, 32), (1, 20, 36, 128, 128)])
+def test_conv3x3_backward_data_and_weight(cuda, n, h, w, cin, cout, wkernel):
+    """Backward data (the forward kernel on the flipped weights) and backward
+    weights (wkernel: the mma.sync or the tcgen05 kernel)."""
     import torch
     import torch.nn.functional as F
 
@@ -81,8 +85,9 @@ def test_conv3x3_backward_data_and_weight(cuda, n, h, w, cin, cout):
     dx = torch.empty(n, h, w, cin, device=cuda)
     nn.conv3x3(dy.to(cuda), wflip, None, out32=dx)
     dw = torch.zeros(cout, 9, cin, device=cuda)
-    nn.conv3x3_wgrad(dy.to(cuda), x.to(cuda), dw)
+    nn.conv3x3_wgrad(dy.to(cuda), x.to(cuda), dw, kernel=wkernel)
     torch.cuda.synchronize()
+    assert nn.umma_status() == 0
     rel, ok = _close(dx, dx_ref, 1e-4)
     print(f"dgrad rel err {rel:.2e}")
     assert ok
@@ -91,7 +96,35 @@ def test_conv3x3_backward_data_and_weight(cuda, n, h, w, cin, cout):
     assert ok
 
 
-def test_conv3x3_wgrad_with_upsampled_concat(cuda):
+@pytest.mark.parametrize("n,h,w,cin,cout", [(2, 24, 40, 16, 32), (1, 32, 32, 48, 64), (2, 16, 24, 64, 32),
+                                             (1, 18, 34, 224, 96), (1, 9, 17, 128, 128), (1, 40, 24, 80, 32)])
+def test_conv3x3_dgrad_tcgen05(cuda, n, h, w, cin, cout):
+    """Backward data on tcgen05 (pbrt_nn_conv3x3_umma_f32: dY with the flipped
+    weights, FP32 out, the input channels in slices that fit in shared memory:
+    224 in four, 128 from 128 in three) against torch's FP32 gradient."""
+    import torch
+    import torch.nn.functional as F
+
+    from vulkanpbrt_gb300 import nn
+
+    g = torch.Generator().manual_seed(17 + cin + cout + h)
+    wt = (torch.randn(cout, 9, cin, generator=g) * 0.1).bfloat16()
+    dy = torch.randn(n, h, w, cout, generator=g).bfloat16()
+    xr = torch.zeros(n, cin, h, w, requires_grad=True)
+    wr = wt.float().reshape(cout, 3, 3, cin).permute(0, 3, 1, 2)
+    F.conv2d(xr, wr, padding=1).backward(dy.float().permute(0, 3, 1, 2))
+    dx_ref = xr.grad.permute(0, 2, 3, 1)
+    wflip = nn.flip_weights(wt.to(cuda))
+    dx = torch.full((n, h, w, cin), float("nan"), device=cuda)
+    nn.conv3x3_umma_f32(dy.to(cuda), wflip, dx)
+    assert nn.umma_status() == 0
+    rel, ok = _close(dx, dx_ref, 1e-4)
+    print(f"tcgen05 dgrad rel err {rel:.2e}")
+    assert ok
+
+
+@pytest.mark.parametrize("wkernel", ["mma", "umma"])
+def test_conv3x3_wgrad_with_upsampled_concat(cuda, wkernel):
     import torch
     import torch.nn.functional as F
 
@@ -108,6 +141,7 @@ def test_conv3x3_wgrad_with_upsampled_concat(cuda):
     F.conv2d(xc, wr, padding=1).backward(dy.float().permute(0, 3, 1, 2))
     dw_ref = wr.grad.permute(0, 2, 3, 1).reshape(cout, 9, c1 + c2)
     dw = torch.zeros(cout, 9, c1 + c2, device=cuda)
-    nn.conv3x3_wgrad(dy.to(cuda), x1.to(cuda), dw, x2=x2.to(cuda))
+    nn.conv3x3_wgrad(dy.to(cuda), x1.to(cuda), dw, x2=x2.to(cuda), kernel=wkernel)
     torch.cuda.synchronize()
+    assert nn.umma_status() == 0
     assert _close(dw, dw_ref, 1e-4)[1]

@@ -12,8 +12,11 @@ to guarantee: the stage holds this tile's data (all parts), a stage is not
 refilled while MMAs still read it, an accumulator buffer is drained before
 it is reused and holds this tile's result when drained. Random schedules
 cover 2-6 stages, with and without the TMA producer and the gather warps,
-and the FP8 form (the TMA completing on its own barrier, the gather warp
-quantising after it). The superseded ownership rule (gather warp i % 4,
+the FP8 form (the TMA completing on its own barrier, the gather warp
+quantising after it), and the TMA load of the second input's
+half-resolution box (completing on its own barrier; the gather warp expands
+it into the stage's planes, and the producer must not refill the box while
+the gather warp reads it). The superseded ownership rule (gather warp i % 4,
 which let two warps share a stage when there were fewer stages than gather
 warps) is checked to fail, so the model is shown to catch that fault."""
 import random
@@ -44,12 +47,15 @@ class Violation(AssertionError):
     pass
 
 
-def run(stages, tiles, tma, gather, fp8, owner, rng):
+def run(stages, tiles, tma, gather, fp8, owner, rng, stg=False):
     """One random schedule of one CTA's roles over `tiles` tiles. Raises Violation on a broken guarantee,
     returns False on a deadlock (no role can move), True when every role finished."""
     full = [Barrier((0 if fp8 else (1 if tma else 0)) + (1 if gather else 0)) for _ in range(stages)]
     empty = [Barrier(1) for _ in range(stages)]
     tmab = [Barrier(1) for _ in range(stages)]  # FP8: the TMA's own barrier
+    stgb = [Barrier(1) for _ in range(stages)]  # the half-resolution box's barrier
+    stg_part = [None] * stages
+    expanding = [False] * stages
     tfull = [Barrier(1) for _ in range(2)]
     tempty = [Barrier(1) for _ in range(2)]
     # stage contents: which tile's TMA part / gathered part is in place; MMAs reading the stage
@@ -69,7 +75,11 @@ def run(stages, tiles, tma, gather, fp8, owner, rng):
                 yield
             if readers[st]:
                 raise Violation(f"TMA refills stage {st} for tile {i} while MMAs read it")
-            inflight_tma.append((st, i))
+            if expanding[st]:
+                raise Violation(f"TMA refills stage {st}'s box for tile {i} while the gather warp expands it")
+            inflight_tma.append((st, i, "x1"))
+            if stg:
+                inflight_tma.append((st, i, "x2"))
             yield
 
     def gatherer(gw):
@@ -83,6 +93,14 @@ def run(stages, tiles, tma, gather, fp8, owner, rng):
                 raise Violation(f"gather warp {gw} refills stage {st} for tile {i} while MMAs read it")
             gat_part[st] = i
             yield
+            if stg:
+                while not stgb[st].passes(k & 1):
+                    yield
+                if stg_part[st] != i:
+                    raise Violation(f"tile {i}: expanded stage {st} before its box landed")
+                expanding[st] = True
+                yield
+                expanding[st] = False
             if fp8:
                 if tma:
                     while not tmab[st].passes(k & 1):
@@ -102,6 +120,8 @@ def run(stages, tiles, tma, gather, fp8, owner, rng):
                 raise Violation(f"MMA of tile {i}: stage {st} holds TMA part of tile {tma_part[st]}")
             if gather and gat_part[st] != i:
                 raise Violation(f"MMA of tile {i}: stage {st} holds gathered part of tile {gat_part[st]}")
+            if stg and stg_part[st] != i:
+                raise Violation(f"MMA of tile {i}: stage {st} expanded from the box of tile {stg_part[st]}")
             if fp8 and converted[st] != i:
                 raise Violation(f"MMA of tile {i}: stage {st} not quantised")
             while not tempty[b].passes((kb & 1) ^ 1):
@@ -135,7 +155,11 @@ def run(stages, tiles, tma, gather, fp8, owner, rng):
 
     def complete_tma():
         j = rng.randrange(len(inflight_tma))
-        st, i = inflight_tma.pop(j)
+        st, i, part = inflight_tma.pop(j)
+        if part == "x2":
+            stg_part[st] = i
+            stgb[st].arrive()
+            return
         tma_part[st] = i
         (tmab if fp8 else full)[st].arrive()
 
@@ -161,12 +185,14 @@ def run(stages, tiles, tma, gather, fp8, owner, rng):
             complete_mma()
             stuck = 0
         else:
-            before = (len(inflight_tma), len(inflight_mma), [b.phase for b in full + empty + tmab + tfull + tempty])
+            before = (len(inflight_tma), len(inflight_mma),
+                      [b.phase for b in full + empty + tmab + stgb + tfull + tempty], list(expanding))
             try:
                 next(r)
             except StopIteration:
                 live.remove(r)
-            after = (len(inflight_tma), len(inflight_mma), [b.phase for b in full + empty + tmab + tfull + tempty])
+            after = (len(inflight_tma), len(inflight_mma),
+                     [b.phase for b in full + empty + tmab + stgb + tfull + tempty], list(expanding))
             stuck = stuck + 1 if before == after else 0
         if stuck > 20000:
             return False
@@ -189,6 +215,15 @@ def test_ring_protocol_holds(stages, tma, gather, fp8):
     for _ in range(150):
         tiles = rng.randrange(1, 4 * stages + 6)
         assert run(stages, tiles, tma, gather, fp8, owner_kernel, rng), "deadlock"
+
+
+@pytest.mark.parametrize("stages", [2, 3, 4, 5, 6])
+@pytest.mark.parametrize("fp8", [False, True])
+def test_ring_protocol_holds_with_box(stages, fp8):
+    rng = random.Random(stages * 13 + fp8)
+    for _ in range(150):
+        tiles = rng.randrange(1, 4 * stages + 6)
+        assert run(stages, tiles, True, True, fp8, owner_kernel, rng, stg=True), "deadlock"
 
 
 def test_model_catches_shared_stage_ownership():

@@ -40,6 +40,9 @@ constexpr int kHaloH = kTileH + 2, kHaloW = kTileW + 2, kHaloPx = kHaloH * kHalo
 constexpr int kKC = 32;                    // input channels per chunk
 constexpr int kPlanes = kKC / 8;           // 8-channel planes per chunk
 constexpr int kPlaneBytes = kHaloPx * 16;  // one plane of the halo: 2880 B
+// the half-resolution second input under a halo: 6 x 10 pixels a plane
+constexpr int kStgW = kTileW / 2 + 2, kStgH = kTileH / 2 + 2;
+constexpr int kStgPlaneBytes = kStgW * kStgH * 16;  // 960 B
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -122,6 +125,10 @@ struct UmmaConvArgs {
   const uint8_t* w8 = nullptr;
   const float* wscale = nullptr;      // [cout]
   const float* inv_xscale = nullptr;  // [c1 + c2]
+  // FP32 output instead of y (warp-specialised BF16 kernel only): pixel p's
+  // channels at y32[p * ldy32 .. + cout)
+  float* y32 = nullptr;
+  int ldy32 = 0;
 };
 
 template <int NC>  // output channels (= MMA N), multiple of 16, <= 128
@@ -549,13 +556,15 @@ __device__ __forceinline__ uint32_t quant4_e4m3(uint32_t lo2, uint32_t hi2, cons
 template <int NC, bool kF8>
 __global__ void __launch_bounds__(kWsThreads, kF8 ? 3 : 0) conv3x3_umma_ws_kernel(UmmaConvArgs a, int tiles_per_image,
                                                                      const __grid_constant__ CUtensorMap x1map,
-                                                                     int use_tma, int stages) {
+                                                                     const __grid_constant__ CUtensorMap x2map,
+                                                                     int use_tma, int stg_planes, int stages) {
   using namespace umma;
   constexpr uint32_t kCols = 2 * NC <= 64 ? 64 : (2 * NC <= 128 ? 128 : 256);
   constexpr int kMaxStages = 6;
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t full_bar[kMaxStages], empty_bar[kMaxStages], tfull_bar[2], tempty_bar[2];
   __shared__ __align__(8) uint64_t tma_bar[kF8 ? kMaxStages : 1];  // FP8: the TMA's arrival per stage
+  __shared__ __align__(8) uint64_t stg_bar[kMaxStages];             // the half-resolution x2 box's arrival
   __shared__ uint32_t tmem_base_slot;
   __shared__ volatile int abort_flag;
   __shared__ __align__(16) float s_bias[NC];
@@ -569,7 +578,10 @@ __global__ void __launch_bounds__(kWsThreads, kF8 ? 3 : 0) conv3x3_umma_ws_kerne
   // them in place into its e4m3 planes (at most the same bytes)
   const int in_planes = cin / 8;
   const int halo_bytes = in_planes * kPlaneBytes;
-  const int halo_pitch = (halo_bytes + 1023) & ~1023;
+  // stage: the halo planes, then (stg_planes > 0) the TMA's half-resolution
+  // box of the second input, which the gather warp expands into its planes
+  const int stg_off = (halo_bytes + 127) & ~127;
+  const int halo_pitch = (stg_off + stg_planes * kStgPlaneBytes + 1023) & ~1023;
   const int tiles_x = (a.W + kTileW - 1) / kTileW;
   const int total_tiles = tiles_per_image * a.N;
   const int H2 = a.H >> 1, W2 = a.W >> 1;
@@ -583,11 +595,13 @@ __global__ void __launch_bounds__(kWsThreads, kF8 ? 3 : 0) conv3x3_umma_ws_kerne
   auto tfb = [&](int b) { return smem_addr(&tfull_bar[b]); };
   auto teb = [&](int b) { return smem_addr(&tempty_bar[b]); };
   auto tmb = [&](int st) { return smem_addr(&tma_bar[kF8 ? st : 0]); };
+  auto sgb = [&](int st) { return smem_addr(&stg_bar[st]); };
   if (tid == 0) {
     for (int st = 0; st < stages; ++st) {
       umma::mbar_init(fb(st), kF8 ? 32u : (x1_planes ? 1u : 0u) + (gather ? 32u : 0u));
       umma::mbar_init(eb(st), 1);
       if (kF8) umma::mbar_init(tmb(st), 1);
+      if (stg_planes) umma::mbar_init(sgb(st), 1);
     }
     for (int b = 0; b < 2; ++b) {
       umma::mbar_init(tfb(b), 1);
@@ -642,13 +656,13 @@ __global__ void __launch_bounds__(kWsThreads, kF8 ? 3 : 0) conv3x3_umma_ws_kerne
   if (warp == 0) {
     // ---- producer (TMA of the x1 planes)
     int i = 0;
-    for (int t = blockIdx.x; t < total_tiles && !abort_flag && x1_planes; t += gridDim.x, ++i) {
+    for (int t = blockIdx.x; t < total_tiles && !abort_flag && (x1_planes || stg_planes); t += gridDim.x, ++i) {
       const int st = i % stages, k = i / stages;
       if (!wait(eb(st), (uint32_t)((k & 1) ^ 1))) break;  // the MMAs of the stage's previous tile are done
       const uint32_t hb = hbase + st * halo_pitch;
       int img, x0, y0;
       tile_origin(t, img, x0, y0);
-      if (lane == 0) {
+      if (lane == 0 && x1_planes) {
         const uint32_t bar = kF8 ? tmb(st) : fb(st);  // FP8: the quantising warp waits for the load
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar),
                      "r"((uint32_t)(x1_planes * kPlaneBytes))
@@ -657,6 +671,19 @@ __global__ void __launch_bounds__(kWsThreads, kF8 ? 3 : 0) conv3x3_umma_ws_kerne
             "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
             "%5, %6}], [%7];\n" ::"r"(hb),
             "l"(reinterpret_cast<uint64_t>(&x1map)), "r"(0), "r"(x0 - 1), "r"(y0 - 1), "r"(0), "r"(img), "r"(bar)
+            : "memory");
+      }
+      if (lane == 0 && stg_planes) {
+        // the 6 x 10 half-resolution pixels under the tile's halo (x0 % 8 == 0,
+        // y0 % 16 == 0: columns x0/2 - 1 .. x0/2 + 4, rows y0/2 - 1 .. y0/2 + 8)
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(sgb(st)),
+                     "r"((uint32_t)(stg_planes * kStgPlaneBytes))
+                     : "memory");
+        asm volatile(
+            "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+            "%5, %6}], [%7];\n" ::"r"(hb + stg_off),
+            "l"(reinterpret_cast<uint64_t>(&x2map)), "r"(0), "r"((x0 >> 1) - 1), "r"((y0 >> 1) - 1), "r"(0), "r"(img),
+            "r"(sgb(st))
             : "memory");
       }
       ++tma_issued;
@@ -676,7 +703,8 @@ __global__ void __launch_bounds__(kWsThreads, kF8 ? 3 : 0) conv3x3_umma_ws_kerne
       int img, x0, y0;
       tile_origin(t, img, x0, y0);
       {
-        for (int q = lane + x1_planes * kHaloPx; q < kHaloPx * in_planes; q += 32) {
+        const int gathered = stg_planes ? a.c1 / 8 : in_planes;  // planes fetched by cp.async end here
+        for (int q = lane + x1_planes * kHaloPx; q < kHaloPx * gathered; q += 32) {
           const int hp = q % kHaloPx, p = q / kHaloPx;
           const int yy = y0 - 1 + hp / kHaloW, xx = x0 - 1 + hp % kHaloW;
           const int ci = p * 8;
@@ -691,6 +719,26 @@ __global__ void __launch_bounds__(kWsThreads, kF8 ? 3 : 0) conv3x3_umma_ws_kerne
         // this lane's copies landed and made visible to the tensor cores, then one arrival
         asm volatile("cp.async.commit_group;\n" ::);
         asm volatile("cp.async.wait_group 0;\n" ::);
+        if (stg_planes) {
+          // nearest upsampling of the half-resolution box into the second
+          // input's planes: halo pixel (hy, hx) is box pixel ((hy + 1) / 2,
+          // (hx + 1) / 2); outside the frame the box holds the TMA's zeros
+          if (!wait(sgb(st), (uint32_t)(k & 1))) break;
+          const uint32_t sb = hb + stg_off, db = hb + (a.c1 / 8) * kPlaneBytes;
+          for (int q = lane; q < stg_planes * kHaloPx; q += 32) {
+            const int p = q / kHaloPx, hp = q - p * kHaloPx;
+            const int hy = hp / kHaloW, hx = hp - hy * kHaloW;
+            const uint32_t src = sb + p * kStgPlaneBytes + (((hy + 1) >> 1) * kStgW + ((hx + 1) >> 1)) * 16;
+            uint32_t v0, v1, v2, v3;
+            asm volatile("ld.shared.v4.b32 {%0, %1, %2, %3}, [%4];\n"
+                         : "=r"(v0), "=r"(v1), "=r"(v2), "=r"(v3)
+                         : "r"(src)
+                         : "memory");
+            asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};\n" ::"r"(db + p * kPlaneBytes + hp * 16), "r"(v0),
+                         "r"(v1), "r"(v2), "r"(v3)
+                         : "memory");
+          }
+        }
         if constexpr (kF8) {
           // every BF16 plane in place (the TMA's and the warp's copies), then
           // each 16-channel pair quantised into e4m3 plane p at the offset of
@@ -783,7 +831,9 @@ __global__ void __launch_bounds__(kWsThreads, kF8 ? 3 : 0) conv3x3_umma_ws_kerne
       const int m = sub * 32 + lane;
       const int oy = y0 + m / kTileW, ox = x0 + m % kTileW;
       const bool inside = oy < a.H && ox < a.W;
-      bf16* dst = a.y + (((size_t)img * a.H + (inside ? oy : 0)) * a.W + (inside ? ox : 0)) * a.cout;
+      const size_t pix = ((size_t)img * a.H + (inside ? oy : 0)) * a.W + (inside ? ox : 0);
+      bf16* dst = a.y32 ? nullptr : a.y + pix * a.cout;
+      float* dst32 = a.y32 ? a.y32 + pix * a.ldy32 : nullptr;
       // two 16-column loads in flight before one wait (fewer tensor-memory round trips)
 #pragma unroll
       for (int c00 = 0; c00 < NC; c00 += 32) {
@@ -806,7 +856,17 @@ __global__ void __launch_bounds__(kWsThreads, kF8 ? 3 : 0) conv3x3_umma_ws_kerne
         const int c0 = c00 + 16 * h;
         if (c0 >= NC) break;
         const uint32_t* v = vv[h];
-        if (inside) {
+        if (inside && dst32) {  // FP32 output (no FP8 scale, no pooling)
+          float f[16];
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            f[j] = __uint_as_float(v[j]) + (a.bias ? s_bias[c0 + j] : 0.f);
+            if (a.relu & 1) f[j] = fmaxf(f[j], 0.f);
+          }
+          float4* d4 = reinterpret_cast<float4*>(dst32 + c0);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) d4[j] = make_float4(f[4 * j], f[4 * j + 1], f[4 * j + 2], f[4 * j + 3]);
+        } else if (inside) {
           uint32_t packed[8];
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
@@ -880,14 +940,15 @@ __global__ void __launch_bounds__(kWsThreads, kF8 ? 3 : 0) conv3x3_umma_ws_kerne
       const int last = n_mine - 1;
       umma::mbar_wait(tfb(last & 1), (uint32_t)((last >> 1) & 1));
     }
-    if (x1_planes && warp == 0 && lane == 0) {
+    if ((x1_planes || stg_planes) && warp == 0 && lane == 0) {
       // TMA loads still in flight land before the CTA's shared memory is
       // released: the last load into each stage, bounded (FP8: the load's own
       // barrier; BF16: the stage's full barrier, which with gather warps also
       // waits for their arrivals and may give up at the bound)
       for (int st = 0; st < stages && st < tma_issued; ++st) {
         const int j = tma_issued - 1 - (tma_issued - 1 - st) % stages;  // last tile loaded into stage st
-        umma::mbar_wait(kF8 ? tmb(st) : fb(st), (uint32_t)((j / stages) & 1));
+        if (x1_planes) umma::mbar_wait(kF8 ? tmb(st) : fb(st), (uint32_t)((j / stages) & 1));
+        if (stg_planes) umma::mbar_wait(sgb(st), (uint32_t)((j / stages) & 1));
       }
     }
     __syncthreads();
@@ -895,6 +956,187 @@ __global__ void __launch_bounds__(kWsThreads, kF8 ? 3 : 0) conv3x3_umma_ws_kerne
   if (warp == 1) {
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kCols));
+  }
+}
+
+// Backward weights on tcgen05: dW[co][tap][ci] += sum over pixels p of
+// dY[p][co] * X(p shifted by the tap)[ci], one CTA a (pixel run, tap). The
+// GEMM has M = 128 output channels (rows past cout are zeros), N = cin and
+// K = pixels, 64 a stage. Both operands sit in shared memory exactly as they
+// are stored in global memory -- each pixel's channels contiguous -- which is
+// the MN-major no-swizzle layout: a core matrix is 8 pixels (K) x 8
+// channels (16 bytes, M or N), core matrices of consecutive pixel groups
+// 128 bytes apart (the K stride) and of consecutive channel groups 1024
+// bytes apart (the M/N stride). So every 16-byte cp.async lands in place.
+// Thread 0 issues four K = 16 MMAs a stage and commits them to the stage's
+// mbarrier; the next loads into that stage wait for it. The FP32
+// accumulator (TMEM lane = co, column = ci) is added into dW with atomics.
+// Every wait is bounded: on a timeout the kernel records the error
+// (pbrt_nn_umma_status), waits again for its own MMAs and frees its tensor
+// memory.
+struct UmmaWgradArgs {
+  const bf16* dy;  // [N][H][W][cout]
+  const bf16* x1;  // [N][H][W][c1]
+  const bf16* x2;  // [N][H/2][W/2][c2], upsampled on load, or null
+  int c1, c2;
+  float* dw;  // [cout][9][c1 + c2]
+  int N, H, W, cout;
+  int pix_per_cta;
+};
+constexpr int kWgK = 64;                     // pixels a stage
+constexpr int kWgStages = 4;
+constexpr int kWgABytes = 16 * 8 * 128;      // 128 rows x 64 pixels
+__host__ __device__ constexpr int wgrad_stage_bytes(int cin) { return kWgABytes + (cin / 8) * 8 * 128; }
+
+__global__ void __launch_bounds__(128) conv3x3_wgrad_umma_kernel(UmmaWgradArgs a) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ __align__(8) uint64_t mbar[kWgStages];
+  __shared__ uint32_t tmem_base_slot;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int cin = a.c1 + a.c2;
+  const int tap = blockIdx.y, dy = tap / 3 - 1, dx = tap % 3 - 1;
+  const long P = (long)a.N * a.H * a.W;
+  const long p_begin = (long)blockIdx.x * a.pix_per_cta;
+  const long p_end = p_begin + a.pix_per_cta < P ? p_begin + a.pix_per_cta : P;
+  const int n_it = p_begin < p_end ? (int)((p_end - p_begin + kWgK - 1) / kWgK) : 0;
+  const int H2 = a.H >> 1, W2 = a.W >> 1;
+  const uint32_t cols = cin <= 32 ? 32u : (cin <= 64 ? 64u : (cin <= 128 ? 128u : 256u));
+  const int stage_bytes = wgrad_stage_bytes(cin);
+  const uint32_t sbase = (umma::smem_addr(smem) + 1023u) & ~1023u;
+  auto mb = [&](int st) { return umma::smem_addr(&mbar[st]); };
+  if (tid == 0) {
+    for (int st = 0; st < kWgStages; ++st) umma::mbar_init(mb(st), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                     umma::smem_addr(&tmem_base_slot)),
+                 "r"(cols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+  }
+  // the A rows past cout stay zero in every stage
+  for (int st = 0; st < kWgStages; ++st)
+    for (int i = tid * 16 + (a.cout / 8) * 1024; i < kWgABytes; i += 128 * 16)
+      asm volatile("st.shared.v4.b32 [%0], {%1, %1, %1, %1};\n" ::"r"(sbase + st * stage_bytes + i), "r"(0)
+                   : "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = tmem_base_slot;
+
+  auto load = [&](int st, int it) {
+    const uint32_t ab = sbase + st * stage_bytes, bb = ab + kWgABytes;
+    const long pb = p_begin + (long)it * kWgK;
+    const int ga = a.cout / 8, gb = cin / 8;
+    for (int q = tid; q < kWgK * (ga + gb); q += 128) {
+      const int pl = q % kWgK, g = q / kWgK;  // consecutive threads: consecutive pixels
+      const long p = pb + pl;
+      const bool pv = p < p_end;
+      const long pp = pv ? p : 0;
+      const uint32_t off = (uint32_t)((pl >> 3) * 128 + (pl & 7) * 16);
+      if (g < ga) {
+        umma::cp16(ab + g * 1024 + off, a.dy + pp * a.cout + g * 8, pv);
+      } else {
+        const int ci = (g - ga) * 8;
+        const int n = (int)(pp / ((long)a.H * a.W));
+        const int rem = (int)(pp - (long)n * a.H * a.W);
+        const int yy = rem / a.W + dy, xx = rem % a.W + dx;
+        const bool ok = pv && yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
+        const bf16* src = a.x1;
+        if (ok) {
+          if (ci < a.c1) src = a.x1 + (((size_t)n * a.H + yy) * a.W + xx) * a.c1 + ci;
+          else src = a.x2 + (((size_t)n * H2 + (yy >> 1)) * W2 + (xx >> 1)) * a.c2 + (ci - a.c1);
+        }
+        umma::cp16(bb + (g - ga) * 1024 + off, src, ok);
+      }
+    }
+  };
+
+  bool failed = false;
+  int issued = 0;  // iterations whose MMAs were issued (the same count in every thread)
+  for (int j = 0; j < kWgStages - 1; ++j) {
+    if (j < n_it) load(j, j);
+    asm volatile("cp.async.commit_group;\n" ::);
+  }
+  // MN-major (transposed) A and B, BF16, FP32 accumulator, M = 128, N = cin
+  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) | ((uint32_t)(cin >> 3) << 17) |
+                         ((uint32_t)(128 >> 4) << 24);
+  for (int it = 0; it < n_it && !failed; ++it) {
+    const int st = it % kWgStages;
+    const int j = it + kWgStages - 1;  // refill the stage the previous iteration's MMAs read
+    if (j < n_it) {
+      bool ok = true;
+      if (it >= 1) ok = umma::mbar_wait(mb((it - 1) % kWgStages), (uint32_t)(((it - 1) / kWgStages) & 1));
+      if (__syncthreads_or(!ok)) {
+        failed = true;
+        break;
+      }
+      load(j % kWgStages, j);
+    }
+    asm volatile("cp.async.commit_group;\n" ::);
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(kWgStages - 1));
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      const uint32_t ab = sbase + st * stage_bytes, bb = ab + kWgABytes;
+#pragma unroll
+      for (int ks = 0; ks < kWgK / 16; ++ks) {
+        // K step of 16 pixels = two core-matrix columns, 128 bytes each
+        const uint64_t da = umma::sdesc(ab + ks * 256, 128, 1024);
+        const uint64_t db = umma::sdesc(bb + ks * 256, 128, 1024);
+        const uint32_t acc = (it > 0 || ks > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "setp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+            "l"(da), "l"(db), "r"(idesc), "r"(acc));
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mb(st))
+                   : "memory");
+    }
+    ++issued;
+  }
+  asm volatile("cp.async.wait_group 0;\n" ::);
+  __syncthreads();
+  if (n_it > 0) {
+    // the last MMAs issued (and with them every earlier one) complete before
+    // the accumulator is read or freed
+    const int last = issued - 1;
+    bool done = true;
+    if (last >= 0) {
+      done = umma::mbar_wait(mb(last % kWgStages), (uint32_t)((last / kWgStages) & 1));
+      if (!done) done = umma::mbar_wait(mb(last % kWgStages), (uint32_t)((last / kWgStages) & 1));
+    }
+    failed = __syncthreads_or(failed || !done);
+    if (failed) {
+      if (tid == 0) atomicOr(&g_umma_error, 1u);
+    } else {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      const int co = warp * 32 + lane;  // TMEM lane
+      float* drow = a.dw + ((size_t)(co < a.cout ? co : 0) * 9 + tap) * cin;
+      for (int c0 = 0; c0 < cin; c0 += 16) {
+        uint32_t v[16];
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+            "[%16];\n"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        if (co < a.cout) {
+#pragma unroll
+          for (int k = 0; k < 16; ++k) atomicAdd(drow + c0 + k, __uint_as_float(v[k]));
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(cols));
   }
 }
 
@@ -955,12 +1197,30 @@ bool make_x1_map(CUtensorMap* m, const void* x1, int n, int h, int w, int c1) {
              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
+// x2 [N][H/2][W/2][c2] BF16 (the half-resolution second input) as
+// [8][W/2][H/2][c2/8][N] with box [8][6][10][c2/8][1]: the pixels under one
+// tile's halo, zeros outside the frame.
+bool make_x2_map(CUtensorMap* m, const void* x2, int n, int h2, int w2, int c2) {
+  EncodeTiledFn enc = encode_tiled();
+  if (!enc || ((uintptr_t)x2 & 15) || c2 % 8 || c2 / 8 > 256 || h2 <= 0 || w2 <= 0) return false;
+  const cuuint64_t dims[5] = {8, (cuuint64_t)w2, (cuuint64_t)h2, (cuuint64_t)(c2 / 8), (cuuint64_t)n};
+  const cuuint64_t strides[4] = {(cuuint64_t)c2 * 2, (cuuint64_t)w2 * c2 * 2, 16, (cuuint64_t)h2 * w2 * c2 * 2};
+  const cuuint32_t box[5] = {8, (cuuint32_t)umma::kStgW, (cuuint32_t)umma::kStgH, (cuuint32_t)(c2 / 8), 1};
+  const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void*>(x2), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 constexpr size_t kPersistentSmemMax = 200 * 1024;
 
-// Warp-specialised form: weights + `stages` halo buffers (1024-aligned).
-size_t ws_smem(int cin, int nc, int stages) {
-  const size_t halo = ((size_t)cin * 360 + 1023) & ~(size_t)1023;
-  return (size_t)9 * cin * nc * 2 + 1024 + stages * halo + 1024;
+// Warp-specialised form: weights + `stages` halo buffers (1024-aligned),
+// each with room for `stg` planes of the second input's half-resolution box
+// (the stage layout of conv3x3_umma_ws_kernel).
+size_t ws_stage_bytes(int cin, int stg) {
+  return ((((size_t)cin * 360 + 127) & ~(size_t)127) + (size_t)stg * umma::kStgPlaneBytes + 1023) & ~(size_t)1023;
+}
+size_t ws_smem(int cin, int nc, int stages, int stg = 0) {
+  return (size_t)9 * cin * nc * 2 + 1024 + stages * ws_stage_bytes(cin, stg) + 1024;
 }
 constexpr size_t kWsSmemMax = 200 * 1024;
 // the FP8 form (at most 3 KB of static shared memory): up to the 227 KB a CTA may hold
@@ -969,14 +1229,26 @@ constexpr size_t kWsSmemMaxF8 = 220 * 1024;
 // The FP8 form holds e4m3 planes of 16 channels, the input padded to a
 // multiple of 32: the shared memory of the BF16 form at half the (padded)
 // channel count.
-size_t ws_smem_f8(int cin, int nc, int stages) {
-  const size_t halo = ((size_t)cin * 360 + 1023) & ~(size_t)1023;  // BF16 planes, quantised in place
-  return (size_t)9 * ((cin + 31) & ~31) * nc + 1024 + stages * halo + 1024;
+size_t ws_smem_f8(int cin, int nc, int stages, int stg = 0) {
+  // BF16 planes, quantised in place
+  return (size_t)9 * ((cin + 31) & ~31) * nc + 1024 + stages * ws_stage_bytes(cin, stg) + 1024;
 }
 
 template <int NC, bool kF8> int launch_umma_ws(const UmmaConvArgs& a, cudaStream_t s, bool use_tma_flag) {
   const int cin = a.c1 + a.c2;
-  auto smem_for = [&](int st) { return kF8 ? ws_smem_f8(cin, NC, st) : ws_smem(cin, NC, st); };
+  // the second input's half-resolution box by TMA (expanded in shared
+  // memory by the gather warps) where the x1 halo comes by TMA and two
+  // stages still fit; else its planes are gathered with cp.async
+  CUtensorMap map, map2;
+  memset(&map, 0, sizeof(map));
+  memset(&map2, 0, sizeof(map2));
+  const int use_tma = use_tma_flag && make_x1_map(&map, a.x1, a.N, a.H, a.W, a.c1) ? 1 : 0;
+  const size_t smem_max = kF8 ? kWsSmemMaxF8 : kWsSmemMax;
+  int stg = 0;
+  if (use_tma && a.c2 > 0 && (kF8 ? ws_smem_f8(cin, NC, 2, a.c2 / 8) : ws_smem(cin, NC, 2, a.c2 / 8)) <= smem_max &&
+      make_x2_map(&map2, a.x2, a.N, a.H >> 1, a.W >> 1, a.c2))
+    stg = a.c2 / 8;
+  auto smem_for = [&](int st) { return kF8 ? ws_smem_f8(cin, NC, st, stg) : ws_smem(cin, NC, st, stg); };
   // input stages in flight: PBRT_WS_STAGES (2..6) fixes the count; by
   // default the count of 2..4 with the most resident CTAs, the deeper ring
   // among equals, and a shallower one only while every CTA still walks 16
@@ -987,7 +1259,6 @@ template <int NC, bool kF8> int launch_umma_ws(const UmmaConvArgs& a, cudaStream
     const char* e = std::getenv("PBRT_WS_STAGES");
     return e ? std::min(6, std::max(2, std::atoi(e))) : 0;
   }();
-  const size_t smem_max = kF8 ? kWsSmemMaxF8 : kWsSmemMax;
   static PerDeviceOnce attrs;
   int ast = once_per_device(attrs, [&]() -> int {
     cudaError_t e = cudaFuncSetAttribute(conv3x3_umma_ws_kernel<NC, kF8>,
@@ -1000,9 +1271,6 @@ template <int NC, bool kF8> int launch_umma_ws(const UmmaConvArgs& a, cudaStream
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   constexpr int kCols = 2 * NC <= 64 ? 64 : (2 * NC <= 128 ? 128 : 256);
-  CUtensorMap map;
-  memset(&map, 0, sizeof(map));
-  const int use_tma = use_tma_flag && make_x1_map(&map, a.x1, a.N, a.H, a.W, a.c1) ? 1 : 0;
   // the gather warps only when some planes are not loaded by the TMA (FP8: always, they quantise)
   const bool gather = kF8 || !use_tma || a.c2 > 0;
   const int threads = gather ? kWsThreads : kWsThreads - 32 * kWsGatherWarps;
@@ -1038,7 +1306,7 @@ template <int NC, bool kF8> int launch_umma_ws(const UmmaConvArgs& a, cudaStream
   const size_t smem = smem_for(stages);
   const int per_sm = resident(smem);
   const int grid = (int)std::min(total_tiles, (long)sms * per_sm);
-  conv3x3_umma_ws_kernel<NC, kF8><<<grid, threads, smem, s>>>(a, tiles_per_image, map, use_tma, stages);
+  conv3x3_umma_ws_kernel<NC, kF8><<<grid, threads, smem, s>>>(a, tiles_per_image, map, map2, use_tma, stg, stages);
   return PBRT_OK;
 }
 
@@ -1162,6 +1430,86 @@ PBRT_API int pbrt_nn_conv3x3_umma_pooled(const void* x1, int32_t c1, const void*
   }
   if (st) return st;
   return check_launch("conv3x3_umma_ws_kernel (pooled)");
+}
+
+// Backward weights on tcgen05 (conv3x3_wgrad_umma_kernel): the arguments of
+// pbrt_nn_conv3x3_wgrad; dw is accumulated into.
+PBRT_API int pbrt_nn_conv3x3_wgrad_umma(const void* dy, const void* x1, int32_t c1, const void* x2, int32_t c2,
+                                        float* dw, int32_t n, int32_t h, int32_t wd, int32_t cout,
+                                        pbrt_stream_t stream) {
+  if (!dy || !x1 || !dw || c1 <= 0 || c1 % 16 || c2 < 0 || c2 % 16 || (c2 && !x2) || c1 + c2 > 256 || cout <= 0 ||
+      cout % 16 || cout > 128 || n <= 0 || h <= 0 || wd <= 0 || (c2 && (h % 2 || wd % 2)) || ((uintptr_t)dy & 15) ||
+      ((uintptr_t)x1 & 15) || ((uintptr_t)x2 & 15))
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "nn conv3x3 wgrad umma: bad arguments (c1 %d, c2 %d, cout %d)", c1, c2,
+                cout);
+  const int cin = c1 + c2;
+  const size_t smem = (size_t)kWgStages * wgrad_stage_bytes(cin) + 1024;
+  static PerDeviceOnce attrs;
+  int ast = once_per_device(attrs, [&]() -> int {
+    cudaError_t e = cudaFuncSetAttribute(conv3x3_wgrad_umma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(kWgStages * wgrad_stage_bytes(256) + 1024));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(conv3x3_wgrad_umma_kernel)");
+    return PBRT_OK;
+  });
+  if (ast) return ast;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int per_sm = std::max(1, (int)((227 * 1024) / (smem + 1024)));
+  const long P = (long)n * h * wd;
+  // two waves of CTAs over the nine taps; pixel runs of whole stages
+  long chunks = std::max(1L, std::min((2L * sms * per_sm + 8) / 9, (P + kWgK - 1) / kWgK));
+  long ppc = (P + chunks - 1) / chunks;
+  ppc = (ppc + kWgK - 1) / kWgK * kWgK;
+  UmmaWgradArgs a{(const bf16*)dy, (const bf16*)x1, (const bf16*)x2, c1, c2, dw, n, h, wd, cout, (int)ppc};
+  dim3 grid((unsigned)((P + ppc - 1) / ppc), 9);
+  conv3x3_wgrad_umma_kernel<<<grid, 128, smem, stream>>>(a);
+  return check_launch("conv3x3_wgrad_umma_kernel");
+}
+
+// tcgen05 convolution of a single input with an FP32 output (the backward-
+// data pass: dY convolved with the flipped weights), any Cout that is a
+// multiple of 16: the output channels are split into slices whose weights
+// and two input stages fit the warp-specialised kernel's shared memory, one
+// launch a slice, each writing its columns of y32 (pixel stride cout).
+// PBRT_ERROR_UNSUPPORTED when no slicing fits (c1 too large).
+PBRT_API int pbrt_nn_conv3x3_umma_f32(const void* x1, int32_t c1, const void* w, const float* bias, float* y32,
+                                      int32_t n, int32_t h, int32_t wd, int32_t cout, int32_t flags,
+                                      pbrt_stream_t stream) {
+  if (!x1 || !w || !y32 || c1 <= 0 || c1 % 16 || cout < 16 || cout % 16 || n <= 0 || h <= 0 || wd <= 0 ||
+      ((uintptr_t)y32 & 15) || ((uintptr_t)x1 & 15) || ((uintptr_t)w & 15))
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "nn conv3x3 umma f32: bad arguments (c1 %d, cout %d)", c1, cout);
+  int slice = 0;
+  for (int parts = (cout + 127) / 128; parts <= cout / 16; ++parts) {
+    const int nc = ((cout + parts - 1) / parts + 15) / 16 * 16;
+    if (nc <= 128 && ws_smem(c1, nc, 2) <= kWsSmemMax) {
+      slice = nc;
+      break;
+    }
+  }
+  if (!slice) return fail(PBRT_ERROR_UNSUPPORTED, "nn conv3x3 umma f32: c1 %d, cout %d", c1, cout);
+  for (int o = 0; o < cout; o += slice) {
+    const int nc = std::min(slice, cout - o);
+    UmmaConvArgs a{(const bf16*)x1, nullptr, c1, 0, (const bf16*)w + (size_t)o * 9 * c1, bias ? bias + o : nullptr,
+                   nullptr, n, h, wd, nc, flags & 1};
+    a.y32 = y32 + o;
+    a.ldy32 = cout;
+    int st;
+    switch (nc) {
+      case 16: st = launch_umma_ws<16, false>(a, stream, !(flags & 4)); break;
+      case 32: st = launch_umma_ws<32, false>(a, stream, !(flags & 4)); break;
+      case 48: st = launch_umma_ws<48, false>(a, stream, !(flags & 4)); break;
+      case 64: st = launch_umma_ws<64, false>(a, stream, !(flags & 4)); break;
+      case 80: st = launch_umma_ws<80, false>(a, stream, !(flags & 4)); break;
+      case 96: st = launch_umma_ws<96, false>(a, stream, !(flags & 4)); break;
+      case 112: st = launch_umma_ws<112, false>(a, stream, !(flags & 4)); break;
+      default: st = launch_umma_ws<128, false>(a, stream, !(flags & 4)); break;
+    }
+    if (st) return st;
+    const int e = check_launch("conv3x3_umma_ws_kernel (f32)");
+    if (e) return e;
+  }
+  return PBRT_OK;
 }
 
 // FP8 (e4m3) convolution on the tensor cores (kind::f8f6f4): the arguments

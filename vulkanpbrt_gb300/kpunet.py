@@ -227,14 +227,23 @@ class Workspace:
         return self.out[0]
 
     # ---- loss and backward --------------------------------------------------
-    def loss_and_grad(self, target, albedo, var_weight=0.1):
+    def loss_and_grad(self, target, albedo, var_weight=0.1, kernel="mma"):
         """relMSE (plus the variance head's loss) into self.loss; gradients into net.grad."""
         self.loss.zero_()
         nn.relmse_loss(self.out[0], target, albedo, self.gout[0], self.loss, var=self.var, dvar=self.gvar,
                        var_weight=var_weight)
-        self.backward()
+        self.backward(kernel)
 
-    def backward(self):
+    def _dgrad(self, gm, name, out32, kernel):
+        """Gradient of a convolution's input: gm convolved with the flipped weights, FP32 out."""
+        if kernel == "umma":
+            nn.conv3x3_umma_f32(gm, self.net.flipped(name), out32)
+        else:
+            nn.conv3x3(gm, self.net.flipped(name), None, out32=out32, store_bf16=False)
+
+    def backward(self, kernel="mma"):
+        """kernel: the backward-data and backward-weight convolutions on "mma" (mma.sync) or "umma"
+        (tcgen05)."""
         net, a, g = self.net, self.act, self.gact
         G = net.grad
         for t in list(g.values()) + list(self.gpool.values()) + [self.gout[1], self.gout[2]]:
@@ -256,13 +265,13 @@ class Workspace:
             nn.relu_bwd(g[name], a[name], gm, db=net._view(G, name + ".b"))
             if name.endswith("b"):
                 prev = name[:-1] + "a"
-                nn.conv3x3_wgrad(gm, a[prev], net._view(G, name + ".w"))
-                nn.conv3x3(gm, net.flipped(name), None, out32=g[prev], store_bf16=False)
+                nn.conv3x3_wgrad(gm, a[prev], net._view(G, name + ".w"), kernel=kernel)
+                self._dgrad(gm, name, g[prev], kernel)
             else:
                 sk, up = skip_of[lvl], up_of[lvl]
-                nn.conv3x3_wgrad(gm, a[sk], net._view(G, name + ".w"), x2=a[up])
+                nn.conv3x3_wgrad(gm, a[sk], net._view(G, name + ".w"), x2=a[up], kernel=kernel)
                 gc = self._scratch(self._gcat_flat, lvl, c1 + c2)
-                nn.conv3x3(gm, net.flipped(name), None, out32=gc, store_bf16=False)
+                self._dgrad(gm, name, gc, kernel)
                 nn.split_upsum(gc, c1, g[sk], g[up])
         # encoder
         for name, (c1, c2), cout, lvl in reversed(ENCODER):
@@ -270,21 +279,22 @@ class Workspace:
             nn.relu_bwd(g[name], a[name], gm, db=net._view(G, name + ".b"))
             if name.endswith("b"):
                 prev = name[:-1] + "a"
-                nn.conv3x3_wgrad(gm, a[prev], net._view(G, name + ".w"))
-                nn.conv3x3(gm, net.flipped(name), None, out32=g[prev], store_bf16=False)
+                nn.conv3x3_wgrad(gm, a[prev], net._view(G, name + ".w"), kernel=kernel)
+                self._dgrad(gm, name, g[prev], kernel)
             elif lvl > 0:
                 xin = self.pool[lvl]
-                nn.conv3x3_wgrad(gm, xin, net._view(G, name + ".w"))
-                nn.conv3x3(gm, net.flipped(name), None, out32=self.gpool[lvl], store_bf16=False)
+                nn.conv3x3_wgrad(gm, xin, net._view(G, name + ".w"), kernel=kernel)
+                self._dgrad(gm, name, self.gpool[lvl], kernel)
                 nn.avgpool2_bwd_add(self.gpool[lvl], g["e%db" % (lvl - 1)])
             else:
-                nn.conv3x3_wgrad(gm, self.feat, net._view(G, name + ".w"))
+                nn.conv3x3_wgrad(gm, self.feat, net._view(G, name + ".w"), kernel=kernel)
 
-    def train_step(self, target, albedo, lr=1e-4, var_weight=0.1):
+    def train_step(self, target, albedo, lr=1e-4, var_weight=0.1, kernel="mma"):
+        """One Adam step; kernel "umma" runs every convolution (forward, backward data and weights) on tcgen05."""
         net = self.net
-        self.forward()
+        self.forward(kernel)
         net.grad.zero_()
-        self.loss_and_grad(target, albedo, var_weight)
+        self.loss_and_grad(target, albedo, var_weight, kernel)
         net.step_count += 1
         nn.adam(net.w32, net.grad, net.m, net.v, net.step_count, lr=lr, w_bf16=net.w16)
         return self.loss

@@ -18,6 +18,7 @@ import argparse
 import json
 import math
 import time
+from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 
@@ -77,11 +78,23 @@ def render_views(views, window=1024, crop=256, full=(1920, 1080), inputs=16, tar
     cache = {}
     m = 0
     t0 = time.time()
+    # the next scene is built on the host while the GPU traces the current one
+    keys = list(dict.fromkeys((kind, sseed) for kind, sseed, _ in views))
+    pool = ThreadPoolExecutor(1)
+    pending = {}
+
+    def want(i):
+        if i < len(keys) and keys[i] not in pending:
+            pending[keys[i]] = pool.submit(_scene, keys[i][0], keys[i][1], texture_size, instances)
+
+    want(0)
     for vi, (kind, sseed, cseed) in enumerate(views):
         key = (kind, sseed)
         if key not in cache:
             cache.clear()
-            sc = _scene(kind, sseed, texture_size, instances)
+            want(keys.index(key))
+            sc = pending.pop(key).result()
+            want(keys.index(key) + 1)
             sh = SceneHandle(sc)
             pipe = PBRTPipeline(sh, g, illu, True, max_recursion_depth=max_depth, min_recursion_depth=min_depth)
             cache[key] = (sc, sh, pipe)
@@ -121,6 +134,7 @@ def render_views(views, window=1024, crop=256, full=(1920, 1080), inputs=16, tar
         if log and (vi % 5 == 0 or vi == len(views) - 1):
             torch.cuda.synchronize()
             log(f"view {vi + 1}/{len(views)} ({kind} seed {sseed}) {time.time() - t0:.1f} s")
+    pool.shutdown()
     return out
 
 
@@ -152,12 +166,14 @@ SPP_CHOICES = (1, 1, 2, 4, 8, 16)  # samples averaged into one network input (1 
 
 
 def train(net, data, steps, batch=16, lr=1e-4, seed=0, log_every=100, var_weight=0.1, log=print,
-          lr_floor=0.1):
+          lr_floor=0.1, kernel="mma"):
     """Adam steps over random crops; each input is the mean of k of the
     crop's one-sample frames (k from SPP_CHOICES, with the matching samples-
     per-pixel channel, as the Accumulator's output carries it) -- so one
     network serves raw 1-spp and accumulated input. Cosine learning-rate
-    decay to lr * lr_floor. Returns the loss history."""
+    decay to lr * lr_floor. kernel: the convolutions (forward, backward data
+    and weights) on "mma" (mma.sync) or "umma" (tcgen05). Returns the loss
+    history."""
     import torch
 
     from . import nn
@@ -185,7 +201,8 @@ def train(net, data, steps, batch=16, lr=1e-4, seed=0, log_every=100, var_weight
         nn.features(illum, b["albedo"].contiguous(), b["normal"].contiguous(), b["depth"].contiguous(), ws.feat,
                     ws.rad[0], spp=b["spp"].contiguous())
         cur = lr * (lr_floor + (1 - lr_floor) * 0.5 * (1 + math.cos(math.pi * it / max(steps, 1))))
-        loss = ws.train_step(b["target"].contiguous(), b["albedo"].contiguous(), lr=cur, var_weight=var_weight)
+        loss = ws.train_step(b["target"].contiguous(), b["albedo"].contiguous(), lr=cur, var_weight=var_weight,
+                             kernel=kernel)
         if it % log_every == 0 or it == steps - 1:
             lv = loss.tolist()
             hist.append((it, lv[0], lv[1]))
@@ -200,6 +217,7 @@ def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--views", type=int, default=24)
     ap.add_argument("--views-per-scene", type=int, default=2, help="views (windows) rendered from each seeded scene")
+    ap.add_argument("--scene-seed", type=int, default=1000, help="first scene seed (the benchmark scene is seed 0)")
     ap.add_argument("--window", type=int, default=1024)
     ap.add_argument("--crop", type=int, default=256)
     ap.add_argument("--inputs", type=int, default=16)
@@ -212,6 +230,8 @@ def main(argv=None):
     ap.add_argument("--texture-size", type=int, default=256)
     ap.add_argument("--instances", type=int, default=2000)
     ap.add_argument("--init", default=None, help="start from these weights")
+    ap.add_argument("--kernel", default="mma", choices=["mma", "umma"],
+                    help="convolutions (forward and backward) on mma.sync or tcgen05")
     ap.add_argument("--out", required=True)
     ap.add_argument("--log", default=None)
     a = ap.parse_args(argv)
@@ -223,20 +243,20 @@ def main(argv=None):
 
     dev = torch.device("cuda", 0)
     t0 = time.time()
-    views = default_views(a.views, views_per_scene=a.views_per_scene)
+    views = default_views(a.views, seed=a.scene_seed, views_per_scene=a.views_per_scene)
     data = render_views(views, a.window, a.crop, inputs=a.inputs, target_spp=a.target_spp, max_depth=a.max_depth,
                         min_depth=a.min_depth, texture_size=a.texture_size, instances=a.instances, device=dev)
     t_data = time.time() - t0
     net = KPUNet.load(a.init, dev) if a.init else KPUNet(dev, seed=0)
     t1 = time.time()
-    hist = train(net, data, a.steps, a.batch, a.lr)
+    hist = train(net, data, a.steps, a.batch, a.lr, kernel=a.kernel)
     torch.cuda.synchronize()
     t_train = time.time() - t1
     net.save(a.out)
     rec = {"views": len(views), "scene_count": len({(k, s) for k, s, _ in views}), "window": a.window,
            "crops": int(data["illum"].shape[0]), "inputs_per_crop": a.inputs,
            "target_spp": a.target_spp, "steps": a.steps, "batch": a.batch, "lr": a.lr, "data_s": t_data,
-           "train_s": t_train, "loss": hist, "scenes": sorted({(k, s) for k, s, _ in views})}
+           "train_s": t_train, "init": a.init, "kernel": a.kernel, "loss": hist, "scenes": sorted({(k, s) for k, s, _ in views})}
     if a.log:
         with open(a.log, "w") as f:
             json.dump(rec, f, indent=1)

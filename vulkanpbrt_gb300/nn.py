@@ -19,6 +19,8 @@ _abi.add_signatures({
     "pbrt_nn_channel_amax": (i32, [H, i64, i32, H, H]),
     "pbrt_nn_conv3x3_umma": (i32, [H, i32, H, i32, H, H, H, i32, i32, i32, i32, i32, H]),
     "pbrt_nn_conv3x3_umma_pooled": (i32, [H, i32, H, H, H, H, i32, i32, i32, i32, i32, H]),
+    "pbrt_nn_conv3x3_umma_f32": (i32, [H, i32, H, H, H, i32, i32, i32, i32, i32, H]),
+    "pbrt_nn_conv3x3_wgrad_umma": (i32, [H, H, i32, H, i32, H, i32, i32, i32, i32, H]),
     "pbrt_nn_conv3x3_fp8_umma": (i32, [H, i32, H, i32, H, H, H, H, H, H, i32, i32, i32, i32, i32, H]),
     "pbrt_nn_umma_status": (i32, [H, C.POINTER(C.c_uint32)]),
     "pbrt_nn_flip_weights": (i32, [H, H, i32, i32, H]),
@@ -147,6 +149,17 @@ def conv3x3_umma_pooled(x1, w, bias=None, relu=False):
     return out, pooled
 
 
+def conv3x3_umma_f32(x1, w, out32, bias=None, relu=False, tma=True):
+    """tcgen05 convolution of one input into the FP32 tensor out32 [N,H,W,Cout] (any Cout that is a
+    multiple of 16, in slices): the backward-data pass with flip_weights' weights."""
+    n, h, wd, c1 = x1.shape
+    cout = w.shape[0]
+    flags = (RELU if relu else 0) | (0 if tma else 4)
+    check(lib().pbrt_nn_conv3x3_umma_f32(_ptr(x1), c1, _ptr(w), _ptr(bias), _ptr(out32), n, h, wd, cout, flags,
+                                         _stream()))
+    return out32
+
+
 def umma_status() -> int:
     """Error flags of the tcgen05 kernels since the last call (0 = none); synchronises."""
     f = C.c_uint32()
@@ -154,12 +167,12 @@ def umma_status() -> int:
     return f.value
 
 
-def conv3x3_wgrad(dy, x1, dw, x2=None):
-    """dw [Cout, 9, Cin] f32 += dY^T . im2col(concat(x1, up2(x2)))."""
+def conv3x3_wgrad(dy, x1, dw, x2=None, kernel="mma"):
+    """dw [Cout, 9, Cin] f32 += dY^T . im2col(concat(x1, up2(x2))); kernel "mma" (mma.sync) or "umma" (tcgen05)."""
     n, h, wd, c1 = x1.shape
     c2 = 0 if x2 is None else x2.shape[3]
-    check(lib().pbrt_nn_conv3x3_wgrad(_ptr(dy), _ptr(x1), c1, _ptr(x2), c2, _ptr(dw), n, h, wd, dy.shape[3],
-                                      _stream()))
+    fn = lib().pbrt_nn_conv3x3_wgrad_umma if kernel == "umma" else lib().pbrt_nn_conv3x3_wgrad
+    check(fn(_ptr(dy), _ptr(x1), c1, _ptr(x2), c2, _ptr(dw), n, h, wd, dy.shape[3], _stream()))
     return dw
 
 
