@@ -878,7 +878,9 @@ def run_full(args):
         "config": {"workload": "full chosen form", "width": W, "height": H, "spp": spp, "max_depth": args.max_depth,
                    "min_depth": args.min_depth, "triangles": int(info.triangle_count), "lights": int(info.light_count),
                    "instances": int(info.instance_count), "network": "FP8 e4m3 (input layer BF16)",
-                   "gate_threshold": args.gate_threshold, "bmfr": "32x32, FP64 re-solve above R-ratio 1e6",
+                   "gate": ("learned per-tile blend of network and BMFR" if args.gate == "learned"
+                            else f"variance threshold {args.gate_threshold}"),
+                   "bmfr": "32x32, FP64 re-solve above R-ratio 1e6",
                    "requests": "16 x 1080p, 1 spp, accumulate + BMFR, own seeded scene each, one graph launch on a "
                                "second stream beside each 4K frame"},
         "fp64_blocks_per_frame_max": max(fp64_blocks), "largest_r_ratio": max(ratios),
@@ -921,7 +923,7 @@ def full_relmse(args, vp, pipe, g, illu, bmfr, neural, pc, pc_den, stream):
     return res
 
 
-UNET_KERNELS = ("bf16_tcgen05", "bf16_mma", "fp8_tcgen05", "fp8_mma")
+UNET_KERNELS = ("bf16_tcgen05", "bf16_mma", "fp8_tcgen05", "fp8_mma", "bf16_tcgen05_gather", "fp8_tcgen05_gather")
 
 
 def _event_time_us(fn, reps):
@@ -975,10 +977,14 @@ def unet_layer_times(width, height, reps, layers, kernels):
             "bf16_mma": lambda: nn.conv3x3(x1, wb, b, x2=x2, relu=True, out=out),
             "fp8_tcgen05": lambda: nn.conv3x3_fp8(x1, w8, ws, xs, b, x2=x2, relu=True, out=out, kernel="umma"),
             "fp8_mma": lambda: nn.conv3x3_fp8(x1, w8, ws, xs, b, x2=x2, relu=True, out=out, kernel="mma"),
+            # the upsampled second input gathered with cp.async instead of its TMA box
+            "bf16_tcgen05_gather": lambda: nn.conv3x3_umma(x1, wb, b, x2=x2, relu=True, out=out, box=False),
+            "fp8_tcgen05_gather": lambda: nn.conv3x3_fp8(x1, w8, ws, xs, b, x2=x2, relu=True, out=out, kernel="umma",
+                                                         box=False),
         }
         t = {}
         for k in UNET_KERNELS:
-            if k not in kernels:
+            if k not in kernels or (k.endswith("_gather") and not c2):
                 t[k] = None
                 continue
             try:

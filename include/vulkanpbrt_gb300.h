@@ -512,12 +512,16 @@ PBRT_API int pbrt_nn_conv3x3(const void* x1, int32_t c1, const void* x2, int32_t
  * in (pbrt_nn_quantize_weights_fp8); BF16 inputs are quantised on load with
  * inv_xscale [c1+c2] (saturating); c1 + c2 <= 256; flags bit 0: ReLU,
  * bit 3: the mma.sync kernel only (default: pbrt_nn_conv3x3_fp8_umma where
- * it applies, this kernel otherwise). */
+ * it applies, this kernel otherwise), bit 4: see pbrt_nn_conv3x3_umma. */
 PBRT_API int pbrt_nn_conv3x3_fp8(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* w8,
                                  const float* wscale, const float* inv_xscale, const float* bias, void* y, int32_t n,
                                  int32_t h, int32_t w_px, int32_t cout, int32_t flags, pbrt_stream_t stream);
 /* tcgen05 variant (5th-generation tensor cores, accumulator in tensor
- * memory): BF16 output only, cout in {16, 32, ..., 128}, flags bit 0 ReLU. */
+ * memory): BF16 output only, cout in {16, 32, ..., 128}, flags bit 0 ReLU,
+ * bit 1: the per-tile kernel only, bit 2: no TMA, bit 3: the single-role
+ * persistent kernel, bit 4: the upsampled second input gathered with
+ * cp.async (default: its half-resolution box by TMA, expanded in shared
+ * memory, where two stages of it fit). */
 PBRT_API int pbrt_nn_conv3x3_umma(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* w,
                                   const float* bias, void* y, int32_t n, int32_t h, int32_t w_px, int32_t cout,
                                   int32_t flags, pbrt_stream_t stream);

@@ -82,6 +82,10 @@ def test_conv3x3_fp8_umma(cuda, n, h, w, c1, c2, cout):
     y = nn.conv3x3_fp8(**args, kernel="umma")
     assert nn.umma_status() == 0
     _check(y, ref, "umma")
+    if c2:  # the upsampled input's TMA box and its cp.async gathers: the same bits
+        y_g = nn.conv3x3_fp8(**args, kernel="umma", box=False)
+        assert nn.umma_status() == 0
+        assert torch.equal(y, y_g)
     # the same operands on the mma.sync kernel: the two agree to the BF16 rounding of the output
     y_mma = nn.conv3x3_fp8(**args, kernel="mma")
     torch.cuda.synchronize()

@@ -92,15 +92,18 @@ def test_pool_relu_split_backward(cuda):
     assert _rel(dx1, x1r.grad) < 1e-6 and _rel(dx2, x2r.grad) < 1e-5
 
 
+@pytest.mark.parametrize("n,h,w", [(2, 12, 20), (1, 10, 14)])
 @pytest.mark.parametrize("scale,k,c", [(2, 25, 64), (1, 26, 48), (0, 27, 32)])
-def test_kp_head_forward_backward(cuda, scale, k, c):
+def test_kp_head_forward_backward(cuda, scale, k, c, n, h, w):
+    """The heads (forward: the 1x1 convolution on the tensor cores with the
+    weights split in three BF16 parts, 16 pixels a warp, a partial last group
+    at 10x14) against the FP32 restatement."""
     import torch
 
     from tests import kpunet_reference as ref
     from vulkanpbrt_gb300 import nn
 
-    g = torch.Generator().manual_seed(10 + k)
-    n, h, w = 2, 12, 20
+    g = torch.Generator().manual_seed(10 + k + h)
     Fm = torch.randn(n, h, w, c, generator=g).bfloat16()
     Wh = torch.randn(k, c, generator=g) * 0.3
     bh = torch.randn(k, generator=g) * 0.1

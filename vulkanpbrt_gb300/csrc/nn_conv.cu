@@ -983,8 +983,8 @@ PBRT_API int pbrt_nn_conv3x3_fp8(const void* x1, int32_t c1, const void* x2, int
     return fail(PBRT_ERROR_INVALID_ARGUMENT, "nn conv3x3 fp8: bad arguments (c1 %d, c2 %d, cout %d)", c1, c2, cout);
   // the tcgen05 form where it applies (flags bit 3: this kernel only)
   if (!(flags & 8) && cout <= 128 && nn_fp8_umma_fits(x1, c1, x2, c2, w8, cout, h, wd, false))
-    return pbrt_nn_conv3x3_fp8_umma(x1, c1, x2, c2, w8, wscale, inv_xscale, bias, y, nullptr, n, h, wd, cout, flags & 1,
-                                    stream);
+    return pbrt_nn_conv3x3_fp8_umma(x1, c1, x2, c2, w8, wscale, inv_xscale, bias, y, nullptr, n, h, wd, cout,
+                                    flags & 17, stream);
   Fp8ConvArgs a{(const bf16*)x1, (const bf16*)x2, c1, c2, (const uint8_t*)w8, wscale, inv_xscale, bias, (bf16*)y,
                 n, h, wd, cout, flags & 1};
   const int bn = cout <= 128 ? cout : (cout / 2 <= 128 && (cout / 2) % 16 == 0 ? cout / 2 : 128);

@@ -231,6 +231,148 @@ __global__ void kp_head_fwd_kernel(HeadArgs a) {
   }
 }
 
+// The network's three heads with the 1x1 convolution on the tensor cores:
+// each warp takes 16 pixels, the logits are a [16 x C] x [C x 32] product
+// (27 logits padded to 32) by mma.sync m16n8k16 with FP32 accumulation. The
+// FP32 head weights are split into three BF16 parts (w = hi + mid + lo to
+// ~24 bits) and the features are BF16 already, so the three products add up
+// to the FP32 logits. Lane (g, t) of the warp then holds, for pixels g and
+// g + 8 of the group, logits n = 8 nt + 2t + {0, 1}: the softmax, the 5x5
+// filter of the radiance and the blend reduce over the four lanes of a
+// pixel with shuffles.
+template <int C, int K>
+__global__ void __launch_bounds__(128) kp_head_fwd_mma_kernel(HeadArgs a) {
+  constexpr int KS = C / 16;  // k steps of 16 channels
+  // B fragments of the three weight parts: [part][ks][nt][lane] x 2 registers
+  __shared__ uint2 sB[3][KS][4][32];
+  __shared__ float sBias[32];
+  for (int i = threadIdx.x; i < 3 * KS * 4 * 32; i += blockDim.x) {
+    const int ln = i % 32, nt = (i / 32) % 4, ks = (i / 128) % KS, part = i / (128 * KS);
+    const int g = ln >> 2, t = ln & 3, n = nt * 8 + g;
+    uint32_t r[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {  // b0: k = 2t, 2t + 1; b1: k = 2t + 8, 2t + 9
+      const int k0 = ks * 16 + 2 * t + 8 * h;
+      float w[2];
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        float v = n < K ? a.Wh[n * C + k0 + j] : 0.f;
+        for (int q = 0; q < part; ++q) v -= __bfloat162float(__float2bfloat16_rn(v));
+        w[j] = v;
+      }
+      const __nv_bfloat162 b2 = __floats2bfloat162_rn(w[0], w[1]);
+      r[h] = *reinterpret_cast<const uint32_t*>(&b2);
+    }
+    sB[part][ks][nt][ln] = make_uint2(r[0], r[1]);
+  }
+  for (int i = threadIdx.x; i < 32; i += blockDim.x) sBias[i] = i < K ? a.bh[i] : 0.f;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const long P = (long)a.N * a.H * a.W;
+  const long groups = (P + 15) / 16;
+  const long warps = (long)gridDim.x * (blockDim.x / 32);
+  for (long grp = blockIdx.x * (long)(blockDim.x / 32) + (threadIdx.x >> 5); grp < groups; grp += warps) {
+    const long p0 = grp * 16;
+    const long pa = min(p0 + g, P - 1), pb = min(p0 + g + 8, P - 1);  // this lane's two pixels (clamped loads)
+    float acc[4][4];
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+      const float b0 = sBias[nt * 8 + 2 * t], b1 = sBias[nt * 8 + 2 * t + 1];
+      acc[nt][0] = b0;
+      acc[nt][1] = b1;
+      acc[nt][2] = b0;
+      acc[nt][3] = b1;
+    }
+    const uint32_t* fa = reinterpret_cast<const uint32_t*>(a.F + pa * C);
+    const uint32_t* fb = reinterpret_cast<const uint32_t*>(a.F + pb * C);
+#pragma unroll
+    for (int ks = 0; ks < KS; ++ks) {
+      const uint32_t a0 = fa[ks * 8 + t], a1 = fb[ks * 8 + t], a2 = fa[ks * 8 + 4 + t], a3 = fb[ks * 8 + 4 + t];
+#pragma unroll
+      for (int part = 2; part >= 0; --part)  // smallest parts first
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt) {
+          const uint2 b = sB[part][ks][nt][lane];
+          asm volatile(
+              "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+              "{%0,%1,%2,%3};\n"
+              : "+f"(acc[nt][0]), "+f"(acc[nt][1]), "+f"(acc[nt][2]), "+f"(acc[nt][3])
+              : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b.x), "r"(b.y));
+        }
+    }
+    // per pixel (h = 0: pixel g, h = 1: pixel g + 8): softmax over the 25 taps
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const long p = p0 + g + 8 * h;
+      const long pc = h ? pb : pa;
+      const int x = (int)(pc % a.W), y = (int)((pc / a.W) % a.H), n = (int)(pc / ((long)a.W * a.H));
+      float lg[8];
+#pragma unroll
+      for (int nt = 0; nt < 4; ++nt) {
+        lg[2 * nt] = acc[nt][2 * h];
+        lg[2 * nt + 1] = acc[nt][2 * h + 1];
+      }
+      float mx = -INFINITY;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int k = (j >> 1) * 8 + 2 * t + (j & 1);
+        if (k < kKP) mx = fmaxf(mx, lg[j]);
+      }
+      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
+      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 2));
+      float e[8], sum = 0.f;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int k = (j >> 1) * 8 + 2 * t + (j & 1);
+        e[j] = k < kKP ? __expf(lg[j] - mx) : 0.f;
+        sum += e[j];
+      }
+      sum += __shfl_xor_sync(0xffffffffu, sum, 1);
+      sum += __shfl_xor_sync(0xffffffffu, sum, 2);
+      const float inv = 1.f / sum;
+      float3 f = f3(0.f);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int k = (j >> 1) * 8 + 2 * t + (j & 1);
+        if (k < kKP) {
+          const float w = e[j] * inv;
+          if (a.kw && p < P) a.kw[p * kKP + k] = w;
+          const int sx = min(max(x + k % 5 - 2, 0), a.W - 1), sy = min(max(y + k / 5 - 2, 0), a.H - 1);
+          const float* r = a.R + (((size_t)n * a.H + sy) * a.W + sx) * 3;
+          f = f + w * f3(r[0], r[1], r[2]);
+        }
+      }
+#pragma unroll
+      for (int m = 1; m <= 2; m <<= 1) {
+        f.x += __shfl_xor_sync(0xffffffffu, f.x, m);
+        f.y += __shfl_xor_sync(0xffffffffu, f.y, m);
+        f.z += __shfl_xor_sync(0xffffffffu, f.z, m);
+      }
+      // logits 25, 26 (nt 3, j 1 and 2): lanes t = 0 (c1) and t = 1 (c0)
+      const float l25 = __shfl_sync(0xffffffffu, lg[7], lane & ~3);
+      const float l26 = __shfl_sync(0xffffffffu, lg[6], (lane & ~3) | 1);
+      if (t == 0 && p < P) {
+        if (a.filt) {
+          a.filt[p * 3 + 0] = f.x;
+          a.filt[p * 3 + 1] = f.y;
+          a.filt[p * 3 + 2] = f.z;
+        }
+        float3 o = f;
+        if (a.coarse) {
+          const float al = 1.f / (1.f + __expf(-l25));
+          if (a.alpha) a.alpha[p] = al;
+          const float* cc = a.coarse + (((size_t)n * (a.H / 2) + y / 2) * (a.W / 2) + x / 2) * 3;
+          o = (1.f - al) * f + al * f3(cc[0], cc[1], cc[2]);
+        }
+        if (a.var) a.var[p] = a.coarse ? l26 : l25;
+        a.out[p * 3 + 0] = o.x;
+        a.out[p * 3 + 1] = o.y;
+        a.out[p * 3 + 2] = o.z;
+      }
+    }
+  }
+}
+
 struct HeadBwdArgs {
   HeadArgs f;
   const float* dout;   // [N][H][W][3]
@@ -611,9 +753,11 @@ PBRT_API int pbrt_nn_kp_head(const void* F, const float* Wh, const float* bh, co
   HeadArgs a{(const bf16*)F, Wh, bh, R, coarse, out, kw, filt, alpha, var, n, h, w, c, k};
   const int g = grid_for((long)n * h * w, 128);
   const size_t sm = (size_t)k * c * sizeof(float);
-  if (c == 64 && k == 25) kp_head_fwd_kernel<64, 25><<<g, 128, sm, s>>>(a);
-  else if (c == 48 && k == 26) kp_head_fwd_kernel<48, 26><<<g, 128, sm, s>>>(a);
-  else if (c == 32 && k == 27) kp_head_fwd_kernel<32, 27><<<g, 128, sm, s>>>(a);
+  // the network's heads: the 1x1 convolution on the tensor cores, 16 pixels a warp
+  const int gm = grid_for(((long)n * h * w + 15) / 16 * 32, 128);
+  if (c == 64 && k == 25) kp_head_fwd_mma_kernel<64, 25><<<gm, 128, 0, s>>>(a);
+  else if (c == 48 && k == 26) kp_head_fwd_mma_kernel<48, 26><<<gm, 128, 0, s>>>(a);
+  else if (c == 32 && k == 27) kp_head_fwd_mma_kernel<32, 27><<<gm, 128, 0, s>>>(a);
   else if (c % 8 == 0) kp_head_fwd_kernel<0, 0><<<g, 128, sm, s>>>(a);
   else return fail(PBRT_ERROR_INVALID_ARGUMENT, "kp head: channels must be a multiple of 8");
   return check_launch("kp_head_fwd");

@@ -1234,7 +1234,8 @@ size_t ws_smem_f8(int cin, int nc, int stages, int stg = 0) {
   return (size_t)9 * ((cin + 31) & ~31) * nc + 1024 + stages * ws_stage_bytes(cin, stg) + 1024;
 }
 
-template <int NC, bool kF8> int launch_umma_ws(const UmmaConvArgs& a, cudaStream_t s, bool use_tma_flag) {
+template <int NC, bool kF8> int launch_umma_ws(const UmmaConvArgs& a, cudaStream_t s, bool use_tma_flag,
+                                               bool box_flag = true) {
   const int cin = a.c1 + a.c2;
   // the second input's half-resolution box by TMA (expanded in shared
   // memory by the gather warps) where the x1 halo comes by TMA and two
@@ -1245,7 +1246,7 @@ template <int NC, bool kF8> int launch_umma_ws(const UmmaConvArgs& a, cudaStream
   const int use_tma = use_tma_flag && make_x1_map(&map, a.x1, a.N, a.H, a.W, a.c1) ? 1 : 0;
   const size_t smem_max = kF8 ? kWsSmemMaxF8 : kWsSmemMax;
   int stg = 0;
-  if (use_tma && a.c2 > 0 && (kF8 ? ws_smem_f8(cin, NC, 2, a.c2 / 8) : ws_smem(cin, NC, 2, a.c2 / 8)) <= smem_max &&
+  if (use_tma && box_flag && a.c2 > 0 && (kF8 ? ws_smem_f8(cin, NC, 2, a.c2 / 8) : ws_smem(cin, NC, 2, a.c2 / 8)) <= smem_max &&
       make_x2_map(&map2, a.x2, a.N, a.H >> 1, a.W >> 1, a.c2))
     stg = a.c2 / 8;
   auto smem_for = [&](int st) { return kF8 ? ws_smem_f8(cin, NC, st, stg) : ws_smem(cin, NC, st, stg); };
@@ -1350,7 +1351,8 @@ extern "C" {
 // tcgen05 forward convolution (BF16 output only): Cout in {16, 32, 48, 64,
 // 80, 96, 112, 128}, channel counts multiples of 16; flags bit 0: ReLU,
 // bit 1: the per-tile kernel only, bit 2: no TMA (cp.async gathers), bit 3:
-// the single-role persistent kernel instead of the warp-specialised one.
+// the single-role persistent kernel instead of the warp-specialised one,
+// bit 4: the upsampled second input by cp.async gathers, not the TMA box.
 PBRT_API int pbrt_nn_conv3x3_umma(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* w,
                                   const float* bias, void* y, int32_t n, int32_t h, int32_t wd, int32_t cout,
                                   int32_t flags, pbrt_stream_t stream) {
@@ -1362,14 +1364,14 @@ PBRT_API int pbrt_nn_conv3x3_umma(const void* x1, int32_t c1, const void* x2, in
   // warp-specialised form (the upsampled second input comes from its gather warps)
   if (!(flags & 10) && ws_smem(c1 + c2, cout, 2) <= kWsSmemMax) {
     switch (cout) {
-      case 16: st = launch_umma_ws<16, false>(a, stream, !(flags & 4)); break;
-      case 32: st = launch_umma_ws<32, false>(a, stream, !(flags & 4)); break;
-      case 48: st = launch_umma_ws<48, false>(a, stream, !(flags & 4)); break;
-      case 64: st = launch_umma_ws<64, false>(a, stream, !(flags & 4)); break;
-      case 80: st = launch_umma_ws<80, false>(a, stream, !(flags & 4)); break;
-      case 96: st = launch_umma_ws<96, false>(a, stream, !(flags & 4)); break;
-      case 112: st = launch_umma_ws<112, false>(a, stream, !(flags & 4)); break;
-      default: st = launch_umma_ws<128, false>(a, stream, !(flags & 4)); break;
+      case 16: st = launch_umma_ws<16, false>(a, stream, !(flags & 4), !(flags & 16)); break;
+      case 32: st = launch_umma_ws<32, false>(a, stream, !(flags & 4), !(flags & 16)); break;
+      case 48: st = launch_umma_ws<48, false>(a, stream, !(flags & 4), !(flags & 16)); break;
+      case 64: st = launch_umma_ws<64, false>(a, stream, !(flags & 4), !(flags & 16)); break;
+      case 80: st = launch_umma_ws<80, false>(a, stream, !(flags & 4), !(flags & 16)); break;
+      case 96: st = launch_umma_ws<96, false>(a, stream, !(flags & 4), !(flags & 16)); break;
+      case 112: st = launch_umma_ws<112, false>(a, stream, !(flags & 4), !(flags & 16)); break;
+      default: st = launch_umma_ws<128, false>(a, stream, !(flags & 4), !(flags & 16)); break;
     }
     if (st) return st;
     return check_launch("conv3x3_umma_ws_kernel");
@@ -1514,7 +1516,8 @@ PBRT_API int pbrt_nn_conv3x3_umma_f32(const void* x1, int32_t c1, const void* w,
 
 // FP8 (e4m3) convolution on the tensor cores (kind::f8f6f4): the arguments
 // and quantisation of pbrt_nn_conv3x3_fp8, plus the optional fused 2x2
-// pooling of pbrt_nn_conv3x3_umma_pooled (single input only).
+// pooling of pbrt_nn_conv3x3_umma_pooled (single input only); flags bit 0:
+// ReLU, bit 4: the upsampled second input by cp.async gathers.
 // PBRT_ERROR_UNSUPPORTED when the weights and two input stages do not fit
 // in shared memory, an operand is not 16-byte aligned, or (pooled) the
 // frame does not divide into 16 x 8 tiles.
@@ -1536,14 +1539,14 @@ PBRT_API int pbrt_nn_conv3x3_fp8_umma(const void* x1, int32_t c1, const void* x2
   a.inv_xscale = inv_xscale;
   int st;
   switch (cout) {
-    case 16: st = launch_umma_ws<16, true>(a, stream, true); break;
-    case 32: st = launch_umma_ws<32, true>(a, stream, true); break;
-    case 48: st = launch_umma_ws<48, true>(a, stream, true); break;
-    case 64: st = launch_umma_ws<64, true>(a, stream, true); break;
-    case 80: st = launch_umma_ws<80, true>(a, stream, true); break;
-    case 96: st = launch_umma_ws<96, true>(a, stream, true); break;
-    case 112: st = launch_umma_ws<112, true>(a, stream, true); break;
-    default: st = launch_umma_ws<128, true>(a, stream, true); break;
+    case 16: st = launch_umma_ws<16, true>(a, stream, true, !(flags & 16)); break;
+    case 32: st = launch_umma_ws<32, true>(a, stream, true, !(flags & 16)); break;
+    case 48: st = launch_umma_ws<48, true>(a, stream, true, !(flags & 16)); break;
+    case 64: st = launch_umma_ws<64, true>(a, stream, true, !(flags & 16)); break;
+    case 80: st = launch_umma_ws<80, true>(a, stream, true, !(flags & 16)); break;
+    case 96: st = launch_umma_ws<96, true>(a, stream, true, !(flags & 16)); break;
+    case 112: st = launch_umma_ws<112, true>(a, stream, true, !(flags & 16)); break;
+    default: st = launch_umma_ws<128, true>(a, stream, true, !(flags & 16)); break;
   }
   if (st) return st;
   return check_launch("conv3x3_umma_ws_kernel (fp8)");

@@ -166,14 +166,15 @@ SPP_CHOICES = (1, 1, 2, 4, 8, 16)  # samples averaged into one network input (1 
 
 
 def train(net, data, steps, batch=16, lr=1e-4, seed=0, log_every=100, var_weight=0.1, log=print,
-          lr_floor=0.1, kernel="mma"):
+          lr_floor=0.1, kernel="mma", checkpoint=None, checkpoint_every=0):
     """Adam steps over random crops; each input is the mean of k of the
     crop's one-sample frames (k from SPP_CHOICES, with the matching samples-
     per-pixel channel, as the Accumulator's output carries it) -- so one
     network serves raw 1-spp and accumulated input. Cosine learning-rate
     decay to lr * lr_floor. kernel: the convolutions (forward, backward data
-    and weights) on "mma" (mma.sync) or "umma" (tcgen05). Returns the loss
-    history."""
+    and weights) on "mma" (mma.sync) or "umma" (tcgen05). With `checkpoint`
+    (a path), the weights are saved there every `checkpoint_every` steps.
+    Returns the loss history."""
     import torch
 
     from . import nn
@@ -208,6 +209,8 @@ def train(net, data, steps, batch=16, lr=1e-4, seed=0, log_every=100, var_weight
             hist.append((it, lv[0], lv[1]))
             if log:
                 log(f"step {it} relMSE {lv[0]:.5f} var {lv[1]:.4f} lr {cur:.2e} {time.time() - t0:.1f} s")
+        if checkpoint and checkpoint_every and (it + 1) % checkpoint_every == 0 and it + 1 < steps:
+            net.save(checkpoint)
     return hist
 
 
@@ -233,6 +236,7 @@ def main(argv=None):
     ap.add_argument("--kernel", default="mma", choices=["mma", "umma"],
                     help="convolutions (forward and backward) on mma.sync or tcgen05")
     ap.add_argument("--out", required=True)
+    ap.add_argument("--checkpoint-every", type=int, default=0, help="also save the weights to --out every N steps")
     ap.add_argument("--log", default=None)
     a = ap.parse_args(argv)
 
@@ -249,7 +253,8 @@ def main(argv=None):
     t_data = time.time() - t0
     net = KPUNet.load(a.init, dev) if a.init else KPUNet(dev, seed=0)
     t1 = time.time()
-    hist = train(net, data, a.steps, a.batch, a.lr, kernel=a.kernel)
+    hist = train(net, data, a.steps, a.batch, a.lr, kernel=a.kernel, checkpoint=a.out,
+                 checkpoint_every=a.checkpoint_every)
     torch.cuda.synchronize()
     t_train = time.time() - t1
     net.save(a.out)

@@ -73,12 +73,13 @@ def conv3x3(x1, w, bias=None, x2=None, relu=False, out=None, out32=None, accumul
 
 
 def conv3x3_fp8(x1, w8, wscale, inv_xscale, bias=None, x2=None, relu=False, out=None, kernel="auto",
-                pooled=False):
+                pooled=False, box=True):
     """FP8 (e4m3) forward: w8 [Cout, 9, Cin] uint8 e4m3 with per-output-channel scales wscale [Cout] (activation
     scales folded in), inv_xscale [Cin] quantises the BF16 input on load. Returns BF16 [N,H,W,Cout].
     kernel: "auto" (tcgen05 where it applies), "mma" (the mma.sync kernel) or "umma" (tcgen05 only: raises
     PbrtError where it does not apply). pooled=True (tcgen05, single input) also returns the 2x2 average
-    pooling of the output, from the epilogue."""
+    pooling of the output, from the epilogue. box=False: the tcgen05 form gathers the upsampled second input with
+    cp.async instead of loading its half-resolution box by TMA."""
     import torch
 
     n, h, wd, c1 = x1.shape
@@ -86,7 +87,7 @@ def conv3x3_fp8(x1, w8, wscale, inv_xscale, bias=None, x2=None, relu=False, out=
     cout = w8.shape[0]
     if out is None:
         out = torch.empty((n, h, wd, cout), dtype=torch.bfloat16, device=x1.device)
-    flags = RELU if relu else 0
+    flags = (RELU if relu else 0) | (0 if box else 16)
     if kernel == "umma" or pooled:
         pool = torch.empty((n, h // 2, wd // 2, cout), dtype=torch.bfloat16, device=x1.device) if pooled else None
         check(lib().pbrt_nn_conv3x3_fp8_umma(_ptr(x1), c1, _ptr(x2), c2, _ptr(w8), _ptr(wscale), _ptr(inv_xscale),
@@ -117,11 +118,13 @@ def channel_amax(x, amax):
     return amax
 
 
-def conv3x3_umma(x1, w, bias=None, x2=None, relu=False, out=None, persistent=True, tma=True, specialised=True):
+def conv3x3_umma(x1, w, bias=None, x2=None, relu=False, out=None, persistent=True, tma=True, specialised=True,
+                 box=True):
     """tcgen05 forward (BF16 out): as conv3x3, Cout in {16, ..., 128}. persistent=False forces the
     per-tile kernel (the persistent one is used when the weights and two input halos fit in shared memory);
     tma=False gathers the persistent kernel's input halo with cp.async instead of a TMA load; specialised=False
-    uses the single-role persistent kernel instead of the warp-specialised one."""
+    uses the single-role persistent kernel instead of the warp-specialised one; box=False gathers the upsampled
+    second input with cp.async instead of loading its half-resolution box by TMA."""
     import torch
 
     n, h, wd, c1 = x1.shape
@@ -129,7 +132,8 @@ def conv3x3_umma(x1, w, bias=None, x2=None, relu=False, out=None, persistent=Tru
     cout = w.shape[0]
     if out is None:
         out = torch.empty((n, h, wd, cout), dtype=torch.bfloat16, device=x1.device)
-    flags = (RELU if relu else 0) | (0 if persistent else 2) | (0 if tma else 4) | (0 if specialised else 8)
+    flags = (RELU if relu else 0) | (0 if persistent else 2) | (0 if tma else 4) | (0 if specialised else 8) | \
+        (0 if box else 16)
     check(lib().pbrt_nn_conv3x3_umma(_ptr(x1), c1, _ptr(x2), c2, _ptr(w), _ptr(bias), _ptr(out), n, h, wd, cout,
                                      flags, _stream()))
     return out
