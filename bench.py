@@ -504,7 +504,7 @@ def run_gb300(args):
     total_ms = max_over_ranks(total_ms, world, dev)
 
     # ---- the same frames with FP8 (e4m3) convolutions, calibrated on the current frame
-    fp8_ms = None
+    fp8_ms, fp8_layers = None, None
     if neural is not None:
         neural.calibrate(stream)
         neural.set_precision(8)
@@ -517,12 +517,8 @@ def run_gb300(args):
         ev[1].record(stream)
         torch.cuda.synchronize()
         fp8_ms = ev[0].elapsed_time(ev[1]) / args.steps
-        e0f, e1f = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0f.record(stream)
-        neural.dispatch(pc, stream)
-        e1f.record(stream)
-        torch.cuda.synchronize()
-        fp8_neural_ms = e0f.elapsed_time(e1f)
+        fp8_neural_ms = _stage_ms(lambda: neural.dispatch(pc, stream), stream)
+        fp8_layers = neural.fp8_layers()
         neural.set_precision(16)
 
     # ---- the BMFR-only path (no network) over the same frames, for the neural-vs-BMFR comparison
@@ -572,12 +568,8 @@ def run_gb300(args):
     e1.record(stream)
     torch.cuda.synchronize()
     stages["bfr" if args.denoiser == "bfr" else "bmfr"] = e0.elapsed_time(e1)
-    if neural is not None:
-        e0.record(stream)
-        neural.dispatch(pc, stream)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        stages["neural"] = e0.elapsed_time(e1)
+    if neural is not None:  # the network's graph launch, mean of 10 after the frames above
+        stages["neural"] = _stage_ms(lambda: neural.dispatch(pc, stream), stream)
         stages["neural_fp8"] = fp8_neural_ms
     quality = None
     if args.ref_spp > 0 and rank == 0:
@@ -662,7 +654,9 @@ def run_gb300(args):
             "clocks": clocks,
             "gpu_launches": steps * (3 + 5 * (args.max_depth + 1) + 1 + 2 + (NEURAL_LAUNCHES if neural else 0)),
             "bmfr_path": None if bmfr_ms is None else {"fps": world * 1e3 / bmfr_ms, "ms_per_step": bmfr_ms},
-            "neural_fp8_path": None if fp8_ms is None else {"fps": world * 1e3 / fp8_ms, "ms_per_step": fp8_ms},
+            "neural_fp8_path": None if fp8_ms is None else {"fps": world * 1e3 / fp8_ms, "ms_per_step": fp8_ms,
+                                                            "e4m3_layers": [n for (n, *_), f in
+                                                                            zip(_conv_table(), fp8_layers) if f]},
             "relmse": quality,
             "bvh": {"nodes": int(info.bvh_nodes), "depth": int(info.bvh_depth), "build_ms": info.build_ms},
         }
@@ -877,7 +871,9 @@ def run_full(args):
         "grays_per_s_4k": rays / (total_ms / 1e3) / 1e9,
         "config": {"workload": "full chosen form", "width": W, "height": H, "spp": spp, "max_depth": args.max_depth,
                    "min_depth": args.min_depth, "triangles": int(info.triangle_count), "lights": int(info.light_count),
-                   "instances": int(info.instance_count), "network": "FP8 e4m3 (input layer BF16)",
+                   "instances": int(info.instance_count),
+                   "network": "FP8 mode: e4m3 on the layers the calibration timed faster, BF16 on the others",
+                   "e4m3_layers": [n for (n, *_), f in zip(_conv_table(), neural.fp8_layers()) if f],
                    "gate": ("learned per-tile blend of network and BMFR" if args.gate == "learned"
                             else f"variance threshold {args.gate_threshold}"),
                    "bmfr": "32x32, FP64 re-solve above R-ratio 1e6",
@@ -924,6 +920,26 @@ def full_relmse(args, vp, pipe, g, illu, bmfr, neural, pc, pc_den, stream):
 
 
 UNET_KERNELS = ("bf16_tcgen05", "bf16_mma", "fp8_tcgen05", "fp8_mma", "bf16_tcgen05_gather", "fp8_tcgen05_gather")
+
+
+def _stage_ms(fn, stream, reps=10):
+    """Mean device time of fn() on `stream` over `reps` back-to-back calls (CUDA events)."""
+    import torch
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def _conv_table():
+    from vulkanpbrt_gb300.kpunet import CONVS
+
+    return CONVS
 
 
 def _event_time_us(fn, reps):
@@ -997,6 +1013,32 @@ def unet_layer_times(width, height, reps, layers, kernels):
     return rows
 
 
+def unet_head_times(width, height, reps):
+    """Device time of each kernel-prediction head at its scale (inference
+    outputs: the filtered, blended radiance and, at full scale, the error
+    prediction) on random inputs. Returns [(name, channels, logits, scale, us)]."""
+    import torch
+
+    from vulkanpbrt_gb300 import nn
+    from vulkanpbrt_gb300.kpunet import HEADS
+
+    dev = torch.device("cuda:0")
+    g = torch.Generator(device=dev).manual_seed(1)
+    rows = []
+    for name, _, c, k, s_ in HEADS:
+        h, w = height >> s_, width >> s_
+        F = torch.rand(1, h, w, c, device=dev, generator=g).bfloat16()
+        Wh = torch.randn(k, c, device=dev, generator=g) * 0.1
+        bh = torch.zeros(k, device=dev)
+        R = torch.rand(1, h, w, 3, device=dev, generator=g)
+        coarse = torch.rand(1, h // 2, w // 2, 3, device=dev, generator=g) if k > 25 else None
+        out = torch.empty(1, h, w, 3, device=dev)
+        var = torch.empty(1, h, w, device=dev) if k == 27 else None
+        us = _event_time_us(lambda: nn.kp_head(F, Wh, bh, R, out, coarse=coarse, var=var), reps)
+        rows.append((name, c, k, s_, us))
+    return rows
+
+
 def run_unet_layers(args):
     """Markdown table of per-convolution times (microseconds per launch) at
     --width x --height rounded up to the network's padded frame (multiples of
@@ -1020,6 +1062,10 @@ def run_unet_layers(args):
             tot[k] += 0.0 if v is None else v
         print(f"| {name} | {c1}+{c2} -> {cout} | {W >> lvl}x{H >> lvl} | " + " | ".join(cells) + " |")
     print("| sum | | | " + " | ".join(f"{tot[k]:.1f}" for k in keys) + " |")
+    heads = unet_head_times(W, H, args.reps)
+    print("\n| head | channels -> logits | size | us |\n|---|---|---|---|")
+    for name, c, k, s_, us in heads:
+        print(f"| {name} | {c} -> {k} | {W >> s_}x{H >> s_} | {us:.1f} |")
     if "fp8_tcgen05" in keys and "fp8_mma" in keys:  # the FP8 path as dispatched: tcgen05 where it fits
         fp8_net = sum((t["fp8_tcgen05"] if t["fp8_tcgen05"] is not None else t["fp8_mma"]) or 0.0 for *_, t in rows)
         print(f"\nFP8 as dispatched (tcgen05 where it fits): {fp8_net:.1f} us")

@@ -681,14 +681,20 @@ PBRT_API int pbrt_neural_set_fallback(PbrtNeural* nd, PbrtBMFR* bmfr, float thre
 PBRT_API int pbrt_neural_set_gate_model(PbrtNeural* nd, const float* coef, int32_t n);
 /* FP8 inference: calibrate runs one BF16 pass on the current inputs
  * (stream-synchronising) and derives per-input-channel activation scales
- * (max |x| / 448) and per-output-channel e4m3 weights; set_precision(8)
- * then runs every convolution but the first (16 input channels, which stays
- * BF16) as e4m3 x e4m3 -> FP32 on the tensor cores (tcgen05 kind::f8f6f4
- * where the layer fits in shared memory, mma.sync otherwise), with the
- * encoder's pooling fused as in BF16; set_precision(16) returns to BF16.
- * New parameters drop the calibration. */
+ * (max |x| / 448) and per-output-channel e4m3 weights, then times every
+ * convolution but the first (16 input channels, which stays BF16) in BF16
+ * and in e4m3 on those activations and marks the layers where e4m3 is
+ * faster; set_precision(8) then runs the marked layers as e4m3 x e4m3 ->
+ * FP32 on the tensor cores (tcgen05 kind::f8f6f4 where the layer fits in
+ * shared memory, mma.sync otherwise), with the encoder's pooling fused as
+ * in BF16, and the others in BF16; set_precision(16) returns to BF16. New
+ * parameters drop the calibration. fp8_layers reads the marks (18 entries,
+ * layer order of vulkanpbrt_gb300/kpunet.py), set_fp8_layers fixes them
+ * (entry 0 must be 0). */
 PBRT_API int pbrt_neural_calibrate(PbrtNeural* nd, pbrt_stream_t stream);
 PBRT_API int pbrt_neural_set_precision(PbrtNeural* nd, int32_t bits);
+PBRT_API int pbrt_neural_fp8_layers(const PbrtNeural* nd, int32_t* mask, int32_t count);
+PBRT_API int pbrt_neural_set_fp8_layers(PbrtNeural* nd, const int32_t* mask, int32_t count);
 /* Per-layer convolution kernel: 0 = warp-level mma.sync kernels, 1 =
  * tcgen05 (tensor memory, TMA). autotune (run by the first dispatch when no
  * choice was set) times both for every layer on the current inputs and

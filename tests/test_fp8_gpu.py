@@ -165,14 +165,24 @@ def test_fp8_network_close_to_bf16(cuda):
     with pytest.raises(vp.PbrtError):
         nd.set_precision(8)  # not calibrated yet
     nd.calibrate()
+    mixed = nd.fp8_layers()
+    assert not mixed[0]
+    nd.set_fp8_layers([False] + [True] * 17)  # every layer but the first in e4m3
     nd.set_precision(8)
     nd.dispatch()
     torch.cuda.synchronize()
     f8 = nd.denoised.tensor().clone()
     assert torch.isfinite(f8).all()
     rel = (((f8[..., :3] - bf[..., :3]) ** 2) / (bf[..., :3] ** 2 + 0.01)).mean().item()
-    print(f"relMSE(FP8 network, BF16 network) = {rel:.3e}")
+    print(f"relMSE(FP8 network, BF16 network) = {rel:.3e}; calibration's e4m3 layers {mixed}")
     assert rel < 2e-2
+    with pytest.raises(vp.PbrtError):
+        nd.set_fp8_layers([True] * 18)  # the first convolution stays BF16
+    nd.set_fp8_layers([False] * 18)  # no e4m3 layer: the BF16 network's bits
+    nd.dispatch()
+    torch.cuda.synchronize()
+    assert torch.equal(nd.denoised.tensor(), bf)
+    nd.set_fp8_layers(mixed)
     nd.set_precision(16)
     nd.dispatch()
     torch.cuda.synchronize()

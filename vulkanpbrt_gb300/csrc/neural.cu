@@ -99,8 +99,10 @@ struct PbrtNeural : pbrt::Object {
   // per layer: 0 = mma.sync kernels, 1 = tcgen05 kernel (chosen by timing both on the first dispatch)
   int32_t conv_kernel[kNumConvs] = {};
   bool tuned = false;
-  // FP8 inference (pbrt_neural_calibrate / pbrt_neural_set_precision)
+  // FP8 inference (pbrt_neural_calibrate / pbrt_neural_set_precision):
+  // per layer, e4m3 where the calibration timed it faster than BF16
   int precision = 16;
+  bool fp8_layer[kNumConvs] = {};
   bool calibrated = false;
   uint8_t* w8 = nullptr;      // e4m3 convolution weights, lay.conv_w_total
   float* wscale = nullptr;    // per output channel, all convolutions
@@ -118,6 +120,48 @@ template <class T> int dalloc(T** p, size_t count) {
   return PBRT_OK;
 }
 
+// Convolution i of the forward pass (x: its input, or its skip-concatenated
+// decoder input's upsampled part), in FP8 (e4m3, after calibration) or BF16
+// on the layer's chosen kernel. *pooled: the convolution also wrote the next
+// encoder level's 2x2-pooled input from its epilogue.
+int conv_layer(PbrtNeural* nd, int i, const bf16* x, bool fp8, cudaStream_t s, bool* pooled) {
+  const int n = 1;
+  const ConvSpec& c = kConvs[i];
+  const int h = nd->ph >> c.level, w = nd->pw >> c.level;
+  const bf16* w16 = nd->w16 + nd->lay.conv_w[i];
+  const float* b = nd->params + nd->lay.conv_b[i];
+  const int skip_of[4] = {1, 3, 5, 7};  // e0b, e1b, e2b, e3b
+  const bf16* in1 = c.c2 ? nd->act[skip_of[c.level]] : x;
+  const bf16* in2 = c.c2 ? x : nullptr;
+  *pooled = false;
+  int st;
+  // an encoder level's second convolution on the tcgen05 kernel pools its
+  // output in the epilogue (levels 0-2; the frame must divide into tiles)
+  const bool pool_here = i < 8 && (i & 1) && c.c2 == 0 && nd->conv_kernel[i] == 1 && !fp8 &&
+                         nn_umma_pooled_fits(c.c1, c.cout, h, w);
+  if (fp8) {
+    const uint8_t* w8 = nd->w8 + nd->lay.conv_w[i];
+    const float* wsc = nd->wscale + nd->wsoff[i];
+    const float* ixs = nd->inv_xscale + nd->xsoff[i];
+    if (i < 8 && (i & 1) && c.c2 == 0 && nn_fp8_umma_fits(in1, c.c1, nullptr, 0, w8, c.cout, h, w, true)) {
+      // the encoder's pooling in the FP8 convolution's epilogue
+      st = pbrt_nn_conv3x3_fp8_umma(in1, c.c1, nullptr, 0, w8, wsc, ixs, b, nd->act[i], nd->pool[c.level + 1], n, h,
+                                    w, c.cout, 1, s);
+      *pooled = st == PBRT_OK;
+      return st;
+    }
+    return pbrt_nn_conv3x3_fp8(in1, c.c1, in2, c.c2, w8, wsc, ixs, b, nd->act[i], n, h, w, c.cout, 1, s);
+  }
+  if (pool_here && (st = pbrt_nn_conv3x3_umma_pooled(in1, c.c1, w16, b, nd->act[i], nd->pool[c.level + 1], n, h, w,
+                                                     c.cout, 1, s)) != PBRT_ERROR_UNSUPPORTED) {
+    *pooled = st == PBRT_OK;
+    return st;
+  }
+  if (nd->conv_kernel[i] == 1) return pbrt_nn_conv3x3_umma(in1, c.c1, in2, c.c2, w16, b, nd->act[i], n, h, w, c.cout,
+                                                          1, s);
+  return pbrt_nn_conv3x3(in1, c.c1, in2, c.c2, w16, b, nd->act[i], nullptr, n, h, w, c.cout, 1, s);
+}
+
 int record_forward(PbrtNeural* nd, cudaStream_t s) {
   const int n = 1, PH = nd->ph, PW = nd->pw;
   const PbrtIlluminationBuffer* ib = nd->illumination;
@@ -131,48 +175,16 @@ int record_forward(PbrtNeural* nd, cudaStream_t s) {
   if ((st = pbrt_nn_avgpool2(nd->rad[0], nd->rad[1], 1, n, PH, PW, 3, s))) return st;
   if ((st = pbrt_nn_avgpool2(nd->rad[1], nd->rad[2], 1, n, PH / 2, PW / 2, 3, s))) return st;
   const bf16* x = nd->feat;
-  const int skip_of[4] = {1, 3, 5, 7};  // e0b, e1b, e2b, e3b
   bool pooled = false;  // the previous convolution also wrote the next level's pooled input
   for (int i = 0; i < kNumConvs; ++i) {
     const ConvSpec& c = kConvs[i];
     const int h = PH >> c.level, w = PW >> c.level;
-    const bf16* w16 = nd->w16 + nd->lay.conv_w[i];
-    const float* b = nd->params + nd->lay.conv_b[i];
     if (i < 10 && c.name[2] == 'a' && c.level > 0) {  // encoder: pool the previous level's output first
       if (!pooled && (st = pbrt_nn_avgpool2(x, nd->pool[c.level], 0, n, h * 2, w * 2, kConvs[i - 1].cout, s)))
         return st;
       x = nd->pool[c.level];
     }
-    pooled = false;
-    const bf16* in1 = c.c2 ? nd->act[skip_of[c.level]] : x;
-    const bf16* in2 = c.c2 ? x : nullptr;
-    // an encoder level's second convolution on the tcgen05 kernel pools its
-    // output in the epilogue (levels 0-2; the frame must divide into tiles)
-    const bool pool_here = i < 8 && (i & 1) && c.c2 == 0 && nd->conv_kernel[i] == 1 && nd->precision != 8 &&
-                           nn_umma_pooled_fits(c.c1, c.cout, h, w);
-    // FP8 inference quantises every convolution but the first: its 16 input
-    // channels pad to 32 in e4m3, the BF16 instruction count, so it stays BF16
-    if (nd->precision == 8 && i > 0) {
-      const uint8_t* w8 = nd->w8 + nd->lay.conv_w[i];
-      const float* wsc = nd->wscale + nd->wsoff[i];
-      const float* ixs = nd->inv_xscale + nd->xsoff[i];
-      if (i < 8 && (i & 1) && c.c2 == 0 && nn_fp8_umma_fits(in1, c.c1, nullptr, 0, w8, c.cout, h, w, true)) {
-        // the encoder's pooling in the FP8 convolution's epilogue
-        st = pbrt_nn_conv3x3_fp8_umma(in1, c.c1, nullptr, 0, w8, wsc, ixs, b, nd->act[i], nd->pool[c.level + 1], n, h,
-                                      w, c.cout, 1, s);
-        pooled = st == PBRT_OK;
-      } else {
-        st = pbrt_nn_conv3x3_fp8(in1, c.c1, in2, c.c2, w8, wsc, ixs, b, nd->act[i], n, h, w, c.cout, 1, s);
-      }
-    } else if (pool_here && (st = pbrt_nn_conv3x3_umma_pooled(in1, c.c1, w16, b, nd->act[i], nd->pool[c.level + 1],
-                                                              n, h, w, c.cout, 1, s)) != PBRT_ERROR_UNSUPPORTED) {
-      pooled = st == PBRT_OK;
-    } else if (nd->conv_kernel[i] == 1) {
-      st = pbrt_nn_conv3x3_umma(in1, c.c1, in2, c.c2, w16, b, nd->act[i], n, h, w, c.cout, 1, s);
-    } else {
-      st = pbrt_nn_conv3x3(in1, c.c1, in2, c.c2, w16, b, nd->act[i], nullptr, n, h, w, c.cout, 1, s);
-    }
-    if (st) return st;
+    if ((st = conv_layer(nd, i, x, nd->precision == 8 && nd->fp8_layer[i], s, &pooled))) return st;
     x = nd->act[i];
   }
   for (int k = 0; k < 3; ++k) {
@@ -467,7 +479,12 @@ PBRT_API int pbrt_neural_dispatch_direct(PbrtNeural* nd, pbrt_stream_t stream) {
 // FP8 calibration: one BF16 forward pass on the current inputs, the
 // per-channel maximum |x| of every convolution's input, sx = amax / 448
 // (e4m3's largest finite value), then the per-output-channel FP8 weights
-// with sx folded in.
+// with sx folded in. Then the FP8 mode's per-layer choice: each
+// convolution but the first (whose 16 input channels pad to 32 in e4m3, the
+// BF16 instruction count) timed in BF16 on its chosen kernel and in FP8,
+// each with the next level's pooling where the encoder needs it (fused in
+// the epilogue or a separate launch), median of 3 after a warm-up on the
+// activations of the BF16 pass; FP8 where it is faster.
 PBRT_API int pbrt_neural_calibrate(PbrtNeural* nd, pbrt_stream_t stream) {
   if (!checked<PbrtNeural>(nd, Kind::Neural)) return fail(PBRT_ERROR_INVALID_ARGUMENT, "neural calibrate: not a handle");
   const int saved = nd->precision;
@@ -509,6 +526,66 @@ PBRT_API int pbrt_neural_calibrate(PbrtNeural* nd, pbrt_stream_t stream) {
   if (st) return st;
   PBRT_CUDA(cudaStreamSynchronize(stream));
   nd->calibrated = true;
+  if (!nd->tuned) {  // the BF16 kernels per layer first (as the first dispatch would)
+    nd->tuned = true;
+    st = pbrt_neural_autotune(nd, stream);
+    if (st && st != PBRT_ERROR_TIMEOUT) return st;
+    st = PBRT_OK;
+  }
+  cudaEvent_t e0, e1;
+  PBRT_CUDA(cudaEventCreate(&e0));
+  PBRT_CUDA(cudaEventCreate(&e1));
+  nd->fp8_layer[0] = false;
+  for (int i = 1; i < kNumConvs && !st; ++i) {
+    const ConvSpec& c = kConvs[i];
+    const int h = nd->ph >> c.level, w = nd->pw >> c.level;
+    const bf16* x = (i < 10 && c.name[2] == 'a') ? nd->pool[c.level] : nd->act[i - 1];
+    float best[2] = {1e30f, 1e30f};
+    for (int k = 0; k < 2 && !st; ++k) {
+      float ms[3];
+      for (int r = 0; r < 4 && !st; ++r) {
+        cudaEventRecord(e0, stream);
+        bool pooled = false;
+        st = conv_layer(nd, i, x, k == 1, stream, &pooled);
+        if (!st && i < 8 && (i & 1) && !pooled)
+          st = pbrt_nn_avgpool2(nd->act[i], nd->pool[c.level + 1], 0, 1, h, w, c.cout, stream);
+        cudaEventRecord(e1, stream);
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (!st && e != cudaSuccess) st = cuda_fail(e, "neural calibrate (timing)");
+        if (r > 0) cudaEventElapsedTime(&ms[r - 1], e0, e1);
+      }
+      if (!st) {
+        std::sort(ms, ms + 3);
+        best[k] = ms[1];
+      }
+    }
+    nd->fp8_layer[i] = best[1] < best[0];
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  uint32_t flags = 0;
+  if ((st = pbrt_nn_umma_status(stream, &flags))) return st;
+  if (flags) return fail(PBRT_ERROR_TIMEOUT, "neural calibrate: a tcgen05 convolution timed out");
+  drop_graph(nd);
+  return PBRT_OK;
+}
+
+// FP8 mode's per-layer precision: mask[i] = 1 where convolution i runs in
+// e4m3 (set by the calibration's timing; the first convolution stays BF16).
+PBRT_API int pbrt_neural_fp8_layers(const PbrtNeural* nd, int32_t* mask, int32_t count) {
+  if (!checked<const PbrtNeural>((void*)nd, Kind::Neural) || !mask || count < kNumConvs)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "neural fp8 layers: bad arguments");
+  for (int i = 0; i < kNumConvs; ++i) mask[i] = nd->fp8_layer[i] ? 1 : 0;
+  return PBRT_OK;
+}
+
+PBRT_API int pbrt_neural_set_fp8_layers(PbrtNeural* nd, const int32_t* mask, int32_t count) {
+  if (!checked<PbrtNeural>(nd, Kind::Neural) || !mask || count != kNumConvs)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "neural set fp8 layers: bad arguments");
+  if (mask[0]) return fail(PBRT_ERROR_INVALID_ARGUMENT, "neural set fp8 layers: the first convolution stays BF16");
+  for (int i = 0; i < kNumConvs; ++i) nd->fp8_layer[i] = mask[i] != 0;
+  drop_graph(nd);
   return PBRT_OK;
 }
 

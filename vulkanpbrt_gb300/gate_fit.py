@@ -68,8 +68,10 @@ def tile_features(var, nn_fin, bm_fin, spp, noisy, depth, nrm, alb8):
     return torch.stack([f0, f1, f2, f3, f4, f5, f6, f7], 1), n
 
 
-def collect(out: str, seeds=(21, 22, 23, 24, 25, 26), frames=(15, 30, 46), ref_spp=2048, width=1920, height=1080):
-    """Renders the training frames on cuda:0 and saves features and errors to `out` (.npz)."""
+def collect(out: str, seeds=(21, 22, 23, 24, 25, 26), frames=(15, 30, 46), ref_spp=2048, width=1920, height=1080,
+            weights=None):
+    """Renders the training frames on cuda:0 and saves features and errors to `out` (.npz); `weights`: the
+    network's .npz (default: the packaged weights)."""
     import sys
 
     import torch
@@ -93,8 +95,8 @@ def collect(out: str, seeds=(21, 22, 23, 24, 25, 26), frames=(15, 30, 46), ref_s
         accu = vp.Accumulator(g, illu, separate_matrices=True)
         acc_illu, abuf = accu.accumulated_illumination, accu.accumulation_buffer
         bm = vp.BMFR(W, H, 32, 32, g, acc_illu, abuf, 256)
-        nd = vp.NeuralDenoiser(W, H, g, acc_illu, fallback=bm, threshold=1e30, tile=TILE, acc_buffer=abuf,
-                               gate_model=None)  # the network alone
+        nd = vp.NeuralDenoiser(W, H, g, acc_illu, weights=weights, fallback=bm, threshold=1e30, tile=TILE,
+                               acc_buffer=abuf, gate_model=None)  # the network alone
         pc = vp.PushConstants()
         prev = bench.orbit(sc, W, H, 0)
         hs = vp._abi.stream_handle(stream)
@@ -211,12 +213,13 @@ def main(argv=None):
     c = sub.add_parser("collect")
     c.add_argument("--out", default="gate_data.npz")
     c.add_argument("--ref-spp", type=int, default=2048)
+    c.add_argument("--weights", default=None, help="the network's .npz (default: the packaged weights)")
     f = sub.add_parser("fit")
     f.add_argument("data")
     f.add_argument("--out", default=str(Path(__file__).resolve().parent / "weights" / "gate.json"))
     a = ap.parse_args(argv)
     if a.cmd == "collect":
-        collect(a.out, ref_spp=a.ref_spp)
+        collect(a.out, ref_spp=a.ref_spp, weights=a.weights)
     else:
         print(json.dumps(fit(a.data, a.out), indent=1))
 

@@ -29,6 +29,8 @@ _abi.add_signatures({
     "pbrt_neural_fallback_mask": (C.c_int32, [H, C.POINTER(PbrtImage)]),
     "pbrt_neural_calibrate": (C.c_int32, [H, H]),
     "pbrt_neural_set_precision": (C.c_int32, [H, C.c_int32]),
+    "pbrt_neural_fp8_layers": (C.c_int32, [H, C.POINTER(C.c_int32), C.c_int32]),
+    "pbrt_neural_set_fp8_layers": (C.c_int32, [H, C.POINTER(C.c_int32), C.c_int32]),
     "pbrt_neural_autotune": (C.c_int32, [H, H]),
     "pbrt_neural_conv_kernels": (C.c_int32, [H, C.POINTER(C.c_int32), C.c_int32]),
     "pbrt_neural_set_conv_kernels": (C.c_int32, [H, C.POINTER(C.c_int32), C.c_int32]),
@@ -121,13 +123,24 @@ class NeuralDenoiser(Handle):
         self.fallback_mask = Image(m, self) if m.data else None
 
     def calibrate(self, stream=None) -> None:
-        """FP8 scales from one BF16 pass over the current inputs."""
+        """FP8 scales from one BF16 pass over the current inputs, then each layer timed in BF16 and FP8
+        (fp8_layers: where FP8 is faster)."""
         check(lib().pbrt_neural_calibrate(self.ptr, stream_handle(stream)))
 
     def set_precision(self, bits: int) -> None:
-        """16: BF16 convolutions; 8: FP8 e4m3 for every convolution but the 16-channel input one (after
-        calibrate)."""
+        """16: BF16 convolutions; 8: FP8 e4m3 for the layers fp8_layers marks (after calibrate)."""
         check(lib().pbrt_neural_set_precision(self.ptr, bits))
+
+    def fp8_layers(self) -> list:
+        """Per convolution (kpunet's layer order): True where the FP8 mode runs it in e4m3."""
+        m = (C.c_int32 * 18)()
+        check(lib().pbrt_neural_fp8_layers(self.ptr, m, 18))
+        return [bool(v) for v in m]
+
+    def set_fp8_layers(self, mask) -> None:
+        """Fix the FP8 mode's per-layer precision (the first convolution stays BF16)."""
+        m = (C.c_int32 * 18)(*[1 if v else 0 for v in mask])
+        check(lib().pbrt_neural_set_fp8_layers(self.ptr, m, 18))
 
     def autotune(self, stream=None) -> list:
         """Times the mma.sync and tcgen05 kernels for every convolution on the current inputs; keeps the faster."""
