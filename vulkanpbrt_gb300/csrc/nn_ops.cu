@@ -231,21 +231,27 @@ __global__ void kp_head_fwd_kernel(HeadArgs a) {
   }
 }
 
-// The network's three heads with the 1x1 convolution on the tensor cores:
-// each warp takes 16 pixels, the logits are a [16 x C] x [C x 32] product
-// (27 logits padded to 32) by mma.sync m16n8k16 with FP32 accumulation. The
-// FP32 head weights are split into three BF16 parts (w = hi + mid + lo to
-// ~24 bits) and the features are BF16 already, so the three products add up
-// to the FP32 logits. Lane (g, t) of the warp then holds, for pixels g and
-// g + 8 of the group, logits n = 8 nt + 2t + {0, 1}: the softmax, the 5x5
-// filter of the radiance and the blend reduce over the four lanes of a
-// pixel with shuffles.
+// The network's three heads, a block per tile of 4 rows x 32 pixels (one
+// row a warp, grid-stride over tiles). The 1x1 convolution runs on the
+// tensor cores: per 16-pixel group the logits are a [16 x C] x [C x 32]
+// product (27 logits padded to 32) by mma.sync m16n8k16 with FP32
+// accumulation; the FP32 head weights are split into three BF16 parts
+// (w = hi + mid + lo to ~24 bits) and the features are BF16 already, so the
+// three products add up to the FP32 logits. The logits go through shared
+// memory to one lane a pixel, which takes the softmax and the 5x5 filter as
+// the per-pixel kernel does, reading the radiance from the tile's halo,
+// staged once in shared memory with the edge replication of that kernel
+// (the radiance gather, not the projection, bounds the per-pixel kernel).
 template <int C, int K>
-__global__ void __launch_bounds__(128) kp_head_fwd_mma_kernel(HeadArgs a) {
-  constexpr int KS = C / 16;  // k steps of 16 channels
-  // B fragments of the three weight parts: [part][ks][nt][lane] x 2 registers
-  __shared__ uint2 sB[3][KS][4][32];
+__global__ void __launch_bounds__(128) kp_head_fwd_tile_kernel(HeadArgs a) {
+  constexpr int KS = C / 16;             // k steps of 16 channels
+  constexpr int TW = 32, TH = 4;         // tile: one 32-pixel row a warp
+  constexpr int RW = TW + 4, RH = TH + 4;  // radiance halo (5x5 taps)
+  constexpr int LS = 27;                 // logits a pixel in shared memory (odd: no bank conflicts)
+  __shared__ uint2 sB[3][KS][4][32];     // B fragments of the three weight parts: [part][ks][nt][lane]
   __shared__ float sBias[32];
+  __shared__ float sR[RH * RW * 3];
+  __shared__ float sL[TH][TW * LS];
   for (int i = threadIdx.x; i < 3 * KS * 4 * 32; i += blockDim.x) {
     const int ln = i % 32, nt = (i / 32) % 4, ks = (i / 128) % KS, part = i / (128 * KS);
     const int g = ln >> 2, t = ln & 3, n = nt * 8 + g;
@@ -266,110 +272,103 @@ __global__ void __launch_bounds__(128) kp_head_fwd_mma_kernel(HeadArgs a) {
     sB[part][ks][nt][ln] = make_uint2(r[0], r[1]);
   }
   for (int i = threadIdx.x; i < 32; i += blockDim.x) sBias[i] = i < K ? a.bh[i] : 0.f;
-  __syncthreads();
-  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  const long P = (long)a.N * a.H * a.W;
-  const long groups = (P + 15) / 16;
-  const long warps = (long)gridDim.x * (blockDim.x / 32);
-  for (long grp = blockIdx.x * (long)(blockDim.x / 32) + (threadIdx.x >> 5); grp < groups; grp += warps) {
-    const long p0 = grp * 16;
-    const long pa = min(p0 + g, P - 1), pb = min(p0 + g + 8, P - 1);  // this lane's two pixels (clamped loads)
-    float acc[4][4];
-#pragma unroll
-    for (int nt = 0; nt < 4; ++nt) {
-      const float b0 = sBias[nt * 8 + 2 * t], b1 = sBias[nt * 8 + 2 * t + 1];
-      acc[nt][0] = b0;
-      acc[nt][1] = b1;
-      acc[nt][2] = b0;
-      acc[nt][3] = b1;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const int tiles_x = (a.W + TW - 1) / TW, tiles_y = (a.H + TH - 1) / TH;
+  const long tiles = (long)tiles_x * tiles_y * a.N;
+  for (long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const int n = (int)(tile / ((long)tiles_x * tiles_y));
+    const int rem = (int)(tile % ((long)tiles_x * tiles_y));
+    const int x0 = (rem % tiles_x) * TW, y0 = (rem / tiles_x) * TH;
+    __syncthreads();  // the previous tile's shared-memory reads are done (and sB, sBias written)
+    for (int i = threadIdx.x; i < RH * RW * 3; i += blockDim.x) {
+      const int q = i / 3, hx = q % RW, hy = q / RW;
+      const int sx = min(max(x0 - 2 + hx, 0), a.W - 1), sy = min(max(y0 - 2 + hy, 0), a.H - 1);
+      sR[i] = a.R[(((size_t)n * a.H + sy) * a.W + sx) * 3 + i % 3];
     }
-    const uint32_t* fa = reinterpret_cast<const uint32_t*>(a.F + pa * C);
-    const uint32_t* fb = reinterpret_cast<const uint32_t*>(a.F + pb * C);
-#pragma unroll
-    for (int ks = 0; ks < KS; ++ks) {
-      const uint32_t a0 = fa[ks * 8 + t], a1 = fb[ks * 8 + t], a2 = fa[ks * 8 + 4 + t], a3 = fb[ks * 8 + 4 + t];
-#pragma unroll
-      for (int part = 2; part >= 0; --part)  // smallest parts first
-#pragma unroll
-        for (int nt = 0; nt < 4; ++nt) {
-          const uint2 b = sB[part][ks][nt][lane];
-          asm volatile(
-              "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-              "{%0,%1,%2,%3};\n"
-              : "+f"(acc[nt][0]), "+f"(acc[nt][1]), "+f"(acc[nt][2]), "+f"(acc[nt][3])
-              : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b.x), "r"(b.y));
-        }
-    }
-    // per pixel (h = 0: pixel g, h = 1: pixel g + 8): softmax over the 25 taps
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const long p = p0 + g + 8 * h;
-      const long pc = h ? pb : pa;
-      const int x = (int)(pc % a.W), y = (int)((pc / a.W) % a.H), n = (int)(pc / ((long)a.W * a.H));
-      float lg[8];
+    const int y = y0 + warp, yc = min(y, a.H - 1);
+    const size_t row = ((size_t)n * a.H + yc) * a.W;
+#pragma unroll 1
+    for (int grp = 0; grp < 2; ++grp) {
+      const int xa = min(x0 + grp * 16 + g, a.W - 1), xb = min(x0 + grp * 16 + g + 8, a.W - 1);
+      const uint32_t* fa = reinterpret_cast<const uint32_t*>(a.F + (row + xa) * C);
+      const uint32_t* fb = reinterpret_cast<const uint32_t*>(a.F + (row + xb) * C);
+      float acc[4][4];
 #pragma unroll
       for (int nt = 0; nt < 4; ++nt) {
-        lg[2 * nt] = acc[nt][2 * h];
-        lg[2 * nt + 1] = acc[nt][2 * h + 1];
+        const float b0 = sBias[nt * 8 + 2 * t], b1 = sBias[nt * 8 + 2 * t + 1];
+        acc[nt][0] = b0;
+        acc[nt][1] = b1;
+        acc[nt][2] = b0;
+        acc[nt][3] = b1;
       }
-      float mx = -INFINITY;
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const int k = (j >> 1) * 8 + 2 * t + (j & 1);
-        if (k < kKP) mx = fmaxf(mx, lg[j]);
+      for (int ks = 0; ks < KS; ++ks) {
+        const uint32_t a0 = fa[ks * 8 + t], a1 = fb[ks * 8 + t], a2 = fa[ks * 8 + 4 + t], a3 = fb[ks * 8 + 4 + t];
+#pragma unroll
+        for (int part = 2; part >= 0; --part)  // smallest parts first
+#pragma unroll
+          for (int nt = 0; nt < 4; ++nt) {
+            const uint2 b = sB[part][ks][nt][lane];
+            asm volatile(
+                "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                "{%0,%1,%2,%3};\n"
+                : "+f"(acc[nt][0]), "+f"(acc[nt][1]), "+f"(acc[nt][2]), "+f"(acc[nt][3])
+                : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b.x), "r"(b.y));
+          }
       }
-      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
-      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 2));
-      float e[8], sum = 0.f;
+      // lane (g, t) holds logits 8 nt + 2t + j of the group's pixels g (c0, c1) and g + 8 (c2, c3)
+      float* la = &sL[warp][(grp * 16 + g) * LS];
+      float* lb = la + 8 * LS;
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const int k = (j >> 1) * 8 + 2 * t + (j & 1);
-        e[j] = k < kKP ? __expf(lg[j] - mx) : 0.f;
-        sum += e[j];
-      }
-      sum += __shfl_xor_sync(0xffffffffu, sum, 1);
-      sum += __shfl_xor_sync(0xffffffffu, sum, 2);
-      const float inv = 1.f / sum;
-      float3 f = f3(0.f);
+      for (int nt = 0; nt < 4; ++nt)
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const int k = (j >> 1) * 8 + 2 * t + (j & 1);
-        if (k < kKP) {
-          const float w = e[j] * inv;
-          if (a.kw && p < P) a.kw[p * kKP + k] = w;
-          const int sx = min(max(x + k % 5 - 2, 0), a.W - 1), sy = min(max(y + k / 5 - 2, 0), a.H - 1);
-          const float* r = a.R + (((size_t)n * a.H + sy) * a.W + sx) * 3;
-          f = f + w * f3(r[0], r[1], r[2]);
+        for (int j = 0; j < 2; ++j) {
+          const int k = nt * 8 + 2 * t + j;
+          if (k < K) {
+            la[k] = acc[nt][j];
+            lb[k] = acc[nt][2 + j];
+          }
         }
-      }
-#pragma unroll
-      for (int m = 1; m <= 2; m <<= 1) {
-        f.x += __shfl_xor_sync(0xffffffffu, f.x, m);
-        f.y += __shfl_xor_sync(0xffffffffu, f.y, m);
-        f.z += __shfl_xor_sync(0xffffffffu, f.z, m);
-      }
-      // logits 25, 26 (nt 3, j 1 and 2): lanes t = 0 (c1) and t = 1 (c0)
-      const float l25 = __shfl_sync(0xffffffffu, lg[7], lane & ~3);
-      const float l26 = __shfl_sync(0xffffffffu, lg[6], (lane & ~3) | 1);
-      if (t == 0 && p < P) {
-        if (a.filt) {
-          a.filt[p * 3 + 0] = f.x;
-          a.filt[p * 3 + 1] = f.y;
-          a.filt[p * 3 + 2] = f.z;
-        }
-        float3 o = f;
-        if (a.coarse) {
-          const float al = 1.f / (1.f + __expf(-l25));
-          if (a.alpha) a.alpha[p] = al;
-          const float* cc = a.coarse + (((size_t)n * (a.H / 2) + y / 2) * (a.W / 2) + x / 2) * 3;
-          o = (1.f - al) * f + al * f3(cc[0], cc[1], cc[2]);
-        }
-        if (a.var) a.var[p] = a.coarse ? l26 : l25;
-        a.out[p * 3 + 0] = o.x;
-        a.out[p * 3 + 1] = o.y;
-        a.out[p * 3 + 2] = o.z;
-      }
     }
+    __syncthreads();  // the halo and this warp's logits in place
+    const int x = x0 + lane;
+    if (x >= a.W || y >= a.H) continue;
+    const long p = (long)row + x;
+    const float* lg = &sL[warp][lane * LS];
+    float mx = lg[0];
+#pragma unroll
+    for (int k = 1; k < kKP; ++k) mx = fmaxf(mx, lg[k]);
+    float e[kKP], sum = 0.f;
+#pragma unroll
+    for (int k = 0; k < kKP; ++k) {
+      e[k] = __expf(lg[k] - mx);
+      sum += e[k];
+    }
+    const float inv = 1.f / sum;
+    float3 acc3 = f3(0.f);
+#pragma unroll
+    for (int k = 0; k < kKP; ++k) {
+      const float w = e[k] * inv;
+      if (a.kw) a.kw[p * kKP + k] = w;
+      const float* r = &sR[((warp + k / 5) * RW + lane + k % 5) * 3];
+      acc3 = acc3 + w * f3(r[0], r[1], r[2]);
+    }
+    if (a.filt) {
+      a.filt[p * 3 + 0] = acc3.x;
+      a.filt[p * 3 + 1] = acc3.y;
+      a.filt[p * 3 + 2] = acc3.z;
+    }
+    float3 o = acc3;
+    if (a.coarse) {
+      const float al = 1.f / (1.f + __expf(-lg[kKP]));
+      if (a.alpha) a.alpha[p] = al;
+      const float* cc = a.coarse + (((size_t)n * (a.H / 2) + y / 2) * (a.W / 2) + x / 2) * 3;
+      o = (1.f - al) * acc3 + al * f3(cc[0], cc[1], cc[2]);
+    }
+    if (a.var) a.var[p] = a.coarse ? lg[kKP + 1] : lg[kKP];
+    a.out[p * 3 + 0] = o.x;
+    a.out[p * 3 + 1] = o.y;
+    a.out[p * 3 + 2] = o.z;
   }
 }
 
@@ -753,11 +752,12 @@ PBRT_API int pbrt_nn_kp_head(const void* F, const float* Wh, const float* bh, co
   HeadArgs a{(const bf16*)F, Wh, bh, R, coarse, out, kw, filt, alpha, var, n, h, w, c, k};
   const int g = grid_for((long)n * h * w, 128);
   const size_t sm = (size_t)k * c * sizeof(float);
-  // the network's heads: the 1x1 convolution on the tensor cores, 16 pixels a warp
-  const int gm = grid_for(((long)n * h * w + 15) / 16 * 32, 128);
-  if (c == 64 && k == 25) kp_head_fwd_mma_kernel<64, 25><<<gm, 128, 0, s>>>(a);
-  else if (c == 48 && k == 26) kp_head_fwd_mma_kernel<48, 26><<<gm, 128, 0, s>>>(a);
-  else if (c == 32 && k == 27) kp_head_fwd_mma_kernel<32, 27><<<gm, 128, 0, s>>>(a);
+  // the network's heads: tiles of 4 x 32 pixels, the 1x1 convolution on the tensor cores
+  const long tiles = (long)n * ((h + 3) / 4) * ((w + 31) / 32);
+  const int gt = (int)std::min<long>(tiles, 152L * 8);
+  if (c == 64 && k == 25) kp_head_fwd_tile_kernel<64, 25><<<gt, 128, 0, s>>>(a);
+  else if (c == 48 && k == 26) kp_head_fwd_tile_kernel<48, 26><<<gt, 128, 0, s>>>(a);
+  else if (c == 32 && k == 27) kp_head_fwd_tile_kernel<32, 27><<<gt, 128, 0, s>>>(a);
   else if (c % 8 == 0) kp_head_fwd_kernel<0, 0><<<g, 128, sm, s>>>(a);
   else return fail(PBRT_ERROR_INVALID_ARGUMENT, "kp head: channels must be a multiple of 8");
   return check_launch("kp_head_fwd");

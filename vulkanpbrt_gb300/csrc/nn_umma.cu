@@ -1237,19 +1237,12 @@ size_t ws_smem_f8(int cin, int nc, int stages, int stg = 0) {
 template <int NC, bool kF8> int launch_umma_ws(const UmmaConvArgs& a, cudaStream_t s, bool use_tma_flag,
                                                bool box_flag = true) {
   const int cin = a.c1 + a.c2;
-  // the second input's half-resolution box by TMA (expanded in shared
-  // memory by the gather warps) where the x1 halo comes by TMA and two
-  // stages still fit; else its planes are gathered with cp.async
   CUtensorMap map, map2;
   memset(&map, 0, sizeof(map));
   memset(&map2, 0, sizeof(map2));
   const int use_tma = use_tma_flag && make_x1_map(&map, a.x1, a.N, a.H, a.W, a.c1) ? 1 : 0;
   const size_t smem_max = kF8 ? kWsSmemMaxF8 : kWsSmemMax;
-  int stg = 0;
-  if (use_tma && box_flag && a.c2 > 0 && (kF8 ? ws_smem_f8(cin, NC, 2, a.c2 / 8) : ws_smem(cin, NC, 2, a.c2 / 8)) <= smem_max &&
-      make_x2_map(&map2, a.x2, a.N, a.H >> 1, a.W >> 1, a.c2))
-    stg = a.c2 / 8;
-  auto smem_for = [&](int st) { return kF8 ? ws_smem_f8(cin, NC, st, stg) : ws_smem(cin, NC, st, stg); };
+  auto smem_at = [&](int st, int stg) { return kF8 ? ws_smem_f8(cin, NC, st, stg) : ws_smem(cin, NC, st, stg); };
   // input stages in flight: PBRT_WS_STAGES (2..6) fixes the count; by
   // default the count of 2..4 with the most resident CTAs, the deeper ring
   // among equals, and a shallower one only while every CTA still walks 16
@@ -1294,17 +1287,33 @@ template <int NC, bool kF8> int launch_umma_ws(const UmmaConvArgs& a, cudaStream
   };
   const int tiles_per_image = ((a.W + umma::kTileW - 1) / umma::kTileW) * ((a.H + umma::kTileH - 1) / umma::kTileH);
   const long total_tiles = (long)tiles_per_image * a.N;
-  int stages = env_stages ? env_stages : 4;
-  while (stages > 2 && smem_for(stages) > smem_max) --stages;
-  if (!env_stages) {
-    int best = stages, best_r = resident(smem_for(stages));
-    for (int st = stages - 1; st >= 2; --st) {
-      const int r = resident(smem_for(st));
-      if (r > best_r && total_tiles >= 16L * sms * r) best = st, best_r = r;
+  // stage count for a stage layout (stg box planes a stage)
+  auto pick_stages = [&](int stg) {
+    int stages = env_stages ? env_stages : 4;
+    while (stages > 2 && smem_at(stages, stg) > smem_max) --stages;
+    if (!env_stages) {
+      int best = stages, best_r = resident(smem_at(stages, stg));
+      for (int st = stages - 1; st >= 2; --st) {
+        const int r = resident(smem_at(st, stg));
+        if (r > best_r && total_tiles >= 16L * sms * r) best = st, best_r = r;
+      }
+      stages = best;
     }
-    stages = best;
-  }
-  const size_t smem = smem_for(stages);
+    return stages;
+  };
+  // the second input's half-resolution box by TMA (expanded in shared
+  // memory by the gather warps) where the x1 halo comes by TMA, two stages
+  // fit and the box's room costs no resident CTA; else its planes are
+  // gathered with cp.async (BF16 d0a at 1080p: box 295 us with one CTA an
+  // SM, gathers 245 us with two; d1a: box 108 us, gathers 148 us, one CTA
+  // either way; FP8 d0a: box 242 us, gathers 309 us, two CTAs either way)
+  int stg = 0;
+  if (use_tma && box_flag && a.c2 > 0 && smem_at(2, a.c2 / 8) <= smem_max &&
+      resident(smem_at(pick_stages(a.c2 / 8), a.c2 / 8)) >= resident(smem_at(pick_stages(0), 0)) &&
+      make_x2_map(&map2, a.x2, a.N, a.H >> 1, a.W >> 1, a.c2))
+    stg = a.c2 / 8;
+  const int stages = pick_stages(stg);
+  const size_t smem = smem_at(stages, stg);
   const int per_sm = resident(smem);
   const int grid = (int)std::min(total_tiles, (long)sms * per_sm);
   conv3x3_umma_ws_kernel<NC, kF8><<<grid, threads, smem, s>>>(a, tiles_per_image, map, map2, use_tma, stg, stages);
