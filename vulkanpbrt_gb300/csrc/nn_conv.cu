@@ -731,13 +731,15 @@ __global__ void __launch_bounds__(256) conv3x3_wgrad_kernel(WgradArgs a) {
   __shared__ __align__(128) bf16 sB[2][kWK * kRowW];  // [pixel][ci]
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int wm = warp & 1, wn = warp >> 1;  // 2 x 4 warps: 32 co x 16 ci each
-  const int tap = blockIdx.y;
+  // blockIdx.x: tap + 9 x channel tile (consecutive CTAs read the same pixel
+  // run: L2 reuse across the taps), blockIdx.y: pixel run
+  const int tap = blockIdx.x % 9, tile = blockIdx.x / 9;
   const int dy = tap / 3 - 1, dx = tap % 3 - 1;
   const int ntile_ci = (a.c1 + a.c2 + kWNt - 1) / kWNt;
-  const int co0 = (blockIdx.z / ntile_ci) * kWM, ci0 = (blockIdx.z % ntile_ci) * kWNt;
+  const int co0 = (tile / ntile_ci) * kWM, ci0 = (tile % ntile_ci) * kWNt;
   const int cin = a.c1 + a.c2;
   const long P = (long)a.N * a.H * a.W;
-  const long p_begin = (long)blockIdx.x * a.pix_per_cta;
+  const long p_begin = (long)blockIdx.y * a.pix_per_cta;
   const long p_end = (p_begin + a.pix_per_cta < P) ? p_begin + a.pix_per_cta : P;
   const int H2 = a.H >> 1, W2 = a.W >> 1;
   // loads: 32 pixels x 64 channels = 256 x 16 B for each operand
@@ -970,7 +972,7 @@ PBRT_API int pbrt_nn_conv3x3_wgrad(const void* dy, const void* x1, int32_t c1, c
   long ppc = (P + chunks - 1) / chunks;
   ppc = (ppc + kWK - 1) / kWK * kWK;
   a.pix_per_cta = (int)ppc;
-  dim3 grid((unsigned)((P + ppc - 1) / ppc), 9, tiles);
+  dim3 grid((unsigned)(9 * tiles), (unsigned)((P + ppc - 1) / ppc));
   conv3x3_wgrad_kernel<<<grid, 256, 0, stream>>>(a);
   return check_launch("conv3x3_wgrad_kernel");
 }

@@ -275,23 +275,62 @@ __global__ void __launch_bounds__(128) kp_head_fwd_tile_kernel(HeadArgs a) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   const int tiles_x = (a.W + TW - 1) / TW, tiles_y = (a.H + TH - 1) / TH;
   const long tiles = (long)tiles_x * tiles_y * a.N;
+  // the next tile's radiance halo and feature fragments are loaded into
+  // registers while the current tile is processed
+  constexpr int HR = (RH * RW * 3 + 127) / 128;  // halo values a thread
+  float hr[HR];
+  uint32_t fr[2][KS][4];
+  auto fetch = [&](long tile) {
+    const int n = (int)(tile / ((long)tiles_x * tiles_y));
+    const int rem = (int)(tile % ((long)tiles_x * tiles_y));
+    const int x0 = (rem % tiles_x) * TW, y0 = (rem / tiles_x) * TH;
+#pragma unroll
+    for (int k = 0; k < HR; ++k) {
+      const int i = threadIdx.x + 128 * k;
+      if (i < RH * RW * 3) {
+        const int q = i / 3, hx = q % RW, hy = q / RW;
+        const int sx = min(max(x0 - 2 + hx, 0), a.W - 1), sy = min(max(y0 - 2 + hy, 0), a.H - 1);
+        hr[k] = a.R[(((size_t)n * a.H + sy) * a.W + sx) * 3 + i % 3];
+      }
+    }
+    const size_t row = ((size_t)n * a.H + min(y0 + warp, a.H - 1)) * a.W;
+#pragma unroll
+    for (int grp = 0; grp < 2; ++grp) {
+      const int xa = min(x0 + grp * 16 + g, a.W - 1), xb = min(x0 + grp * 16 + g + 8, a.W - 1);
+      const uint32_t* fa = reinterpret_cast<const uint32_t*>(a.F + (row + xa) * C);
+      const uint32_t* fb = reinterpret_cast<const uint32_t*>(a.F + (row + xb) * C);
+#pragma unroll
+      for (int ks = 0; ks < KS; ++ks) {
+        fr[grp][ks][0] = fa[ks * 8 + t];
+        fr[grp][ks][1] = fb[ks * 8 + t];
+        fr[grp][ks][2] = fa[ks * 8 + 4 + t];
+        fr[grp][ks][3] = fb[ks * 8 + 4 + t];
+      }
+    }
+  };
+  if (blockIdx.x < tiles) fetch(blockIdx.x);
   for (long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
     const int n = (int)(tile / ((long)tiles_x * tiles_y));
     const int rem = (int)(tile % ((long)tiles_x * tiles_y));
     const int x0 = (rem % tiles_x) * TW, y0 = (rem / tiles_x) * TH;
     __syncthreads();  // the previous tile's shared-memory reads are done (and sB, sBias written)
-    for (int i = threadIdx.x; i < RH * RW * 3; i += blockDim.x) {
-      const int q = i / 3, hx = q % RW, hy = q / RW;
-      const int sx = min(max(x0 - 2 + hx, 0), a.W - 1), sy = min(max(y0 - 2 + hy, 0), a.H - 1);
-      sR[i] = a.R[(((size_t)n * a.H + sy) * a.W + sx) * 3 + i % 3];
+#pragma unroll
+    for (int k = 0; k < HR; ++k) {
+      const int i = threadIdx.x + 128 * k;
+      if (i < RH * RW * 3) sR[i] = hr[k];
     }
+    uint32_t fc[2][KS][4];
+#pragma unroll
+    for (int grp = 0; grp < 2; ++grp)
+#pragma unroll
+      for (int ks = 0; ks < KS; ++ks)
+#pragma unroll
+        for (int r = 0; r < 4; ++r) fc[grp][ks][r] = fr[grp][ks][r];
+    if (tile + gridDim.x < tiles) fetch(tile + gridDim.x);
     const int y = y0 + warp, yc = min(y, a.H - 1);
     const size_t row = ((size_t)n * a.H + yc) * a.W;
-#pragma unroll 1
+#pragma unroll
     for (int grp = 0; grp < 2; ++grp) {
-      const int xa = min(x0 + grp * 16 + g, a.W - 1), xb = min(x0 + grp * 16 + g + 8, a.W - 1);
-      const uint32_t* fa = reinterpret_cast<const uint32_t*>(a.F + (row + xa) * C);
-      const uint32_t* fb = reinterpret_cast<const uint32_t*>(a.F + (row + xb) * C);
       float acc[4][4];
 #pragma unroll
       for (int nt = 0; nt < 4; ++nt) {
@@ -303,7 +342,7 @@ __global__ void __launch_bounds__(128) kp_head_fwd_tile_kernel(HeadArgs a) {
       }
 #pragma unroll
       for (int ks = 0; ks < KS; ++ks) {
-        const uint32_t a0 = fa[ks * 8 + t], a1 = fb[ks * 8 + t], a2 = fa[ks * 8 + 4 + t], a3 = fb[ks * 8 + 4 + t];
+        const uint32_t a0 = fc[grp][ks][0], a1 = fc[grp][ks][1], a2 = fc[grp][ks][2], a3 = fc[grp][ks][3];
 #pragma unroll
         for (int part = 2; part >= 0; --part)  // smallest parts first
 #pragma unroll
@@ -382,68 +421,129 @@ struct HeadBwdArgs {
   float* dcoarse;      // [N][H/2][W/2][3] accumulated, or null
 };
 
-__global__ void kp_head_bwd_kernel(HeadBwdArgs b) {
-  extern __shared__ float sm[];
+// Backward of a head, 128 pixels a block per batch (one a thread): the
+// thread takes its pixel's softmax, filter and blend backward and the
+// feature gradient (dF += W^T dl), and leaves dl and the pixel's features
+// in shared memory; then the block sums the weight gradient dW = sum over
+// the batch of dl F^T with each thread owning (logit, 8 channels) blocks in
+// registers -- no shared-memory atomics on addresses every lane shares --
+// and adds its blocks to dWh once at the end.
+constexpr int kHeadBwdThreads = 128;
+__host__ __device__ constexpr int head_bwd_dl_stride(int k) { return k | 1; }  // odd: no bank conflicts
+__host__ __device__ constexpr int head_bwd_f_stride(int c) { return c + 8; }   // BF16, 16-byte rows
+__host__ __device__ constexpr size_t head_bwd_smem(int k, int c) {
+  return ((size_t)k * c + (size_t)kHeadBwdThreads * head_bwd_dl_stride(k)) * sizeof(float) +
+         (size_t)kHeadBwdThreads * head_bwd_f_stride(c) * sizeof(bf16);
+}
+
+// CT, KT > 0: the network's three heads (sizes fixed at compile time, so the
+// per-pixel logit gradients stay in registers); 0: any.
+template <int CT, int KT>
+__global__ void __launch_bounds__(kHeadBwdThreads) kp_head_bwd_kernel(HeadBwdArgs b) {
+  extern __shared__ __align__(16) float sm[];
   const HeadArgs& a = b.f;
-  float* sW = sm;                  // [K][C]
-  float* sdW = sm + a.K * a.C;     // [K][C]
-  float* sdb = sdW + a.K * a.C;    // [K]
-  for (int i = threadIdx.x; i < a.K * a.C; i += blockDim.x) {
-    sW[i] = a.Wh[i];
-    sdW[i] = 0.f;
-  }
-  for (int i = threadIdx.x; i < a.K; i += blockDim.x) sdb[i] = 0.f;
-  __syncthreads();
+  const int K = KT > 0 ? KT : a.K, C = CT > 0 ? CT : a.C, DLS = head_bwd_dl_stride(K), FS = head_bwd_f_stride(C);
+  float* sW = sm;                                          // [K][C]
+  float* sDL = sW + K * C;                                 // [128][DLS]
+  bf16* sF = reinterpret_cast<bf16*>(sDL + kHeadBwdThreads * DLS);  // [128][FS]
+  const int tid = threadIdx.x;
+  for (int i = tid; i < K * C; i += blockDim.x) sW[i] = a.Wh[i];
+  const int cb = C / 8, owners = K * cb;
+  float acc[2][8];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int e = 0; e < 8; ++e) acc[i][e] = 0.f;
+  float accb = 0.f;
   const long P = (long)a.N * a.H * a.W;
-  GRID_STRIDE(p, P) {
-    const int x = (int)(p % a.W), y = (int)((p / a.W) % a.H), n = (int)(p / ((long)a.W * a.H));
-    float3 dout = f3(b.dout[p * 3], b.dout[p * 3 + 1], b.dout[p * 3 + 2]);
+  for (long base = (long)blockIdx.x * kHeadBwdThreads; base < P; base += (long)gridDim.x * kHeadBwdThreads) {
+    __syncthreads();  // sW written; the previous batch's shared-memory reads done
+    const long p = base + tid;
     float dl[27];
-    for (int k = 0; k < a.K; ++k) dl[k] = 0.f;
-    float3 df = dout;
-    if (a.coarse) {
-      const float al = a.alpha[p];
-      const float* cc = a.coarse + (((size_t)n * (a.H / 2) + y / 2) * (a.W / 2) + x / 2) * 3;
-      const float3 fl = f3(a.filt[p * 3], a.filt[p * 3 + 1], a.filt[p * 3 + 2]);
-      const float da = dot(dout, f3(cc[0], cc[1], cc[2]) - fl);
-      dl[kKP] = da * al * (1.f - al);
-      df = (1.f - al) * dout;
-      if (b.dcoarse) {
-        float* dc = b.dcoarse + (((size_t)n * (a.H / 2) + y / 2) * (a.W / 2) + x / 2) * 3;
-        atomicAdd(dc + 0, al * dout.x);
-        atomicAdd(dc + 1, al * dout.y);
-        atomicAdd(dc + 2, al * dout.z);
+#pragma unroll
+    for (int k = 0; k < 27; ++k) dl[k] = 0.f;
+    if (p < P) {
+      const int x = (int)(p % a.W), y = (int)((p / a.W) % a.H), n = (int)(p / ((long)a.W * a.H));
+      const float3 dout = f3(b.dout[p * 3], b.dout[p * 3 + 1], b.dout[p * 3 + 2]);
+      float3 df = dout;
+      if (a.coarse) {
+        const float al = a.alpha[p];
+        const float* cc = a.coarse + (((size_t)n * (a.H / 2) + y / 2) * (a.W / 2) + x / 2) * 3;
+        const float3 fl = f3(a.filt[p * 3], a.filt[p * 3 + 1], a.filt[p * 3 + 2]);
+        const float da = dot(dout, f3(cc[0], cc[1], cc[2]) - fl);
+        dl[kKP] = da * al * (1.f - al);
+        df = (1.f - al) * dout;
+        if (b.dcoarse) {
+          float* dc = b.dcoarse + (((size_t)n * (a.H / 2) + y / 2) * (a.W / 2) + x / 2) * 3;
+          atomicAdd(dc + 0, al * dout.x);
+          atomicAdd(dc + 1, al * dout.y);
+          atomicAdd(dc + 2, al * dout.z);
+        }
+      }
+      if (b.dvar) dl[a.coarse ? kKP + 1 : kKP] = b.dvar[p];
+      // softmax backward
+      float dw[kKP], sum = 0.f;
+      for (int k = 0; k < kKP; ++k) {
+        const int sx = min(max(x + k % 5 - 2, 0), a.W - 1), sy = min(max(y + k / 5 - 2, 0), a.H - 1);
+        const float* r = a.R + (((size_t)n * a.H + sy) * a.W + sx) * 3;
+        dw[k] = dot(df, f3(r[0], r[1], r[2]));
+        sum += a.kw[p * kKP + k] * dw[k];
+      }
+      for (int k = 0; k < kKP; ++k) dl[k] = a.kw[p * kKP + k] * (dw[k] - sum);
+      const bf16* f = a.F + p * C;
+      float* dF = b.dF + p * C;
+      for (int c = 0; c < C; c += 8) {
+        const uint4 raw = *reinterpret_cast<const uint4*>(f + c);
+        *reinterpret_cast<uint4*>(&sF[tid * FS + c]) = raw;
+        for (int h = 0; h < 8; h += 2) {
+          float g0 = 0.f, g1 = 0.f;
+#pragma unroll
+          for (int k = 0; k < 27; ++k) {
+            if (k >= K) break;
+            g0 += sW[k * C + c + h] * dl[k];
+            g1 += sW[k * C + c + h + 1] * dl[k];
+          }
+          dF[c + h] += g0;
+          dF[c + h + 1] += g1;
+        }
+      }
+    } else {
+      for (int c = 0; c < C; c += 8) *reinterpret_cast<uint4*>(&sF[tid * FS + c]) = make_uint4(0u, 0u, 0u, 0u);
+    }
+#pragma unroll
+    for (int k = 0; k < 27; ++k)
+      if (k < K) sDL[tid * DLS + k] = dl[k];
+    __syncthreads();
+    // dW over the batch: thread owns (k, channels c0 .. c0 + 7) for j = tid, tid + 128
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const int j = tid + i * kHeadBwdThreads;
+      if (j >= owners) break;
+      const int k = j / cb, c0 = (j % cb) * 8;
+      for (int q = 0; q < kHeadBwdThreads; ++q) {
+        const float d = sDL[q * DLS + k];
+        const uint4 raw = *reinterpret_cast<const uint4*>(&sF[q * FS + c0]);
+        const uint32_t w4[4] = {raw.x, raw.y, raw.z, raw.w};
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          const float2 v = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w4[h]));
+          acc[i][2 * h] += d * v.x;
+          acc[i][2 * h + 1] += d * v.y;
+        }
       }
     }
-    if (b.dvar) dl[a.coarse ? kKP + 1 : kKP] = b.dvar[p];
-    // softmax backward
-    float dw[kKP], sum = 0.f;
-    for (int k = 0; k < kKP; ++k) {
-      const int sx = min(max(x + k % 5 - 2, 0), a.W - 1), sy = min(max(y + k / 5 - 2, 0), a.H - 1);
-      const float* r = a.R + (((size_t)n * a.H + sy) * a.W + sx) * 3;
-      dw[k] = dot(df, f3(r[0], r[1], r[2]));
-      sum += a.kw[p * kKP + k] * dw[k];
-    }
-    for (int k = 0; k < kKP; ++k) dl[k] = a.kw[p * kKP + k] * (dw[k] - sum);
-    const bf16* f = a.F + p * a.C;
-    float* dF = b.dF + p * a.C;
-    for (int c = 0; c < a.C; c += 2) {
-      float2 v = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(f + c));
-      float g0 = 0.f, g1 = 0.f;
-      for (int k = 0; k < a.K; ++k) {
-        g0 += sW[k * a.C + c] * dl[k];
-        g1 += sW[k * a.C + c + 1] * dl[k];
-        atomicAdd(&sdW[k * a.C + c], dl[k] * v.x);
-        atomicAdd(&sdW[k * a.C + c + 1], dl[k] * v.y);
-      }
-      dF[c] += g0;
-      dF[c + 1] += g1;
-    }
-    for (int k = 0; k < a.K; ++k) atomicAdd(&sdb[k], dl[k]);
+    if (tid < K)
+      for (int q = 0; q < kHeadBwdThreads; ++q) accb += sDL[q * DLS + tid];
   }
-  __syncthreads();
-  for (int i = threadIdx.x; i < a.K * a.C; i += blockDim.x) atomicAdd(&b.dWh[i], sdW[i]);
-  for (int i = threadIdx.x; i < a.K; i += blockDim.x) atomicAdd(&b.dbh[i], sdb[i]);
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const int j = tid + i * kHeadBwdThreads;
+    if (j >= owners) break;
+    const int k = j / cb, c0 = (j % cb) * 8;
+#pragma unroll
+    for (int e = 0; e < 8; ++e) atomicAdd(&b.dWh[k * C + c0 + e], acc[i][e]);
+  }
+  if (tid < K) atomicAdd(&b.dbh[tid], accb);
 }
 
 // relMSE of the remodulated output against the remodulated target:
@@ -695,6 +795,18 @@ using namespace pbrt::nn;
 
 namespace {
 inline int grid_for(long n, int block = 256) { return (int)std::min<long>((n + block - 1) / block, 152L * 16); }
+// Blocks of 128 threads of `kernel` resident on the device at once (at
+// least one an SM), capped at `work` units.
+template <class Kernel> int head_grid(Kernel kernel, long work) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, 0) != cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  return (int)std::max<long>(1, std::min<long>(work, (long)sms * per_sm));
+}
 }  // namespace
 
 extern "C" {
@@ -752,14 +864,20 @@ PBRT_API int pbrt_nn_kp_head(const void* F, const float* Wh, const float* bh, co
   HeadArgs a{(const bf16*)F, Wh, bh, R, coarse, out, kw, filt, alpha, var, n, h, w, c, k};
   const int g = grid_for((long)n * h * w, 128);
   const size_t sm = (size_t)k * c * sizeof(float);
-  // the network's heads: tiles of 4 x 32 pixels, the 1x1 convolution on the tensor cores
+  // the network's heads: tiles of 4 x 32 pixels, the 1x1 convolution on the
+  // tensor cores; one wave of resident blocks walks the tiles
   const long tiles = (long)n * ((h + 3) / 4) * ((w + 31) / 32);
-  const int gt = (int)std::min<long>(tiles, 152L * 8);
-  if (c == 64 && k == 25) kp_head_fwd_tile_kernel<64, 25><<<gt, 128, 0, s>>>(a);
-  else if (c == 48 && k == 26) kp_head_fwd_tile_kernel<48, 26><<<gt, 128, 0, s>>>(a);
-  else if (c == 32 && k == 27) kp_head_fwd_tile_kernel<32, 27><<<gt, 128, 0, s>>>(a);
-  else if (c % 8 == 0) kp_head_fwd_kernel<0, 0><<<g, 128, sm, s>>>(a);
-  else return fail(PBRT_ERROR_INVALID_ARGUMENT, "kp head: channels must be a multiple of 8");
+  if (c == 64 && k == 25) {
+    kp_head_fwd_tile_kernel<64, 25><<<head_grid(kp_head_fwd_tile_kernel<64, 25>, tiles), 128, 0, s>>>(a);
+  } else if (c == 48 && k == 26) {
+    kp_head_fwd_tile_kernel<48, 26><<<head_grid(kp_head_fwd_tile_kernel<48, 26>, tiles), 128, 0, s>>>(a);
+  } else if (c == 32 && k == 27) {
+    kp_head_fwd_tile_kernel<32, 27><<<head_grid(kp_head_fwd_tile_kernel<32, 27>, tiles), 128, 0, s>>>(a);
+  } else if (c % 8 == 0) {
+    kp_head_fwd_kernel<0, 0><<<g, 128, sm, s>>>(a);
+  } else {
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "kp head: channels must be a multiple of 8");
+  }
   return check_launch("kp_head_fwd");
 }
 
@@ -768,8 +886,8 @@ PBRT_API int pbrt_nn_kp_head_bwd(const void* F, const float* Wh, const float* bh
                                  int32_t k, const float* dout, const float* dvar, float* dF, float* dWh, float* dbh,
                                  float* dcoarse, pbrt_stream_t s) {
   if (!F || !Wh || !R || !kw || !filt || (coarse && !alpha) || !dout || !dF || !dWh || !dbh || k < kKP || k > 27 ||
-      c % 2 || (2 * (size_t)k * c + k) * sizeof(float) > 48 * 1024 || (dvar && k <= (coarse ? kKP + 1 : kKP)) ||
-      (coarse && k < kKP + 1))
+      c % 8 || c <= 0 || head_bwd_smem(k, c) > 48 * 1024 || k * (c / 8) > 2 * kHeadBwdThreads ||
+      (dvar && k <= (coarse ? kKP + 1 : kKP)) || (coarse && k < kKP + 1) || ((uintptr_t)F & 15))
     return fail(PBRT_ERROR_INVALID_ARGUMENT, "kp head bwd: bad arguments");
   HeadBwdArgs b;
   b.f = HeadArgs{(const bf16*)F, Wh, bh, R, coarse, nullptr, kw, filt, alpha, nullptr, n, h, w, c, k};
@@ -779,8 +897,12 @@ PBRT_API int pbrt_nn_kp_head_bwd(const void* F, const float* Wh, const float* bh
   b.dWh = dWh;
   b.dbh = dbh;
   b.dcoarse = dcoarse;
-  const size_t smem = (2 * (size_t)k * c + k) * sizeof(float);
-  kp_head_bwd_kernel<<<grid_for((long)n * h * w, 128), 128, smem, s>>>(b);
+  const int g = grid_for((long)n * h * w, kHeadBwdThreads);
+  const size_t sm = head_bwd_smem(k, c);
+  if (c == 64 && k == 25) kp_head_bwd_kernel<64, 25><<<g, kHeadBwdThreads, sm, s>>>(b);
+  else if (c == 48 && k == 26) kp_head_bwd_kernel<48, 26><<<g, kHeadBwdThreads, sm, s>>>(b);
+  else if (c == 32 && k == 27) kp_head_bwd_kernel<32, 27><<<g, kHeadBwdThreads, sm, s>>>(b);
+  else kp_head_bwd_kernel<0, 0><<<g, kHeadBwdThreads, sm, s>>>(b);
   return check_launch("kp_head_bwd");
 }
 

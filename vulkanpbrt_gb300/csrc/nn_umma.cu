@@ -994,9 +994,11 @@ __global__ void __launch_bounds__(128) conv3x3_wgrad_umma_kernel(UmmaWgradArgs a
   __shared__ uint32_t tmem_base_slot;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int cin = a.c1 + a.c2;
-  const int tap = blockIdx.y, dy = tap / 3 - 1, dx = tap % 3 - 1;
+  // blockIdx.x: tap (consecutive CTAs read the same pixel run: L2 reuse
+  // across the taps), blockIdx.y: pixel run
+  const int tap = blockIdx.x, dy = tap / 3 - 1, dx = tap % 3 - 1;
   const long P = (long)a.N * a.H * a.W;
-  const long p_begin = (long)blockIdx.x * a.pix_per_cta;
+  const long p_begin = (long)blockIdx.y * a.pix_per_cta;
   const long p_end = p_begin + a.pix_per_cta < P ? p_begin + a.pix_per_cta : P;
   const int n_it = p_begin < p_end ? (int)((p_end - p_begin + kWgK - 1) / kWgK) : 0;
   const int H2 = a.H >> 1, W2 = a.W >> 1;
@@ -1024,37 +1026,39 @@ __global__ void __launch_bounds__(128) conv3x3_wgrad_umma_kernel(UmmaWgradArgs a
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   const uint32_t tmem = tmem_base_slot;
 
+  // a stage: thread tid copies pixel tid % 64 of the run, channel groups
+  // tid / 64, + 2, ...: the pixel's coordinates once per stage
   auto load = [&](int st, int it) {
     const uint32_t ab = sbase + st * stage_bytes, bb = ab + kWgABytes;
-    const long pb = p_begin + (long)it * kWgK;
     const int ga = a.cout / 8, gb = cin / 8;
-    for (int q = tid; q < kWgK * (ga + gb); q += 128) {
-      const int pl = q % kWgK, g = q / kWgK;  // consecutive threads: consecutive pixels
-      const long p = pb + pl;
-      const bool pv = p < p_end;
-      const long pp = pv ? p : 0;
-      const uint32_t off = (uint32_t)((pl >> 3) * 128 + (pl & 7) * 16);
+    const int pl = tid % kWgK;
+    const long p = p_begin + (long)it * kWgK + pl;
+    const bool pv = p < p_end;
+    const long pp = pv ? p : 0;
+    const int n = (int)(pp / ((long)a.H * a.W));
+    const int rem = (int)(pp - (long)n * a.H * a.W);
+    const int yy = rem / a.W + dy, xx = rem % a.W + dx;
+    const bool inb = pv && yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
+    const bf16* px1 = inb ? a.x1 + (((size_t)n * a.H + yy) * a.W + xx) * a.c1 : a.x1;
+    const bf16* px2 = inb && a.c2 ? a.x2 + (((size_t)n * H2 + (yy >> 1)) * W2 + (xx >> 1)) * a.c2 : a.x1;
+    const bf16* pdy = a.dy + pp * a.cout;
+    const uint32_t off = (uint32_t)((pl >> 3) * 128 + (pl & 7) * 16);
+    for (int g = tid / kWgK; g < ga + gb; g += 128 / kWgK) {
       if (g < ga) {
-        umma::cp16(ab + g * 1024 + off, a.dy + pp * a.cout + g * 8, pv);
+        umma::cp16(ab + g * 1024 + off, pdy + g * 8, pv);
       } else {
         const int ci = (g - ga) * 8;
-        const int n = (int)(pp / ((long)a.H * a.W));
-        const int rem = (int)(pp - (long)n * a.H * a.W);
-        const int yy = rem / a.W + dy, xx = rem % a.W + dx;
-        const bool ok = pv && yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
-        const bf16* src = a.x1;
-        if (ok) {
-          if (ci < a.c1) src = a.x1 + (((size_t)n * a.H + yy) * a.W + xx) * a.c1 + ci;
-          else src = a.x2 + (((size_t)n * H2 + (yy >> 1)) * W2 + (xx >> 1)) * a.c2 + (ci - a.c1);
-        }
-        umma::cp16(bb + (g - ga) * 1024 + off, src, ok);
+        umma::cp16(bb + (g - ga) * 1024 + off, ci < a.c1 ? px1 + ci : px2 + (ci - a.c1), inb);
       }
     }
   };
 
   bool failed = false;
   int issued = 0;  // iterations whose MMAs were issued (the same count in every thread)
-  for (int j = 0; j < kWgStages - 1; ++j) {
+  // loads run kWgAhead iterations ahead; a refill waits for the MMAs of the
+  // iteration kWgStages back, issued kWgStages - kWgAhead iterations earlier
+  constexpr int kWgAhead = kWgStages - 2;
+  for (int j = 0; j < kWgAhead; ++j) {
     if (j < n_it) load(j, j);
     asm volatile("cp.async.commit_group;\n" ::);
   }
@@ -1063,10 +1067,11 @@ __global__ void __launch_bounds__(128) conv3x3_wgrad_umma_kernel(UmmaWgradArgs a
                          ((uint32_t)(128 >> 4) << 24);
   for (int it = 0; it < n_it && !failed; ++it) {
     const int st = it % kWgStages;
-    const int j = it + kWgStages - 1;  // refill the stage the previous iteration's MMAs read
+    const int j = it + kWgAhead;  // refill the stage iteration j - kWgStages read
     if (j < n_it) {
       bool ok = true;
-      if (it >= 1) ok = umma::mbar_wait(mb((it - 1) % kWgStages), (uint32_t)(((it - 1) / kWgStages) & 1));
+      const int prev = j - kWgStages;
+      if (prev >= 0) ok = umma::mbar_wait(mb(prev % kWgStages), (uint32_t)((prev / kWgStages) & 1));
       if (__syncthreads_or(!ok)) {
         failed = true;
         break;
@@ -1074,7 +1079,7 @@ __global__ void __launch_bounds__(128) conv3x3_wgrad_umma_kernel(UmmaWgradArgs a
       load(j % kWgStages, j);
     }
     asm volatile("cp.async.commit_group;\n" ::);
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(kWgStages - 1));
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(kWgAhead));
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     __syncthreads();
     if (tid == 0) {
@@ -1473,7 +1478,7 @@ PBRT_API int pbrt_nn_conv3x3_wgrad_umma(const void* dy, const void* x1, int32_t 
   long ppc = (P + chunks - 1) / chunks;
   ppc = (ppc + kWgK - 1) / kWgK * kWgK;
   UmmaWgradArgs a{(const bf16*)dy, (const bf16*)x1, (const bf16*)x2, c1, c2, dw, n, h, wd, cout, (int)ppc};
-  dim3 grid((unsigned)((P + ppc - 1) / ppc), 9);
+  dim3 grid(9, (unsigned)((P + ppc - 1) / ppc));
   conv3x3_wgrad_umma_kernel<<<grid, 128, smem, stream>>>(a);
   return check_launch("conv3x3_wgrad_umma_kernel");
 }
