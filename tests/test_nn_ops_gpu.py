@@ -92,6 +92,27 @@ def test_pool_relu_split_backward(cuda):
     assert _rel(dx1, x1r.grad) < 1e-6 and _rel(dx2, x2r.grad) < 1e-5
 
 
+@pytest.mark.parametrize("c", [48, 96, 128])
+def test_relu_backward_channel_groups(cuda, c):
+    """ReLU backward at the network's other widths (8-channel groups: 6, 12,
+    16 a pixel) over more pixels than one block's first pass."""
+    import torch
+
+    from vulkanpbrt_gb300 import nn
+
+    g = torch.Generator().manual_seed(c)
+    n, h, w = 1, 96, 160
+    ya = torch.randn(n, h, w, c, generator=g).bfloat16()
+    dya = torch.randn(n, h, w, c, generator=g)
+    gm = torch.empty(n, h, w, c, dtype=torch.bfloat16, device=cuda)
+    db = torch.zeros(c, device=cuda)
+    nn.relu_bwd(dya.to(cuda), ya.to(cuda), gm, db)
+    torch.cuda.synchronize()
+    gm_ref = (dya * (ya.float() > 0)).bfloat16()
+    assert torch.equal(gm.cpu(), gm_ref)
+    assert _rel(db, gm_ref.float().sum((0, 1, 2))) < 1e-4
+
+
 @pytest.mark.parametrize("n,h,w", [(2, 12, 20), (1, 10, 14)])
 @pytest.mark.parametrize("scale,k,c", [(2, 25, 64), (1, 26, 48), (0, 27, 32)])
 def test_kp_head_forward_backward(cuda, scale, k, c, n, h, w):

@@ -103,22 +103,48 @@ __global__ void avgpool2_bwd_add_kernel(const float* __restrict__ dy, float* __r
 
 // out = bf16(dy * (y > 0)) and db[c] += sum of it (block partials, one
 // atomic per channel per block).
-__global__ void relu_bwd_kernel(const float* __restrict__ dy, const bf16* __restrict__ y, bf16* __restrict__ out,
-                                float* __restrict__ db, long P, int C) {
+// ReLU backward, 8 channels (16 bytes of BF16) a thread: out = bf16(dy) where
+// y > 0, else 0, and the bias gradient db += sum over pixels of out. 192
+// threads a block (a multiple of every channel-group count C / 8 up to 24),
+// so a thread keeps one channel group for all its pixels and sums its 8
+// bias partials in registers; one shared-memory and one global atomic a
+// channel, thread and block at the end.
+constexpr int kReluBwdThreads = 192;
+__global__ void __launch_bounds__(kReluBwdThreads) relu_bwd_kernel(const float* __restrict__ dy,
+                                                                   const bf16* __restrict__ y, bf16* __restrict__ out,
+                                                                   float* __restrict__ db, long P, int C) {
   extern __shared__ float sdb[];
   for (int c = threadIdx.x; c < C; c += blockDim.x) sdb[c] = 0.f;
   __syncthreads();
-  const long total = P * C;
-  GRID_STRIDE(i, total) {
-    const int c = (int)(i % C);
-    float g = __bfloat162float(y[i]) > 0.f ? dy[i] : 0.f;
-    bf16 gb = __float2bfloat16_rn(g);
-    out[i] = gb;
-    if (db) atomicAdd(&sdb[c], __bfloat162float(gb));
+  const int G = C / 8, per_block = kReluBwdThreads / G;
+  const int gi = threadIdx.x % G, c0 = gi * 8;
+  float part[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if ((int)threadIdx.x < per_block * G) {
+    for (long p = (long)blockIdx.x * per_block + threadIdx.x / G; p < P; p += (long)gridDim.x * per_block) {
+      const size_t i = (size_t)p * C + c0;
+      const uint4 yr = *reinterpret_cast<const uint4*>(y + i);
+      const float4 d0 = *reinterpret_cast<const float4*>(dy + i), d1 = *reinterpret_cast<const float4*>(dy + i + 4);
+      const uint32_t yw[4] = {yr.x, yr.y, yr.z, yr.w};
+      const float dv[8] = {d0.x, d0.y, d0.z, d0.w, d1.x, d1.y, d1.z, d1.w};
+      uint32_t o[4];
+#pragma unroll
+      for (int h = 0; h < 4; ++h) {
+        const float2 yv = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&yw[h]));
+        const __nv_bfloat162 g2 = __floats2bfloat162_rn(yv.x > 0.f ? dv[2 * h] : 0.f, yv.y > 0.f ? dv[2 * h + 1] : 0.f);
+        const float2 gf = __bfloat1622float2(g2);
+        part[2 * h] += gf.x;
+        part[2 * h + 1] += gf.y;
+        o[h] = *reinterpret_cast<const uint32_t*>(&g2);
+      }
+      *reinterpret_cast<uint4*>(out + i) = make_uint4(o[0], o[1], o[2], o[3]);
+    }
   }
-  __syncthreads();
-  if (db)
+  if (db) {
+#pragma unroll
+    for (int e = 0; e < 8; ++e) atomicAdd(&sdb[c0 + e], part[e]);
+    __syncthreads();
     for (int c = threadIdx.x; c < C; c += blockDim.x) atomicAdd(&db[c], sdb[c]);
+  }
 }
 
 // Backward of "concat(x1, upsample2(x2))": dx1 += dcat[:, :c1];
@@ -275,62 +301,23 @@ __global__ void __launch_bounds__(128) kp_head_fwd_tile_kernel(HeadArgs a) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   const int tiles_x = (a.W + TW - 1) / TW, tiles_y = (a.H + TH - 1) / TH;
   const long tiles = (long)tiles_x * tiles_y * a.N;
-  // the next tile's radiance halo and feature fragments are loaded into
-  // registers while the current tile is processed
-  constexpr int HR = (RH * RW * 3 + 127) / 128;  // halo values a thread
-  float hr[HR];
-  uint32_t fr[2][KS][4];
-  auto fetch = [&](long tile) {
-    const int n = (int)(tile / ((long)tiles_x * tiles_y));
-    const int rem = (int)(tile % ((long)tiles_x * tiles_y));
-    const int x0 = (rem % tiles_x) * TW, y0 = (rem / tiles_x) * TH;
-#pragma unroll
-    for (int k = 0; k < HR; ++k) {
-      const int i = threadIdx.x + 128 * k;
-      if (i < RH * RW * 3) {
-        const int q = i / 3, hx = q % RW, hy = q / RW;
-        const int sx = min(max(x0 - 2 + hx, 0), a.W - 1), sy = min(max(y0 - 2 + hy, 0), a.H - 1);
-        hr[k] = a.R[(((size_t)n * a.H + sy) * a.W + sx) * 3 + i % 3];
-      }
-    }
-    const size_t row = ((size_t)n * a.H + min(y0 + warp, a.H - 1)) * a.W;
-#pragma unroll
-    for (int grp = 0; grp < 2; ++grp) {
-      const int xa = min(x0 + grp * 16 + g, a.W - 1), xb = min(x0 + grp * 16 + g + 8, a.W - 1);
-      const uint32_t* fa = reinterpret_cast<const uint32_t*>(a.F + (row + xa) * C);
-      const uint32_t* fb = reinterpret_cast<const uint32_t*>(a.F + (row + xb) * C);
-#pragma unroll
-      for (int ks = 0; ks < KS; ++ks) {
-        fr[grp][ks][0] = fa[ks * 8 + t];
-        fr[grp][ks][1] = fb[ks * 8 + t];
-        fr[grp][ks][2] = fa[ks * 8 + 4 + t];
-        fr[grp][ks][3] = fb[ks * 8 + 4 + t];
-      }
-    }
-  };
-  if (blockIdx.x < tiles) fetch(blockIdx.x);
   for (long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
     const int n = (int)(tile / ((long)tiles_x * tiles_y));
     const int rem = (int)(tile % ((long)tiles_x * tiles_y));
     const int x0 = (rem % tiles_x) * TW, y0 = (rem / tiles_x) * TH;
     __syncthreads();  // the previous tile's shared-memory reads are done (and sB, sBias written)
-#pragma unroll
-    for (int k = 0; k < HR; ++k) {
-      const int i = threadIdx.x + 128 * k;
-      if (i < RH * RW * 3) sR[i] = hr[k];
+    for (int i = threadIdx.x; i < RH * RW * 3; i += blockDim.x) {
+      const int q = i / 3, hx = q % RW, hy = q / RW;
+      const int sx = min(max(x0 - 2 + hx, 0), a.W - 1), sy = min(max(y0 - 2 + hy, 0), a.H - 1);
+      sR[i] = a.R[(((size_t)n * a.H + sy) * a.W + sx) * 3 + i % 3];
     }
-    uint32_t fc[2][KS][4];
-#pragma unroll
-    for (int grp = 0; grp < 2; ++grp)
-#pragma unroll
-      for (int ks = 0; ks < KS; ++ks)
-#pragma unroll
-        for (int r = 0; r < 4; ++r) fc[grp][ks][r] = fr[grp][ks][r];
-    if (tile + gridDim.x < tiles) fetch(tile + gridDim.x);
     const int y = y0 + warp, yc = min(y, a.H - 1);
     const size_t row = ((size_t)n * a.H + yc) * a.W;
-#pragma unroll
+#pragma unroll 1
     for (int grp = 0; grp < 2; ++grp) {
+      const int xa = min(x0 + grp * 16 + g, a.W - 1), xb = min(x0 + grp * 16 + g + 8, a.W - 1);
+      const uint32_t* fa = reinterpret_cast<const uint32_t*>(a.F + (row + xa) * C);
+      const uint32_t* fb = reinterpret_cast<const uint32_t*>(a.F + (row + xb) * C);
       float acc[4][4];
 #pragma unroll
       for (int nt = 0; nt < 4; ++nt) {
@@ -342,7 +329,7 @@ __global__ void __launch_bounds__(128) kp_head_fwd_tile_kernel(HeadArgs a) {
       }
 #pragma unroll
       for (int ks = 0; ks < KS; ++ks) {
-        const uint32_t a0 = fc[grp][ks][0], a1 = fc[grp][ks][1], a2 = fc[grp][ks][2], a3 = fc[grp][ks][3];
+        const uint32_t a0 = fa[ks * 8 + t], a1 = fb[ks * 8 + t], a2 = fa[ks * 8 + 4 + t], a3 = fb[ks * 8 + 4 + t];
 #pragma unroll
         for (int part = 2; part >= 0; --part)  // smallest parts first
 #pragma unroll
@@ -843,8 +830,12 @@ PBRT_API int pbrt_nn_avgpool2_bwd_add(const float* dy, float* dx, int32_t n, int
 
 PBRT_API int pbrt_nn_relu_bwd(const float* dy, const void* y, void* out, float* db, int64_t pixels, int32_t c,
                               pbrt_stream_t s) {
-  if (!dy || !y || !out || c <= 0) return fail(PBRT_ERROR_INVALID_ARGUMENT, "relu bwd");
-  relu_bwd_kernel<<<grid_for(pixels * c), 256, c * sizeof(float), s>>>(dy, (const bf16*)y, (bf16*)out, db, pixels, c);
+  if (!dy || !y || !out || c <= 0 || c % 8 || kReluBwdThreads % (c / 8) || ((uintptr_t)dy & 15) ||
+      ((uintptr_t)y & 15) || ((uintptr_t)out & 15))
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "relu bwd: channels a multiple of 8 dividing 192 x 8, 16-byte aligned");
+  const long groups = pixels * (c / 8);
+  relu_bwd_kernel<<<grid_for(groups, kReluBwdThreads), kReluBwdThreads, c * sizeof(float), s>>>(
+      dy, (const bf16*)y, (bf16*)out, db, pixels, c);
   return check_launch("relu_bwd");
 }
 
