@@ -59,6 +59,7 @@ def parse():
                     help="neural path, threshold rule: tiles whose predicted relative squared error exceeds this "
                          "show BMFR")
     ap.add_argument("--weights", default=None, help="neural path: .npz of trained parameters (default: packaged)")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-request batch measured after the frames")
     ap.add_argument("--ref-spp", type=int, default=4096, help="samples of the relMSE reference render (0: skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sort-rays", action="store_true", help="sort extension / shadow rays before traversal")
@@ -660,6 +661,12 @@ def run_gb300(args):
             "relmse": quality,
             "bvh": {"nodes": int(info.bvh_nodes), "depth": int(info.bvh_depth), "build_ms": info.build_ms},
         }
+        if world == 1 and not args.no_batch:
+            # the 64-request batch, measured here too (fixed tuning, 3 submits
+            # after 1): BVH queries of requests of 10k-2M triangles each
+            bl = batch64_measure(3, 1, tune=False)
+            line["batch64"] = {k: bl[k] for k in ("ms_per_batch", "requests_per_s", "pixel_samples_per_s",
+                                                  "grays_per_s", "tuning", "steps", "warmup")}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.barrier()
@@ -676,11 +683,21 @@ def batch_scene(rng, seed):
     return S.cornell_spheres(seed=seed, spheres=max(1, int(tris / 20480)), subdiv=5)
 
 
+# the autotuner's pick for the 64-request batch on a GB300 (python bench.py --workload batch64)
+BATCH64_TUNING = dict(branches=16, trace_blocks_per_sm=4, shade_blocks_per_sm=8, order=1)
+
+
 def run_batch(args):
     """64 independent requests (own scene of 10k-2M triangles, resolution
     log-uniform 256^2..1080p, 1/2/4/8/16 spp, depth 4-8, accumulator + BMFR
     each) in one graph launch; the autotuner picks the chain count and the
     tracer's launch shape."""
+    print(json.dumps(batch64_measure(args.steps, args.warmup, tune=True)), flush=True)
+
+
+def batch64_measure(steps, warmup, tune=True):
+    """The 64-request batch timed over `steps` submits after `warmup`; tune:
+    run the autotuner first, else take BATCH64_TUNING. Returns the line."""
     import torch
 
     from vulkanpbrt_gb300 import build as B
@@ -719,30 +736,33 @@ def run_batch(args):
         b.add(r["pipe"], r["pc"], spp=r["spp"], accumulator=r["acc"], bmfr=r["bmfr"], camera=r["cm"])
     stream = torch.cuda.current_stream()
     t1 = time.perf_counter()
-    best, best_ms = b.autotune(repeats=3)
+    if tune:
+        best, best_ms = b.autotune(repeats=3)
+    else:
+        b.set_tuning(**BATCH64_TUNING)
+        best, best_ms = b.tuning, None
     tune_s = time.perf_counter() - t1
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         b.submit()
     torch.cuda.synchronize()
     st0 = [r["pipe"].stats() for r in reqs]
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         b.submit()
     e1.record(stream)
     torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / args.steps
+    ms = e0.elapsed_time(e1) / steps
     st1 = [r["pipe"].stats() for r in reqs]
     rays = sum((a.primary_rays + a.extension_rays + a.shadow_rays) - (z.primary_rays + z.extension_rays + z.shadow_rays)
-               for a, z in zip(st1, st0)) / args.steps
-    line = {"metric": "batched render requests (64 per graph launch)", "value": 1e3 / ms, "unit": "batches/s",
+               for a, z in zip(st1, st0)) / steps
+    return {"metric": "batched render requests (64 per graph launch)", "value": 1e3 / ms, "unit": "batches/s",
             "ms_per_batch": ms, "requests_per_s": 64e3 / ms, "pixel_samples_per_s": pixels_spp / ms * 1e3,
             "grays_per_s": rays / ms / 1e6, "rays_per_batch": rays, "tuning": best, "autotune_best_ms": best_ms,
-            "setup_s": setup_s, "autotune_s": tune_s, "steps": args.steps, "warmup": args.warmup,
+            "setup_s": setup_s, "autotune_s": tune_s, "steps": steps, "warmup": warmup,
             "config": {"requests": 64, "scenes": "own seeded scene each, 10k-2M tris (log-uniform)",
                        "resolution": "log-uniform 256^2..1080p", "spp": "uniform {1,2,4,8,16}", "depth": "4-8",
                        "denoiser": "accumulate + BMFR 32x32 per request"}}
-    print(json.dumps(line), flush=True)
 
 def run_full(args):
     """The full chosen form: 3840x2160, 4 samples per pixel, max depth 8 with
