@@ -826,17 +826,21 @@ def run_full(args):
     img = illu.illumination_images[0].tensor()
     sample_sum = torch.zeros_like(img)
 
+    tr0, tr1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
     def frame(f, stream):
         # the frame's 4 samples are traced and averaged into the illumination
         # buffer, then accumulated once with the frame's own camera motion
         cam, prev = cams[f % args.frames], state["prev"]
         sh_ = vp._abi.stream_handle(stream)
         sample_sum.zero_()
+        tr0.record(stream)
         for s_ in range(spp):
             pc.set(view_inverse=cam.inv_view, proj_inverse=cam.inv_proj, prev_view=prev.view,
                    frame_number=f * spp + s_)
             pipe.trace(pc, stream)
             sample_sum.add_(img)
+        tr1.record(stream)
         img.copy_(sample_sum / spp)
         accu.set_camera_matrices(f, vp.CameraMatrices(cam.view, cam.inv_view, cam.proj, cam.inv_proj),
                                  vp.CameraMatrices(prev.view, prev.inv_view))
@@ -857,8 +861,13 @@ def run_full(args):
     torch.cuda.synchronize()
     measure = {int(x) for x in args.relmse_frames.split(",") if x}
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    st0 = pipe.stats()
-    total_ms, per_frame, fp64_blocks, ratios, fallback = 0.0, [], [], [], []
+    req_pipes = [k[4] for k in keep]
+
+    def queries(pipes):
+        return sum(st.primary_rays + st.extension_rays + st.shadow_rays for st in (q.stats() for q in pipes))
+
+    st0, req0 = queries([pipe]), queries(req_pipes)
+    total_ms, trace_ms, ref_rays, per_frame, fp64_blocks, ratios, fallback = 0.0, 0.0, 0, [], [], [], []
     quality = []
     state["prev"] = cams[0]
     for f in range(args.frames):
@@ -874,21 +883,28 @@ def run_full(args):
         torch.cuda.synchronize()
         ms = ev0.elapsed_time(ev1)
         total_ms += ms
+        trace_ms += tr0.elapsed_time(tr1)
         per_frame.append(ms)
         n, r = bmfr.condition_stats(main_s)
         fp64_blocks.append(n)
         ratios.append(r)
         fallback.append(neural.fallback_tiles(main_s))
-        if f in measure:
+        if f in measure:  # outside the timed region; its reference renders' rays are not counted
+            q0 = queries([pipe])
             quality.append(dict(frame=f, **full_relmse(args, vp, pipe, g, illu, bmfr, neural, pc, pc_den, main_s)))
-    st1 = pipe.stats()
-    rays = (st1.primary_rays - st0.primary_rays) + (st1.extension_rays - st0.extension_rays) + \
-        (st1.shadow_rays - st0.shadow_rays)
+            ref_rays += queries([pipe]) - q0
+    rays = queries([pipe]) - st0 - ref_rays
+    req_rays = queries(req_pipes) - req0
     line = {
         "metric": "4K 4spp denoised frames/s with 16 concurrent 1080p requests", "value": args.frames / (total_ms / 1e3),
         "unit": "fps", "frames": args.frames, "ms_per_step": total_ms / args.frames,
         "ms_per_step_max": max(per_frame), "requests_per_s": 16 * args.frames / (total_ms / 1e3),
-        "grays_per_s_4k": rays / (total_ms / 1e3) / 1e9,
+        # BVH queries (primary + extension + shadow) of the 4K frames over the
+        # 4K tracing time (its launches run beside the requests' stream), and
+        # of the whole step (4K frames and requests) over the step time
+        "grays_per_s_4k": rays / (trace_ms / 1e3) / 1e9,
+        "grays_per_s_step": (rays + req_rays) / (total_ms / 1e3) / 1e9,
+        "trace_ms_4k_per_frame": trace_ms / args.frames,
         "config": {"workload": "full chosen form", "width": W, "height": H, "spp": spp, "max_depth": args.max_depth,
                    "min_depth": args.min_depth, "triangles": int(info.triangle_count), "lights": int(info.light_count),
                    "instances": int(info.instance_count),

@@ -960,20 +960,23 @@ __global__ void __launch_bounds__(kWsThreads, kF8 ? 3 : 0) conv3x3_umma_ws_kerne
 }
 
 // Backward weights on tcgen05: dW[co][tap][ci] += sum over pixels p of
-// dY[p][co] * X(p shifted by the tap)[ci], one CTA a (pixel run, tap). The
-// GEMM has M = 128 output channels (rows past cout are zeros), N = cin and
-// K = pixels, 64 a stage. Both operands sit in shared memory exactly as they
-// are stored in global memory -- each pixel's channels contiguous -- which is
-// the MN-major no-swizzle layout: a core matrix is 8 pixels (K) x 8
-// channels (16 bytes, M or N), core matrices of consecutive pixel groups
-// 128 bytes apart (the K stride) and of consecutive channel groups 1024
-// bytes apart (the M/N stride). So every 16-byte cp.async lands in place.
-// Thread 0 issues four K = 16 MMAs a stage and commits them to the stage's
-// mbarrier; the next loads into that stage wait for it. The FP32
-// accumulator (TMEM lane = co, column = ci) is added into dW with atomics.
-// Every wait is bounded: on a timeout the kernel records the error
+// dY[p][co] * X(p shifted by the tap)[ci]. A CTA walks 8x8-pixel tiles of
+// the images (grid-stride) for a group of taps, the sums of the whole walk
+// in tensor memory: per tile and tap a GEMM with M = 128 output channels
+// (rows past cout are zeros), N = cin and K = the tile's 64 pixels, four
+// K = 16 MMAs. Both operands sit in shared memory as they are stored in
+// global memory -- each pixel's channels contiguous -- which is the MN-major
+// no-swizzle layout: a core matrix is 8 pixels (K) x 8 channels (16 bytes).
+// dY's tile: pixel rows 128 bytes apart (the K stride), channel groups 1 KB
+// apart. X's 10x10-pixel halo of the tile: halo rows 160 bytes apart, channel
+// groups 1600 bytes apart; the tap (dy, dx) is the same descriptor with its
+// start moved by dy halo rows and dx pixels -- no copy per tap. Thread 0
+// issues the MMAs and commits them to the stage's mbarrier; the loads of a
+// stage wait for the MMAs that read it (two tiles ahead, 4 stages). Every
+// wait is bounded: on a timeout the kernel records the error
 // (pbrt_nn_umma_status), waits again for its own MMAs and frees its tensor
-// memory.
+// memory. The accumulators (TMEM lane = co, column = tap x cin + ci) are
+// added into dW with atomics once, at the end of the walk.
 struct UmmaWgradArgs {
   const bf16* dy;  // [N][H][W][cout]
   const bf16* x1;  // [N][H][W][c1]
@@ -981,12 +984,19 @@ struct UmmaWgradArgs {
   int c1, c2;
   float* dw;  // [cout][9][c1 + c2]
   int N, H, W, cout;
-  int pix_per_cta;
+  int ntaps;   // taps a CTA: blockIdx.x * ntaps .. + ntaps - 1
+  int stages;  // 3 or 4 input stages
 };
-constexpr int kWgK = 64;                     // pixels a stage
-constexpr int kWgStages = 4;
-constexpr int kWgABytes = 16 * 8 * 128;      // 128 rows x 64 pixels
-__host__ __device__ constexpr int wgrad_stage_bytes(int cin) { return kWgABytes + (cin / 8) * 8 * 128; }
+constexpr int kWgT = 8, kWgHalo = kWgT + 2;  // 8x8-pixel tile, 10x10 halo
+constexpr int kWgStages = 4;                 // at most
+constexpr int kWgABytes = 16 * 64 * 16;                       // 128 rows (16 groups) x 64 pixels
+constexpr int kWgBGroup = kWgHalo * kWgHalo * 16;             // one 8-channel group of the halo: 1600 B
+__host__ __device__ constexpr int wgrad_stage_bytes(int cin) {
+  return kWgABytes + (((cin / 8) * kWgBGroup + 127) & ~127);
+}
+__host__ __device__ constexpr uint32_t wgrad_cols(int cols) {
+  return cols <= 32 ? 32u : (cols <= 64 ? 64u : (cols <= 128 ? 128u : (cols <= 256 ? 256u : 512u)));
+}
 
 __global__ void __launch_bounds__(128) conv3x3_wgrad_umma_kernel(UmmaWgradArgs a) {
   extern __shared__ __align__(1024) uint8_t smem[];
@@ -994,20 +1004,18 @@ __global__ void __launch_bounds__(128) conv3x3_wgrad_umma_kernel(UmmaWgradArgs a
   __shared__ uint32_t tmem_base_slot;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int cin = a.c1 + a.c2;
-  // blockIdx.x: tap (consecutive CTAs read the same pixel run: L2 reuse
-  // across the taps), blockIdx.y: pixel run
-  const int tap = blockIdx.x, dy = tap / 3 - 1, dx = tap % 3 - 1;
-  const long P = (long)a.N * a.H * a.W;
-  const long p_begin = (long)blockIdx.y * a.pix_per_cta;
-  const long p_end = p_begin + a.pix_per_cta < P ? p_begin + a.pix_per_cta : P;
-  const int n_it = p_begin < p_end ? (int)((p_end - p_begin + kWgK - 1) / kWgK) : 0;
+  const int tap0 = blockIdx.x * a.ntaps;
+  const int tiles_x = (a.W + kWgT - 1) / kWgT, tiles_y = (a.H + kWgT - 1) / kWgT;
+  const long tiles = (long)tiles_x * tiles_y * a.N;
+  const int n_it = blockIdx.y < tiles ? (int)((tiles - 1 - blockIdx.y) / gridDim.y + 1) : 0;
   const int H2 = a.H >> 1, W2 = a.W >> 1;
-  const uint32_t cols = cin <= 32 ? 32u : (cin <= 64 ? 64u : (cin <= 128 ? 128u : 256u));
+  const uint32_t cols = wgrad_cols(a.ntaps * cin);
+  const int S = a.stages;
   const int stage_bytes = wgrad_stage_bytes(cin);
   const uint32_t sbase = (umma::smem_addr(smem) + 1023u) & ~1023u;
   auto mb = [&](int st) { return umma::smem_addr(&mbar[st]); };
   if (tid == 0) {
-    for (int st = 0; st < kWgStages; ++st) umma::mbar_init(mb(st), 1);
+    for (int st = 0; st < S; ++st) umma::mbar_init(mb(st), 1);
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   if (warp == 0) {
@@ -1017,7 +1025,7 @@ __global__ void __launch_bounds__(128) conv3x3_wgrad_umma_kernel(UmmaWgradArgs a
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
   }
   // the A rows past cout stay zero in every stage
-  for (int st = 0; st < kWgStages; ++st)
+  for (int st = 0; st < S; ++st)
     for (int i = tid * 16 + (a.cout / 8) * 1024; i < kWgABytes; i += 128 * 16)
       asm volatile("st.shared.v4.b32 [%0], {%1, %1, %1, %1};\n" ::"r"(sbase + st * stage_bytes + i), "r"(0)
                    : "memory");
@@ -1026,38 +1034,41 @@ __global__ void __launch_bounds__(128) conv3x3_wgrad_umma_kernel(UmmaWgradArgs a
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   const uint32_t tmem = tmem_base_slot;
 
-  // a stage: thread tid copies pixel tid % 64 of the run, channel groups
-  // tid / 64, + 2, ...: the pixel's coordinates once per stage
+  // stage st <- tile number it of this CTA: dY's 64 pixels (zeros outside
+  // the image) and X's 100 halo pixels (zeros outside: the padding)
   auto load = [&](int st, int it) {
     const uint32_t ab = sbase + st * stage_bytes, bb = ab + kWgABytes;
+    const long t = blockIdx.y + (long)it * gridDim.y;
+    const int img = (int)(t / ((long)tiles_x * tiles_y));
+    const int rem = (int)(t - (long)img * tiles_x * tiles_y);
+    const int x0 = (rem % tiles_x) * kWgT, y0 = (rem / tiles_x) * kWgT;
     const int ga = a.cout / 8, gb = cin / 8;
-    const int pl = tid % kWgK;
-    const long p = p_begin + (long)it * kWgK + pl;
-    const bool pv = p < p_end;
-    const long pp = pv ? p : 0;
-    const int n = (int)(pp / ((long)a.H * a.W));
-    const int rem = (int)(pp - (long)n * a.H * a.W);
-    const int yy = rem / a.W + dy, xx = rem % a.W + dx;
-    const bool inb = pv && yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
-    const bf16* px1 = inb ? a.x1 + (((size_t)n * a.H + yy) * a.W + xx) * a.c1 : a.x1;
-    const bf16* px2 = inb && a.c2 ? a.x2 + (((size_t)n * H2 + (yy >> 1)) * W2 + (xx >> 1)) * a.c2 : a.x1;
-    const bf16* pdy = a.dy + pp * a.cout;
-    const uint32_t off = (uint32_t)((pl >> 3) * 128 + (pl & 7) * 16);
-    for (int g = tid / kWgK; g < ga + gb; g += 128 / kWgK) {
-      if (g < ga) {
-        umma::cp16(ab + g * 1024 + off, pdy + g * 8, pv);
-      } else {
-        const int ci = (g - ga) * 8;
-        umma::cp16(bb + (g - ga) * 1024 + off, ci < a.c1 ? px1 + ci : px2 + (ci - a.c1), inb);
+    for (int q = tid; q < 64 * ga; q += 128) {
+      const int pl = q & 63, g = q >> 6;
+      const int yy = y0 + (pl >> 3), xx = x0 + (pl & 7);
+      const bool ok = yy < a.H && xx < a.W;
+      const bf16* src = ok ? a.dy + (((size_t)img * a.H + yy) * a.W + xx) * a.cout + g * 8 : a.dy;
+      umma::cp16(ab + g * 1024 + pl * 16, src, ok);
+    }
+    for (int q = tid; q < kWgHalo * kWgHalo * gb; q += 128) {
+      const int hp = q % (kWgHalo * kWgHalo), g = q / (kWgHalo * kWgHalo);
+      const int yy = y0 - 1 + hp / kWgHalo, xx = x0 - 1 + hp % kWgHalo;
+      const int ci = g * 8;
+      const bool ok = yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
+      const bf16* src = a.x1;
+      if (ok) {
+        if (ci < a.c1) src = a.x1 + (((size_t)img * a.H + yy) * a.W + xx) * a.c1 + ci;
+        else src = a.x2 + (((size_t)img * H2 + (yy >> 1)) * W2 + (xx >> 1)) * a.c2 + (ci - a.c1);
       }
+      umma::cp16(bb + g * kWgBGroup + hp * 16, src, ok);
     }
   };
 
   bool failed = false;
-  int issued = 0;  // iterations whose MMAs were issued (the same count in every thread)
-  // loads run kWgAhead iterations ahead; a refill waits for the MMAs of the
-  // iteration kWgStages back, issued kWgStages - kWgAhead iterations earlier
-  constexpr int kWgAhead = kWgStages - 2;
+  int issued = 0;  // tiles whose MMAs were issued (the same count in every thread)
+  // loads run two tiles ahead; a refill waits for the MMAs of the tile S
+  // back, issued S - 2 tiles earlier
+  constexpr int kWgAhead = 2;
   for (int j = 0; j < kWgAhead; ++j) {
     if (j < n_it) load(j, j);
     asm volatile("cp.async.commit_group;\n" ::);
@@ -1066,17 +1077,17 @@ __global__ void __launch_bounds__(128) conv3x3_wgrad_umma_kernel(UmmaWgradArgs a
   const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) | ((uint32_t)(cin >> 3) << 17) |
                          ((uint32_t)(128 >> 4) << 24);
   for (int it = 0; it < n_it && !failed; ++it) {
-    const int st = it % kWgStages;
-    const int j = it + kWgAhead;  // refill the stage iteration j - kWgStages read
+    const int st = it % S;
+    const int j = it + kWgAhead;  // refill the stage tile j - S read
     if (j < n_it) {
       bool ok = true;
-      const int prev = j - kWgStages;
-      if (prev >= 0) ok = umma::mbar_wait(mb(prev % kWgStages), (uint32_t)((prev / kWgStages) & 1));
+      const int prev = j - S;
+      if (prev >= 0) ok = umma::mbar_wait(mb(prev % S), (uint32_t)((prev / S) & 1));
       if (__syncthreads_or(!ok)) {
         failed = true;
         break;
       }
-      load(j % kWgStages, j);
+      load(j % S, j);
     }
     asm volatile("cp.async.commit_group;\n" ::);
     asm volatile("cp.async.wait_group %0;\n" ::"n"(kWgAhead));
@@ -1085,17 +1096,20 @@ __global__ void __launch_bounds__(128) conv3x3_wgrad_umma_kernel(UmmaWgradArgs a
     if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
       const uint32_t ab = sbase + st * stage_bytes, bb = ab + kWgABytes;
+      for (int tl = 0; tl < a.ntaps; ++tl) {
+        const int tap = tap0 + tl, dy = tap / 3, dx = tap % 3;
+        const uint32_t d = tmem + (uint32_t)(tl * cin);
 #pragma unroll
-      for (int ks = 0; ks < kWgK / 16; ++ks) {
-        // K step of 16 pixels = two core-matrix columns, 128 bytes each
-        const uint64_t da = umma::sdesc(ab + ks * 256, 128, 1024);
-        const uint64_t db = umma::sdesc(bb + ks * 256, 128, 1024);
-        const uint32_t acc = (it > 0 || ks > 0) ? 1u : 0u;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "setp.ne.b32 p, %4, 0;\n\t"
-            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
-            "l"(da), "l"(db), "r"(idesc), "r"(acc));
+        for (int ks = 0; ks < 4; ++ks) {  // K = 16: tile rows 2ks, 2ks + 1
+          const uint64_t da = umma::sdesc(ab + ks * 256, 128, 1024);
+          const uint64_t db = umma::sdesc(bb + ((2 * ks + dy) * kWgHalo + dx) * 16, kWgHalo * 16, kWgBGroup);
+          const uint32_t acc = (it > 0 || ks > 0) ? 1u : 0u;
+          asm volatile(
+              "{\n\t.reg .pred p;\n\t"
+              "setp.ne.b32 p, %4, 0;\n\t"
+              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+              "l"(da), "l"(db), "r"(idesc), "r"(acc));
+        }
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mb(st))
                    : "memory");
@@ -1110,29 +1124,31 @@ __global__ void __launch_bounds__(128) conv3x3_wgrad_umma_kernel(UmmaWgradArgs a
     const int last = issued - 1;
     bool done = true;
     if (last >= 0) {
-      done = umma::mbar_wait(mb(last % kWgStages), (uint32_t)((last / kWgStages) & 1));
-      if (!done) done = umma::mbar_wait(mb(last % kWgStages), (uint32_t)((last / kWgStages) & 1));
+      done = umma::mbar_wait(mb(last % S), (uint32_t)((last / S) & 1));
+      if (!done) done = umma::mbar_wait(mb(last % S), (uint32_t)((last / S) & 1));
     }
     failed = __syncthreads_or(failed || !done);
     if (failed) {
       if (tid == 0) atomicOr(&g_umma_error, 1u);
-    } else {
+    } else if (issued > 0) {
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
       const int co = warp * 32 + lane;  // TMEM lane
-      float* drow = a.dw + ((size_t)(co < a.cout ? co : 0) * 9 + tap) * cin;
-      for (int c0 = 0; c0 < cin; c0 += 16) {
-        uint32_t v[16];
-        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-            "[%16];\n"
-            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-            : "r"(taddr));
-        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-        if (co < a.cout) {
+      for (int tl = 0; tl < a.ntaps; ++tl) {
+        float* drow = a.dw + ((size_t)(co < a.cout ? co : 0) * 9 + tap0 + tl) * cin;
+        for (int c0 = 0; c0 < cin; c0 += 16) {
+          uint32_t v[16];
+          const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(tl * cin + c0);
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+              "[%16];\n"
+              : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+              : "r"(taddr));
+          asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+          if (co < a.cout) {
 #pragma unroll
-          for (int k = 0; k < 16; ++k) atomicAdd(drow + c0 + k, __uint_as_float(v[k]));
+            for (int k = 0; k < 16; ++k) atomicAdd(drow + c0 + k, __uint_as_float(v[k]));
+          }
         }
       }
     }
@@ -1459,11 +1475,16 @@ PBRT_API int pbrt_nn_conv3x3_wgrad_umma(const void* dy, const void* x1, int32_t 
     return fail(PBRT_ERROR_INVALID_ARGUMENT, "nn conv3x3 wgrad umma: bad arguments (c1 %d, c2 %d, cout %d)", c1, c2,
                 cout);
   const int cin = c1 + c2;
-  const size_t smem = (size_t)kWgStages * wgrad_stage_bytes(cin) + 1024;
+  // taps a CTA: all nine while their accumulators fit in tensor memory, else three, else one
+  const int ntaps = 9 * cin <= 512 ? 9 : (3 * cin <= 512 ? 3 : 1);
+  const int cols = (int)wgrad_cols(ntaps * cin);
+  constexpr size_t kMaxSmem = 227 * 1024;
+  const int stages = (size_t)kWgStages * wgrad_stage_bytes(cin) + 1024 <= kMaxSmem ? kWgStages : 3;
+  const size_t smem = (size_t)stages * wgrad_stage_bytes(cin) + 1024;
   static PerDeviceOnce attrs;
   int ast = once_per_device(attrs, [&]() -> int {
     cudaError_t e = cudaFuncSetAttribute(conv3x3_wgrad_umma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(kWgStages * wgrad_stage_bytes(256) + 1024));
+                                         (int)kMaxSmem);
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(conv3x3_wgrad_umma_kernel)");
     return PBRT_OK;
   });
@@ -1471,14 +1492,14 @@ PBRT_API int pbrt_nn_conv3x3_wgrad_umma(const void* dy, const void* x1, int32_t 
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int per_sm = std::max(1, (int)((227 * 1024) / (smem + 1024)));
-  const long P = (long)n * h * wd;
-  // two waves of CTAs over the nine taps; pixel runs of whole stages
-  long chunks = std::max(1L, std::min((2L * sms * per_sm + 8) / 9, (P + kWgK - 1) / kWgK));
-  long ppc = (P + chunks - 1) / chunks;
-  ppc = (ppc + kWgK - 1) / kWgK * kWgK;
-  UmmaWgradArgs a{(const bf16*)dy, (const bf16*)x1, (const bf16*)x2, c1, c2, dw, n, h, wd, cout, (int)ppc};
-  dim3 grid(9, (unsigned)((P + ppc - 1) / ppc));
+  // resident CTAs an SM: shared memory and the 512 tensor-memory columns
+  const int per_sm = std::max(1, std::min((int)((227 * 1024) / (smem + 1024)), 512 / cols));
+  const long tiles = (long)n * ((h + kWgT - 1) / kWgT) * ((wd + kWgT - 1) / kWgT);
+  const int groups = 9 / ntaps;
+  // one wave: each CTA walks its share of the tiles for its taps
+  const long per_group = std::max(1L, std::min(tiles, (long)sms * per_sm / groups));
+  UmmaWgradArgs a{(const bf16*)dy, (const bf16*)x1, (const bf16*)x2, c1, c2, dw, n, h, wd, cout, ntaps, stages};
+  dim3 grid((unsigned)groups, (unsigned)per_group);
   conv3x3_wgrad_umma_kernel<<<grid, 128, smem, stream>>>(a);
   return check_launch("conv3x3_wgrad_umma_kernel");
 }

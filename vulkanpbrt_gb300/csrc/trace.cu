@@ -657,9 +657,10 @@ struct QueryIO {
   uint32_t* errflag;
 };
 
-// Traversal CTAs resident per SM the register allocation targets (8 x 128
-// threads at <= 64 registers).
-constexpr int kTraverseMinBlocks = 8;
+// Traversal CTAs resident per SM the register allocation targets (7 x 128
+// threads at <= 72 registers; 1080p tracer 5.66 -> 5.55 ms against 8 CTAs
+// at 64 registers; 6 CTAs: 5.60 ms).
+constexpr int kTraverseMinBlocks = 7;
 template <int MODE>
 __global__ void __launch_bounds__(128, kTraverseMinBlocks) k_traverse(SceneView sc, Queues q, Counters* c, int k,
                                                                     QueryIO io) {
@@ -1909,7 +1910,7 @@ PBRT_API int pbrt_pipeline_create(PbrtScene* scene, PbrtGBuffer* g, PbrtIllumina
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    pp->grid_persistent = sms * 8;  // 8 resident 128-thread CTAs per SM at <= 64 registers
+    pp->grid_persistent = sms * kTraverseMinBlocks;  // the resident 128-thread traversal CTAs
     pp->grid_shade = sms * 8;
   }
   if (st) {
