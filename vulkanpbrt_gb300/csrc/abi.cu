@@ -22,6 +22,9 @@ int fail(int status, const char* fmt, ...) {
 }
 
 int cuda_fail(cudaError_t e, const char* what) {
+  // a failed call leaves its error as the runtime's last error; take it off
+  // so that the next launch check reports its own (a sticky error stays)
+  cudaGetLastError();
   int st = (e == cudaErrorMemoryAllocation) ? PBRT_ERROR_OUT_OF_MEMORY : PBRT_ERROR_CUDA;
   return fail(st, "%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
 }

@@ -1478,7 +1478,7 @@ PBRT_API int pbrt_nn_conv3x3_wgrad_umma(const void* dy, const void* x1, int32_t 
   // taps a CTA: all nine while their accumulators fit in tensor memory, else three, else one
   const int ntaps = 9 * cin <= 512 ? 9 : (3 * cin <= 512 ? 3 : 1);
   const int cols = (int)wgrad_cols(ntaps * cin);
-  constexpr size_t kMaxSmem = 227 * 1024;
+  constexpr size_t kMaxSmem = 210 * 1024;  // below the opt-in limit less the kernel's static shared memory
   const int stages = (size_t)kWgStages * wgrad_stage_bytes(cin) + 1024 <= kMaxSmem ? kWgStages : 3;
   const size_t smem = (size_t)stages * wgrad_stage_bytes(cin) + 1024;
   static PerDeviceOnce attrs;
