@@ -166,7 +166,7 @@ SPP_CHOICES = (1, 1, 2, 4, 8, 16)  # samples averaged into one network input (1 
 
 
 def train(net, data, steps, batch=16, lr=1e-4, seed=0, log_every=100, var_weight=0.1, log=print,
-          lr_floor=0.1, kernel="mma", checkpoint=None, checkpoint_every=0):
+          lr_floor=0.1, kernel="umma", checkpoint=None, checkpoint_every=0):
     """Adam steps over random crops; each input is the mean of k of the
     crop's one-sample frames (k from SPP_CHOICES, with the matching samples-
     per-pixel channel, as the Accumulator's output carries it) -- so one
@@ -233,8 +233,8 @@ def main(argv=None):
     ap.add_argument("--texture-size", type=int, default=256)
     ap.add_argument("--instances", type=int, default=2000)
     ap.add_argument("--init", default=None, help="start from these weights")
-    ap.add_argument("--kernel", default="mma", choices=["mma", "umma"],
-                    help="convolutions (forward and backward) on mma.sync or tcgen05")
+    ap.add_argument("--kernel", default="umma", choices=["mma", "umma"],
+                    help="convolutions (forward and backward) on tcgen05 (default) or mma.sync")
     ap.add_argument("--out", required=True)
     ap.add_argument("--checkpoint-every", type=int, default=0, help="also save the weights to --out every N steps")
     ap.add_argument("--log", default=None)
