@@ -602,13 +602,10 @@ __global__ void k_shadow_consumed(Counters* c) {
 // Primary rays enter the queue in 8x4-pixel tiles when the frame divides
 // into them: the 32 rays a packet-traversal warp takes then cover a compact
 // patch of the image (a smaller union of nodes than a 32-pixel row).
-#ifndef PBRT_TILE_RAYGEN
-#define PBRT_TILE_RAYGEN 1
-#endif
 __global__ void k_raygen(const FrameParams* __restrict__ fpp, Queues q) {
   const FrameParams& fp = *fpp;
   const int N = fp.W * fp.H;
-  const bool tiled = PBRT_TILE_RAYGEN && fp.W % 8 == 0 && fp.H % 4 == 0;
+  const bool tiled = fp.W % 8 == 0 && fp.H % 4 == 0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
     int x, y;
     if (tiled) {
@@ -1197,20 +1194,17 @@ __global__ void k_sort_scatter(const uint32_t* __restrict__ count_ptr, Queues q,
   }
 }
 
-// Shading CTAs resident per SM the register allocation targets (a build
-// knob: more CTAs, fewer registers per thread). Measured at 1080p: 8 (64
-// registers, a few spills) 1.58 ms per frame; 4-5 (unbounded, ~110
-// registers) 1.90; 6 1.96; 10 1.79; 12 1.95; 16 2.38.
-#ifndef PBRT_SHADE_MIN_BLOCKS
-#define PBRT_SHADE_MIN_BLOCKS 8
-#endif
-#define PBRT_SHADE_BOUNDS __launch_bounds__(128, PBRT_SHADE_MIN_BLOCKS)
+// Shading CTAs resident per SM the register allocation targets (more CTAs,
+// fewer registers per thread). Measured at 1080p: 8 (64 registers, a few
+// spills) 1.52 ms per frame; 7 1.53; 6 1.56; 5 1.59; 4 (unbounded, ~110
+// registers) 1.90; 10 1.79; 12 1.95; 16 2.38.
+constexpr int kShadeMinBlocks = 8;
 // LM: the light-sampling mode (FrameParams::light_mode) and FIRST: the
 // primary bounce, both fixed per instantiation so each launch carries only
 // the code of its own mode and bounce (a smaller loop body: fewer
 // instruction-fetch stalls).
 template <int LM, bool FIRST>
-__global__ void PBRT_SHADE_BOUNDS k_shade(SceneView sc, const FrameParams* __restrict__ fpp, Queues q,
+__global__ void __launch_bounds__(128, kShadeMinBlocks) k_shade(SceneView sc, const FrameParams* __restrict__ fpp, Queues q,
                                                Counters* c, GBufferOut g, int k) {
   const FrameParams& fp = *fpp;
   if (*((volatile uint32_t*)&c->stop)) return;  // stopped frame: shade nothing, queue nothing
@@ -1911,7 +1905,7 @@ PBRT_API int pbrt_pipeline_create(PbrtScene* scene, PbrtGBuffer* g, PbrtIllumina
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     pp->grid_persistent = sms * kTraverseMinBlocks;  // the resident 128-thread traversal CTAs
-    pp->grid_shade = sms * 8;
+    pp->grid_shade = sms * kShadeMinBlocks;
   }
   if (st) {
     delete pp;
