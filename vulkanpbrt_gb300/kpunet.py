@@ -301,39 +301,63 @@ class Workspace:
 
 
 def main(argv=None):
-    """Times the network's forward pass (and its layers) on random inputs:
-    python -m vulkanpbrt_gb300.kpunet [--height 1088 --width 1920 --iters 10]."""
+    """Times the network's forward pass on random inputs:
+    python -m vulkanpbrt_gb300.kpunet [--height 1088 --width 1920 --iters 10];
+    with --train, Adam training steps instead (random inputs and targets,
+    default batch 16 of 256x256, the training kernels)."""
     import argparse
     import json
 
     import torch
 
-    ap = argparse.ArgumentParser(description="time the kernel-predicting U-Net forward pass")
-    ap.add_argument("--height", type=int, default=1088)
-    ap.add_argument("--width", type=int, default=1920)
-    ap.add_argument("--batch", type=int, default=1)
+    ap = argparse.ArgumentParser(description="time the kernel-predicting U-Net forward pass or training step")
+    ap.add_argument("--height", type=int, default=None, help="default 1088 (forward), 256 (--train)")
+    ap.add_argument("--width", type=int, default=None, help="default 1920 (forward), 256 (--train)")
+    ap.add_argument("--batch", type=int, default=None, help="default 1 (forward), 16 (--train)")
     ap.add_argument("--iters", type=int, default=10)
     ap.add_argument("--kernel", default="mma", choices=["mma", "umma"], help="convolutions: mma.sync or tcgen05")
+    ap.add_argument("--train", action="store_true", help="time training steps (forward, loss, backward, Adam)")
     a = ap.parse_args(argv)
+    h = a.height or (256 if a.train else 1088)
+    w = a.width or (256 if a.train else 1920)
+    n = a.batch or (16 if a.train else 1)
     from . import build
 
     build.build()
     dev = torch.device("cuda", 0)
     net = KPUNet(dev, seed=0)
-    ws = net.workspace(a.batch, a.height, a.width, training=False)
+    ws = net.workspace(n, h, w, training=a.train)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if a.train:
+        g = torch.Generator(device=dev).manual_seed(0)
+        illum = torch.rand(n, h, w, 4, device=dev, generator=g) ** 3 * 6
+        albedo = torch.randint(20, 256, (n, h, w, 4), device=dev, generator=g, dtype=torch.uint8)
+        normal = torch.rand(n, h, w, 2, device=dev, generator=g) * 3
+        depth = torch.rand(n, h, w, device=dev, generator=g) * 30
+        target = illum[..., :3].contiguous()
+        ws.set_input(illum, albedo, normal, depth)
+        ws.train_step(target, albedo, kernel=a.kernel)  # warm-up
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(a.iters):
+            ws.train_step(target, albedo, kernel=a.kernel)
+        e1.record()
+        torch.cuda.synchronize()
+        print(json.dumps({"train_step_ms": e0.elapsed_time(e1) / a.iters, "batch": n, "height": h, "width": w,
+                          "kernel": a.kernel}))
+        return
     ws.feat.normal_()
     ws.rad[0].uniform_()
     ws.forward(a.kernel)  # warm-up
     torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(a.iters):
         ws.forward(a.kernel)
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / a.iters
-    flop = sum(2 * 9 * (c1 + c2) * co * (a.height >> l) * (a.width >> l) for _, (c1, c2), co, l in CONVS) * a.batch
-    print(json.dumps({"forward_ms": ms, "conv_tflops_per_s": flop / ms / 1e9, "pixels": a.height * a.width * a.batch}))
+    flop = sum(2 * 9 * (c1 + c2) * co * (h >> l) * (w >> l) for _, (c1, c2), co, l in CONVS) * n
+    print(json.dumps({"forward_ms": ms, "conv_tflops_per_s": flop / ms / 1e9, "pixels": h * w * n}))
 
 
 if __name__ == "__main__":
