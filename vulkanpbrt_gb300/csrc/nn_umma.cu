@@ -1475,11 +1475,15 @@ PBRT_API int pbrt_nn_conv3x3_wgrad_umma(const void* dy, const void* x1, int32_t 
     return fail(PBRT_ERROR_INVALID_ARGUMENT, "nn conv3x3 wgrad umma: bad arguments (c1 %d, c2 %d, cout %d)", c1, c2,
                 cout);
   const int cin = c1 + c2;
-  // taps a CTA: all nine while their accumulators fit in tensor memory, else three, else one
-  const int ntaps = 9 * cin <= 512 ? 9 : (3 * cin <= 512 ? 3 : 1);
+  // taps a CTA: three while their accumulators take at most half the
+  // tensor memory, else one; three stages. Two or three CTAs an SM on the
+  // full- and half-resolution layers (one CTA of all nine taps, 512
+  // columns and four stages, left the SM's issue slots 88 % idle: d0b
+  // 310 us, d0a 808 us at 16 x 256^2)
+  const int ntaps = wgrad_cols(3 * cin) <= 256 ? 3 : 1;
   const int cols = (int)wgrad_cols(ntaps * cin);
   constexpr size_t kMaxSmem = 210 * 1024;  // below the opt-in limit less the kernel's static shared memory
-  const int stages = (size_t)kWgStages * wgrad_stage_bytes(cin) + 1024 <= kMaxSmem ? kWgStages : 3;
+  const int stages = 3;
   const size_t smem = (size_t)stages * wgrad_stage_bytes(cin) + 1024;
   static PerDeviceOnce attrs;
   int ast = once_per_device(attrs, [&]() -> int {
