@@ -998,9 +998,13 @@ __host__ __device__ constexpr uint32_t wgrad_cols(int cols) {
   return cols <= 32 ? 32u : (cols <= 64 ? 64u : (cols <= 128 ? 128u : (cols <= 256 ? 256u : 512u)));
 }
 
-__global__ void __launch_bounds__(128) conv3x3_wgrad_umma_kernel(UmmaWgradArgs a) {
+__global__ void __launch_bounds__(128) conv3x3_wgrad_umma_kernel(UmmaWgradArgs a,
+                                                                 const __grid_constant__ CUtensorMap dymap,
+                                                                 const __grid_constant__ CUtensorMap x1map,
+                                                                 int use_tma) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t mbar[kWgStages];
+  __shared__ __align__(8) uint64_t tbar[kWgStages];  // the TMA loads' arrival per stage
   __shared__ uint32_t tmem_base_slot;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int cin = a.c1 + a.c2;
@@ -1014,8 +1018,12 @@ __global__ void __launch_bounds__(128) conv3x3_wgrad_umma_kernel(UmmaWgradArgs a
   const int stage_bytes = wgrad_stage_bytes(cin);
   const uint32_t sbase = (umma::smem_addr(smem) + 1023u) & ~1023u;
   auto mb = [&](int st) { return umma::smem_addr(&mbar[st]); };
+  auto tb = [&](int st) { return umma::smem_addr(&tbar[st]); };
   if (tid == 0) {
-    for (int st = 0; st < S; ++st) umma::mbar_init(mb(st), 1);
+    for (int st = 0; st < S; ++st) {
+      umma::mbar_init(mb(st), 1);
+      umma::mbar_init(tb(st), 1);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   if (warp == 0) {
@@ -1035,7 +1043,12 @@ __global__ void __launch_bounds__(128) conv3x3_wgrad_umma_kernel(UmmaWgradArgs a
   const uint32_t tmem = tmem_base_slot;
 
   // stage st <- tile number it of this CTA: dY's 64 pixels (zeros outside
-  // the image) and X's 100 halo pixels (zeros outside: the padding)
+  // the image) and X's 100 halo pixels (zeros outside: the padding). With
+  // use_tma, dY's tile and x1's halo come in two TMA tile loads issued by
+  // thread 0 (5-D maps [8 channels][x][y][channel group][image], whose
+  // boxes land in exactly the operand layout), the upsampled x2 part by
+  // cp.async gathers of all threads.
+  const int gb1 = use_tma ? a.c1 / 8 : 0;  // halo channel groups the TMA loads
   auto load = [&](int st, int it) {
     const uint32_t ab = sbase + st * stage_bytes, bb = ab + kWgABytes;
     const long t = blockIdx.y + (long)it * gridDim.y;
@@ -1043,6 +1056,31 @@ __global__ void __launch_bounds__(128) conv3x3_wgrad_umma_kernel(UmmaWgradArgs a
     const int rem = (int)(t - (long)img * tiles_x * tiles_y);
     const int x0 = (rem % tiles_x) * kWgT, y0 = (rem / tiles_x) * kWgT;
     const int ga = a.cout / 8, gb = cin / 8;
+    if (use_tma) {
+      if (tid == 0) {
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(tb(st)),
+                     "r"((uint32_t)(ga * 1024 + gb1 * kWgBGroup))
+                     : "memory");
+        asm volatile(
+            "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+            "%5, %6}], [%7];\n" ::"r"(ab),
+            "l"(reinterpret_cast<uint64_t>(&dymap)), "r"(0), "r"(x0), "r"(y0), "r"(0), "r"(img), "r"(tb(st))
+            : "memory");
+        asm volatile(
+            "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+            "%5, %6}], [%7];\n" ::"r"(bb),
+            "l"(reinterpret_cast<uint64_t>(&x1map)), "r"(0), "r"(x0 - 1), "r"(y0 - 1), "r"(0), "r"(img), "r"(tb(st))
+            : "memory");
+      }
+      for (int q = tid; q < kWgHalo * kWgHalo * (gb - gb1); q += 128) {
+        const int hp = q % (kWgHalo * kWgHalo), g = gb1 + q / (kWgHalo * kWgHalo);
+        const int yy = y0 - 1 + hp / kWgHalo, xx = x0 - 1 + hp % kWgHalo;
+        const bool ok = yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
+        const bf16* src = ok ? a.x2 + (((size_t)img * H2 + (yy >> 1)) * W2 + (xx >> 1)) * a.c2 + (g * 8 - a.c1) : a.x1;
+        umma::cp16(bb + g * kWgBGroup + hp * 16, src, ok);
+      }
+      return;
+    }
     for (int q = tid; q < 64 * ga; q += 128) {
       const int pl = q & 63, g = q >> 6;
       const int yy = y0 + (pl >> 3), xx = x0 + (pl & 7);
@@ -1066,11 +1104,15 @@ __global__ void __launch_bounds__(128) conv3x3_wgrad_umma_kernel(UmmaWgradArgs a
 
   bool failed = false;
   int issued = 0;  // tiles whose MMAs were issued (the same count in every thread)
+  int loaded = 0;  // tiles whose loads were issued
   // loads run two tiles ahead; a refill waits for the MMAs of the tile S
   // back, issued S - 2 tiles earlier
   constexpr int kWgAhead = 2;
   for (int j = 0; j < kWgAhead; ++j) {
-    if (j < n_it) load(j, j);
+    if (j < n_it) {
+      load(j, j);
+      ++loaded;
+    }
     asm volatile("cp.async.commit_group;\n" ::);
   }
   // MN-major (transposed) A and B, BF16, FP32 accumulator, M = 128, N = cin
@@ -1088,11 +1130,17 @@ __global__ void __launch_bounds__(128) conv3x3_wgrad_umma_kernel(UmmaWgradArgs a
         break;
       }
       load(j % S, j);
+      ++loaded;
     }
     asm volatile("cp.async.commit_group;\n" ::);
     asm volatile("cp.async.wait_group %0;\n" ::"n"(kWgAhead));
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-    __syncthreads();
+    bool landed = true;
+    if (use_tma && tid == 0) landed = umma::mbar_wait(tb(st), (uint32_t)((it / S) & 1));  // this tile's TMA loads
+    if (__syncthreads_or(!landed)) {
+      failed = true;
+      break;
+    }
     if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
       const uint32_t ab = sbase + st * stage_bytes, bb = ab + kWgABytes;
@@ -1117,6 +1165,14 @@ __global__ void __launch_bounds__(128) conv3x3_wgrad_umma_kernel(UmmaWgradArgs a
     ++issued;
   }
   asm volatile("cp.async.wait_group 0;\n" ::);
+  if (failed && use_tma && tid == 0) {
+    // TMA loads still in flight land before the CTA's shared memory is
+    // released: the last load into each stage, bounded
+    for (int st = 0; st < S && st < loaded; ++st) {
+      const int jl = loaded - 1 - (loaded - 1 - st) % S;  // last tile loaded into stage st
+      umma::mbar_wait(tb(st), (uint32_t)((jl / S) & 1));
+    }
+  }
   __syncthreads();
   if (n_it > 0) {
     // the last MMAs issued (and with them every earlier one) complete before
@@ -1503,8 +1559,29 @@ PBRT_API int pbrt_nn_conv3x3_wgrad_umma(const void* dy, const void* x1, int32_t 
   // one wave: each CTA walks its share of the tiles for its taps
   const long per_group = std::max(1L, std::min(tiles, (long)sms * per_sm / groups));
   UmmaWgradArgs a{(const bf16*)dy, (const bf16*)x1, (const bf16*)x2, c1, c2, dw, n, h, wd, cout, ntaps, stages};
+  // dY's 8x8 tile and x1's 10x10 halo by TMA: 5-D maps [8 channels][x][y]
+  // [channel group][image] whose boxes land in the operands' layout
+  CUtensorMap dymap, x1map;
+  memset(&dymap, 0, sizeof(dymap));
+  memset(&x1map, 0, sizeof(x1map));
+  int use_tma = 0;
+  if (EncodeTiledFn enc = encode_tiled()) {
+    const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    const cuuint64_t ddims[5] = {8, (cuuint64_t)wd, (cuuint64_t)h, (cuuint64_t)(cout / 8), (cuuint64_t)n};
+    const cuuint64_t dstr[4] = {(cuuint64_t)cout * 2, (cuuint64_t)wd * cout * 2, 16, (cuuint64_t)h * wd * cout * 2};
+    const cuuint32_t dbox[5] = {8, kWgT, kWgT, (cuuint32_t)(cout / 8), 1};
+    const cuuint64_t xdims[5] = {8, (cuuint64_t)wd, (cuuint64_t)h, (cuuint64_t)(c1 / 8), (cuuint64_t)n};
+    const cuuint64_t xstr[4] = {(cuuint64_t)c1 * 2, (cuuint64_t)wd * c1 * 2, 16, (cuuint64_t)h * wd * c1 * 2};
+    const cuuint32_t xbox[5] = {8, kWgHalo, kWgHalo, (cuuint32_t)(c1 / 8), 1};
+    use_tma = enc(&dymap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void*>(dy), ddims, dstr, dbox, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS &&
+              enc(&x1map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void*>(x1), xdims, xstr, xbox, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  }
   dim3 grid((unsigned)groups, (unsigned)per_group);
-  conv3x3_wgrad_umma_kernel<<<grid, 128, smem, stream>>>(a);
+  conv3x3_wgrad_umma_kernel<<<grid, 128, smem, stream>>>(a, dymap, x1map, use_tma);
   return check_launch("conv3x3_wgrad_umma_kernel");
 }
 
