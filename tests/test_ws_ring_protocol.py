@@ -47,10 +47,13 @@ class Violation(AssertionError):
     pass
 
 
-def run(stages, tiles, tma, gather, fp8, owner, rng, stg=False):
+def run(stages, tiles, tma, gather, fp8, owner, rng, stg=False, gather_all=False):
     """One random schedule of one CTA's roles over `tiles` tiles. Raises Violation on a broken guarantee,
     returns False on a deadlock (no role can move), True when every role finished."""
-    full = [Barrier((0 if fp8 else (1 if tma else 0)) + (1 if gather else 0)) for _ in range(stages)]
+    # gather_all: every gather warp fills part of every stage and arrives on it
+    # (the backward-weights kernel); else each stage has one owning warp
+    n_arrive = GATHER_WARPS if gather_all else 1
+    full = [Barrier((0 if fp8 else (1 if tma else 0)) + (n_arrive if gather else 0)) for _ in range(stages)]
     empty = [Barrier(1) for _ in range(stages)]
     tmab = [Barrier(1) for _ in range(stages)]  # FP8: the TMA's own barrier
     stgb = [Barrier(1) for _ in range(stages)]  # the half-resolution box's barrier
@@ -82,16 +85,24 @@ def run(stages, tiles, tma, gather, fp8, owner, rng, stg=False):
                 inflight_tma.append((st, i, "x2"))
             yield
 
+    gat_parts = [set() for _ in range(stages)]  # gather_all: which warps filled the stage for its tile
+
     def gatherer(gw):
         for i in range(tiles):
-            if owner(i, stages) != gw:
+            if not gather_all and owner(i, stages) != gw:
                 continue
             st, k = i % stages, i // stages
             while not empty[st].passes((k & 1) ^ 1):
                 yield
             if readers[st]:
                 raise Violation(f"gather warp {gw} refills stage {st} for tile {i} while MMAs read it")
-            gat_part[st] = i
+            if gather_all:
+                if gat_part[st] != i:
+                    gat_part[st] = i
+                    gat_parts[st] = set()
+                gat_parts[st].add(gw)
+            else:
+                gat_part[st] = i
             yield
             if stg:
                 while not stgb[st].passes(k & 1):
@@ -120,6 +131,8 @@ def run(stages, tiles, tma, gather, fp8, owner, rng, stg=False):
                 raise Violation(f"MMA of tile {i}: stage {st} holds TMA part of tile {tma_part[st]}")
             if gather and gat_part[st] != i:
                 raise Violation(f"MMA of tile {i}: stage {st} holds gathered part of tile {gat_part[st]}")
+            if gather_all and len(gat_parts[st]) != GATHER_WARPS:
+                raise Violation(f"MMA of tile {i}: stage {st} filled by warps {sorted(gat_parts[st])} only")
             if stg and stg_part[st] != i:
                 raise Violation(f"MMA of tile {i}: stage {st} expanded from the box of tile {stg_part[st]}")
             if fp8 and converted[st] != i:
@@ -224,6 +237,16 @@ def test_ring_protocol_holds_with_box(stages, fp8):
     for _ in range(150):
         tiles = rng.randrange(1, 4 * stages + 6)
         assert run(stages, tiles, True, True, fp8, owner_kernel, rng, stg=True), "deadlock"
+
+
+@pytest.mark.parametrize("stages", [2, 3, 4])
+def test_ring_protocol_holds_with_every_warp_on_every_stage(stages):
+    """The backward-weights kernel's form: the gather warps all fill part of
+    every stage, each arriving on its full barrier (count 1 + warps)."""
+    rng = random.Random(stages * 17)
+    for _ in range(200):
+        tiles = rng.randrange(1, 4 * stages + 6)
+        assert run(stages, tiles, True, True, False, owner_kernel, rng, gather_all=True), "deadlock"
 
 
 def test_model_catches_shared_stage_ownership():

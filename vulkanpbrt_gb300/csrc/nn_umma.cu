@@ -1217,6 +1217,209 @@ __global__ void __launch_bounds__(128) conv3x3_wgrad_umma_kernel(UmmaWgradArgs a
   }
 }
 
+// Warp-specialised form of the backward-weights kernel (used where the TMA
+// maps can be made): no block-wide barrier inside the tile loop. Warp 0's
+// lane 0 loads dY's tile and x1's halo of each tile by TMA into a ring of S
+// stages (stage "full" barrier: its transaction bytes); warps 2-3 gather the
+// upsampled x2 part of the halo with cp.async and arrive on the same full
+// barrier (64 arrivals); warp 1's lane 0 issues each tile's MMAs as soon as
+// its stage is full and commits them to the stage's "empty" barrier, which
+// the loaders wait for before refilling it. At the end every warp drains
+// its 32 tensor-memory lanes into dW. Every wait is bounded (2 s); a
+// timeout raises a shared abort flag that ends every role's loop; the MMA
+// lane then waits (bounded) for its last commit and the TMA lane for its
+// last load into each stage before the tensor memory is freed.
+__global__ void __launch_bounds__(128) conv3x3_wgrad_umma_ws_kernel(UmmaWgradArgs a,
+                                                                    const __grid_constant__ CUtensorMap dymap,
+                                                                    const __grid_constant__ CUtensorMap x1map) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ __align__(8) uint64_t full_bar[kWgStages], empty_bar[kWgStages];
+  __shared__ uint32_t tmem_base_slot;
+  __shared__ volatile int abort_flag;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int cin = a.c1 + a.c2;
+  const int tap0 = blockIdx.x * a.ntaps;
+  const int tiles_x = (a.W + kWgT - 1) / kWgT, tiles_y = (a.H + kWgT - 1) / kWgT;
+  const long tiles = (long)tiles_x * tiles_y * a.N;
+  const int n_it = blockIdx.y < tiles ? (int)((tiles - 1 - blockIdx.y) / gridDim.y + 1) : 0;
+  const int H2 = a.H >> 1, W2 = a.W >> 1;
+  const uint32_t cols = wgrad_cols(a.ntaps * cin);
+  const int S = a.stages;
+  const int stage_bytes = wgrad_stage_bytes(cin);
+  const int ga = a.cout / 8, gb = cin / 8, gb1 = a.c1 / 8;
+  const bool gather = gb > gb1;  // the upsampled second input
+  const uint32_t sbase = (umma::smem_addr(smem) + 1023u) & ~1023u;
+  auto fb = [&](int st) { return umma::smem_addr(&full_bar[st]); };
+  auto eb = [&](int st) { return umma::smem_addr(&empty_bar[st]); };
+  if (tid == 0) {
+    for (int st = 0; st < S; ++st) {
+      umma::mbar_init(fb(st), 1u + (gather ? 64u : 0u));
+      umma::mbar_init(eb(st), 1);
+    }
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                     umma::smem_addr(&tmem_base_slot)),
+                 "r"(cols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+  }
+  // the A rows past cout stay zero in every stage
+  for (int st = 0; st < S; ++st)
+    for (int i = tid * 16 + ga * 1024; i < kWgABytes; i += 128 * 16)
+      asm volatile("st.shared.v4.b32 [%0], {%1, %1, %1, %1};\n" ::"r"(sbase + st * stage_bytes + i), "r"(0)
+                   : "memory");
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = tmem_base_slot;
+  auto wait = [&](uint32_t bar, uint32_t parity) {
+    if (umma::mbar_wait(bar, parity)) return true;
+    abort_flag = 1;
+    return false;
+  };
+  auto tile_origin = [&](int it, int& img, int& x0, int& y0) {
+    const long t = blockIdx.y + (long)it * gridDim.y;
+    img = (int)(t / ((long)tiles_x * tiles_y));
+    const int rem = (int)(t - (long)img * tiles_x * tiles_y);
+    x0 = (rem % tiles_x) * kWgT;
+    y0 = (rem / tiles_x) * kWgT;
+  };
+
+  int loaded = 0;  // producer lane: tiles whose TMA loads were issued
+  if (warp == 0) {
+    if (lane == 0) {
+      for (int it = 0; it < n_it && !abort_flag; ++it) {
+        const int st = it % S, k = it / S;
+        if (!wait(eb(st), (uint32_t)((k & 1) ^ 1))) break;  // the MMAs of the stage's previous tile are done
+        int img, x0, y0;
+        tile_origin(it, img, x0, y0);
+        const uint32_t ab = sbase + st * stage_bytes, bb = ab + kWgABytes;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb(st)),
+                     "r"((uint32_t)(ga * 1024 + gb1 * kWgBGroup))
+                     : "memory");
+        asm volatile(
+            "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+            "%5, %6}], [%7];\n" ::"r"(ab),
+            "l"(reinterpret_cast<uint64_t>(&dymap)), "r"(0), "r"(x0), "r"(y0), "r"(0), "r"(img), "r"(fb(st))
+            : "memory");
+        asm volatile(
+            "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+            "%5, %6}], [%7];\n" ::"r"(bb),
+            "l"(reinterpret_cast<uint64_t>(&x1map)), "r"(0), "r"(x0 - 1), "r"(y0 - 1), "r"(0), "r"(img), "r"(fb(st))
+            : "memory");
+        ++loaded;
+      }
+    }
+    __syncwarp();
+  } else if (warp >= 2) {
+    // ---- gather of the upsampled x2 planes of the halo (64 threads, every stage)
+    const int tg = tid - 64;
+    for (int it = 0; it < n_it && !abort_flag && gather; ++it) {
+      const int st = it % S, k = it / S;
+      if (!wait(eb(st), (uint32_t)((k & 1) ^ 1))) break;
+      int img, x0, y0;
+      tile_origin(it, img, x0, y0);
+      const uint32_t bb = sbase + st * stage_bytes + kWgABytes;
+      for (int q = tg; q < kWgHalo * kWgHalo * (gb - gb1); q += 64) {
+        const int hp = q % (kWgHalo * kWgHalo), g = gb1 + q / (kWgHalo * kWgHalo);
+        const int yy = y0 - 1 + hp / kWgHalo, xx = x0 - 1 + hp % kWgHalo;
+        const bool ok = yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
+        const bf16* src = ok ? a.x2 + (((size_t)img * H2 + (yy >> 1)) * W2 + (xx >> 1)) * a.c2 + (g * 8 - a.c1) : a.x1;
+        umma::cp16(bb + g * kWgBGroup + hp * 16, src, ok);
+      }
+      asm volatile("cp.async.commit_group;\n" ::);
+      asm volatile("cp.async.wait_group 0;\n" ::);
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(fb(st)) : "memory");
+    }
+    asm volatile("cp.async.wait_group 0;\n" ::);
+  } else if (lane == 0) {
+    // ---- MMA issue (warp 1, one lane)
+    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) |
+                           ((uint32_t)(cin >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+    for (int it = 0; it < n_it && !abort_flag; ++it) {
+      const int st = it % S, k = it / S;
+      if (!wait(fb(st), (uint32_t)(k & 1))) break;  // this tile's operands in place
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      const uint32_t ab = sbase + st * stage_bytes, bb = ab + kWgABytes;
+      for (int tl = 0; tl < a.ntaps; ++tl) {
+        const int tap = tap0 + tl, dy = tap / 3, dx = tap % 3;
+        const uint32_t d = tmem + (uint32_t)(tl * cin);
+#pragma unroll
+        for (int ks = 0; ks < 4; ++ks) {  // K = 16: tile rows 2ks, 2ks + 1
+          const uint64_t da = umma::sdesc(ab + ks * 256, 128, 1024);
+          const uint64_t db = umma::sdesc(bb + ((2 * ks + dy) * kWgHalo + dx) * 16, kWgHalo * 16, kWgBGroup);
+          const uint32_t acc = (it > 0 || ks > 0) ? 1u : 0u;
+          asm volatile(
+              "{\n\t.reg .pred p;\n\t"
+              "setp.ne.b32 p, %4, 0;\n\t"
+              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+              "l"(da), "l"(db), "r"(idesc), "r"(acc));
+        }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(eb(st))
+                   : "memory");
+    }
+  }
+  // every role is past its loop: the last tile's MMAs (and every earlier
+  // one) complete before the accumulator is read or freed
+  __syncthreads();
+  bool ok = !abort_flag;
+  if (n_it > 0) {
+    const int last = n_it - 1;
+    if (ok) {
+      ok = umma::mbar_wait(eb(last % S), (uint32_t)((last / S) & 1));
+      if (!ok) ok = umma::mbar_wait(eb(last % S), (uint32_t)((last / S) & 1));
+    }
+  }
+  const bool failed = __syncthreads_or(!ok);
+  if (failed) {
+    if (tid == 0) {
+      atomicOr(&g_umma_error, 1u);
+      // TMA loads still in flight land before the shared memory is
+      // released: the last load into each stage, bounded
+      for (int st = 0; st < S && st < loaded; ++st) {
+        const int jl = loaded - 1 - (loaded - 1 - st) % S;
+        umma::mbar_wait(fb(st), (uint32_t)((jl / S) & 1));
+      }
+    }
+    if (warp == 1 && lane == 0 && n_it > 0) {  // MMAs in flight, bounded
+      const int last = n_it - 1;
+      umma::mbar_wait(eb(last % S), (uint32_t)((last / S) & 1));
+    }
+  } else if (n_it > 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const int co = warp * 32 + lane;  // TMEM lane
+    for (int tl = 0; tl < a.ntaps; ++tl) {
+      float* drow = a.dw + ((size_t)(co < a.cout ? co : 0) * 9 + tap0 + tl) * cin;
+      for (int c0 = 0; c0 < cin; c0 += 16) {
+        uint32_t v[16];
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(tl * cin + c0);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+            "[%16];\n"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        if (co < a.cout) {
+#pragma unroll
+          for (int k = 0; k < 16; ++k) atomicAdd(drow + c0 + k, __uint_as_float(v[k]));
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(cols));
+  }
+}
+
 }  // namespace nn
 }  // namespace pbrt
 
@@ -1545,6 +1748,9 @@ PBRT_API int pbrt_nn_conv3x3_wgrad_umma(const void* dy, const void* x1, int32_t 
   int ast = once_per_device(attrs, [&]() -> int {
     cudaError_t e = cudaFuncSetAttribute(conv3x3_wgrad_umma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)kMaxSmem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(conv3x3_wgrad_umma_ws_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)kMaxSmem);
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(conv3x3_wgrad_umma_kernel)");
     return PBRT_OK;
   });
@@ -1581,7 +1787,8 @@ PBRT_API int pbrt_nn_conv3x3_wgrad_umma(const void* dy, const void* x1, int32_t 
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
   }
   dim3 grid((unsigned)groups, (unsigned)per_group);
-  conv3x3_wgrad_umma_kernel<<<grid, 128, smem, stream>>>(a, dymap, x1map, use_tma);
+  if (use_tma) conv3x3_wgrad_umma_ws_kernel<<<grid, 128, smem, stream>>>(a, dymap, x1map);  // warp-specialised
+  else conv3x3_wgrad_umma_kernel<<<grid, 128, smem, stream>>>(a, dymap, x1map, 0);
   return check_launch("conv3x3_wgrad_umma_kernel");
 }
 
