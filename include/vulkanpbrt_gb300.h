@@ -535,9 +535,11 @@ PBRT_API int pbrt_nn_conv3x3_umma_pooled(const void* x1, int32_t c1, const void*
                                          pbrt_stream_t stream);
 /* Backward weights on tcgen05: the arguments of pbrt_nn_conv3x3_wgrad (dw
  * [cout][9][c1+c2] FP32, added to), cout <= 128, c1 + c2 <= 256, 16-byte
- * aligned inputs. One CTA a (pixel run, tap): dY and the shifted input are
- * the MMA's MN-major operands as stored, the sum over the run in tensor
- * memory, then atomics into dw. */
+ * aligned inputs. A CTA walks 8x8-pixel tiles for a group of taps: dY's tile
+ * and the input's 10x10 halo (by TMA; the upsampled second input gathered)
+ * are the MMA's MN-major operands as stored, each tap a shift of the halo
+ * descriptor, the sums in tensor memory, then atomics into dw.
+ * PBRT_ERROR_UNSUPPORTED when the tensor maps cannot be made. */
 PBRT_API int pbrt_nn_conv3x3_wgrad_umma(const void* dy, const void* x1, int32_t c1, const void* x2, int32_t c2,
                                         float* dw, int32_t n, int32_t h, int32_t w_px, int32_t cout,
                                         pbrt_stream_t stream);

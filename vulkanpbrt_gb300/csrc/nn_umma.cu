@@ -970,13 +970,11 @@ __global__ void __launch_bounds__(kWsThreads, kF8 ? 3 : 0) conv3x3_umma_ws_kerne
 // dY's tile: pixel rows 128 bytes apart (the K stride), channel groups 1 KB
 // apart. X's 10x10-pixel halo of the tile: halo rows 160 bytes apart, channel
 // groups 1600 bytes apart; the tap (dy, dx) is the same descriptor with its
-// start moved by dy halo rows and dx pixels -- no copy per tap. Thread 0
-// issues the MMAs and commits them to the stage's mbarrier; the loads of a
-// stage wait for the MMAs that read it (two tiles ahead, 4 stages). Every
-// wait is bounded: on a timeout the kernel records the error
-// (pbrt_nn_umma_status), waits again for its own MMAs and frees its tensor
-// memory. The accumulators (TMEM lane = co, column = tap x cin + ci) are
-// added into dW with atomics once, at the end of the walk.
+// start moved by dy halo rows and dx pixels -- no copy per tap. dY's tile
+// and x1's halo come by TMA (5-D maps [8 channels][x][y][channel group]
+// [image] whose boxes land in exactly this layout). The accumulators (TMEM
+// lane = co, column = tap x cin + ci) are added into dW with atomics once,
+// at the end of the walk.
 struct UmmaWgradArgs {
   const bf16* dy;  // [N][H][W][cout]
   const bf16* x1;  // [N][H][W][c1]
@@ -998,227 +996,7 @@ __host__ __device__ constexpr uint32_t wgrad_cols(int cols) {
   return cols <= 32 ? 32u : (cols <= 64 ? 64u : (cols <= 128 ? 128u : (cols <= 256 ? 256u : 512u)));
 }
 
-__global__ void __launch_bounds__(128) conv3x3_wgrad_umma_kernel(UmmaWgradArgs a,
-                                                                 const __grid_constant__ CUtensorMap dymap,
-                                                                 const __grid_constant__ CUtensorMap x1map,
-                                                                 int use_tma) {
-  extern __shared__ __align__(1024) uint8_t smem[];
-  __shared__ __align__(8) uint64_t mbar[kWgStages];
-  __shared__ __align__(8) uint64_t tbar[kWgStages];  // the TMA loads' arrival per stage
-  __shared__ uint32_t tmem_base_slot;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int cin = a.c1 + a.c2;
-  const int tap0 = blockIdx.x * a.ntaps;
-  const int tiles_x = (a.W + kWgT - 1) / kWgT, tiles_y = (a.H + kWgT - 1) / kWgT;
-  const long tiles = (long)tiles_x * tiles_y * a.N;
-  const int n_it = blockIdx.y < tiles ? (int)((tiles - 1 - blockIdx.y) / gridDim.y + 1) : 0;
-  const int H2 = a.H >> 1, W2 = a.W >> 1;
-  const uint32_t cols = wgrad_cols(a.ntaps * cin);
-  const int S = a.stages;
-  const int stage_bytes = wgrad_stage_bytes(cin);
-  const uint32_t sbase = (umma::smem_addr(smem) + 1023u) & ~1023u;
-  auto mb = [&](int st) { return umma::smem_addr(&mbar[st]); };
-  auto tb = [&](int st) { return umma::smem_addr(&tbar[st]); };
-  if (tid == 0) {
-    for (int st = 0; st < S; ++st) {
-      umma::mbar_init(mb(st), 1);
-      umma::mbar_init(tb(st), 1);
-    }
-    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-  }
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
-                     umma::smem_addr(&tmem_base_slot)),
-                 "r"(cols));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
-  }
-  // the A rows past cout stay zero in every stage
-  for (int st = 0; st < S; ++st)
-    for (int i = tid * 16 + (a.cout / 8) * 1024; i < kWgABytes; i += 128 * 16)
-      asm volatile("st.shared.v4.b32 [%0], {%1, %1, %1, %1};\n" ::"r"(sbase + st * stage_bytes + i), "r"(0)
-                   : "memory");
-  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-  const uint32_t tmem = tmem_base_slot;
-
-  // stage st <- tile number it of this CTA: dY's 64 pixels (zeros outside
-  // the image) and X's 100 halo pixels (zeros outside: the padding). With
-  // use_tma, dY's tile and x1's halo come in two TMA tile loads issued by
-  // thread 0 (5-D maps [8 channels][x][y][channel group][image], whose
-  // boxes land in exactly the operand layout), the upsampled x2 part by
-  // cp.async gathers of all threads.
-  const int gb1 = use_tma ? a.c1 / 8 : 0;  // halo channel groups the TMA loads
-  auto load = [&](int st, int it) {
-    const uint32_t ab = sbase + st * stage_bytes, bb = ab + kWgABytes;
-    const long t = blockIdx.y + (long)it * gridDim.y;
-    const int img = (int)(t / ((long)tiles_x * tiles_y));
-    const int rem = (int)(t - (long)img * tiles_x * tiles_y);
-    const int x0 = (rem % tiles_x) * kWgT, y0 = (rem / tiles_x) * kWgT;
-    const int ga = a.cout / 8, gb = cin / 8;
-    if (use_tma) {
-      if (tid == 0) {
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(tb(st)),
-                     "r"((uint32_t)(ga * 1024 + gb1 * kWgBGroup))
-                     : "memory");
-        asm volatile(
-            "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
-            "%5, %6}], [%7];\n" ::"r"(ab),
-            "l"(reinterpret_cast<uint64_t>(&dymap)), "r"(0), "r"(x0), "r"(y0), "r"(0), "r"(img), "r"(tb(st))
-            : "memory");
-        asm volatile(
-            "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
-            "%5, %6}], [%7];\n" ::"r"(bb),
-            "l"(reinterpret_cast<uint64_t>(&x1map)), "r"(0), "r"(x0 - 1), "r"(y0 - 1), "r"(0), "r"(img), "r"(tb(st))
-            : "memory");
-      }
-      for (int q = tid; q < kWgHalo * kWgHalo * (gb - gb1); q += 128) {
-        const int hp = q % (kWgHalo * kWgHalo), g = gb1 + q / (kWgHalo * kWgHalo);
-        const int yy = y0 - 1 + hp / kWgHalo, xx = x0 - 1 + hp % kWgHalo;
-        const bool ok = yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
-        const bf16* src = ok ? a.x2 + (((size_t)img * H2 + (yy >> 1)) * W2 + (xx >> 1)) * a.c2 + (g * 8 - a.c1) : a.x1;
-        umma::cp16(bb + g * kWgBGroup + hp * 16, src, ok);
-      }
-      return;
-    }
-    for (int q = tid; q < 64 * ga; q += 128) {
-      const int pl = q & 63, g = q >> 6;
-      const int yy = y0 + (pl >> 3), xx = x0 + (pl & 7);
-      const bool ok = yy < a.H && xx < a.W;
-      const bf16* src = ok ? a.dy + (((size_t)img * a.H + yy) * a.W + xx) * a.cout + g * 8 : a.dy;
-      umma::cp16(ab + g * 1024 + pl * 16, src, ok);
-    }
-    for (int q = tid; q < kWgHalo * kWgHalo * gb; q += 128) {
-      const int hp = q % (kWgHalo * kWgHalo), g = q / (kWgHalo * kWgHalo);
-      const int yy = y0 - 1 + hp / kWgHalo, xx = x0 - 1 + hp % kWgHalo;
-      const int ci = g * 8;
-      const bool ok = yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
-      const bf16* src = a.x1;
-      if (ok) {
-        if (ci < a.c1) src = a.x1 + (((size_t)img * a.H + yy) * a.W + xx) * a.c1 + ci;
-        else src = a.x2 + (((size_t)img * H2 + (yy >> 1)) * W2 + (xx >> 1)) * a.c2 + (ci - a.c1);
-      }
-      umma::cp16(bb + g * kWgBGroup + hp * 16, src, ok);
-    }
-  };
-
-  bool failed = false;
-  int issued = 0;  // tiles whose MMAs were issued (the same count in every thread)
-  int loaded = 0;  // tiles whose loads were issued
-  // loads run two tiles ahead; a refill waits for the MMAs of the tile S
-  // back, issued S - 2 tiles earlier
-  constexpr int kWgAhead = 2;
-  for (int j = 0; j < kWgAhead; ++j) {
-    if (j < n_it) {
-      load(j, j);
-      ++loaded;
-    }
-    asm volatile("cp.async.commit_group;\n" ::);
-  }
-  // MN-major (transposed) A and B, BF16, FP32 accumulator, M = 128, N = cin
-  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) | ((uint32_t)(cin >> 3) << 17) |
-                         ((uint32_t)(128 >> 4) << 24);
-  for (int it = 0; it < n_it && !failed; ++it) {
-    const int st = it % S;
-    const int j = it + kWgAhead;  // refill the stage tile j - S read
-    if (j < n_it) {
-      bool ok = true;
-      const int prev = j - S;
-      if (prev >= 0) ok = umma::mbar_wait(mb(prev % S), (uint32_t)((prev / S) & 1));
-      if (__syncthreads_or(!ok)) {
-        failed = true;
-        break;
-      }
-      load(j % S, j);
-      ++loaded;
-    }
-    asm volatile("cp.async.commit_group;\n" ::);
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(kWgAhead));
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-    bool landed = true;
-    if (use_tma && tid == 0) landed = umma::mbar_wait(tb(st), (uint32_t)((it / S) & 1));  // this tile's TMA loads
-    if (__syncthreads_or(!landed)) {
-      failed = true;
-      break;
-    }
-    if (tid == 0) {
-      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-      const uint32_t ab = sbase + st * stage_bytes, bb = ab + kWgABytes;
-      for (int tl = 0; tl < a.ntaps; ++tl) {
-        const int tap = tap0 + tl, dy = tap / 3, dx = tap % 3;
-        const uint32_t d = tmem + (uint32_t)(tl * cin);
-#pragma unroll
-        for (int ks = 0; ks < 4; ++ks) {  // K = 16: tile rows 2ks, 2ks + 1
-          const uint64_t da = umma::sdesc(ab + ks * 256, 128, 1024);
-          const uint64_t db = umma::sdesc(bb + ((2 * ks + dy) * kWgHalo + dx) * 16, kWgHalo * 16, kWgBGroup);
-          const uint32_t acc = (it > 0 || ks > 0) ? 1u : 0u;
-          asm volatile(
-              "{\n\t.reg .pred p;\n\t"
-              "setp.ne.b32 p, %4, 0;\n\t"
-              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
-              "l"(da), "l"(db), "r"(idesc), "r"(acc));
-        }
-      }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mb(st))
-                   : "memory");
-    }
-    ++issued;
-  }
-  asm volatile("cp.async.wait_group 0;\n" ::);
-  if (failed && use_tma && tid == 0) {
-    // TMA loads still in flight land before the CTA's shared memory is
-    // released: the last load into each stage, bounded
-    for (int st = 0; st < S && st < loaded; ++st) {
-      const int jl = loaded - 1 - (loaded - 1 - st) % S;  // last tile loaded into stage st
-      umma::mbar_wait(tb(st), (uint32_t)((jl / S) & 1));
-    }
-  }
-  __syncthreads();
-  if (n_it > 0) {
-    // the last MMAs issued (and with them every earlier one) complete before
-    // the accumulator is read or freed
-    const int last = issued - 1;
-    bool done = true;
-    if (last >= 0) {
-      done = umma::mbar_wait(mb(last % S), (uint32_t)((last / S) & 1));
-      if (!done) done = umma::mbar_wait(mb(last % S), (uint32_t)((last / S) & 1));
-    }
-    failed = __syncthreads_or(failed || !done);
-    if (failed) {
-      if (tid == 0) atomicOr(&g_umma_error, 1u);
-    } else if (issued > 0) {
-      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-      const int co = warp * 32 + lane;  // TMEM lane
-      for (int tl = 0; tl < a.ntaps; ++tl) {
-        float* drow = a.dw + ((size_t)(co < a.cout ? co : 0) * 9 + tap0 + tl) * cin;
-        for (int c0 = 0; c0 < cin; c0 += 16) {
-          uint32_t v[16];
-          const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(tl * cin + c0);
-          asm volatile(
-              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-              "[%16];\n"
-              : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-              : "r"(taddr));
-          asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-          if (co < a.cout) {
-#pragma unroll
-            for (int k = 0; k < 16; ++k) atomicAdd(drow + c0 + k, __uint_as_float(v[k]));
-          }
-        }
-      }
-    }
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-  __syncthreads();
-  if (warp == 0) {
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(cols));
-  }
-}
-
-// Warp-specialised form of the backward-weights kernel (used where the TMA
-// maps can be made): no block-wide barrier inside the tile loop. Warp 0's
+// Warp-specialised: no block-wide barrier inside the tile loop. Warp 0's
 // lane 0 loads dY's tile and x1's halo of each tile by TMA into a ring of S
 // stages (stage "full" barrier: its transaction bytes); warps 2-3 gather the
 // upsampled x2 part of the halo with cp.async and arrive on the same full
@@ -1723,7 +1501,7 @@ PBRT_API int pbrt_nn_conv3x3_umma_pooled(const void* x1, int32_t c1, const void*
   return check_launch("conv3x3_umma_ws_kernel (pooled)");
 }
 
-// Backward weights on tcgen05 (conv3x3_wgrad_umma_kernel): the arguments of
+// Backward weights on tcgen05 (conv3x3_wgrad_umma_ws_kernel): the arguments of
 // pbrt_nn_conv3x3_wgrad; dw is accumulated into.
 PBRT_API int pbrt_nn_conv3x3_wgrad_umma(const void* dy, const void* x1, int32_t c1, const void* x2, int32_t c2,
                                         float* dw, int32_t n, int32_t h, int32_t wd, int32_t cout,
@@ -1746,12 +1524,9 @@ PBRT_API int pbrt_nn_conv3x3_wgrad_umma(const void* dy, const void* x1, int32_t 
   const size_t smem = (size_t)stages * wgrad_stage_bytes(cin) + 1024;
   static PerDeviceOnce attrs;
   int ast = once_per_device(attrs, [&]() -> int {
-    cudaError_t e = cudaFuncSetAttribute(conv3x3_wgrad_umma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(conv3x3_wgrad_umma_ws_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)kMaxSmem);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(conv3x3_wgrad_umma_ws_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)kMaxSmem);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(conv3x3_wgrad_umma_kernel)");
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(conv3x3_wgrad_umma_ws_kernel)");
     return PBRT_OK;
   });
   if (ast) return ast;
@@ -1786,10 +1561,10 @@ PBRT_API int pbrt_nn_conv3x3_wgrad_umma(const void* dy, const void* x1, int32_t 
                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
   }
+  if (!use_tma) return fail(PBRT_ERROR_UNSUPPORTED, "nn conv3x3 wgrad umma: no tensor maps (c1 %d, cout %d)", c1, cout);
   dim3 grid((unsigned)groups, (unsigned)per_group);
-  if (use_tma) conv3x3_wgrad_umma_ws_kernel<<<grid, 128, smem, stream>>>(a, dymap, x1map);  // warp-specialised
-  else conv3x3_wgrad_umma_kernel<<<grid, 128, smem, stream>>>(a, dymap, x1map, 0);
-  return check_launch("conv3x3_wgrad_umma_kernel");
+  conv3x3_wgrad_umma_ws_kernel<<<grid, 128, smem, stream>>>(a, dymap, x1map);
+  return check_launch("conv3x3_wgrad_umma_ws_kernel");
 }
 
 // tcgen05 convolution of a single input with an FP32 output (the backward-
