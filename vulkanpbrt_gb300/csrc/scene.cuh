@@ -64,9 +64,9 @@ struct SceneView {
   const DevMaterial* materials;
   const DevLight* lights;
   const float4* light_sum;  // per light: ambient + diffuse + specular colour (xyz), w = its power (sampleLight's sums)
-  // vertex attributes interleaved, two float4 a vertex: position xyz and
-  // normal x, then normal yz and uv -- one 32-byte sector a vertex
-  const float4* vtx;
+  const float* pos;
+  const float* nor;
+  const float* uv;
   const uint32_t* idx;
   const DevTexture* textures;
   const uchar4* texels;

@@ -241,17 +241,8 @@ PBRT_D uint3 unpack_index(const SceneView& sc, uint32_t ibase, uint32_t prim, ui
   }
   return r;
 }
-// Vertex v of the interleaved pool: position, normal, texture coordinate.
-PBRT_D void vload(const float4* vtx, uint32_t v, float3& p, float3& n, float2& t) {
-  const float4 a = vtx[2 * v], b = vtx[2 * v + 1];
-  p = f3(a.x, a.y, a.z);
-  n = f3(a.w, b.x, b.y);
-  t = make_float2(b.z, b.w);
-}
-PBRT_D float2 vload_uv(const float4* vtx, uint32_t v) {
-  const float4 b = vtx[2 * v + 1];
-  return make_float2(b.z, b.w);
-}
+PBRT_D float3 vload3(const float* pool, uint32_t v) { return f3(pool[3 * v], pool[3 * v + 1], pool[3 * v + 2]); }
+PBRT_D float2 vload2(const float* pool, uint32_t v) { return make_float2(pool[2 * v], pool[2 * v + 1]); }
 
 // ptAlphaHit.rahit: keep the candidate unless the diffuse alpha < .01.
 PBRT_D bool alpha_accept(const SceneView& sc, uint32_t inst_id, uint32_t prim, float bu, float bv) {
@@ -259,7 +250,7 @@ PBRT_D bool alpha_accept(const SceneView& sc, uint32_t inst_id, uint32_t prim, f
   if (inst.opaque) return true;
   const uint32_t vb = inst.vbase;
   uint3 ix = unpack_index(sc, inst.ibase, prim, inst.index_stride);
-  float2 t0 = vload_uv(sc.vtx, vb + ix.x), t1 = vload_uv(sc.vtx, vb + ix.y), t2 = vload_uv(sc.vtx, vb + ix.z);
+  float2 t0 = vload2(sc.uv, vb + ix.x), t1 = vload2(sc.uv, vb + ix.y), t2 = vload2(sc.uv, vb + ix.z);
   float b0 = 1.0f - bu - bv;
   float u = t0.x * b0 + t1.x * bu + t2.x * bv;
   float v = t0.y * b0 + t1.y * bu + t2.y * bv;
@@ -288,11 +279,9 @@ PBRT_D float3 closest_hit(const SceneView& sc, float3 ray_dir, uint32_t inst_id,
   const uint32_t vb = inst.vbase;
   const int32_t* mtex = inst.tex;
   uint3 ix = unpack_index(sc, inst.ibase, prim, inst.index_stride);
-  float3 p0, p1, p2, n0, n1, n2;
-  float2 t0, t1, t2;
-  vload(sc.vtx, vb + ix.x, p0, n0, t0);
-  vload(sc.vtx, vb + ix.y, p1, n1, t1);
-  vload(sc.vtx, vb + ix.z, p2, n2, t2);
+  float3 p0 = vload3(sc.pos, vb + ix.x), p1 = vload3(sc.pos, vb + ix.y), p2 = vload3(sc.pos, vb + ix.z);
+  float3 n0 = vload3(sc.nor, vb + ix.x), n1 = vload3(sc.nor, vb + ix.y), n2 = vload3(sc.nor, vb + ix.z);
+  float2 t0 = vload2(sc.uv, vb + ix.x), t1 = vload2(sc.uv, vb + ix.y), t2 = vload2(sc.uv, vb + ix.z);
   const float b0 = 1.0f - bu - bv, b1 = bu, b2 = bv;
   float2 tc = make_float2(t0.x * b0 + t1.x * b1 + t2.x * b2, t0.y * b0 + t1.y * b1 + t2.y * b2);
   float4 dm = tex_sample(sc, mtex[0], tc.x, tc.y);

@@ -98,21 +98,21 @@ PBRT_D bool tri_intersect(const RayPre& r, float4 a, float4 b, float4 c, float t
 // ptAlphaHit out of line: it runs rarely, and inlined into the node visit it
 // inflated the traversal loop (instruction-fetch stalls).
 __device__ __noinline__ bool alpha_accept_slow(const DevInstance* instances, const DevMesh* meshes,
-                                               const uint32_t* idx, const float4* vtx, const DevTexture* textures,
+                                               const uint32_t* idx, const float* uvs, const DevTexture* textures,
                                                const uchar4* texels, uint32_t inst_id, uint32_t prim, float bu,
                                                float bv) {
   SceneView sc{};
   sc.instances = instances;
   sc.meshes = meshes;
   sc.idx = idx;
-  sc.vtx = vtx;
+  sc.uv = uvs;
   sc.textures = textures;
   sc.texels = texels;
   return alpha_accept(sc, inst_id, prim, bu, bv);
 }
 PBRT_D bool alpha_accept_call(const SceneView& sc, uint32_t inst_id, uint32_t prim, float bu, float bv) {
   if (__ldg(&sc.instances[inst_id].opaque)) return true;
-  return alpha_accept_slow(sc.instances, sc.meshes, sc.idx, sc.vtx, sc.textures, sc.texels, inst_id, prim, bu, bv);
+  return alpha_accept_slow(sc.instances, sc.meshes, sc.idx, sc.uv, sc.textures, sc.texels, inst_id, prim, bu, bv);
 }
 
 // Per-ray traversal state: the node to visit next, the short stack of node
@@ -1774,7 +1774,7 @@ PBRT_API int pbrt_scene_create(const PbrtSceneDesc* d, PbrtScene** out) {
   DevMaterial* dmat = nullptr;
   DevLight* dlight = nullptr;
   float4* dlsum = nullptr;
-  float4* dvtx = nullptr;
+  float *dpos = nullptr, *dnor = nullptr, *duv = nullptr;
   uint32_t* didx = nullptr;
   DevTexture* dtex = nullptr;
   if (!st) st = sc->up(&dtris, tris.data(), tris.size());
@@ -1784,16 +1784,9 @@ PBRT_API int pbrt_scene_create(const PbrtSceneDesc* d, PbrtScene** out) {
   if (!st) st = sc->up(&dmat, mats.data(), mats.size());
   if (!st) st = sc->up(&dlight, lights.data(), lights.size());
   if (!st) st = sc->up(&dlsum, light_sum.data(), light_sum.size());
-  {
-    // interleaved vertex attributes (SceneView::vtx)
-    const size_t nv = pos.size() / 3;
-    std::vector<float4> vtx(2 * nv);
-    for (size_t i = 0; i < nv; ++i) {
-      vtx[2 * i] = make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], nor[3 * i]);
-      vtx[2 * i + 1] = make_float4(nor[3 * i + 1], nor[3 * i + 2], uv[2 * i], uv[2 * i + 1]);
-    }
-    if (!st) st = sc->up(&dvtx, vtx.data(), vtx.size());
-  }
+  if (!st) st = sc->up(&dpos, pos.data(), pos.size());
+  if (!st) st = sc->up(&dnor, nor.data(), nor.size());
+  if (!st) st = sc->up(&duv, uv.data(), uv.size());
   if (!st) st = sc->up(&didx, idx.data(), idx.size());
   if (!st) st = sc->up(&dtex, texd.data(), texd.size());
   if (st) {
@@ -1807,7 +1800,9 @@ PBRT_API int pbrt_scene_create(const PbrtSceneDesc* d, PbrtScene** out) {
   v.materials = dmat;
   v.lights = dlight;
   v.light_sum = dlsum;
-  v.vtx = dvtx;
+  v.pos = dpos;
+  v.nor = dnor;
+  v.uv = duv;
   v.idx = didx;
   v.textures = dtex;
   v.texels = texpool;
