@@ -75,6 +75,24 @@ __host__ __device__ constexpr uint32_t idesc_e4m3(int n) {
   return (1u << 4) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kM >> 4) << 24);
 }
 
+// One tcgen05.mma with A and B in shared memory; accumulate = false
+// overwrites D. kF8: kind::f8f6f4 (E4M3), else kind::f16 (BF16).
+template <bool kF8>
+__device__ __forceinline__ void mma_ss(uint32_t d, uint64_t da, uint64_t db, uint32_t idesc, bool accumulate) {
+  if constexpr (kF8)
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+        "l"(da), "l"(db), "r"(idesc), "r"((uint32_t)accumulate));
+  else
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+        "l"(da), "l"(db), "r"(idesc), "r"((uint32_t)accumulate));
+}
+
 __device__ __forceinline__ void mbar_init(uint32_t addr, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(addr), "r"(count));
 }
@@ -445,20 +463,15 @@ __global__ void __launch_bounds__(128) conv3x3_umma_persistent_kernel(UmmaConvAr
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
       constexpr uint32_t idesc = umma::idesc_bf16(NC);
       const uint32_t d = tmem + b * NC;
-#pragma unroll 1
+      // descriptors advance by constants (16-byte units)
+      const uint64_t da0 = umma::sdesc(hb, kPlaneBytes, kHaloW * 16);
+      const uint64_t db0 = umma::sdesc(wbase, NC * 16, 8 * 16);
+#pragma unroll
       for (int tap = 0; tap < 9; ++tap) {
-        const int dy = tap / 3, dx = tap % 3;
-        for (int ks = 0; ks < planes / 2; ++ks) {
-          const uint64_t da = umma::sdesc(hb + (2 * ks) * kPlaneBytes + (dy * kHaloW + dx) * 16, kPlaneBytes,
-                                          kHaloW * 16);
-          const uint64_t db = umma::sdesc(wbase + ((tap * planes + 2 * ks) * NC) * 16, NC * 16, 8 * 16);
-          const uint32_t acc = (tap > 0 || ks > 0) ? 1u : 0u;
-          asm volatile(
-              "{\n\t.reg .pred p;\n\t"
-              "setp.ne.b32 p, %4, 0;\n\t"
-              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
-              "l"(da), "l"(db), "r"(idesc), "r"(acc));
-        }
+        uint64_t da = da0 + (uint64_t)((((tap / 3) * kHaloW + tap % 3) * 16) >> 4);
+        uint64_t db = db0 + (uint64_t)(tap * planes * NC);
+        for (int ks = 0; ks < planes / 2; ++ks, da += (2 * kPlaneBytes) >> 4, db += 2 * NC)
+          umma::mma_ss<false>(d, da, db, idesc, tap > 0 || ks > 0);
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
                        b ? mb1 : mb0)
@@ -786,26 +799,20 @@ __global__ void __launch_bounds__(kWsThreads, kF8 ? 3 : 0) conv3x3_umma_ws_kerne
         if (!wait(teb(b), (uint32_t)((kb & 1) ^ 1))) break;    // accumulator buffer drained
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
         const uint32_t hb = hbase + st * halo_pitch, d = tmem + (uint32_t)b * NC;
+        // The descriptors advance by constants (a tap shifts the halo's
+        // start, a K step moves two planes; every sum is a shared-memory
+        // address, so the 14-bit address field never carries): a single
+        // issuing thread that rebuilt them per instruction spent ~40 cycles
+        // an MMA on it, as much as the ~50-cycle MMA itself at small N.
+        const uint64_t da0 = umma::sdesc(hb, kPlaneBytes, kHaloW * 16);
+        const uint64_t db0 = umma::sdesc(wbase, NC * 16, 8 * 16);
+        const int ksteps = planes / 2;
+#pragma unroll
         for (int tap = 0; tap < 9; ++tap) {
-          const int dy = tap / 3, dx = tap % 3;
-          for (int ks = 0; ks < planes / 2; ++ks) {
-            const uint64_t da = umma::sdesc(hb + (2 * ks) * kPlaneBytes + (dy * kHaloW + dx) * 16, kPlaneBytes,
-                                            kHaloW * 16);
-            const uint64_t db = umma::sdesc(wbase + ((tap * planes + 2 * ks) * NC) * 16, NC * 16, 8 * 16);
-            const uint32_t acc = (tap > 0 || ks > 0) ? 1u : 0u;
-            if constexpr (kF8)
-              asm volatile(
-                  "{\n\t.reg .pred p;\n\t"
-                  "setp.ne.b32 p, %4, 0;\n\t"
-                  "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
-                  "l"(da), "l"(db), "r"(idesc), "r"(acc));
-            else
-              asm volatile(
-                  "{\n\t.reg .pred p;\n\t"
-                  "setp.ne.b32 p, %4, 0;\n\t"
-                  "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
-                  "l"(da), "l"(db), "r"(idesc), "r"(acc));
-          }
+          uint64_t da = da0 + (uint64_t)((((tap / 3) * kHaloW + tap % 3) * 16) >> 4);
+          uint64_t db = db0 + (uint64_t)(tap * planes * NC);
+          for (int ks = 0; ks < ksteps; ++ks, da += (2 * kPlaneBytes) >> 4, db += 2 * NC)
+            umma::mma_ss<kF8>(d, da, db, idesc, tap > 0 || ks > 0);
         }
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(eb(st))
                      : "memory");
@@ -1123,20 +1130,17 @@ __global__ void __launch_bounds__(128) conv3x3_wgrad_umma_ws_kernel(UmmaWgradArg
       if (!wait(fb(st), (uint32_t)(k & 1))) break;  // this tile's operands in place
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
       const uint32_t ab = sbase + st * stage_bytes, bb = ab + kWgABytes;
+      // descriptors advance by constants (16-byte units)
+      const uint64_t da0 = umma::sdesc(ab, 128, 1024);
+      const uint64_t db0 = umma::sdesc(bb, kWgHalo * 16, kWgBGroup);
       for (int tl = 0; tl < a.ntaps; ++tl) {
         const int tap = tap0 + tl, dy = tap / 3, dx = tap % 3;
         const uint32_t d = tmem + (uint32_t)(tl * cin);
+        const uint64_t dbt = db0 + (uint64_t)(dy * kWgHalo + dx);
 #pragma unroll
-        for (int ks = 0; ks < 4; ++ks) {  // K = 16: tile rows 2ks, 2ks + 1
-          const uint64_t da = umma::sdesc(ab + ks * 256, 128, 1024);
-          const uint64_t db = umma::sdesc(bb + ((2 * ks + dy) * kWgHalo + dx) * 16, kWgHalo * 16, kWgBGroup);
-          const uint32_t acc = (it > 0 || ks > 0) ? 1u : 0u;
-          asm volatile(
-              "{\n\t.reg .pred p;\n\t"
-              "setp.ne.b32 p, %4, 0;\n\t"
-              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
-              "l"(da), "l"(db), "r"(idesc), "r"(acc));
-        }
+        for (int ks = 0; ks < 4; ++ks)  // K = 16: tile rows 2ks, 2ks + 1
+          umma::mma_ss<false>(d, da0 + (uint64_t)(ks * 16), dbt + (uint64_t)(2 * ks * kWgHalo), idesc,
+                              it > 0 || ks > 0);
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(eb(st))
                    : "memory");
