@@ -65,7 +65,7 @@ def parse():
     ap.add_argument("--sort-rays", action="store_true", help="sort extension / shadow rays before traversal")
     ap.add_argument("--separate-shadow", action="store_true",
                     help="trace shadow rays in their own launch (default: merged into the next bounce's launch)")
-    ap.add_argument("--workload", default="frame1080p", choices=["frame1080p", "batch64", "unet_layers", "full"],
+    ap.add_argument("--workload", default="frame1080p", choices=["frame1080p", "batch64", "unet_layers", "full", "bvh_build"],
                     help="batch64: 64 uneven render requests in one graph launch; unet_layers: per-convolution "
                          "times of the U-Net; full: 4K 4 spp frames of a 4M-triangle scene (FP8 network, gate, "
                          "BMFR with the FP64 re-solve) beside 16 concurrent 1080p requests (none of these is the "
@@ -1107,6 +1107,76 @@ def run_unet_layers(args):
         print(f"\nFP8 as dispatched (tcgen05 where it fits): {fp8_net:.1f} us")
 
 
+def run_bvh_build(args):
+    """The two BVH builds side by side -- FAST_TRACE (binned SAH on the host,
+    SAH-optimal collapse; the default) and FAST_BUILD (linear BVH on the
+    device) -- on the benchmark scene and the full-form 4.3M-triangle scene:
+    scene set-up and build time, tree size and depth, and what each tree
+    costs a 1080p path-traced frame (frame ms by CUDA events over graph
+    launches; traversal ms, nodes and triangles a ray from one profiled
+    frame). Frames are bit-identical under both (tested)."""
+    import torch
+
+    from vulkanpbrt_gb300 import build as B
+
+    B.build()
+    import vulkanpbrt_gb300 as vp
+    from vulkanpbrt_gb300 import scene as S
+
+    W, H = args.width, args.height
+    stream = torch.cuda.current_stream()
+    scenes = {"bench_1M": lambda: workload(args),
+              "full_4M": lambda: S.instanced_field(seed=0, instances=8000, point_lights=30)}
+    out = {"metric": "BVH build ms and 1080p path-tracing ms: host binned SAH vs device linear BVH",
+           "width": W, "height": H, "steps": args.steps, "scenes": {}}
+    for name, make in scenes.items():
+        sc = make()
+        cams = [orbit(sc, W, H, f) for f in range(16)]
+        rows = {}
+        for build in ("fast_trace", "fast_build"):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            sh = vp.SceneHandle(sc, build=build)
+            torch.cuda.synchronize()
+            create_s = time.perf_counter() - t0
+            info = sh.info()
+            g = vp.GBuffer(W, H)
+            illu = vp.IlluminationBufferDemodulatedFloat(W, H)
+            pipe = vp.PBRTPipeline(sh, g, illu, True, max_recursion_depth=args.max_depth,
+                                   min_recursion_depth=args.min_depth)
+            pc = vp.PushConstants()
+
+            def set_cam(f):
+                cam = cams[f % 16]
+                pc.set(view_inverse=cam.inv_view, proj_inverse=cam.inv_proj, prev_view=cam.view, frame_number=f)
+
+            for f in range(max(3, args.warmup)):
+                set_cam(f)
+                pipe.trace(pc, stream)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for f in range(args.steps):
+                set_cam(f)
+                pipe.trace(pc, stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            frame_ms = e0.elapsed_time(e1) / args.steps
+            set_cam(5)
+            t = pipe.profile(pc, stream)
+            rays = t.closest_rays + t.shadow_rays
+            rows[build] = {"scene_create_s": round(create_s, 3), "build_ms": round(info.build_ms, 1),
+                           "nodes": int(info.bvh_nodes), "depth": int(info.bvh_depth),
+                           "frame_ms": round(frame_ms, 3),
+                           "traversal_ms": round(t.trace_closest_ms + t.trace_shadow_ms, 3),
+                           "nodes_per_ray": round((t.closest_nodes + t.shadow_nodes) / max(1, rays), 2),
+                           "tris_per_ray": round((t.closest_tris + t.shadow_tris) / max(1, rays), 2)}
+            del pipe, g, illu, sh
+            torch.cuda.synchronize()
+        out["scenes"][name] = {"triangles": int(sc.tri_count), **rows}
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -1117,6 +1187,8 @@ def main():
         run_full(args)
     elif args.workload == "batch64":
         run_batch(args)
+    elif args.workload == "bvh_build":
+        run_bvh_build(args)
     else:
         run_gb300(args)
 

@@ -334,6 +334,16 @@ typedef struct PbrtSceneInfo {
   double build_ms;
 } PbrtSceneInfo;
 PBRT_API int pbrt_scene_create(const PbrtSceneDesc* desc, PbrtScene** out);
+/* The build's speed-for-quality trade, as Vulkan's acceleration-structure
+ * build flags offer it (VK_BUILD_ACCELERATION_STRUCTURE_PREFER_FAST_TRACE_BIT_KHR
+ * / _PREFER_FAST_BUILD_BIT_KHR; the reference builds with vsg's defaults,
+ * VulkanPBRT.cpp:365-367). FAST_TRACE (what pbrt_scene_create does): binned
+ * SAH on the host, collapsed SAH-optimally to 8-wide nodes. FAST_BUILD: a
+ * linear BVH (Morton order) built on the device and collapsed greedily;
+ * lower quality, for scenes rendered few times. Hits, and so frames, are
+ * identical under either build. */
+enum { PBRT_BUILD_PREFER_FAST_TRACE = 0, PBRT_BUILD_PREFER_FAST_BUILD = 1 };
+PBRT_API int pbrt_scene_create_ex(const PbrtSceneDesc* desc, uint32_t build_flags, PbrtScene** out);
 /* Mesh preparation the visitor applies before it hands a mesh on
  * (RayTracingVisitor.cpp:52-127, 133-166), host side: area-weighted running
  * average of face normals into normals[3 * vertex_count] (not normalised,

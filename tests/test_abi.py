@@ -45,6 +45,14 @@ def test_version_and_error_plumbing(native_lib):
     assert rc == -1 and "unknown type" in last_error()
     rc = native_lib.pbrt_bmfr_set_options(None, 0, 0)
     assert rc == -1
+    # the scene build's flags: FAST_TRACE (0) or FAST_BUILD (1), nothing else
+    from vulkanpbrt_gb300.pipeline import PbrtSceneDesc
+
+    desc = PbrtSceneDesc()
+    rc = native_lib.pbrt_scene_create_ex(ctypes.byref(desc), 2, ctypes.byref(h))
+    assert rc == -1 and "build flags" in last_error()
+    rc = native_lib.pbrt_scene_create_ex(ctypes.byref(desc), 1, ctypes.byref(h))
+    assert rc == -1 and "needs meshes" in last_error() and not h.value
     try:
         check(-4)
     except PbrtError as e:

@@ -13,6 +13,8 @@
 #include <cstdint>
 #include <vector>
 
+#include <vector_types.h>
+
 namespace pbrt {
 
 struct alignas(16) Node8 {
@@ -38,5 +40,14 @@ struct Bvh8Stats {
 // tri_order receives, for every triangle slot of the BVH, the input index.
 void build_bvh8(const float* verts9, size_t n, std::vector<Node8>& nodes, std::vector<uint32_t>& tri_order,
                 Bvh8Stats* stats);
+
+// Device build of the same layout (bvh_gpu.cu): a linear BVH collapsed to
+// 8-wide nodes. Takes the triangles (9 floats each) and each triangle's
+// instance and primitive; returns device arrays (cudaMalloc'd, the caller
+// frees them): the nodes and the leaf-ordered triangle records, 3 float4 a
+// triangle (v0 | flattening index, v1 | instance, v2 | primitive). Fails
+// with PBRT_ERROR_UNSUPPORTED past max_depth wide levels.
+int build_bvh8_device(const float* verts9, const uint32_t* instance, const uint32_t* primitive, size_t n,
+                      int max_depth, Node8** nodes, float4** tris, Bvh8Stats* stats);
 
 }  // namespace pbrt

@@ -1593,7 +1593,14 @@ static int record_frame(PbrtPipeline* pp, cudaStream_t s, StageEvents* ev) {
 extern "C" {
 
 PBRT_API int pbrt_scene_create(const PbrtSceneDesc* d, PbrtScene** out) {
+  return pbrt_scene_create_ex(d, PBRT_BUILD_PREFER_FAST_TRACE, out);
+}
+
+PBRT_API int pbrt_scene_create_ex(const PbrtSceneDesc* d, uint32_t build_flags, PbrtScene** out) {
   if (!out || !d) return fail(PBRT_ERROR_INVALID_ARGUMENT, "scene: null argument");
+  if (build_flags & ~(uint32_t)PBRT_BUILD_PREFER_FAST_BUILD)
+    return fail(PBRT_ERROR_INVALID_ARGUMENT, "scene: unknown build flags 0x%x", build_flags);
+  const bool device_build = (build_flags & PBRT_BUILD_PREFER_FAST_BUILD) != 0;
   *out = nullptr;
   if (d->mesh_count == 0 || d->instance_count == 0 || !d->meshes || !d->instances || !d->materials)
     return fail(PBRT_ERROR_INVALID_ARGUMENT, "scene: needs meshes, instances and materials");
@@ -1713,19 +1720,34 @@ PBRT_API int pbrt_scene_create(const PbrtSceneDesc* d, PbrtScene** out) {
     }
   }
   std::vector<Node8> nodes;
-  std::vector<uint32_t> order;
-  build_bvh8(world.data(), total, nodes, order, &sc->stats);
+  std::vector<float4> tris;
+  float4* dtris = nullptr;
+  Node8* dnodes = nullptr;
+  if (device_build) {
+    // linear BVH built on the device, written there (bvh_gpu.cu)
+    const int bst = build_bvh8_device(world.data(), tri_inst.data(), tri_prim.data(), total, kStackSize - 3, &dnodes,
+                                      &dtris, &sc->stats);
+    if (bst) {
+      delete sc;
+      return bst;
+    }
+    sc->allocs.push_back(dnodes);
+    sc->allocs.push_back(dtris);
+  } else {
+    std::vector<uint32_t> order;
+    build_bvh8(world.data(), total, nodes, order, &sc->stats);
+    tris.resize(3 * total);
+    for (size_t s = 0; s < total; ++s) {
+      const uint32_t o = order[s];
+      const float* w = &world[9 * (size_t)o];
+      tris[3 * s + 0] = make_float4(w[0], w[1], w[2], bits_f(o));
+      tris[3 * s + 1] = make_float4(w[3], w[4], w[5], bits_f(tri_inst[o]));
+      tris[3 * s + 2] = make_float4(w[6], w[7], w[8], bits_f(tri_prim[o]));
+    }
+  }
   if (sc->stats.depth >= kStackSize - 2) {
     delete sc;
     return fail(PBRT_ERROR_UNSUPPORTED, "scene: BVH depth %d exceeds the traversal stack", sc->stats.depth);
-  }
-  std::vector<float4> tris(3 * total);
-  for (size_t s = 0; s < total; ++s) {
-    const uint32_t o = order[s];
-    const float* w = &world[9 * (size_t)o];
-    tris[3 * s + 0] = make_float4(w[0], w[1], w[2], bits_f(o));
-    tris[3 * s + 1] = make_float4(w[3], w[4], w[5], bits_f(tri_inst[o]));
-    tris[3 * s + 2] = make_float4(w[6], w[7], w[8], bits_f(tri_prim[o]));
   }
   // --- textures
   std::vector<DevTexture> texd(d->texture_count);
@@ -1767,8 +1789,6 @@ PBRT_API int pbrt_scene_create(const PbrtSceneDesc* d, PbrtScene** out) {
     light_sum[i] = make_float4(sx, sy, sz, ((sx + sy) + sz) + sw);
   }
   SceneView& v = sc->view;
-  float4* dtris = nullptr;
-  Node8* dnodes = nullptr;
   DevInstance* dinst = nullptr;
   DevMesh* dmesh = nullptr;
   DevMaterial* dmat = nullptr;
@@ -1777,8 +1797,8 @@ PBRT_API int pbrt_scene_create(const PbrtSceneDesc* d, PbrtScene** out) {
   float *dpos = nullptr, *dnor = nullptr, *duv = nullptr;
   uint32_t* didx = nullptr;
   DevTexture* dtex = nullptr;
-  if (!st) st = sc->up(&dtris, tris.data(), tris.size());
-  if (!st) st = sc->up(&dnodes, nodes.data(), nodes.size());
+  if (!st && !device_build) st = sc->up(&dtris, tris.data(), tris.size());
+  if (!st && !device_build) st = sc->up(&dnodes, nodes.data(), nodes.size());
   if (!st) st = sc->up(&dinst, inst.data(), inst.size());
   if (!st) st = sc->up(&dmesh, meshes.data(), meshes.size());
   if (!st) st = sc->up(&dmat, mats.data(), mats.size());

@@ -55,6 +55,7 @@ class PbrtStageTimes(C.Structure):
 H, P = C.c_void_p, C.POINTER
 _abi.add_signatures({
     "pbrt_scene_create": (C.c_int32, [P(PbrtSceneDesc), P(H)]),
+    "pbrt_scene_create_ex": (C.c_int32, [P(PbrtSceneDesc), C.c_uint32, P(H)]),
     "pbrt_scene_info": (C.c_int32, [H, P(PbrtSceneInfo)]),
     "pbrt_scene_trace_rays": (C.c_int32, [H, H, H, C.c_uint32, C.c_int32, H, H, H]),
     "pbrt_pipeline_create": (C.c_int32, [H, H, H, C.c_int32, P(H)]),
@@ -81,9 +82,16 @@ def col_major16(m) -> list:
 
 class SceneHandle(Handle):
     """The scene uploaded to HBM with its 8-wide BVH (RayTracingSceneDescriptorCreationVisitor output
-    plus the acceleration-structure build)."""
+    plus the acceleration-structure build).
 
-    def __init__(self, scene: Scene):
+    build: "fast_trace" (binned-SAH BVH built on the host, the default) or
+    "fast_build" (linear BVH built on the device; lower quality, same hits)."""
+
+    BUILDS = {"fast_trace": 0, "fast_build": 1}
+
+    def __init__(self, scene: Scene, build: str = "fast_trace"):
+        if build not in self.BUILDS:
+            raise ValueError(f"build must be one of {sorted(self.BUILDS)}, not {build!r}")
         keep = []  # host arrays alive for the duration of the call
 
         def arr(a, dt):
@@ -112,7 +120,7 @@ class SceneHandle(Handle):
         d = PbrtSceneDesc(len(scene.meshes), meshes, len(insts), insts, _ptr(opaque), _ptr(mats), len(scene.lights),
                           _ptr(lights), len(scene.textures), texs, _ptr(mt))
         h = C.c_void_p()
-        check(lib().pbrt_scene_create(C.byref(d), C.byref(h)))
+        check(lib().pbrt_scene_create_ex(C.byref(d), self.BUILDS[build], C.byref(h)))
         super().__init__(h)
         self.scene = scene
 
