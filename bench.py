@@ -1110,7 +1110,7 @@ def run_unet_layers(args):
 def run_bvh_build(args):
     """The two BVH builds side by side -- FAST_TRACE (binned SAH on the host,
     SAH-optimal collapse; the default) and FAST_BUILD (linear BVH on the
-    device) -- on the benchmark scene and the full-form 4.3M-triangle scene:
+    device, SAH-optimal or greedy collapse) -- on the benchmark scene and the full-form 4.3M-triangle scene:
     scene set-up and build time, tree size and depth, and what each tree
     costs a 1080p path-traced frame (frame ms by CUDA events over graph
     launches; traversal ms, nodes and triangles a ray from one profiled
@@ -1133,12 +1133,16 @@ def run_bvh_build(args):
         sc = make()
         cams = [orbit(sc, W, H, f) for f in range(16)]
         rows = {}
-        for build in ("fast_trace", "fast_build"):
+        for label, build, collapse in (("fast_trace", "fast_trace", None), ("fast_build", "fast_build", None),
+                                       ("fast_build_greedy", "fast_build", "greedy")):
             torch.cuda.synchronize()
+            if collapse:
+                os.environ["PBRT_BVH_COLLAPSE"] = collapse
             t0 = time.perf_counter()
             sh = vp.SceneHandle(sc, build=build)
             torch.cuda.synchronize()
             create_s = time.perf_counter() - t0
+            os.environ.pop("PBRT_BVH_COLLAPSE", None)
             info = sh.info()
             g = vp.GBuffer(W, H)
             illu = vp.IlluminationBufferDemodulatedFloat(W, H)
@@ -1165,7 +1169,7 @@ def run_bvh_build(args):
             set_cam(5)
             t = pipe.profile(pc, stream)
             rays = t.closest_rays + t.shadow_rays
-            rows[build] = {"scene_create_s": round(create_s, 3), "build_ms": round(info.build_ms, 1),
+            rows[label] = {"scene_create_s": round(create_s, 3), "build_ms": round(info.build_ms, 1),
                            "nodes": int(info.bvh_nodes), "depth": int(info.bvh_depth),
                            "frame_ms": round(frame_ms, 3),
                            "traversal_ms": round(t.trace_closest_ms + t.trace_shadow_ms, 3),

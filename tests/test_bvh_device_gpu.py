@@ -81,14 +81,18 @@ def test_duplicate_triangles_tie_to_the_lowest_key(cuda):
         assert np.array_equal(_hits(host, org, dirs, any_hit), _hits(dev, org, dirs, any_hit))
 
 
-def test_instanced_alpha_scene_hits_the_same(cuda):
+@pytest.mark.parametrize("collapse", ["sah", "greedy"])
+def test_instanced_alpha_scene_hits_the_same(cuda, collapse, monkeypatch):
     from vulkanpbrt_gb300 import scene as S
+
+    if collapse == "greedy":
+        monkeypatch.setenv("PBRT_BVH_COLLAPSE", "greedy")  # both builds: open the largest child until eight
 
     sc = S.instanced_field(seed=3, instances=120, unique_meshes=12, texture_size=64, alpha_fraction=0.5, radius=8.0)
     host, dev = _both(sc)
     hi, di = host.info(), dev.info()
     assert hi.triangle_count == di.triangle_count == sc.tri_count
-    print(f"instanced field, {sc.tri_count} triangles: host {hi.bvh_nodes} nodes depth {hi.bvh_depth} "
+    print(f"instanced field ({collapse} collapse), {sc.tri_count} triangles: host {hi.bvh_nodes} nodes depth {hi.bvh_depth} "
           f"{hi.build_ms:.1f} ms; device {di.bvh_nodes} nodes depth {di.bvh_depth} {di.build_ms:.1f} ms")
     org, dirs = _rays(200000, seed=5, lo=-8.0, hi=8.0)
     for any_hit in (False, True):

@@ -10,15 +10,18 @@
 // trade: a linear BVH over 63-bit Morton codes of the triangle centroids
 // (Karras, "Maximizing Parallelism in the Construction of BVHs, Octrees, and
 // k-d Trees", HPG 2012), its boxes by one bottom-up pass, then a
-// level-by-level collapse into 8-wide nodes (open the child with the largest
-// surface area until eight; subtrees of at most three triangles become
-// leaves, their triangles consecutive in Morton order). Closest hits do not
-// depend on the tree (ties go to the lowest triangle key, the flattening
-// index), so frames rendered over either build are bit-identical.
+// level-by-level collapse into 8-wide nodes (the SAH-optimal distribution
+// of Ylitie, Karras & Laine 2017, its programme evaluated in the same
+// bottom-up pass; or greedily, opening the child with the largest surface
+// area until eight), leaves of at most three triangles, consecutive in
+// Morton order. Closest hits do not depend on the tree (ties go to the
+// lowest triangle key, the flattening index), so frames rendered over either
+// build are bit-identical.
 #include <cub/device/device_radix_sort.cuh>
 
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -167,20 +170,100 @@ __global__ void __launch_bounds__(kThreads) k_radix_tree(const uint64_t* __restr
   last[i] = hi;
 }
 
-// Boxes, bottom-up: each leaf writes its triangle's box and climbs; of the
-// two threads reaching a node, the second (which sees the first's box
-// through L2) forms the union and goes on.
+// The SAH-optimal collapse's dynamic programme (Ylitie, Karras & Laine,
+// HPG 2017, section 3.1, as the host build runs it), per binary node m:
+// cost[m][i-1] = the cheapest way to represent m's subtree as at most i
+// slots of a wide node (i = 1..8); split[m][i-1] = k > 0: k slots to the
+// left child, i - k to the right; 0: as with i - 1 slots; -1: one slot (a
+// leaf of at most three triangles when leaf[m], else a wide node);
+// wsplit[m] = the left share of the 8-slot distribution of m's own wide node.
+struct WideDp {
+  float* cost;       // [2n - 1][8]
+  int8_t* split;     // [2n - 1][8]
+  uint8_t* leaf;     // [2n - 1]
+  uint8_t* wsplit;   // [2n - 1]
+  float prim_cost;   // a triangle test against a node visit (1)
+};
+
+__device__ __forceinline__ float box_area(float4 a, float4 c) {
+  const float dx = fmaxf(0.f, c.x - a.x), dy = fmaxf(0.f, c.y - a.y), dz = fmaxf(0.f, c.z - a.z);
+  return 2.f * (dx * dy + dy * dz + dz * dx);
+}
+
+__device__ void dp_node(const WideDp& dp, int m, int l, int r, int count, float area) {
+  constexpr float kInf = INFINITY;
+  float cl[8], cr[8];
+  const float4* pl = reinterpret_cast<const float4*>(dp.cost + 8 * (size_t)l);
+  const float4* pr = reinterpret_cast<const float4*>(dp.cost + 8 * (size_t)r);
+  const float4 l0 = __ldcg(pl), l1 = __ldcg(pl + 1), r0 = __ldcg(pr), r1 = __ldcg(pr + 1);
+  cl[0] = l0.x; cl[1] = l0.y; cl[2] = l0.z; cl[3] = l0.w; cl[4] = l1.x; cl[5] = l1.y; cl[6] = l1.z; cl[7] = l1.w;
+  cr[0] = r0.x; cr[1] = r0.y; cr[2] = r0.z; cr[3] = r0.w; cr[4] = r1.x; cr[5] = r1.y; cr[6] = r1.z; cr[7] = r1.w;
+  float dist[9];
+  int8_t arg[9];
+#pragma unroll
+  for (int j = 2; j <= 8; ++j) {
+    dist[j] = kInf;
+    arg[j] = 1;
+#pragma unroll
+    for (int k = 1; k < j; ++k) {
+      const float v = cl[k - 1] + cr[j - k - 1];
+      if (v < dist[j]) {
+        dist[j] = v;
+        arg[j] = (int8_t)k;
+      }
+    }
+  }
+  const float leafc = count <= kLeafMax ? area * dp.prim_cost * (float)count : kInf;
+  const float internal = area + dist[8];
+  float c[8];
+  int8_t sp[8];
+  c[0] = fminf(leafc, internal);
+  sp[0] = -1;
+#pragma unroll
+  for (int i = 2; i <= 8; ++i) {
+    if (dist[i] < c[i - 2]) {
+      c[i - 1] = dist[i];
+      sp[i - 1] = arg[i];
+    } else {
+      c[i - 1] = c[i - 2];
+      sp[i - 1] = 0;
+    }
+  }
+  float4* pc = reinterpret_cast<float4*>(dp.cost + 8 * (size_t)m);
+  pc[0] = make_float4(c[0], c[1], c[2], c[3]);
+  pc[1] = make_float4(c[4], c[5], c[6], c[7]);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) dp.split[8 * (size_t)m + i] = sp[i];
+  dp.leaf[m] = leafc <= internal ? 1 : 0;
+  dp.wsplit[m] = (uint8_t)arg[8];
+}
+
+// Boxes (and, with dp.cost set, the collapse's programme), bottom-up: each
+// leaf writes its triangle's box and climbs; of the two threads reaching a
+// node, the second (which sees the first's results through L2) forms the
+// node's and goes on.
 __global__ void __launch_bounds__(kThreads) k_boxes(const float* __restrict__ world, const uint32_t* __restrict__ vals,
                                                     int n, const int* __restrict__ left, const int* __restrict__ right,
-                                                    const int* __restrict__ parent, float4* lo, float4* hi,
-                                                    int* __restrict__ flag) {
+                                                    const int* __restrict__ parent, const int* __restrict__ first,
+                                                    const int* __restrict__ last, float4* lo, float4* hi,
+                                                    int* __restrict__ flag, WideDp dp) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   float a[3], b[3];
   tri_box(world + 9 * (size_t)vals[i], a, b);
   const int leaf = n - 1 + i;
-  lo[leaf] = make_float4(a[0], a[1], a[2], 0.f);
-  hi[leaf] = make_float4(b[0], b[1], b[2], 0.f);
+  const float4 bl = make_float4(a[0], a[1], a[2], 0.f), bh = make_float4(b[0], b[1], b[2], 0.f);
+  lo[leaf] = bl;
+  hi[leaf] = bh;
+  if (dp.cost) {
+    const float lc = box_area(bl, bh) * dp.prim_cost;
+    float4* pc = reinterpret_cast<float4*>(dp.cost + 8 * (size_t)leaf);
+    pc[0] = make_float4(lc, lc, lc, lc);
+    pc[1] = make_float4(lc, lc, lc, lc);
+    for (int k = 0; k < 8; ++k) dp.split[8 * (size_t)leaf + k] = -1;
+    dp.leaf[leaf] = 1;
+    dp.wsplit[leaf] = 1;
+  }
   int node = parent[leaf];
   for (int guard = 0; node >= 0 && guard < n; ++guard) {
     __threadfence();
@@ -188,8 +271,11 @@ __global__ void __launch_bounds__(kThreads) k_boxes(const float* __restrict__ wo
     __threadfence();
     const int l = left[node], r = right[node];
     const float4 l0 = __ldcg(&lo[l]), l1 = __ldcg(&hi[l]), r0 = __ldcg(&lo[r]), r1 = __ldcg(&hi[r]);
-    lo[node] = make_float4(fminf(l0.x, r0.x), fminf(l0.y, r0.y), fminf(l0.z, r0.z), 0.f);
-    hi[node] = make_float4(fmaxf(l1.x, r1.x), fmaxf(l1.y, r1.y), fmaxf(l1.z, r1.z), 0.f);
+    const float4 nl = make_float4(fminf(l0.x, r0.x), fminf(l0.y, r0.y), fminf(l0.z, r0.z), 0.f);
+    const float4 nh = make_float4(fmaxf(l1.x, r1.x), fmaxf(l1.y, r1.y), fmaxf(l1.z, r1.z), 0.f);
+    lo[node] = nl;
+    hi[node] = nh;
+    if (dp.cost) dp_node(dp, node, l, r, last[node] - first[node] + 1, box_area(nl, nh));
     node = parent[node];
   }
 }
@@ -202,11 +288,7 @@ struct Tree {
   __device__ int count(int b) const { return is_leaf(b) ? 1 : last[b] - first[b] + 1; }
   __device__ int pos(int b) const { return is_leaf(b) ? b - (n - 1) : first[b]; }
   __device__ bool leaf_slot(int b) const { return is_leaf(b) || count(b) <= kLeafMax; }
-  __device__ float area(int b) const {
-    const float4 a = lo[b], c = hi[b];
-    const float dx = fmaxf(0.f, c.x - a.x), dy = fmaxf(0.f, c.y - a.y), dz = fmaxf(0.f, c.z - a.z);
-    return 2.f * (dx * dy + dy * dz + dz * dx);
-  }
+  __device__ float area(int b) const { return box_area(lo[b], hi[b]); }
 };
 
 struct Out {
@@ -226,7 +308,7 @@ __device__ __forceinline__ uint8_t exponent_for(double extent) {
 }
 
 // One level of the collapse: item = (binary node, its wide node's index).
-__global__ void __launch_bounds__(128) k_collapse(Tree t, const float* __restrict__ world,
+__global__ void __launch_bounds__(128) k_collapse(Tree t, WideDp dp, const float* __restrict__ world,
                                                   const uint32_t* __restrict__ vals, const uint32_t* __restrict__ inst,
                                                   const uint32_t* __restrict__ prim, const uint2* __restrict__ items,
                                                   int count, uint2* __restrict__ next, Out o) {
@@ -236,8 +318,36 @@ __global__ void __launch_bounds__(128) k_collapse(Tree t, const float* __restric
   const uint32_t out_index = items[it].y;
   int ch[8];
   int nch = 0;
+  // a slot is a leaf: the programme's choice, else any subtree of <= 3 triangles
+  auto is_leaf_slot = [&](int c) { return dp.cost ? (t.is_leaf(c) || dp.leaf[c] != 0) : t.leaf_slot(c); };
   if (t.leaf_slot(b)) {
     ch[nch++] = b;
+  } else if (dp.cost) {
+    // the programme's eight-slot distribution (the host build's slots())
+    int stn[8], stj[8], sp = 0;
+    const int ws = dp.wsplit[b];
+    stn[sp] = t.right[b];
+    stj[sp++] = 8 - ws;
+    stn[sp] = t.left[b];
+    stj[sp++] = ws;
+    while (sp > 0 && nch < 8) {
+      --sp;
+      const int m = stn[sp], j = stj[sp];
+      const int s = (j == 1 || t.is_leaf(m)) ? -1 : dp.split[8 * (size_t)m + (j - 1)];
+      if (s < 0) {
+        ch[nch++] = m;
+      } else if (s == 0) {
+        stn[sp] = m;
+        stj[sp++] = j - 1;
+      } else if (sp + 2 <= 8) {
+        stn[sp] = t.right[m];
+        stj[sp++] = j - s;
+        stn[sp] = t.left[m];
+        stj[sp++] = s;
+      } else {
+        ch[nch++] = m;  // cannot happen: the entries' slot counts sum to at most 8
+      }
+    }
   } else {
     ch[nch++] = t.left[b];
     ch[nch++] = t.right[b];
@@ -289,7 +399,7 @@ __global__ void __launch_bounds__(128) k_collapse(Tree t, const float* __restric
   int n_inner = 0, n_tris = 0;
   for (int s = 0; s < 8; ++s) {
     if (!(used >> s & 1u)) continue;
-    if (t.leaf_slot(slot_child[s]))
+    if (is_leaf_slot(slot_child[s]))
       n_tris += t.count(slot_child[s]);
     else
       ++n_inner;
@@ -333,7 +443,7 @@ __global__ void __launch_bounds__(128) k_collapse(Tree t, const float* __restric
       nd.qlo[a][s] = (uint8_t)fmin(255.0, fmax(0.0, ql));
       nd.qhi[a][s] = (uint8_t)fmin(255.0, fmax(0.0, qh));
     }
-    if (!t.leaf_slot(c)) {
+    if (!is_leaf_slot(c)) {
       nd.imask |= (uint8_t)(1u << s);
       nd.meta[s] = 0x80;
       const unsigned q = atomicAdd(&o.counters[2], 1u);
@@ -440,7 +550,19 @@ int build_bvh8_device(const float* world_h, const uint32_t* inst_h, const uint32
   PBRT_CUDA(cudaMemset(parent, 0xff, nodes_total * sizeof(int)));
   PBRT_CUDA(cudaMemset(flag, 0, (size_t)n * sizeof(int)));
   if (n > 1) k_radix_tree<<<(n - 1 + kThreads - 1) / kThreads, kThreads>>>(keys, n, left, right, parent, first, last);
-  k_boxes<<<nblk, kThreads>>>(world, vals, n, left, right, parent, lo, hi, flag);
+  // the SAH-optimal collapse (default) or, with PBRT_BVH_COLLAPSE=greedy,
+  // opening the largest child until eight -- the host build's two modes
+  WideDp dp{nullptr, nullptr, nullptr, nullptr, 0.3f};
+  const char* mode = std::getenv("PBRT_BVH_COLLAPSE");
+  if (const char* pc = std::getenv("PBRT_BVH_PRIM_COST")) dp.prim_cost = (float)std::atof(pc);
+  if (!(mode && std::strcmp(mode, "greedy") == 0)) {
+    if (!st) st = ar.get(&dp.cost, 8 * nodes_total);
+    if (!st) st = ar.get(&dp.split, 8 * nodes_total);
+    if (!st) st = ar.get(&dp.leaf, nodes_total);
+    if (!st) st = ar.get(&dp.wsplit, nodes_total);
+    if (st) return st;
+  }
+  k_boxes<<<nblk, kThreads>>>(world, vals, n, left, right, parent, first, last, lo, hi, flag, dp);
   if ((st = check_launch("device BVH build: tree"))) return st;
   // collapse, one launch a level from the root (binary node 0: internal,
   // or the only leaf when n == 1) into wide node 0
@@ -455,7 +577,7 @@ int build_bvh8_device(const float* world_h, const uint32_t* inst_h, const uint32
     if (levels > max_depth)
       return fail(PBRT_ERROR_UNSUPPORTED, "device BVH build: depth above %d (the traversal stack)", max_depth);
     PBRT_CUDA(cudaMemset(counters + 2, 0, sizeof(unsigned)));
-    k_collapse<<<(level_items + 127) / 128, 128>>>(tr, world, vals, inst, prim, items_a, level_items, items_b, o);
+    k_collapse<<<(level_items + 127) / 128, 128>>>(tr, dp, world, vals, inst, prim, items_a, level_items, items_b, o);
     if ((st = check_launch("device BVH build: collapse"))) return st;
     unsigned nxt = 0;
     PBRT_CUDA(cudaMemcpy(&nxt, counters + 2, sizeof(unsigned), cudaMemcpyDeviceToHost));
