@@ -65,11 +65,15 @@ def parse():
     ap.add_argument("--sort-rays", action="store_true", help="sort extension / shadow rays before traversal")
     ap.add_argument("--separate-shadow", action="store_true",
                     help="trace shadow rays in their own launch (default: merged into the next bounce's launch)")
-    ap.add_argument("--workload", default="frame1080p", choices=["frame1080p", "batch64", "unet_layers", "full", "bvh_build"],
+    ap.add_argument("--workload", default="frame1080p",
+                    choices=["frame1080p", "batch64", "unet_layers", "full", "bvh_build"],
                     help="batch64: 64 uneven render requests in one graph launch; unet_layers: per-convolution "
                          "times of the U-Net; full: 4K 4 spp frames of a 4M-triangle scene (FP8 network, gate, "
-                         "BMFR with the FP64 re-solve) beside 16 concurrent 1080p requests (none of these is the "
-                         "headline line)")
+                         "BMFR with the FP64 re-solve) beside 16 concurrent 1080p requests; bvh_build: host and "
+                         "device BVH builds side by side (none of these is the headline line)")
+    ap.add_argument("--bvh", default="fast_trace", choices=["fast_trace", "fast_build"],
+                    help="BVH build of the workload's scenes: binned SAH on the host (fast_trace) or the linear "
+                         "BVH built on the device (fast_build)")
     ap.add_argument("--frames", type=int, default=60, help="full: frames of the camera path")
     ap.add_argument("--relmse-frames", default="59", help="full: comma-separated frames whose relMSE is measured")
     ap.add_argument("--full-ref-spp", type=int, default=1024, help="full: samples of each 4K relMSE reference")
@@ -426,7 +430,7 @@ def run_gb300(args):
 
     W, H = args.width, args.height
     sc = workload(args, seed_offset=0)  # every rank renders its own request stream of the same scene
-    sh = vp.SceneHandle(sc)
+    sh = vp.SceneHandle(sc, build=args.bvh)
     info = sh.info()
     g = vp.GBuffer(W, H)
     illu = vp.IlluminationBufferDemodulatedFloat(W, H)
@@ -659,12 +663,13 @@ def run_gb300(args):
                                                             "e4m3_layers": [n for (n, *_), f in
                                                                             zip(_conv_table(), fp8_layers) if f]},
             "relmse": quality,
-            "bvh": {"nodes": int(info.bvh_nodes), "depth": int(info.bvh_depth), "build_ms": info.build_ms},
+            "bvh": {"build": args.bvh, "nodes": int(info.bvh_nodes), "depth": int(info.bvh_depth),
+                    "build_ms": info.build_ms},
         }
         if world == 1 and not args.no_batch:
             # the 64-request batch, measured here too (fixed tuning, 3 submits
             # after 1): BVH queries of requests of 10k-2M triangles each
-            bl = batch64_measure(3, 1, tune=False)
+            bl = batch64_measure(3, 1, tune=False, bvh=args.bvh)
             line["batch64"] = {k: bl[k] for k in ("ms_per_batch", "requests_per_s", "pixel_samples_per_s",
                                                   "grays_per_s", "tuning", "steps", "warmup")}
         print(json.dumps(line), flush=True)
@@ -692,12 +697,13 @@ def run_batch(args):
     log-uniform 256^2..1080p, 1/2/4/8/16 spp, depth 4-8, accumulator + BMFR
     each) in one graph launch; the autotuner picks the chain count and the
     tracer's launch shape."""
-    print(json.dumps(batch64_measure(args.steps, args.warmup, tune=True)), flush=True)
+    print(json.dumps(batch64_measure(args.steps, args.warmup, tune=True, bvh=args.bvh)), flush=True)
 
 
-def batch64_measure(steps, warmup, tune=True):
+def batch64_measure(steps, warmup, tune=True, bvh="fast_trace"):
     """The 64-request batch timed over `steps` submits after `warmup`; tune:
-    run the autotuner first, else take BATCH64_TUNING. Returns the line."""
+    run the autotuner first, else take BATCH64_TUNING; bvh: the scenes' BVH
+    build. Returns the line."""
     import torch
 
     from vulkanpbrt_gb300 import build as B
@@ -711,7 +717,7 @@ def batch64_measure(steps, warmup, tune=True):
     t0 = time.perf_counter()
     for i in range(64):
         sc = batch_scene(rng, 5000 + i)
-        sh = vp.SceneHandle(sc)
+        sh = vp.SceneHandle(sc, build=bvh)
         side = float(np.exp(rng.uniform(np.log(256 * 256), np.log(1920 * 1080))))
         aspect = rng.uniform(1.0, 16 / 9)
         H = max(64, int(np.sqrt(side / aspect)) // 32 * 32)
@@ -759,7 +765,7 @@ def batch64_measure(steps, warmup, tune=True):
     return {"metric": "batched render requests (64 per graph launch)", "value": 1e3 / ms, "unit": "batches/s",
             "ms_per_batch": ms, "requests_per_s": 64e3 / ms, "pixel_samples_per_s": pixels_spp / ms * 1e3,
             "grays_per_s": rays / ms / 1e6, "rays_per_batch": rays, "tuning": best, "autotune_best_ms": best_ms,
-            "setup_s": setup_s, "autotune_s": tune_s, "steps": steps, "warmup": warmup,
+            "setup_s": setup_s, "autotune_s": tune_s, "steps": steps, "warmup": warmup, "bvh": bvh,
             "config": {"requests": 64, "scenes": "own seeded scene each, 10k-2M tris (log-uniform)",
                        "resolution": "log-uniform 256^2..1080p", "spp": "uniform {1,2,4,8,16}", "depth": "4-8",
                        "denoiser": "accumulate + BMFR 32x32 per request"}}
@@ -788,7 +794,7 @@ def run_full(args):
     W, H, spp = 3840, 2160, 4
     t0 = time.perf_counter()
     sc = S.instanced_field(seed=0, instances=8000, point_lights=30)
-    sh = vp.SceneHandle(sc)
+    sh = vp.SceneHandle(sc, build=args.bvh)
     info = sh.info()
     g = vp.GBuffer(W, H)
     illu = vp.IlluminationBufferDemodulatedFloat(W, H)
@@ -804,7 +810,7 @@ def run_full(args):
     batch, keep = vp.Batch(), []
     for i in range(16):
         rsc = batch_scene(rng, 9000 + i)
-        rsh = vp.SceneHandle(rsc)
+        rsh = vp.SceneHandle(rsc, build=args.bvh)
         rg, ri = vp.GBuffer(1920, 1080), vp.IlluminationBufferDemodulatedFloat(1920, 1080)
         rp = vp.PBRTPipeline(rsh, rg, ri, True, max_recursion_depth=args.max_depth, min_recursion_depth=args.min_depth)
         ra = vp.Accumulator(rg, ri, separate_matrices=True)
