@@ -324,12 +324,14 @@ class Accumulator : public Inherit<Handle, Accumulator> {
 
 // The scene the pipeline traces: stands for the vsg scene graph after
 // RayTracingSceneDescriptorCreationVisitor and the acceleration-structure
-// build (pbrt_scene_create builds the 8-wide BVH).
+// build (pbrt_scene_create_ex builds the 8-wide BVH: binned SAH on the host
+// by default, or PBRT_BUILD_PREFER_FAST_BUILD for the device build, as a
+// Vulkan acceleration-structure build's PREFER_FAST_TRACE / FAST_BUILD flags).
 class Scene : public Inherit<Handle, Scene> {
  public:
-  explicit Scene(const PbrtSceneDesc& desc) {
+  explicit Scene(const PbrtSceneDesc& desc, uint32_t build_flags = PBRT_BUILD_PREFER_FAST_TRACE) {
     PbrtScene* s = nullptr;
-    check(pbrt_scene_create(&desc, &s), "Scene");
+    check(pbrt_scene_create_ex(&desc, build_flags, &s), "Scene");
     handle_ = s;
   }
   PbrtSceneInfo info() const {
