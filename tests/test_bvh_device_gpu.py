@@ -81,12 +81,16 @@ def test_duplicate_triangles_tie_to_the_lowest_key(cuda):
         assert np.array_equal(_hits(host, org, dirs, any_hit), _hits(dev, org, dirs, any_hit))
 
 
-@pytest.mark.parametrize("collapse", ["sah", "greedy"])
+@pytest.mark.parametrize("collapse", ["sah", "greedy", "sah_triangle_cost_1"])
 def test_instanced_alpha_scene_hits_the_same(cuda, collapse, monkeypatch):
     from vulkanpbrt_gb300 import scene as S
 
     if collapse == "greedy":
         monkeypatch.setenv("PBRT_BVH_COLLAPSE", "greedy")  # both builds: open the largest child until eight
+    if collapse == "sah_triangle_cost_1":
+        # triangles as dear as node visits: subtrees of 2-3 triangles become
+        # wide nodes of single-triangle leaves where that is cheaper
+        monkeypatch.setenv("PBRT_BVH_PRIM_COST", "1.0")
 
     sc = S.instanced_field(seed=3, instances=120, unique_meshes=12, texture_size=64, alpha_fraction=0.5, radius=8.0)
     host, dev = _both(sc)

@@ -320,7 +320,10 @@ __global__ void __launch_bounds__(128) k_collapse(Tree t, WideDp dp, const float
   int nch = 0;
   // a slot is a leaf: the programme's choice, else any subtree of <= 3 triangles
   auto is_leaf_slot = [&](int c) { return dp.cost ? (t.is_leaf(c) || dp.leaf[c] != 0) : t.leaf_slot(c); };
-  if (t.leaf_slot(b)) {
+  // one leaf slot: the root when it is a leaf; any other wide node was made
+  // for a subtree that is not one (with the programme, a subtree of <= 3
+  // triangles can be cheaper as a wide node of several leaves)
+  if (is_leaf_slot(b)) {
     ch[nch++] = b;
   } else if (dp.cost) {
     // the programme's eight-slot distribution (the host build's slots())
@@ -565,25 +568,40 @@ int build_bvh8_device(const float* world_h, const uint32_t* inst_h, const uint32
   k_boxes<<<nblk, kThreads>>>(world, vals, n, left, right, parent, first, last, lo, hi, flag, dp);
   if ((st = check_launch("device BVH build: tree"))) return st;
   // collapse, one launch a level from the root (binary node 0: internal,
-  // or the only leaf when n == 1) into wide node 0
-  const unsigned init[8] = {1u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
-  PBRT_CUDA(cudaMemcpy(counters, init, sizeof(init), cudaMemcpyHostToDevice));
-  const uint2 root = make_uint2(0u, 0u);
-  PBRT_CUDA(cudaMemcpy(items_a, &root, sizeof(root), cudaMemcpyHostToDevice));
+  // or the only leaf when n == 1) into wide node 0. The SAH cost does not
+  // see the traversal stack: on a deep, unbalanced stretch of the linear
+  // tree the programme can keep one inner slot a level, so a collapse that
+  // runs past max_depth is redone greedily (which opens the largest child).
   Tree tr{n, left, right, first, last, lo, hi};
   Out o{nodes, tris, order, counters, (uint32_t)n};
-  int level_items = 1, levels = 0;
-  while (level_items > 0) {
-    if (levels > max_depth)
+  int levels = 0;
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    const unsigned init[8] = {1u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+    PBRT_CUDA(cudaMemcpy(counters, init, sizeof(init), cudaMemcpyHostToDevice));
+    const uint2 root = make_uint2(0u, 0u);
+    PBRT_CUDA(cudaMemcpy(items_a, &root, sizeof(root), cudaMemcpyHostToDevice));
+    int level_items = 1;
+    levels = 0;
+    bool too_deep = false;
+    while (level_items > 0) {
+      if (levels > max_depth) {
+        too_deep = true;
+        break;
+      }
+      PBRT_CUDA(cudaMemset(counters + 2, 0, sizeof(unsigned)));
+      k_collapse<<<(level_items + 127) / 128, 128>>>(tr, dp, world, vals, inst, prim, items_a, level_items, items_b,
+                                                     o);
+      if ((st = check_launch("device BVH build: collapse"))) return st;
+      unsigned nxt = 0;
+      PBRT_CUDA(cudaMemcpy(&nxt, counters + 2, sizeof(unsigned), cudaMemcpyDeviceToHost));
+      level_items = (int)nxt;
+      std::swap(items_a, items_b);
+      ++levels;
+    }
+    if (!too_deep) break;
+    if (!dp.cost || attempt == 1)
       return fail(PBRT_ERROR_UNSUPPORTED, "device BVH build: depth above %d (the traversal stack)", max_depth);
-    PBRT_CUDA(cudaMemset(counters + 2, 0, sizeof(unsigned)));
-    k_collapse<<<(level_items + 127) / 128, 128>>>(tr, dp, world, vals, inst, prim, items_a, level_items, items_b, o);
-    if ((st = check_launch("device BVH build: collapse"))) return st;
-    unsigned nxt = 0;
-    PBRT_CUDA(cudaMemcpy(&nxt, counters + 2, sizeof(unsigned), cudaMemcpyDeviceToHost));
-    level_items = (int)nxt;
-    std::swap(items_a, items_b);
-    ++levels;
+    dp.cost = nullptr;  // greedy from here
   }
   unsigned c[8];
   PBRT_CUDA(cudaMemcpy(c, counters, sizeof(c), cudaMemcpyDeviceToHost));
