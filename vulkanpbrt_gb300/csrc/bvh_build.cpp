@@ -61,6 +61,10 @@ struct Builder {
   std::vector<uint32_t> idx;
   std::vector<BNode> nodes;
   std::atomic<uint32_t> next{0};
+  // binary leaves: up to 3 triangles, or (with the SAH-optimal collapse)
+  // single triangles, the collapse then choosing which subtrees of <= 3
+  // triangles become leaves
+  uint32_t binary_leaf = (uint32_t)kMaxLeaf;
 
   uint32_t alloc() { return next.fetch_add(1); }
 
@@ -74,7 +78,7 @@ struct Builder {
     nd.box = box;
     nd.begin = begin;
     nd.count = count;
-    if (count <= (uint32_t)kMaxLeaf) return;  // leaves hold up to 3 triangles
+    if (count <= binary_leaf) return;
     // Binned SAH over all three axes.
     double best_cost = std::numeric_limits<double>::infinity();
     int best_axis = -1, best_split = -1;
@@ -395,19 +399,24 @@ void build_bvh8(const float* v, size_t n, std::vector<Node8>& nodes, std::vector
     b.idx[i] = (uint32_t)i;
   }
   b.nodes.resize(std::max<size_t>(1, 2 * n));
+  // PBRT_BVH_COLLAPSE=greedy: open the largest child until 8 (the default is
+  // the SAH-optimal collapse)
+  const char* mode = std::getenv("PBRT_BVH_COLLAPSE");
+  const bool greedy = mode && std::strcmp(mode, "greedy") == 0;
+  if (!greedy) {
+    const char* bl = std::getenv("PBRT_BVH_BINARY_LEAF");
+    b.binary_leaf = (uint32_t)std::min(kMaxLeaf, std::max(1, bl ? std::atoi(bl) : 1));
+  }
   uint32_t root = b.alloc();
   b.build(root, 0, (uint32_t)n);
   nodes.clear();
   tri_order.clear();
   tri_order.reserve(n);
   nodes.resize(1);
-  // PBRT_BVH_COLLAPSE=greedy: open the largest child until 8 (the default is
-  // the SAH-optimal collapse)
-  const char* mode = std::getenv("PBRT_BVH_COLLAPSE");
   WideDP dp(b);
   if (const char* pc = std::getenv("PBRT_BVH_PRIM_COST")) dp.kPrim = (float)std::atof(pc);
   Collapser c{b, nodes, tri_order, {}};
-  if (!(mode && std::strcmp(mode, "greedy") == 0) && b.nodes[root].left >= 0) {
+  if (!greedy && b.nodes[root].left >= 0) {
     dp.solve(root);
     c.dp = &dp;
   }
