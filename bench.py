@@ -961,7 +961,8 @@ def full_relmse(args, vp, pipe, g, illu, bmfr, neural, pc, pc_den, stream):
     return res
 
 
-UNET_KERNELS = ("bf16_tcgen05", "bf16_mma", "fp8_tcgen05", "fp8_mma", "bf16_tcgen05_gather", "fp8_tcgen05_gather")
+UNET_KERNELS = ("bf16_tcgen05", "bf16_mma", "fp8_tcgen05", "fp8_mma", "bf16_tcgen05_gather", "fp8_tcgen05_gather",
+                "bf16_tcgen05_planes")
 
 
 def _stage_ms(fn, stream, reps=10):
@@ -1039,10 +1040,13 @@ def unet_layer_times(width, height, reps, layers, kernels):
             "bf16_tcgen05_gather": lambda: nn.conv3x3_umma(x1, wb, b, x2=x2, relu=True, out=out, box=False),
             "fp8_tcgen05_gather": lambda: nn.conv3x3_fp8(x1, w8, ws, xs, b, x2=x2, relu=True, out=out, kernel="umma",
                                                          box=False),
+            # the first input's halo as 8-channel planes instead of swizzled pixel rows
+            "bf16_tcgen05_planes": lambda: nn.conv3x3_umma(x1, wb, b, x2=x2, relu=True, out=out, swizzle=False),
         }
         t = {}
         for k in UNET_KERNELS:
-            if k not in kernels or (k.endswith("_gather") and not c2):
+            swz = c1 in (16, 32) and not c2 and cout in (32, 48)  # the swizzled form applies
+            if k not in kernels or (k.endswith("_gather") and not c2) or (k.endswith("_planes") and not swz):
                 t[k] = None
                 continue
             try:

@@ -531,7 +531,9 @@ PBRT_API int pbrt_nn_conv3x3_fp8(const void* x1, int32_t c1, const void* x2, int
  * bit 1: the per-tile kernel only, bit 2: no TMA, bit 3: the single-role
  * persistent kernel, bit 4: the upsampled second input gathered with
  * cp.async (default: its half-resolution box by TMA, expanded in shared
- * memory, where two stages of it fit). */
+ * memory, where two stages of it fit), bit 5: the first input's halo as
+ * 8-channel planes (default for a single input of 16 or 32 channels and
+ * cout 32 or 48: whole pixels by one swizzled TMA row each). */
 PBRT_API int pbrt_nn_conv3x3_umma(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* w,
                                   const float* bias, void* y, int32_t n, int32_t h, int32_t w_px, int32_t cout,
                                   int32_t flags, pbrt_stream_t stream);
@@ -539,7 +541,8 @@ PBRT_API int pbrt_nn_conv3x3_umma(const void* x1, int32_t c1, const void* x2, in
  * also writes the 2x2 average pooling of its BF16 output y into pooled
  * ([n][h/2][wd/2][cout], the same bits as pbrt_nn_avgpool2 of y): the
  * encoder's pooling fused into the producing convolution's epilogue. Needs
- * h % 16 == 0 and wd % 8 == 0 (else PBRT_ERROR_UNSUPPORTED). */
+ * h % 16 == 0 and wd % 8 == 0 (else PBRT_ERROR_UNSUPPORTED). flags bit 0:
+ * ReLU, bit 5: as pbrt_nn_conv3x3_umma. */
 PBRT_API int pbrt_nn_conv3x3_umma_pooled(const void* x1, int32_t c1, const void* w, const float* bias, void* y,
                                          void* pooled, int32_t n, int32_t h, int32_t wd, int32_t cout, int32_t flags,
                                          pbrt_stream_t stream);
@@ -708,9 +711,11 @@ PBRT_API int pbrt_neural_set_precision(PbrtNeural* nd, int32_t bits);
 PBRT_API int pbrt_neural_fp8_layers(const PbrtNeural* nd, int32_t* mask, int32_t count);
 PBRT_API int pbrt_neural_set_fp8_layers(PbrtNeural* nd, const int32_t* mask, int32_t count);
 /* Per-layer convolution kernel: 0 = warp-level mma.sync kernels, 1 =
- * tcgen05 (tensor memory, TMA). autotune (run by the first dispatch when no
- * choice was set) times both for every layer on the current inputs and
- * keeps the faster (stream-synchronising); conv_kernels reads the choice
+ * tcgen05 (tensor memory, TMA; the first input's halo as swizzled pixel rows
+ * for a single input of 16 or 32 channels and 32 or 48 out), 2 = tcgen05
+ * with that halo as 8-channel planes (the same bits as 1). autotune (run by the first dispatch
+ * when no choice was set) times them for every layer on the current inputs
+ * and keeps the fastest (stream-synchronising); conv_kernels reads the choice
  * (18 entries, layer order of vulkanpbrt_gb300/kpunet.py), set_conv_kernels
  * fixes it. */
 PBRT_API int pbrt_neural_autotune(PbrtNeural* nd, pbrt_stream_t stream);

@@ -60,8 +60,9 @@ def test_native_forward_equals_training_forward(cuda):
     want = ws.forward(kinds)[0, :H, :W].cpu()
     torch.cuda.synchronize()
     assert torch.equal(got, want)
-    # a fixed choice: every layer on the tcgen05 kernel, then every layer on mma.sync
-    for kind in ("umma", "mma"):
+    # a fixed choice: every layer on the tcgen05 kernel (swizzled or plane
+    # halos), then every layer on mma.sync
+    for kind in ("umma", "umma_planes", "mma"):
         nd.set_conv_kernels([kind] * 18)
         nd.dispatch()
         torch.cuda.synchronize()

@@ -1,7 +1,9 @@
 """The tcgen05 convolutions (accumulator in tensor memory; the per-tile
 form, and the persistent form with its input halo from a TMA load or from
-cp.async gathers; the warp-specialised form with the upsampled second input
-from a TMA load of its half-resolution box or from cp.async gathers) against torch's FP32 conv2d on the same BF16 operands:
+cp.async gathers; the warp-specialised form with the first input's halo as
+swizzled whole-pixel rows or 8-channel planes, and the upsampled second
+input from a TMA load of its half-resolution box or from cp.async gathers)
+against torch's FP32 conv2d on the same BF16 operands:
 within one BF16 ulp (4e-3) of the output scale, no error flag from their
 bounded waits. Larger images exercise the persistent form's tile loop."""
 import pytest
@@ -15,7 +17,7 @@ pytestmark = pytest.mark.gpu
                                              (1, 34, 46, 32, 48, 32), (2, 136, 240, 32, 48, 32),
                                              (2, 128, 256, 48, 64, 48),
                                              (1, 128, 200, 16, 0, 32)])
-@pytest.mark.parametrize("mode", ["ws", "ws_nobox", "ws_gather", "tma", "persistent", "tile"])
+@pytest.mark.parametrize("mode", ["ws", "ws_planes", "ws_nobox", "ws_gather", "tma", "persistent", "tile"])
 def test_conv3x3_umma_forward(cuda, n, h, w, c1, c2, cout, mode):
     import torch
 
@@ -27,8 +29,8 @@ def test_conv3x3_umma_forward(cuda, n, h, w, c1, c2, cout, mode):
     x2 = torch.randn(n, h // 2, w // 2, c2, generator=g).bfloat16().to(cuda) if c2 else None
     wt = (torch.randn(cout, 9, c1 + c2, generator=g) * 0.1).bfloat16().to(cuda)
     b = torch.randn(cout, generator=g).float().to(cuda)
-    kw = dict(persistent=mode != "tile", tma=mode in ("ws", "ws_nobox", "tma"), specialised=mode.startswith("ws"),
-              box=mode != "ws_nobox")
+    kw = dict(persistent=mode != "tile", tma=mode in ("ws", "ws_planes", "ws_nobox", "tma"),
+              specialised=mode.startswith("ws"), box=mode != "ws_nobox", swizzle=mode != "ws_planes")
     y = nn.conv3x3_umma(x1, wt, b, x2=x2, relu=False, **kw)
     yr = nn.conv3x3_umma(x1, wt, b, x2=x2, relu=True, **kw)
     assert nn.umma_status() == 0
@@ -37,6 +39,10 @@ def test_conv3x3_umma_forward(cuda, n, h, w, c1, c2, cout, mode):
     print(f"umma conv rel err {rel:.2e}")
     assert ok
     assert _close(yr, ref.clamp_min(0), 4e-3)[1]
+    if mode == "ws":
+        # the first input's halo as swizzled pixel rows (default) or as
+        # 8-channel planes: the same operands, MMAs and order, the same bits
+        assert torch.equal(y, nn.conv3x3_umma(x1, wt, b, x2=x2, relu=False, **dict(kw, swizzle=False)))
 
 
 @pytest.mark.parametrize("c1,c2", [(32, 48), (32, 0)])
@@ -62,6 +68,8 @@ def test_conv3x3_umma_full_frame(cuda, c1, c2):
     assert ok
     if c2:  # the upsampled input's TMA box and its cp.async gathers: the same bits
         assert torch.equal(y, nn.conv3x3_umma(x1, wt, b, x2=x2, box=False))
+    # swizzled pixel rows against 8-channel planes for the first input: the same bits
+    assert torch.equal(y, nn.conv3x3_umma(x1, wt, b, x2=x2, swizzle=False))
 
 
 @pytest.mark.parametrize("n,h,w,c1,cout", [(1, 32, 48, 16, 32), (2, 64, 40, 32, 48), (1, 48, 64, 48, 64),
@@ -86,3 +94,5 @@ def test_conv3x3_umma_pooled(cuda, n, h, w, c1, cout):
     assert nn.umma_status() == 0
     assert torch.equal(y, y_plain)
     assert torch.equal(pooled, p_ref)
+    y_pl, pooled_pl = nn.conv3x3_umma_pooled(x1, wt, b, relu=True, swizzle=False)
+    assert torch.equal(y, y_pl) and torch.equal(pooled, pooled_pl)

@@ -137,8 +137,11 @@ int conv_layer(PbrtNeural* nd, int i, const bf16* x, bool fp8, cudaStream_t s, b
   int st;
   // an encoder level's second convolution on the tcgen05 kernel pools its
   // output in the epilogue (levels 0-2; the frame must divide into tiles)
-  const bool pool_here = i < 8 && (i & 1) && c.c2 == 0 && nd->conv_kernel[i] == 1 && !fp8 &&
+  const bool pool_here = i < 8 && (i & 1) && c.c2 == 0 && nd->conv_kernel[i] >= 1 && !fp8 &&
                          nn_umma_pooled_fits(c.c1, c.cout, h, w);
+  // tcgen05: kind 1 loads the first input's halo as swizzled pixel rows
+  // where the layer's shape allows, kind 2 as 8-channel planes (flags bit 5)
+  const int umma_flags = 1 | (nd->conv_kernel[i] == 2 ? 32 : 0);
   if (fp8) {
     const uint8_t* w8 = nd->w8 + nd->lay.conv_w[i];
     const float* wsc = nd->wscale + nd->wsoff[i];
@@ -153,12 +156,12 @@ int conv_layer(PbrtNeural* nd, int i, const bf16* x, bool fp8, cudaStream_t s, b
     return pbrt_nn_conv3x3_fp8(in1, c.c1, in2, c.c2, w8, wsc, ixs, b, nd->act[i], n, h, w, c.cout, 1, s);
   }
   if (pool_here && (st = pbrt_nn_conv3x3_umma_pooled(in1, c.c1, w16, b, nd->act[i], nd->pool[c.level + 1], n, h, w,
-                                                     c.cout, 1, s)) != PBRT_ERROR_UNSUPPORTED) {
+                                                     c.cout, umma_flags, s)) != PBRT_ERROR_UNSUPPORTED) {
     *pooled = st == PBRT_OK;
     return st;
   }
-  if (nd->conv_kernel[i] == 1) return pbrt_nn_conv3x3_umma(in1, c.c1, in2, c.c2, w16, b, nd->act[i], n, h, w, c.cout,
-                                                          1, s);
+  if (nd->conv_kernel[i] >= 1)
+    return pbrt_nn_conv3x3_umma(in1, c.c1, in2, c.c2, w16, b, nd->act[i], n, h, w, c.cout, umma_flags, s);
   return pbrt_nn_conv3x3(in1, c.c1, in2, c.c2, w16, b, nd->act[i], nullptr, n, h, w, c.cout, 1, s);
 }
 
@@ -394,12 +397,17 @@ PBRT_API int pbrt_neural_autotune(PbrtNeural* nd, pbrt_stream_t stream) {
     else in1 = nd->act[i - 1];
     const bf16* w16 = nd->w16 + nd->lay.conv_w[i];
     const float* b = nd->params + nd->lay.conv_b[i];
-    float best[2] = {1e30f, 1e30f};
-    for (int k = 0; k < 2 && !st; ++k) {
+    // 0: mma.sync; 1: tcgen05 (swizzled pixel rows for one input of 16 or
+    // 32 channels and 32 or 48 out); 2: tcgen05 with 8-channel planes
+    // (timed only where 1 differs)
+    float best[3] = {1e30f, 1e30f, 1e30f};
+    const int kinds = (c.c1 == 16 || c.c1 == 32) && c.c2 == 0 && (c.cout == 32 || c.cout == 48) ? 3 : 2;
+    for (int k = 0; k < kinds && !st; ++k) {
       float ms[3];
       for (int r = 0; r < 4 && !st; ++r) {
         cudaEventRecord(e0, stream);
-        st = k ? pbrt_nn_conv3x3_umma(in1, c.c1, in2, c.c2, w16, b, nd->act[i], 1, h, w, c.cout, 1, stream)
+        st = k ? pbrt_nn_conv3x3_umma(in1, c.c1, in2, c.c2, w16, b, nd->act[i], 1, h, w, c.cout, k == 2 ? 33 : 1,
+                                      stream)
                : pbrt_nn_conv3x3(in1, c.c1, in2, c.c2, w16, b, nd->act[i], nullptr, 1, h, w, c.cout, 1, stream);
         cudaEventRecord(e1, stream);
         cudaError_t e = cudaEventSynchronize(e1);
@@ -411,7 +419,9 @@ PBRT_API int pbrt_neural_autotune(PbrtNeural* nd, pbrt_stream_t stream) {
         best[k] = ms[1];
       }
     }
-    nd->conv_kernel[i] = best[1] < best[0] ? 1 : 0;
+    int pick = best[1] < best[0] ? 1 : 0;
+    if (best[2] < best[pick]) pick = 2;
+    nd->conv_kernel[i] = pick;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -438,7 +448,7 @@ PBRT_API int pbrt_neural_set_conv_kernels(PbrtNeural* nd, const int32_t* kinds, 
   if (!checked<PbrtNeural>(nd, Kind::Neural) || !kinds || count != kNumConvs)
     return fail(PBRT_ERROR_INVALID_ARGUMENT, "neural set conv kernels: bad arguments");
   for (int i = 0; i < kNumConvs; ++i) {
-    if (kinds[i] != 0 && kinds[i] != 1) return fail(PBRT_ERROR_INVALID_ARGUMENT, "neural set conv kernels: 0 or 1");
+    if (kinds[i] < 0 || kinds[i] > 2) return fail(PBRT_ERROR_INVALID_ARGUMENT, "neural set conv kernels: 0, 1 or 2");
     nd->conv_kernel[i] = kinds[i];
   }
   nd->tuned = true;

@@ -63,6 +63,23 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo_bytes, uin
   return d;
 }
 
+// Shared-memory matrix descriptor, K-major, swizzled rows of `row_bytes`
+// (32, 64 or 128: one pixel of 16, 32 or 64 BF16 channels, as a TMA with
+// the same swizzle writes it): the stride between groups of 8 rows; the
+// leading offset is unused (a K step of 16 elements stays inside a row and
+// moves the start by 32 bytes). The swizzle is a function of the address
+// bits, so a start shifted by whole rows (the taps) needs no base offset.
+__device__ __forceinline__ uint64_t sdesc_sw(uint32_t addr, uint32_t sbo_bytes, uint32_t row_bytes) {
+  const uint64_t layout = row_bytes == 128 ? 2u : (row_bytes == 64 ? 4u : 6u);
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3fffu);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)((sbo_bytes >> 4) & 0x3fffu) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= layout << 61;
+  return d;
+}
+
 // Instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both
 // K-major, M = 128, N = n.
 __host__ __device__ constexpr uint32_t idesc_bf16(int n) {
@@ -566,11 +583,12 @@ __device__ __forceinline__ uint32_t quant4_e4m3(uint32_t lo2, uint32_t hi2, cons
 
 // FP8: at most 64 registers, three CTAs an SM (the full-resolution layers
 // run out of CTAs in flight with two); BF16: the compiler's allocation.
-template <int NC, bool kF8>
+template <int NC, bool kF8, bool kSwz = false>
 __global__ void __launch_bounds__(kWsThreads, kF8 ? 3 : 0) conv3x3_umma_ws_kernel(UmmaConvArgs a, int tiles_per_image,
                                                                      const __grid_constant__ CUtensorMap x1map,
                                                                      const __grid_constant__ CUtensorMap x2map,
-                                                                     int use_tma, int stg_planes, int stages) {
+                                                                     int use_tma, int stg_planes, int stages,
+                                                                     int x1_swz) {
   using namespace umma;
   constexpr uint32_t kCols = 2 * NC <= 64 ? 64 : (2 * NC <= 128 ? 128 : 256);
   constexpr int kMaxStages = 6;
@@ -680,11 +698,18 @@ __global__ void __launch_bounds__(kWsThreads, kF8 ? 3 : 0) conv3x3_umma_ws_kerne
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar),
                      "r"((uint32_t)(x1_planes * kPlaneBytes))
                      : "memory");
-        asm volatile(
-            "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
-            "%5, %6}], [%7];\n" ::"r"(hb),
-            "l"(reinterpret_cast<uint64_t>(&x1map)), "r"(0), "r"(x0 - 1), "r"(y0 - 1), "r"(0), "r"(img), "r"(bar)
-            : "memory");
+        if constexpr (kSwz)  // whole pixels, swizzled rows: [18][10][c1] (the same bytes as the planes)
+          asm volatile(
+              "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+              "%4, %5}], [%6];\n" ::"r"(hb),
+              "l"(reinterpret_cast<uint64_t>(&x1map)), "r"(0), "r"(x0 - 1), "r"(y0 - 1), "r"(img), "r"(bar)
+              : "memory");
+        else
+          asm volatile(
+              "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+              "%4, %5, %6}], [%7];\n" ::"r"(hb),
+              "l"(reinterpret_cast<uint64_t>(&x1map)), "r"(0), "r"(x0 - 1), "r"(y0 - 1), "r"(0), "r"(img), "r"(bar)
+              : "memory");
       }
       if (lane == 0 && stg_planes) {
         // the 6 x 10 half-resolution pixels under the tile's halo (x0 % 8 == 0,
@@ -800,19 +825,32 @@ __global__ void __launch_bounds__(kWsThreads, kF8 ? 3 : 0) conv3x3_umma_ws_kerne
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
         const uint32_t hb = hbase + st * halo_pitch, d = tmem + (uint32_t)b * NC;
         // The descriptors advance by constants (a tap shifts the halo's
-        // start, a K step moves two planes; every sum is a shared-memory
-        // address, so the 14-bit address field never carries): a single
-        // issuing thread that rebuilt them per instruction spent ~40 cycles
-        // an MMA on it, as much as the ~50-cycle MMA itself at small N.
-        const uint64_t da0 = umma::sdesc(hb, kPlaneBytes, kHaloW * 16);
+        // start, a K step moves two planes -- or, kSwz, 32 bytes along the
+        // swizzled pixel rows; every sum is a shared-memory address, so the
+        // 14-bit address field never carries): a single issuing thread that
+        // rebuilt them per instruction spent ~40 cycles an MMA on it, as much
+        // as the ~50-cycle MMA itself at small N.
         const uint64_t db0 = umma::sdesc(wbase, NC * 16, 8 * 16);
         const int ksteps = planes / 2;
+        if constexpr (kSwz) {
+          const uint64_t da0 = umma::sdesc_sw(hb, kHaloW * x1_swz, x1_swz);
+          const uint32_t px16 = (uint32_t)x1_swz >> 4;  // one pixel, 16-byte units
 #pragma unroll
-        for (int tap = 0; tap < 9; ++tap) {
-          uint64_t da = da0 + (uint64_t)((((tap / 3) * kHaloW + tap % 3) * 16) >> 4);
-          uint64_t db = db0 + (uint64_t)(tap * planes * NC);
-          for (int ks = 0; ks < ksteps; ++ks, da += (2 * kPlaneBytes) >> 4, db += 2 * NC)
-            umma::mma_ss<kF8>(d, da, db, idesc, tap > 0 || ks > 0);
+          for (int tap = 0; tap < 9; ++tap) {
+            uint64_t da = da0 + (uint64_t)(((tap / 3) * kHaloW + tap % 3) * px16);
+            uint64_t db = db0 + (uint64_t)(tap * planes * NC);
+            for (int ks = 0; ks < ksteps; ++ks, da += 2, db += 2 * NC)
+              umma::mma_ss<kF8>(d, da, db, idesc, tap > 0 || ks > 0);
+          }
+        } else {
+          const uint64_t da0 = umma::sdesc(hb, kPlaneBytes, kHaloW * 16);
+#pragma unroll
+          for (int tap = 0; tap < 9; ++tap) {
+            uint64_t da = da0 + (uint64_t)((((tap / 3) * kHaloW + tap % 3) * 16) >> 4);
+            uint64_t db = db0 + (uint64_t)(tap * planes * NC);
+            for (int ks = 0; ks < ksteps; ++ks, da += (2 * kPlaneBytes) >> 4, db += 2 * NC)
+              umma::mma_ss<kF8>(d, da, db, idesc, tap > 0 || ks > 0);
+          }
         }
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(eb(st))
                      : "memory");
@@ -1259,6 +1297,22 @@ bool make_x1_map(CUtensorMap* m, const void* x1, int n, int h, int w, int c1) {
              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
+// x1 [N][H][W][c1] BF16, c1 in {16, 32, 64}, as [c1][W][H][N] with box
+// [c1][10][18][1] and the swizzle of a c1 * 2-byte row: one request a pixel
+// instead of one per 8 channels; lands as the halo's pixel rows.
+bool make_x1_swz_map(CUtensorMap* m, const void* x1, int n, int h, int w, int c1) {
+  EncodeTiledFn enc = encode_tiled();
+  if (!enc || ((uintptr_t)x1 & 15) || (c1 != 16 && c1 != 32 && c1 != 64)) return false;
+  const cuuint64_t dims[4] = {(cuuint64_t)c1, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n};
+  const cuuint64_t strides[3] = {(cuuint64_t)c1 * 2, (cuuint64_t)w * c1 * 2, (cuuint64_t)h * w * c1 * 2};
+  const cuuint32_t box[4] = {(cuuint32_t)c1, (cuuint32_t)umma::kHaloW, (cuuint32_t)umma::kHaloH, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  const CUtensorMapSwizzle sw =
+      c1 == 16 ? CU_TENSOR_MAP_SWIZZLE_32B : (c1 == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B);
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(x1), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 // x2 [N][H/2][W/2][c2] BF16 (the half-resolution second input) as
 // [8][W/2][H/2][c2/8][N] with box [8][6][10][c2/8][1]: the pixels under one
 // tile's halo, zeros outside the frame.
@@ -1297,12 +1351,23 @@ size_t ws_smem_f8(int cin, int nc, int stages, int stg = 0) {
 }
 
 template <int NC, bool kF8> int launch_umma_ws(const UmmaConvArgs& a, cudaStream_t s, bool use_tma_flag,
-                                               bool box_flag = true) {
+                                               bool box_flag = true, bool swz_flag = true) {
   const int cin = a.c1 + a.c2;
   CUtensorMap map, map2;
   memset(&map, 0, sizeof(map));
   memset(&map2, 0, sizeof(map2));
-  const int use_tma = use_tma_flag && make_x1_map(&map, a.x1, a.N, a.H, a.W, a.c1) ? 1 : 0;
+  // BF16, one input of 16 or 32 channels, 32 or 48 out (the network's
+  // full- and half-resolution first layers and e0b, d0b): the x1 halo as
+  // swizzled pixel rows, one TMA request a pixel instead of one per 8
+  // channels (1088x1920: e0b 87 -> 77 us, d0b 88 -> 79); elsewhere the
+  // planes, which timed as fast or faster (64 channels; beside the
+  // upsampled second input)
+  constexpr bool kSwzForm = !kF8 && (NC == 32 || NC == 48);
+  int x1_swz = 0;
+  if (kSwzForm && use_tma_flag && swz_flag && a.c2 == 0 && (a.c1 == 16 || a.c1 == 32) &&
+      make_x1_swz_map(&map, a.x1, a.N, a.H, a.W, a.c1))
+    x1_swz = a.c1 * 2;
+  const int use_tma = x1_swz || (use_tma_flag && make_x1_map(&map, a.x1, a.N, a.H, a.W, a.c1)) ? 1 : 0;
   const size_t smem_max = kF8 ? kWsSmemMaxF8 : kWsSmemMax;
   auto smem_at = [&](int st, int stg) { return kF8 ? ws_smem_f8(cin, NC, st, stg) : ws_smem(cin, NC, st, stg); };
   // input stages in flight: PBRT_WS_STAGES (2..6) fixes the count; by
@@ -1319,6 +1384,9 @@ template <int NC, bool kF8> int launch_umma_ws(const UmmaConvArgs& a, cudaStream
   int ast = once_per_device(attrs, [&]() -> int {
     cudaError_t e = cudaFuncSetAttribute(conv3x3_umma_ws_kernel<NC, kF8>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
+    if (e == cudaSuccess && kSwzForm)
+      e = cudaFuncSetAttribute(conv3x3_umma_ws_kernel<NC, kF8, kSwzForm>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem_max);
     if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(conv3x3_umma_ws_kernel)");
     return PBRT_OK;
   });
@@ -1336,7 +1404,9 @@ template <int NC, bool kF8> int launch_umma_ws(const UmmaConvArgs& a, cudaStream
   int regs_cta = 0, static_smem = 0;
   {
     cudaFuncAttributes fa;
-    if (cudaFuncGetAttributes(&fa, conv3x3_umma_ws_kernel<NC, kF8>) == cudaSuccess && fa.numRegs > 0) {
+    const cudaError_t e = x1_swz ? cudaFuncGetAttributes(&fa, conv3x3_umma_ws_kernel<NC, kF8, kSwzForm>)
+                                 : cudaFuncGetAttributes(&fa, conv3x3_umma_ws_kernel<NC, kF8>);
+    if (e == cudaSuccess && fa.numRegs > 0) {
       regs_cta = (threads / 32) * ((fa.numRegs * 32 + 255) / 256 * 256);
       static_smem = (int)fa.sharedSizeBytes;
     } else {
@@ -1378,7 +1448,12 @@ template <int NC, bool kF8> int launch_umma_ws(const UmmaConvArgs& a, cudaStream
   const size_t smem = smem_at(stages, stg);
   const int per_sm = resident(smem);
   const int grid = (int)std::min(total_tiles, (long)sms * per_sm);
-  conv3x3_umma_ws_kernel<NC, kF8><<<grid, threads, smem, s>>>(a, tiles_per_image, map, map2, use_tma, stg, stages);
+  if (x1_swz)
+    conv3x3_umma_ws_kernel<NC, kF8, kSwzForm><<<grid, threads, smem, s>>>(a, tiles_per_image, map, map2, use_tma, stg,
+                                                                         stages, x1_swz);
+  else
+    conv3x3_umma_ws_kernel<NC, kF8><<<grid, threads, smem, s>>>(a, tiles_per_image, map, map2, use_tma, stg, stages,
+                                                                 0);
   return PBRT_OK;
 }
 
@@ -1423,7 +1498,8 @@ extern "C" {
 // 80, 96, 112, 128}, channel counts multiples of 16; flags bit 0: ReLU,
 // bit 1: the per-tile kernel only, bit 2: no TMA (cp.async gathers), bit 3:
 // the single-role persistent kernel instead of the warp-specialised one,
-// bit 4: the upsampled second input by cp.async gathers, not the TMA box.
+// bit 4: the upsampled second input by cp.async gathers, not the TMA box,
+// bit 5: the x1 halo as 8-channel planes, not swizzled pixel rows.
 PBRT_API int pbrt_nn_conv3x3_umma(const void* x1, int32_t c1, const void* x2, int32_t c2, const void* w,
                                   const float* bias, void* y, int32_t n, int32_t h, int32_t wd, int32_t cout,
                                   int32_t flags, pbrt_stream_t stream) {
@@ -1435,14 +1511,14 @@ PBRT_API int pbrt_nn_conv3x3_umma(const void* x1, int32_t c1, const void* x2, in
   // warp-specialised form (the upsampled second input comes from its gather warps)
   if (!(flags & 10) && ws_smem(c1 + c2, cout, 2) <= kWsSmemMax) {
     switch (cout) {
-      case 16: st = launch_umma_ws<16, false>(a, stream, !(flags & 4), !(flags & 16)); break;
-      case 32: st = launch_umma_ws<32, false>(a, stream, !(flags & 4), !(flags & 16)); break;
-      case 48: st = launch_umma_ws<48, false>(a, stream, !(flags & 4), !(flags & 16)); break;
-      case 64: st = launch_umma_ws<64, false>(a, stream, !(flags & 4), !(flags & 16)); break;
-      case 80: st = launch_umma_ws<80, false>(a, stream, !(flags & 4), !(flags & 16)); break;
-      case 96: st = launch_umma_ws<96, false>(a, stream, !(flags & 4), !(flags & 16)); break;
-      case 112: st = launch_umma_ws<112, false>(a, stream, !(flags & 4), !(flags & 16)); break;
-      default: st = launch_umma_ws<128, false>(a, stream, !(flags & 4), !(flags & 16)); break;
+      case 16: st = launch_umma_ws<16, false>(a, stream, !(flags & 4), !(flags & 16), !(flags & 32)); break;
+      case 32: st = launch_umma_ws<32, false>(a, stream, !(flags & 4), !(flags & 16), !(flags & 32)); break;
+      case 48: st = launch_umma_ws<48, false>(a, stream, !(flags & 4), !(flags & 16), !(flags & 32)); break;
+      case 64: st = launch_umma_ws<64, false>(a, stream, !(flags & 4), !(flags & 16), !(flags & 32)); break;
+      case 80: st = launch_umma_ws<80, false>(a, stream, !(flags & 4), !(flags & 16), !(flags & 32)); break;
+      case 96: st = launch_umma_ws<96, false>(a, stream, !(flags & 4), !(flags & 16), !(flags & 32)); break;
+      case 112: st = launch_umma_ws<112, false>(a, stream, !(flags & 4), !(flags & 16), !(flags & 32)); break;
+      default: st = launch_umma_ws<128, false>(a, stream, !(flags & 4), !(flags & 16), !(flags & 32)); break;
     }
     if (st) return st;
     return check_launch("conv3x3_umma_ws_kernel");
@@ -1492,14 +1568,14 @@ PBRT_API int pbrt_nn_conv3x3_umma_pooled(const void* x1, int32_t c1, const void*
   a.pooled = (bf16*)pooled;
   int st;
   switch (cout) {
-    case 16: st = launch_umma_ws<16, false>(a, stream, true); break;
-    case 32: st = launch_umma_ws<32, false>(a, stream, true); break;
-    case 48: st = launch_umma_ws<48, false>(a, stream, true); break;
-    case 64: st = launch_umma_ws<64, false>(a, stream, true); break;
-    case 80: st = launch_umma_ws<80, false>(a, stream, true); break;
-    case 96: st = launch_umma_ws<96, false>(a, stream, true); break;
-    case 112: st = launch_umma_ws<112, false>(a, stream, true); break;
-    default: st = launch_umma_ws<128, false>(a, stream, true); break;
+    case 16: st = launch_umma_ws<16, false>(a, stream, true, true, !(flags & 32)); break;
+    case 32: st = launch_umma_ws<32, false>(a, stream, true, true, !(flags & 32)); break;
+    case 48: st = launch_umma_ws<48, false>(a, stream, true, true, !(flags & 32)); break;
+    case 64: st = launch_umma_ws<64, false>(a, stream, true, true, !(flags & 32)); break;
+    case 80: st = launch_umma_ws<80, false>(a, stream, true, true, !(flags & 32)); break;
+    case 96: st = launch_umma_ws<96, false>(a, stream, true, true, !(flags & 32)); break;
+    case 112: st = launch_umma_ws<112, false>(a, stream, true, true, !(flags & 32)); break;
+    default: st = launch_umma_ws<128, false>(a, stream, true, true, !(flags & 32)); break;
   }
   if (st) return st;
   return check_launch("conv3x3_umma_ws_kernel (pooled)");

@@ -196,10 +196,15 @@ class Workspace:
 
     def forward(self, kernel="mma"):
         """kernel: "mma" (warp-level mma.sync convolutions, the training path), "umma" (tcgen05), or a
-        list with one of the two per convolution (layer order of CONVS)."""
+        list with one per convolution (layer order of CONVS; "umma_planes": tcgen05 with the first
+        input's halo as 8-channel planes, the same bits as "umma")."""
+        import functools
+
         net, a = self.net, self.act
         kinds = list(kernel) if isinstance(kernel, (list, tuple)) else [kernel] * len(CONVS)
-        layer = {name: (nn.conv3x3_umma if k == "umma" else nn.conv3x3) for (name, _, _, _), k in zip(CONVS, kinds)}
+        conv = {"mma": nn.conv3x3, "umma": nn.conv3x3_umma,
+                "umma_planes": functools.partial(nn.conv3x3_umma, swizzle=False)}
+        layer = {name: conv[k] for (name, _, _, _), k in zip(CONVS, kinds)}
         nn.avgpool2(self.rad[0], self.rad[1])
         nn.avgpool2(self.rad[1], self.rad[2])
         x = self.feat

@@ -142,19 +142,23 @@ class NeuralDenoiser(Handle):
         m = (C.c_int32 * 18)(*[1 if v else 0 for v in mask])
         check(lib().pbrt_neural_set_fp8_layers(self.ptr, m, 18))
 
+    KINDS = ("mma", "umma", "umma_planes")
+
     def autotune(self, stream=None) -> list:
-        """Times the mma.sync and tcgen05 kernels for every convolution on the current inputs; keeps the faster."""
+        """Times the mma.sync and tcgen05 kernels (the latter with the first input's halo as swizzled
+        pixel rows and as 8-channel planes) for every convolution on the current inputs; keeps the fastest."""
         check(lib().pbrt_neural_autotune(self.ptr, stream_handle(stream)))
         return self.conv_kernels()
 
     def conv_kernels(self) -> list:
-        """Per-layer convolution kernel: "mma" or "umma" (tcgen05)."""
+        """Per-layer convolution kernel: "mma", "umma" (tcgen05) or "umma_planes" (tcgen05, the first
+        input's halo as 8-channel planes; the same bits as "umma")."""
         k = (C.c_int32 * 18)()
         check(lib().pbrt_neural_conv_kernels(self.ptr, k, 18))
-        return ["umma" if v else "mma" for v in k]
+        return [self.KINDS[v] for v in k]
 
     def set_conv_kernels(self, kinds) -> None:
-        k = (C.c_int32 * 18)(*[1 if x == "umma" else 0 for x in kinds])
+        k = (C.c_int32 * 18)(*[self.KINDS.index(x) for x in kinds])
         check(lib().pbrt_neural_set_conv_kernels(self.ptr, k, 18))
 
     def dispatch(self, push_constants=None, stream=None, graph: bool = True) -> None:

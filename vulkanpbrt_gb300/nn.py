@@ -119,12 +119,14 @@ def channel_amax(x, amax):
 
 
 def conv3x3_umma(x1, w, bias=None, x2=None, relu=False, out=None, persistent=True, tma=True, specialised=True,
-                 box=True):
+                 box=True, swizzle=True):
     """tcgen05 forward (BF16 out): as conv3x3, Cout in {16, ..., 128}. persistent=False forces the
     per-tile kernel (the persistent one is used when the weights and two input halos fit in shared memory);
     tma=False gathers the persistent kernel's input halo with cp.async instead of a TMA load; specialised=False
     uses the single-role persistent kernel instead of the warp-specialised one; box=False gathers the upsampled
-    second input with cp.async instead of loading its half-resolution box by TMA."""
+    second input with cp.async instead of loading its half-resolution box by TMA; swizzle=False loads the
+    first input's halo as 8-channel planes instead of swizzled whole-pixel rows (the default for a single
+    input of 16 or 32 channels and Cout 32 or 48)."""
     import torch
 
     n, h, wd, c1 = x1.shape
@@ -133,13 +135,13 @@ def conv3x3_umma(x1, w, bias=None, x2=None, relu=False, out=None, persistent=Tru
     if out is None:
         out = torch.empty((n, h, wd, cout), dtype=torch.bfloat16, device=x1.device)
     flags = (RELU if relu else 0) | (0 if persistent else 2) | (0 if tma else 4) | (0 if specialised else 8) | \
-        (0 if box else 16)
+        (0 if box else 16) | (0 if swizzle else 32)
     check(lib().pbrt_nn_conv3x3_umma(_ptr(x1), c1, _ptr(x2), c2, _ptr(w), _ptr(bias), _ptr(out), n, h, wd, cout,
                                      flags, _stream()))
     return out
 
 
-def conv3x3_umma_pooled(x1, w, bias=None, relu=False):
+def conv3x3_umma_pooled(x1, w, bias=None, relu=False, swizzle=True):
     """conv3x3_umma of a single input that also returns the 2x2 average pooling of its output
     (the same bits as avgpool2 of it), from the warp-specialised kernel's epilogue."""
     import torch
@@ -149,7 +151,7 @@ def conv3x3_umma_pooled(x1, w, bias=None, relu=False):
     out = torch.empty((n, h, wd, cout), dtype=torch.bfloat16, device=x1.device)
     pooled = torch.empty((n, h // 2, wd // 2, cout), dtype=torch.bfloat16, device=x1.device)
     check(lib().pbrt_nn_conv3x3_umma_pooled(_ptr(x1), c1, _ptr(w), _ptr(bias), _ptr(out), _ptr(pooled), n, h, wd,
-                                            cout, RELU if relu else 0, _stream()))
+                                            cout, (RELU if relu else 0) | (0 if swizzle else 32), _stream()))
     return out, pooled
 
 
