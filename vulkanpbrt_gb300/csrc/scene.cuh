@@ -23,7 +23,7 @@
 namespace pbrt {
 
 struct DevTexture {
-  uint64_t offset;  // in texels
+  uint64_t offset;  // in texels; the texture in 4 x 2-texel tiles (texture_tile_index)
   uint32_t w, h;
 };
 struct DevMesh {

@@ -209,8 +209,14 @@ PBRT_D float3 sky_color(float3 dir) {
 
 // ---------------------------------------------------------------------------
 // Scene access (geometry.glsl, layoutPTGeometry*.glsl).
+// The texel pool holds each texture in 4 x 2-texel tiles, one 32-byte
+// sector each, tiles in row-major order (texture_tile_index): a bilinear
+// footprint touches 1.875 sectors on average instead of 2.25 row-major.
+PBRT_HD uint32_t texture_tile_index(uint32_t w, uint32_t x, uint32_t y) {
+  return (((y >> 1) * ((w + 3) >> 2) + (x >> 2)) << 3) + ((y & 1u) << 2) + (x & 3u);
+}
 PBRT_D float4 tex_fetch(const SceneView& sc, const DevTexture& t, int x, int y) {
-  uchar4 c = sc.texels[t.offset + (size_t)y * t.w + x];
+  uchar4 c = sc.texels[t.offset + texture_tile_index(t.w, (uint32_t)x, (uint32_t)y)];
   return make_float4(u82f(c.x), u82f(c.y), u82f(c.z), u82f(c.w));
 }
 PBRT_D float4 tex_sample(const SceneView& sc, int tex, float u, float v) {

@@ -1377,6 +1377,14 @@ __global__ void k_finalize(const FrameParams* __restrict__ fpp, Queues q, float4
   }
 }
 
+// Row-major RGBA8 texture -> the pool's 4 x 2-texel tiles (texture_tile_index).
+__global__ void k_tile_texture(const uchar4* __restrict__ src, uchar4* __restrict__ dst, uint32_t w, uint32_t h) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)w * h) return;
+  const uint32_t x = (uint32_t)(i % w), y = (uint32_t)(i / w);
+  dst[texture_tile_index(w, x, y)] = src[i];
+}
+
 }  // namespace pbrt
 
 // ===========================================================================
@@ -1751,7 +1759,7 @@ PBRT_API int pbrt_scene_create_ex(const PbrtSceneDesc* d, uint32_t build_flags, 
   }
   // --- textures
   std::vector<DevTexture> texd(d->texture_count);
-  size_t texels = 0;
+  size_t texels = 0, max_texels = 0;
   for (uint32_t i = 0; i < d->texture_count; ++i) {
     const PbrtTextureDesc& td = d->textures[i];
     if (!td.rgba8 || td.width == 0 || td.height == 0) {
@@ -1761,16 +1769,32 @@ PBRT_API int pbrt_scene_create_ex(const PbrtSceneDesc* d, uint32_t build_flags, 
     texd[i].offset = texels;
     texd[i].w = td.width;
     texd[i].h = td.height;
-    texels += (size_t)td.width * td.height;
+    // 4 x 2-texel tiles: the width padded to a multiple of 4, the height of 2
+    texels += (size_t)((td.width + 3) & ~3u) * ((td.height + 1) & ~1u);
+    max_texels = std::max(max_texels, (size_t)td.width * td.height);
   }
   int st = PBRT_OK;
   uchar4* texpool = nullptr;
   st = dalloc(&texpool, texels);
   if (!st) sc->allocs.push_back(texpool);
+  if (!st && cudaMemset(texpool, 0, texels * sizeof(uchar4)) != cudaSuccess) st = cuda_fail(cudaGetLastError(), "texture pool");
+  // each texture uploaded row-major into a staging buffer, then tiled on the device
+  uchar4* staging = nullptr;
+  if (!st) st = dalloc(&staging, max_texels);
   for (uint32_t i = 0; !st && i < d->texture_count; ++i) {
-    cudaError_t e = cudaMemcpy(texpool + texd[i].offset, d->textures[i].rgba8,
-                               (size_t)d->textures[i].width * d->textures[i].height * 4, cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) st = cuda_fail(e, "texture upload");
+    const uint32_t w = d->textures[i].width, h = d->textures[i].height;
+    cudaError_t e = cudaMemcpy(staging, d->textures[i].rgba8, (size_t)w * h * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      st = cuda_fail(e, "texture upload");
+      break;
+    }
+    const size_t n = (size_t)w * h;
+    k_tile_texture<<<(unsigned)((n + 255) / 256), 256>>>(staging, texpool + texd[i].offset, w, h);
+    st = check_launch("texture tiling");
+  }
+  if (staging) {
+    cudaDeviceSynchronize();  // the tiling kernels read the staging buffer
+    cudaFree(staging);
   }
   std::vector<DevMaterial> mats(d->mesh_count);
   std::memcpy(mats.data(), d->materials, sizeof(DevMaterial) * d->mesh_count);
