@@ -27,6 +27,7 @@
 
 #include "bvh.hpp"
 #include "internal.hpp"
+#include "lbvh.cuh"
 
 namespace pbrt {
 namespace lbvh {
@@ -34,17 +35,6 @@ namespace lbvh {
 constexpr int kLeafMax = 3;        // triangles a leaf slot holds (5-bit offsets, 3-bit counts)
 constexpr int kReduceBlocks = 1024;
 constexpr int kThreads = 256;
-
-// 21-bit value -> bits at positions 3k (the "magic bits" interleave).
-__device__ __forceinline__ uint64_t spread21(uint64_t v) {
-  v &= 0x1fffffull;
-  v = (v | v << 32) & 0x1f00000000ffffull;
-  v = (v | v << 16) & 0x1f0000ff0000ffull;
-  v = (v | v << 8) & 0x100f00f00f00f00full;
-  v = (v | v << 4) & 0x10c30c30c30c30c3ull;
-  v = (v | v << 2) & 0x1249249249249249ull;
-  return v;
-}
 
 __device__ __forceinline__ void tri_box(const float* w, float lo[3], float hi[3]) {
 #pragma unroll
@@ -126,15 +116,6 @@ __global__ void __launch_bounds__(kThreads) k_morton(const float4* __restrict__ 
   }
 }
 
-// Length of the common prefix of sorted keys i and j (the index breaks ties),
-// -1 outside [0, n).
-__device__ __forceinline__ int delta(const uint64_t* __restrict__ k, long long n, long long i, long long j) {
-  if (j < 0 || j >= n) return -1;
-  const uint64_t a = k[i], b = k[j];
-  if (a == b) return 64 + __clz((int)((uint32_t)i ^ (uint32_t)j));
-  return __clzll((long long)(a ^ b));
-}
-
 // Internal node i of the radix tree over n sorted keys (0 <= i < n - 1):
 // its children (internal index, or n - 1 + leaf position), parent links and
 // the range of sorted positions it covers.
@@ -143,25 +124,8 @@ __global__ void __launch_bounds__(kThreads) k_radix_tree(const uint64_t* __restr
                                                          int* __restrict__ first, int* __restrict__ last) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n - 1) return;
-  const int d = delta(k, n, i, i + 1) - delta(k, n, i, i - 1) >= 0 ? 1 : -1;
-  const int dmin = delta(k, n, i, (long long)i - d);
-  long long lmax = 2;
-  while (delta(k, n, i, i + lmax * d) > dmin) lmax <<= 1;  // ends once i + lmax * d leaves [0, n)
-  long long l = 0;
-  for (long long t = lmax >> 1; t >= 1; t >>= 1)
-    if (delta(k, n, i, i + (l + t) * d) > dmin) l += t;
-  const long long j = i + l * d;
-  const int dnode = delta(k, n, i, j);
-  long long s = 0;
-  for (long long div = 2;; div <<= 1) {
-    const long long t = (l + div - 1) / div;
-    if (delta(k, n, i, i + (s + t) * d) > dnode) s += t;
-    if (t == 1) break;
-  }
-  const int gamma = (int)(i + s * d + (d < 0 ? -1 : 0));
-  const int lo = (int)(i < j ? i : j), hi = (int)(i < j ? j : i);
-  const int lc = lo == gamma ? n - 1 + gamma : gamma;
-  const int rc = hi == gamma + 1 ? n - 1 + gamma + 1 : gamma + 1;
+  int lc, rc, lo, hi;
+  radix_node(k, n, i, &lc, &rc, &lo, &hi);
   left[i] = lc;
   right[i] = rc;
   parent[lc] = i;
