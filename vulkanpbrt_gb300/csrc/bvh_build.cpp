@@ -168,20 +168,24 @@ struct WideDP {
     split.assign(n * 9, -1);
     is_leaf.assign(n, 0);
     wide_split.assign(n, 1);
-    // post-order with an explicit stack
-    std::vector<std::pair<uint32_t, bool>> stk{{root, false}};
-    while (!stk.empty()) {
-      auto [ni, done] = stk.back();
-      stk.pop_back();
-      const BNode& nd = b.nodes[ni];
-      if (nd.left >= 0 && !done) {
-        stk.push_back({ni, true});
-        stk.push_back({(uint32_t)nd.left, false});
-        stk.push_back({(uint32_t)nd.right, false});
-        continue;
+    post_order(root);
+  }
+
+  // children before parents; large subtrees on their own threads (a node's
+  // values depend on its children's alone, so the result is the serial one)
+  void post_order(uint32_t ni) {
+    const BNode& nd = b.nodes[ni];
+    if (nd.left >= 0) {
+      if (nd.count > kParallelCutoff) {
+        auto f = std::async(std::launch::async, [=]() { post_order((uint32_t)nd.left); });
+        post_order((uint32_t)nd.right);
+        f.get();
+      } else {
+        post_order((uint32_t)nd.left);
+        post_order((uint32_t)nd.right);
       }
-      node(ni);
     }
+    node(ni);
   }
 
   void node(uint32_t ni) {
@@ -227,26 +231,26 @@ struct WideDP {
   }
 
   // the slots representing node ni with at most i of them
-  void slots(uint32_t ni, int i, std::vector<uint32_t>& out) const {
+  void slots(uint32_t ni, int i, uint32_t* out, int& n) const {
     const int8_t s = split[9 * (size_t)ni + i];
     if (i == 1 || s < 0) {
-      out.push_back(ni);
+      out[n++] = ni;
       return;
     }
     if (s == 0) {
-      slots(ni, i - 1, out);
+      slots(ni, i - 1, out, n);
       return;
     }
     const BNode& nd = b.nodes[ni];
-    slots((uint32_t)nd.left, s, out);
-    slots((uint32_t)nd.right, i - s, out);
+    slots((uint32_t)nd.left, s, out, n);
+    slots((uint32_t)nd.right, i - s, out, n);
   }
-  // children slots of the wide node made from binary node ni
-  void children(uint32_t ni, std::vector<uint32_t>& out) const {
+  // children slots (at most 8) of the wide node made from binary node ni
+  void children(uint32_t ni, uint32_t* out, int& n) const {
     const BNode& nd = b.nodes[ni];
     const int k = wide_split[ni];
-    slots((uint32_t)nd.left, k, out);
-    slots((uint32_t)nd.right, 8 - k, out);
+    slots((uint32_t)nd.left, k, out, n);
+    slots((uint32_t)nd.right, 8 - k, out, n);
   }
 };
 
@@ -268,31 +272,32 @@ struct Collapser {
   void encode(uint32_t out_index, uint32_t bnode, int depth) {
     st.depth = std::max(st.depth, depth);
     // Open the largest child until 8 children (or only leaves remain).
-    std::vector<uint32_t> ch;
+    uint32_t ch[8];
+    int nch = 0;
     const BNode& root = b.nodes[bnode];
     if (root.left < 0) {
-      ch.push_back(bnode);  // single leaf under this node
+      ch[nch++] = bnode;  // single leaf under this node
     } else if (dp) {
-      dp->children(bnode, ch);
+      dp->children(bnode, ch, nch);
     } else {
-      ch.push_back((uint32_t)root.left);
-      ch.push_back((uint32_t)root.right);
-      while (ch.size() < 8) {
+      ch[nch++] = (uint32_t)root.left;
+      ch[nch++] = (uint32_t)root.right;
+      while (nch < 8) {
         int best = -1;
         double best_area = -1.0;
-        for (size_t i = 0; i < ch.size(); ++i) {
+        for (int i = 0; i < nch; ++i) {
           const BNode& c = b.nodes[ch[i]];
           if (c.left < 0) continue;
           double a = c.box.area();
           if (a > best_area) {
             best_area = a;
-            best = (int)i;
+            best = i;
           }
         }
         if (best < 0) break;
         uint32_t open = ch[best];
         ch[best] = (uint32_t)b.nodes[open].left;
-        ch.push_back((uint32_t)b.nodes[open].right);
+        ch[nch++] = (uint32_t)b.nodes[open].right;
       }
     }
     // Leaves with more than 3 triangles (identical centroids beyond the leaf
@@ -303,21 +308,28 @@ struct Collapser {
     for (int a = 0; a < 3; ++a) pc[a] = 0.5f * (nb.lo[a] + nb.hi[a]);
     int slot_of[8];
     bool used[8] = {false};
-    std::vector<bool> placed(ch.size(), false);
-    for (size_t round = 0; round < ch.size(); ++round) {
+    bool placed[8] = {false};
+    // each child's score for each slot (its centre's offset along the slot's
+    // octant direction), once; the rounds then take the best free pair
+    double score_of[8][8];
+    for (int i = 0; i < nch; ++i) {
+      const Box& cbx = b.nodes[ch[i]].box;
+      double d[3];
+      for (int a = 0; a < 3; ++a) d[a] = 0.5 * ((double)cbx.lo[a] + cbx.hi[a]) - pc[a];
+      for (int s = 0; s < 8; ++s)
+        score_of[i][s] = (s & 1 ? d[0] : -d[0]) + (s & 2 ? d[1] : -d[1]) + (s & 4 ? d[2] : -d[2]);
+    }
+    for (int round = 0; round < nch; ++round) {
       double best = -std::numeric_limits<double>::infinity();
       int bc = -1, bs = -1;
-      for (size_t i = 0; i < ch.size(); ++i) {
+      for (int i = 0; i < nch; ++i) {
         if (placed[i]) continue;
-        const Box& cbx = b.nodes[ch[i]].box;
-        double d[3];
-        for (int a = 0; a < 3; ++a) d[a] = 0.5 * ((double)cbx.lo[a] + cbx.hi[a]) - pc[a];
         for (int s = 0; s < 8; ++s) {
           if (used[s]) continue;
-          double score = (s & 1 ? d[0] : -d[0]) + (s & 2 ? d[1] : -d[1]) + (s & 4 ? d[2] : -d[2]);
+          const double score = score_of[i][s];
           if (score > best) {
             best = score;
-            bc = (int)i;
+            bc = i;
             bs = s;
           }
         }
@@ -328,7 +340,7 @@ struct Collapser {
     }
     uint32_t slot_child[8];
     bool slot_used[8] = {false};
-    for (size_t i = 0; i < ch.size(); ++i) {
+    for (int i = 0; i < nch; ++i) {
       slot_child[slot_of[i]] = ch[i];
       slot_used[slot_of[i]] = true;
     }
@@ -348,7 +360,8 @@ struct Collapser {
     n.ez = ex[2];
     const float p[3] = {n.px, n.py, n.pz};
     // internal children first (to allocate them consecutively), in slot order
-    std::vector<std::pair<uint32_t, uint32_t>> inner;  // (slot, bnode)
+    uint32_t inner[8];  // binary nodes of the internal children, slot order
+    int ninner = 0;
     uint32_t tri_off = 0;
     n.tri_base = (uint32_t)tri_order.size();
     for (int s = 0; s < 8; ++s) {
@@ -364,7 +377,7 @@ struct Collapser {
       if (!leaf_slot) {
         n.imask |= (uint8_t)(1u << s);
         n.meta[s] = 0x80;
-        inner.push_back({(uint32_t)s, slot_child[s]});
+        inner[ninner++] = slot_child[s];
       } else {
         n.meta[s] = (uint8_t)((c.count << 5) | tri_off);
         for (uint32_t k = 0; k < c.count; ++k) tri_order.push_back(b.idx[c.begin + k]);
@@ -373,10 +386,10 @@ struct Collapser {
       }
     }
     n.child_base = (uint32_t)out.size();
-    out.resize(out.size() + inner.size());
+    out.resize(out.size() + (size_t)ninner);
     out[out_index] = n;
     uint32_t base = n.child_base;
-    for (size_t i = 0; i < inner.size(); ++i) encode(base + (uint32_t)i, inner[i].second, depth + 1);
+    for (int i = 0; i < ninner; ++i) encode(base + (uint32_t)i, inner[i], depth + 1);
   }
 };
 
