@@ -7,6 +7,7 @@
 #include <cstring>
 #include <future>
 #include <limits>
+#include <memory>
 #include <thread>
 
 #include "bvh.hpp"
@@ -67,33 +68,99 @@ struct Builder {
   uint32_t binary_leaf = (uint32_t)kMaxLeaf;
 
   uint32_t alloc() { return next.fetch_add(1); }
+  // ranges of at least kParallelScan primitives are scanned and binned in
+  // scan_threads chunks
+  static constexpr uint32_t kParallelScan = 1u << 17;
+  const int scan_threads = std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
+
+  // per-axis bins of a range of primitives: boxes and counts
+  struct Bins {
+    Box bb[3][kMaxBins];
+    uint32_t bc[3][kMaxBins] = {};
+    void merge(const Bins& o, int bins) {
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < bins; ++b) {
+          bb[a][b].grow(o.bb[a][b]);
+          bc[a][b] += o.bc[a][b];
+        }
+    }
+  };
+  void scan(uint32_t begin, uint32_t end, Box& box, Box& cb) const {
+    for (uint32_t i = begin; i < end; ++i) {
+      box.grow(pbox[idx[i]]);
+      cb.grow(&cent[3 * idx[i]]);
+    }
+  }
+  void bin(uint32_t begin, uint32_t end, const Box& cb, const float* k, Bins& out) const {
+    for (uint32_t i = begin; i < end; ++i) {
+      const uint32_t p = idx[i];
+      for (int a = 0; a < 3; ++a) {
+        if (!(k[a] > 0.f)) continue;
+        const int b = std::min(kBins - 1, (int)((cent[3 * p + a] - cb.lo[a]) * k[a]));
+        out.bb[a][b].grow(pbox[p]);
+        out.bc[a][b]++;
+      }
+    }
+  }
 
   void build(uint32_t ni, uint32_t begin, uint32_t count) {
     BNode& nd = nodes[ni];
+    // The node's box and centroid box, then the bins of all three axes; a
+    // large range in chunks on their own threads, merged in order (minima,
+    // maxima and counts: the serial result)
+    const int chunks = count >= kParallelScan ? scan_threads : 1;
+    const uint32_t step = (count + (uint32_t)chunks - 1) / (uint32_t)chunks;
     Box box, cb;
-    for (uint32_t i = begin; i < begin + count; ++i) {
-      box.grow(pbox[idx[i]]);
-      cb.grow(&cent[3 * idx[i]]);
+    if (chunks == 1) {
+      scan(begin, begin + count, box, cb);
+    } else {
+      std::vector<std::future<std::pair<Box, Box>>> f;
+      for (int c = 0; c < chunks; ++c) {
+        const uint32_t s = begin + std::min(count, (uint32_t)c * step), e = begin + std::min(count, (uint32_t)(c + 1) * step);
+        f.push_back(std::async(std::launch::async, [=]() {
+          Box bx, cx;
+          scan(s, e, bx, cx);
+          return std::make_pair(bx, cx);
+        }));
+      }
+      for (auto& x : f) {
+        const auto r = x.get();
+        box.grow(r.first);
+        cb.grow(r.second);
+      }
     }
     nd.box = box;
     nd.begin = begin;
     nd.count = count;
     if (count <= binary_leaf) return;
+    float kax[3];
+    for (int a = 0; a < 3; ++a) {
+      const float ext = cb.hi[a] - cb.lo[a];
+      kax[a] = ext > 0.f ? (float)kBins / ext : 0.f;
+    }
+    Bins local;  // serial: on the stack (most nodes); large ranges merge into it
+    Bins* bins = &local;
+    if (chunks == 1) {
+      bin(begin, begin + count, cb, kax, *bins);
+    } else {
+      std::vector<std::future<std::unique_ptr<Bins>>> f;
+      for (int c = 0; c < chunks; ++c) {
+        const uint32_t s = begin + std::min(count, (uint32_t)c * step), e = begin + std::min(count, (uint32_t)(c + 1) * step);
+        f.push_back(std::async(std::launch::async, [=, &cb]() {
+          std::unique_ptr<Bins> part(new Bins());
+          bin(s, e, cb, kax, *part);
+          return part;
+        }));
+      }
+      for (auto& x : f) bins->merge(*x.get(), kBins);
+    }
     // Binned SAH over all three axes.
     double best_cost = std::numeric_limits<double>::infinity();
     int best_axis = -1, best_split = -1;
     for (int a = 0; a < 3; ++a) {
-      float ext = cb.hi[a] - cb.lo[a];
-      if (!(ext > 0.f)) continue;
-      Box bb[kMaxBins];
-      uint32_t bc[kMaxBins] = {0};
-      float k = (float)kBins / ext;
-      for (uint32_t i = begin; i < begin + count; ++i) {
-        uint32_t p = idx[i];
-        int b = std::min(kBins - 1, (int)((cent[3 * p + a] - cb.lo[a]) * k));
-        bb[b].grow(pbox[p]);
-        bc[b]++;
-      }
+      if (!(kax[a] > 0.f)) continue;
+      const Box* bb = bins->bb[a];
+      const uint32_t* bc = bins->bc[a];
       double ra[kMaxBins];
       uint32_t rc[kMaxBins];
       Box acc;
