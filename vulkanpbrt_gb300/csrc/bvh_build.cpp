@@ -327,6 +327,17 @@ struct Collapser {
   std::vector<uint32_t>& tri_order;
   Bvh8Stats st;
   const WideDP* dp = nullptr;  // SAH collapse (else: open the largest child)
+  // The output is laid out depth first: a wide node's children block is
+  // appended when the node is encoded, after its earlier siblings' whole
+  // subtrees; its leaves' triangles likewise. wide_below[b] (wide nodes
+  // under the one made from binary node b) gives every subtree its ranges
+  // in advance, so subtrees are encoded on their own threads into the same
+  // places.
+  std::vector<uint32_t> wide_below;
+  std::atomic<int> max_depth{0};
+  std::atomic<size_t> leaves{0};
+
+  bool leaf_slot(uint32_t c) const { return b.nodes[c].left < 0 || (dp && dp->is_leaf[c]); }
 
   static uint8_t exponent_for(double extent) {
     // smallest power of two s with extent / s <= 255 (extent taken in double)
@@ -336,10 +347,9 @@ struct Collapser {
     return (uint8_t)std::min(254, std::max(1, e + 127));
   }
 
-  void encode(uint32_t out_index, uint32_t bnode, int depth) {
-    st.depth = std::max(st.depth, depth);
+  // the child slots of the wide node made from binary node bnode
+  int gather(uint32_t bnode, uint32_t* ch) const {
     // Open the largest child until 8 children (or only leaves remain).
-    uint32_t ch[8];
     int nch = 0;
     const BNode& root = b.nodes[bnode];
     if (root.left < 0) {
@@ -367,6 +377,39 @@ struct Collapser {
         ch[nch++] = (uint32_t)b.nodes[open].right;
       }
     }
+    return nch;
+  }
+
+  uint32_t count_below(uint32_t bnode) {
+    uint32_t ch[8];
+    const int nch = gather(bnode, ch);
+    uint32_t sum = 0;
+    std::future<uint32_t> big[8];
+    bool async_[8] = {false};
+    for (int i = 0; i < nch; ++i) {
+      if (leaf_slot(ch[i])) continue;
+      if (b.nodes[ch[i]].count > kParallelCutoff) {
+        const uint32_t c = ch[i];
+        big[i] = std::async(std::launch::async, [this, c]() { return count_below(c); });
+        async_[i] = true;
+      } else {
+        sum += 1 + count_below(ch[i]);
+      }
+    }
+    for (int i = 0; i < nch; ++i)
+      if (async_[i]) sum += 1 + big[i].get();
+    wide_below[bnode] = sum;
+    return sum;
+  }
+
+  // the wide node made from binary node bnode into out[out_index]; its
+  // children block at child_base, its leaves' triangles from tri_base on
+  void encode(uint32_t out_index, uint32_t bnode, int depth, uint32_t child_base, uint32_t tri_base) {
+    for (int d = max_depth.load(); depth > d && !max_depth.compare_exchange_weak(d, depth);) {
+    }
+    uint32_t ch[8];
+    const int nch = gather(bnode, ch);
+    const BNode& root = b.nodes[bnode];
     // Leaves with more than 3 triangles (identical centroids beyond the leaf
     // size) cannot happen: build() splits them by index.
     const Box& nb = root.box;
@@ -430,33 +473,43 @@ struct Collapser {
     uint32_t inner[8];  // binary nodes of the internal children, slot order
     int ninner = 0;
     uint32_t tri_off = 0;
-    n.tri_base = (uint32_t)tri_order.size();
+    n.tri_base = tri_base;
     for (int s = 0; s < 8; ++s) {
       if (!slot_used[s]) continue;
       const BNode& c = b.nodes[slot_child[s]];
-      const bool leaf_slot = c.left < 0 || (dp && dp->is_leaf[slot_child[s]]);
+      const bool is_leaf = leaf_slot(slot_child[s]);
       for (int a = 0; a < 3; ++a) {
         double lo = std::floor(((double)c.box.lo[a] - p[a]) / scale[a]);
         double hi = std::ceil(((double)c.box.hi[a] - p[a]) / scale[a]);
         n.qlo[a][s] = (uint8_t)std::min(255.0, std::max(0.0, lo));
         n.qhi[a][s] = (uint8_t)std::min(255.0, std::max(0.0, hi));
       }
-      if (!leaf_slot) {
+      if (!is_leaf) {
         n.imask |= (uint8_t)(1u << s);
         n.meta[s] = 0x80;
         inner[ninner++] = slot_child[s];
       } else {
         n.meta[s] = (uint8_t)((c.count << 5) | tri_off);
-        for (uint32_t k = 0; k < c.count; ++k) tri_order.push_back(b.idx[c.begin + k]);
+        for (uint32_t k = 0; k < c.count; ++k) tri_order[tri_base + tri_off + k] = b.idx[c.begin + k];
         tri_off += c.count;
-        st.leaves++;
+        leaves.fetch_add(1, std::memory_order_relaxed);
       }
     }
-    n.child_base = (uint32_t)out.size();
-    out.resize(out.size() + (size_t)ninner);
+    n.child_base = child_base;
     out[out_index] = n;
-    uint32_t base = n.child_base;
-    for (int i = 0; i < ninner; ++i) encode(base + (uint32_t)i, inner[i], depth + 1);
+    // each inner child's subtree: its block after the earlier siblings' subtrees
+    uint32_t next_node = child_base + (uint32_t)ninner, next_tri = tri_base + tri_off;
+    std::vector<std::future<void>> big;
+    for (int i = 0; i < ninner; ++i) {
+      const uint32_t c = inner[i], idx = child_base + (uint32_t)i, cb = next_node, tb = next_tri;
+      if (b.nodes[c].count > kParallelCutoff)
+        big.push_back(std::async(std::launch::async, [=]() { encode(idx, c, depth + 1, cb, tb); }));
+      else
+        encode(idx, c, depth + 1, cb, tb);
+      next_node += wide_below[c];
+      next_tri += b.nodes[c].count;
+    }
+    for (auto& f : big) f.get();
   }
 };
 
@@ -491,8 +544,6 @@ void build_bvh8(const float* v, size_t n, std::vector<Node8>& nodes, std::vector
   b.build(root, 0, (uint32_t)n);
   nodes.clear();
   tri_order.clear();
-  tri_order.reserve(n);
-  nodes.resize(1);
   WideDP dp(b);
   if (const char* pc = std::getenv("PBRT_BVH_PRIM_COST")) dp.kPrim = (float)std::atof(pc);
   Collapser c{b, nodes, tri_order, {}};
@@ -500,7 +551,14 @@ void build_bvh8(const float* v, size_t n, std::vector<Node8>& nodes, std::vector
     dp.solve(root);
     c.dp = &dp;
   }
-  c.encode(0, root, 0);
+  c.wide_below.assign(b.next.load(), 0);
+  // the root is distributed over its children unless it is a single triangle leaf
+  const uint32_t below = b.nodes[root].left < 0 ? 0u : c.count_below(root);
+  nodes.resize(1 + (size_t)below);
+  tri_order.resize(n);
+  c.encode(0, root, 0, 1, 0);
+  c.st.depth = c.max_depth.load();
+  c.st.leaves = c.leaves.load();
   if (stats) {
     *stats = c.st;
     stats->nodes = nodes.size();
